@@ -1,0 +1,173 @@
+/*
+ * lts_capi.h -- C-ABI of the GB300 (sm_103a) renderer for the hot path of
+ * tierChampion/LightTransportSimulation: the Karras LBVH build and the unidirectional path
+ * tracer.  Plain pointers and sizes only; every call returns an int status (LTS_OK == 0) and
+ * never exits the process.  One host thread per context; calls are synchronous on the
+ * context's own CUDA stream unless the name ends in _async.  The context owns all device
+ * memory it allocates; the caller owns every host buffer it passes.
+ *
+ * Each entry point names the reference code it replaces (paths inside the reference tree).
+ */
+#ifndef LTS_CAPI_H
+#define LTS_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define LTS_OK 0
+#define LTS_ERR_ARG 1         /* bad argument / size                                   */
+#define LTS_ERR_IO 2          /* file missing or unreadable                            */
+#define LTS_ERR_PARSE 3       /* malformed app.params / .scene / .subject / .bin       */
+#define LTS_ERR_CUDA 4        /* CUDA runtime error (message in lts_last_error)        */
+#define LTS_ERR_OOM 5         /* device allocation failed or exceeded LTS_MAX_DEVICE_MB */
+#define LTS_ERR_UNSUPPORTED 6 /* input uses a feature outside this renderer's scope    */
+#define LTS_ERR_STATE 7       /* call order (e.g. render before load)                  */
+#define LTS_ERR_DEVICE 8      /* a kernel reported an error flag (queue overflow, wait limit) */
+
+typedef struct lts_ctx lts_ctx;
+
+/* Replaces the process-wide setup of LightTransportSimulation.cu:23-61 (no exit on error).
+ * device == -1 makes a host-only context: files can be parsed and the scene queried, every
+ * call that needs the GPU returns LTS_ERR_STATE.  There is no CPU rendering fallback. */
+int lts_create(lts_ctx** out, int device);
+void lts_destroy(lts_ctx* ctx);
+/* Last error message of this context ("" if none).  Replaces gpuAssert's stderr print +
+ * exit (core/ErrorHelper.cuh:26-32). */
+const char* lts_last_error(const lts_ctx* ctx);
+/* The cudaStream_t every call of this context is issued on (as void*). */
+void* lts_stream(lts_ctx* ctx);
+
+/* ---------------------------------------------------------------- inputs */
+typedef struct {
+    int32_t width, height, spp, max_bounce, rr_start, format;
+    char output[256]; /* token + ".pfm" (format 1) or ".hdr" (format 0, PPM content) */
+    char scene[256];
+    char subject[256];
+} lts_app_params;
+
+/* Parses app.params: `W H spp bounces rrStart format output scene subject`.
+ * Replaces readApplicationParameters (core/FileIO.cuh:234-257). */
+int lts_read_app_params(const char* path, lts_app_params* out);
+
+/* Loads `root + scene + ".scene"` and optionally `root + subject + ".subject"` with their
+ * `.bin` meshes, transforms subject meshes, builds the camera for a width x height film and
+ * the light table, and uploads SoA tables to the device.  subject may be NULL or "".
+ * Replaces parseScene (core/SceneLoader.cuh:195-360) and the init kernels of
+ * core/SceneLoader_kernels.cu:8-111.  Image textures ('i') are rejected with
+ * LTS_ERR_UNSUPPORTED. */
+int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char* subject,
+                   int32_t width, int32_t height);
+
+typedef struct {
+    int32_t triangles, meshes, subject_meshes, materials, lights, area_light_meshes, has_infinite;
+    int32_t width, height;
+    int32_t max_mesh_triangles; /* largest mesh: bounds the reference's Morton launch */
+} lts_scene_info;
+int lts_scene_info_get(lts_ctx* ctx, lts_scene_info* out);
+
+/* World-space vertex positions of every primitive in scene order (9 floats per triangle),
+ * the camera as 23 floats {o, right, up, llc, u, v, w (3 each), lensRadius, focalDist}
+ * (rendering/Camera.cu:9-43), and the light power distribution func[lights], cdf[lights+1]
+ * (intergrators/IntegratorHelper.cuh:147-162, sampling/Sampling.cuh:123-144). */
+int lts_scene_get_triangles(lts_ctx* ctx, float* out_p9);
+int lts_scene_get_camera(lts_ctx* ctx, float* out23);
+int lts_scene_get_light_distribution(lts_ctx* ctx, float* func, float* cdf);
+
+/* ---------------------------------------------------------------- LBVH */
+/* LTS_BVH_REFERENCE: the reference's build exactly (acceleration/BVH.cuh:77-452): Morton
+ *   codes only for primitives below code_limit (SceneLoader.cuh:324-339 launches
+ *   ceil(maxMeshTris/16)*16 threads; the rest keep code 0 / id 0 from zeroed memory), and
+ *   leaf l holds primitive l, not the sorted primitive (BVH.cuh:242,315,383).
+ * LTS_BVH_SORTED: the textbook LBVH: every primitive coded, leaf l holds sorted primitive
+ *   ids[l].  Same Morton arithmetic, stable order and Karras topology. */
+#define LTS_BVH_REFERENCE 0
+#define LTS_BVH_SORTED 1
+
+/* Host buffers to receive the build; any pointer may be NULL.  N primitives, 2N-1 nodes in
+ * the reference's flattened order (interior 0..N-2, leaves N-1..2N-2, BVH.cuh:311-329). */
+typedef struct {
+    uint32_t* sorted_codes; /* [N]   */
+    int32_t* sorted_ids;    /* [N]   */
+    int32_t* node_key;      /* [2N-1] -1 for interior nodes, leaf index l for leaves */
+    int32_t* node_left;     /* [2N-1] child node index, -1 for leaves */
+    int32_t* node_right;    /* [2N-1] */
+    float* node_bounds;     /* [6(2N-1)] pMin xyz, pMax xyz */
+} lts_bvh_dump;
+
+/* Builds the LBVH of the loaded scene.  Replaces CreateBVHTree (BVH.cuh:411-452) with the
+ * Morton pass (BVH_kernels.cu:8-15) and the bounds of sceneInitKernel
+ * (SceneLoader_kernels.cu:87, BVH.cuh:92-97). */
+int lts_bvh_build(lts_ctx* ctx, int32_t mode, lts_bvh_dump* dump);
+
+/* Same build over a host triangle soup (9 floats per triangle, n >= 1); code_limit < 0
+ * means "all primitives".  The BVH is kept in the context for lts_bvh_dump_get. */
+int lts_bvh_build_triangles(lts_ctx* ctx, const float* tri_p9, int32_t n, int32_t mode, int32_t code_limit,
+                            lts_bvh_dump* dump);
+
+/* Device-resident variant for benchmarks: d_tri_p9 is a device pointer (9 floats per
+ * triangle, 4-byte aligned).  Enqueued on the context stream; returns without waiting. */
+int lts_bvh_build_device_async(lts_ctx* ctx, const float* d_tri_p9, int32_t n, int32_t mode,
+                               int32_t code_limit);
+/* Copies the last build to host buffers (synchronises the stream). */
+int lts_bvh_dump_get(lts_ctx* ctx, lts_bvh_dump* dump);
+
+/* ---------------------------------------------------------------- rendering */
+#define LTS_INTEGRATOR_MEGAKERNEL 0 /* one thread per pixel, all spp and bounces        */
+#define LTS_INTEGRATOR_WAVEFRONT 1  /* generate / extend / shade / shadow / film queues  */
+
+typedef struct {
+    int32_t spp, max_bounce, rr_start;
+    uint32_t seed;
+    int32_t integrator; /* LTS_INTEGRATOR_* */
+    /* Pixel crop [x0,x1) x [y0,y1) of the loaded film; x1 = y1 = 0 means the whole film. */
+    int32_t x0, y0, x1, y1;
+    /* Non-zero: record per-(pixel, sample) radiance and event hash for parity checks. */
+    int32_t record_samples;
+    int32_t bvh_mode; /* LTS_BVH_* used for traversal (results agree up to exact-t ties) */
+} lts_render_desc;
+
+typedef struct {
+    float* film_rgb;      /* [W*H*3] resolved film (Camera::getRender: rgb/w, clamp >= 0,
+                             Y flipped), or NULL */
+    double* film_sums;    /* [W*H*4] FP64 resolve of the compensated sums {r,g,b,w}, or NULL */
+    float* sample_L;      /* [crop pixels * spp * 3], requires record_samples, or NULL */
+    uint64_t* sample_sig; /* [crop pixels * spp] FNV-1a hash of each sample's events, or NULL */
+    double render_ms;     /* device time of the render kernels (CUDA events) */
+    double rays;          /* ray queries issued (extension + shadow + MIS) */
+} lts_render_out;
+
+/* Renders the loaded scene.  Replaces PathTracingKernel / PathTracingIntegrator::evaluate
+ * (intergrators/IntegratorKernels.cu:17-23, PathTracingIntegrator.cuh:26-109) and the film
+ * (rendering/Camera.cu:192-218,256-289).  Builds the LBVH first if none matches bvh_mode. */
+int lts_render(lts_ctx* ctx, const lts_render_desc* desc, lts_render_out* out);
+
+/* Enqueues one render of the whole film on the context stream without copying anything back
+ * (film stays on the device); used for device-time benchmarks. */
+int lts_render_async(lts_ctx* ctx, const lts_render_desc* desc);
+/* Copies the film of the last render (synchronises). */
+int lts_film_get(lts_ctx* ctx, float* film_rgb, double* film_sums);
+
+/* Writes a film as the reference does: format 0 -> PPM P3 with gamma 1/2.2, format 1 -> PFM
+ * (little-endian, scale -1).  Replaces writeToPPM / writeToPFM (core/ImageO.cuh:16-78). */
+int lts_write_image(const char* path, const float* rgb, int32_t width, int32_t height, int32_t format);
+
+/* ---------------------------------------------------------------- metrics */
+typedef struct {
+    double bvh_build_ms;  /* device time of the last LBVH build */
+    double bvh_stage_ms[5]; /* bounds, morton, sort, topology, refit */
+    double render_ms;
+    double paths, rays;
+    int64_t device_bytes; /* bytes currently allocated by the context */
+    int32_t kernel_launches; /* kernels launched by the last build + render */
+} lts_metrics;
+int lts_get_metrics(lts_ctx* ctx, lts_metrics* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

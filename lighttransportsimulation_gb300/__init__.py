@@ -1,0 +1,283 @@
+"""GB300 (sm_103a) renderer for the hot path of tierChampion/LightTransportSimulation.
+
+The compute path is the in-tree CUDA library `_lib/liblts_gb300.so` behind the C-ABI of
+`include/lts_capi.h`; this module is a thin ctypes layer over it that mirrors the reference's
+host-side interfaces:
+
+  read_application_parameters(path)          core/FileIO.cuh:234-257
+  Scene.parse(root, scene, subject, w, h)    core/SceneLoader.cuh:195-360 (parseScene)
+  Scene.create_bvh_tree(mode)                acceleration/BVH.cuh:411-452 (CreateBVHTree)
+  PathTracingIntegrator(max_bounce, rr_start, scene).render(spp, seed)
+                                             intergrators/PathTracingIntegrator.cuh:18-109
+  write_image(path, rgb, format)             core/ImageO.cuh:16-78
+
+There is no CPU fallback: without the compiled library, or without a GPU, the calls raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "liblts_gb300.so")
+
+LTS_OK = 0
+ERRORS = {1: "LTS_ERR_ARG", 2: "LTS_ERR_IO", 3: "LTS_ERR_PARSE", 4: "LTS_ERR_CUDA", 5: "LTS_ERR_OOM",
+          6: "LTS_ERR_UNSUPPORTED", 7: "LTS_ERR_STATE", 8: "LTS_ERR_DEVICE"}
+BVH_REFERENCE = 0
+BVH_SORTED = 1
+INTEGRATOR_MEGAKERNEL = 0
+INTEGRATOR_WAVEFRONT = 1
+
+# Every symbol include/lts_capi.h declares.
+EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_read_app_params", "lts_load_scene",
+           "lts_scene_info_get", "lts_scene_get_triangles", "lts_scene_get_camera",
+           "lts_scene_get_light_distribution", "lts_bvh_build", "lts_bvh_build_triangles",
+           "lts_bvh_build_device_async", "lts_bvh_dump_get", "lts_render", "lts_render_async", "lts_film_get",
+           "lts_write_image", "lts_get_metrics"]
+
+
+class LtsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class AppParams(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("spp", ctypes.c_int32),
+                ("max_bounce", ctypes.c_int32), ("rr_start", ctypes.c_int32), ("format", ctypes.c_int32),
+                ("output", ctypes.c_char * 256), ("scene", ctypes.c_char * 256), ("subject", ctypes.c_char * 256)]
+
+
+class SceneInfo(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in ("triangles", "meshes", "subject_meshes", "materials", "lights",
+                                               "area_light_meshes", "has_infinite", "width", "height",
+                                               "max_mesh_triangles")]
+
+
+class BvhDump(ctypes.Structure):
+    _fields_ = [("sorted_codes", ctypes.c_void_p), ("sorted_ids", ctypes.c_void_p), ("node_key", ctypes.c_void_p),
+                ("node_left", ctypes.c_void_p), ("node_right", ctypes.c_void_p), ("node_bounds", ctypes.c_void_p)]
+
+
+class RenderDesc(ctypes.Structure):
+    _fields_ = [("spp", ctypes.c_int32), ("max_bounce", ctypes.c_int32), ("rr_start", ctypes.c_int32),
+                ("seed", ctypes.c_uint32), ("integrator", ctypes.c_int32), ("x0", ctypes.c_int32),
+                ("y0", ctypes.c_int32), ("x1", ctypes.c_int32), ("y1", ctypes.c_int32),
+                ("record_samples", ctypes.c_int32), ("bvh_mode", ctypes.c_int32)]
+
+
+class RenderOut(ctypes.Structure):
+    _fields_ = [("film_rgb", ctypes.c_void_p), ("film_sums", ctypes.c_void_p), ("sample_L", ctypes.c_void_p),
+                ("sample_sig", ctypes.c_void_p), ("render_ms", ctypes.c_double), ("rays", ctypes.c_double)]
+
+
+class Metrics(ctypes.Structure):
+    _fields_ = [("bvh_build_ms", ctypes.c_double), ("bvh_stage_ms", ctypes.c_double * 5),
+                ("render_ms", ctypes.c_double), ("paths", ctypes.c_double), ("rays", ctypes.c_double),
+                ("device_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def library():
+    """Loads the compiled renderer; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with lighttransportsimulation_gb300.build.build()")
+        lib = ctypes.CDLL(LIB_PATH)
+        P, I, V = ctypes.c_void_p, ctypes.c_int32, None
+        sig = {
+            "lts_create": (I, [ctypes.POINTER(P), I]), "lts_destroy": (V, [P]),
+            "lts_last_error": (ctypes.c_char_p, [P]), "lts_stream": (P, [P]),
+            "lts_read_app_params": (I, [ctypes.c_char_p, ctypes.POINTER(AppParams)]),
+            "lts_load_scene": (I, [P, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, I, I]),
+            "lts_scene_info_get": (I, [P, ctypes.POINTER(SceneInfo)]),
+            "lts_scene_get_triangles": (I, [P, P]), "lts_scene_get_camera": (I, [P, P]),
+            "lts_scene_get_light_distribution": (I, [P, P, P]),
+            "lts_bvh_build": (I, [P, I, ctypes.POINTER(BvhDump)]),
+            "lts_bvh_build_triangles": (I, [P, P, I, I, I, ctypes.POINTER(BvhDump)]),
+            "lts_bvh_build_device_async": (I, [P, P, I, I, I]),
+            "lts_bvh_dump_get": (I, [P, ctypes.POINTER(BvhDump)]),
+            "lts_render": (I, [P, ctypes.POINTER(RenderDesc), ctypes.POINTER(RenderOut)]),
+            "lts_render_async": (I, [P, ctypes.POINTER(RenderDesc)]),
+            "lts_film_get": (I, [P, P, P]),
+            "lts_write_image": (I, [ctypes.c_char_p, P, I, I, I]),
+            "lts_get_metrics": (I, [P, ctypes.POINTER(Metrics)]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One renderer context (lts_create / lts_destroy).  device=-1: host-only (parsing)."""
+
+    def __init__(self, device=0):
+        self.lib = library()
+        h = ctypes.c_void_p()
+        rc = self.lib.lts_create(ctypes.byref(h), device)
+        if rc != LTS_OK:
+            raise LtsError(rc, "lts_create failed (no CUDA device or driver)" if device >= 0 else "lts_create")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lts_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc):
+        if rc != LTS_OK:
+            raise LtsError(rc, self.lib.lts_last_error(self.h).decode())
+
+    def stream(self):
+        return self.lib.lts_stream(self.h)
+
+    def metrics(self):
+        m = Metrics()
+        self.check(self.lib.lts_get_metrics(self.h, ctypes.byref(m)))
+        return m
+
+
+def read_application_parameters(path):
+    """app.params -> dict (width, height, spp, max_bounce, rr_start, format, output, scene, subject)."""
+    p = AppParams()
+    rc = library().lts_read_app_params(path.encode(), ctypes.byref(p))
+    if rc != LTS_OK:
+        raise LtsError(rc, path)
+    d = {f: getattr(p, f) for f, _ in AppParams._fields_}
+    for k in ("output", "scene", "subject"):
+        d[k] = d[k].decode()
+    return d
+
+
+class Scene:
+    """Scene{intersect, simpleIntersect, lights, lightCount} (acceleration/Scene.cuh:10-33) as
+    device tables owned by a Context; parse() replaces parseScene."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+
+    @classmethod
+    def parse(cls, ctx, root, scene, subject, width, height):
+        root = os.path.join(root, "")
+        ctx.check(ctx.lib.lts_load_scene(ctx.h, root.encode(), scene.encode(),
+                                         (subject or "").encode(), width, height))
+        s = cls(ctx)
+        s.info = s.query_info()
+        return s
+
+    def query_info(self):
+        i = SceneInfo()
+        self.ctx.check(self.ctx.lib.lts_scene_info_get(self.ctx.h, ctypes.byref(i)))
+        return {f: getattr(i, f) for f, _ in SceneInfo._fields_}
+
+    @property
+    def light_count(self):
+        return self.info["lights"]
+
+    def triangles(self):
+        out = np.empty(self.info["triangles"] * 9, np.float32)
+        self.ctx.check(self.ctx.lib.lts_scene_get_triangles(self.ctx.h, _ptr(out)))
+        return out.reshape(-1, 3, 3)
+
+    def camera(self):
+        out = np.empty(23, np.float32)
+        self.ctx.check(self.ctx.lib.lts_scene_get_camera(self.ctx.h, _ptr(out)))
+        return out
+
+    def light_distribution(self):
+        n = self.info["lights"]
+        func = np.empty(max(n, 1), np.float32)
+        cdf = np.empty(n + 1, np.float32)
+        self.ctx.check(self.ctx.lib.lts_scene_get_light_distribution(self.ctx.h, _ptr(func), _ptr(cdf)))
+        return func[:n], cdf
+
+    def create_bvh_tree(self, mode=BVH_SORTED, dump=True):
+        """LBVH of the scene; returns the dump dict (codes, ids, node arrays) when dump."""
+        n = self.info["triangles"]
+        arrays, d = _dump_arrays(n) if dump else (None, None)
+        self.ctx.check(self.ctx.lib.lts_bvh_build(self.ctx.h, mode, ctypes.byref(d) if dump else None))
+        return arrays
+
+
+def _dump_arrays(n):
+    nodes = 2 * n - 1
+    a = {"sorted_codes": np.empty(n, np.uint32), "sorted_ids": np.empty(n, np.int32),
+         "node_key": np.empty(nodes, np.int32), "node_left": np.empty(nodes, np.int32),
+         "node_right": np.empty(nodes, np.int32), "node_bounds": np.empty(nodes * 6, np.float32)}
+    d = BvhDump(*[a[f].ctypes.data for f, _ in BvhDump._fields_])
+    return a, d
+
+
+def build_bvh_triangles(ctx, tris, mode=BVH_SORTED, code_limit=-1):
+    """LBVH over an (n, 3, 3) float32 triangle soup; returns the dump dict."""
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    arrays, d = _dump_arrays(tris.shape[0])
+    ctx.check(ctx.lib.lts_bvh_build_triangles(ctx.h, _ptr(tris), tris.shape[0], mode, code_limit, ctypes.byref(d)))
+    return arrays
+
+
+class PathTracingIntegrator:
+    """PathTracingIntegrator(maxBounce, rrStart, camera, sampler, scene) and its evaluate()
+    over the film (intergrators/PathTracingIntegrator.cuh:18-109); the camera and the Gaussian
+    filter come from the parsed scene, the sampler from (spp, seed)."""
+
+    def __init__(self, max_bounce, rr_start, scene, integrator=INTEGRATOR_MEGAKERNEL, bvh_mode=BVH_SORTED):
+        self.max_bounce, self.rr_start, self.scene = max_bounce, rr_start, scene
+        self.integrator, self.bvh_mode = integrator, bvh_mode
+
+    def desc(self, spp, seed, crop=None, record=False):
+        x0, y0, x1, y1 = crop if crop is not None else (0, 0, 0, 0)
+        return RenderDesc(spp, self.max_bounce, self.rr_start, seed, self.integrator, x0, y0, x1, y1,
+                          1 if record else 0, self.bvh_mode)
+
+    def render(self, spp, seed, crop=None, record=False, film=True, sums=False):
+        info = self.scene.info
+        W, H = info["width"], info["height"]
+        d = self.desc(spp, seed, crop, record)
+        cw = (crop[2] - crop[0]) if crop else W
+        ch = (crop[3] - crop[1]) if crop else H
+        res = {}
+        rgb = np.empty(W * H * 3, np.float32) if film else None
+        fs = np.empty(W * H * 4, np.float64) if sums else None
+        L = np.empty(cw * ch * spp * 3, np.float32) if record else None
+        sig = np.empty(cw * ch * spp, np.uint64) if record else None
+        o = RenderOut(rgb.ctypes.data if film else None, fs.ctypes.data if sums else None,
+                      L.ctypes.data if record else None, sig.ctypes.data if record else None, 0.0, 0.0)
+        ctx = self.scene.ctx
+        ctx.check(ctx.lib.lts_render(ctx.h, ctypes.byref(d), ctypes.byref(o)))
+        if film:
+            res["film"] = rgb.reshape(H, W, 3)
+        if sums:
+            res["film_sums"] = fs.reshape(H, W, 4)
+        if record:
+            res["L"] = L.reshape(ch, cw, spp, 3)
+            res["sig"] = sig.reshape(ch, cw, spp)
+        res["render_ms"] = o.render_ms
+        res["rays"] = o.rays
+        return res
+
+
+def write_image(path, rgb, fmt):
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    h, w = rgb.shape[:2]
+    rc = library().lts_write_image(path.encode(), _ptr(rgb), w, h, fmt)
+    if rc != LTS_OK:
+        raise LtsError(rc, path)

@@ -1,0 +1,438 @@
+// C-ABI of include/lts_capi.h: context, inputs, LBVH build and rendering orchestration.
+// Host code only; kernels live in lbvh.cu and tracer.cu.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/lts_capi.h"
+#include "dev_common.cuh"
+#include "host_scene.hpp"
+#include "lbvh.cuh"
+#include "tracer.cuh"
+
+namespace lts {
+
+static std::atomic<long long> g_bytes{0};
+static std::mutex g_mu;
+static std::unordered_map<void*, size_t> g_sizes;
+
+static long long cap_bytes() {
+    static long long cap = [] {
+        const char* e = getenv("LTS_MAX_DEVICE_MB");
+        return e ? (long long)atoll(e) * 1024 * 1024 : -1LL;
+    }();
+    return cap;
+}
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+    *p = nullptr;
+    const long long cap = cap_bytes();
+    if (cap >= 0 && g_bytes.load() + (long long)bytes > cap) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e == cudaSuccess) {
+        g_bytes += (long long)bytes;
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_sizes[*p] = bytes;
+    }
+    return e;
+}
+
+void dev_free(void* p) {
+    if (!p) return;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_sizes.find(p);
+        if (it != g_sizes.end()) {
+            g_bytes -= (long long)it->second;
+            g_sizes.erase(it);
+        }
+    }
+    cudaFree(p);
+}
+
+size_t dev_bytes_in_use() { return (size_t)g_bytes.load(); }
+
+}  // namespace lts
+
+using namespace lts;
+
+struct lts_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint32_t* d_error = nullptr;
+
+    HostScene scene;
+    bool loaded = false;
+    float* d_tri = nullptr;  // scene triangle soup, 9 floats per triangle (scene order)
+    size_t d_tri_cap = 0;
+    std::unique_ptr<Lbvh> bvh;
+    int bvh_mode = -1;        // mode of the BVH currently held (-1: none)
+    bool bvh_is_scene = false;
+    std::unique_ptr<Tracer> tracer;
+    lts_metrics metrics{};
+};
+
+namespace {
+
+int fail(lts_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+int cuda_fail(lts_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? LTS_ERR_OOM : LTS_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                       \
+    do {                                               \
+        cudaError_t e_ = (call);                       \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+int check_device_error(lts_ctx* ctx) {
+    uint32_t h = 0;
+    CK(cudaMemcpyAsync(&h, ctx->d_error, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (h) {
+        CK(cudaMemsetAsync(ctx->d_error, 0, 4, ctx->stream));
+        return fail(ctx, LTS_ERR_DEVICE, "a kernel reported device error flags 0x" + std::to_string(h));
+    }
+    return LTS_OK;
+}
+
+int ensure_tri_buffer(lts_ctx* ctx, size_t floats) {
+    if (floats * 4 <= ctx->d_tri_cap) return LTS_OK;
+    dev_free(ctx->d_tri);
+    ctx->d_tri = nullptr;
+    ctx->d_tri_cap = 0;
+    CK(dev_alloc((void**)&ctx->d_tri, floats * 4));
+    ctx->d_tri_cap = floats * 4;
+    return LTS_OK;
+}
+
+int do_build(lts_ctx* ctx, const float* d_tri, int n, int mode, int code_limit) {
+    if (mode != LTS_BVH_REFERENCE && mode != LTS_BVH_SORTED) return fail(ctx, LTS_ERR_ARG, "unknown BVH mode");
+    if (!ctx->bvh) ctx->bvh.reset(new Lbvh());
+    std::string e = ctx->bvh->build(d_tri, n, mode, code_limit, ctx->stream, ctx->d_error);
+    if (!e.empty()) {
+        ctx->bvh_mode = -1;
+        return fail(ctx, e.find("memory") != std::string::npos ? LTS_ERR_OOM : LTS_ERR_CUDA, e);
+    }
+    ctx->bvh_mode = mode;
+    return LTS_OK;
+}
+
+int dump_bvh(lts_ctx* ctx, lts_bvh_dump* d) {
+    if (!ctx->bvh || ctx->bvh_mode < 0) return fail(ctx, LTS_ERR_STATE, "no BVH has been built");
+    int rc = check_device_error(ctx);
+    if (rc) return rc;
+    Lbvh& b = *ctx->bvh;
+    float st[5];
+    b.stage_ms(st);
+    ctx->metrics.bvh_build_ms = 0;
+    for (int i = 0; i < 5; ++i) {
+        ctx->metrics.bvh_stage_ms[i] = st[i];
+        ctx->metrics.bvh_build_ms += st[i];
+    }
+    if (!d) return LTS_OK;
+    const int n = b.n, nodes = 2 * n - 1;
+    if (d->sorted_codes) CK(cudaMemcpy(d->sorted_codes, b.codes, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+    if (d->sorted_ids) CK(cudaMemcpy(d->sorted_ids, b.ids, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+    if (!d->node_key && !d->node_left && !d->node_right && !d->node_bounds) return LTS_OK;
+    std::vector<BvhNode> h((size_t)(n > 1 ? n - 1 : 0));
+    if (n > 1) CK(cudaMemcpy(h.data(), b.nodes, sizeof(BvhNode) * (n - 1), cudaMemcpyDeviceToHost));
+    float root[6];
+    CK(cudaMemcpy(root, b.root_bounds, 24, cudaMemcpyDeviceToHost));
+    // Reference flattened order: interior 0..n-2, leaves n-1..2n-2 (BVH.cuh:311-329).
+    std::vector<int32_t> key(nodes, -1), left(nodes, -1), right(nodes, -1);
+    std::vector<float> bnd((size_t)nodes * 6, 0.f);
+    for (int l = 0; l < n; ++l) key[n - 1 + l] = l;
+    auto flat = [n](int c) { return c < 0 ? (n - 1) + ~c : c; };
+    memcpy(&bnd[0], root, 24);
+    if (n == 1) memcpy(&bnd[0], root, 24);
+    for (int i = 0; i < n - 1; ++i) {
+        const float* f = reinterpret_cast<const float*>(&h[i]);
+        const int lc = flat(h[i].d.x), rc = flat(h[i].d.y);
+        left[i] = lc;
+        right[i] = rc;
+        memcpy(&bnd[(size_t)lc * 6], f, 24);
+        memcpy(&bnd[(size_t)rc * 6], f + 6, 24);
+    }
+    if (d->node_key) memcpy(d->node_key, key.data(), 4 * (size_t)nodes);
+    if (d->node_left) memcpy(d->node_left, left.data(), 4 * (size_t)nodes);
+    if (d->node_right) memcpy(d->node_right, right.data(), 4 * (size_t)nodes);
+    if (d->node_bounds) memcpy(d->node_bounds, bnd.data(), 24 * (size_t)nodes);
+    return LTS_OK;
+}
+
+void copy_str(char* dst, const std::string& s) {
+    strncpy(dst, s.c_str(), 255);
+    dst[255] = 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lts_create(lts_ctx** out, int device) {
+    if (!out) return LTS_ERR_ARG;
+    *out = nullptr;
+    std::unique_ptr<lts_ctx> c(new lts_ctx());
+    c->device = device;
+    lts_ctx* ctx = c.get();
+    if (device == -1) {  // host-only context: parsing and scene queries, no device work
+        *out = c.release();
+        return LTS_OK;
+    }
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0)
+        return LTS_ERR_CUDA;  // no device: the renderer has no CPU fallback
+    if (device < 0 || device >= count) return LTS_ERR_ARG;
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(dev_alloc((void**)&c->d_error, 4));
+    CK(cudaMemset(c->d_error, 0, 4));
+    *out = c.release();
+    return LTS_OK;
+}
+
+void lts_destroy(lts_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->device == -1) {
+        delete ctx;
+        return;
+    }
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->tracer.reset();
+    ctx->bvh.reset();
+    dev_free(ctx->d_tri);
+    dev_free(ctx->d_error);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* lts_last_error(const lts_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+void* lts_stream(lts_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int lts_read_app_params(const char* path, lts_app_params* out) {
+    if (!path || !out) return LTS_ERR_ARG;
+    AppParams p;
+    int code = LTS_OK;
+    read_app_params(path, &p, &code);
+    if (code) return code;
+    out->width = p.width;
+    out->height = p.height;
+    out->spp = p.spp;
+    out->max_bounce = p.max_bounce;
+    out->rr_start = p.rr_start;
+    out->format = p.format;
+    copy_str(out->output, p.output);
+    copy_str(out->scene, p.scene);
+    copy_str(out->subject, p.subject);
+    return LTS_OK;
+}
+
+int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char* subject, int32_t width,
+                   int32_t height) {
+    if (!ctx || !root || !scene) return fail(ctx, LTS_ERR_ARG, "null argument");
+    int code = LTS_OK;
+    HostScene sc;
+    std::string msg = load_scene(root, scene, subject ? subject : "", width, height, &sc, &code);
+    if (code) return fail(ctx, code, msg);
+    ctx->scene = std::move(sc);
+    ctx->loaded = true;
+    ctx->bvh_mode = -1;
+    ctx->bvh_is_scene = false;
+    if (ctx->device == -1) return LTS_OK;
+    CK(cudaSetDevice(ctx->device));
+    std::vector<float> soup;
+    ctx->scene.triangle_soup(soup);
+    int rc = ensure_tri_buffer(ctx, soup.size());
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_tri, soup.data(), soup.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    if (!ctx->tracer) ctx->tracer.reset(new Tracer());
+    std::string e = ctx->tracer->upload_scene(ctx->scene, ctx->stream);
+    if (!e.empty()) return fail(ctx, e.find("memory") != std::string::npos ? LTS_ERR_OOM : LTS_ERR_CUDA, e);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return LTS_OK;
+}
+
+int lts_scene_info_get(lts_ctx* ctx, lts_scene_info* out) {
+    if (!ctx || !out) return fail(ctx, LTS_ERR_ARG, "null argument");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    const HostScene& s = ctx->scene;
+    out->triangles = s.triangles();
+    out->meshes = (int32_t)s.mesh_tri_count.size();
+    out->subject_meshes = s.subject_meshes;
+    out->materials = (int32_t)s.materials.size();
+    out->lights = (int32_t)s.lights.size();
+    out->area_light_meshes = s.area_light_meshes;
+    out->has_infinite = s.has_infinite ? 1 : 0;
+    out->width = s.width;
+    out->height = s.height;
+    out->max_mesh_triangles = s.max_mesh_triangles();
+    return LTS_OK;
+}
+
+int lts_scene_get_triangles(lts_ctx* ctx, float* out) {
+    if (!ctx || !out) return fail(ctx, LTS_ERR_ARG, "null argument");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    std::vector<float> soup;
+    ctx->scene.triangle_soup(soup);
+    memcpy(out, soup.data(), soup.size() * 4);
+    return LTS_OK;
+}
+
+int lts_scene_get_camera(lts_ctx* ctx, float* out23) {
+    if (!ctx || !out23) return fail(ctx, LTS_ERR_ARG, "null argument");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    memcpy(out23, ctx->scene.cam, sizeof ctx->scene.cam);
+    return LTS_OK;
+}
+
+int lts_scene_get_light_distribution(lts_ctx* ctx, float* func, float* cdf) {
+    if (!ctx) return LTS_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    if (func) memcpy(func, ctx->scene.light_func.data(), 4 * ctx->scene.light_func.size());
+    if (cdf) memcpy(cdf, ctx->scene.light_cdf.data(), 4 * ctx->scene.light_cdf.size());
+    return LTS_OK;
+}
+
+int lts_bvh_build(lts_ctx* ctx, int32_t mode, lts_bvh_dump* dump) {
+    if (!ctx) return LTS_ERR_ARG;
+    if (ctx->device == -1) return fail(ctx, LTS_ERR_STATE, "host-only context (device -1) cannot run kernels");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    CK(cudaSetDevice(ctx->device));
+    const int n = ctx->scene.triangles();
+    // The reference's Morton launch covers ceil(maxMeshTris/16)*16 primitives
+    // (SceneLoader.cuh:323-339, BVH_kernels.cu:10-12).
+    const int limit = mode == LTS_BVH_REFERENCE ? ((ctx->scene.max_mesh_triangles() + 15) / 16) * 16 : -1;
+    int rc = do_build(ctx, ctx->d_tri, n, mode, limit);
+    if (rc) return rc;
+    ctx->bvh_is_scene = true;
+    return dump_bvh(ctx, dump);
+}
+
+int lts_bvh_build_triangles(lts_ctx* ctx, const float* tri, int32_t n, int32_t mode, int32_t code_limit,
+                            lts_bvh_dump* dump) {
+    if (!ctx || !tri || n < 1) return fail(ctx, LTS_ERR_ARG, "bad triangle input");
+    if (ctx->device == -1) return fail(ctx, LTS_ERR_STATE, "host-only context (device -1) cannot run kernels");
+    CK(cudaSetDevice(ctx->device));
+    float* d = nullptr;
+    CK(dev_alloc((void**)&d, 36 * (size_t)n));
+    cudaError_t e = cudaMemcpyAsync(d, tri, 36 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) {
+        dev_free(d);
+        return cuda_fail(ctx, e, "copy triangles");
+    }
+    int rc = do_build(ctx, d, n, mode, code_limit);
+    if (rc == LTS_OK) rc = dump_bvh(ctx, dump);
+    cudaStreamSynchronize(ctx->stream);
+    dev_free(d);
+    ctx->bvh_is_scene = false;
+    return rc;
+}
+
+int lts_bvh_build_device_async(lts_ctx* ctx, const float* d_tri, int32_t n, int32_t mode, int32_t code_limit) {
+    if (!ctx || !d_tri || n < 1) return fail(ctx, LTS_ERR_ARG, "bad triangle input");
+    if (ctx->device == -1) return fail(ctx, LTS_ERR_STATE, "host-only context (device -1) cannot run kernels");
+    ctx->bvh_is_scene = false;
+    return do_build(ctx, d_tri, n, mode, code_limit);
+}
+
+int lts_bvh_dump_get(lts_ctx* ctx, lts_bvh_dump* dump) {
+    if (!ctx) return LTS_ERR_ARG;
+    return dump_bvh(ctx, dump);
+}
+
+int lts_render(lts_ctx* ctx, const lts_render_desc* desc, lts_render_out* out) {
+    if (!ctx || !desc) return fail(ctx, LTS_ERR_ARG, "null argument");
+    if (ctx->device == -1) return fail(ctx, LTS_ERR_STATE, "host-only context (device -1) cannot run kernels");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    CK(cudaSetDevice(ctx->device));
+    const int mode = desc->bvh_mode == LTS_BVH_REFERENCE ? LTS_BVH_REFERENCE : LTS_BVH_SORTED;
+    if (!(ctx->bvh_is_scene && ctx->bvh_mode == mode)) {
+        int rc = lts_bvh_build(ctx, mode, nullptr);
+        if (rc) return rc;
+    }
+    std::string e = ctx->tracer->render(ctx->scene, *ctx->bvh, *desc, out, ctx->stream, ctx->d_error);
+    if (!e.empty()) return fail(ctx, e.find("argument") != std::string::npos ? LTS_ERR_ARG : LTS_ERR_CUDA, e);
+    int rc = check_device_error(ctx);
+    if (rc) return rc;
+    ctx->metrics.render_ms = ctx->tracer->last_ms;
+    ctx->metrics.paths = ctx->tracer->last_paths;
+    ctx->metrics.rays = ctx->tracer->last_rays;
+    return LTS_OK;
+}
+
+int lts_render_async(lts_ctx* ctx, const lts_render_desc* desc) {
+    if (!ctx || !desc) return fail(ctx, LTS_ERR_ARG, "null argument");
+    if (ctx->device == -1) return fail(ctx, LTS_ERR_STATE, "host-only context (device -1) cannot run kernels");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    const int mode = desc->bvh_mode == LTS_BVH_REFERENCE ? LTS_BVH_REFERENCE : LTS_BVH_SORTED;
+    if (!(ctx->bvh_is_scene && ctx->bvh_mode == mode)) {
+        int rc = lts_bvh_build(ctx, mode, nullptr);
+        if (rc) return rc;
+    }
+    std::string e = ctx->tracer->render_async(ctx->scene, *ctx->bvh, *desc, ctx->stream, ctx->d_error);
+    if (!e.empty()) return fail(ctx, LTS_ERR_ARG, e);
+    return LTS_OK;
+}
+
+int lts_film_get(lts_ctx* ctx, float* film_rgb, double* film_sums) {
+    if (!ctx) return LTS_ERR_ARG;
+    if (!ctx->tracer) return fail(ctx, LTS_ERR_STATE, "nothing rendered");
+    int rc = check_device_error(ctx);
+    if (rc) return rc;
+    std::string e = ctx->tracer->film_get(ctx->scene, film_rgb, film_sums, ctx->stream);
+    if (!e.empty()) return fail(ctx, LTS_ERR_CUDA, e);
+    return LTS_OK;
+}
+
+int lts_write_image(const char* path, const float* rgb, int32_t w, int32_t h, int32_t format) {
+    if (!path || !rgb || w < 1 || h < 1) return LTS_ERR_ARG;
+    if (format == 1) {  // ImageO.cuh:16-50
+        FILE* f = fopen(path, "wb");
+        if (!f) return LTS_ERR_IO;
+        fprintf(f, "PF\n%d %d\n%f\n", w, h, -1.0f);
+        const size_t cnt = 3 * (size_t)w * h;
+        const bool ok = fwrite(rgb, sizeof(float), cnt, f) == cnt;
+        fclose(f);
+        return ok ? LTS_OK : LTS_ERR_IO;
+    }
+    FILE* f = fopen(path, "w");  // ImageO.cuh:52-78
+    if (!f) return LTS_ERR_IO;
+    fprintf(f, "P3\n%d %d\n%d\n", w, h, 255);
+    for (long i = 0; i < (long)w * h; ++i) {
+        int c[3];
+        for (int k = 0; k < 3; ++k) {
+            float x = rgb[3 * i + k];
+            x = (x < 0) ? 0 : ((x > 1) ? 1 : x);
+            c[k] = int(powf(x, 1 / 2.2f) * 255 + 0.5);
+        }
+        fprintf(f, "%d %d %d ", c[0], c[1], c[2]);
+    }
+    fclose(f);
+    return LTS_OK;
+}
+
+int lts_get_metrics(lts_ctx* ctx, lts_metrics* out) {
+    if (!ctx || !out) return LTS_ERR_ARG;
+    *out = ctx->metrics;
+    out->device_bytes = (int64_t)dev_bytes_in_use();
+    out->kernel_launches = (ctx->bvh ? ctx->bvh->launches : 0) + (ctx->tracer ? ctx->tracer->last_launches : 0);
+    return LTS_OK;
+}
+
+}  // extern "C"

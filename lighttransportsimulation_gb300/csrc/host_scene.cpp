@@ -1,0 +1,487 @@
+// Host loader for the reference's input files.  Compiled with -ffp-contract=off so that
+// every float expression below rounds exactly as the reference's host code does
+// (core/SceneLoader.cuh, core/FileIO.cuh, geometry/Transform.cuh, rendering/Camera.cu,
+// rendering/Filter.cuh, intergrators/IntegratorHelper.cuh, sampling/Sampling.cuh).
+#include "host_scene.hpp"
+
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+#include "../../include/lts_capi.h"
+
+namespace lts {
+namespace {
+
+// M_PI as <math.h> defines it on Linux (a double): the reference's `#ifndef M_PI` fallback
+// (core/GeneralHelper.cuh:8-10) is not taken there.
+constexpr double kPi = 3.14159265358979323846;
+
+struct V3 {
+    float x, y, z;
+};
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 scale(V3 a, float f) { return {f * a.x, f * a.y, f * a.z}; }  // Vector3::operator*(U f): f * x
+inline float len2(V3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+// geometry/Geometry.cuh:76-83: products and differences in double, rounded to float once.
+inline V3 cross_d(V3 a, V3 b) {
+    const double ax = a.x, ay = a.y, az = a.z, bx = b.x, by = b.y, bz = b.z;
+    return {(float)((ay * bz) - (az * by)), (float)((az * bx) - (ax * bz)), (float)((ax * by) - (ay * bx))};
+}
+inline V3 normalize_q(V3 v) { return scale(v, quake_rsqrt(len2(v))); }
+
+struct Quat {
+    float w = 1, x = 0, y = 0, z = 0;
+};
+// geometry/Transform.cuh:71-80 (quaternionMult), left-to-right sums.
+inline Quat qmul(const Quat& a, const Quat& b) {
+    Quat r;
+    r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
+    r.x = a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y;
+    r.y = a.w * b.y - a.x * b.z + a.y * b.w + a.z * b.x;
+    r.z = a.w * b.z + a.x * b.y - a.y * b.x + a.z * b.w;
+    return r;
+}
+inline Quat conj(const Quat& q) { return Quat{q.w, -q.x, -q.y, -q.z}; }
+
+struct Xform {  // geometry/Transform.cuh:138-200 (translation, rotation, scale)
+    V3 t{0, 0, 0};
+    Quat r;
+    float s = 1;
+    // Point/vector transform, Transform.cuh:222-233: rotate, scale, translate.
+    V3 point(V3 p) const {
+        Quat q{0.0f, p.x, p.y, p.z};
+        Quat tq = qmul(qmul(r, q), conj(r));
+        return add(scale(V3{tq.x, tq.y, tq.z}, s), t);
+    }
+    // Normal transform, Transform.cuh:235-240: inverse rotation, then normalize.
+    V3 normal(V3 n) const {
+        Quat q{0.0f, n.x, n.y, n.z};
+        Quat tq = qmul(qmul(conj(r), q), r);
+        return normalize_q(V3{tq.x, tq.y, tq.z});
+    }
+};
+
+Xform make_xform(V3 t, V3 axis, float theta, float scl) {
+    Xform x;
+    x.t = t;
+    const float th = fmodf(theta, (float)(2 * kPi));  // Transform.cuh:170-175
+    x.r.w = cosf(th / 2);                              // axisAngleToQuaternion, :109-115
+    x.r.x = axis.x * sinf(th / 2);
+    x.r.y = axis.y * sinf(th / 2);
+    x.r.z = axis.z * sinf(th / 2);
+    x.s = scl;
+    return x;
+}
+
+class Tokens {
+   public:
+    bool open(const std::string& path) {
+        std::ifstream f(path);
+        if (!f.is_open()) return false;
+        std::stringstream ss;
+        ss << f.rdbuf();
+        data_ = ss.str();
+        return true;
+    }
+    bool next(std::string* t) {
+        while (pos_ < data_.size() && isspace((unsigned char)data_[pos_])) ++pos_;
+        if (pos_ >= data_.size()) return false;
+        size_t b = pos_;
+        while (pos_ < data_.size() && !isspace((unsigned char)data_[pos_])) ++pos_;
+        *t = data_.substr(b, pos_ - b);
+        return true;
+    }
+
+   private:
+    std::string data_;
+    size_t pos_ = 0;
+};
+
+struct ParseError {
+    int code;
+    std::string msg;
+};
+
+std::string tok(Tokens& s, const char* what) {
+    std::string t;
+    if (!s.next(&t)) throw ParseError{LTS_ERR_PARSE, std::string("unexpected end of file reading ") + what};
+    return t;
+}
+float tokf(Tokens& s, const char* what) {
+    std::string t = tok(s, what);
+    try {
+        return std::stof(t);
+    } catch (...) {
+        throw ParseError{LTS_ERR_PARSE, std::string("bad number '") + t + "' for " + what};
+    }
+}
+int toki(Tokens& s, const char* what) {
+    std::string t = tok(s, what);
+    try {
+        return std::stoi(t);
+    } catch (...) {
+        throw ParseError{LTS_ERR_PARSE, std::string("bad integer '") + t + "' for " + what};
+    }
+}
+
+struct MeshData {
+    int32_t ntri = 0, np = 0, nuv = 0, nn = 0;
+    std::vector<float> p, uv, n;
+    std::vector<int32_t> idx;
+};
+
+// core/FileIO.cuh:170-206 (binMeshRead), with size checks the reference does not make.
+MeshData read_bin(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f.good()) throw ParseError{LTS_ERR_IO, "cannot open mesh " + path + " (.obj input is not supported)"};
+    f.seekg(0, std::ios::end);
+    const long long size = (long long)f.tellg();
+    f.seekg(0, std::ios::beg);
+    MeshData m;
+    int32_t hdr[4];
+    if (size < 16 || !f.read((char*)hdr, 16)) throw ParseError{LTS_ERR_PARSE, "short mesh header in " + path};
+    m.ntri = hdr[0];
+    m.np = hdr[1];
+    m.nuv = hdr[2];
+    m.nn = hdr[3];
+    if (m.ntri < 0 || m.np < 0 || m.nuv < 0 || m.nn < 0)
+        throw ParseError{LTS_ERR_PARSE, "negative counts in " + path};
+    const long long need = 16 + 12LL * m.np + 8LL * m.nuv + 12LL * m.nn + 36LL * m.ntri;
+    if (size < need) throw ParseError{LTS_ERR_PARSE, "truncated mesh " + path};
+    m.p.resize(3 * (size_t)m.np);
+    m.uv.resize(2 * (size_t)m.nuv);
+    m.n.resize(3 * (size_t)m.nn);
+    m.idx.resize(9 * (size_t)m.ntri);
+    f.read((char*)m.p.data(), 12LL * m.np);
+    f.read((char*)m.uv.data(), 8LL * m.nuv);
+    f.read((char*)m.n.data(), 12LL * m.nn);
+    f.read((char*)m.idx.data(), 36LL * m.ntri);
+    for (int32_t t = 0; t < m.ntri; ++t)
+        for (int c = 0; c < 3; ++c) {
+            const int32_t ip = m.idx[9 * t + 3 * c], iu = m.idx[9 * t + 3 * c + 1], in = m.idx[9 * t + 3 * c + 2];
+            if (ip < 0 || ip >= m.np || (m.nuv > 0 && (iu < 0 || iu >= m.nuv)) || (m.nn > 0 && (in < 0 || in >= m.nn)))
+                throw ParseError{LTS_ERR_PARSE, "vertex index out of range in " + path};
+        }
+    return m;
+}
+
+HostTexture read_texture(Tokens& s, bool scene_stream, int subject_images) {
+    HostTexture t;
+    const std::string ty = tok(s, "texture type");
+    const char c = ty[0];
+    int len = 0;  // SceneLoader.cuh:147-150
+    if (c == 'i') len = 1;
+    else if (c == 'f' || c == 'w') len = 2;
+    else if (c == 'c') len = 3;
+    else if (c == 'm') len = 4;
+    float v[4] = {0, 0, 0, 0};
+    for (int i = 0; i < len; ++i) {
+        v[i] = tokf(s, "texture parameter");
+        if (c == 'i' && scene_stream) v[i] += subject_images;
+    }
+    switch (c) {  // setMatTexture, SceneLoader.cuh:362-391
+        case 'c': t.kind = TEX_CONSTANT; break;
+        case 'f': t.kind = TEX_FBM; break;
+        case 'w': t.kind = TEX_WRINKLED; break;
+        case 'm': t.kind = TEX_MARBLE; break;
+        case 'v': t.kind = TEX_WINDY; break;
+        case 'i':
+            throw ParseError{LTS_ERR_UNSUPPORTED, "image textures ('i') are outside this renderer's scope"};
+        default:
+            throw ParseError{LTS_ERR_UNSUPPORTED, std::string("texture type '") + c + "' is not supported"};
+    }
+    memcpy(t.v, v, sizeof v);
+    return t;
+}
+
+}  // namespace
+
+// geometry/Geometry.cuh:15-29 with the 32-bit integer read of the Windows (LLP64) build.
+float quake_rsqrt(float f) {
+    const float threehalfs = 1.5f;
+    float x2 = f * 0.5f, y = f;
+    int32_t i;
+    memcpy(&i, &y, 4);
+    i = 0x5f3759df - (i >> 1);
+    memcpy(&y, &i, 4);
+    y = y * (threehalfs - (x2 * y * y));
+    y = y * (threehalfs - (x2 * y * y));
+    return y;
+}
+
+int32_t HostScene::max_mesh_triangles() const {
+    int32_t m = 0;
+    for (int32_t c : mesh_tri_count) m = c > m ? c : m;
+    return m;
+}
+
+void HostScene::triangle_soup(std::vector<float>& out) const {
+    const int32_t nt = triangles();
+    out.resize(9 * (size_t)nt);
+    for (int32_t t = 0; t < nt; ++t)
+        for (int c = 0; c < 3; ++c)
+            for (int k = 0; k < 3; ++k) out[9 * (size_t)t + 3 * c + k] = p[3 * (size_t)tri_p[3 * t + c] + k];
+}
+
+std::string read_app_params(const std::string& path, AppParams* out, int* code) {
+    Tokens s;
+    if (!s.open(path)) {
+        *code = LTS_ERR_IO;
+        return "cannot open " + path;
+    }
+    try {  // core/FileIO.cuh:234-257
+        out->width = toki(s, "width");
+        out->height = toki(s, "height");
+        out->spp = toki(s, "spp");
+        out->max_bounce = toki(s, "bounces");
+        out->rr_start = toki(s, "roulette start");
+        out->format = toki(s, "format");
+        out->output = tok(s, "output") + (out->format ? ".pfm" : ".hdr");
+        out->scene = tok(s, "scene");
+        std::string sub;
+        out->subject = s.next(&sub) ? sub : "";
+    } catch (const ParseError& e) {
+        *code = e.code;
+        return e.msg;
+    }
+    *code = LTS_OK;
+    return "";
+}
+
+std::string load_scene(const std::string& root, const std::string& scene_name, const std::string& subject_name,
+                       int32_t width, int32_t height, HostScene* sc, int* code) {
+    *code = LTS_OK;
+    if (width < 2 || height < 2) {
+        *code = LTS_ERR_ARG;
+        return "film must be at least 2x2 (the camera divides by resolution - 1)";
+    }
+    const bool has_subject = !subject_name.empty();
+    Tokens ss, sb;
+    if (!ss.open(root + scene_name + ".scene")) {
+        *code = LTS_ERR_IO;
+        return "cannot open " + root + scene_name + ".scene";
+    }
+    if (has_subject && !sb.open(root + subject_name + ".subject")) {
+        *code = LTS_ERR_IO;
+        return "cannot open " + root + subject_name + ".subject";
+    }
+    try {
+        // Camera (SceneLoader.cuh:33-57).
+        float cf[11];
+        for (int i = 0; i < 11; ++i) cf[i] = tokf(ss, "camera");
+        // Subject transform (SceneLoader.cuh:59-77).
+        float xf[8];
+        for (int i = 0; i < 8; ++i) xf[i] = tokf(ss, "subject transform");
+        const Xform subject_xf = make_xform({xf[0], xf[1], xf[2]}, {xf[3], xf[4], xf[5]}, xf[6], xf[7]);
+
+        // Images (SceneLoader.cuh:79-97): counted and skipped, never decoded here.
+        int sub_images = 0, images = 0;
+        if (has_subject) images = sub_images = toki(sb, "subject image count");
+        images += toki(ss, "scene image count");
+        for (int i = 0; i < images; ++i) {
+            Tokens& s = i >= sub_images ? ss : sb;
+            tok(s, "image wrap");
+            tok(s, "image path");
+        }
+        // Meshes (SceneLoader.cuh:99-113).
+        int sub_meshes = 0, meshes = 0;
+        if (has_subject) meshes = sub_meshes = toki(sb, "subject mesh count");
+        meshes += toki(ss, "scene mesh count");
+        std::vector<std::string> files;
+        for (int m = 0; m < meshes; ++m) files.push_back(root + tok(m >= sub_meshes ? ss : sb, "mesh path"));
+        // Materials (SceneLoader.cuh:115-171; codes of SceneLoader_kernels.cu:8-50).
+        int sub_mats = 0, mats = 0;
+        if (has_subject) mats = sub_mats = toki(sb, "subject material count");
+        mats += toki(ss, "scene material count");
+        sc->materials.clear();
+        for (int m = 0; m < mats; ++m) {
+            const bool scene_stream = m >= sub_mats;
+            Tokens& s = scene_stream ? ss : sb;
+            const std::string ty = tok(s, "material type");
+            HostMaterial hm;
+            switch (ty[0]) {
+                case 'L': hm.kind = MAT_MATTE; hm.tex[0] = read_texture(s, scene_stream, sub_images); break;
+                case 'R': hm.kind = MAT_MIRROR; hm.tex[0] = read_texture(s, scene_stream, sub_images); break;
+                case 'G':
+                    hm.kind = MAT_GLASS;
+                    hm.tex[0] = read_texture(s, scene_stream, sub_images);
+                    hm.tex[1] = read_texture(s, scene_stream, sub_images);
+                    break;
+                case 'M': hm.kind = MAT_NONE; break;
+                case 'C':
+                    hm.kind = MAT_METAL;
+                    hm.tex[0] = read_texture(s, scene_stream, sub_images);
+                    hm.tex[1] = read_texture(s, scene_stream, sub_images);
+                    if (hm.tex[1].kind != TEX_CONSTANT)
+                        throw ParseError{LTS_ERR_PARSE, "conductor eta must be a constant ('c') record"};
+                    break;
+                default: throw ParseError{LTS_ERR_PARSE, std::string("unknown material type '") + ty + "'"};
+            }
+            hm.extra = tokf(s, "material extra parameter");
+            if (hm.kind == MAT_MATTE && hm.extra != 0) {  // OrenNayar ctor, Microfacet.cuh:18-25
+                const float sigma = (float)((double)hm.extra * (kPi / 180));  // toRadians, GeneralHelper.cuh
+                const float sigma2 = sigma * sigma;
+                hm.on_a = 1.0f - (sigma2 / (2.0f * (sigma2 + 0.33f)));
+                hm.on_b = 0.45f * sigma2 / (sigma2 + 0.09f);
+            }
+            sc->materials.push_back(hm);
+        }
+        // Lights (SceneLoader.cuh:173-193).
+        const int area_meshes = toki(ss, "area light mesh count");
+        std::vector<float> les;
+        for (int i = 0; i < 3 * area_meshes; ++i) les.push_back(tokf(ss, "area light Le"));
+        const bool has_inf = toki(ss, "infinite light flag") > 0;
+        float inf_le[3] = {0, 0, 0};
+        if (has_inf)
+            for (int i = 0; i < 3; ++i) inf_le[i] = tokf(ss, "infinite light Le");
+        if (area_meshes < 0 || area_meshes > meshes)
+            throw ParseError{LTS_ERR_PARSE, "area light mesh count exceeds mesh count"};
+        if (mats < meshes)
+            throw ParseError{LTS_ERR_PARSE, "fewer materials than meshes (material index == mesh index)"};
+
+        // Mesh loading + transforms (SceneLoader.cuh:264-282, shapes/Triangle.cu:20-43).
+        sc->p.clear(); sc->n.clear(); sc->uv.clear();
+        sc->tri_p.clear(); sc->tri_n.clear(); sc->tri_uv.clear(); sc->tri_mesh.clear();
+        sc->mesh_first_tri.clear(); sc->mesh_tri_count.clear();
+        const Xform ident;  // Transform(1)
+        for (int m = 0; m < meshes; ++m) {
+            MeshData md = read_bin(files[m] + ".bin");
+            const Xform& X = m >= sub_meshes ? ident : subject_xf;
+            const int32_t pbase = (int32_t)(sc->p.size() / 3), nbase = (int32_t)(sc->n.size() / 3),
+                          uvbase = (int32_t)(sc->uv.size() / 2);
+            for (int32_t i = 0; i < md.np; ++i) {
+                V3 w = X.point({md.p[3 * i], md.p[3 * i + 1], md.p[3 * i + 2]});
+                sc->p.push_back(w.x); sc->p.push_back(w.y); sc->p.push_back(w.z);
+            }
+            for (int32_t i = 0; i < md.nn; ++i) {
+                V3 w = X.normal({md.n[3 * i], md.n[3 * i + 1], md.n[3 * i + 2]});
+                sc->n.push_back(w.x); sc->n.push_back(w.y); sc->n.push_back(w.z);
+            }
+            sc->uv.insert(sc->uv.end(), md.uv.begin(), md.uv.end());
+            sc->mesh_first_tri.push_back((int32_t)sc->tri_mesh.size());
+            sc->mesh_tri_count.push_back(md.ntri);
+            for (int32_t t = 0; t < md.ntri; ++t) {
+                for (int c = 0; c < 3; ++c) {
+                    sc->tri_p.push_back(pbase + md.idx[9 * t + 3 * c]);
+                    sc->tri_uv.push_back(md.nuv > 0 ? uvbase + md.idx[9 * t + 3 * c + 1] : -1);
+                    sc->tri_n.push_back(md.nn > 0 ? nbase + md.idx[9 * t + 3 * c + 2] : -1);
+                }
+                sc->tri_mesh.push_back(m);
+            }
+        }
+        sc->subject_meshes = sub_meshes;
+        sc->area_light_meshes = area_meshes;
+        sc->has_infinite = has_inf;
+        const int32_t ntri = sc->triangles();
+        if (ntri < 1) throw ParseError{LTS_ERR_PARSE, "scene has no triangles"};
+
+        // Lights (SceneLoader_kernels.cu:52-111).  With one emissive mesh this is the
+        // reference's array exactly (slot = triangle index within the mesh); several emissive
+        // meshes race for the same slots in the reference, and are concatenated here.
+        sc->lights.clear();
+        sc->prim_light.assign(ntri, -1);
+        for (int m = meshes - area_meshes; m < meshes; ++m) {
+            const int le = meshes - m - 1;  // Le listed in reverse mesh order
+            for (int32_t k = 0; k < sc->mesh_tri_count[m]; ++k) {
+                HostLight L;
+                L.kind = LIGHT_AREA;
+                L.prim = sc->mesh_first_tri[m] + k;
+                for (int c = 0; c < 3; ++c) L.L[c] = les[3 * le + c];
+                const float* P = sc->p.data();
+                const int32_t* ti = &sc->tri_p[3 * (size_t)L.prim];
+                V3 p0{P[3 * ti[0]], P[3 * ti[0] + 1], P[3 * ti[0] + 2]};
+                V3 p1{P[3 * ti[1]], P[3 * ti[1] + 1], P[3 * ti[1] + 2]};
+                V3 p2{P[3 * ti[2]], P[3 * ti[2] + 1], P[3 * ti[2] + 2]};
+                V3 c = cross_d(sub(p1, p0), sub(p2, p0));
+                L.area = 0.5f * sqrtf(len2(c));  // Triangle.cuh:57-62
+                sc->prim_light[L.prim] = (int32_t)sc->lights.size();
+                sc->lights.push_back(L);
+            }
+        }
+        if (has_inf) {
+            HostLight L;
+            L.kind = LIGHT_INFINITE;
+            for (int c = 0; c < 3; ++c) L.L[c] = inf_le[c];
+            // preprocess(info->bounds[0]) (SceneLoader_kernels.cu:102): triangle 0's AABB.
+            const float* P = sc->p.data();
+            float mn[3], mx[3];
+            for (int k = 0; k < 3; ++k) {
+                const float a = P[3 * sc->tri_p[0] + k], b = P[3 * sc->tri_p[1] + k], c = P[3 * sc->tri_p[2] + k];
+                mn[k] = fminf(fminf(a, b), c);
+                mx[k] = fmaxf(fmaxf(a, b), c);
+            }
+            for (int k = 0; k < 3; ++k) L.p[k] = mn[k] * 0.5f + mx[k] * 0.5f;  // Light.cuh:136-139
+            V3 d{mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2]};
+            L.radius = sqrtf(len2(d)) / 2.0f;
+            sc->lights.push_back(L);
+        }
+        // Light power distribution (IntegratorHelper.cuh:147-162, Sampling.cuh:123-144).
+        const int nl = (int)sc->lights.size();
+        sc->light_func.assign(nl, 0.f);
+        for (int l = 0; l < nl; ++l) {
+            const HostLight& L = sc->lights[l];
+            float s[3];
+            if (L.kind == LIGHT_AREA) {
+                for (int c = 0; c < 3; ++c) s[c] = (L.L[c] * L.area) * (float)kPi;  // Light.cuh:104-106
+            } else if (L.kind == LIGHT_INFINITE) {
+                const float v = (float)(kPi * (double)L.radius);  // Light.cuh:141-143
+                for (int c = 0; c < 3; ++c) s[c] = L.L[c] * v;
+            } else {
+                const float v = (float)(4 * kPi);  // Light.cuh:83-85
+                for (int c = 0; c < 3; ++c) s[c] = L.L[c] * v;
+            }
+            sc->light_func[l] = 0.212671f * s[0] + 0.715160f * s[1] + 0.072169f * s[2];  // Spectrum.cuh:217-220
+        }
+        sc->light_cdf.assign(nl + 1, 0.f);
+        for (int i = 1; i < nl + 1; ++i) sc->light_cdf[i] = sc->light_cdf[i - 1] + sc->light_func[i - 1] / nl;
+        const float func_int = sc->light_cdf[nl];
+        sc->light_func_int = func_int;
+        if (func_int == 0) {
+            for (int i = 1; i < nl + 1; ++i) sc->light_cdf[i] = (float)i / (float)nl;
+        } else {
+            for (int i = 1; i < nl + 1; ++i) sc->light_cdf[i] /= func_int;
+        }
+
+        // Camera (rendering/Camera.cu:9-43), aperture 0 (LightTransportSimulation.cu:70).
+        sc->width = width;
+        sc->height = height;
+        {
+            const V3 from{cf[0], cf[1], cf[2]}, at{cf[3], cf[4], cf[5]}, vup{cf[6], cf[7], cf[8]};
+            const float vfov = cf[9], focus = cf[10];
+            const float aspect = (float)width / (float)height;
+            const float theta = (float)((double)vfov * kPi / 180.0f);
+            const float h = tanf(theta / 2);
+            const float vh = 2 * h, vw = aspect * vh;
+            const V3 w = normalize_q(sub(from, at));
+            const V3 u = normalize_q(cross_d(vup, w));
+            const V3 v = cross_d(w, u);
+            const V3 right = scale(u, focus * vw), up = scale(v, focus * vh);
+            const V3 llc = sub(sub(sub(from, scale(right, 0.5f)), scale(up, 0.5f)), scale(w, focus));
+            const float camv[23] = {from.x, from.y, from.z, right.x, right.y, right.z, up.x, up.y, up.z,
+                                    llc.x,  llc.y,  llc.z,  u.x,     u.y,     u.z,     v.x,  v.y,  v.z,
+                                    w.x,    w.y,    w.z,    0.0f / 2, focus};
+            memcpy(sc->cam, camv, sizeof camv);
+        }
+        // Gaussian filter table (Filter.cuh:32-50,82-99): radius (1,1), alpha 1.
+        {
+            const float alpha = 1.0f, rx = 1.0f, ry = 1.0f;
+            const float expx = expf(-alpha * rx * rx), expy = expf(-alpha * ry * ry);
+            for (int y = 0; y < 16; ++y)
+                for (int x = 0; x < 16; ++x) {
+                    const float px = (x + 0.5f) * rx / 16, py = (y + 0.5f) * ry / 16;
+                    const float gx = fmaxf(0, expf(-alpha * px * px) - expx);
+                    const float gy = fmaxf(0, expf(-alpha * py * py) - expy);
+                    sc->filter[y * 16 + x] = gx * gy;
+                }
+        }
+    } catch (const ParseError& e) {
+        *code = e.code;
+        return e.msg;
+    }
+    return "";
+}
+
+}  // namespace lts

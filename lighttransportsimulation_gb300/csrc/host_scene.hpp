@@ -1,0 +1,89 @@
+// Host-side scene model: what the reference's loader builds on the device with `new`
+// (core/SceneLoader.cuh:195-360, core/SceneLoader_kernels.cu:8-111), held here as flat
+// tables that are uploaded to the GPU as structure-of-arrays.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace lts {
+
+enum TexKind : int32_t { TEX_CONSTANT = 0, TEX_FBM = 1, TEX_WRINKLED = 2, TEX_MARBLE = 3, TEX_WINDY = 4 };
+enum MatKind : int32_t {
+    MAT_NONE = 0,   // 'M' in the reference: parsed, no material constructed -> no BSDF
+    MAT_MATTE = 1,  // 'L' MatteMaterial (Material.cuh:31-55)
+    MAT_GLASS = 2,  // 'G' GlassMaterial (Material.cuh:57-76)
+    MAT_MIRROR = 3, // 'R' MirrorMaterial (Material.cuh:78-95)
+    MAT_METAL = 4   // 'C' (grammar extension) MetalMaterial with alpha given directly (Material.cuh:97-130)
+};
+enum LightKind : int32_t { LIGHT_AREA = 0, LIGHT_INFINITE = 1, LIGHT_POINT = 2 };
+
+struct HostTexture {
+    int32_t kind = TEX_CONSTANT;
+    float v[4] = {0, 0, 0, 0};  // constant rgb | octaves, omega | octaves, omega, scale, variation
+};
+
+struct HostMaterial {
+    int32_t kind = MAT_NONE;
+    HostTexture tex[2];  // matte Kd | glass R, T | mirror R | metal k, eta
+    float extra = 0;     // matte sigma (degrees) | glass eta | metal alpha
+    float on_a = 0, on_b = 0;  // Oren-Nayar A, B (models/Microfacet.cuh:18-25) for sigma != 0
+};
+
+struct HostLight {
+    int32_t kind = LIGHT_AREA;
+    int32_t prim = -1;          // area light: primitive index in scene order
+    float L[3] = {0, 0, 0};     // Lemit / Lmap / I
+    float p[3] = {0, 0, 0};     // point light position; infinite light world center
+    float radius = 0;           // infinite light world radius
+    float area = 0;             // area light triangle area
+};
+
+struct HostScene {
+    int32_t width = 0, height = 0;
+    // Camera (rendering/Camera.cu:9-43): o, right, up, llc, u, v, w, lensRadius, focalDist.
+    float cam[23] = {0};
+    // Gaussian filter table (rendering/Filter.cuh:32-50,82-99), 16 x 16, radius 1, alpha 1.
+    float filter[256] = {0};
+
+    // Vertex pools (world space) and per-triangle corner indices into them.
+    std::vector<float> p;       // 3 per vertex
+    std::vector<float> n;       // 3 per normal
+    std::vector<float> uv;      // 2 per uv
+    std::vector<int32_t> tri_p;   // 3 per triangle
+    std::vector<int32_t> tri_n;   // 3 per triangle, -1 when the mesh has no normals
+    std::vector<int32_t> tri_uv;  // 3 per triangle, -1 when the mesh has no uvs
+    std::vector<int32_t> tri_mesh;
+
+    std::vector<int32_t> mesh_first_tri, mesh_tri_count;
+    int32_t subject_meshes = 0;
+    int32_t area_light_meshes = 0;
+    bool has_infinite = false;
+
+    std::vector<HostMaterial> materials;  // one per mesh (material index == mesh index)
+    std::vector<int32_t> prim_light;      // per triangle: light index or -1
+    std::vector<HostLight> lights;        // sampling order of the reference's light array
+    std::vector<float> light_func, light_cdf;  // Distribution1D over power().y()
+    float light_func_int = 0;                  // Distribution1D::funcInt (before normalising)
+
+    int32_t triangles() const { return (int32_t)tri_mesh.size(); }
+    int32_t max_mesh_triangles() const;
+    // World-space positions of every triangle, 9 floats each, in scene order.
+    void triangle_soup(std::vector<float>& out) const;
+};
+
+struct AppParams {
+    int32_t width = 0, height = 0, spp = 0, max_bounce = 0, rr_start = 0, format = 0;
+    std::string output, scene, subject;
+};
+
+// All return "" on success, else an error message; *code receives an LTS_ERR_* value.
+std::string read_app_params(const std::string& path, AppParams* out, int* code);
+std::string load_scene(const std::string& root, const std::string& scene, const std::string& subject,
+                       int32_t width, int32_t height, HostScene* out, int* code);
+
+// Reference float helpers shared by loader code paths (host, no FMA contraction).
+float quake_rsqrt(float f);
+
+}  // namespace lts

@@ -1,0 +1,486 @@
+// LBVH build kernels (sm_103a).  Stages and the reference code each one restates:
+//   1 k_scene_bounds   per-triangle AABB + scene AABB            BVH.cuh:92-97, Triangle.cuh:48-53,
+//                                                                 Geometry.cuh:647-655
+//   2 k_morton         centroid -> 30-bit Morton code + ids, and the 4x256 radix histograms
+//                                                                 BVH.cuh:101-116,134-137, Bound.cuh:169-175
+//   3 k_digit_prefix + 4 x k_onesweep   stable LSD radix sort of (code, id), 8-bit digits,
+//                      decoupled look-back (replaces thrust::stable_sort_by_key, BVH.cuh:140-146)
+//   4 k_topology       Karras split per interior node             BVH.cuh:173-236
+//   5 k_refit          bottom-up AABBs, second arrival unions     BVH.cuh:238-262
+// Output layout: one 64-byte node per interior node carrying both child boxes (see lbvh.cuh).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <string>
+
+#include "dev_common.cuh"
+#include "lbvh.cuh"
+
+namespace lts {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr uint32_t kFlagAgg = 1u << 30, kFlagPrefix = 2u << 30, kCountMask = (1u << 30) - 1;
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Stage a block's run of `count` triangles (9 floats each) into shared memory with 16-byte
+// loads when the run start is 16-byte aligned, scalar loads otherwise.
+__device__ __forceinline__ void stage_tris(const float* __restrict__ tri, long first, int count, float* s) {
+    const long f0 = first * 9;
+    const int nf = count * 9;
+    const float* src = tri + f0;
+    if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+        const int n4 = nf >> 2;
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+        for (int i = threadIdx.x; i < n4; i += blockDim.x) reinterpret_cast<float4*>(s)[i] = __ldg(s4 + i);
+        for (int i = (n4 << 2) + threadIdx.x; i < nf; i += blockDim.x) s[i] = __ldg(src + i);
+    } else {
+        for (int i = threadIdx.x; i < nf; i += blockDim.x) s[i] = __ldg(src + i);
+    }
+}
+
+__device__ __forceinline__ void tri_bounds(const float* t, float mn[3], float mx[3]) {
+    // Triangle::worldBound: bUnion(Bounds3f(p0, p1), p2)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        mn[k] = fminf(fminf(t[k], t[3 + k]), t[6 + k]);
+        mx[k] = fmaxf(fmaxf(t[k], t[3 + k]), t[6 + k]);
+    }
+}
+
+// ------------------------------------------------------------------ 1. scene bounds
+__global__ __launch_bounds__(kBlock) void k_scene_bounds(const float* __restrict__ tri, int n,
+                                                         uint32_t* __restrict__ gb) {
+    __shared__ float s_tri[kBlock * 9];
+    uint32_t kmn[3] = {~0u, ~0u, ~0u}, kmx[3] = {0u, 0u, 0u};
+    for (long first = (long)blockIdx.x * kBlock; first < n; first += (long)gridDim.x * kBlock) {
+        const int cnt = (int)min((long)kBlock, n - first);
+        __syncthreads();
+        stage_tris(tri, first, cnt, s_tri);
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            float mn[3], mx[3];
+            tri_bounds(s_tri + 9 * threadIdx.x, mn, mx);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                kmn[k] = min(kmn[k], float_key(mn[k]));
+                kmx[k] = max(kmx[k], float_key(mx[k]));
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            kmn[k] = min(kmn[k], __shfl_xor_sync(0xffffffffu, kmn[k], o));
+            kmx[k] = max(kmx[k], __shfl_xor_sync(0xffffffffu, kmx[k], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(gb + k, kmn[k]);
+            atomicMax(gb + 3 + k, kmx[k]);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ 2. Morton codes + histograms
+__device__ __forceinline__ uint32_t left_shift3(uint32_t x) {
+    // BVH.cuh:101-109
+    if (x == (1u << 10)) --x;
+    x = (x | (x << 16)) & 0b00000011000000000000000011111111u;
+    x = (x | (x << 8)) & 0b00000011000000001111000000001111u;
+    x = (x | (x << 4)) & 0b00000011000011000011000011000011u;
+    x = (x | (x << 2)) & 0b00001001001001001001001001001001u;
+    return x;
+}
+
+__global__ __launch_bounds__(kBlock) void k_morton(const float* __restrict__ tri, int n, const uint32_t* __restrict__ gb,
+                                                   int code_limit, uint32_t* __restrict__ codes,
+                                                   int32_t* __restrict__ ids, uint32_t* __restrict__ hist) {
+    __shared__ float s_tri[kBlock * 9];
+    __shared__ uint32_t s_hist[4 * 256];
+    for (int i = threadIdx.x; i < 4 * 256; i += kBlock) s_hist[i] = 0;
+    float gmn[3], gmx[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        gmn[k] = key_float(gb[k]);
+        gmx[k] = key_float(gb[3 + k]);
+    }
+    for (long first = (long)blockIdx.x * kBlock; first < n; first += (long)gridDim.x * kBlock) {
+        const int cnt = (int)min((long)kBlock, n - first);
+        __syncthreads();
+        stage_tris(tri, first, cnt, s_tri);
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            const long i = first + threadIdx.x;
+            uint32_t code = 0;
+            int32_t id = 0;
+            if (code_limit < 0 || i < code_limit) {
+                float mn[3], mx[3];
+                tri_bounds(s_tri + 9 * threadIdx.x, mn, mx);
+                uint32_t q[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float c = mn[k] * 0.5f + mx[k] * 0.5f;        // BVH.cuh:95
+                    float o = c - gmn[k];                                // Bound.cuh:169-175
+                    if (gmx[k] > gmn[k]) o = __fdiv_rn(o, gmx[k] - gmn[k]);
+                    const float s = __fmul_rn((float)(1 << 10), o);     // * mortonScale (BVH.cuh:136)
+                    q[k] = (uint32_t)s;                                  // float -> uint32_t truncation
+                }
+                code = left_shift3(q[0]) | (left_shift3(q[1]) << 1) | (left_shift3(q[2]) << 2);
+                id = (int32_t)i;
+            }
+            codes[i] = code;
+            ids[i] = id;
+#pragma unroll
+            for (int p = 0; p < 4; ++p) atomicAdd(&s_hist[p * 256 + ((code >> (8 * p)) & 255u)], 1u);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 4 * 256; i += kBlock)
+        if (s_hist[i]) atomicAdd(hist + i, s_hist[i]);
+}
+
+// ------------------------------------------------------------------ 3. radix sort
+__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t wsum = 0;
+    for (int w = 0; w < warp; ++w) wsum += s_warp[w];
+    __syncthreads();
+    return wsum + x - v;
+}
+
+__global__ void k_digit_prefix(const uint32_t* __restrict__ hist, uint32_t* __restrict__ prefix) {
+    __shared__ uint32_t s_warp[8];
+    const uint32_t v = hist[blockIdx.x * 256 + threadIdx.x];
+    prefix[blockIdx.x * 256 + threadIdx.x] = block_excl_scan256(v, s_warp);
+}
+
+__global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __restrict__ kin, const int32_t* __restrict__ vin,
+                                                           uint32_t* __restrict__ kout, int32_t* __restrict__ vout,
+                                                           int n, int shift, const uint32_t* __restrict__ gprefix,
+                                                           uint32_t* __restrict__ status, uint32_t* __restrict__ tile_counter,
+                                                           uint32_t* __restrict__ err) {
+    __shared__ uint32_t s_keys[kSortTile];
+    __shared__ int32_t s_vals[kSortTile];
+    __shared__ uint32_t s_whist[kSortThreads / 32][256];
+    __shared__ uint32_t s_tile_start[256];
+    __shared__ uint32_t s_dst[256];
+    __shared__ uint32_t s_warp[8];
+    __shared__ int s_tile;
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(tile_counter, 1u);
+    for (int i = threadIdx.x; i < (kSortThreads / 32) * 256; i += kSortThreads) (&s_whist[0][0])[i] = 0;
+    __syncthreads();
+    const int tile = s_tile;
+    const long base = (long)tile * kSortTile;
+    const long wbase = base + (long)warp * 32 * kSortItems;
+
+    uint32_t key[kSortItems];
+    int32_t val[kSortItems];
+    uint32_t rank[kSortItems];
+#pragma unroll
+    for (int i = 0; i < kSortItems; ++i) {
+        const long idx = wbase + i * 32 + lane;
+        if (idx < n) {
+            key[i] = __ldg(kin + idx);
+            val[i] = __ldg(vin + idx);
+        } else {
+            key[i] = 0;
+            val[i] = 0;
+        }
+    }
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int i = 0; i < kSortItems; ++i) {
+        const long idx = wbase + i * 32 + lane;
+        const bool valid = idx < n;
+        const uint32_t d = (key[i] >> shift) & 255u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u);
+        const int leader = __ffs(peers) - 1;
+        uint32_t b = 0;
+        if (valid && lane == leader) {
+            b = s_whist[warp][d];
+            s_whist[warp][d] = b + __popc(peers);
+        }
+        b = __shfl_sync(0xffffffffu, b, leader);
+        rank[i] = b + __popc(peers & lt);
+    }
+    __syncthreads();
+    const uint32_t dig = threadIdx.x;
+    uint32_t tot = 0;
+#pragma unroll
+    for (int w = 0; w < kSortThreads / 32; ++w) {
+        const uint32_t c = s_whist[w][dig];
+        s_whist[w][dig] = tot;
+        tot += c;
+    }
+    uint32_t* st = status + (size_t)tile * 256;
+    st_relaxed(st + dig, (tile == 0 ? kFlagPrefix : kFlagAgg) | tot);
+    const uint32_t start = block_excl_scan256(tot, s_warp);
+    s_tile_start[dig] = start;
+    uint32_t excl = 0;
+    if (tile > 0) {
+        int k = tile - 1, spins = 0;
+        while (k >= 0) {
+            const uint32_t v = ld_relaxed(status + (size_t)k * 256 + dig);
+            const uint32_t f = v & ~kCountMask;
+            if (f == 0) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(err, DEV_ERR_LOOKBACK_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+                continue;
+            }
+            excl += v & kCountMask;
+            if (f == kFlagPrefix) break;
+            --k;
+        }
+        st_relaxed(st + dig, kFlagPrefix | (excl + tot));
+    }
+    s_dst[dig] = gprefix[dig] + excl;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kSortItems; ++i) {
+        const long idx = wbase + i * 32 + lane;
+        if (idx < n) {
+            const uint32_t d = (key[i] >> shift) & 255u;
+            const uint32_t pos = s_tile_start[d] + s_whist[warp][d] + rank[i];
+            s_keys[pos] = key[i];
+            s_vals[pos] = val[i];
+        }
+    }
+    __syncthreads();
+    const int tile_n = (int)min((long)kSortTile, n - base);
+    for (int j = threadIdx.x; j < tile_n; j += kSortThreads) {
+        const uint32_t k = s_keys[j];
+        const uint32_t d = (k >> shift) & 255u;
+        const uint32_t dst = s_dst[d] + (uint32_t)j - s_tile_start[d];
+        kout[dst] = k;
+        vout[dst] = s_vals[j];
+    }
+}
+
+// ------------------------------------------------------------------ 4. Karras topology
+__device__ __forceinline__ int delta(const uint32_t* __restrict__ c, int n, int a, int b) {
+    // BVH.cuh:173-190 (a is always in range)
+    if (b < 0 || b >= n) return -1;
+    uint32_t x = __ldg(c + a) ^ __ldg(c + b);
+    int extra = 0;
+    if (x == 0) {
+        extra = 40;
+        x = (uint32_t)(a ^ b);
+    }
+    return __clz((int)x) + extra;
+}
+
+__global__ __launch_bounds__(kBlock) void k_topology(const uint32_t* __restrict__ codes, int n, BvhNode* __restrict__ nodes,
+                                                     int32_t* __restrict__ parent) {
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= n - 1) return;
+    // BVH.cuh:192-236
+    const int d = (delta(codes, n, i, i + 1) - delta(codes, n, i, i - 1)) > 0 ? 1 : -1;
+    const int dmin = delta(codes, n, i, i - d);
+    long lmax = 128;
+    while (delta(codes, n, i, (int)(i + lmax * d)) > dmin) lmax *= 4;
+    int l = 0;
+    for (long t = lmax / 2; t >= 1; t /= 2)
+        if (delta(codes, n, i, (int)(i + (l + t) * d)) > dmin) l += (int)t;
+    const int j = i + l * d;
+    const int dnode = delta(codes, n, i, j);
+    int s = 0;
+    for (int t = (l + 1) / 2; t >= 1; t = (t == 1) ? 0 : (t + 1) / 2)
+        if (delta(codes, n, i, i + (s + t) * d) > dnode) s += t;
+    const int gamma = i + s * d + min(d, 0);
+    const int lo = min(i, j), hi = max(i, j);
+    const int left = (lo == gamma) ? ~gamma : gamma;
+    const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    nodes[i].d = make_int4(left, right, -1, 0);
+    const int lc = left < 0 ? (n - 1) + ~left : left;
+    const int rc = right < 0 ? (n - 1) + ~right : right;
+    parent[lc] = i << 1;
+    parent[rc] = (i << 1) | 1;
+}
+
+// ------------------------------------------------------------------ 5. refit
+__global__ __launch_bounds__(kBlock) void k_refit(const float* __restrict__ tri, int n, int mode, const int32_t* __restrict__ ids,
+                                                  const int32_t* __restrict__ parent, BvhNode* __restrict__ nodes,
+                                                  uint32_t* __restrict__ flags, int32_t* __restrict__ leaf_prim,
+                                                  float* __restrict__ root_bounds) {
+    const int l = blockIdx.x * kBlock + threadIdx.x;
+    if (l >= n) return;
+    const int prim = (mode == BVH_MODE_REFERENCE) ? l : __ldg(ids + l);
+    leaf_prim[l] = prim;
+    float t[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9L * prim + k);
+    float mn[3], mx[3];
+    tri_bounds(t, mn, mx);
+    if (n == 1) {
+        for (int k = 0; k < 3; ++k) {
+            root_bounds[k] = mn[k];
+            root_bounds[3 + k] = mx[k];
+        }
+        return;
+    }
+    int node = (n - 1) + l;
+    for (;;) {
+        const int pe = __ldg(parent + node);
+        const int p = pe >> 1;
+        float* P = reinterpret_cast<float*>(nodes + p);
+        if ((pe & 1) == 0) {  // left slot: a.xyz = min, a.w, b.x, b.y = max
+            P[0] = mn[0]; P[1] = mn[1]; P[2] = mn[2]; P[3] = mx[0]; P[4] = mx[1]; P[5] = mx[2];
+        } else {              // right slot: b.z, b.w, c.x = min, c.yzw = max
+            P[6] = mn[0]; P[7] = mn[1]; P[8] = mn[2]; P[9] = mx[0]; P[10] = mx[1]; P[11] = mx[2];
+        }
+        __threadfence();
+        if (atomicAdd(flags + p, 1u) == 0u) return;  // first arrival stops (BVH.cuh:251-255)
+        __threadfence();
+        const float4 a = __ldcg(&nodes[p].a), b = __ldcg(&nodes[p].b), c = __ldcg(&nodes[p].c);
+        mn[0] = fminf(a.x, b.z); mn[1] = fminf(a.y, b.w); mn[2] = fminf(a.z, c.x);  // bUnion(left, right)
+        mx[0] = fmaxf(a.w, c.y); mx[1] = fmaxf(b.x, c.z); mx[2] = fmaxf(b.y, c.w);
+        if (p == 0) {
+            for (int k = 0; k < 3; ++k) {
+                root_bounds[k] = mn[k];
+                root_bounds[3 + k] = mx[k];
+            }
+            return;
+        }
+        node = p;
+    }
+}
+
+inline int grid_for(long items, int per_block) { return (int)((items + per_block - 1) / per_block); }
+
+}  // namespace
+
+#define LTS_TRY(call)                                                                   \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) return std::string(#call ": ") + cudaGetErrorString(e_); \
+    } while (0)
+
+Lbvh::~Lbvh() {
+    void* ptrs[] = {nodes, root_bounds, leaf_prim, codes, ids, codes_alt_, hist_, status_, counters_, gbounds_, flags_, ids_alt_, parent_};
+    for (void* p : ptrs)
+        if (p) dev_free(p);
+    for (auto& e : ev_)
+        if (e) cudaEventDestroy(e);
+}
+
+std::string Lbvh::reserve(int nn) {
+    if (!ev_[0])
+        for (auto& e : ev_) LTS_TRY(cudaEventCreate(&e));
+    if (nn <= cap_) return "";
+    void* ptrs[] = {nodes, root_bounds, leaf_prim, codes, ids, codes_alt_, hist_, status_, counters_, gbounds_, flags_, ids_alt_, parent_};
+    for (void* p : ptrs)
+        if (p) dev_free(p);
+    const size_t N = (size_t)nn, tiles = (N + kSortTile - 1) / kSortTile;
+    bytes_ = 0;
+    auto al = [&](void** p, size_t b) -> cudaError_t {
+        bytes_ += b;
+        return dev_alloc(p, b);
+    };
+    LTS_TRY(al((void**)&nodes, sizeof(BvhNode) * (N > 1 ? N - 1 : 1)));
+    LTS_TRY(al((void**)&root_bounds, 6 * sizeof(float)));
+    LTS_TRY(al((void**)&leaf_prim, 4 * N));
+    LTS_TRY(al((void**)&codes, 4 * N));
+    LTS_TRY(al((void**)&ids, 4 * N));
+    LTS_TRY(al((void**)&codes_alt_, 4 * N));
+    LTS_TRY(al((void**)&ids_alt_, 4 * N));
+    LTS_TRY(al((void**)&hist_, 4 * 2 * 4 * 256));  // histograms then prefixes
+    LTS_TRY(al((void**)&status_, 4 * 4 * 256 * tiles));
+    LTS_TRY(al((void**)&counters_, 4 * 8));
+    LTS_TRY(al((void**)&gbounds_, 4 * 6));
+    LTS_TRY(al((void**)&flags_, 4 * (N > 1 ? N - 1 : 1)));
+    LTS_TRY(al((void**)&parent_, 4 * (2 * N - 1)));
+    cap_ = nn;
+    return "";
+}
+
+std::string Lbvh::build(const float* d_tri, int nn, int md, int code_limit, cudaStream_t s, uint32_t* d_error) {
+    if (nn < 1) return "LBVH needs at least one primitive";
+    if (nn > (1 << 24)) return "LBVH is limited to 2^24 primitives (the reference's float index arithmetic)";
+    std::string e = reserve(nn);
+    if (!e.empty()) return e;
+    n = nn;
+    mode = md;
+    launches = 0;
+    ++serial;
+    const size_t N = (size_t)nn, tiles = (N + kSortTile - 1) / kSortTile;
+    int dev = 0, sms = 0;
+    LTS_TRY(cudaGetDevice(&dev));
+    LTS_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int stream_grid = std::min(grid_for((long)N, kBlock), sms * 8);
+
+    LTS_TRY(cudaEventRecord(ev_[0], s));
+    LTS_TRY(cudaMemsetAsync(gbounds_, 0xff, 12, s));
+    LTS_TRY(cudaMemsetAsync(gbounds_ + 3, 0x00, 12, s));
+    k_scene_bounds<<<stream_grid, kBlock, 0, s>>>(d_tri, nn, gbounds_);
+    ++launches;
+    LTS_TRY(cudaEventRecord(ev_[1], s));
+    LTS_TRY(cudaMemsetAsync(hist_, 0, 4 * 4 * 256, s));
+    k_morton<<<stream_grid, kBlock, 0, s>>>(d_tri, nn, gbounds_, code_limit, codes, ids, hist_);
+    ++launches;
+    LTS_TRY(cudaEventRecord(ev_[2], s));
+    LTS_TRY(cudaMemsetAsync(status_, 0, 4 * 4 * 256 * tiles, s));
+    LTS_TRY(cudaMemsetAsync(counters_, 0, 4 * 8, s));
+    k_digit_prefix<<<4, 256, 0, s>>>(hist_, hist_ + 4 * 256);
+    ++launches;
+    uint32_t* kin = codes;
+    int32_t* vin = ids;
+    uint32_t* kout = codes_alt_;
+    int32_t* vout = ids_alt_;
+    for (int p = 0; p < 4; ++p) {
+        k_onesweep<<<(int)tiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, nn, 8 * p, hist_ + 4 * 256 + 256 * p,
+                                                        status_ + (size_t)p * 256 * tiles, counters_ + p, d_error);
+        ++launches;
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    LTS_TRY(cudaEventRecord(ev_[3], s));
+    if (nn > 1) {
+        LTS_TRY(cudaMemsetAsync(parent_, 0xff, 4 * (2 * N - 1), s));
+        k_topology<<<grid_for((long)N - 1, kBlock), kBlock, 0, s>>>(codes, nn, nodes, parent_);
+        ++launches;
+    }
+    LTS_TRY(cudaEventRecord(ev_[4], s));
+    if (nn > 1) LTS_TRY(cudaMemsetAsync(flags_, 0, 4 * (N - 1), s));
+    k_refit<<<grid_for((long)N, kBlock), kBlock, 0, s>>>(d_tri, nn, md, ids, parent_, nodes, flags_, leaf_prim, root_bounds);
+    ++launches;
+    LTS_TRY(cudaEventRecord(ev_[5], s));
+    LTS_TRY(cudaGetLastError());
+    return "";
+}
+
+void Lbvh::stage_ms(float out[5]) const {
+    for (int i = 0; i < 5; ++i) {
+        out[i] = 0.f;
+        if (ev_[i] && ev_[i + 1]) {
+            cudaEventSynchronize(ev_[i + 1]);
+            cudaEventElapsedTime(&out[i], ev_[i], ev_[i + 1]);
+        }
+    }
+}
+
+}  // namespace lts

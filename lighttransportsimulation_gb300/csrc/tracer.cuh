@@ -1,0 +1,98 @@
+// Path tracer (sm_103a): the reference's PathTracingIntegrator over SoA scene tables.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/lts_capi.h"
+#include "host_scene.hpp"
+#include "lbvh.cuh"
+
+namespace lts {
+
+struct DevTex {
+    int32_t kind;
+    float v[4];
+};
+struct DevMat {
+    int32_t kind;
+    float extra, on_a, on_b;
+    DevTex tex[2];
+};
+struct DevLight {
+    int32_t kind, prim;
+    float L[3], p[3], radius, area;
+};
+
+// Everything a render kernel reads, passed by value.
+struct SceneView {
+    int32_t ntri, nlight, width, height, has_normals_any;
+    const float4* __restrict__ leaf_v;   // [3 ntri] triangle of leaf l: p0 (w = prim id bits), p1, p2
+    const float4* __restrict__ prim_v;   // [3 ntri] scene order
+    const int4* __restrict__ prim_n;     // [ntri] normal indices (-1: none), w = mesh (= material) index
+    const int4* __restrict__ prim_uv;    // [ntri] uv indices (-1: none)
+    const float* __restrict__ normals;   // [3 nn]
+    const float* __restrict__ uvs;       // [2 nuv]
+    const int32_t* __restrict__ prim_light;
+    const DevMat* __restrict__ mats;
+    const DevLight* __restrict__ lights;
+    const float* __restrict__ light_func;
+    const float* __restrict__ light_cdf;
+    float light_func_int;
+    const BvhNode* __restrict__ nodes;
+    const float* __restrict__ root_bounds;
+    const float* __restrict__ filter;    // 16 x 16 Gaussian table
+    float cam[23];
+};
+
+struct RenderParams {
+    int32_t spp, max_bounce, rr_start;
+    uint32_t seed;
+    int32_t x0, y0, x1, y1;
+    float spp_scale;                 // quake_rsqrt(spp) for ray differentials
+    double* __restrict__ film;       // [W*H*4] compensated sums resolved in FP64
+    float* __restrict__ sample_L;    // [crop * spp * 3] (record mode)
+    uint64_t* __restrict__ sample_sig;
+    unsigned long long* __restrict__ counters;  // [0] rays issued
+    uint32_t* __restrict__ err;
+};
+
+class Tracer {
+   public:
+    Tracer() = default;
+    ~Tracer();
+    Tracer(const Tracer&) = delete;
+    Tracer& operator=(const Tracer&) = delete;
+
+    std::string upload_scene(const HostScene& sc, cudaStream_t s);
+    std::string render(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, lts_render_out* out,
+                       cudaStream_t s, uint32_t* d_err);
+    std::string render_async(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
+                             uint32_t* d_err);
+    std::string film_get(const HostScene& sc, float* rgb, double* sums, cudaStream_t s);
+
+    double last_ms = 0, last_paths = 0, last_rays = 0;
+    int last_launches = 0;
+
+   private:
+    std::string prepare(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
+                        uint32_t* d_err, RenderParams* rp, SceneView* sv, long* crop_samples);
+    void free_all();
+    SceneView view_{};
+    void* bufs_[16] = {nullptr};
+    float4* leaf_v_ = nullptr;
+    int leaf_n_ = 0;
+    uint64_t leaf_serial_ = 0;  // Lbvh::serial the leaf_v_ copy was gathered for
+    double* film_ = nullptr;
+    size_t film_cap_ = 0;
+    float* rec_L_ = nullptr;
+    uint64_t* rec_sig_ = nullptr;
+    size_t rec_cap_ = 0;
+    unsigned long long* counters_ = nullptr;
+    float* rgb_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+};
+
+}  // namespace lts

@@ -1,0 +1,2 @@
+/* Test infrastructure: empty stand-in for <cuda.h>; oracle/ref/shim/lts_ref_shim.h supplies the host definitions. */
+#pragma once
