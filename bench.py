@@ -1,0 +1,325 @@
+#!/usr/bin/env python
+"""Benchmark: plain path tracer on the displaced-icosphere workload, 1 GB300.
+
+Workload (one step = one full render): the open-front box of 5 Lambertian walls and a 0.5x0.5
+ceiling light (Le 10) holding a level-8 icosphere (1,310,720 triangles) radially displaced by
+0.1 * fbm(8 octaves, omega 0.5) with a wrinkled Lambertian texture (8 octaves, omega 0.5);
+1024 x 1024 pixels, 64 spp, 8 bounces, Russian roulette from bounce 3, sampler seed 0.
+67,108,864 paths per step.  Synthetic seeded data written in the reference's own .scene /
+.subject / .bin formats (lighttransportsimulation_gb300.scenes).
+
+Reported (one JSON line on rank 0):
+  value      Mpaths/s with the scene and BVH resident in HBM (device time, CUDA events on the
+             renderer's stream, max over ranks);
+  e2e        Mpaths/s through the public API per step: scene upload from host (H2D), LBVH
+             build, render, film read back (D2H);
+  roofline   the render kernel's BVH-node + triangle + film bytes (counted by the kernel) per
+             launch / launch time, against the measured HBM copy bandwidth;
+  lbvh       device time of the bit-exact LBVH build on 1M and 16M random triangles (seed 1)
+             against the 304 B/primitive algorithmic model;
+  cpu_baseline  the oracle's CPU port of the reference integrator (OpenMP, all host cores) on
+             a bounded pixel sample of the same workload.
+--impl reference times that CPU port alone, on the same workload and metric.
+Inputs (BVH + triangles, ~150 MB) exceed the 129 MB L2, so no flush runs between steps.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="displaced_icosphere_box", width=1024, height=1024, spp=64, max_bounce=8, rr_start=3,
+                seed=0, level=8)
+SMALL = dict(name="displaced_icosphere_box_small", width=256, height=256, spp=16, max_bounce=8, rr_start=3,
+             seed=0, level=6)
+
+
+def scene_dir(wl):
+    from lighttransportsimulation_gb300 import scenes
+    d = os.path.join(tempfile.gettempdir(), f"lts_bench_{wl['name']}_{wl['level']}")
+    marker = os.path.join(d, "done")
+    if not os.path.exists(marker):
+        os.makedirs(d, exist_ok=True)
+        scenes.write_displaced(d, level=wl["level"])
+        open(marker, "w").write("ok")
+    return d, "box", "displaced"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 2 + k and r[2 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_port_sample(wl, seconds_target=15.0, threads=None):
+    """Times the oracle's CPU port of the reference integrator on a pixel band of the workload.
+    Returns dict(value=Mpaths/s, cores, sample) or None when the port is not built."""
+    exe = os.path.join(ROOT, "oracle", "_build", "lts_port")
+    if not os.path.exists(exe):
+        return None
+    d, sc, sub = scene_dir(wl)
+    threads = threads or os.cpu_count()
+    # grow the band until the run takes a meaningful time (bounded)
+    rows = 8
+    while True:
+        y0 = wl["height"] // 2 - rows // 2
+        out = os.path.join(tempfile.gettempdir(), "lts_port_bench.ltsd")
+        cmd = [exe, "render", d + "/", sc, sub, out, wl["width"], wl["height"], wl["spp"], wl["max_bounce"],
+               wl["rr_start"], wl["seed"], 0, y0, wl["width"], y0 + rows, threads, 0, 1]
+        t0 = time.time()
+        subprocess.run([str(c) for c in cmd], check=True, capture_output=True)
+        el = time.time() - t0
+        from oracle import ltsd
+        r = ltsd.read(out)
+        secs = float(r["time_s"][0])
+        if secs >= seconds_target / 4 or rows >= wl["height"] or el > seconds_target:
+            paths = wl["width"] * rows * wl["spp"]
+            return {"value": paths / secs / 1e6, "unit": "Mpaths/s", "cores": int(r["threads"][0]), "kind": "port",
+                    "sample": f"rows {y0}..{y0 + rows} of {wl['width']}x{wl['height']} at {wl['spp']} spp "
+                              f"({paths} paths, {secs:.2f} s)"}
+        rows = min(wl["height"], rows * max(2, int(seconds_target / 4 / max(secs, 1e-3)) + 1))
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world, local, dist
+
+
+def barrier_max(dist, value):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, wl):
+    rank, world, local, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    vals = []
+    for _ in range(args.warmup):
+        cpu_port_sample(wl, seconds_target=4.0)
+    t0 = time.time()
+    res = None
+    for _ in range(args.steps):
+        res = cpu_port_sample(wl, seconds_target=8.0)
+        if res is None:
+            print(json.dumps({"impl": "reference", "unavailable": "oracle CPU port not built (oracle/_build/lts_port)"}))
+            return
+        vals.append(res["value"])
+    el = time.time() - t0
+    v = statistics.median(vals)
+    line = {"metric": "Mpaths/s", "value": v, "unit": "Mpaths/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * el / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": wl["name"], "width": wl["width"], "height": wl["height"], "spp": wl["spp"],
+                       "max_bounce": wl["max_bounce"], "rr_start": wl["rr_start"], "seed": wl["seed"],
+                       "triangles": 20 * 4 ** wl["level"] + 12},
+            "cpu_baseline": {**res, "value": v},
+            "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def lbvh_bench(ctx, n, steps, warmup, mode, peaks):
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from lighttransportsimulation_gb300 import scenes
+    tris = torch.from_numpy(scenes.random_triangles(n, seed=1).reshape(-1)).cuda()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    torch.cuda.synchronize()
+    for _ in range(warmup):
+        ctx.check(ctx.lib.lts_bvh_build_device_async(ctx.h, ctypes.c_void_p(tris.data_ptr()), n, mode, -1))
+    ctx.check(ctx.lib.lts_bvh_dump_get(ctx.h, None))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.check(ctx.lib.lts_bvh_build_device_async(ctx.h, ctypes.c_void_p(tris.data_ptr()), n, mode, -1))
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    m = ctx.metrics()
+    ctx.check(ctx.lib.lts_bvh_dump_get(ctx.h, None))
+    m = ctx.metrics()
+    stages = [round(x, 4) for x in m.bvh_stage_ms]
+    alg = 304.0 * n
+    gbs = alg / (ms * 1e-3) / 1e9
+    del tris
+    torch.cuda.empty_cache()
+    return {"n": n, "ms": round(ms, 4), "stage_ms_last": stages, "algorithmic_bytes": alg, "achieved_gbs": round(gbs, 1),
+            "frac_of_hbm": round(gbs / peaks["hbm_gbs"], 4)}
+
+
+def run_gpu(args, wl):
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import lighttransportsimulation_gb300 as lts
+    rank, world, local, dist = dist_setup(args.gpus)
+    peaks, peak_kind = measured_peaks()
+    d, sc, sub = scene_dir(wl)
+    ctx = lts.Context(local)
+    scene = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
+    integ = lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], scene)
+    desc = integ.desc(wl["spp"], wl["seed"])
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    paths = wl["width"] * wl["height"] * wl["spp"]
+
+    # warm-up (also builds the LBVH and the leaf-ordered triangles)
+    for _ in range(args.warmup):
+        ctx.check(ctx.lib.lts_render_async(ctx.h, ctypes.byref(desc)))
+    torch.cuda.synchronize()
+    ctx.check(ctx.lib.lts_film_get(ctx.h, None, None))
+
+    # device-resident timed region
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kernel_ms = []
+    with ClockSampler(local) as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            ctx.check(ctx.lib.lts_render_async(ctx.h, ctypes.byref(desc)))
+        e1.record(stream)
+        e1.synchronize()
+    ctx.check(ctx.lib.lts_film_get(ctx.h, None, None))
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = barrier_max(dist, ms)
+    value = world * paths / (ms * 1e-3) / 1e6
+
+    # one counted render for the roofline's algorithmic bytes (same kernel, same launch)
+    r = integ.render(wl["spp"], wl["seed"], film=False)
+    alg_bytes = 64.0 * r["node_visits"] + 48.0 * r["tri_tests"] + 32.0 * paths
+    achieved = alg_bytes / (r["render_ms"] * 1e-3) / 1e9
+
+    # end to end through the public API: upload scene (H2D), build, render, read film (D2H)
+    h2d = scene.info["triangles"] * 48 + scene.info["triangles"] * 16 * 2
+    d2h = wl["width"] * wl["height"] * 12
+    t_e2e = []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
+        lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], s2).render(wl["spp"], wl["seed"])
+        t_e2e.append(time.perf_counter() - t0)
+    e2e_s = barrier_max(dist, statistics.median(t_e2e))
+    e2e = world * paths / e2e_s / 1e6
+
+    lbvh = None
+    if rank == 0 and not args.skip_lbvh:
+        lbvh = [lbvh_bench(ctx, n, 5, 3, lts.BVH_SORTED, peaks) for n in (1_000_000, 16_000_000)]
+    cpu = cpu_port_sample(wl) if (rank == 0 and world == 1 and not args.skip_cpu) else None
+    m = ctx.metrics()
+    if rank == 0:
+        line = {
+            "metric": "Mpaths/s", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl["name"], "width": wl["width"], "height": wl["height"], "spp": wl["spp"],
+                       "max_bounce": wl["max_bounce"], "rr_start": wl["rr_start"], "seed": wl["seed"],
+                       "triangles": scene.info["triangles"], "integrator": "megakernel", "bvh": "sorted-leaf LBVH",
+                       "l2": "inputs (BVH + triangles) exceed L2; no flush", "parallelism": f"replicas x{world}"},
+            "mrays_per_s": round(r["rays"] / (r["render_ms"] * 1e-3) / 1e6, 2),
+            "e2e": {"value": round(e2e, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "seconds_per_step": round(e2e_s, 4)},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                         "kernel": "k_pathtrace", "peak_kind": peak_kind,
+                         "algorithmic": "64 B per BVH node visit + 48 B per triangle test + 32 B film per path"},
+            "traversal": {"node_visits": r["node_visits"], "tri_tests": r["tri_tests"], "rays": r["rays"]},
+            "lbvh": lbvh,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": int(args.steps),
+            "kernel_launches_per_step": m.kernel_launches,
+        }
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--small", action="store_true", help="256x256x16 spp level-6 sphere (quick check)")
+    ap.add_argument("--skip-lbvh", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    wl = SMALL if args.small else WORKLOAD
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_gpu(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -139,6 +139,8 @@ typedef struct {
     uint64_t* sample_sig; /* [crop pixels * spp] FNV-1a hash of each sample's events, or NULL */
     double render_ms;     /* device time of the render kernels (CUDA events) */
     double rays;          /* ray queries issued (extension + shadow + MIS) */
+    double node_visits;   /* BVH interior nodes fetched (64 bytes each) */
+    double tri_tests;     /* ray-triangle tests (48 bytes of triangle data each) */
 } lts_render_out;
 
 /* Renders the loaded scene.  Replaces PathTracingKernel / PathTracingIntegrator::evaluate

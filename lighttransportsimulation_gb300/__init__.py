@@ -69,7 +69,8 @@ class RenderDesc(ctypes.Structure):
 
 class RenderOut(ctypes.Structure):
     _fields_ = [("film_rgb", ctypes.c_void_p), ("film_sums", ctypes.c_void_p), ("sample_L", ctypes.c_void_p),
-                ("sample_sig", ctypes.c_void_p), ("render_ms", ctypes.c_double), ("rays", ctypes.c_double)]
+                ("sample_sig", ctypes.c_void_p), ("render_ms", ctypes.c_double), ("rays", ctypes.c_double),
+                ("node_visits", ctypes.c_double), ("tri_tests", ctypes.c_double)]
 
 
 class Metrics(ctypes.Structure):
@@ -260,7 +261,7 @@ class PathTracingIntegrator:
         L = np.empty(cw * ch * spp * 3, np.float32) if record else None
         sig = np.empty(cw * ch * spp, np.uint64) if record else None
         o = RenderOut(rgb.ctypes.data if film else None, fs.ctypes.data if sums else None,
-                      L.ctypes.data if record else None, sig.ctypes.data if record else None, 0.0, 0.0)
+                      L.ctypes.data if record else None, sig.ctypes.data if record else None, 0.0, 0.0, 0.0, 0.0)
         ctx = self.scene.ctx
         ctx.check(ctx.lib.lts_render(ctx.h, ctypes.byref(d), ctypes.byref(o)))
         if film:
@@ -272,6 +273,8 @@ class PathTracingIntegrator:
             res["sig"] = sig.reshape(ch, cw, spp)
         res["render_ms"] = o.render_ms
         res["rays"] = o.rays
+        res["node_visits"] = o.node_visits
+        res["tri_tests"] = o.tri_tests
         return res
 
 

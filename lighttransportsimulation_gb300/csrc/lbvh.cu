@@ -8,6 +8,7 @@
 //   4 k_topology       Karras split per interior node             BVH.cuh:173-236
 //   5 k_refit          bottom-up AABBs, second arrival unions     BVH.cuh:238-262
 // Output layout: one 64-byte node per interior node carrying both child boxes (see lbvh.cuh).
+#include <cuda/atomic>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -353,9 +354,9 @@ __global__ __launch_bounds__(kBlock) void k_refit(const float* __restrict__ tri,
         } else {              // right slot: b.z, b.w, c.x = min, c.yzw = max
             P[6] = mn[0]; P[7] = mn[1]; P[8] = mn[2]; P[9] = mx[0]; P[10] = mx[1]; P[11] = mx[2];
         }
-        __threadfence();
-        if (atomicAdd(flags + p, 1u) == 0u) return;  // first arrival stops (BVH.cuh:251-255)
-        __threadfence();
+        // acq_rel: the first arrival releases its child box, the second acquires it
+        cuda::atomic_ref<uint32_t, cuda::thread_scope_device> flag(flags[p]);
+        if (flag.fetch_add(1u, cuda::memory_order_acq_rel) == 0u) return;  // first arrival stops (BVH.cuh:251-255)
         const float4 a = __ldcg(&nodes[p].a), b = __ldcg(&nodes[p].b), c = __ldcg(&nodes[p].c);
         mn[0] = fminf(a.x, b.z); mn[1] = fminf(a.y, b.w); mn[2] = fminf(a.z, c.x);  // bUnion(left, right)
         mx[0] = fmaxf(a.w, c.y); mx[1] = fmaxf(b.x, c.z); mx[2] = fmaxf(b.y, c.w);

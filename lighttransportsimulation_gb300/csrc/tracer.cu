@@ -291,15 +291,20 @@ __device__ __forceinline__ bool leaf_test(const SceneView& sv, int leaf, const T
 
 // BVH::intersect / simpleIntersect (acceleration/BVH.cuh:331-398).  Returns the hit primitive
 // (closest) or 1/-1 (any), -1 for a miss.  `stack` is this thread's column of the shared stack.
+struct Work {
+    uint32_t nodes, tris;
+};
+
 template <bool ANY>
 __device__ int traverse(const SceneView& sv, int nleaf, const TraceRay& r, float& tmax, float& bu, float& bv,
-                        float& binv, uint32_t* stack, uint32_t* err) {
+                        float& binv, uint32_t* stack, uint32_t* err, Work& wk) {
     int best = -1;
     float te;
     const float* rb = sv.root_bounds;
     if (!slab(r, tmax, __ldg(rb), __ldg(rb + 1), __ldg(rb + 2), __ldg(rb + 3), __ldg(rb + 4), __ldg(rb + 5), te))
         return -1;
     if (nleaf == 1) {
+        ++wk.tris;
         if (leaf_test<ANY>(sv, 0, r, tmax, best, bu, bv, binv)) return 1;
         return ANY ? -1 : best;
     }
@@ -308,14 +313,17 @@ __device__ int traverse(const SceneView& sv, int nleaf, const TraceRay& r, float
         const BvhNode* nd = sv.nodes + node;
         const float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
         const int4 lr = __ldg(&nd->d);
+        ++wk.nodes;
         float tl, tr;
         bool hl = slab(r, tmax, a.x, a.y, a.z, a.w, b.x, b.y, tl);
         bool hr = slab(r, tmax, b.z, b.w, c.x, c.y, c.z, c.w, tr);
         if (hl && lr.x < 0) {
+            ++wk.tris;
             if (leaf_test<ANY>(sv, ~lr.x, r, tmax, best, bu, bv, binv)) return 1;
             hl = false;
         }
         if (hr && lr.y < 0) {
+            ++wk.tris;
             if (leaf_test<ANY>(sv, ~lr.y, r, tmax, best, bu, bv, binv)) return 1;
             hr = false;
         }
@@ -345,10 +353,10 @@ struct Hit {
 };
 
 __device__ __forceinline__ bool scene_intersect(const SceneView& sv, int nleaf, V3 o, V3 d, float tmax, SI& si,
-                                                uint32_t* stack, uint32_t* err) {
+                                                uint32_t* stack, uint32_t* err, Work& wk) {
     const TraceRay r = make_trace_ray(o, d);
     float bu = 0, bv = 0, binv = 0;
-    const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, stack, err);
+    const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk);
     if (prim < 0) return false;
     V3 p0, p1, p2;
     prim_tri(sv, prim, p0, p1, p2);
@@ -356,10 +364,10 @@ __device__ __forceinline__ bool scene_intersect(const SceneView& sv, int nleaf, 
     return true;
 }
 __device__ __forceinline__ bool scene_occluded(const SceneView& sv, int nleaf, V3 o, V3 d, float tmax, uint32_t* stack,
-                                               uint32_t* err) {
+                                               uint32_t* err, Work& wk) {
     const TraceRay r = make_trace_ray(o, d);
     float bu, bv, binv;
-    return traverse<true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err) > 0;
+    return traverse<true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk) > 0;
 }
 
 // ------------------------------------------------------------------ rays from interactions
@@ -925,6 +933,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
     const int W = sv.width, H = sv.height;
     const int id = j * W + i;
     unsigned long long rays = 0;
+    Work wk{0u, 0u};
 #pragma unroll
     for (int k = 0; k < 32; ++k) acc[k * kThreads] = 0.0f;
 
@@ -958,7 +967,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
         for (int bounce = 0; bounce < rp.max_bounce; ++bounce) {
             SI si;
             ++rays;
-            const bool hit = scene_intersect(sv, nleaf, ro, rd, INFINITY, si, stack, rp.err);
+            const bool hit = scene_intersect(sv, nleaf, ro, rd, INFINITY, si, stack, rp.err, wk);
             if (RECORD) fnv_mix(sig, 0x100000000ull + (uint64_t)((hit ? si.prim : -1) + 1));
             if (bounce == 0 || specular) {
                 if (hit) {
@@ -1028,7 +1037,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                         const V3 org = offset_origin(si.p, si.perr, si.n, ls.p1 - si.p);
                         const V3 tgt = offset_origin(ls.p1, ls.perr1, ls.n1, org - ls.p1);
                         ++rays;
-                        const bool occ = scene_occluded(sv, nleaf, org, tgt - org, 1 - kShadowEps, stack, rp.err);
+                        const bool occ = scene_occluded(sv, nleaf, org, tgt - org, 1 - kShadowEps, stack, rp.err, wk);
                         if (RECORD) fnv_mix(sig, 0x300000000ull + (occ ? 0u : 1u));
                         Spec Li = ls.Li;
                         if (occ) Li = spec(0.0f);
@@ -1068,7 +1077,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                             SI lit;
                             const V3 org = offset_origin(si.p, si.perr, si.n, wi);
                             ++rays;
-                            const bool found = scene_intersect(sv, nleaf, org, wi, INFINITY, lit, stack, rp.err);
+                            const bool found = scene_intersect(sv, nleaf, org, wi, INFINITY, lit, stack, rp.err, wk);
                             if (RECORD) fnv_mix(sig, 0x200000000ull + (uint64_t)((found ? lit.prim : -1) + 1));
                             Spec Li = spec(0.0f);
                             if (found) {
@@ -1154,8 +1163,13 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
     // ray counter: one atomic per warp (lanes outside the crop have already returned)
     const unsigned mask = __activemask();
     const unsigned tot = __reduce_add_sync(mask, (unsigned)rays);
+    const unsigned tn = __reduce_add_sync(mask, wk.nodes), tt = __reduce_add_sync(mask, wk.tris);
     const unsigned lane = (unsigned)tid & 31u;
-    if ((mask & ((1u << lane) - 1u)) == 0u && rp.counters) atomicAdd(rp.counters, (unsigned long long)tot);
+    if ((mask & ((1u << lane) - 1u)) == 0u && rp.counters) {
+        atomicAdd(rp.counters, (unsigned long long)tot);
+        atomicAdd(rp.counters + 1, (unsigned long long)tn);
+        atomicAdd(rp.counters + 2, (unsigned long long)tt);
+    }
 }
 
 // Camera::getRender (Camera.cu:256-289): divide by the filter weight (in FP64 here), clamp at 0,
@@ -1430,12 +1444,17 @@ std::string Tracer::render(const HostScene& sc, const Lbvh& bvh, const lts_rende
     float ms = 0;
     TRY(cudaEventElapsedTime(&ms, ev0_, ev1_));
     last_ms = ms;
-    unsigned long long rays = 0;
-    TRY(cudaMemcpy(&rays, counters_, 8, cudaMemcpyDeviceToHost));
-    last_rays = (double)rays;
+    unsigned long long cnt[3] = {0, 0, 0};
+    TRY(cudaMemcpy(cnt, counters_, 24, cudaMemcpyDeviceToHost));
+    last_rays = (double)cnt[0];
+    last_node_visits = (double)cnt[1];
+    last_tri_tests = (double)cnt[2];
+    const double rays = (double)cnt[0];
     if (out) {
         out->render_ms = ms;
-        out->rays = (double)rays;
+        out->rays = rays;
+        out->node_visits = last_node_visits;
+        out->tri_tests = last_tri_tests;
         if (out->film_rgb || out->film_sums) {
             e = film_get(sc, out->film_rgb, out->film_sums, s);
             if (!e.empty()) return e;

@@ -73,7 +73,7 @@ class Tracer {
                              uint32_t* d_err);
     std::string film_get(const HostScene& sc, float* rgb, double* sums, cudaStream_t s);
 
-    double last_ms = 0, last_paths = 0, last_rays = 0;
+    double last_ms = 0, last_paths = 0, last_rays = 0, last_node_visits = 0, last_tri_tests = 0;
     int last_launches = 0;
 
    private:

@@ -273,3 +273,34 @@ def write_app_params(path, width, height, spp, bounces, rr, fmt, output, scene, 
     """app.params: 9 whitespace-separated tokens (FileIO.cuh:234-257)."""
     with open(path, "w") as fh:
         fh.write(f"{width} {height}\n{spp}\n{bounces}\n{rr}\n{fmt}\n{output}\n{scene}\n{subject}\n")
+
+
+def write_materials_scene(d, level=3):
+    """Parity workload exercising the non-Lambertian paths the reference can load: a glass
+    icosphere (eta 1.5) on the left, a mirror icosphere on the right, Oren-Nayar walls
+    (sigma 20 deg), a marble-textured floor, fBm and wrinkled side walls, the ceiling area light
+    and a constant infinite light (0.5) seen through the open front."""
+    os.makedirs(d, exist_ok=True)
+    write_quads(os.path.join(d, "m_back.bin"), [((-1, -1, -1), (2, 0, 0), (0, 2, 0)),
+                                                  ((-1, 1, -1), (2, 0, 0), (0, 0, 2))])
+    write_quads(os.path.join(d, "m_floor.bin"), [((-1, -1, -1), (0, 0, 2), (2, 0, 0))])
+    write_quads(os.path.join(d, "m_left.bin"), [((-1, -1, -1), (0, 2, 0), (0, 0, 2))])
+    write_quads(os.path.join(d, "m_right.bin"), [((1, -1, -1), (0, 0, 2), (0, 2, 0))])
+    write_quads(os.path.join(d, "box_light.bin"), [((-0.25, 0.999, -0.25), (0.5, 0, 0), (0, 0, 0.5))])
+    v, f = icosphere(level)
+    write_bin(os.path.join(d, "glass.bin"), v * 0.35 + np.array([-0.4, -0.6, 0.1]), v, f, f)
+    write_bin(os.path.join(d, "mirror.bin"), v * 0.3 + np.array([0.45, -0.65, -0.3]), v, f, f)
+    with open(os.path.join(d, "materials.scene"), "w") as fh:
+        fh.write(CAMERA_BOX + IDENTITY_SUBJECT + "0\n"
+                 "5\tm_back\tm_floor\tm_left\tm_right\tbox_light\n"
+                 "5\n"
+                 "L\tc\t0.7 0.7 0.7\t20\n"
+                 "L\tm\t8 0.5 4 1\t0\n"
+                 "L\tf\t8 0.5\t0\n"
+                 "L\tw\t8 0.5\t10\n"
+                 "L\tc\t0 0 0\t0\n"
+                 "1\t10 10 10\n"
+                 "1\t0.5 0.5 0.5\n")
+    with open(os.path.join(d, "spheres.subject"), "w") as fh:
+        fh.write("0\n2\tglass\tmirror\n2\nG\tc\t1 1 1\tc\t1 1 1\t1.5\nR\tc\t0.9 0.9 0.9\t0\n")
+    return "materials", "spheres"

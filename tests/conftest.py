@@ -1,0 +1,57 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def built_lib():
+    """The compiled renderer library (built in-tree on first use)."""
+    from lighttransportsimulation_gb300 import build
+    return build.build()
+
+
+def write_scene(kind, d):
+    from lighttransportsimulation_gb300 import scenes
+    return {"box_sphere": scenes.write_box_sphere, "materials": scenes.write_materials_scene}[kind](d)
+
+
+def scene_digest(d):
+    import hashlib
+    out = []
+    for f in sorted(os.listdir(d)):
+        with open(os.path.join(d, f), "rb") as fh:
+            out.append(f"{f}:{hashlib.sha256(fh.read()).hexdigest()}")
+    return out
+
+
+@pytest.fixture(scope="session")
+def scene_dirs(tmp_path_factory):
+    """Generated parity scenes, checked against the digests recorded in the fixtures."""
+    out = {}
+    for kind in ("box_sphere", "materials"):
+        d = str(tmp_path_factory.mktemp(kind))
+        sc, sub = write_scene(kind, d)
+        fx = np.load(os.path.join(GOLDEN, f"lbvh_{kind}.npz"))
+        assert list(fx["scene_digest"]) == scene_digest(d), f"scene generator drifted for {kind}"
+        out[kind] = (d, sc, sub)
+    return out
+
+
+def has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False

@@ -1,0 +1,91 @@
+"""CPU tests of the C-ABI library: it loads, exports every symbol the header declares, and its
+host-side loader reproduces the reference's parseScene outputs bit for bit."""
+import os
+import re
+import struct
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+
+def test_library_exports_header_symbols(built_lib):
+    import ctypes
+    import lighttransportsimulation_gb300 as lts
+    hdr = open(os.path.join(ROOT, "include", "lts_capi.h")).read()
+    declared = sorted(set(re.findall(r"\b(lts_[a-z0-9_]+)\s*\(", hdr)))
+    lib = ctypes.CDLL(built_lib)
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert sorted(lts.EXPORTS) == declared
+
+
+@pytest.mark.parametrize("kind", ["box_sphere", "materials"])
+def test_loader_matches_reference(built_lib, scene_dirs, kind):
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs[kind]
+    fx = np.load(os.path.join(GOLDEN, f"lbvh_{kind}.npz"))
+    meta = np.load(os.path.join(GOLDEN, f"render_{kind}.npz"))["meta"]
+    ctx = lts.Context(-1)
+    s = lts.Scene.parse(ctx, d, sc, sub, int(meta[0]), int(meta[1]))
+    tri = s.triangles().reshape(-1)
+    assert np.array_equal(tri.view(np.uint32), fx["tri_p"].view(np.uint32))
+    assert np.array_equal(s.camera().view(np.uint32), fx["camera"].view(np.uint32))
+    func, cdf = s.light_distribution()
+    assert np.array_equal(func.view(np.uint32), fx["light_func"].view(np.uint32))
+    assert np.array_equal(cdf.view(np.uint32), fx["light_cdf"].view(np.uint32))
+    assert s.light_count == len(fx["light_flags"])
+
+
+def test_app_params(tmp_path, built_lib):
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    p = tmp_path / "app.params"
+    scenes.write_app_params(p, 320, 200, 16, 5, 3, 1, "out", "res/a", "res/b")
+    d = lts.read_application_parameters(str(p))
+    assert (d["width"], d["height"], d["spp"], d["max_bounce"], d["rr_start"], d["format"]) == (320, 200, 16, 5, 3, 1)
+    assert d["output"] == "out.pfm" and d["scene"] == "res/a" and d["subject"] == "res/b"
+    with pytest.raises(lts.LtsError):
+        lts.read_application_parameters(str(tmp_path / "missing.params"))
+
+
+def _load_err(d, sc, sub):
+    import lighttransportsimulation_gb300 as lts
+    ctx = lts.Context(-1)
+    with pytest.raises(lts.LtsError) as e:
+        lts.Scene.parse(ctx, d, sc, sub, 64, 64)
+    return e.value.code
+
+
+def test_loader_errors(tmp_path, built_lib):
+    from lighttransportsimulation_gb300 import scenes
+    d = str(tmp_path)
+    sc, sub = scenes.write_box_sphere(d)
+    assert _load_err(d, "nope", sub) == 2                        # missing .scene -> IO
+    b = os.path.join(d, "sphere.bin")
+    raw = open(b, "rb").read()
+    open(b, "wb").write(raw[:100])
+    assert _load_err(d, sc, sub) == 3                            # truncated .bin -> PARSE
+    bad = bytearray(raw)
+    ntri, npnt, nuv, nn = struct.unpack("<4i", raw[:16])
+    off = 16 + 12 * npnt + 8 * nuv + 12 * nn
+    bad[off:off + 4] = struct.pack("<i", npnt + 5)
+    open(b, "wb").write(bytes(bad))
+    assert _load_err(d, sc, sub) == 3                            # vertex index out of range
+    open(b, "wb").write(raw)
+    txt = open(os.path.join(d, "sphere.subject")).read()
+    open(os.path.join(d, "sphere.subject"), "w").write(txt.replace("L\tc\t0.8 0.8 0.8", "L\ti\t0"))
+    assert _load_err(d, sc, sub) == 6                            # image texture -> UNSUPPORTED
+    open(os.path.join(d, "sphere.subject"), "w").write("0\n1\tsphere\n")
+    assert _load_err(d, sc, sub) == 3                            # premature end of file
+
+
+def test_host_only_context_has_no_device_path(built_lib, scene_dirs):
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs["box_sphere"]
+    ctx = lts.Context(-1)
+    s = lts.Scene.parse(ctx, d, sc, sub, 32, 32)
+    with pytest.raises(lts.LtsError) as e:
+        s.create_bvh_tree(lts.BVH_REFERENCE)
+    assert e.value.code == 7

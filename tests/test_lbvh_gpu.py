@@ -1,0 +1,121 @@
+"""GPU parity of the LBVH build (through the C-ABI) against the reference's own builds and the
+numpy statement of its arithmetic."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(built_lib):
+    import lighttransportsimulation_gb300 as lts
+    c = lts.Context(0)
+    yield c
+    c.close()
+
+
+def _u32(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+@pytest.mark.parametrize("kind", ["box_sphere", "materials"])
+def test_reference_mode_bit_exact(ctx, scene_dirs, kind):
+    """Codes, stable order, children and every node's AABB bit pattern equal the reference's."""
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs[kind]
+    fx = np.load(os.path.join(GOLDEN, f"lbvh_{kind}.npz"))
+    meta = np.load(os.path.join(GOLDEN, f"render_{kind}.npz"))["meta"]
+    s = lts.Scene.parse(ctx, d, sc, sub, int(meta[0]), int(meta[1]))
+    out = s.create_bvh_tree(lts.BVH_REFERENCE)
+    assert np.array_equal(out["sorted_codes"], fx["sorted_codes"])
+    assert np.array_equal(out["sorted_ids"], fx["sorted_ids"])
+    assert np.array_equal(out["node_left"], fx["node_left"])
+    assert np.array_equal(out["node_right"], fx["node_right"])
+    assert np.array_equal(out["node_key"], fx["node_key"])
+    assert np.array_equal(_u32(out["node_bounds"]), _u32(fx["node_bounds"]))
+
+
+@pytest.mark.parametrize("kind", ["box_sphere", "materials"])
+def test_sorted_mode_is_the_textbook_lbvh(ctx, scene_dirs, kind):
+    """Every primitive coded; leaf l holds ids[l]; same topology rules; boxes consistent."""
+    import lighttransportsimulation_gb300 as lts
+    from oracle import lbvh_np
+    d, sc, sub = scene_dirs[kind]
+    s = lts.Scene.parse(ctx, d, sc, sub, 64, 64)
+    out = s.create_bvh_tree(lts.BVH_SORTED)
+    tris = s.triangles()
+    codes, ids = lbvh_np.stable_sort(*lbvh_np.morton_codes(tris))
+    assert np.array_equal(out["sorted_codes"], codes) and np.array_equal(out["sorted_ids"], ids)
+    left, right = lbvh_np.karras_topology(codes)
+    n = len(tris)
+    assert np.array_equal(out["node_left"][: n - 1], left) and np.array_equal(out["node_right"][: n - 1], right)
+    mn, mx = lbvh_np.tri_bounds(tris)
+    lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"], np.concatenate([mn, mx], 1)[ids])
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 3841, 100_003])
+def test_edge_sizes(ctx, n):
+    """Single primitive, tiny trees and sizes straddling the sort tile (3840 keys)."""
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    from oracle import lbvh_np
+    tris = scenes.random_triangles(n, seed=n)
+    out = lts.build_bvh_triangles(ctx, tris, lts.BVH_SORTED)
+    codes, ids = lbvh_np.stable_sort(*lbvh_np.morton_codes(tris))
+    assert np.array_equal(out["sorted_codes"], codes) and np.array_equal(out["sorted_ids"], ids)
+    mn, mx = lbvh_np.tri_bounds(tris)
+    if n == 1:
+        assert np.array_equal(_u32(out["node_bounds"]), _u32(np.concatenate([mn, mx], 1).reshape(-1)))
+        return
+    left, right = lbvh_np.karras_topology(codes)
+    assert np.array_equal(out["node_left"][: n - 1], left) and np.array_equal(out["node_right"][: n - 1], right)
+    lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"], np.concatenate([mn, mx], 1)[ids])
+
+
+def test_duplicate_codes_keep_stable_order(ctx):
+    """Many equal centroids: equal codes keep input order; delta's index tie-break shapes the tree."""
+    import lighttransportsimulation_gb300 as lts
+    from oracle import lbvh_np
+    rng = np.random.default_rng(3)
+    base = rng.random((50, 1, 3), dtype=np.float32)
+    tris = np.repeat(base, 200, axis=0) + np.zeros((1, 3, 3), np.float32)
+    tris = tris[rng.permutation(len(tris))]
+    out = lts.build_bvh_triangles(ctx, tris, lts.BVH_SORTED)
+    codes, ids = lbvh_np.stable_sort(*lbvh_np.morton_codes(tris))
+    assert np.array_equal(out["sorted_codes"], codes) and np.array_equal(out["sorted_ids"], ids)
+    left, right = lbvh_np.karras_topology(codes)
+    n = len(tris)
+    assert np.array_equal(out["node_left"][: n - 1], left) and np.array_equal(out["node_right"][: n - 1], right)
+
+
+def test_one_million_random_triangles(ctx):
+    """The build benchmark's 1M case (seed 1): codes, order and topology bit-exact; boxes consistent."""
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    from oracle import lbvh_np
+    tris = scenes.random_triangles(1_000_000, seed=1)
+    out = lts.build_bvh_triangles(ctx, tris, lts.BVH_SORTED)
+    codes, ids = lbvh_np.stable_sort(*lbvh_np.morton_codes(tris))
+    assert np.array_equal(out["sorted_codes"], codes) and np.array_equal(out["sorted_ids"], ids)
+    left, right = lbvh_np.karras_topology(codes)
+    assert np.array_equal(out["node_left"][:-1][: len(left)], left)
+    assert np.array_equal(out["node_right"][: len(right)], right)
+    mn, mx = lbvh_np.tri_bounds(tris)
+    lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"], np.concatenate([mn, mx], 1)[ids])
+
+
+def test_reference_mode_code_limit(ctx):
+    """Primitives past the reference's Morton launch extent keep code 0 and id 0."""
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    from oracle import lbvh_np
+    tris = scenes.random_triangles(5000, seed=9)
+    out = lts.build_bvh_triangles(ctx, tris, lts.BVH_REFERENCE, code_limit=4096)
+    codes, ids = lbvh_np.stable_sort(*lbvh_np.morton_codes(tris, code_limit=4096))
+    assert np.array_equal(out["sorted_codes"], codes) and np.array_equal(out["sorted_ids"], ids)
+    mn, mx = lbvh_np.tri_bounds(tris)
+    lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"], np.concatenate([mn, mx], 1))

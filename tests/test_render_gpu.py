@@ -1,0 +1,72 @@
+"""GPU parity of the path tracer (through the C-ABI) against the reference integrator's own
+per-(pixel, sample) radiance, with the shared project sampler.
+
+Tolerance (FP32): a sample whose event hash (hit primitive per bounce, shadow visibility,
+MIS-ray hit) equals the reference's is "non-divergent" and its radiance must match to 1e-4
+relative (plus 1e-6 absolute for near-zero values).  Hash mismatches are paths that diverged at
+a grazing hit or an epsilon-boundary decision (the GPU rounds with FMA, the reference's host
+build does not); they are counted and bounded, not compared.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL = 1e-4, 1e-6
+MAX_DIVERGENT = 0.01   # fraction of samples whose event hash differs
+MAX_MISMATCH = 0.001   # fraction of non-divergent samples outside the tolerance
+
+
+@pytest.fixture(scope="module")
+def ctx(built_lib):
+    import lighttransportsimulation_gb300 as lts
+    c = lts.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("kind", ["box_sphere", "materials"])
+@pytest.mark.parametrize("bvh_mode", [0, 1])
+def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode):
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs[kind]
+    fx = np.load(os.path.join(GOLDEN, f"render_{kind}.npz"))
+    w, h, spp, maxb, rr, seed, x0, y0, x1, y1 = (int(v) for v in fx["meta"])
+    s = lts.Scene.parse(ctx, d, sc, sub, w, h)
+    integ = lts.PathTracingIntegrator(maxb, rr, s, bvh_mode=bvh_mode)
+    r = integ.render(spp, seed, crop=(x0, y0, x1, y1), record=True, film=False)
+    L = r["L"].reshape(-1, 3)
+    sig = r["sig"].reshape(-1)
+    Lr = fx["L"].reshape(-1, 3)
+    sr = fx["sig"].reshape(-1)
+    same = sig == sr
+    div = 1.0 - same.mean()
+    ok = np.all(np.abs(L - Lr) <= RTOL * np.abs(Lr) + ATOL, axis=1)
+    mism = 1.0 - ok[same].mean()
+    print(f"{kind} bvh={bvh_mode}: samples={len(sig)} divergent={div:.5f} mismatched={mism:.6f} "
+          f"maxrel={np.max(np.abs(L - Lr)[same] / (np.abs(Lr[same]) + 1e-6)):.3g}")
+    assert np.isfinite(L).all()
+    assert div <= MAX_DIVERGENT
+    assert mism <= MAX_MISMATCH
+
+
+@pytest.mark.parametrize("kind", ["box_sphere", "materials"])
+def test_film_matches_reference(ctx, scene_dirs, kind):
+    """Full-frame film (Kahan FP32 + FP64 resolve) against the reference's single-thread film."""
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs[kind]
+    fx = np.load(os.path.join(GOLDEN, f"film_{kind}.npz"))
+    w, h, spp, maxb, rr, seed = (int(v) for v in fx["meta"])
+    s = lts.Scene.parse(ctx, d, sc, sub, w, h)
+    r = lts.PathTracingIntegrator(maxb, rr, s).render(spp, seed)
+    film = r["film"].reshape(-1)
+    ref = fx["film"].reshape(-1)
+    err = np.abs(film - ref)
+    rel_rmse = np.sqrt(np.mean(err ** 2)) / np.sqrt(np.mean(ref ** 2))
+    print(f"{kind}: film rel-RMSE vs reference {rel_rmse:.3g}, pixels off by >1e-3 rel: "
+          f"{np.mean(err > 1e-3 * np.abs(ref) + 1e-5):.4f}")
+    assert rel_rmse < 5e-3
