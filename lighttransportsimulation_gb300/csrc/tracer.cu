@@ -429,9 +429,10 @@ __device__ __forceinline__ float octaves_of(V3 dpdx, V3 dpdy, int max_oct) {
     return clampf(-1 - 0.5f * log2f(l2), 0, (float)max_oct);
 }
 // Procedural.cuh:161-179
-__device__ float fbm(V3 p, V3 dpdx, V3 dpdy, float omega, int max_oct) {
+__device__ float fbm(V3 p, V3 dpdx, V3 dpdy, float omega, int max_oct, uint64_t* sig) {
     const float n = octaves_of(dpdx, dpdy, max_oct);
     const int ni = (int)floorf(n);
+    if (sig) fnv_mix(*sig, 0x400000000ull + (unsigned)ni);
     float sum = 0, lambda = 1, o = 1;
     for (int i = 0; i < ni; ++i) {
         sum += o * perlin(p.x * lambda, p.y * lambda, p.z * lambda);
@@ -443,9 +444,10 @@ __device__ float fbm(V3 p, V3 dpdx, V3 dpdy, float omega, int max_oct) {
     return sum;
 }
 // Procedural.cuh:181-205
-__device__ float turbulence(V3 p, V3 dpdx, V3 dpdy, float omega, int max_oct) {
+__device__ float turbulence(V3 p, V3 dpdx, V3 dpdy, float omega, int max_oct, uint64_t* sig) {
     const float n = octaves_of(dpdx, dpdy, max_oct);
     const int ni = (int)floorf(n);
+    if (sig) fnv_mix(*sig, 0x400000000ull + (unsigned)ni);
     float sum = 0, lambda = 1, o = 1;
     for (int i = 0; i < ni; ++i) {
         sum += o * fabsf(perlin(p.x * lambda, p.y * lambda, p.z * lambda));
@@ -461,18 +463,19 @@ __device__ float turbulence(V3 p, V3 dpdx, V3 dpdy, float omega, int max_oct) {
     return sum;
 }
 
-__device__ Spec eval_texture(const DevTex& t, const SI& si) {
+__device__ Spec eval_texture(const DevTex& t, const SI& si, uint64_t* sig) {
     switch (t.kind) {
         case 1:  // FBmTexture (Procedural.cuh:207-225)
-            return spec(fbm(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0]));
+            return spec(fbm(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0], sig));
         case 2:  // WrinkledTexture (Procedural.cuh:227-245)
-            return spec(turbulence(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0]));
+            return spec(turbulence(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0], sig));
         case 3: {  // MarbleTexture (Procedural.cuh:267-311)
             const float scale = t.v[2], var = t.v[3];
             const V3 p = si.p * scale;
-            const float marble = p.y + var * fbm(p, si.dpdx * scale, si.dpdy * scale, t.v[1], (int)t.v[0]);
+            const float marble = p.y + var * fbm(p, si.dpdx * scale, si.dpdy * scale, t.v[1], (int)t.v[0], sig);
             float tt = 0.5f + 0.5f * sinf(marble);
             const int first = (int)floorf(tt * 6.0f);
+            if (sig) fnv_mix(*sig, 0x500000000ull + (unsigned)first);
             tt = (tt * 6.0f - first);
             Spec c[4];
 #pragma unroll
@@ -485,8 +488,8 @@ __device__ Spec eval_texture(const DevTex& t, const SI& si) {
             return (s0 * (1.0f - tt) + s1 * tt) * 1.5f;
         }
         case 4: {  // WindyTexture (Procedural.cuh:247-265)
-            const float wind = fbm(si.p * 0.1f, si.dpdx * 0.1f, si.dpdy * 0.1f, 0.5f, 3);
-            const float wave = fbm(si.p, si.dpdx, si.dpdy, 0.5f, 6);
+            const float wind = fbm(si.p * 0.1f, si.dpdx * 0.1f, si.dpdy * 0.1f, 0.5f, 3, sig);
+            const float wave = fbm(si.p, si.dpdx, si.dpdy, 0.5f, 6, sig);
             return spec(fabsf(wind) * wave);
         }
         default:
@@ -772,7 +775,7 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, ui
 
 // Material::computeScatteringFunctions (materials/Material.cuh:31-130) into a Bsdf record.
 // Returns false when the primitive has no material (the reference's skipped 'M' entries).
-__device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f) {
+__device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, uint64_t* sig) {
     const int mesh = __ldg(&sv.prim_n[si.prim].w);
     const DevMat& m = sv.mats[mesh];
     if (m.kind == 0) return false;
@@ -785,7 +788,7 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f) {
     f.eta = 1;
     switch (m.kind) {
         case 1: {  // Matte
-            const Spec kd = eval_texture(m.tex[0], si);
+            const Spec kd = eval_texture(m.tex[0], si, sig);
             if (!is_black(kd)) {
                 f.R = kd;
                 if (m.extra == 0) {
@@ -801,7 +804,7 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f) {
         }
         case 2: {  // Glass
             f.eta = m.extra;
-            const Spec r = eval_texture(m.tex[0], si), t = eval_texture(m.tex[1], si);
+            const Spec r = eval_texture(m.tex[0], si, sig), t = eval_texture(m.tex[1], si, sig);
             if (is_black(r) && is_black(t)) break;
             f.R = r;
             f.T = t;
@@ -810,7 +813,7 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f) {
             break;
         }
         case 3: {  // Mirror
-            const Spec r = eval_texture(m.tex[0], si);
+            const Spec r = eval_texture(m.tex[0], si, sig);
             if (is_black(r)) break;
             f.R = r;
             f.lobe = LOBE_SPECULAR_REFL;
@@ -818,7 +821,7 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f) {
             break;
         }
         case 4: {  // Metal (alpha given directly)
-            f.k = eval_texture(m.tex[0], si);
+            f.k = eval_texture(m.tex[0], si, sig);
             f.eta3 = Spec{m.tex[1].v[0], m.tex[1].v[1], m.tex[1].v[2]};
             f.R = spec(1.0f);
             f.alpha = m.extra;
@@ -1000,7 +1003,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                 si.dpdy = v3(0, 0, 0);
             }
             Bsdf f;
-            if (!make_bsdf(sv, si, f)) break;
+            if (!make_bsdf(sv, si, f, RECORD ? &sig : nullptr)) break;
             // 7a. direct lighting: uniformSampleOneLight + estimateDirect (IntegratorHelper.cuh:51-149)
             if (sv.nlight > 0) {
                 const float ul = rng_1d(rng);

@@ -492,10 +492,12 @@ static float smooth(float mn, float mx, float v) {
     const float t = clampf((v - mn) / (mx - mn), 0, 1);
     return t * t * (-2 * t + 3);
 }
-static float fbm(V p, V dx, V dy, float omega, int maxo) {
+static void fnv(uint64_t& h, uint64_t v);
+static float fbm(V p, V dx, V dy, float omega, int maxo, uint64_t* sig) {
     const float l2 = fmaxf(len2(dx), len2(dy));
     const float n = clampf(-1 - 0.5f * log2f(l2), 0, maxo);
     const int ni = (int)floorf(n);
+    if (sig) fnv(*sig, 0x400000000ull + (unsigned)ni);
     float sum = 0, lam = 1, o = 1;
     for (int i = 0; i < ni; ++i) {
         sum += o * perlin(p.x * lam, p.y * lam, p.z * lam);
@@ -506,10 +508,11 @@ static float fbm(V p, V dx, V dy, float omega, int maxo) {
     sum += o * smooth(0.3f, 0.7f, np) * perlin(p.x * lam, p.y * lam, p.z * lam);
     return sum;
 }
-static float turbulence(V p, V dx, V dy, float omega, int maxo) {
+static float turbulence(V p, V dx, V dy, float omega, int maxo, uint64_t* sig) {
     const float l2 = fmaxf(len2(dx), len2(dy));
     const float n = clampf(-1 - 0.5f * log2f(l2), 0, maxo);
     const int ni = (int)floorf(n);
+    if (sig) fnv(*sig, 0x400000000ull + (unsigned)ni);
     float sum = 0, lam = 1, o = 1;
     for (int i = 0; i < ni; ++i) {
         sum += o * fabsf(perlin(p.x * lam, p.y * lam, p.z * lam));
@@ -527,16 +530,17 @@ static float turbulence(V p, V dx, V dy, float omega, int maxo) {
 static const float kMarble[10][3] = {{.58f, .58f, .6f}, {.58f, .58f, .6f}, {.58f, .58f, .6f}, {.5f, .5f, .5f},
                                      {.6f, .59f, .58f}, {.58f, .58f, .6f}, {.58f, .58f, .6f}, {.2f, .2f, .33f},
                                      {.58f, .58f, .6f}, {.58f, .58f, .6f}};
-static S texture(const lts::HostTexture& t, const SI& si) {
+static S texture(const lts::HostTexture& t, const SI& si, uint64_t* sig) {
     switch (t.kind) {
-        case lts::TEX_FBM: return sp(fbm(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0]));
-        case lts::TEX_WRINKLED: return sp(turbulence(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0]));
+        case lts::TEX_FBM: return sp(fbm(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0], sig));
+        case lts::TEX_WRINKLED: return sp(turbulence(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0], sig));
         case lts::TEX_MARBLE: {
             const float scale = t.v[2], var = t.v[3];
             const V p = si.p * scale;
-            const float marble = p.y + var * fbm(p, si.dpdx * scale, si.dpdy * scale, t.v[1], (int)t.v[0]);
+            const float marble = p.y + var * fbm(p, si.dpdx * scale, si.dpdy * scale, t.v[1], (int)t.v[0], sig);
             float tt = 0.5f + 0.5f * sinf(marble);
             const int first = (int)floorf(tt * (float)6);
+            if (sig) fnv(*sig, 0x500000000ull + (unsigned)first);
             tt = (tt * (float)6 - first);
             S c[4];
             for (int k = 0; k < 4; ++k) c[k] = S{kMarble[first + k][0], kMarble[first + k][1], kMarble[first + k][2]};
@@ -547,8 +551,8 @@ static S texture(const lts::HostTexture& t, const SI& si) {
             return (s0 * (1.0f - tt) + s1 * tt) * 1.5f;
         }
         case lts::TEX_WINDY: {
-            const float wind = fbm(si.p * 0.1f, si.dpdx * 0.1f, si.dpdy * 0.1f, 0.5f, 3);
-            const float wave = fbm(si.p, si.dpdx, si.dpdy, 0.5f, 6);
+            const float wind = fbm(si.p * 0.1f, si.dpdx * 0.1f, si.dpdy * 0.1f, 0.5f, 3, sig);
+            const float wave = fbm(si.p, si.dpdx, si.dpdy, 0.5f, 6, sig);
             return sp(fabsf(wind) * wave);
         }
         default: return S{t.v[0], t.v[1], t.v[2]};
@@ -811,7 +815,7 @@ static S bsdf_sample(const Bsdf& f, V woW, V* wiW, P2 u, float* pdf, uint32_t fl
     return val;
 }
 
-static bool make_bsdf(const Scene& sc, const SI& si, Bsdf* f) {  // Material.cuh:31-130
+static bool make_bsdf(const Scene& sc, const SI& si, Bsdf* f, uint64_t* sig) {  // Material.cuh:31-130
     const int mesh = sc.h->tri_mesh[si.prim];
     const lts::HostMaterial& m = sc.h->materials[mesh];
     if (m.kind == lts::MAT_NONE) return false;
@@ -821,7 +825,7 @@ static bool make_bsdf(const Scene& sc, const SI& si, Bsdf* f) {  // Material.cuh
     f->ts = cross(f->ns, f->ss);
     switch (m.kind) {
         case lts::MAT_MATTE: {
-            const S kd = texture(m.tex[0], si);
+            const S kd = texture(m.tex[0], si, sig);
             if (!black(kd)) {
                 f->R = kd;
                 f->lobe = m.extra == 0 ? LAMBERT : OREN;
@@ -833,7 +837,7 @@ static bool make_bsdf(const Scene& sc, const SI& si, Bsdf* f) {  // Material.cuh
         }
         case lts::MAT_GLASS: {
             f->eta = m.extra;
-            const S r = texture(m.tex[0], si), t = texture(m.tex[1], si);
+            const S r = texture(m.tex[0], si, sig), t = texture(m.tex[1], si, sig);
             if (black(r) && black(t)) break;
             f->R = r;
             f->T = t;
@@ -842,7 +846,7 @@ static bool make_bsdf(const Scene& sc, const SI& si, Bsdf* f) {  // Material.cuh
             break;
         }
         case lts::MAT_MIRROR: {
-            const S r = texture(m.tex[0], si);
+            const S r = texture(m.tex[0], si, sig);
             if (black(r)) break;
             f->R = r;
             f->lobe = SREFL;
@@ -850,7 +854,7 @@ static bool make_bsdf(const Scene& sc, const SI& si, Bsdf* f) {  // Material.cuh
             break;
         }
         case lts::MAT_METAL: {
-            f->k = texture(m.tex[0], si);
+            f->k = texture(m.tex[0], si, sig);
             f->eta3 = S{m.tex[1].v[0], m.tex[1].v[1], m.tex[1].v[2]};
             f->R = sp(1.0f);
             f->alpha = m.extra;
@@ -997,7 +1001,7 @@ static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* out
                 si.dpdx = si.dpdy = mk(0, 0, 0);
             }
             Bsdf f;
-            if (!make_bsdf(sc, si, &f)) break;
+            if (!make_bsdf(sc, si, &f, &sig)) break;
             if (nl > 0) {  // uniformSampleOneLight + estimateDirect (IntegratorHelper.cuh:51-149)
                 const float ul = r1(rng);
                 int off = 0;
