@@ -313,8 +313,16 @@ def main():
     ap.add_argument("--small", action="store_true", help="256x256x16 spp level-6 sphere (quick check)")
     ap.add_argument("--skip-lbvh", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--lbvh-only", type=int, default=0, metavar="N",
+                    help="only time the LBVH build over N random triangles (seed 1)")
     args = ap.parse_args()
     wl = SMALL if args.small else WORKLOAD
+    if args.lbvh_only:
+        import lighttransportsimulation_gb300 as lts
+        ctx = lts.Context(0)
+        print(json.dumps(lbvh_bench(ctx, args.lbvh_only, args.steps, args.warmup, lts.BVH_SORTED, measured_peaks()[0])))
+        ctx.close()
+        return
     if args.impl == "reference":
         run_reference(args, wl)
     else:
