@@ -152,8 +152,8 @@ def barrier_max(dist, value):
 
 
 def run_reference(args, wl):
-    rank, world, local, dist = dist_setup(args.gpus)
-    if rank != 0:
+    # CPU arm: rank 0 alone runs; other ranks of a torchrun launch exit without work
+    if int(os.environ.get("RANK", "0")) != 0:
         return
     vals = []
     for _ in range(args.warmup):
