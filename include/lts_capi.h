@@ -116,6 +116,22 @@ int lts_bvh_build_device_async(lts_ctx* ctx, const float* d_tri_p9, int32_t n, i
 /* Copies the last build to host buffers (synchronises the stream). */
 int lts_bvh_dump_get(lts_ctx* ctx, lts_bvh_dump* dump);
 
+/* No counterpart in the reference.  The same LBVH build for callers that may not allocate
+ * device memory (memory-pool or allocator callbacks, real-time loops that forbid cudaMalloc,
+ * plugins whose host owns every allocation): no context, no cudaMalloc/cudaFree, all scratch in
+ * one fixed file-scope device array of about 5.3 MiB that each GPU loading the library keeps
+ * until exit.  n <= LTS_NOALLOC_MAX_PRIMITIVES, else LTS_ERR_ARG.  The caller passes device
+ * buffers: d_tri_p9 [9n floats], outputs d_sorted_codes [n], d_sorted_ids [n], d_nodes
+ * [(n-1) x 64 bytes: left box, right box, children (>= 0 interior, < 0 leaf ~l)], d_leaf_prim
+ * [n], d_root_bounds [6].  Runs on `stream` (a cudaStream_t, NULL for the default stream) and
+ * waits for it before returning.  The first call on a device looks up the array's address
+ * (may load the module): make it before any stream capture.  Calls share the array, so calls
+ * that overlap on the GPU race. */
+#define LTS_NOALLOC_MAX_PRIMITIVES 262144
+int lts_bvh_build_noalloc(const float* d_tri_p9, int32_t n, int32_t mode, int32_t code_limit,
+                          uint32_t* d_sorted_codes, int32_t* d_sorted_ids, void* d_nodes, int32_t* d_leaf_prim,
+                          float* d_root_bounds, void* stream);
+
 /* ---------------------------------------------------------------- rendering */
 #define LTS_INTEGRATOR_MEGAKERNEL 0 /* one thread per pixel, all spp and bounces        */
 #define LTS_INTEGRATOR_WAVEFRONT 1  /* generate / extend / shade / shadow / film queues  */

@@ -13,7 +13,10 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <string>
+
+#include "../../include/lts_capi.h"
 
 #include "dev_common.cuh"
 #include "lbvh.cuh"
@@ -485,3 +488,125 @@ void Lbvh::stage_ms(float out[5]) const {
 }
 
 }  // namespace lts
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free LBVH build.
+//
+// Some callers cannot allocate device memory at all: code running inside a host allocator or
+// memory-pool callback, real-time render loops that forbid cudaMalloc/cudaFree (both can
+// synchronise the whole device), and plugins whose host application owns every device
+// allocation.  This variant keeps all of the build's scratch (the sort's ping-pong buffers and
+// look-back table, histograms, parent links, refit counters, the scene box and an error word) in
+// one file-scope device array of fixed size, so a call allocates nothing; the caller supplies the
+// triangles and every output buffer.
+//
+// Limits and sharing: at most kNoAllocMaxPrims primitives (about 5.3 MiB of device memory that
+// every GPU which loads the library keeps until process exit).  All calls share the one array and
+// it keeps the previous call's contents, so everything that must start at zero is cleared at the
+// start of each call, and two calls that overlap on the GPU (different streams, or different host
+// threads) race on it.  The first call on a device looks up the array's device address with
+// cudaGetSymbolAddress (which may load the module), so that first call should be made before any
+// stream capture begins.
+// ---------------------------------------------------------------------------------------------
+namespace lts {
+namespace {
+
+constexpr int kNoAllocMaxPrims = 1 << 18;
+constexpr size_t kNoAllocTiles = (kNoAllocMaxPrims + kSortTile - 1) / kSortTile;
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t kOffCodes = 0;
+constexpr size_t kOffIds = kOffCodes + align256(4ull * kNoAllocMaxPrims);
+constexpr size_t kOffHist = kOffIds + align256(4ull * kNoAllocMaxPrims);
+constexpr size_t kOffStatus = kOffHist + align256(4ull * 2 * 4 * 256);
+constexpr size_t kOffCounters = kOffStatus + align256(4ull * 4 * 256 * kNoAllocTiles);
+constexpr size_t kOffBounds = kOffCounters + 256;
+constexpr size_t kOffError = kOffBounds + 256;
+constexpr size_t kOffFlags = kOffError + 256;
+constexpr size_t kOffParent = kOffFlags + align256(4ull * kNoAllocMaxPrims);
+constexpr size_t kNoAllocBytes = kOffParent + align256(4ull * (2ull * kNoAllocMaxPrims - 1));
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+}  // namespace
+
+int lbvh_noalloc_limit() { return kNoAllocMaxPrims; }
+
+}  // namespace lts
+
+
+
+
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {nullptr};
+}  // namespace
+
+extern "C" int lts_bvh_build_noalloc(const float* d_tri, int32_t n, int32_t mode, int32_t code_limit,
+                                     uint32_t* d_codes, int32_t* d_ids, void* d_nodes, int32_t* d_leaf_prim,
+                                     float* d_root_bounds, void* stream) {
+    using namespace lts;
+    if (!d_tri || !d_codes || !d_ids || !d_leaf_prim || !d_root_bounds || n < 1) return LTS_ERR_ARG;
+    if (n > kNoAllocMaxPrims) return LTS_ERR_ARG;
+    if (n > 1 && !d_nodes) return LTS_ERR_ARG;
+    if (mode != BVH_MODE_REFERENCE && mode != BVH_MODE_SORTED) return LTS_ERR_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return LTS_ERR_CUDA;
+    unsigned char* base;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return LTS_ERR_CUDA;
+            g_noalloc_addr[dev] = p;
+        }
+        base = static_cast<unsigned char*>(g_noalloc_addr[dev]);
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t* codes_alt = reinterpret_cast<uint32_t*>(base + kOffCodes);
+    int32_t* ids_alt = reinterpret_cast<int32_t*>(base + kOffIds);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(base + kOffHist);
+    uint32_t* status = reinterpret_cast<uint32_t*>(base + kOffStatus);
+    uint32_t* counters = reinterpret_cast<uint32_t*>(base + kOffCounters);
+    uint32_t* gbounds = reinterpret_cast<uint32_t*>(base + kOffBounds);
+    uint32_t* err = reinterpret_cast<uint32_t*>(base + kOffError);
+    uint32_t* flags = reinterpret_cast<uint32_t*>(base + kOffFlags);
+    int32_t* parent = reinterpret_cast<int32_t*>(base + kOffParent);
+    BvhNode* nodes = static_cast<BvhNode*>(d_nodes);
+    const size_t N = (size_t)n, tiles = (N + kSortTile - 1) / kSortTile;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return LTS_ERR_CUDA;
+    const int stream_grid = std::min(grid_for((long)N, kBlock), sms * 8);
+    // clear everything the kernels expect to start zeroed (or all-ones)
+    cudaMemsetAsync(err, 0, 4, s);
+    cudaMemsetAsync(gbounds, 0xff, 12, s);
+    cudaMemsetAsync(gbounds + 3, 0x00, 12, s);
+    cudaMemsetAsync(hist, 0, 4 * 4 * 256, s);
+    cudaMemsetAsync(status, 0, 4 * 4 * 256 * tiles, s);
+    cudaMemsetAsync(counters, 0, 4 * 8, s);
+    k_scene_bounds<<<stream_grid, kBlock, 0, s>>>(d_tri, n, gbounds);
+    k_morton<<<stream_grid, kBlock, 0, s>>>(d_tri, n, gbounds, code_limit, d_codes, d_ids, hist);
+    k_digit_prefix<<<4, 256, 0, s>>>(hist, hist + 4 * 256);
+    uint32_t* kin = d_codes;
+    int32_t* vin = d_ids;
+    uint32_t* kout = codes_alt;
+    int32_t* vout = ids_alt;
+    for (int p = 0; p < 4; ++p) {
+        k_onesweep<<<(int)tiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, 8 * p, hist + 4 * 256 + 256 * p,
+                                                        status + (size_t)p * 256 * tiles, counters + p, err);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    if (n > 1) {
+        cudaMemsetAsync(parent, 0xff, 4 * (2 * N - 1), s);
+        k_topology<<<grid_for((long)N - 1, kBlock), kBlock, 0, s>>>(d_codes, n, nodes, parent);
+        cudaMemsetAsync(flags, 0, 4 * (N - 1), s);
+    }
+    k_refit<<<grid_for((long)N, kBlock), kBlock, 0, s>>>(d_tri, n, mode, d_ids, parent, nodes, flags, d_leaf_prim,
+                                                        d_root_bounds);
+    if (cudaGetLastError() != cudaSuccess) return LTS_ERR_CUDA;
+    uint32_t h_err = 0;
+    if (cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return LTS_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return LTS_ERR_CUDA;
+    return h_err ? LTS_ERR_DEVICE : LTS_OK;
+}
