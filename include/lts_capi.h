@@ -174,6 +174,13 @@ int lts_film_get(lts_ctx* ctx, float* film_rgb, double* film_sums);
  * (little-endian, scale -1).  Replaces writeToPPM / writeToPFM (core/ImageO.cuh:16-78). */
 int lts_write_image(const char* path, const float* rgb, int32_t width, int32_t height, int32_t format);
 
+/* Parity debugging (no counterpart in the reference): the next record-mode lts_render also
+ * writes the intermediate values of one sample -- crop sample index k = (row * crop width +
+ * column) * spp + sample, -1 to stop -- as up to 64 records of 16 floats (record[0] = event tag:
+ * 1 hit, 2 material, 3 light sample, 4 MIS BSDF sample, 5 path BSDF sample, 6 final radiance). */
+int lts_debug_trace_sample(lts_ctx* ctx, int64_t crop_sample_index);
+int lts_debug_trace_get(lts_ctx* ctx, float* out_64x16);
+
 /* ---------------------------------------------------------------- metrics */
 typedef struct {
     double bvh_build_ms;  /* device time of the last LBVH build */

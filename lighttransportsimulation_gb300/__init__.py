@@ -34,7 +34,8 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_scene_info_get", "lts_scene_get_triangles", "lts_scene_get_camera",
            "lts_scene_get_light_distribution", "lts_bvh_build", "lts_bvh_build_triangles",
            "lts_bvh_build_device_async", "lts_bvh_dump_get", "lts_render", "lts_render_async", "lts_film_get",
-           "lts_write_image", "lts_get_metrics", "lts_bvh_build_noalloc"]
+           "lts_write_image", "lts_get_metrics", "lts_bvh_build_noalloc", "lts_debug_trace_sample",
+           "lts_debug_trace_get"]
 
 
 class LtsError(RuntimeError):
@@ -108,6 +109,8 @@ def library():
             "lts_write_image": (I, [ctypes.c_char_p, P, I, I, I]),
             "lts_get_metrics": (I, [P, ctypes.POINTER(Metrics)]),
             "lts_bvh_build_noalloc": (I, [P, I, I, I, P, P, P, P, P, P]),
+            "lts_debug_trace_sample": (I, [P, ctypes.c_int64]),
+            "lts_debug_trace_get": (I, [P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)

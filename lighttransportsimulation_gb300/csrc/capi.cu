@@ -427,6 +427,20 @@ int lts_write_image(const char* path, const float* rgb, int32_t w, int32_t h, in
     return LTS_OK;
 }
 
+int lts_debug_trace_sample(lts_ctx* ctx, int64_t k) {
+    if (!ctx) return LTS_ERR_ARG;
+    if (!ctx->tracer) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    ctx->tracer->trace_sample_ = (long)k;
+    return LTS_OK;
+}
+
+int lts_debug_trace_get(lts_ctx* ctx, float* out) {
+    if (!ctx || !out) return LTS_ERR_ARG;
+    if (!ctx->tracer || !ctx->tracer->trace_) return fail(ctx, LTS_ERR_STATE, "no trace recorded");
+    CK(cudaMemcpy(out, ctx->tracer->trace_, 64 * 16 * 4, cudaMemcpyDeviceToHost));
+    return LTS_OK;
+}
+
 int lts_get_metrics(lts_ctx* ctx, lts_metrics* out) {
     if (!ctx || !out) return LTS_ERR_ARG;
     *out = ctx->metrics;

@@ -112,6 +112,20 @@ __device__ __forceinline__ void fnv_mix(uint64_t& h, uint64_t v) {
     }
 }
 
+// ------------------------------------------------------------------ single-sample trace (record mode)
+struct Tracer16 {
+    float* out;
+    int n;
+    __device__ void put(float tag, float a = 0, float b = 0, float c = 0, float d = 0, float e = 0, float f = 0,
+                        float g = 0, float h = 0, float i = 0, float j = 0, float k = 0, float l = 0, float m = 0,
+                        float o = 0, float p = 0) {
+        if (!out || n >= 64) return;
+        float* r = out + 16 * n++;
+        r[0] = tag; r[1] = a; r[2] = b; r[3] = c; r[4] = d; r[5] = e; r[6] = f; r[7] = g; r[8] = h;
+        r[9] = i; r[10] = j; r[11] = k; r[12] = l; r[13] = m; r[14] = o; r[15] = p;
+    }
+};
+
 // ------------------------------------------------------------------ geometry fetch
 __device__ __forceinline__ V3 f4v(float4 a) { return v3(a.x, a.y, a.z); }
 __device__ __forceinline__ void prim_tri(const SceneView& sv, int prim, V3& p0, V3& p1, V3& p2) {
@@ -507,7 +521,11 @@ __device__ __forceinline__ float tan2t(V3 w) { return sin2t(w) / cos2t(w); }
 // sin == 0 branch (models/BxDF.cuh:144-153).
 __device__ __forceinline__ float cosphi(V3 w) { return clampf(w.x / sint(w), -1, 1); }
 __device__ __forceinline__ float sinphi(V3 w) { return clampf(w.y / sint(w), -1, 1); }
-__device__ __forceinline__ bool same_hemi(V3 a, V3 b) { return a.z * b.z > 0; }
+__device__ __forceinline__ bool same_hemi(V3 a, V3 b, uint64_t* sig) {  // sameHemisphere, recorded
+    const bool v = a.z * b.z > 0;
+    if (sig) fnv_mix(*sig, 0x700000000ull + (v ? 1u : 0u));
+    return v;
+}
 
 // models/BxDF.cuh:16-37 with the swapped clamp bounds of line 17.
 __device__ float fresnel_dielectric(float cos_i, float eta_i, float eta_t) {
@@ -669,13 +687,13 @@ __device__ Spec lobe_f(const Bsdf& f, V3 wo, V3 wi) {
     }
 }
 // BxDF::Pdf
-__device__ float lobe_pdf(const Bsdf& f, V3 wo, V3 wi) {
+__device__ float lobe_pdf(const Bsdf& f, V3 wo, V3 wi, uint64_t* sig) {
     switch (f.lobe) {
         case LOBE_LAMBERT:
         case LOBE_OREN_NAYAR:
-            return same_hemi(wo, wi) ? mul_dc(fabsf(wi.z), LTS_1_PI_HI, LTS_1_PI_LO) : 0.0f;
+            return same_hemi(wo, wi, sig) ? mul_dc(fabsf(wi.z), LTS_1_PI_HI, LTS_1_PI_LO) : 0.0f;
         case LOBE_MICROFACET: {
-            if (!same_hemi(wo, wi)) return 0;
+            if (!same_hemi(wo, wi, sig)) return 0;
             const V3 wh = normalize(wo + wi);
             const float pd = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha, f.alpha) * absdot(wo, wh) / fabsf(wo.z);
             return pd / (4 * dot(wo, wh));
@@ -684,25 +702,27 @@ __device__ float lobe_pdf(const Bsdf& f, V3 wo, V3 wi) {
     }
 }
 // BSDF::f (materials/BSDF.cuh:192-204)
-__device__ Spec bsdf_f(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags) {
+__device__ Spec bsdf_f(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags, uint64_t* sig) {
+    const bool reflect = dot(wiW, f.ng) * dot(woW, f.ng) > 0;
+    if (sig) fnv_mix(*sig, 0x600000000ull + (reflect ? 1u : 0u));
     if (f.lobe == LOBE_NONE || !matches(f.type, flags)) return spec(0.0f);
     const V3 wi = to_local(f, wiW), wo = to_local(f, woW);
-    const bool reflect = dot(wiW, f.ng) * dot(woW, f.ng) > 0;
     if ((reflect && (f.type & BSDF_REFLECTION)) || (!reflect && (f.type & BSDF_TRANSMISSION)))
         return spec(0.0f) + lobe_f(f, wo, wi);
     return spec(0.0f);
 }
 // BSDF::Pdf (BSDF.cuh:261-276)
-__device__ float bsdf_pdf(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags) {
+__device__ float bsdf_pdf(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags, uint64_t* sig) {
     if (f.lobe == LOBE_NONE) return 0.0f;
     const V3 wo = to_local(f, woW), wi = to_local(f, wiW);
     if (wo.z == 0) return 0.0f;
     if (!matches(f.type, flags)) return 0.0f;
-    const float pdf = 0.0f + lobe_pdf(f, wo, wi);
+    const float pdf = 0.0f + lobe_pdf(f, wo, wi, sig);
     return pdf / 1;
 }
 // BSDF::sampleF with a single matching lobe (BSDF.cuh:206-259) and the lobes' sampleF.
-__device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, uint32_t flags, uint32_t& sampled) {
+__device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, uint32_t flags, uint32_t& sampled,
+                            uint64_t* sig) {
     if (f.lobe == LOBE_NONE || !matches(f.type, flags)) {
         pdf = 0;
         return spec(0.0f);
@@ -721,7 +741,7 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, ui
             const float dx = r * cosf(th), dy = r * sinf(th);
             wi = v3(dx, dy, sqrtf(fmaxf(0.0f, 1 - dx * dx - dy * dy)));
             if (wo.z < 0) wi.z *= -1;
-            pdf = lobe_pdf(f, wo, wi);
+            pdf = lobe_pdf(f, wo, wi, sig);
             val = lobe_f(f, wo, wi);
             break;
         }
@@ -761,7 +781,7 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, ui
             if (flip) wh = -wh;
             if (dot(wo, wh) < 0) return spec(0.0f);
             wi = -wo + wh * (2 * dot(wo, wh));
-            if (!same_hemi(wo, wi)) return spec(0.0f);
+            if (!same_hemi(wo, wi, sig)) return spec(0.0f);
             const float pd = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha, f.alpha) * absdot(wo, wh) / fabsf(wo.z);
             pdf = pd / (4 * dot(wo, wh));
             val = lobe_f(f, wo, wi);
@@ -952,6 +972,10 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
         rng.sample = (uint32_t)s;
         rng.draw = 0;
         uint64_t sig = 0xcbf29ce484222325ull;
+        Tracer16 tr{nullptr, 0};
+        if (RECORD && rp.trace &&
+            ((long)((j - rp.y0) * (rp.x1 - rp.x0) + (i - rp.x0)) * rp.spp + s) == rp.trace_sample)
+            tr.out = rp.trace;
         // 3. camera ray (PathTracingIntegrator.cuh:40-46, Camera.cu:51-81); aperture is 0, so the
         // lens sample moves nothing, but it is drawn.
         const F2 fs = rng_2d(rng);
@@ -972,6 +996,8 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
             ++rays;
             const bool hit = scene_intersect(sv, nleaf, ro, rd, INFINITY, si, stack, rp.err, wk);
             if (RECORD) fnv_mix(sig, 0x100000000ull + (uint64_t)((hit ? si.prim : -1) + 1));
+            if (RECORD) tr.put(1, hit, hit ? si.prim : -1, si.p.x, si.p.y, si.p.z, si.n.x, si.n.y, si.n.z, si.sn.x, si.sn.y,
+                               si.sn.z, beta.r, beta.g, beta.b, L.r);
             if (bounce == 0 || specular) {
                 if (hit) {
                     const int li = __ldg(sv.prim_light + si.prim);
@@ -1004,6 +1030,8 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
             }
             Bsdf f;
             if (!make_bsdf(sv, si, f, RECORD ? &sig : nullptr)) break;
+            if (RECORD) tr.put(2, f.lobe, f.R.r, f.R.g, f.R.b, f.ss.x, f.ss.y, f.ss.z, f.ts.x, f.ts.y, f.ts.z, si.dpdx.x,
+                               si.dpdx.y, si.dpdx.z);
             // 7a. direct lighting: uniformSampleOneLight + estimateDirect (IntegratorHelper.cuh:51-149)
             if (sv.nlight > 0) {
                 const float ul = rng_1d(rng);
@@ -1033,14 +1061,15 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                 LightSample ls;
                 const bool delta = sample_li(sv, Lt, si, ulight, ls);
                 if (ls.pdf > 0 && !is_black(ls.Li)) {
-                    const Spec fv = bsdf_f(f, si.wo, ls.wi, flags) * absdot(ls.wi, si.sn);
-                    const float spdf = bsdf_pdf(f, si.wo, ls.wi, flags);
+                    const Spec fv = bsdf_f(f, si.wo, ls.wi, flags, RECORD ? &sig : nullptr) * absdot(ls.wi, si.sn);
+                    const float spdf = bsdf_pdf(f, si.wo, ls.wi, flags, RECORD ? &sig : nullptr);
                     if (!is_black(fv)) {
                         // VisibilityTester::unoccluded -> spawnRayTo(Interaction) (Interaction.cuh:47-51)
                         const V3 org = offset_origin(si.p, si.perr, si.n, ls.p1 - si.p);
                         const V3 tgt = offset_origin(ls.p1, ls.perr1, ls.n1, org - ls.p1);
                         ++rays;
                         const bool occ = scene_occluded(sv, nleaf, org, tgt - org, 1 - kShadowEps, stack, rp.err, wk);
+                        if (RECORD) tr.put(3, off, lpdf_sel, ls.pdf, ls.Li.r, ls.wi.x, ls.wi.y, ls.wi.z, fv.r, fv.g, fv.b, spdf, occ);
                         if (RECORD) fnv_mix(sig, 0x300000000ull + (occ ? 0u : 1u));
                         Spec Li = ls.Li;
                         if (occ) Li = spec(0.0f);
@@ -1059,7 +1088,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                     V3 wi = ls.wi;
                     float spdf = 0;
                     uint32_t stype = 0;
-                    Spec fv = bsdf_sample(f, si.wo, wi, uscat, spdf, flags, stype);
+                    Spec fv = bsdf_sample(f, si.wo, wi, uscat, spdf, flags, stype, RECORD ? &sig : nullptr);
                     fv = fv * absdot(wi, si.sn);
                     const bool sampled_spec = (stype & BSDF_SPECULAR) != 0;
                     if (!is_black(fv) && spdf > 0) {
@@ -1090,6 +1119,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                                 Li = Lt.kind == 1 ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
                             }
                             if (!is_black(Li)) Ld = Ld + fv * Li * spec(1.0f) * wgt / spdf;
+                            if (RECORD) tr.put(4, spdf, fv.r, fv.g, fv.b, wgt, found, Li.r, Ld.r, Ld.g, Ld.b, wi.x, wi.y, wi.z);
                         }
                     }
                 }
@@ -1100,10 +1130,11 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
             float pdf = 0;
             uint32_t stype = 0;
             const F2 ub = rng_2d(rng);
-            const Spec fv = bsdf_sample(f, si.wo, wi, ub, pdf, BSDF_ALL, stype);
+            const Spec fv = bsdf_sample(f, si.wo, wi, ub, pdf, BSDF_ALL, stype, RECORD ? &sig : nullptr);
             if (is_black(fv) || pdf == 0) break;
             specular = (stype & BSDF_SPECULAR) != 0;
             beta = beta * (fv * absdot(wi, si.sn) / pdf);
+            if (RECORD) tr.put(5, wi.x, wi.y, wi.z, pdf, fv.r, fv.g, fv.b, beta.r, beta.g, beta.b, L.r, L.g, L.b);
             // 8. new ray: spawnRay, no differentials
             ro = offset_origin(si.p, si.perr, si.n, wi);
             rd = wi;
@@ -1143,6 +1174,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                 }
             }
         }
+        if (RECORD) tr.put(6, L.r, L.g, L.b);
         if (RECORD) {
             const size_t k = ((size_t)(j - rp.y0) * (rp.x1 - rp.x0) + (i - rp.x0)) * rp.spp + s;
             rp.sample_L[3 * k + 0] = L.r;
@@ -1238,6 +1270,8 @@ void Tracer::free_all() {
     counters_ = nullptr;
     dev_free(rgb_);
     rgb_ = nullptr;
+    dev_free(trace_);
+    trace_ = nullptr;
     film_cap_ = rec_cap_ = 0;
     leaf_serial_ = 0;
 }
@@ -1415,6 +1449,14 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
     rp->sample_sig = d.record_samples ? rec_sig_ : nullptr;
     rp->counters = counters_;
     rp->err = d_err;
+    rp->trace = nullptr;
+    rp->trace_sample = -1;
+    if (d.record_samples && trace_sample_ >= 0) {
+        if (!trace_) TRY(dev_alloc((void**)&trace_, 64 * 16 * 4));
+        TRY(cudaMemsetAsync(trace_, 0, 64 * 16 * 4, s));
+        rp->trace = trace_;
+        rp->trace_sample = trace_sample_;
+    }
     return "";
 }
 

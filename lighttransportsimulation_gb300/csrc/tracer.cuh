@@ -57,6 +57,8 @@ struct RenderParams {
     uint64_t* __restrict__ sample_sig;
     unsigned long long* __restrict__ counters;  // [0] rays issued
     uint32_t* __restrict__ err;
+    float* __restrict__ trace;       // record mode: 16-float event records of one sample
+    long trace_sample;               // crop sample index traced (-1: none)
 };
 
 class Tracer {
@@ -74,6 +76,9 @@ class Tracer {
     std::string film_get(const HostScene& sc, float* rgb, double* sums, cudaStream_t s);
 
     double last_ms = 0, last_paths = 0, last_rays = 0, last_node_visits = 0, last_tri_tests = 0;
+    // Parity debugging: the record-mode render writes the events of this crop sample index.
+    long trace_sample_ = -1;
+    float* trace_ = nullptr;
     int last_launches = 0;
 
    private:

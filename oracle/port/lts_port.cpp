@@ -681,7 +681,12 @@ static V to_world(const Bsdf& f, V v) {
               f.ss.z * v.x + f.ts.z * v.y + f.ns.z * v.z);
 }
 static bool match(uint32_t type, uint32_t flags) { return (type & flags) == type; }
-static float default_pdf(V wo, V wi) { return same(wo, wi) ? fabsf(wi.z) * k1Pi : 0; }  // BxDF.cuh:192-194
+static inline bool same_h(V a, V b, uint64_t* sig) {  // sameHemisphere, recorded
+    const bool v = same(a, b);
+    if (sig) fnv(*sig, 0x700000000ull + (v ? 1u : 0u));
+    return v;
+}
+static float default_pdf(V wo, V wi, uint64_t* sig) { return same_h(wo, wi, sig) ? fabsf(wi.z) * k1Pi : 0; }  // BxDF.cuh:192-194
 
 static S lobe_f(const Bsdf& f, V wo, V wi) {
     switch (f.lobe) {
@@ -715,27 +720,28 @@ static S lobe_f(const Bsdf& f, V wo, V wi) {
         default: return sp(0.0f);
     }
 }
-static float lobe_pdf(const Bsdf& f, V wo, V wi) {
+static float lobe_pdf(const Bsdf& f, V wo, V wi, uint64_t* sig) {
     switch (f.lobe) {
         case LAMBERT:
-        case OREN: return default_pdf(wo, wi);
+        case OREN: return default_pdf(wo, wi, sig);
         case MICRO: {
-            if (!same(wo, wi)) return 0;
+            if (!same_h(wo, wi, sig)) return 0;
             const V wh = normalize(wo + wi);
             return tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha) * absdot(wo, wh) / fabsf(wo.z) / (4 * dot(wo, wh));
         }
         default: return 0.0f;
     }
 }
-static S bsdf_f(const Bsdf& f, V woW, V wiW, uint32_t flags) {  // BSDF.cuh:192-204
+static S bsdf_f(const Bsdf& f, V woW, V wiW, uint32_t flags, uint64_t* sig) {  // BSDF.cuh:192-204
     S r = sp(0.0f);
-    if (f.lobe == NONE) return r;
     const V wi = to_local(f, wiW), wo = to_local(f, woW);
     const bool reflect = dot(wiW, f.ng) * dot(woW, f.ng) > 0;
+    if (sig) fnv(*sig, 0x600000000ull + (reflect ? 1u : 0u));
+    if (f.lobe == NONE) return r;
     if (match(f.type, flags) && ((reflect && (f.type & REFL)) || (!reflect && (f.type & TRANS)))) r = r + lobe_f(f, wo, wi);
     return r;
 }
-static float bsdf_pdf(const Bsdf& f, V woW, V wiW, uint32_t flags) {  // BSDF.cuh:261-276
+static float bsdf_pdf(const Bsdf& f, V woW, V wiW, uint32_t flags, uint64_t* sig) {  // BSDF.cuh:261-276
     if (f.lobe == NONE) return 0.0f;
     const V wo = to_local(f, woW), wi = to_local(f, wiW);
     if (wo.z == 0) return 0.0f;
@@ -743,11 +749,12 @@ static float bsdf_pdf(const Bsdf& f, V woW, V wiW, uint32_t flags) {  // BSDF.cu
     int m = 0;
     if (match(f.type, flags)) {
         ++m;
-        pdf = pdf + lobe_pdf(f, wo, wi);
+        pdf = pdf + lobe_pdf(f, wo, wi, sig);
     }
     return m > 0 ? pdf / m : 0.0f;
 }
-static S bsdf_sample(const Bsdf& f, V woW, V* wiW, P2 u, float* pdf, uint32_t flags, uint32_t* stype) {
+static S bsdf_sample(const Bsdf& f, V woW, V* wiW, P2 u, float* pdf, uint32_t flags, uint32_t* stype,
+                     uint64_t* sig) {
     if (f.lobe == NONE || !match(f.type, flags)) {  // matchingComps == 0
         *pdf = 0;
         return sp(0.0f);
@@ -767,7 +774,7 @@ static S bsdf_sample(const Bsdf& f, V woW, V* wiW, P2 u, float* pdf, uint32_t fl
             const float dx = r * cosf(th), dy = r * sinf(th);
             wi = mk(dx, dy, sqrtf(fmaxf(0.0f, 1 - dx * dx - dy * dy)));
             if (wo.z < 0) wi.z *= -1;
-            *pdf = default_pdf(wo, wi);
+            *pdf = default_pdf(wo, wi, sig);
             val = lobe_f(f, wo, wi);
             break;
         }
@@ -803,7 +810,7 @@ static S bsdf_sample(const Bsdf& f, V woW, V* wiW, P2 u, float* pdf, uint32_t fl
             if (flip) wh = -wh;
             if (dot(wo, wh) < 0) return sp(0.0f);
             wi = -wo + wh * (2 * dot(wo, wh));
-            if (!same(wo, wi)) return sp(0.0f);
+            if (!same_h(wo, wi, sig)) return sp(0.0f);
             *pdf = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha) * absdot(wo, wh) / fabsf(wo.z) / (4 * dot(wo, wh));
             val = lobe_f(f, wo, wi);
             break;
@@ -946,8 +953,26 @@ static void fnv(uint64_t& h, uint64_t v) {
     }
 }
 
+// Parity debugging: the intermediate values of one crop sample (LTS_PORT_TRACE=k), as 16-float
+// records with the renderer's tags (1 hit, 2 material, 3 light sample, 4 MIS, 5 BSDF sample, 6 L).
+static long g_trace_k = -1;
+static std::vector<float> g_trace;
+struct Tr {
+    bool on = false;
+    void put(float tag, std::initializer_list<float> v) {
+        if (!on || g_trace.size() >= 64 * 16) return;
+        float r[16] = {0};
+        r[0] = tag;
+        int i = 1;
+        for (float x : v)
+            if (i < 16) r[i++] = x;
+        g_trace.insert(g_trace.end(), r, r + 16);
+    }
+};
+
 // PathTracingIntegrator::evaluate (PathTracingIntegrator.cuh:26-109) for one pixel.
-static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* outL, uint64_t* outsig, Film* film) {
+static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* outL, uint64_t* outsig, Film* film,
+                     long crop_index) {
     const HostScene& h = *sc.h;
     const float* cm = h.cam;
     const V o = mk(cm[0], cm[1], cm[2]), right = mk(cm[3], cm[4], cm[5]), up = mk(cm[6], cm[7], cm[8]),
@@ -959,6 +984,8 @@ static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* out
         rng.sample = (uint32_t)s;
         rng.draw = 0;
         uint64_t sig = 0xcbf29ce484222325ull;
+        Tr tr;
+        tr.on = g_trace_k >= 0 && crop_index * pr.spp + s == g_trace_k;
         const P2 fs = r2(rng);
         (void)r2(rng);  // lens sample (aperture 0)
         const float pfx = (float)(i + fs.x), pfy = (float)(j + fs.y);
@@ -977,6 +1004,8 @@ static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* out
             float tmax = INFINITY;
             const bool hit = bvh_trace(sc, ro, rd, tmax, &si, false);
             fnv(sig, 0x100000000ull + (uint64_t)((hit ? si.prim : -1) + 1));
+            tr.put(1, {(float)hit, (float)(hit ? si.prim : -1), si.p.x, si.p.y, si.p.z, si.n.x, si.n.y, si.n.z, si.sn.x,
+                       si.sn.y, si.sn.z, beta.r, beta.g, beta.b, L.r});
             if (bounce == 0 || specular) {
                 if (hit) {
                     const int li = h.prim_light[si.prim];
@@ -1002,6 +1031,8 @@ static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* out
             }
             Bsdf f;
             if (!make_bsdf(sc, si, &f, &sig)) break;
+            tr.put(2, {(float)f.lobe, f.R.r, f.R.g, f.R.b, f.ss.x, f.ss.y, f.ss.z, f.ts.x, f.ts.y, f.ts.z, si.dpdx.x,
+                       si.dpdx.y, si.dpdx.z});
             if (nl > 0) {  // uniformSampleOneLight + estimateDirect (IntegratorHelper.cuh:51-149)
                 const float ul = r1(rng);
                 int off = 0;
@@ -1027,14 +1058,16 @@ static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* out
                 LSample ls;
                 sample_li(sc, Lt, si, ulight, &ls);
                 if (ls.pdf > 0 && !black(ls.Li)) {
-                    const S fv = bsdf_f(f, si.wo, ls.wi, flags) * absdot(ls.wi, si.sn);
-                    const float spdf = bsdf_pdf(f, si.wo, ls.wi, flags);
+                    const S fv = bsdf_f(f, si.wo, ls.wi, flags, &sig) * absdot(ls.wi, si.sn);
+                    const float spdf = bsdf_pdf(f, si.wo, ls.wi, flags, &sig);
                     if (!black(fv)) {
                         const V org = offset_origin(si.p, si.perr, si.n, ls.p1 - si.p);
                         const V tgt = offset_origin(ls.p1, ls.perr1, ls.n1, org - ls.p1);
                         float tm = 1 - kShadowEps;
                         const bool occ = bvh_trace(sc, org, tgt - org, tm, nullptr, true);
                         fnv(sig, 0x300000000ull + (occ ? 0u : 1u));
+                        tr.put(3, {(float)off, lpdf, ls.pdf, ls.Li.r, ls.wi.x, ls.wi.y, ls.wi.z, fv.r, fv.g, fv.b, spdf,
+                                   (float)occ});
                         S Li = ls.Li;
                         if (occ) Li = sp(0.0f);
                         if (!black(Li)) {
@@ -1052,7 +1085,7 @@ static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* out
                     V wi = ls.wi;
                     float spdf = 0;
                     uint32_t st = 0;
-                    S fv = bsdf_sample(f, si.wo, &wi, uscat, &spdf, flags, &st);
+                    S fv = bsdf_sample(f, si.wo, &wi, uscat, &spdf, flags, &st, &sig);
                     fv = fv * absdot(wi, si.sn);
                     const bool sspec = (st & SPEC) != 0;
                     if (!black(fv) && spdf > 0) {
@@ -1082,6 +1115,7 @@ static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* out
                                 Li = Lt.kind == lts::LIGHT_INFINITE ? S{Lt.L[0], Lt.L[1], Lt.L[2]} : sp(0.0f);
                             }
                             if (!black(Li)) Ld = Ld + fv * Li * sp(1.0f) * w / spdf;
+                            tr.put(4, {spdf, fv.r, fv.g, fv.b, w, (float)found, Li.r, Ld.r, Ld.g, Ld.b, wi.x, wi.y, wi.z});
                         }
                     }
                 }
@@ -1091,10 +1125,11 @@ static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* out
             float pdf = 0;
             uint32_t st = 0;
             const P2 ub = r2(rng);
-            const S fv = bsdf_sample(f, si.wo, &wi, ub, &pdf, ALL, &st);
+            const S fv = bsdf_sample(f, si.wo, &wi, ub, &pdf, ALL, &st, &sig);
             if (black(fv) || pdf == 0) break;
             specular = (st & SPEC) != 0;
             beta = beta * (fv * absdot(wi, si.sn) / pdf);
+            tr.put(5, {wi.x, wi.y, wi.z, pdf, fv.r, fv.g, fv.b, beta.r, beta.g, beta.b, L.r, L.g, L.b});
             ro = offset_origin(si.p, si.perr, si.n, wi);
             rd = wi;
             diff = false;
@@ -1104,6 +1139,7 @@ static void evaluate(const Scene& sc, const Params& pr, int i, int j, float* out
                 beta = beta / (1 - q);
             }
         }
+        tr.put(6, {L.r, L.g, L.b});
         outL[3 * s + 0] = L.r;
         outL[3 * s + 1] = L.g;
         outL[3 * s + 2] = L.b;
@@ -1221,6 +1257,7 @@ int main(int argc, char** argv) {
         if (load(argv[2], argv[3], argv[4], pr.W, pr.H, &hs)) return 1;
         Scene sc = make_scene(&hs, mode);
         if (threads > 0) omp_set_num_threads(threads);
+        if (const char* t = getenv("LTS_PORT_TRACE")) g_trace_k = atol(t);
         const int cw = x1 - x0, ch = y1 - y0;
         std::vector<float> L((size_t)cw * ch * pr.spp * 3);
         std::vector<uint64_t> sig((size_t)cw * ch * pr.spp);
@@ -1233,11 +1270,11 @@ int main(int argc, char** argv) {
         auto t0 = std::chrono::steady_clock::now();
         if (want_film) {  // the film accumulation is sequential, in pixel order
             for (long p = 0; p < np; ++p)
-                evaluate(sc, pr, x0 + (int)(p % cw), y0 + (int)(p / cw), &L[3 * p * pr.spp], &sig[p * pr.spp], &film);
+                evaluate(sc, pr, x0 + (int)(p % cw), y0 + (int)(p / cw), &L[3 * p * pr.spp], &sig[p * pr.spp], &film, p);
         } else {
 #pragma omp parallel for schedule(dynamic, 16)
             for (long p = 0; p < np; ++p)
-                evaluate(sc, pr, x0 + (int)(p % cw), y0 + (int)(p / cw), &L[3 * p * pr.spp], &sig[p * pr.spp], nullptr);
+                evaluate(sc, pr, x0 + (int)(p % cw), y0 + (int)(p / cw), &L[3 * p * pr.spp], &sig[p * pr.spp], nullptr, p);
         }
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         const int32_t nth = want_film ? 1 : omp_get_max_threads();
@@ -1246,6 +1283,7 @@ int main(int argc, char** argv) {
         wr.put("sig", 'q', sig.data(), sig.size(), 8);
         wr.put("time_s", 'd', &secs, 1, 8);
         wr.put("threads", 'i', &nth, 1, 4);
+        if (g_trace_k >= 0) wr.put("trace", 'f', g_trace.data(), g_trace.size(), 4);
         if (want_film) {  // Camera::getRender (Camera.cu:256-289)
             std::vector<float> rgb((size_t)pr.W * pr.H * 3);
             for (int jj = 0; jj < pr.H; ++jj)

@@ -13,7 +13,7 @@
  *       PathTracingIntegrator::evaluate (PathTracingIntegrator.cuh:26-109) over the pixel
  *       crop [X0,X1)x[Y0,Y1) -> per-(pixel, sample) radiance L and a 64-bit FNV-1a hash of the
  *       sample's events (extension hit primitive per bounce, shadow-ray visibility, MIS-ray
- *       hit primitive, texture branch decisions), the render wall time, and (FILM=1) the resolved film of
+ *       hit primitive, texture branch decisions, BSDF grazing tests), the render wall time, and (FILM=1) the resolved film of
  *       Camera::getRender (Camera.cu:256-289).
  *
  * Build: oracle/ref/build_ref.sh (g++ -E | instrument.pl | g++).  Output: oracle/_ref/lts_ref.
@@ -93,6 +93,10 @@ void lts_hook_begin_sample(int id, int s) {
 }
 void lts_hook_hit(const void* prim) { fnv_mix(0x100000000ull + (uint64_t)(prim_index(prim) + 1)); }
 void lts_hook_branch(unsigned long long v) { fnv_mix(v); }
+bool lts_hook_bool(unsigned long long tag, bool v) {
+    fnv_mix(tag + (v ? 1u : 0u));
+    return v;
+}
 void lts_hook_mis(const void* prim) { fnv_mix(0x200000000ull + (uint64_t)(prim_index(prim) + 1)); }
 bool lts_hook_vis(bool unoccluded) {
     fnv_mix(0x300000000ull + (unoccluded ? 1u : 0u));

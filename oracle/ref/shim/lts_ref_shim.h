@@ -224,3 +224,4 @@ void lts_hook_mis(const void* prim);
 bool lts_hook_vis(bool unoccluded);
 void lts_hook_sample(int id, int s, float r, float g, float b);
 void lts_hook_branch(unsigned long long v);
+bool lts_hook_bool(unsigned long long tag, bool v);
