@@ -224,7 +224,7 @@ def run_gpu(args, wl):
     d, sc, sub = scene_dir(wl)
     ctx = lts.Context(local)
     scene = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
-    integ = lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], scene)
+    integ = lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], scene, integrator=args.integrator)
     desc = integ.desc(wl["spp"], wl["seed"])
     stream = torch.cuda.ExternalStream(ctx.stream())
     paths = wl["width"] * wl["height"] * wl["spp"]
@@ -248,6 +248,8 @@ def run_gpu(args, wl):
         e1.record(stream)
         e1.synchronize()
     ctx.check(ctx.lib.lts_film_get(ctx.h, None, None))
+    mt = ctx.metrics()
+    launches_step, iters_step = mt.render_launches, mt.render_iterations
     ms = e0.elapsed_time(e1) / args.steps
     ms = barrier_max(dist, ms)
     value = world * paths / (ms * 1e-3) / 1e6
@@ -265,7 +267,8 @@ def run_gpu(args, wl):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         s2 = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
-        lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], s2).render(wl["spp"], wl["seed"])
+        lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], s2, integrator=args.integrator).render(
+            wl["spp"], wl["seed"])
         t_e2e.append(time.perf_counter() - t0)
     e2e_s = barrier_max(dist, statistics.median(t_e2e))
     e2e = world * paths / e2e_s / 1e6
@@ -274,7 +277,6 @@ def run_gpu(args, wl):
     if rank == 0 and not args.skip_lbvh:
         lbvh = [lbvh_bench(ctx, n, 5, 3, lts.BVH_SORTED, peaks) for n in (1_000_000, 16_000_000)]
     cpu = cpu_port_sample(wl) if (rank == 0 and world == 1 and not args.skip_cpu) else None
-    m = ctx.metrics()
     if rank == 0:
         line = {
             "metric": "Mpaths/s", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
@@ -282,7 +284,8 @@ def run_gpu(args, wl):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": wl["name"], "width": wl["width"], "height": wl["height"], "spp": wl["spp"],
                        "max_bounce": wl["max_bounce"], "rr_start": wl["rr_start"], "seed": wl["seed"],
-                       "triangles": scene.info["triangles"], "integrator": "megakernel", "bvh": "sorted-leaf LBVH",
+                       "triangles": scene.info["triangles"],
+                       "integrator": ["megakernel", "wavefront"][args.integrator], "bvh": "sorted-leaf LBVH",
                        "l2": "inputs (BVH + triangles) exceed L2; no flush", "parallelism": f"replicas x{world}"},
             "mrays_per_s": round(r["rays"] / (r["render_ms"] * 1e-3) / 1e6, 2),
             "e2e": {"value": round(e2e, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -295,8 +298,9 @@ def run_gpu(args, wl):
             "lbvh": lbvh,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            "gpu_launches": int(args.steps),
-            "kernel_launches_per_step": m.kernel_launches,
+            "gpu_launches": int(args.steps) * launches_step,
+            "kernel_launches_per_step": launches_step,
+            "wavefront_iterations_per_step": iters_step,
         }
         print(json.dumps(line))
     ctx.close()
@@ -313,6 +317,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="256x256x16 spp level-6 sphere (quick check)")
     ap.add_argument("--skip-lbvh", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--integrator", type=int, default=1, choices=[0, 1], help="0 megakernel, 1 wavefront")
     ap.add_argument("--lbvh-only", type=int, default=0, metavar="N",
                     help="only time the LBVH build over N random triangles (seed 1)")
     args = ap.parse_args()

@@ -189,6 +189,8 @@ typedef struct {
     double paths, rays;
     int64_t device_bytes; /* bytes currently allocated by the context */
     int32_t kernel_launches; /* kernels launched by the last build + render */
+    int32_t render_launches; /* kernels launched by the last render alone */
+    int32_t render_iterations; /* wavefront: stage-loop iterations of the last render (1 for the megakernel) */
 } lts_metrics;
 int lts_get_metrics(lts_ctx* ctx, lts_metrics* out);
 

@@ -77,7 +77,8 @@ class RenderOut(ctypes.Structure):
 class Metrics(ctypes.Structure):
     _fields_ = [("bvh_build_ms", ctypes.c_double), ("bvh_stage_ms", ctypes.c_double * 5),
                 ("render_ms", ctypes.c_double), ("paths", ctypes.c_double), ("rays", ctypes.c_double),
-                ("device_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int32)]
+                ("device_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int32),
+                ("render_launches", ctypes.c_int32), ("render_iterations", ctypes.c_int32)]
 
 
 _lib = None

@@ -446,6 +446,8 @@ int lts_get_metrics(lts_ctx* ctx, lts_metrics* out) {
     *out = ctx->metrics;
     out->device_bytes = (int64_t)dev_bytes_in_use();
     out->kernel_launches = (ctx->bvh ? ctx->bvh->launches : 0) + (ctx->tracer ? ctx->tracer->last_launches : 0);
+    out->render_launches = ctx->tracer ? ctx->tracer->last_launches : 0;
+    out->render_iterations = ctx->tracer ? ctx->tracer->last_iterations : 0;
     return LTS_OK;
 }
 

@@ -25,911 +25,10 @@
 #include "dev_common.cuh"
 #include "dev_math.cuh"
 #include "tracer.cuh"
+#include "tracer_dev.cuh"
 
 namespace lts {
 namespace {
-
-// Float forms of the reference's double-precision comparisons:
-//   u > 1.0 - SHADOW_EPSILON  <=>  u >= kOneMinusEpsUp   (Triangle.cu:116,122)
-//   u > 1.0 + SHADOW_EPSILON  <=>  u >= kOnePlusEpsUp    (Triangle.cu:72,78)
-//   x > 1e-4                  <=>  x >= 0.0001f          (models/Microfacet.cuh:32)
-//   cosT > .9999              <=>  cosT >= kOneMinusEpsUp (models/Microfacet.cuh:56)
-#define kShadowEps 0.0001f
-#define kOneMinusEpsUp __int_as_float(0x3f7ff973)
-#define kOnePlusEpsUp __int_as_float(0x3f800347)
-#define kSlabScale (1.0f + 2.0f * gamma_n(3))
-
-constexpr int kStack = 40;
-constexpr int kBX = 16, kBY = 8, kThreads = kBX * kBY;
-
-enum BxdfType : uint32_t {
-    BSDF_REFLECTION = 1u,
-    BSDF_TRANSMISSION = 2u,
-    BSDF_DIFFUSE = 4u,
-    BSDF_GLOSSY = 8u,
-    BSDF_SPECULAR = 16u,
-    BSDF_ALL = 31u
-};
-enum LobeKind : int { LOBE_NONE = 0, LOBE_LAMBERT, LOBE_OREN_NAYAR, LOBE_FRESNEL_SPECULAR, LOBE_SPECULAR_REFL, LOBE_MICROFACET };
-
-// ------------------------------------------------------------------ sampler (project Philox)
-struct Rng {
-    uint32_t key, sample, draw;
-    uint32_t w0, w1, w2, w3;
-};
-__device__ __forceinline__ void philox_block(Rng& r) {
-    uint32_t c0 = r.draw >> 2, c1 = r.sample, c2 = 0u, c3 = 0u, k0 = r.key, k1 = 0x4c54530au;
-#pragma unroll
-    for (int i = 0; i < 10; ++i) {
-        const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-        c0 = hi1 ^ c1 ^ k0;
-        c1 = lo1;
-        c2 = hi0 ^ c3 ^ k1;
-        c3 = lo0;
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
-    }
-    r.w0 = c0;
-    r.w1 = c1;
-    r.w2 = c2;
-    r.w3 = c3;
-}
-__device__ __forceinline__ uint32_t wang_hash(uint32_t a) {
-    a = (a ^ 61u) ^ (a >> 16);
-    a = a + (a << 3);
-    a = a ^ (a >> 4);
-    a = a * 0x27d4eb2du;
-    a = a ^ (a >> 15);
-    return a;
-}
-__device__ __forceinline__ float rng_1d(Rng& r) {
-    if ((r.draw & 3u) == 0u) philox_block(r);
-    const uint32_t x = r.w0;
-    r.w0 = r.w1;
-    r.w1 = r.w2;
-    r.w2 = r.w3;
-    ++r.draw;
-    return (float)((x >> 8) + 1u) * (1.0f / 16777216.0f);
-}
-struct F2 {
-    float x, y;
-};
-// Sampler::uniformSample (Sampler.cuh:70-73) as the reference's host build evaluates it:
-// the constructor arguments are evaluated right to left, so x receives the second draw.
-__device__ __forceinline__ F2 rng_2d(Rng& r) {
-    const float a = rng_1d(r);
-    const float b = rng_1d(r);
-    return F2{b, a};
-}
-
-// ------------------------------------------------------------------ event hash (record mode)
-__device__ __forceinline__ void fnv_mix(uint64_t& h, uint64_t v) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        h ^= (v >> (8 * i)) & 0xffull;
-        h *= 0x100000001b3ull;
-    }
-}
-
-// ------------------------------------------------------------------ single-sample trace (record mode)
-struct Tracer16 {
-    float* out;
-    int n;
-    __device__ void put(float tag, float a = 0, float b = 0, float c = 0, float d = 0, float e = 0, float f = 0,
-                        float g = 0, float h = 0, float i = 0, float j = 0, float k = 0, float l = 0, float m = 0,
-                        float o = 0, float p = 0) {
-        if (!out || n >= 64) return;
-        float* r = out + 16 * n++;
-        r[0] = tag; r[1] = a; r[2] = b; r[3] = c; r[4] = d; r[5] = e; r[6] = f; r[7] = g; r[8] = h;
-        r[9] = i; r[10] = j; r[11] = k; r[12] = l; r[13] = m; r[14] = o; r[15] = p;
-    }
-};
-
-// ------------------------------------------------------------------ geometry fetch
-__device__ __forceinline__ V3 f4v(float4 a) { return v3(a.x, a.y, a.z); }
-__device__ __forceinline__ void prim_tri(const SceneView& sv, int prim, V3& p0, V3& p1, V3& p2) {
-    p0 = f4v(__ldg(sv.prim_v + 3 * prim));
-    p1 = f4v(__ldg(sv.prim_v + 3 * prim + 1));
-    p2 = f4v(__ldg(sv.prim_v + 3 * prim + 2));
-}
-__device__ __forceinline__ V3 normal_at(const SceneView& sv, int idx) {
-    return v3(__ldg(sv.normals + 3 * idx), __ldg(sv.normals + 3 * idx + 1), __ldg(sv.normals + 3 * idx + 2));
-}
-
-// ------------------------------------------------------------------ triangle tests
-// Triangle::intersect test part (shapes/Triangle.cu:94-128).
-__device__ __forceinline__ bool tri_test(V3 p0, V3 p1, V3 p2, V3 o, V3 d, float tmax, float& t_out, float& u_out,
-                                         float& v_out, float& inv_out) {
-    const V3 e1 = p1 - p0, e2 = p2 - p0;
-    const V3 pv = cross(d, e2);
-    const float det = dot(e1, pv);
-    if (det == 0) return false;
-    const float inv = __frcp_rn(det);  // == (float)(1.0 / (double)det)
-    const V3 tv = o - p0;
-    const float u = inv * dot(tv, pv);
-    if (u < kShadowEps || u >= kOneMinusEpsUp) return false;
-    const V3 qv = cross(tv, e1);
-    const float v = inv * dot(d, qv);
-    if (v < kShadowEps || u + v >= kOneMinusEpsUp) return false;
-    const float t = inv * dot(e2, qv);
-    if (!(t > 0 && t < tmax)) return false;
-    t_out = t;
-    u_out = u;
-    v_out = v;
-    inv_out = inv;
-    return true;
-}
-// Triangle::simpleIntersect (shapes/Triangle.cu:50-84): swapped edges, grown bound.
-__device__ __forceinline__ bool tri_test_shadow(V3 p0, V3 p1, V3 p2, V3 o, V3 d, float tmax) {
-    const V3 e1 = p1 - p0, e2 = p2 - p0;
-    const V3 pv = cross(d, e1);
-    const float det = dot(e2, pv);
-    if (det == 0) return false;
-    const float inv = __frcp_rn(det);
-    const V3 tv = o - p0;
-    const float u = inv * dot(tv, pv);
-    if (u < kShadowEps || u >= kOnePlusEpsUp) return false;
-    const V3 qv = cross(tv, e2);
-    const float v = inv * dot(d, qv);
-    if (v < kShadowEps || u + v >= kOnePlusEpsUp) return false;
-    const float t = inv * dot(e1, qv);
-    return t > 0 && t < tmax;
-}
-
-// ------------------------------------------------------------------ surface interaction
-struct SI {
-    V3 p, perr, wo, n;  // Interaction
-    V3 dpdu, dpdv;      // geometric partials
-    V3 sn, sdpdu;       // shading normal and tangent
-    V3 dpdx, dpdy;      // computeDifferentials
-    int prim;
-};
-
-__device__ __forceinline__ void coordinate_system(V3 v1, V3& v2, V3& v3o) {
-    // Geometry.cuh:250-258
-    if (fabsf(v1.x) > fabsf(v1.y))
-        v2 = v3(-v1.z, 0, v1.x) * rsqrt_q3(v1.x * v1.x + v1.z * v1.z);
-    else
-        v2 = v3(0, v1.z, -v1.y) * rsqrt_q3(v1.y * v1.y + v1.z * v1.z);
-    v3o = cross(v1, v2);
-}
-
-// Builds the SurfaceInteraction of a hit (Triangle.cu:128-199 and the SurfaceInteraction
-// constructor, geometry/Interaction.cuh:85-116).
-__device__ void make_si(const SceneView& sv, int prim, V3 p0, V3 p1, V3 p2, V3 d, float u, float v, float inv,
-                        SI& si) {
-    const float w = 1 - u - v;
-    const V3 e1 = p1 - p0, e2 = p2 - p0;
-    const int4 uvi = __ldg(sv.prim_uv + prim);
-    float uv0x = 0, uv0y = 0, uv1x = 1, uv1y = 0, uv2x = 1, uv2y = 1;
-    if (uvi.x >= 0) {
-        uv0x = __ldg(sv.uvs + 2 * uvi.x); uv0y = __ldg(sv.uvs + 2 * uvi.x + 1);
-        uv1x = __ldg(sv.uvs + 2 * uvi.y); uv1y = __ldg(sv.uvs + 2 * uvi.y + 1);
-        uv2x = __ldg(sv.uvs + 2 * uvi.z); uv2y = __ldg(sv.uvs + 2 * uvi.z + 1);
-    }
-    const float d02x = uv0x - uv2x, d02y = uv0y - uv2y, d12x = uv1x - uv2x, d12y = uv1y - uv2y;
-    const V3 dp02 = p0 - p2, dp12 = p1 - p2;
-    const float determinant = d02x * d12y - d02y * d12x;
-    V3 dpdu, dpdv;
-    if (determinant == 0) {
-        coordinate_system(normalize(cross(e2, e1)), dpdu, dpdv);
-    } else {
-        // the reference scales by the ray's invDet, not the uv determinant (Triangle.cu:148-149)
-        dpdu = (dp02 * d12y - dp12 * d02y) * inv;
-        dpdv = (dp02 * -d12x + dp12 * d02x) * inv;
-    }
-    const float xs = fabsf(w * p0.x) + fabsf(u * p1.x) + fabsf(v * p2.x);
-    const float ys = fabsf(w * p0.y) + fabsf(u * p1.y) + fabsf(v * p2.y);
-    const float zs = fabsf(w * p0.z) + fabsf(u * p1.z) + fabsf(v * p2.z);
-    si.perr = v3(xs, ys, zs) * gamma_n(7);
-    si.p = p0 * w + p1 * u + p2 * v;
-    si.wo = -d;
-    si.dpdu = dpdu;
-    si.dpdv = dpdv;
-    si.n = normalize(cross(dpdu, dpdv));
-    si.sn = si.n;
-    si.sdpdu = dpdu;
-    si.prim = prim;
-    const int4 ni = __ldg(sv.prim_n + prim);
-    if (ni.x >= 0) {
-        const V3 n0 = normal_at(sv, ni.x), n1 = normal_at(sv, ni.y), n2 = normal_at(sv, ni.z);
-        const V3 ns = normalize(n0 * w + n1 * u + n2 * v);
-        V3 ss = si.dpdu;
-        V3 ts = cross(ns, ss);
-        if (len2(ts) > 0.0f) {
-            ts = normalize(ts);
-            ss = cross(ts, ns);
-        } else {
-            coordinate_system(ns, ss, ts);
-        }
-        si.sn = normalize(cross(ss, ts));         // setShaddingGeometry
-        si.n = face_towards(si.n, si.sn);
-        si.sdpdu = ss;
-        si.n = face_towards(si.n, si.sn);         // Triangle.cu:196
-    }
-}
-
-// ------------------------------------------------------------------ BVH traversal
-struct TraceRay {
-    V3 o, d, inv;
-    int neg[3];
-};
-__device__ __forceinline__ TraceRay make_trace_ray(V3 o, V3 d) {
-    TraceRay r;
-    r.o = o;
-    r.d = d;
-    r.inv = v3(__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z));
-    r.neg[0] = r.inv.x < 0;
-    r.neg[1] = r.inv.y < 0;
-    r.neg[2] = r.inv.z < 0;
-    return r;
-}
-// Bounds3::simpleIntersect (geometry/Bound.cuh:199-227), returning the entry distance.
-__device__ __forceinline__ bool slab(const TraceRay& r, float tmax_ray, float mnx, float mny, float mnz, float mxx,
-                                     float mxy, float mxz, float& tentry) {
-    float tMin = ((r.neg[0] ? mxx : mnx) - r.o.x) * r.inv.x;
-    float tMax = ((r.neg[0] ? mnx : mxx) - r.o.x) * r.inv.x;
-    const float tyMin = ((r.neg[1] ? mxy : mny) - r.o.y) * r.inv.y;
-    float tyMax = ((r.neg[1] ? mny : mxy) - r.o.y) * r.inv.y;
-    tMax *= kSlabScale;
-    tyMax *= kSlabScale;
-    if (tMin > tyMax || tyMin > tMax) return false;
-    if (tyMin > tMin) tMin = tyMin;
-    if (tyMax < tMax) tMax = tyMax;
-    const float tzMin = ((r.neg[2] ? mxz : mnz) - r.o.z) * r.inv.z;
-    float tzMax = ((r.neg[2] ? mnz : mxz) - r.o.z) * r.inv.z;
-    tzMax *= kSlabScale;
-    if (tMin > tzMax || tzMin > tMax) return false;
-    if (tzMin > tMin) tMin = tzMin;
-    if (tzMax < tMax) tMax = tzMax;
-    tentry = tMin;
-    return (tMin < tmax_ray) && (tMax > 0);
-}
-
-template <bool ANY>
-__device__ __forceinline__ bool leaf_test(const SceneView& sv, int leaf, const TraceRay& r, float& tmax, int& best,
-                                          float& bu, float& bv, float& binv) {
-    const float4 a = __ldg(sv.leaf_v + 3 * leaf), b = __ldg(sv.leaf_v + 3 * leaf + 1), c = __ldg(sv.leaf_v + 3 * leaf + 2);
-    if (ANY) return tri_test_shadow(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax);
-    float t, u, v, inv;
-    if (tri_test(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax, t, u, v, inv)) {
-        tmax = t;
-        best = __float_as_int(a.w);
-        bu = u;
-        bv = v;
-        binv = inv;
-    }
-    return false;
-}
-
-// BVH::intersect / simpleIntersect (acceleration/BVH.cuh:331-398).  Returns the hit primitive
-// (closest) or 1/-1 (any), -1 for a miss.  `stack` is this thread's column of the shared stack.
-struct Work {
-    uint32_t nodes, tris;
-};
-
-template <bool ANY>
-__device__ int traverse(const SceneView& sv, int nleaf, const TraceRay& r, float& tmax, float& bu, float& bv,
-                        float& binv, uint32_t* stack, uint32_t* err, Work& wk) {
-    int best = -1;
-    float te;
-    const float* rb = sv.root_bounds;
-    if (!slab(r, tmax, __ldg(rb), __ldg(rb + 1), __ldg(rb + 2), __ldg(rb + 3), __ldg(rb + 4), __ldg(rb + 5), te))
-        return -1;
-    if (nleaf == 1) {
-        ++wk.tris;
-        if (leaf_test<ANY>(sv, 0, r, tmax, best, bu, bv, binv)) return 1;
-        return ANY ? -1 : best;
-    }
-    int node = 0, sp = 0;
-    for (;;) {
-        const BvhNode* nd = sv.nodes + node;
-        const float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
-        const int4 lr = __ldg(&nd->d);
-        ++wk.nodes;
-        float tl, tr;
-        bool hl = slab(r, tmax, a.x, a.y, a.z, a.w, b.x, b.y, tl);
-        bool hr = slab(r, tmax, b.z, b.w, c.x, c.y, c.z, c.w, tr);
-        if (hl && lr.x < 0) {
-            ++wk.tris;
-            if (leaf_test<ANY>(sv, ~lr.x, r, tmax, best, bu, bv, binv)) return 1;
-            hl = false;
-        }
-        if (hr && lr.y < 0) {
-            ++wk.tris;
-            if (leaf_test<ANY>(sv, ~lr.y, r, tmax, best, bu, bv, binv)) return 1;
-            hr = false;
-        }
-        if (hl && hr) {
-            const bool left_first = tl <= tr;
-            if (sp >= kStack) {
-                atomicOr(err, DEV_ERR_STACK_OVERFLOW);
-                return ANY ? -1 : best;
-            }
-            stack[(sp++) * kThreads] = left_first ? lr.y : lr.x;
-            node = left_first ? lr.x : lr.y;
-        } else if (hl) {
-            node = lr.x;
-        } else if (hr) {
-            node = lr.y;
-        } else {
-            if (sp == 0) break;
-            node = stack[(--sp) * kThreads];
-        }
-    }
-    return ANY ? -1 : best;
-}
-
-struct Hit {
-    bool found;
-    SI si;
-};
-
-__device__ __forceinline__ bool scene_intersect(const SceneView& sv, int nleaf, V3 o, V3 d, float tmax, SI& si,
-                                                uint32_t* stack, uint32_t* err, Work& wk) {
-    const TraceRay r = make_trace_ray(o, d);
-    float bu = 0, bv = 0, binv = 0;
-    const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk);
-    if (prim < 0) return false;
-    V3 p0, p1, p2;
-    prim_tri(sv, prim, p0, p1, p2);
-    make_si(sv, prim, p0, p1, p2, d, bu, bv, binv, si);
-    return true;
-}
-__device__ __forceinline__ bool scene_occluded(const SceneView& sv, int nleaf, V3 o, V3 d, float tmax, uint32_t* stack,
-                                               uint32_t* err, Work& wk) {
-    const TraceRay r = make_trace_ray(o, d);
-    float bu, bv, binv;
-    return traverse<true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk) > 0;
-}
-
-// ------------------------------------------------------------------ rays from interactions
-// offsetRayOrigin (Geometry.cuh:782-797)
-__device__ __forceinline__ V3 offset_origin(V3 p, V3 perr, V3 n, V3 w) {
-    const float dd = dot(vabs(n), perr);
-    V3 off = n * dd;
-    if (dot(w, n) < 0) off = -off;
-    V3 po = p + off;
-    if (off.x > 0) po.x = next_float_up(po.x); else if (off.x < 0) po.x = next_float_down(po.x);
-    if (off.y > 0) po.y = next_float_up(po.y); else if (off.y < 0) po.y = next_float_down(po.y);
-    if (off.z > 0) po.z = next_float_up(po.z); else if (off.z < 0) po.z = next_float_down(po.z);
-    return po;
-}
-
-// ------------------------------------------------------------------ textures
-__constant__ unsigned char c_perm[512];
-__constant__ float c_marble[10][3];
-
-__device__ __forceinline__ float noise_weight(float t) {
-    const float t3 = t * t * t, t4 = t3 * t;
-    return 6 * t4 * t - 15 * t4 + 10 * t3;
-}
-__device__ __forceinline__ float lerpf(float t, float a, float b) { return (1 - t) * a + t * b; }
-__device__ __forceinline__ float grad(int x, int y, int z, float dx, float dy, float dz) {
-    int h = c_perm[c_perm[c_perm[x] + y] + z];
-    h &= 15;
-    const float u = h < 8 || h == 12 || h == 13 ? dx : dy;
-    const float v = h < 4 || h == 12 || h == 13 ? dy : dz;
-    return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
-}
-// textures/Procedural.cuh:130-155 (improved Perlin noise)
-__device__ float perlin(float x, float y, float z) {
-    int ix = (int)floorf(x), iy = (int)floorf(y), iz = (int)floorf(z);
-    const float dx = x - ix, dy = y - iy, dz = z - iz;
-    ix &= 255;
-    iy &= 255;
-    iz &= 255;
-    const float w000 = grad(ix, iy, iz, dx, dy, dz);
-    const float w100 = grad(ix + 1, iy, iz, dx - 1, dy, dz);
-    const float w010 = grad(ix, iy + 1, iz, dx, dy - 1, dz);
-    const float w001 = grad(ix, iy, iz + 1, dx, dy, dz - 1);
-    const float w110 = grad(ix + 1, iy + 1, iz, dx - 1, dy - 1, dz);
-    const float w011 = grad(ix, iy + 1, iz + 1, dx, dy - 1, dz - 1);
-    const float w101 = grad(ix + 1, iy, iz + 1, dx - 1, dy, dz - 1);
-    const float w111 = grad(ix + 1, iy + 1, iz + 1, dx - 1, dy - 1, dz - 1);
-    const float wx = noise_weight(dx), wy = noise_weight(dy), wz = noise_weight(dz);
-    const float x00 = lerpf(wx, w000, w100), x10 = lerpf(wx, w010, w110);
-    const float x01 = lerpf(wx, w001, w101), x11 = lerpf(wx, w011, w111);
-    const float y0 = lerpf(wy, x00, x10), y1 = lerpf(wy, x01, x11);
-    return lerpf(wz, y0, y1);
-}
-__device__ __forceinline__ float smooth_step(float mn, float mx, float val) {
-    const float v = clampf((val - mn) / (mx - mn), 0, 1);
-    return v * v * (-2 * v + 3);
-}
-__device__ __forceinline__ float octaves_of(V3 dpdx, V3 dpdy, int max_oct) {
-    const float l2 = fmaxf(len2(dpdx), len2(dpdy));
-    return clampf(-1 - 0.5f * log2f(l2), 0, (float)max_oct);
-}
-// Procedural.cuh:161-179
-__device__ float fbm(V3 p, V3 dpdx, V3 dpdy, float omega, int max_oct, uint64_t* sig) {
-    const float n = octaves_of(dpdx, dpdy, max_oct);
-    const int ni = (int)floorf(n);
-    if (sig) fnv_mix(*sig, 0x400000000ull + (unsigned)ni);
-    float sum = 0, lambda = 1, o = 1;
-    for (int i = 0; i < ni; ++i) {
-        sum += o * perlin(p.x * lambda, p.y * lambda, p.z * lambda);
-        lambda *= 1.99f;
-        o *= omega;
-    }
-    const float np = n - ni;
-    sum += o * smooth_step(0.3f, 0.7f, np) * perlin(p.x * lambda, p.y * lambda, p.z * lambda);
-    return sum;
-}
-// Procedural.cuh:181-205
-__device__ float turbulence(V3 p, V3 dpdx, V3 dpdy, float omega, int max_oct, uint64_t* sig) {
-    const float n = octaves_of(dpdx, dpdy, max_oct);
-    const int ni = (int)floorf(n);
-    if (sig) fnv_mix(*sig, 0x400000000ull + (unsigned)ni);
-    float sum = 0, lambda = 1, o = 1;
-    for (int i = 0; i < ni; ++i) {
-        sum += o * fabsf(perlin(p.x * lambda, p.y * lambda, p.z * lambda));
-        lambda *= 1.99f;
-        o *= omega;
-    }
-    const float np = n - ni;
-    sum += o * lerpf(smooth_step(0.3f, 0.7f, np), 0.2f, fabsf(perlin(p.x * lambda, p.y * lambda, p.z * lambda)));
-    for (int i = ni; i < max_oct; ++i) {
-        sum += o * 0.2f;
-        o *= omega;
-    }
-    return sum;
-}
-
-__device__ Spec eval_texture(const DevTex& t, const SI& si, uint64_t* sig) {
-    switch (t.kind) {
-        case 1:  // FBmTexture (Procedural.cuh:207-225)
-            return spec(fbm(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0], sig));
-        case 2:  // WrinkledTexture (Procedural.cuh:227-245)
-            return spec(turbulence(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0], sig));
-        case 3: {  // MarbleTexture (Procedural.cuh:267-311)
-            const float scale = t.v[2], var = t.v[3];
-            const V3 p = si.p * scale;
-            const float marble = p.y + var * fbm(p, si.dpdx * scale, si.dpdy * scale, t.v[1], (int)t.v[0], sig);
-            float tt = 0.5f + 0.5f * sinf(marble);
-            const int first = (int)floorf(tt * 6.0f);
-            if (sig) fnv_mix(*sig, 0x500000000ull + (unsigned)first);
-            tt = (tt * 6.0f - first);
-            Spec c[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) c[k] = Spec{c_marble[first + k][0], c_marble[first + k][1], c_marble[first + k][2]};
-            Spec s0 = c[0] * (1.0f - tt) + c[1] * tt;
-            Spec s1 = c[1] * (1.0f - tt) + c[2] * tt;
-            const Spec s2 = c[2] * (1.0f - tt) + c[3] * tt;
-            s0 = s0 * (1.0f - tt) + s1 * tt;
-            s1 = s1 * (1.0f - tt) + s2 * tt;
-            return (s0 * (1.0f - tt) + s1 * tt) * 1.5f;
-        }
-        case 4: {  // WindyTexture (Procedural.cuh:247-265)
-            const float wind = fbm(si.p * 0.1f, si.dpdx * 0.1f, si.dpdy * 0.1f, 0.5f, 3, sig);
-            const float wave = fbm(si.p, si.dpdx, si.dpdy, 0.5f, 6, sig);
-            return spec(fabsf(wind) * wave);
-        }
-        default:
-            return Spec{t.v[0], t.v[1], t.v[2]};
-    }
-}
-
-// ------------------------------------------------------------------ BxDFs
-__device__ __forceinline__ float cos2t(V3 w) { return w.z * w.z; }
-__device__ __forceinline__ float sin2t(V3 w) { return fmaxf(1 - cos2t(w), 0.0f); }
-__device__ __forceinline__ float sint(V3 w) { return sqrtf(sin2t(w)); }
-__device__ __forceinline__ float tant(V3 w) { return sint(w) / w.z; }
-__device__ __forceinline__ float tan2t(V3 w) { return sin2t(w) / cos2t(w); }
-// cosPhi/sinPhi compare the function sinTheta (not its value) with 0, so they never take the
-// sin == 0 branch (models/BxDF.cuh:144-153).
-__device__ __forceinline__ float cosphi(V3 w) { return clampf(w.x / sint(w), -1, 1); }
-__device__ __forceinline__ float sinphi(V3 w) { return clampf(w.y / sint(w), -1, 1); }
-__device__ __forceinline__ bool same_hemi(V3 a, V3 b, uint64_t* sig) {  // sameHemisphere, recorded
-    const bool v = a.z * b.z > 0;
-    if (sig) fnv_mix(*sig, 0x700000000ull + (v ? 1u : 0u));
-    return v;
-}
-
-// models/BxDF.cuh:16-37 with the swapped clamp bounds of line 17.
-__device__ float fresnel_dielectric(float cos_i, float eta_i, float eta_t) {
-    cos_i = clampf(cos_i, 1, -1);
-    const bool entering = cos_i > 0.0f;
-    if (!entering) {
-        const float tmp = eta_i;
-        eta_i = eta_t;
-        eta_t = tmp;
-        cos_i = fabsf(cos_i);
-    }
-    const float sin_i = sqrtf(fmaxf(0.0f, 1 - cos_i * cos_i));
-    const float sin_t = eta_i / eta_t * sin_i;
-    if (sin_t >= 1) return 1;
-    const float cos_t = sqrtf(fmaxf(0.0f, 1 - sin_t * sin_t));
-    const float rpar = ((eta_t * cos_i) - (eta_i * cos_t)) / ((eta_t * cos_i) + (eta_i * cos_t));
-    const float rperp = ((eta_i * cos_i) - (eta_t * cos_t)) / ((eta_i * cos_i) + (eta_t * cos_t));
-    return (rpar * rpar + rperp * rperp) / 2;
-}
-// models/BxDF.cuh:44-67 (etaI = 1)
-__device__ Spec fresnel_conductor(float cos_i, Spec eta_t, Spec k) {
-    cos_i = clampf(cos_i, -1, 1);
-    const Spec eta = eta_t / 1.0f, etak = k / 1.0f;
-    const float c2 = cos_i * cos_i, s2 = 1.0f - c2;
-    const Spec eta2 = eta * eta, etak2 = etak * etak;
-    const Spec t0 = eta2 - etak2 - spec(s2);
-    const Spec a2b2 = ssqrt(t0 * t0 + eta2 * 4.0f * etak2);
-    const Spec t1 = a2b2 + spec(c2);
-    const Spec a = ssqrt((a2b2 + t0) * 0.5f);
-    const Spec t2 = a * (2.0f * cos_i);
-    const Spec rs = (t1 - t2) / (t1 + t2);
-    const Spec t3 = a2b2 * c2 + spec(s2 * s2);
-    const Spec t4 = t2 * s2;
-    const Spec rp = rs * (t3 - t4) / (t3 + t4);
-    return (rp + rs) * 0.5f;
-}
-// models/BxDF.cuh:156-166
-__device__ __forceinline__ bool refract(V3 wi, V3 n, float eta, V3& wt) {
-    const float ci = dot(n, wi);
-    const float s2i = fmaxf(0.0f, 1.0f - ci * ci);
-    const float s2t = eta * eta * s2i;
-    if (s2t >= 1) return false;
-    const float ct = sqrtf(1 - s2t);
-    wt = -wi * eta + n * (eta * ci - ct);
-    return true;
-}
-
-// Trowbridge-Reitz (models/Microfacet.cuh:53-181)
-__device__ float tr_lambda(V3 w, float ax, float ay) {
-    const float at = fabsf(tant(w));
-    if (isinf(at)) return 0.0f;
-    const float cp = cosphi(w), sp = sinphi(w);
-    const float alpha = sqrtf(cp * cp * ax * ax + sp * sp * ay * ay);
-    const float a2t2 = (alpha * at) * (alpha * at);
-    return (-1 + sqrtf(1.0f + a2t2)) / 2;
-}
-__device__ float tr_d(V3 wh, float ax, float ay) {
-    const float t2 = tan2t(wh);
-    if (isinf(t2)) return 0;
-    const float c4 = cos2t(wh) * cos2t(wh);
-    const float cp = cosphi(wh), sp = sinphi(wh);
-    const float e = (cp * cp / (ax * ax) + sp * sp / (ay * ay)) * t2;
-    return 1 / (3.14159265358979f * ax * ay * c4 * (1 + e) * (1 + e));
-}
-__device__ __forceinline__ float tr_g1(V3 w, float ax, float ay) { return 1 / (1 + tr_lambda(w, ax, ay)); }
-__device__ __forceinline__ float tr_g(V3 wo, V3 wi, float ax, float ay) {
-    return 1 / (1 + tr_lambda(wo, ax, ay) + tr_lambda(wi, ax, ay));
-}
-__device__ void tr_sample11(float cosT, float U1, float U2, float& sx, float& sy) {
-    if (cosT >= kOneMinusEpsUp) {
-        const float r = sqrtf(U1 / (1 - U1));
-        const float phi = mul_dc(U2, LTS_2PI_HI, LTS_2PI_LO);
-        sx = r * cosf(phi);
-        sy = r * sinf(phi);
-        return;
-    }
-    const float sinT = sqrtf(fmaxf(0.0f, 1.0f - cosT * cosT));
-    const float tanT = sinT / cosT;
-    const float a = 1 / tanT;
-    const float G1 = 2 / (1 + sqrtf(1.f + 1.f / (a * a)));
-    const float A = 2 * U1 / G1 - 1;
-    float tmp = 1.f / (A * A - 1.f);
-    if (tmp > 1e10f) tmp = 1e10f;
-    const float B = tanT;
-    const float D = sqrtf(fmaxf(float(B * B * tmp * tmp - (A * A - B * B) * tmp), 0.0f));
-    const float s1 = B * tmp - D, s2 = B * tmp + D;
-    sx = (A < 0 || s2 > 1.f / tanT) ? s1 : s2;
-    float S;
-    if (U2 > 0.5f) {
-        S = 1.f;
-        U2 = 2.f * (U2 - .5f);
-    } else {
-        S = -1.f;
-        U2 = 2.f * (.5f - U2);
-    }
-    const float z = (U2 * (U2 * (U2 * 0.27385f - 0.73369f) + 0.46341f)) /
-                    (U2 * (U2 * (U2 * 0.093073f + 0.309420f) - 1.000000f) + 0.597999f);
-    sy = S * z * sqrtf(1.f + sx * sx);
-}
-__device__ V3 tr_sample(V3 wi, float ax, float ay, float U1, float U2) {
-    const V3 ws = normalize(v3(ax * wi.x, ay * wi.y, wi.z));
-    float sx, sy;
-    tr_sample11(ws.z, U1, U2, sx, sy);
-    const float tmp = cosphi(ws) * sx - sinphi(ws) * sy;
-    sy = sinphi(ws) * sx + cosphi(ws) * sy;
-    sx = tmp;
-    sx = ax * sx;
-    sy = ay * sy;
-    return normalize(v3(-sx, -sy, 1.f));
-}
-
-struct Bsdf {
-    int lobe;           // LobeKind; at most one lobe for every reachable material
-    uint32_t type;      // BxDF type bits of the lobe
-    V3 ns, ng, ss, ts;
-    Spec R, T, k, eta3;
-    float eta, a, b, alpha;
-};
-
-__device__ __forceinline__ V3 to_local(const Bsdf& f, V3 v) { return v3(dot(v, f.ss), dot(v, f.ts), dot(v, f.ns)); }
-__device__ __forceinline__ V3 to_world(const Bsdf& f, V3 v) {
-    return v3(f.ss.x * v.x + f.ts.x * v.y + f.ns.x * v.z, f.ss.y * v.x + f.ts.y * v.y + f.ns.y * v.z,
-              f.ss.z * v.x + f.ts.z * v.y + f.ns.z * v.z);
-}
-__device__ __forceinline__ bool matches(uint32_t type, uint32_t flags) { return (type & flags) == type; }
-
-// BxDF::f
-__device__ Spec lobe_f(const Bsdf& f, V3 wo, V3 wi) {
-    switch (f.lobe) {
-        case LOBE_LAMBERT: return f.R * LTS_1_PI_HI;
-        case LOBE_OREN_NAYAR: {  // Microfacet.cuh:27-50
-            const float so = sint(wo), si_ = sint(wi);
-            float maxcos = 0.0f;
-            if (si_ >= 0.0001f && so >= 0.0001f) {
-                const float spo = sinphi(wo), cpo = cosphi(wo), spi = sinphi(wi), cpi = cosphi(wi);
-                const float dcos = cpi * cpo + spi * spo;
-                maxcos = fmaxf(0.0f, dcos);
-            }
-            float sin_a, tan_b;
-            if (fabsf(wi.z) > fabsf(wo.z)) {
-                sin_a = so;
-                tan_b = si_ / fabsf(wi.z);
-            } else {
-                sin_a = si_;
-                tan_b = so / fabsf(wo.z);
-            }
-            return f.R * LTS_1_PI_HI * (f.a + f.b * maxcos * sin_a * tan_b);
-        }
-        case LOBE_MICROFACET: {  // Microfacet.cuh:200-209
-            const float co = fabsf(wo.z), ci = fabsf(wi.z);
-            V3 wh = wi + wo;
-            if (ci == 0 || co == 0) return spec(0.0f);
-            if (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) return spec(0.0f);
-            wh = normalize(wh);
-            const Spec F = fresnel_conductor(fabsf(dot(wi, wh)), f.eta3, f.k);
-            return f.R * tr_d(wh, f.alpha, f.alpha) * tr_g(wo, wi, f.alpha, f.alpha) * F / (4 * ci * co);
-        }
-        default: return spec(0.0f);  // specular lobes
-    }
-}
-// BxDF::Pdf
-__device__ float lobe_pdf(const Bsdf& f, V3 wo, V3 wi, uint64_t* sig) {
-    switch (f.lobe) {
-        case LOBE_LAMBERT:
-        case LOBE_OREN_NAYAR:
-            return same_hemi(wo, wi, sig) ? mul_dc(fabsf(wi.z), LTS_1_PI_HI, LTS_1_PI_LO) : 0.0f;
-        case LOBE_MICROFACET: {
-            if (!same_hemi(wo, wi, sig)) return 0;
-            const V3 wh = normalize(wo + wi);
-            const float pd = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha, f.alpha) * absdot(wo, wh) / fabsf(wo.z);
-            return pd / (4 * dot(wo, wh));
-        }
-        default: return 0.0f;
-    }
-}
-// BSDF::f (materials/BSDF.cuh:192-204)
-__device__ Spec bsdf_f(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags, uint64_t* sig) {
-    const bool reflect = dot(wiW, f.ng) * dot(woW, f.ng) > 0;
-    if (sig) fnv_mix(*sig, 0x600000000ull + (reflect ? 1u : 0u));
-    if (f.lobe == LOBE_NONE || !matches(f.type, flags)) return spec(0.0f);
-    const V3 wi = to_local(f, wiW), wo = to_local(f, woW);
-    if ((reflect && (f.type & BSDF_REFLECTION)) || (!reflect && (f.type & BSDF_TRANSMISSION)))
-        return spec(0.0f) + lobe_f(f, wo, wi);
-    return spec(0.0f);
-}
-// BSDF::Pdf (BSDF.cuh:261-276)
-__device__ float bsdf_pdf(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags, uint64_t* sig) {
-    if (f.lobe == LOBE_NONE) return 0.0f;
-    const V3 wo = to_local(f, woW), wi = to_local(f, wiW);
-    if (wo.z == 0) return 0.0f;
-    if (!matches(f.type, flags)) return 0.0f;
-    const float pdf = 0.0f + lobe_pdf(f, wo, wi, sig);
-    return pdf / 1;
-}
-// BSDF::sampleF with a single matching lobe (BSDF.cuh:206-259) and the lobes' sampleF.
-__device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, uint32_t flags, uint32_t& sampled,
-                            uint64_t* sig) {
-    if (f.lobe == LOBE_NONE || !matches(f.type, flags)) {
-        pdf = 0;
-        return spec(0.0f);
-    }
-    // comp = min((int)floorf(u.x * 1), 0) = 0; the remapped sample is u itself
-    const V3 wo = to_local(f, woW);
-    V3 wi = v3(0, 0, 0);
-    pdf = 0;
-    sampled = f.type;
-    Spec val = spec(0.0f);
-    switch (f.lobe) {
-        case LOBE_LAMBERT:
-        case LOBE_OREN_NAYAR: {  // BxDF::sampleF (BxDF.cuh:196-204)
-            const float r = sqrtf(u.x);
-            const float th = mul_dc(u.y, LTS_2PI_HI, LTS_2PI_LO);
-            const float dx = r * cosf(th), dy = r * sinf(th);
-            wi = v3(dx, dy, sqrtf(fmaxf(0.0f, 1 - dx * dx - dy * dy)));
-            if (wo.z < 0) wi.z *= -1;
-            pdf = lobe_pdf(f, wo, wi, sig);
-            val = lobe_f(f, wo, wi);
-            break;
-        }
-        case LOBE_SPECULAR_REFL: {  // Specular.cuh:30-39, FresnelNoOp
-            wi = v3(-wo.x, -wo.y, wo.z);
-            pdf = 1.0f;
-            val = (spec(1.0f) * f.R) / fabsf(wi.z);
-            break;
-        }
-        case LOBE_FRESNEL_SPECULAR: {  // Specular.cuh:107-135
-            const float F = fresnel_dielectric(wo.z, 1.0f, f.eta);
-            if (u.x < F) {
-                wi = v3(-wo.x, -wo.y, -wo.z);  // the reference's "reflection" keeps going straight
-                sampled = BSDF_SPECULAR | BSDF_REFLECTION;
-                pdf = F;
-                val = (f.R * F) / fabsf(wi.z);
-            } else {
-                const bool entering = wo.z > 0;
-                const float ei = entering ? 1.0f : f.eta, et = entering ? f.eta : 1.0f;
-                const V3 n = face_towards(v3(0, 0, 1), wo);
-                if (!refract(wo, n, ei / et, wi)) {
-                    pdf = 0;
-                    return spec(0.0f);
-                }
-                Spec ft = f.T * (1 - F);
-                ft = ft * ((ei * ei) / (et * et));
-                sampled = BSDF_SPECULAR | BSDF_TRANSMISSION;
-                pdf = 1.0f - F;
-                val = ft / fabsf(wi.z);
-            }
-            break;
-        }
-        case LOBE_MICROFACET: {  // Microfacet.cuh:211-222
-            if (wo.z == 0) return spec(0.0f);
-            const bool flip = wo.z < 0;
-            V3 wh = tr_sample(flip ? -wo : wo, f.alpha, f.alpha, u.x, u.y);
-            if (flip) wh = -wh;
-            if (dot(wo, wh) < 0) return spec(0.0f);
-            wi = -wo + wh * (2 * dot(wo, wh));
-            if (!same_hemi(wo, wi, sig)) return spec(0.0f);
-            const float pd = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha, f.alpha) * absdot(wo, wh) / fabsf(wo.z);
-            pdf = pd / (4 * dot(wo, wh));
-            val = lobe_f(f, wo, wi);
-            break;
-        }
-    }
-    if (pdf == 0) return spec(0.0f);
-    wiW = to_world(f, wi);
-    return val;
-}
-
-// Material::computeScatteringFunctions (materials/Material.cuh:31-130) into a Bsdf record.
-// Returns false when the primitive has no material (the reference's skipped 'M' entries).
-__device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, uint64_t* sig) {
-    const int mesh = __ldg(&sv.prim_n[si.prim].w);
-    const DevMat& m = sv.mats[mesh];
-    if (m.kind == 0) return false;
-    f.ns = si.sn;
-    f.ng = si.n;
-    f.ss = normalize(si.sdpdu);
-    f.ts = cross(f.ns, f.ss);
-    f.lobe = LOBE_NONE;
-    f.type = 0;
-    f.eta = 1;
-    switch (m.kind) {
-        case 1: {  // Matte
-            const Spec kd = eval_texture(m.tex[0], si, sig);
-            if (!is_black(kd)) {
-                f.R = kd;
-                if (m.extra == 0) {
-                    f.lobe = LOBE_LAMBERT;
-                } else {
-                    f.lobe = LOBE_OREN_NAYAR;
-                    f.a = m.on_a;
-                    f.b = m.on_b;
-                }
-                f.type = BSDF_REFLECTION | BSDF_DIFFUSE;
-            }
-            break;
-        }
-        case 2: {  // Glass
-            f.eta = m.extra;
-            const Spec r = eval_texture(m.tex[0], si, sig), t = eval_texture(m.tex[1], si, sig);
-            if (is_black(r) && is_black(t)) break;
-            f.R = r;
-            f.T = t;
-            f.lobe = LOBE_FRESNEL_SPECULAR;
-            f.type = BSDF_REFLECTION | BSDF_TRANSMISSION | BSDF_SPECULAR;
-            break;
-        }
-        case 3: {  // Mirror
-            const Spec r = eval_texture(m.tex[0], si, sig);
-            if (is_black(r)) break;
-            f.R = r;
-            f.lobe = LOBE_SPECULAR_REFL;
-            f.type = BSDF_REFLECTION | BSDF_SPECULAR;
-            break;
-        }
-        case 4: {  // Metal (alpha given directly)
-            f.k = eval_texture(m.tex[0], si, sig);
-            f.eta3 = Spec{m.tex[1].v[0], m.tex[1].v[1], m.tex[1].v[2]};
-            f.R = spec(1.0f);
-            f.alpha = m.extra;
-            f.lobe = LOBE_MICROFACET;
-            f.type = BSDF_REFLECTION | BSDF_GLOSSY;
-            break;
-        }
-    }
-    return true;
-}
-
-// ------------------------------------------------------------------ lights
-struct LightSample {
-    Spec Li;
-    V3 wi;
-    float pdf;
-    V3 p1, perr1, n1;  // visibility target interaction
-};
-__device__ __forceinline__ float sph_pdf_infinite(V3 w) {
-    // uniformSampleHemispherePDF() / (2 * M_PI * M_PI * sinf(sphericalTheta(w)))
-    const float s = sinf(acosf(clampf(w.z, -1.0f, 1.0f)));
-    return 0.159154937f / (19.7392088f * s);
-}
-
-// Triangle::Pdf(it, wi) (shapes/Triangle.cu:211-225): re-intersects the light triangle.
-__device__ float area_pdf(const SceneView& sv, const DevLight& L, V3 p, V3 perr, V3 n, V3 wi) {
-    const V3 o = offset_origin(p, perr, n, wi);
-    V3 p0, p1, p2;
-    prim_tri(sv, L.prim, p0, p1, p2);
-    float t, u, v, inv;
-    if (!tri_test(p0, p1, p2, o, wi, INFINITY, t, u, v, inv)) return 0;
-    SI is;
-    make_si(sv, L.prim, p0, p1, p2, wi, u, v, inv, is);
-    const V3 dpt = p - is.p;
-    return len2(dpt) / (absdot(is.n, -wi) * L.area);
-}
-
-__device__ bool sample_li(const SceneView& sv, const DevLight& L, const SI& si, F2 u, LightSample& ls) {
-    ls.Li = spec(0.0f);
-    ls.pdf = 0;
-    ls.perr1 = v3(0, 0, 0);
-    ls.n1 = v3(0, 0, 0);
-    if (L.kind == 0) {  // AreaLight::sampleLi (Light.cu:28-37) + Triangle::sample (Triangle.cu:232-259)
-        const float su = sqrtf(u.x);
-        const float b0 = 1 - su, b1 = u.y * su;
-        V3 p0, p1, p2;
-        prim_tri(sv, L.prim, p0, p1, p2);
-        const float b2 = 1 - b0 - b1;
-        const V3 ps = p0 * b0 + p1 * b1 + p2 * b2;
-        V3 ns;
-        const int4 ni = __ldg(sv.prim_n + L.prim);
-        if (ni.x >= 0)
-            ns = normalize(normal_at(sv, ni.x) * b0 + normal_at(sv, ni.y) * b1 + normal_at(sv, ni.z) * b2);
-        else
-            ns = normalize(cross(p1 - p0, p2 - p0));
-        const V3 pabs = vabs(p0 * b0) + vabs(p1 * b1) + vabs(p2 * b2);
-        ls.perr1 = pabs * gamma_n(6);
-        ls.p1 = ps;
-        ls.n1 = ns;
-        ls.wi = normalize(ps - si.p);
-        ls.pdf = area_pdf(sv, L, si.p, si.perr, si.n, ls.wi);
-        ls.Li = dot(ns, -ls.wi) > 0.f ? Spec{L.L[0], L.L[1], L.L[2]} : spec(0.0f);
-        return false;
-    }
-    if (L.kind == 1) {  // InfiniteLight::sampleLi (Light.cu:68-90)
-        const float z = u.x;
-        const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
-        const float phi = mul_dc(u.y, LTS_2PI_HI, LTS_2PI_LO);
-        const V3 w0 = v3(r * cosf(phi), r * sinf(phi), z);
-        const V3 ref = v3(0, 1, 0);
-        V3 a, b;
-        coordinate_system(ref, a, b);
-        const V3 w = a * w0.x + b * w0.y + ref * w0.z;
-        const V3 pl = v3(L.p[0], L.p[1], L.p[2]) + w * L.radius;
-        ls.wi = normalize(pl - si.p);
-        ls.pdf = sph_pdf_infinite(ls.wi);
-        ls.p1 = pl;
-        ls.Li = Spec{L.L[0], L.L[1], L.L[2]};
-        return false;
-    }
-    // PointLight::sampleLi (Light.cu:8-17)
-    const V3 pl = v3(L.p[0], L.p[1], L.p[2]);
-    ls.wi = normalize(pl - si.p);
-    ls.pdf = 1.0f;
-    ls.p1 = pl;
-    ls.Li = Spec{L.L[0], L.L[1], L.L[2]} / len2(pl - si.p);
-    return true;  // delta light
-}
 
 // ------------------------------------------------------------------ film
 struct FilmAcc {
@@ -972,6 +71,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
         rng.sample = (uint32_t)s;
         rng.draw = 0;
         uint64_t sig = 0xcbf29ce484222325ull;
+        EvSink evs{&sig, 0};
         Tracer16 tr{nullptr, 0};
         if (RECORD && rp.trace &&
             ((long)((j - rp.y0) * (rp.x1 - rp.x0) + (i - rp.x0)) * rp.spp + s) == rp.trace_sample)
@@ -1029,7 +129,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                 si.dpdy = v3(0, 0, 0);
             }
             Bsdf f;
-            if (!make_bsdf(sv, si, f, RECORD ? &sig : nullptr)) break;
+            if (!make_bsdf(sv, si, f, RECORD ? &evs : nullptr)) break;
             if (RECORD) tr.put(2, f.lobe, f.R.r, f.R.g, f.R.b, f.ss.x, f.ss.y, f.ss.z, f.ts.x, f.ts.y, f.ts.z, si.dpdx.x,
                                si.dpdx.y, si.dpdx.z);
             // 7a. direct lighting: uniformSampleOneLight + estimateDirect (IntegratorHelper.cuh:51-149)
@@ -1061,8 +161,8 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                 LightSample ls;
                 const bool delta = sample_li(sv, Lt, si, ulight, ls);
                 if (ls.pdf > 0 && !is_black(ls.Li)) {
-                    const Spec fv = bsdf_f(f, si.wo, ls.wi, flags, RECORD ? &sig : nullptr) * absdot(ls.wi, si.sn);
-                    const float spdf = bsdf_pdf(f, si.wo, ls.wi, flags, RECORD ? &sig : nullptr);
+                    const Spec fv = bsdf_f(f, si.wo, ls.wi, flags, RECORD ? &evs : nullptr) * absdot(ls.wi, si.sn);
+                    const float spdf = bsdf_pdf(f, si.wo, ls.wi, flags, RECORD ? &evs : nullptr);
                     if (!is_black(fv)) {
                         // VisibilityTester::unoccluded -> spawnRayTo(Interaction) (Interaction.cuh:47-51)
                         const V3 org = offset_origin(si.p, si.perr, si.n, ls.p1 - si.p);
@@ -1088,7 +188,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                     V3 wi = ls.wi;
                     float spdf = 0;
                     uint32_t stype = 0;
-                    Spec fv = bsdf_sample(f, si.wo, wi, uscat, spdf, flags, stype, RECORD ? &sig : nullptr);
+                    Spec fv = bsdf_sample(f, si.wo, wi, uscat, spdf, flags, stype, RECORD ? &evs : nullptr);
                     fv = fv * absdot(wi, si.sn);
                     const bool sampled_spec = (stype & BSDF_SPECULAR) != 0;
                     if (!is_black(fv) && spdf > 0) {
@@ -1130,7 +230,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
             float pdf = 0;
             uint32_t stype = 0;
             const F2 ub = rng_2d(rng);
-            const Spec fv = bsdf_sample(f, si.wo, wi, ub, pdf, BSDF_ALL, stype, RECORD ? &sig : nullptr);
+            const Spec fv = bsdf_sample(f, si.wo, wi, ub, pdf, BSDF_ALL, stype, RECORD ? &evs : nullptr);
             if (is_black(fv) || pdf == 0) break;
             specular = (stype & BSDF_SPECULAR) != 0;
             beta = beta * (fv * absdot(wi, si.sn) / pdf);
@@ -1233,6 +333,16 @@ __global__ void k_gather_leaves(const float4* __restrict__ prim_v, const int32_t
     leaf_v[3 * l + 2] = __ldg(prim_v + 3 * p + 2);
 }
 
+}  // namespace
+}  // namespace lts
+
+#include "wavefront.cuh"
+
+namespace lts {
+namespace {
+
+static_assert(kWfBlock == kThreads, "wavefront stages share the traversal stack layout");
+
 #define TRY(call)                                                                       \
     do {                                                                                \
         cudaError_t e_ = (call);                                                        \
@@ -1272,12 +382,18 @@ void Tracer::free_all() {
     rgb_ = nullptr;
     dev_free(trace_);
     trace_ = nullptr;
+    for (void*& p : wf_bufs_) {
+        if (p) dev_free(p);
+        p = nullptr;
+    }
+    wf_cap_ = 0;
     film_cap_ = rec_cap_ = 0;
     leaf_serial_ = 0;
 }
 
 Tracer::~Tracer() {
     free_all();
+    if (wf_counts_host_) cudaFreeHost(wf_counts_host_);
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
 }
@@ -1387,7 +503,10 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
 std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                             uint32_t* d_err, RenderParams* rp, SceneView* sv, long* crop_samples) {
     if (d.spp < 1 || d.max_bounce < 0) return "bad argument: spp must be >= 1 and max_bounce >= 0";
-    if (d.integrator != LTS_INTEGRATOR_MEGAKERNEL) return "bad argument: only the megakernel integrator is built";
+    if (d.integrator != LTS_INTEGRATOR_MEGAKERNEL && d.integrator != LTS_INTEGRATOR_WAVEFRONT)
+        return "bad argument: unknown integrator";
+    if (d.integrator == LTS_INTEGRATOR_WAVEFRONT && d.max_bounce < 1)
+        return "bad argument: the wavefront integrator needs max_bounce >= 1";
     int x0 = d.x0, y0 = d.y0, x1 = d.x1, y1 = d.y1;
     if (x1 == 0 && y1 == 0) {
         x0 = y0 = 0;
@@ -1467,6 +586,8 @@ std::string Tracer::render_async(const HostScene& sc, const Lbvh& bvh, const lts
     long ns = 0;
     std::string e = prepare(sc, bvh, d, s, d_err, &rp, &sv, &ns);
     if (!e.empty()) return e;
+    last_paths = (double)ns;
+    if (d.integrator == LTS_INTEGRATOR_WAVEFRONT) return render_wavefront(sc, bvh, d, s, d_err, rp, sv, ns);
     const dim3 block(kBX, kBY);
     const dim3 grid((rp.x1 - rp.x0 + kBX - 1) / kBX, (rp.y1 - rp.y0 + kBY - 1) / kBY);
     TRY(cudaEventRecord(ev0_, s));
@@ -1477,7 +598,82 @@ std::string Tracer::render_async(const HostScene& sc, const Lbvh& bvh, const lts
     TRY(cudaEventRecord(ev1_, s));
     TRY(cudaGetLastError());
     last_launches = 1;
+    last_iterations = 1;
     last_paths = (double)ns;
+    return "";
+}
+
+std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
+                                     uint32_t* d_err, const RenderParams& rp, const SceneView& sv, long total) {
+    (void)sc;
+    (void)d;
+    (void)d_err;
+    const long P = std::max<long>(1, std::min<long>(total, wf_pool > 0 ? wf_pool : (1l << 21)));
+    WfState st{};
+    if (wf_cap_ < P) {
+        for (void*& p : wf_bufs_) {
+            if (p) dev_free(p);
+            p = nullptr;
+        }
+        wf_cap_ = 0;
+        const size_t n = (size_t)P;
+        const size_t sizes[] = {4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n,                       // pix smp draw flags pend vis
+                                16 * n, 16 * n, 16 * n, 16 * n, 8 * n, 8 * n, 4 * n, 16 * n,  // ro rd beta L pf sig hprim huvi
+                                16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n,  // sh_* mis_* ld nee
+                                8 * n, 8 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 64};
+        for (size_t k = 0; k < sizeof sizes / sizeof sizes[0]; ++k) TRY(dev_alloc(&wf_bufs_[k], sizes[k]));
+        wf_cap_ = P;
+    }
+    if (!wf_counts_host_) TRY(cudaMallocHost((void**)&wf_counts_host_, 64));
+    void** b = wf_bufs_;
+    st.pix = (int32_t*)b[0]; st.smp = (int32_t*)b[1]; st.draw = (uint32_t*)b[2]; st.flags = (uint32_t*)b[3];
+    st.pend = (uint32_t*)b[4]; st.vis = (uint32_t*)b[5];
+    st.ro = (float4*)b[6]; st.rd = (float4*)b[7]; st.beta = (float4*)b[8]; st.L = (float4*)b[9];
+    st.pf = (float2*)b[10]; st.sig = (uint64_t*)b[11]; st.hprim = (int32_t*)b[12]; st.huvi = (float4*)b[13];
+    st.sh_o = (float4*)b[14]; st.sh_d = (float4*)b[15]; st.sh_c = (float4*)b[16];
+    st.mis_o = (float4*)b[17]; st.mis_d = (float4*)b[18]; st.mis_fv = (float4*)b[19]; st.mis_x = (float4*)b[20];
+    st.ld_mis = (float4*)b[21]; st.nee_beta = (float4*)b[22];
+    st.ev_mis = (uint64_t*)b[23]; st.ev_main = (uint64_t*)b[24]; st.mis_hit = (int32_t*)b[25];
+    st.q_a = (int32_t*)b[26]; st.q_b = (int32_t*)b[27]; st.q_shadow = (int32_t*)b[28]; st.q_mis = (int32_t*)b[29];
+    st.q_free = (int32_t*)b[30]; st.counts = (uint32_t*)b[31];
+    TRY(cudaMemsetAsync(st.counts, 0, 64, s));
+    if (rp.sample_sig) {
+        TRY(cudaMemsetAsync(st.ev_mis, 0, 8 * (size_t)P, s));
+        TRY(cudaMemsetAsync(st.ev_main, 0, 8 * (size_t)P, s));
+    }
+    const int grid = (int)((P + kWfBlock - 1) / kWfBlock);
+    k_wf_init_free<<<grid, kWfBlock, 0, s>>>(st.q_free, st.counts, (int)P);
+    TRY(cudaEventRecord(ev0_, s));
+    int32_t *cur = st.q_a, *next = st.q_b;
+    uint32_t *c_cur = st.counts + 0, *c_next = st.counts + 1;
+    const bool rec = rp.sample_sig != nullptr;
+    int it = 0, launches = 0;
+    for (;; ++it) {
+        k_wf_generate<<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, total);
+        k_wf_generate_done<<<1, 1, 0, s>>>(st, total);
+        TRY(cudaMemsetAsync(c_next, 0, 4, s));
+        TRY(cudaMemsetAsync(st.counts + 2, 0, 8, s));
+        k_wf_extend<<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, bvh.n);
+        if (rec) k_wf_shade<true><<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur);
+        else k_wf_shade<false><<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur);
+        k_wf_shadow<<<grid, kWfBlock, 0, s>>>(sv, rp, st, bvh.n);
+        k_wf_mis<<<grid, kWfBlock, 0, s>>>(sv, rp, st, bvh.n);
+        if (rec) k_wf_finalize<true><<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, next, c_next);
+        else k_wf_finalize<false><<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, next, c_next);
+        launches += 8;
+        TRY(cudaGetLastError());
+        TRY(cudaMemcpyAsync(wf_counts_host_, st.counts, 32, cudaMemcpyDeviceToHost, s));
+        TRY(cudaStreamSynchronize(s));
+        const uint32_t nnext = wf_counts_host_[it & 1 ? 0 : 1];
+        const long generated = (long)wf_counts_host_[5];
+        if (nnext == 0 && generated >= total) break;
+        if (it > 100000) return "wavefront did not converge";
+        std::swap(cur, next);
+        std::swap(c_cur, c_next);
+    }
+    TRY(cudaEventRecord(ev1_, s));
+    last_launches = launches;
+    last_iterations = it + 1;
     return "";
 }
 

@@ -76,6 +76,9 @@ class Tracer {
     std::string film_get(const HostScene& sc, float* rgb, double* sums, cudaStream_t s);
 
     double last_ms = 0, last_paths = 0, last_rays = 0, last_node_visits = 0, last_tri_tests = 0;
+    // Path-pool capacity of the wavefront integrator (0: automatic).
+    long wf_pool = 0;
+    int last_iterations = 0;
     // Parity debugging: the record-mode render writes the events of this crop sample index.
     long trace_sample_ = -1;
     float* trace_ = nullptr;
@@ -85,6 +88,11 @@ class Tracer {
     std::string prepare(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                         uint32_t* d_err, RenderParams* rp, SceneView* sv, long* crop_samples);
     void free_all();
+    std::string render_wavefront(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
+                                 uint32_t* d_err, const RenderParams& rp, const SceneView& sv, long total);
+    void* wf_bufs_[40] = {nullptr};
+    long wf_cap_ = 0;
+    uint32_t* wf_counts_host_ = nullptr;
     SceneView view_{};
     void* bufs_[16] = {nullptr};
     float4* leaf_v_ = nullptr;

@@ -1,0 +1,478 @@
+// Wavefront path tracer (sm_103a): the same integrator as k_pathtrace, split into stage kernels
+// over a pool of path states and index queues, so each stage runs with its own (small) register
+// budget and all lanes of a warp execute the same stage:
+//
+//   generate  fill free pool slots with new (pixel, sample) work: film + lens draws, camera ray
+//   extend    closest-hit traversal of every queued path ray
+//   shade     emission, SurfaceInteraction, material, light sample (NEE) + MIS BSDF sample,
+//             path BSDF sample, throughput, Russian roulette; queues shadow and MIS rays
+//   shadow    any-hit traversal of the NEE shadow rays
+//   mis       closest-hit traversal of the MIS BSDF rays, light radiance where they land
+//   finalize  adds the bounce's direct light in the reference's order (Ld = light part + MIS
+//             part, L += beta * Ld / lightPdf), mixes the deferred parity events, then splats
+//             finished samples to the FP64 film and frees their slot, or requeues the path
+//
+// The sampler is keyed per (pixel, sample) with a draw counter kept in the path state, so a path
+// produces exactly the draws of the megakernel (PathTracingIntegrator.cuh:41-99) in any order of
+// execution.  Included by tracer.cu (one translation unit shares the constant tables).
+#pragma once
+
+namespace lts {
+namespace {
+
+enum : uint32_t { WF_VIS = 1u, WF_MIS = 2u, WF_NEE = 4u, WF_DONE = 8u };
+constexpr int kWfBlock = 128;
+constexpr uint64_t kSigBasis = 0xcbf29ce484222325ull;
+
+struct WfState {
+    int32_t *pix, *smp;
+    uint32_t *draw, *flags, *pend, *vis;
+    float4 *ro, *rd, *beta, *L;
+    float2* pf;
+    uint64_t* sig;
+    int32_t* hprim;
+    float4* huvi;
+    float4 *sh_o, *sh_d, *sh_c;
+    float4 *mis_o, *mis_d, *mis_fv, *mis_x, *ld_mis;
+    float4* nee_beta;
+    uint64_t *ev_mis, *ev_main;
+    int32_t* mis_hit;
+    int32_t *q_a, *q_b, *q_shadow, *q_mis, *q_free;
+    uint32_t* counts;  // [0] q_a size, [1] q_b size, [2] shadow, [3] mis, [4] free, [5] generated
+};
+
+// Resume a (pixel, sample) stream at draw `draw` (regenerates the current Philox block).
+__device__ __forceinline__ void rng_resume(Rng& r) {
+    const uint32_t k = r.draw & 3u;
+    if (k == 0u) return;
+    const uint32_t d = r.draw;
+    r.draw = d & ~3u;
+    philox_block(r);
+    r.draw = d;
+    for (uint32_t q = 0; q < k; ++q) {
+        r.w0 = r.w1;
+        r.w1 = r.w2;
+        r.w2 = r.w3;
+    }
+}
+
+__device__ __forceinline__ int warp_push(uint32_t* counter, bool pred) {
+    const unsigned mask = __activemask();
+    const unsigned vote = __ballot_sync(mask, pred);
+    if (!pred) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(vote) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(vote));
+    base = __shfl_sync(vote, base, leader);
+    return (int)(base + __popc(vote & ((1u << lane) - 1u)));
+}
+
+__device__ __forceinline__ void camera_ray(const SceneView& sv, float pfx, float pfy, V3& rd, V3& rxd, V3& ryd,
+                                           float spp_scale) {
+    const float* cam = sv.cam;
+    const V3 co = v3(cam[0], cam[1], cam[2]), cright = v3(cam[3], cam[4], cam[5]), cup = v3(cam[6], cam[7], cam[8]),
+             cllc = v3(cam[9], cam[10], cam[11]);
+    const float rx = (float)(sv.width - 1), ry = (float)(sv.height - 1);
+    rd = normalize(cllc + cright * (pfx / rx) + cup * (pfy / ry) - co);
+    const V3 dx0 = normalize(cllc + cright * ((pfx + 1) / rx) + cup * (pfy / ry) - co);
+    const V3 dy0 = normalize(cllc + cright * (pfx / rx) + cup * ((pfy + 1) / ry) - co);
+    rxd = rd + (dx0 - rd) * spp_scale;
+    ryd = rd + (dy0 - rd) * spp_scale;
+}
+
+// generate: pops free slots and starts new samples (sample-major over the crop's pixels).
+__global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, const RenderParams rp, WfState st,
+                                                          int32_t* q_cur, uint32_t* c_cur, long total) {
+    const long t = (long)blockIdx.x * kWfBlock + threadIdx.x;
+    const uint32_t nfree = st.counts[4];
+    const long generated = (long)st.counts[5];
+    const long take = min((long)nfree, total - generated);
+    if (t >= take) return;
+    const long w = generated + t;
+    const int slot = st.q_free[nfree - 1 - t];
+    const int cw = rp.x1 - rp.x0;
+    const long npix = (long)cw * (rp.y1 - rp.y0);
+    const int s = (int)(w / npix);
+    const long pc = w % npix;
+    const int i = rp.x0 + (int)(pc % cw), j = rp.y0 + (int)(pc / cw);
+    const int id = j * sv.width + i;
+    Rng rng;
+    rng.key = rp.seed + wang_hash((uint32_t)id);
+    rng.sample = (uint32_t)s;
+    rng.draw = 0;
+    const F2 fs = rng_2d(rng);
+    (void)rng_2d(rng);
+    const float pfx = (float)(i + fs.x), pfy = (float)(j + fs.y);
+    V3 rd, rxd, ryd;
+    camera_ray(sv, pfx, pfy, rd, rxd, ryd, rp.spp_scale);
+    st.pix[slot] = id;
+    st.smp[slot] = s;
+    st.draw[slot] = rng.draw;
+    st.flags[slot] = 0u;
+    st.pf[slot] = make_float2(pfx, pfy);
+    st.ro[slot] = make_float4(sv.cam[0], sv.cam[1], sv.cam[2], 0.f);
+    st.rd[slot] = make_float4(rd.x, rd.y, rd.z, 0.f);
+    st.beta[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
+    st.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    st.sig[slot] = kSigBasis;
+    const int pos = warp_push(c_cur, true);
+    q_cur[pos] = slot;
+}
+
+__global__ void k_wf_generate_done(WfState st, long total) {
+    const uint32_t nfree = st.counts[4];
+    const long generated = (long)st.counts[5];
+    const long take = min((long)nfree, total - generated);
+    st.counts[4] = nfree - (uint32_t)take;
+    st.counts[5] = (uint32_t)(generated + take);
+}
+
+__device__ __forceinline__ void count_work(const RenderParams& rp, unsigned rays, const Work& wk) {
+    const unsigned mask = __activemask();
+    const unsigned tot = __reduce_add_sync(mask, rays);
+    const unsigned tn = __reduce_add_sync(mask, wk.nodes), tt = __reduce_add_sync(mask, wk.tris);
+    const unsigned lane = threadIdx.x & 31u;
+    if ((mask & ((1u << lane) - 1u)) == 0u && rp.counters) {
+        atomicAdd(rp.counters, (unsigned long long)tot);
+        atomicAdd(rp.counters + 1, (unsigned long long)tn);
+        atomicAdd(rp.counters + 2, (unsigned long long)tt);
+    }
+}
+
+// extend: closest hit of each queued path ray (BVH::intersect, BVH.cuh:365-398).
+__global__ __launch_bounds__(kWfBlock) void k_wf_extend(const SceneView sv, const RenderParams rp, WfState st,
+                                                        const int32_t* __restrict__ q, const uint32_t* __restrict__ cnt,
+                                                        int nleaf) {
+    __shared__ uint32_t s_stack[kStack * kWfBlock];
+    const int t = blockIdx.x * kWfBlock + threadIdx.x;
+    if (t >= (int)*cnt) return;
+    const int p = q[t];
+    const float4 o = st.ro[p], d = st.rd[p];
+    const TraceRay r = make_trace_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z));
+    float tmax = INFINITY, bu = 0, bv = 0, binv = 0;
+    Work wk{0u, 0u};
+    const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, s_stack + threadIdx.x, rp.err, wk);
+    st.hprim[p] = prim;
+    st.huvi[p] = make_float4(bu, bv, binv, tmax);
+    count_work(rp, 1u, wk);
+}
+
+// shadow: any hit (VisibilityTester::unoccluded, VisibilityTester.cu:9-12).
+__global__ __launch_bounds__(kWfBlock) void k_wf_shadow(const SceneView sv, const RenderParams rp, WfState st,
+                                                        int nleaf) {
+    __shared__ uint32_t s_stack[kStack * kWfBlock];
+    const int t = blockIdx.x * kWfBlock + threadIdx.x;
+    if (t >= (int)st.counts[2]) return;
+    const int p = st.q_shadow[t];
+    const float4 o = st.sh_o[p], d = st.sh_d[p];
+    Work wk{0u, 0u};
+    const bool occ = scene_occluded(sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), d.w, s_stack + threadIdx.x, rp.err, wk);
+    st.vis[p] = occ ? 0u : 1u;
+    count_work(rp, 1u, wk);
+}
+
+// mis: closest hit of the MIS BSDF ray; radiance of the sampled light where it lands
+// (IntegratorHelper.cuh:225-243).
+__global__ __launch_bounds__(kWfBlock) void k_wf_mis(const SceneView sv, const RenderParams rp, WfState st, int nleaf) {
+    __shared__ uint32_t s_stack[kStack * kWfBlock];
+    const int t = blockIdx.x * kWfBlock + threadIdx.x;
+    if (t >= (int)st.counts[3]) return;
+    const int p = st.q_mis[t];
+    const float4 o = st.mis_o[p], d = st.mis_d[p], fv = st.mis_fv[p], x = st.mis_x[p];
+    const V3 wi = v3(d.x, d.y, d.z);
+    const int off = __float_as_int(x.y);
+    const DevLight& Lt = sv.lights[off];
+    Work wk{0u, 0u};
+    SI lit;
+    const bool found = scene_intersect(sv, nleaf, v3(o.x, o.y, o.z), wi, INFINITY, lit, s_stack + threadIdx.x, rp.err, wk);
+    Spec Li = spec(0.0f);
+    if (found) {
+        if (__ldg(sv.prim_light + lit.prim) == off && Lt.kind == 0)
+            Li = dot(lit.n, -wi) > 0.f ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
+    } else {
+        Li = Lt.kind == 1 ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
+    }
+    Spec c = spec(0.0f);
+    const bool add = !is_black(Li);
+    if (add) c = Spec{fv.x, fv.y, fv.z} * Li * spec(1.0f) * fv.w / x.x;
+    st.ld_mis[p] = make_float4(c.r, c.g, c.b, add ? 1.f : 0.f);
+    st.mis_hit[p] = found ? lit.prim + 1 : 0;
+    count_work(rp, 1u, wk);
+}
+
+// shade: one bounce of PathTracingIntegrator::evaluate up to the next ray.
+template <bool RECORD>
+__global__ __launch_bounds__(kWfBlock) void k_wf_shade(const SceneView sv, const RenderParams rp, WfState st,
+                                                       const int32_t* __restrict__ q, const uint32_t* __restrict__ cnt) {
+    const int t = blockIdx.x * kWfBlock + threadIdx.x;
+    if (t >= (int)*cnt) return;
+    const int p = q[t];
+    const uint32_t flags = st.flags[p];
+    const int bounce = (int)(flags >> 8);
+    bool specular = (flags & 1u) != 0;
+    const float4 o4 = st.ro[p], d4 = st.rd[p];
+    const V3 ro = v3(o4.x, o4.y, o4.z), rd = v3(d4.x, d4.y, d4.z);
+    const float4 b4 = st.beta[p], l4 = st.L[p];
+    Spec beta{b4.x, b4.y, b4.z}, L{l4.x, l4.y, l4.z};
+    uint64_t sig = RECORD ? st.sig[p] : 0ull;
+    EvSink evs{&sig, 0};
+    const int prim = st.hprim[p];
+    const bool hit = prim >= 0;
+    uint32_t pend = 0;
+    if (RECORD) fnv_mix(sig, 0x100000000ull + (uint64_t)(prim + 1));
+    SI si;
+    if (hit) {
+        const float4 h = st.huvi[p];
+        V3 p0, p1, p2;
+        prim_tri(sv, prim, p0, p1, p2);
+        make_si(sv, prim, p0, p1, p2, rd, h.x, h.y, h.z, si);
+    }
+    if (bounce == 0 || specular) {
+        if (hit) {
+            const int li = __ldg(sv.prim_light + prim);
+            if (li >= 0) {
+                const DevLight& Lt = sv.lights[li];
+                const Spec le = dot(si.n, -rd) > 0.f ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
+                L = L + beta * le;
+            } else {
+                L = L + beta * spec(0.0f);
+            }
+        } else {
+            for (int l = 0; l < sv.nlight; ++l) {
+                const DevLight& Lt = sv.lights[l];
+                L = L + beta * (Lt.kind == 1 ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f));
+            }
+        }
+    }
+    Rng rng;
+    rng.key = rp.seed + wang_hash((uint32_t)st.pix[p]);
+    rng.sample = (uint32_t)st.smp[p];
+    rng.draw = st.draw[p];
+    rng_resume(rng);
+    bool done = !hit;
+    Bsdf f;
+    if (!done) {
+        if (bounce == 0) {  // camera-ray differentials (Interaction.cuh:118-160)
+            const float2 pf = st.pf[p];
+            V3 rd0, rxd, ryd;
+            camera_ray(sv, pf.x, pf.y, rd0, rxd, ryd, rp.spp_scale);
+            const V3 n = si.n;
+            const float dd = -dot(n, si.p);
+            const float tx = (-dot(n, ro) - dd) / dot(n, rxd);
+            const float ty = (-dot(n, ro) - dd) / dot(n, ryd);
+            si.dpdx = (ro + rxd * tx) - si.p;
+            si.dpdy = (ro + ryd * ty) - si.p;
+        } else {
+            si.dpdx = v3(0, 0, 0);
+            si.dpdy = v3(0, 0, 0);
+        }
+        if (!make_bsdf(sv, si, f, RECORD ? &evs : nullptr)) done = true;
+    }
+    uint64_t ev_mis = 0, ev_main = 0;
+    if (!done) {
+        if (sv.nlight > 0) {
+            pend |= WF_NEE;
+            const float ul = rng_1d(rng);
+            int off = 0;
+            {
+                const int size = sv.nlight;
+                if (size != 1) {
+                    int first = 0, len = size;
+                    while (len > 0) {
+                        const int half = len >> 1, middle = first + half;
+                        if (__ldg(sv.light_cdf + middle) <= ul) {
+                            first = middle + 1;
+                            len -= half + 1;
+                        } else {
+                            len = half;
+                        }
+                    }
+                    off = (int)clampf((float)(first - 1), 0.0f, (float)(size - 2));
+                }
+            }
+            const float lpdf_sel = __ldg(sv.light_func + off) / (sv.light_func_int * sv.nlight);
+            st.nee_beta[p] = make_float4(beta.r, beta.g, beta.b, lpdf_sel);
+            const F2 ulight = rng_2d(rng);
+            const F2 uscat = rng_2d(rng);
+            const DevLight& Lt = sv.lights[off];
+            const uint32_t fl = specular ? BSDF_ALL : (BSDF_ALL & ~BSDF_SPECULAR);
+            LightSample ls;
+            const bool delta = sample_li(sv, Lt, si, ulight, ls);
+            if (ls.pdf > 0 && !is_black(ls.Li)) {
+                const Spec fv = bsdf_f(f, si.wo, ls.wi, fl, RECORD ? &evs : nullptr) * absdot(ls.wi, si.sn);
+                const float spdf = bsdf_pdf(f, si.wo, ls.wi, fl, RECORD ? &evs : nullptr);
+                if (!is_black(fv)) {
+                    const V3 org = offset_origin(si.p, si.perr, si.n, ls.p1 - si.p);
+                    const V3 tgt = offset_origin(ls.p1, ls.perr1, ls.n1, org - ls.p1);
+                    Spec c;
+                    if (delta) {
+                        c = fv * ls.Li / ls.pdf;
+                    } else {
+                        const float fp = 1 * ls.pdf, gp = 1 * spdf;
+                        const float wgt = (fp * fp) / (fp * fp + gp * gp);
+                        c = fv * ls.Li * wgt / ls.pdf;
+                    }
+                    const V3 dir = tgt - org;
+                    st.sh_o[p] = make_float4(org.x, org.y, org.z, 0.f);
+                    st.sh_d[p] = make_float4(dir.x, dir.y, dir.z, 1 - kShadowEps);
+                    st.sh_c[p] = make_float4(c.r, c.g, c.b, is_black(ls.Li) ? 0.f : 1.f);
+                    pend |= WF_VIS;
+                }
+            }
+            if (!delta) {
+                V3 wi = ls.wi;
+                float spdf = 0;
+                uint32_t stype = 0;
+                EvSink cap{nullptr, 0};
+                Spec fv = bsdf_sample(f, si.wo, wi, uscat, spdf, fl, stype, RECORD ? &cap : nullptr);
+                ev_mis = cap.cap;
+                fv = fv * absdot(wi, si.sn);
+                const bool sampled_spec = (stype & BSDF_SPECULAR) != 0;
+                if (!is_black(fv) && spdf > 0) {
+                    float wgt = 1;
+                    bool skip = false;
+                    if (!sampled_spec) {
+                        float lp;
+                        if (Lt.kind == 0) lp = area_pdf(sv, Lt, si.p, si.perr, si.n, wi);
+                        else if (Lt.kind == 1) lp = sph_pdf_infinite(wi);
+                        else lp = 0.0f;
+                        if (lp == 0) skip = true;
+                        else {
+                            const float fp = 1 * spdf, gp = 1 * lp;
+                            wgt = (fp * fp) / (fp * fp + gp * gp);
+                        }
+                    }
+                    if (!skip) {
+                        const V3 org = offset_origin(si.p, si.perr, si.n, wi);
+                        st.mis_o[p] = make_float4(org.x, org.y, org.z, 0.f);
+                        st.mis_d[p] = make_float4(wi.x, wi.y, wi.z, 0.f);
+                        st.mis_fv[p] = make_float4(fv.r, fv.g, fv.b, wgt);
+                        st.mis_x[p] = make_float4(spdf, __int_as_float(off), 0.f, 0.f);
+                        pend |= WF_MIS;
+                    }
+                }
+            }
+        }
+        // path BSDF sample, throughput, spawn, Russian roulette (PathTracingIntegrator.cuh:80-103)
+        V3 wi = v3(0, 0, 0);
+        float pdf = 0;
+        uint32_t stype = 0;
+        const F2 ub = rng_2d(rng);
+        EvSink cap{nullptr, 0};
+        const Spec fv = bsdf_sample(f, si.wo, wi, ub, pdf, BSDF_ALL, stype, RECORD ? &cap : nullptr);
+        ev_main = cap.cap;
+        if (is_black(fv) || pdf == 0) {
+            done = true;
+        } else {
+            specular = (stype & BSDF_SPECULAR) != 0;
+            beta = beta * (fv * absdot(wi, si.sn) / pdf);
+            const V3 no = offset_origin(si.p, si.perr, si.n, wi);
+            st.ro[p] = make_float4(no.x, no.y, no.z, 0.f);
+            st.rd[p] = make_float4(wi.x, wi.y, wi.z, 0.f);
+            if (bounce >= rp.rr_start) {
+                const float qq = fmaxf(0.05f, 1 - lum(beta));
+                if (rng_1d(rng) < qq) done = true;
+                else beta = beta / (1 - qq);
+            }
+            if (bounce + 1 >= rp.max_bounce) done = true;
+        }
+    }
+    const int pos_s = warp_push(&st.counts[2], (pend & WF_VIS) != 0);
+    if (pos_s >= 0) st.q_shadow[pos_s] = p;
+    const int pos_m = warp_push(&st.counts[3], (pend & WF_MIS) != 0);
+    if (pos_m >= 0) st.q_mis[pos_m] = p;
+    st.pend[p] = pend | (done ? WF_DONE : 0u);
+    st.draw[p] = rng.draw;
+    st.flags[p] = ((uint32_t)(bounce + 1) << 8) | (specular ? 1u : 0u);
+    st.beta[p] = make_float4(beta.r, beta.g, beta.b, 0.f);
+    st.L[p] = make_float4(L.r, L.g, L.b, 0.f);
+    if (RECORD) {
+        st.sig[p] = sig;
+        st.ev_mis[p] = ev_mis;
+        st.ev_main[p] = ev_main;
+    }
+}
+
+// finalize: direct light of the bounce, deferred parity events, film or requeue.
+template <bool RECORD>
+__global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, const RenderParams rp, WfState st,
+                                                          const int32_t* __restrict__ q, const uint32_t* __restrict__ cnt,
+                                                          int32_t* q_next, uint32_t* c_next) {
+    const int t = blockIdx.x * kWfBlock + threadIdx.x;
+    if (t >= (int)*cnt) return;
+    const int p = q[t];
+    const uint32_t pend = st.pend[p];
+    float4 l4 = st.L[p];
+    Spec L{l4.x, l4.y, l4.z};
+    uint64_t sig = RECORD ? st.sig[p] : 0ull;
+    if (pend & WF_NEE) {
+        Spec Ld = spec(0.0f);
+        if (pend & WF_VIS) {
+            const uint32_t vis = st.vis[p];
+            if (RECORD) fnv_mix(sig, 0x300000000ull + vis);
+            const float4 c = st.sh_c[p];
+            if (vis && c.w != 0.f) Ld = Ld + Spec{c.x, c.y, c.z};
+        }
+        if (RECORD && st.ev_mis[p]) fnv_mix(sig, st.ev_mis[p]);
+        if (pend & WF_MIS) {
+            if (RECORD) fnv_mix(sig, 0x200000000ull + (uint64_t)st.mis_hit[p]);
+            const float4 c = st.ld_mis[p];
+            if (c.w != 0.f) Ld = Ld + Spec{c.x, c.y, c.z};
+        }
+        const float4 nb = st.nee_beta[p];
+        L = L + Spec{nb.x, nb.y, nb.z} * (Ld / nb.w);
+    }
+    if (RECORD && st.ev_main[p]) fnv_mix(sig, st.ev_main[p]);
+    if (RECORD) {
+        st.sig[p] = sig;
+        st.ev_mis[p] = 0;
+        st.ev_main[p] = 0;
+    }
+    if (!(pend & WF_DONE)) {
+        st.L[p] = make_float4(L.r, L.g, L.b, 0.f);
+        const int pos = warp_push(c_next, true);
+        q_next[pos] = p;
+        return;
+    }
+    // Camera::addSample (Camera.cu:192-218) into FP64 sums
+    const float2 pf = st.pf[p];
+    const int W = sv.width, H = sv.height;
+    const int px0 = max((int)ceilf(pf.x - 1.0f), 0), py0 = max((int)ceilf(pf.y - 1.0f), 0);
+    const int px1 = min((int)floorf(pf.x + 1.0f) + 1, W), py1 = min((int)floorf(pf.y + 1.0f) + 1, H);
+    for (int y = py0; y < py1; ++y)
+        for (int x = px0; x < px1; ++x) {
+            const float fdx = fabsf((x - pf.x - 0.5f) * 1.0f * 16);
+            const float fdy = fabsf((y - pf.y - 0.5f) * 1.0f * 16);
+            const int ix = min((int)floorf(fdx), 15), iy = min((int)floorf(fdy), 15);
+            const float wgt = __ldg(sv.filter + iy * 16 + ix);
+            const Spec c = L * wgt;
+            double* fp = rp.film + 4 * ((size_t)y * W + x);
+            atomicAdd(fp + 0, (double)c.r);
+            atomicAdd(fp + 1, (double)c.g);
+            atomicAdd(fp + 2, (double)c.b);
+            atomicAdd(fp + 3, (double)wgt);
+        }
+    if (RECORD) {
+        const int id = st.pix[p];
+        const int i = id % W, j = id / W;
+        const size_t k = ((size_t)(j - rp.y0) * (rp.x1 - rp.x0) + (i - rp.x0)) * rp.spp + st.smp[p];
+        rp.sample_L[3 * k + 0] = L.r;
+        rp.sample_L[3 * k + 1] = L.g;
+        rp.sample_L[3 * k + 2] = L.b;
+        rp.sample_sig[k] = sig;
+    }
+    st.pix[p] = -1;
+    const int pos = warp_push(&st.counts[4], true);
+    st.q_free[pos] = p;
+}
+
+// Every slot starts free; counts (zeroed by the host) get the free-list size.
+__global__ void k_wf_init_free(int32_t* q_free, uint32_t* counts, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) q_free[t] = n - 1 - t;
+    if (t == 0) counts[4] = (uint32_t)n;
+}
+
+}  // namespace
+}  // namespace lts

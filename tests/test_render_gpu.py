@@ -37,14 +37,14 @@ def ctx(built_lib):
 
 
 @pytest.mark.parametrize("kind", ["box_sphere", "materials"])
-@pytest.mark.parametrize("bvh_mode", [0, 1])
-def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode):
+@pytest.mark.parametrize("bvh_mode,integrator", [(0, 0), (1, 0), (1, 1)])
+def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator):
     import lighttransportsimulation_gb300 as lts
     d, sc, sub = scene_dirs[kind]
     fx = np.load(os.path.join(GOLDEN, f"render_{kind}.npz"))
     w, h, spp, maxb, rr, seed, x0, y0, x1, y1 = (int(v) for v in fx["meta"])
     s = lts.Scene.parse(ctx, d, sc, sub, w, h)
-    integ = lts.PathTracingIntegrator(maxb, rr, s, bvh_mode=bvh_mode)
+    integ = lts.PathTracingIntegrator(maxb, rr, s, integrator=integrator, bvh_mode=bvh_mode)
     r = integ.render(spp, seed, crop=(x0, y0, x1, y1), record=True, film=False)
     L = r["L"].reshape(-1, 3)
     sig = r["sig"].reshape(-1)
@@ -54,7 +54,7 @@ def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode):
     div = 1.0 - same.mean()
     ok = np.all(np.abs(L - Lr) <= RTOL * np.abs(Lr) + ATOL, axis=1)
     mism = 1.0 - ok[same].mean()
-    print(f"{kind} bvh={bvh_mode}: samples={len(sig)} divergent={div:.5f} mismatched={mism:.6f} "
+    print(f"{kind} bvh={bvh_mode} integrator={integrator}: samples={len(sig)} divergent={div:.5f} mismatched={mism:.6f} "
           f"maxrel={np.max(np.abs(L - Lr)[same] / (np.abs(Lr[same]) + 1e-6)):.3g}")
     assert np.isfinite(L).all()
     assert div <= MAX_DIVERGENT
@@ -64,18 +64,35 @@ def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode):
 
 
 @pytest.mark.parametrize("kind", ["box_sphere", "materials"])
-def test_film_matches_reference(ctx, scene_dirs, kind):
+@pytest.mark.parametrize("integrator", [0, 1])
+def test_film_matches_reference(ctx, scene_dirs, kind, integrator):
     """Full-frame film (Kahan FP32 + FP64 resolve) against the reference's single-thread film."""
     import lighttransportsimulation_gb300 as lts
     d, sc, sub = scene_dirs[kind]
     fx = np.load(os.path.join(GOLDEN, f"film_{kind}.npz"))
     w, h, spp, maxb, rr, seed = (int(v) for v in fx["meta"])
     s = lts.Scene.parse(ctx, d, sc, sub, w, h)
-    r = lts.PathTracingIntegrator(maxb, rr, s).render(spp, seed)
+    r = lts.PathTracingIntegrator(maxb, rr, s, integrator=integrator).render(spp, seed)
     film = r["film"].reshape(-1)
     ref = fx["film"].reshape(-1)
     err = np.abs(film - ref)
     rel_rmse = np.sqrt(np.mean(err ** 2)) / np.sqrt(np.mean(ref ** 2))
-    print(f"{kind}: film rel-RMSE vs reference {rel_rmse:.3g}, pixels off by >1e-3 rel: "
+    print(f"{kind} integrator={integrator}: film rel-RMSE vs reference {rel_rmse:.3g}, pixels off by >1e-3 rel: "
           f"{np.mean(err > 1e-3 * np.abs(ref) + 1e-5):.4f}")
     assert rel_rmse < 5e-3
+
+
+def test_wavefront_equals_megakernel_bit_for_bit(ctx, scene_dirs):
+    """Same device functions, different schedule: every sample takes the same decisions (identical
+    event hashes); radiance differs only by FMA contraction across kernel boundaries."""
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs["materials"]
+    s = lts.Scene.parse(ctx, d, sc, sub, 96, 96)
+    a = lts.PathTracingIntegrator(8, 3, s, integrator=0).render(4, 11, crop=(0, 0, 96, 96), record=True, film=False)
+    b = lts.PathTracingIntegrator(8, 3, s, integrator=1).render(4, 11, crop=(0, 0, 96, 96), record=True, film=False)
+    assert np.array_equal(a["sig"], b["sig"])
+    La, Lb = a["L"].reshape(-1, 3), b["L"].reshape(-1, 3)
+    ok = np.all(np.abs(La - Lb) <= RTOL * np.abs(La) + ATOL, axis=1)
+    print(f"wavefront vs megakernel: bit-equal {np.mean(np.all(La == Lb, axis=1)):.4f}, within 1e-4 {ok.mean():.5f}")
+    assert 1.0 - ok.mean() <= MAX_MISMATCH
+    assert np.all(np.abs(La - Lb) <= DRIFT_RTOL * np.abs(La) + 1e-5)
