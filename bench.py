@@ -254,10 +254,29 @@ def run_gpu(args, wl):
     ms = barrier_max(dist, ms)
     value = world * paths / (ms * 1e-3) / 1e6
 
-    # one counted render for the roofline's algorithmic bytes (same kernel, same launch)
+    # one counted render for the roofline's algorithmic bytes (same kernels, same launches)
     r = integ.render(wl["spp"], wl["seed"], film=False)
-    alg_bytes = 64.0 * r["node_visits"] + 48.0 * r["tri_tests"] + 32.0 * paths
-    achieved = alg_bytes / (r["render_ms"] * 1e-3) / 1e9
+    mr = ctx.metrics()
+    stages = None
+    if args.integrator == 0:
+        kernel, kernel_ms, kernel_launches = "k_pathtrace", r["render_ms"], 1
+        alg_bytes = 64.0 * r["node_visits"] + 48.0 * r["tri_tests"] + 32.0 * paths
+        alg_text = "64 B per BVH node visit + 48 B per triangle test + 32 B film per path"
+    else:
+        names = ["generate", "extend", "shade", "shadow", "mis", "finalize"]
+        stages = {n: round(mr.render_stage_ms[k], 3) for k, n in enumerate(names)}
+        # per traversal kernel: nodes, triangles, plus the path-state bytes it reads and writes per ray
+        state = {"extend": 56.0, "shadow": 40.0, "mis": 88.0}
+        kinds = {"extend": 0, "shadow": 1, "mis": 2}
+        kernel = max(kinds, key=lambda n: mr.render_stage_ms[names.index(n)])
+        k = kinds[kernel]
+        kernel_ms = mr.render_stage_ms[names.index(kernel)]
+        kernel_launches = mr.render_iterations
+        alg_bytes = (64.0 * mr.kind_node_visits[k] + 48.0 * mr.kind_tri_tests[k] + state[kernel] * mr.kind_rays[k])
+        alg_text = (f"64 B per BVH node visit + 48 B per triangle test + {int(state[kernel])} B path state per ray "
+                    f"(k_wf_{kernel})")
+        kernel = "k_wf_" + kernel
+    achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
 
     # end to end through the public API: upload scene (H2D), build, render, read film (D2H)
     h2d = scene.info["triangles"] * 48 + scene.info["triangles"] * 16 * 2
@@ -292,8 +311,10 @@ def run_gpu(args, wl):
                     "seconds_per_step": round(e2e_s, 4)},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
-                         "kernel": "k_pathtrace", "peak_kind": peak_kind,
-                         "algorithmic": "64 B per BVH node visit + 48 B per triangle test + 32 B film per path"},
+                         "kernel": kernel, "launches_per_step": kernel_launches,
+                         "kernel_ms_per_step": round(kernel_ms, 3), "peak_kind": peak_kind,
+                         "algorithmic": alg_text, "algorithmic_bytes_per_step": alg_bytes},
+            "stage_ms": stages,
             "traversal": {"node_visits": r["node_visits"], "tri_tests": r["tri_tests"], "rays": r["rays"]},
             "lbvh": lbvh,
             "cpu_baseline": cpu,

@@ -181,6 +181,13 @@ int lts_write_image(const char* path, const float* rgb, int32_t width, int32_t h
 int lts_debug_trace_sample(lts_ctx* ctx, int64_t crop_sample_index);
 int lts_debug_trace_get(lts_ctx* ctx, float* out_64x16);
 
+/* Tuning knobs of the wavefront integrator (no counterpart in the reference).  Keys:
+ *   "wavefront_pool"          path-state pool capacity in paths (0: automatic, 2^21)
+ *   "wavefront_sample_chunk"  finished-sample buffer capacity in samples (0: automatic, 2^27);
+ *                             samples per pixel are rendered in chunks that fit it
+ * Unknown keys and negative values return LTS_ERR_ARG. */
+int lts_set_option(lts_ctx* ctx, const char* key, int64_t value);
+
 /* ---------------------------------------------------------------- metrics */
 typedef struct {
     double bvh_build_ms;  /* device time of the last LBVH build */
@@ -191,6 +198,11 @@ typedef struct {
     int32_t kernel_launches; /* kernels launched by the last build + render */
     int32_t render_launches; /* kernels launched by the last render alone */
     int32_t render_iterations; /* wavefront: stage-loop iterations of the last render (1 for the megakernel) */
+    /* wavefront: device ms per stage (generate, extend, shade, shadow, mis, finalize) of the last
+     * render, and per traversal kind (extend, shadow, mis) its rays, node visits and triangle tests
+     * (filled by a synchronous lts_render); zero for the megakernel */
+    double render_stage_ms[6];
+    double kind_rays[3], kind_node_visits[3], kind_tri_tests[3];
 } lts_metrics;
 int lts_get_metrics(lts_ctx* ctx, lts_metrics* out);
 

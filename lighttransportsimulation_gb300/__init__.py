@@ -35,7 +35,7 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_scene_get_light_distribution", "lts_bvh_build", "lts_bvh_build_triangles",
            "lts_bvh_build_device_async", "lts_bvh_dump_get", "lts_render", "lts_render_async", "lts_film_get",
            "lts_write_image", "lts_get_metrics", "lts_bvh_build_noalloc", "lts_debug_trace_sample",
-           "lts_debug_trace_get"]
+           "lts_debug_trace_get", "lts_set_option"]
 
 
 class LtsError(RuntimeError):
@@ -78,7 +78,9 @@ class Metrics(ctypes.Structure):
     _fields_ = [("bvh_build_ms", ctypes.c_double), ("bvh_stage_ms", ctypes.c_double * 5),
                 ("render_ms", ctypes.c_double), ("paths", ctypes.c_double), ("rays", ctypes.c_double),
                 ("device_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int32),
-                ("render_launches", ctypes.c_int32), ("render_iterations", ctypes.c_int32)]
+                ("render_launches", ctypes.c_int32), ("render_iterations", ctypes.c_int32),
+                ("render_stage_ms", ctypes.c_double * 6), ("kind_rays", ctypes.c_double * 3),
+                ("kind_node_visits", ctypes.c_double * 3), ("kind_tri_tests", ctypes.c_double * 3)]
 
 
 _lib = None
@@ -112,6 +114,7 @@ def library():
             "lts_bvh_build_noalloc": (I, [P, I, I, I, P, P, P, P, P, P]),
             "lts_debug_trace_sample": (I, [P, ctypes.c_int64]),
             "lts_debug_trace_get": (I, [P, P]),
+            "lts_set_option": (I, [P, ctypes.c_char_p, ctypes.c_int64]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -154,6 +157,10 @@ class Context:
 
     def stream(self):
         return self.lib.lts_stream(self.h)
+
+    def set_option(self, key, value):
+        """Wavefront tuning knobs ("wavefront_pool", "wavefront_sample_chunk"); needs a loaded scene."""
+        self.check(self.lib.lts_set_option(self.h, key.encode(), int(value)))
 
     def metrics(self):
         m = Metrics()

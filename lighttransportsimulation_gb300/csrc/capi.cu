@@ -427,6 +427,21 @@ int lts_write_image(const char* path, const float* rgb, int32_t w, int32_t h, in
     return LTS_OK;
 }
 
+int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
+    if (!ctx || !key) return LTS_ERR_ARG;
+    if (value < 0) return fail(ctx, LTS_ERR_ARG, "option value must be >= 0");
+    if (!ctx->tracer) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    if (!strcmp(key, "wavefront_pool")) {
+        if (value >= (1ll << 30)) return fail(ctx, LTS_ERR_ARG, "wavefront_pool too large");
+        ctx->tracer->wf_pool = (long)value;
+    } else if (!strcmp(key, "wavefront_sample_chunk")) {
+        ctx->tracer->wf_sample_cap = (long)value;
+    } else {
+        return fail(ctx, LTS_ERR_ARG, std::string("unknown option ") + key);
+    }
+    return LTS_OK;
+}
+
 int lts_debug_trace_sample(lts_ctx* ctx, int64_t k) {
     if (!ctx) return LTS_ERR_ARG;
     if (!ctx->tracer) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
@@ -448,6 +463,12 @@ int lts_get_metrics(lts_ctx* ctx, lts_metrics* out) {
     out->kernel_launches = (ctx->bvh ? ctx->bvh->launches : 0) + (ctx->tracer ? ctx->tracer->last_launches : 0);
     out->render_launches = ctx->tracer ? ctx->tracer->last_launches : 0;
     out->render_iterations = ctx->tracer ? ctx->tracer->last_iterations : 0;
+    for (int k = 0; k < 6; ++k) out->render_stage_ms[k] = ctx->tracer ? ctx->tracer->last_stage_ms[k] : 0.0;
+    for (int k = 0; k < 3; ++k) {
+        out->kind_rays[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k] : 0.0;
+        out->kind_node_visits[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k + 1] : 0.0;
+        out->kind_tri_tests[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k + 2] : 0.0;
+    }
     return LTS_OK;
 }
 

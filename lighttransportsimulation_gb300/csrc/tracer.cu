@@ -386,7 +386,7 @@ void Tracer::free_all() {
         if (p) dev_free(p);
         p = nullptr;
     }
-    wf_cap_ = 0;
+    wf_cap_ = wf_fs_cap_ = 0;
     film_cap_ = rec_cap_ = 0;
     leaf_serial_ = 0;
 }
@@ -396,6 +396,8 @@ Tracer::~Tracer() {
     if (wf_counts_host_) cudaFreeHost(wf_counts_host_);
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
+    for (cudaEvent_t e : wf_ev_)
+        if (e) cudaEventDestroy(e);
 }
 
 std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
@@ -478,7 +480,7 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
     if (!(e = upload(bufs_[8], sc.light_func, s)).empty()) return e;
     if (!(e = upload(bufs_[9], sc.light_cdf, s)).empty()) return e;
     if (!(e = upload(bufs_[10], filt, s)).empty()) return e;
-    TRY(dev_alloc((void**)&counters_, 64));
+    TRY(dev_alloc((void**)&counters_, 128));
     view_ = SceneView{};
     view_.ntri = nt;
     view_.nlight = (int)lights.size();
@@ -535,7 +537,7 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
         film_cap_ = film_bytes;
     }
     TRY(cudaMemsetAsync(film_, 0, film_bytes, s));
-    TRY(cudaMemsetAsync(counters_, 0, 64, s));
+    TRY(cudaMemsetAsync(counters_, 0, 128, s));
     const long ns = (long)(x1 - x0) * (y1 - y0) * d.spp;
     *crop_samples = ns;
     if (d.record_samples) {
@@ -599,6 +601,7 @@ std::string Tracer::render_async(const HostScene& sc, const Lbvh& bvh, const lts
     TRY(cudaGetLastError());
     last_launches = 1;
     last_iterations = 1;
+    for (double& x : last_stage_ms) x = 0;
     last_paths = (double)ns;
     return "";
 }
@@ -606,23 +609,40 @@ std::string Tracer::render_async(const HostScene& sc, const Lbvh& bvh, const lts
 std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                                      uint32_t* d_err, const RenderParams& rp, const SceneView& sv, long total) {
     (void)sc;
-    (void)d;
     (void)d_err;
-    const long P = std::max<long>(1, std::min<long>(total, wf_pool > 0 ? wf_pool : (1l << 21)));
+    (void)total;
+    // Samples per pixel are rendered in chunks whose finished samples fit the sample buffer; the
+    // path pool drains at the end of each chunk and the chunk is gathered into the film.
+    const long npix = (long)(rp.x1 - rp.x0) * (rp.y1 - rp.y0);
+    const long cap = wf_sample_cap > 0 ? wf_sample_cap : (1l << 27);
+    const int chunk = (int)std::max<long>(1, std::min<long>(d.spp, cap / npix));
+    const long chunk_total = npix * chunk;
+    if (chunk_total >= (1l << 31)) return "wavefront: crop too large for one sample chunk";
+    const long P = std::max<long>(1, std::min<long>(chunk_total, wf_pool > 0 ? wf_pool : (1l << 21)));
     WfState st{};
     if (wf_cap_ < P) {
-        for (void*& p : wf_bufs_) {
-            if (p) dev_free(p);
-            p = nullptr;
+        for (int k = 0; k < 33; ++k) {
+            if (wf_bufs_[k]) dev_free(wf_bufs_[k]);
+            wf_bufs_[k] = nullptr;
         }
         wf_cap_ = 0;
         const size_t n = (size_t)P;
         const size_t sizes[] = {4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n,                       // pix smp draw flags pend vis
                                 16 * n, 16 * n, 16 * n, 16 * n, 8 * n, 8 * n, 4 * n, 16 * n,  // ro rd beta L pf sig hprim huvi
                                 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n,  // sh_* mis_* ld nee
-                                8 * n, 8 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 64};
+                                8 * n, 8 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 64,  // ev mis_hit queues counts
+                                4 * n};                                                          // wid
         for (size_t k = 0; k < sizeof sizes / sizeof sizes[0]; ++k) TRY(dev_alloc(&wf_bufs_[k], sizes[k]));
         wf_cap_ = P;
+    }
+    if (wf_fs_cap_ < chunk_total) {
+        dev_free(wf_bufs_[33]);
+        dev_free(wf_bufs_[34]);
+        wf_bufs_[33] = wf_bufs_[34] = nullptr;
+        wf_fs_cap_ = 0;
+        TRY(dev_alloc(&wf_bufs_[33], 16 * (size_t)chunk_total));
+        TRY(dev_alloc(&wf_bufs_[34], 4 * (size_t)chunk_total));
+        wf_fs_cap_ = chunk_total;
     }
     if (!wf_counts_host_) TRY(cudaMallocHost((void**)&wf_counts_host_, 64));
     void** b = wf_bufs_;
@@ -635,45 +655,86 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
     st.ld_mis = (float4*)b[21]; st.nee_beta = (float4*)b[22];
     st.ev_mis = (uint64_t*)b[23]; st.ev_main = (uint64_t*)b[24]; st.mis_hit = (int32_t*)b[25];
     st.q_a = (int32_t*)b[26]; st.q_b = (int32_t*)b[27]; st.q_shadow = (int32_t*)b[28]; st.q_mis = (int32_t*)b[29];
-    st.q_free = (int32_t*)b[30]; st.counts = (uint32_t*)b[31];
+    st.q_free = (int32_t*)b[30]; st.counts = (uint32_t*)b[31]; st.wid = (int32_t*)b[32];
+    st.fs_L = (float4*)b[33]; st.fs_y = (float*)b[34];
     TRY(cudaMemsetAsync(st.counts, 0, 64, s));
     if (rp.sample_sig) {
         TRY(cudaMemsetAsync(st.ev_mis, 0, 8 * (size_t)P, s));
         TRY(cudaMemsetAsync(st.ev_main, 0, 8 * (size_t)P, s));
     }
-    const int grid = (int)((P + kWfBlock - 1) / kWfBlock);
-    k_wf_init_free<<<grid, kWfBlock, 0, s>>>(st.q_free, st.counts, (int)P);
+    auto blocks = [](long n) { return (unsigned)((n + kWfBlock - 1) / kWfBlock); };
+    k_wf_init_free<<<blocks(P), kWfBlock, 0, s>>>(st.q_free, st.counts, (int)P);
     TRY(cudaEventRecord(ev0_, s));
     int32_t *cur = st.q_a, *next = st.q_b;
     uint32_t *c_cur = st.counts + 0, *c_next = st.counts + 1;
+    int i_cur = 0;
     const bool rec = rp.sample_sig != nullptr;
-    int it = 0, launches = 0;
-    for (;; ++it) {
-        k_wf_generate<<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, total);
-        k_wf_generate_done<<<1, 1, 0, s>>>(st, total);
-        TRY(cudaMemsetAsync(c_next, 0, 4, s));
-        TRY(cudaMemsetAsync(st.counts + 2, 0, 8, s));
-        k_wf_extend<<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, bvh.n);
-        if (rec) k_wf_shade<true><<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur);
-        else k_wf_shade<false><<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur);
-        k_wf_shadow<<<grid, kWfBlock, 0, s>>>(sv, rp, st, bvh.n);
-        k_wf_mis<<<grid, kWfBlock, 0, s>>>(sv, rp, st, bvh.n);
-        if (rec) k_wf_finalize<true><<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, next, c_next);
-        else k_wf_finalize<false><<<grid, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, next, c_next);
-        launches += 8;
+    int iters = 0, launches = 1;
+    for (cudaEvent_t& e : wf_ev_)
+        if (!e) TRY(cudaEventCreate(&e));
+    for (double& x : last_stage_ms) x = 0;
+    const dim3 gblock(32, 4);
+    for (int s0 = 0; s0 < d.spp; s0 += chunk) {
+        const int nsc = std::min(chunk, d.spp - s0);
+        const long ctot = npix * nsc;
+        long generated = 0;
+        uint32_t nfree = (uint32_t)P, nnext = 0;
+        for (;; ++iters) {
+            const uint32_t take = (uint32_t)std::min<long>(nfree, ctot - generated);
+            const long ncur = (long)nnext + take;
+            if (ncur == 0) break;
+            if (iters > 1000000) return "wavefront did not converge";
+            TRY(cudaEventRecord(wf_ev_[0], s));
+            if (take) {
+                k_wf_generate<<<blocks(take), kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, generated, nfree, take, s0, npix);
+                ++launches;
+            }
+            TRY(cudaEventRecord(wf_ev_[1], s));
+            const unsigned g = blocks(ncur);
+            k_wf_extend<<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, c_next, bvh.n);
+            TRY(cudaEventRecord(wf_ev_[2], s));
+            if (rec) k_wf_shade<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur);
+            else k_wf_shade<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur);
+            TRY(cudaEventRecord(wf_ev_[3], s));
+            k_wf_shadow<<<g, kWfBlock, 0, s>>>(sv, rp, st, bvh.n);
+            TRY(cudaEventRecord(wf_ev_[4], s));
+            k_wf_mis<<<g, kWfBlock, 0, s>>>(sv, rp, st, bvh.n);
+            TRY(cudaEventRecord(wf_ev_[5], s));
+            if (rec) k_wf_finalize<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, next, c_next);
+            else k_wf_finalize<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, next, c_next);
+            TRY(cudaEventRecord(wf_ev_[6], s));
+            launches += 5;
+            TRY(cudaGetLastError());
+            TRY(cudaMemcpyAsync(wf_counts_host_, st.counts, 32, cudaMemcpyDeviceToHost, s));
+            TRY(cudaStreamSynchronize(s));
+            for (int k = 0; k < 6; ++k) {
+                float ms = 0;
+                TRY(cudaEventElapsedTime(&ms, wf_ev_[k], wf_ev_[k + 1]));
+                last_stage_ms[k] += ms;
+            }
+            generated += take;
+            nnext = wf_counts_host_[1 - i_cur];
+            nfree = wf_counts_host_[4];
+            std::swap(cur, next);
+            std::swap(c_cur, c_next);
+            i_cur = 1 - i_cur;
+        }
+        if (nfree != (uint32_t)P) return "wavefront: path pool did not drain";
+        TRY(cudaEventRecord(wf_ev_[0], s));
+        const dim3 ggrid((unsigned)((std::min(rp.x1 + 2, sv.width) - rp.x0 + 31) / 32),
+                         (unsigned)((std::min(rp.y1 + 2, sv.height) - rp.y0 + 3) / 4));
+        k_film_gather<<<ggrid, gblock, 0, s>>>(sv, rp, st.fs_L, st.fs_y, nsc, npix);
+        TRY(cudaEventRecord(wf_ev_[6], s));
+        ++launches;
         TRY(cudaGetLastError());
-        TRY(cudaMemcpyAsync(wf_counts_host_, st.counts, 32, cudaMemcpyDeviceToHost, s));
-        TRY(cudaStreamSynchronize(s));
-        const uint32_t nnext = wf_counts_host_[it & 1 ? 0 : 1];
-        const long generated = (long)wf_counts_host_[5];
-        if (nnext == 0 && generated >= total) break;
-        if (it > 100000) return "wavefront did not converge";
-        std::swap(cur, next);
-        std::swap(c_cur, c_next);
+        TRY(cudaEventSynchronize(wf_ev_[6]));
+        float ms = 0;
+        TRY(cudaEventElapsedTime(&ms, wf_ev_[0], wf_ev_[6]));
+        last_stage_ms[5] += ms;
     }
     TRY(cudaEventRecord(ev1_, s));
     last_launches = launches;
-    last_iterations = it + 1;
+    last_iterations = iters;
     return "";
 }
 
@@ -685,8 +746,9 @@ std::string Tracer::render(const HostScene& sc, const Lbvh& bvh, const lts_rende
     float ms = 0;
     TRY(cudaEventElapsedTime(&ms, ev0_, ev1_));
     last_ms = ms;
-    unsigned long long cnt[3] = {0, 0, 0};
-    TRY(cudaMemcpy(cnt, counters_, 24, cudaMemcpyDeviceToHost));
+    unsigned long long cnt[12] = {0};
+    TRY(cudaMemcpy(cnt, counters_, sizeof cnt, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 9; ++k) last_kind_work[k] = (double)cnt[3 + k];
     last_rays = (double)cnt[0];
     last_node_visits = (double)cnt[1];
     last_tri_tests = (double)cnt[2];

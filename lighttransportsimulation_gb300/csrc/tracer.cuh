@@ -78,11 +78,18 @@ class Tracer {
     double last_ms = 0, last_paths = 0, last_rays = 0, last_node_visits = 0, last_tri_tests = 0;
     // Path-pool capacity of the wavefront integrator (0: automatic).
     long wf_pool = 0;
+    // Finished-sample buffer capacity of the wavefront film gather, in samples (0: 2^27).
+    long wf_sample_cap = 0;
     int last_iterations = 0;
     // Parity debugging: the record-mode render writes the events of this crop sample index.
     long trace_sample_ = -1;
     float* trace_ = nullptr;
     int last_launches = 0;
+    // Wavefront: device time per stage (generate, extend, shade, shadow, mis, finalize) summed over
+    // the loop's iterations, and rays / node visits / triangle tests per traversal kind (extend,
+    // shadow, mis).  Zero for the megakernel.
+    double last_stage_ms[6] = {0, 0, 0, 0, 0, 0};
+    double last_kind_work[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 
    private:
     std::string prepare(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
@@ -91,8 +98,9 @@ class Tracer {
     std::string render_wavefront(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                                  uint32_t* d_err, const RenderParams& rp, const SceneView& sv, long total);
     void* wf_bufs_[40] = {nullptr};
-    long wf_cap_ = 0;
+    long wf_cap_ = 0, wf_fs_cap_ = 0;
     uint32_t* wf_counts_host_ = nullptr;
+    cudaEvent_t wf_ev_[7] = {nullptr};
     SceneView view_{};
     void* bufs_[16] = {nullptr};
     float4* leaf_v_ = nullptr;

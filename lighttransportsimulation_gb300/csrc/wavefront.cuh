@@ -9,8 +9,11 @@
 //   shadow    any-hit traversal of the NEE shadow rays
 //   mis       closest-hit traversal of the MIS BSDF rays, light radiance where they land
 //   finalize  adds the bounce's direct light in the reference's order (Ld = light part + MIS
-//             part, L += beta * Ld / lightPdf), mixes the deferred parity events, then splats
-//             finished samples to the FP64 film and frees their slot, or requeues the path
+//             part, L += beta * Ld / lightPdf), mixes the deferred parity events, then stores a
+//             finished sample (radiance, film position) and frees its slot, or requeues the path
+//   gather    after a chunk of samples per pixel has finished: one thread per film pixel sums the
+//             filter-weighted samples of its 3x3 source pixels in a fixed order (compensated FP32,
+//             then added to the FP64 film), so the film has no atomics and is reproducible
 //
 // The sampler is keyed per (pixel, sample) with a draw counter kept in the path state, so a path
 // produces exactly the draws of the megakernel (PathTracingIntegrator.cuh:41-99) in any order of
@@ -25,7 +28,7 @@ constexpr int kWfBlock = 128;
 constexpr uint64_t kSigBasis = 0xcbf29ce484222325ull;
 
 struct WfState {
-    int32_t *pix, *smp;
+    int32_t *pix, *smp, *wid;  // pixel, sample, index of the sample within its chunk
     uint32_t *draw, *flags, *pend, *vis;
     float4 *ro, *rd, *beta, *L;
     float2* pf;
@@ -38,7 +41,9 @@ struct WfState {
     uint64_t *ev_mis, *ev_main;
     int32_t* mis_hit;
     int32_t *q_a, *q_b, *q_shadow, *q_mis, *q_free;
-    uint32_t* counts;  // [0] q_a size, [1] q_b size, [2] shadow, [3] mis, [4] free, [5] generated
+    uint32_t* counts;  // [0] q_a size, [1] q_b size, [2] shadow, [3] mis, [4] free
+    float4* fs_L;      // finished samples of the chunk: radiance rgb, film x (chunk index order)
+    float* fs_y;       // film y
 };
 
 // Resume a (pixel, sample) stream at draw `draw` (regenerates the current Philox block).
@@ -81,19 +86,18 @@ __device__ __forceinline__ void camera_ray(const SceneView& sv, float pfx, float
     ryd = rd + (dy0 - rd) * spp_scale;
 }
 
-// generate: pops free slots and starts new samples (sample-major over the crop's pixels).
+// generate: pops `take` free slots and starts samples gen0 .. gen0 + take - 1 of the chunk
+// (sample-major over the crop's pixels: w = (s - s0) * npix + pixel).
 __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, const RenderParams rp, WfState st,
-                                                          int32_t* q_cur, uint32_t* c_cur, long total) {
+                                                          int32_t* q_cur, uint32_t* c_cur, long gen0, uint32_t nfree,
+                                                          uint32_t take, int s0, long npix) {
     const long t = (long)blockIdx.x * kWfBlock + threadIdx.x;
-    const uint32_t nfree = st.counts[4];
-    const long generated = (long)st.counts[5];
-    const long take = min((long)nfree, total - generated);
-    if (t >= take) return;
-    const long w = generated + t;
+    if (t == 0) st.counts[4] = nfree - take;
+    if (t >= (long)take) return;
+    const long w = gen0 + t;
     const int slot = st.q_free[nfree - 1 - t];
     const int cw = rp.x1 - rp.x0;
-    const long npix = (long)cw * (rp.y1 - rp.y0);
-    const int s = (int)(w / npix);
+    const int s = s0 + (int)(w / npix);
     const long pc = w % npix;
     const int i = rp.x0 + (int)(pc % cw), j = rp.y0 + (int)(pc / cw);
     const int id = j * sv.width + i;
@@ -108,6 +112,7 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, co
     camera_ray(sv, pfx, pfy, rd, rxd, ryd, rp.spp_scale);
     st.pix[slot] = id;
     st.smp[slot] = s;
+    st.wid[slot] = (int32_t)w;
     st.draw[slot] = rng.draw;
     st.flags[slot] = 0u;
     st.pf[slot] = make_float2(pfx, pfy);
@@ -120,32 +125,36 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, co
     q_cur[pos] = slot;
 }
 
-__global__ void k_wf_generate_done(WfState st, long total) {
-    const uint32_t nfree = st.counts[4];
-    const long generated = (long)st.counts[5];
-    const long take = min((long)nfree, total - generated);
-    st.counts[4] = nfree - (uint32_t)take;
-    st.counts[5] = (uint32_t)(generated + take);
-}
-
-__device__ __forceinline__ void count_work(const RenderParams& rp, unsigned rays, const Work& wk) {
+// Work counters: [0..2] all rays (rays, node visits, triangle tests), then the same three per
+// traversal kind (0 extend, 1 shadow, 2 MIS) at [3 + 3 * kind].
+__device__ __forceinline__ void count_work(const RenderParams& rp, const Work& wk, int kind) {
     const unsigned mask = __activemask();
-    const unsigned tot = __reduce_add_sync(mask, rays);
+    const unsigned tot = __popc(mask);
     const unsigned tn = __reduce_add_sync(mask, wk.nodes), tt = __reduce_add_sync(mask, wk.tris);
     const unsigned lane = threadIdx.x & 31u;
     if ((mask & ((1u << lane) - 1u)) == 0u && rp.counters) {
-        atomicAdd(rp.counters, (unsigned long long)tot);
-        atomicAdd(rp.counters + 1, (unsigned long long)tn);
-        atomicAdd(rp.counters + 2, (unsigned long long)tt);
+        unsigned long long* c = rp.counters;
+        unsigned long long* k = rp.counters + 3 + 3 * kind;
+        atomicAdd(c, (unsigned long long)tot);
+        atomicAdd(c + 1, (unsigned long long)tn);
+        atomicAdd(c + 2, (unsigned long long)tt);
+        atomicAdd(k, (unsigned long long)tot);
+        atomicAdd(k + 1, (unsigned long long)tn);
+        atomicAdd(k + 2, (unsigned long long)tt);
     }
 }
 
 // extend: closest hit of each queued path ray (BVH::intersect, BVH.cuh:365-398).
 __global__ __launch_bounds__(kWfBlock) void k_wf_extend(const SceneView sv, const RenderParams rp, WfState st,
                                                         const int32_t* __restrict__ q, const uint32_t* __restrict__ cnt,
-                                                        int nleaf) {
+                                                        uint32_t* c_next, int nleaf) {
     __shared__ uint32_t s_stack[kStack * kWfBlock];
     const int t = blockIdx.x * kWfBlock + threadIdx.x;
+    if (t == 0) {  // queues this iteration's shade and finalize push into
+        st.counts[2] = 0u;
+        st.counts[3] = 0u;
+        *c_next = 0u;
+    }
     if (t >= (int)*cnt) return;
     const int p = q[t];
     const float4 o = st.ro[p], d = st.rd[p];
@@ -155,7 +164,7 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_extend(const SceneView sv, cons
     const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, s_stack + threadIdx.x, rp.err, wk);
     st.hprim[p] = prim;
     st.huvi[p] = make_float4(bu, bv, binv, tmax);
-    count_work(rp, 1u, wk);
+    count_work(rp, wk, 0);
 }
 
 // shadow: any hit (VisibilityTester::unoccluded, VisibilityTester.cu:9-12).
@@ -169,7 +178,7 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_shadow(const SceneView sv, cons
     Work wk{0u, 0u};
     const bool occ = scene_occluded(sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), d.w, s_stack + threadIdx.x, rp.err, wk);
     st.vis[p] = occ ? 0u : 1u;
-    count_work(rp, 1u, wk);
+    count_work(rp, wk, 1);
 }
 
 // mis: closest hit of the MIS BSDF ray; radiance of the sampled light where it lands
@@ -198,7 +207,7 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_mis(const SceneView sv, const R
     if (add) c = Spec{fv.x, fv.y, fv.z} * Li * spec(1.0f) * fv.w / x.x;
     st.ld_mis[p] = make_float4(c.r, c.g, c.b, add ? 1.f : 0.f);
     st.mis_hit[p] = found ? lit.prim + 1 : 0;
-    count_work(rp, 1u, wk);
+    count_work(rp, wk, 2);
 }
 
 // shade: one bounce of PathTracingIntegrator::evaluate up to the next ray.
@@ -435,27 +444,35 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
         q_next[pos] = p;
         return;
     }
-    // Camera::addSample (Camera.cu:192-218) into FP64 sums
+    // Camera::addSample (Camera.cu:192-218): the sample reaches film pixels [ceil(pf - 1),
+    // floor(pf + 1)] per axis.  With pf in [i, i + 1] that is i .. i + 2, gathered later, plus
+    // the column i - 1 (row j - 1) when pf rounds to exactly i (j), added here.
     const float2 pf = st.pf[p];
+    const int id = st.pix[p];
     const int W = sv.width, H = sv.height;
+    const int i = id % W, j = id / W;
     const int px0 = max((int)ceilf(pf.x - 1.0f), 0), py0 = max((int)ceilf(pf.y - 1.0f), 0);
-    const int px1 = min((int)floorf(pf.x + 1.0f) + 1, W), py1 = min((int)floorf(pf.y + 1.0f) + 1, H);
-    for (int y = py0; y < py1; ++y)
-        for (int x = px0; x < px1; ++x) {
-            const float fdx = fabsf((x - pf.x - 0.5f) * 1.0f * 16);
-            const float fdy = fabsf((y - pf.y - 0.5f) * 1.0f * 16);
-            const int ix = min((int)floorf(fdx), 15), iy = min((int)floorf(fdy), 15);
-            const float wgt = __ldg(sv.filter + iy * 16 + ix);
-            const Spec c = L * wgt;
-            double* fp = rp.film + 4 * ((size_t)y * W + x);
-            atomicAdd(fp + 0, (double)c.r);
-            atomicAdd(fp + 1, (double)c.g);
-            atomicAdd(fp + 2, (double)c.b);
-            atomicAdd(fp + 3, (double)wgt);
-        }
+    if (px0 < i || py0 < j) {
+        const int px1 = min((int)floorf(pf.x + 1.0f) + 1, W), py1 = min((int)floorf(pf.y + 1.0f) + 1, H);
+        for (int y = py0; y < py1; ++y)
+            for (int x = px0; x < px1; ++x) {
+                if (x >= i && y >= j) continue;
+                const float fdx = fabsf((x - pf.x - 0.5f) * 1.0f * 16);
+                const float fdy = fabsf((y - pf.y - 0.5f) * 1.0f * 16);
+                const int ix = min((int)floorf(fdx), 15), iy = min((int)floorf(fdy), 15);
+                const float wgt = __ldg(sv.filter + iy * 16 + ix);
+                const Spec c = L * wgt;
+                double* fp = rp.film + 4 * ((size_t)y * W + x);
+                atomicAdd(fp + 0, (double)c.r);
+                atomicAdd(fp + 1, (double)c.g);
+                atomicAdd(fp + 2, (double)c.b);
+                atomicAdd(fp + 3, (double)wgt);
+            }
+    }
+    const int w = st.wid[p];
+    st.fs_L[w] = make_float4(L.r, L.g, L.b, pf.x);
+    st.fs_y[w] = pf.y;
     if (RECORD) {
-        const int id = st.pix[p];
-        const int i = id % W, j = id / W;
         const size_t k = ((size_t)(j - rp.y0) * (rp.x1 - rp.x0) + (i - rp.x0)) * rp.spp + st.smp[p];
         rp.sample_L[3 * k + 0] = L.r;
         rp.sample_L[3 * k + 1] = L.g;
@@ -472,6 +489,55 @@ __global__ void k_wf_init_free(int32_t* q_free, uint32_t* counts, int n) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) q_free[t] = n - 1 - t;
     if (t == 0) counts[4] = (uint32_t)n;
+}
+
+// Film gather: thread (x, y) over the crop's film footprint [x0, x1 + 2) x [y0, y1 + 2) sums, in
+// the fixed order (source row, source column, sample), every finished sample of the chunk whose
+// filter footprint covers it from source pixels x - 2 .. x (y - 2 .. y): the pixels i .. i + 2
+// that k_wf_finalize left to this kernel.  Kahan-compensated FP32 per channel, then one
+// non-atomic FP64 add per channel (each film pixel has exactly one thread).
+__global__ __launch_bounds__(128) void k_film_gather(const SceneView sv, const RenderParams rp,
+                                                     const float4* __restrict__ fs_L, const float* __restrict__ fs_y,
+                                                     int nsc, long npix) {
+    __shared__ float s_filter[256];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int k = tid; k < 256; k += blockDim.x * blockDim.y) s_filter[k] = sv.filter[k];
+    __syncthreads();
+    const int W = sv.width, H = sv.height;
+    const int x = rp.x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = rp.y0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (x >= min(rp.x1 + 2, W) || y >= min(rp.y1 + 2, H)) return;
+    const int cw = rp.x1 - rp.x0;
+    float sum[4] = {0, 0, 0, 0}, cmp[4] = {0, 0, 0, 0};
+    const int j0 = max(y - 2, rp.y0), j1 = min(y, rp.y1 - 1);
+    const int i0 = max(x - 2, rp.x0), i1 = min(x, rp.x1 - 1);
+    for (int j = j0; j <= j1; ++j)
+        for (int i = i0; i <= i1; ++i) {
+            const long pc = (long)(j - rp.y0) * cw + (i - rp.x0);
+            for (int s = 0; s < nsc; ++s) {
+                const long k = (long)s * npix + pc;
+                const float4 v = __ldg(fs_L + k);
+                const float fy = __ldg(fs_y + k);
+                const int px1 = min((int)floorf(v.w + 1.0f) + 1, W), py1 = min((int)floorf(fy + 1.0f) + 1, H);
+                if (x >= px1 || y >= py1) continue;
+                const float fdx = fabsf((x - v.w - 0.5f) * 1.0f * 16);
+                const float fdy = fabsf((y - fy - 0.5f) * 1.0f * 16);
+                const int ix = min((int)floorf(fdx), 15), iy = min((int)floorf(fdy), 15);
+                const float wgt = s_filter[iy * 16 + ix];
+                const float c[4] = {v.x * wgt, v.y * wgt, v.z * wgt, wgt};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {  // Kahan compensation
+                    const float yv = __fsub_rn(c[q], cmp[q]);
+                    const float tv = __fadd_rn(sum[q], yv);
+                    cmp[q] = __fsub_rn(__fsub_rn(tv, sum[q]), yv);
+                    sum[q] = tv;
+                }
+            }
+        }
+    if (sum[3] == 0.f && cmp[3] == 0.f) return;
+    double* fp = rp.film + 4 * ((size_t)y * W + x);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) fp[q] += (double)sum[q] - (double)cmp[q];
 }
 
 }  // namespace
