@@ -224,6 +224,7 @@ def run_gpu(args, wl):
     d, sc, sub = scene_dir(wl)
     ctx = lts.Context(local)
     scene = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
+    ctx.set_option("bvh_width", args.bvh_width)
     integ = lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], scene, integrator=args.integrator)
     desc = integ.desc(wl["spp"], wl["seed"])
     stream = torch.cuda.ExternalStream(ctx.stream())
@@ -272,10 +273,11 @@ def run_gpu(args, wl):
         k = kinds[kernel]
         kernel_ms = mr.render_stage_ms[names.index(kernel)]
         kernel_launches = mr.render_iterations
-        alg_bytes = (64.0 * mr.kind_node_visits[k] + 48.0 * mr.kind_tri_tests[k] + state[kernel] * mr.kind_rays[k])
-        alg_text = (f"64 B per BVH node visit + 48 B per triangle test + {int(state[kernel])} B path state per ray "
-                    f"(k_wf_{kernel})")
-        kernel = "k_wf_" + kernel
+        node_b = 80.0 if args.bvh_width == 8 else 64.0
+        alg_bytes = (node_b * mr.kind_node_visits[k] + 48.0 * mr.kind_tri_tests[k] + state[kernel] * mr.kind_rays[k])
+        alg_text = (f"{int(node_b)} B per BVH node visit + 48 B per triangle test + {int(state[kernel])} B path state "
+                    f"per ray (k_wf_trace, {kernel} rays)")
+        kernel = f"k_wf_trace<{kernel}>"
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
 
     # end to end through the public API: upload scene (H2D), build, render, read film (D2H)
@@ -304,7 +306,8 @@ def run_gpu(args, wl):
             "config": {"workload": wl["name"], "width": wl["width"], "height": wl["height"], "spp": wl["spp"],
                        "max_bounce": wl["max_bounce"], "rr_start": wl["rr_start"], "seed": wl["seed"],
                        "triangles": scene.info["triangles"],
-                       "integrator": ["megakernel", "wavefront"][args.integrator], "bvh": "sorted-leaf LBVH",
+                       "integrator": ["megakernel", "wavefront"][args.integrator],
+                       "bvh": "sorted-leaf LBVH" + (", collapsed 8-wide" if args.bvh_width == 8 else ""),
                        "l2": "inputs (BVH + triangles) exceed L2; no flush", "parallelism": f"replicas x{world}"},
             "mrays_per_s": round(r["rays"] / (r["render_ms"] * 1e-3) / 1e6, 2),
             "e2e": {"value": round(e2e, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -339,6 +342,8 @@ def main():
     ap.add_argument("--skip-lbvh", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--integrator", type=int, default=1, choices=[0, 1], help="0 megakernel, 1 wavefront")
+    ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8],
+                    help="traversal structure: 8-wide compressed BVH or the binary LBVH")
     ap.add_argument("--lbvh-only", type=int, default=0, metavar="N",
                     help="only time the LBVH build over N random triangles (seed 1)")
     args = ap.parse_args()

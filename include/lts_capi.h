@@ -181,7 +181,9 @@ int lts_write_image(const char* path, const float* rgb, int32_t width, int32_t h
 int lts_debug_trace_sample(lts_ctx* ctx, int64_t crop_sample_index);
 int lts_debug_trace_get(lts_ctx* ctx, float* out_64x16);
 
-/* Tuning knobs of the wavefront integrator (no counterpart in the reference).  Keys:
+/* Tuning knobs of the renderer (no counterpart in the reference).  Keys:
+ *   "bvh_width"               traversal structure: 8 (default) the 8-wide compressed BVH collapsed
+ *                             from the LBVH, 2 the binary LBVH itself; both give the same hits
  *   "wavefront_pool"          path-state pool capacity in paths (0: automatic, 2^21)
  *   "wavefront_sample_chunk"  finished-sample buffer capacity in samples (0: automatic, 2^27);
  *                             samples per pixel are rendered in chunks that fit it

@@ -434,6 +434,9 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
     if (!strcmp(key, "wavefront_pool")) {
         if (value >= (1ll << 30)) return fail(ctx, LTS_ERR_ARG, "wavefront_pool too large");
         ctx->tracer->wf_pool = (long)value;
+    } else if (!strcmp(key, "bvh_width")) {
+        if (value != 2 && value != 8) return fail(ctx, LTS_ERR_ARG, "bvh_width must be 2 or 8");
+        ctx->tracer->bvh_width = (int)value;
     } else if (!strcmp(key, "wavefront_sample_chunk")) {
         ctx->tracer->wf_sample_cap = (long)value;
     } else {

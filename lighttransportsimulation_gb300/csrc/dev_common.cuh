@@ -36,6 +36,7 @@ enum DeviceError : uint32_t {
     DEV_ERR_STACK_OVERFLOW = 2u,
     DEV_ERR_QUEUE_OVERFLOW = 4u,
     DEV_ERR_BAD_INDEX = 8u,
+    DEV_ERR_CAPACITY = 16u,
 };
 
 // Upper bound of spin iterations of any wait on another block's flag.  A tile's predecessor

@@ -526,6 +526,14 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
         leaf_serial_ = bvh.serial;
         leaf_n_ = bvh.n;
     }
+    // 8-wide compressed BVH collapsed from the binary tree (kept while the tree is unchanged); it
+    // is used when the wide tree's depth fits the traversal stack
+    bool use_wide = bvh_width == 8 && bvh.n >= 2;
+    if (use_wide && wide_.serial != bvh.serial) {
+        const std::string e = wide_.build(bvh, leaf_v_, s, d_err);
+        if (!e.empty()) return e;
+    }
+    if (use_wide && wide_.levels - 1 > kStack / 2) use_wide = false;
     const size_t film_bytes = 32 * (size_t)sc.width * sc.height;
     if (film_cap_ < film_bytes) {
         dev_free(film_);
@@ -555,6 +563,10 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
     sv->leaf_v = leaf_v_;
     sv->nodes = bvh.nodes;
     sv->root_bounds = bvh.root_bounds;
+    sv->wnodes = use_wide ? wide_.nodes : nullptr;
+    sv->wtris = use_wide ? wide_.tris : nullptr;
+    sv->wcount = use_wide ? wide_.count : 0;
+    last_wide = use_wide;
     *rp = RenderParams{};
     rp->spp = d.spp;
     rp->max_bounce = d.max_bounce;
@@ -674,6 +686,22 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
         if (!e) TRY(cudaEventCreate(&e));
     for (double& x : last_stage_ms) x = 0;
     const dim3 gblock(32, 4);
+    // persistent trace grids: every SM filled with as many blocks as stay resident
+    const bool wide = sv.wnodes != nullptr;
+    if (wf_trace_blocks_[0] == 0) {
+        int dev = 0, sms = 0;
+        TRY(cudaGetDevice(&dev));
+        TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        int per[6] = {0, 0, 0, 0, 0, 0};
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], k_wf_trace<TR_EXTEND, true>, kWfBlock, 0));
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], k_wf_trace<TR_SHADOW, true>, kWfBlock, 0));
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[2], k_wf_trace<TR_MIS, true>, kWfBlock, 0));
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[3], k_wf_trace<TR_EXTEND, false>, kWfBlock, 0));
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[4], k_wf_trace<TR_SHADOW, false>, kWfBlock, 0));
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[5], k_wf_trace<TR_MIS, false>, kWfBlock, 0));
+        for (int k = 0; k < 6; ++k) wf_trace_blocks_[k] = (unsigned)std::max(1, per[k] * sms);
+    }
+    const unsigned* tb = wf_trace_blocks_ + (wide ? 0 : 3);
     for (int s0 = 0; s0 < d.spp; s0 += chunk) {
         const int nsc = std::min(chunk, d.spp - s0);
         const long ctot = npix * nsc;
@@ -691,14 +719,24 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
             }
             TRY(cudaEventRecord(wf_ev_[1], s));
             const unsigned g = blocks(ncur);
-            k_wf_extend<<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, c_next, bvh.n);
+            TRY(cudaMemsetAsync(st.counts + 8, 0, 12, s));  // fetch counters of the three trace launches
+            if (wide) k_wf_trace<TR_EXTEND, true><<<std::min(g, tb[0]), kWfBlock, 0, s>>>(
+                    sv, rp, st, cur, c_cur, st.counts + 8, c_next, bvh.n);
+            else k_wf_trace<TR_EXTEND, false><<<std::min(g, tb[0]), kWfBlock, 0, s>>>(
+                    sv, rp, st, cur, c_cur, st.counts + 8, c_next, bvh.n);
             TRY(cudaEventRecord(wf_ev_[2], s));
             if (rec) k_wf_shade<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur);
             else k_wf_shade<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur);
             TRY(cudaEventRecord(wf_ev_[3], s));
-            k_wf_shadow<<<g, kWfBlock, 0, s>>>(sv, rp, st, bvh.n);
+            if (wide) k_wf_trace<TR_SHADOW, true><<<std::min(g, tb[1]), kWfBlock, 0, s>>>(
+                    sv, rp, st, st.q_shadow, st.counts + 2, st.counts + 9, nullptr, bvh.n);
+            else k_wf_trace<TR_SHADOW, false><<<std::min(g, tb[1]), kWfBlock, 0, s>>>(
+                    sv, rp, st, st.q_shadow, st.counts + 2, st.counts + 9, nullptr, bvh.n);
             TRY(cudaEventRecord(wf_ev_[4], s));
-            k_wf_mis<<<g, kWfBlock, 0, s>>>(sv, rp, st, bvh.n);
+            if (wide) k_wf_trace<TR_MIS, true><<<std::min(g, tb[2]), kWfBlock, 0, s>>>(
+                    sv, rp, st, st.q_mis, st.counts + 3, st.counts + 10, nullptr, bvh.n);
+            else k_wf_trace<TR_MIS, false><<<std::min(g, tb[2]), kWfBlock, 0, s>>>(
+                    sv, rp, st, st.q_mis, st.counts + 3, st.counts + 10, nullptr, bvh.n);
             TRY(cudaEventRecord(wf_ev_[5], s));
             if (rec) k_wf_finalize<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, next, c_next);
             else k_wf_finalize<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, next, c_next);

@@ -9,6 +9,7 @@
 #include "../../include/lts_capi.h"
 #include "host_scene.hpp"
 #include "lbvh.cuh"
+#include "wide_bvh.cuh"
 
 namespace lts {
 
@@ -43,6 +44,9 @@ struct SceneView {
     float light_func_int;
     const BvhNode* __restrict__ nodes;
     const float* __restrict__ root_bounds;
+    const WideNode* __restrict__ wnodes;  // 8-wide compressed BVH (null: traverse the binary tree)
+    const float4* __restrict__ wtris;     // [3 ntri] triangles in wide-leaf order
+    int32_t wcount;                       // wide nodes
     const float* __restrict__ filter;    // 16 x 16 Gaussian table
     float cam[23];
 };
@@ -78,6 +82,9 @@ class Tracer {
     double last_ms = 0, last_paths = 0, last_rays = 0, last_node_visits = 0, last_tri_tests = 0;
     // Path-pool capacity of the wavefront integrator (0: automatic).
     long wf_pool = 0;
+    // Traversal structure: 8 = the collapsed 8-wide compressed BVH, 2 = the binary LBVH.
+    int bvh_width = 8;
+    bool last_wide = false;  // the last render traversed the wide BVH
     // Finished-sample buffer capacity of the wavefront film gather, in samples (0: 2^27).
     long wf_sample_cap = 0;
     int last_iterations = 0;
@@ -101,7 +108,9 @@ class Tracer {
     long wf_cap_ = 0, wf_fs_cap_ = 0;
     uint32_t* wf_counts_host_ = nullptr;
     cudaEvent_t wf_ev_[7] = {nullptr};
+    unsigned wf_trace_blocks_[6] = {0, 0, 0, 0, 0, 0};  // resident blocks of k_wf_trace (wide x3, binary x3)
     SceneView view_{};
+    WideBvh wide_;
     void* bufs_[16] = {nullptr};
     float4* leaf_v_ = nullptr;
     int leaf_n_ = 0;

@@ -23,7 +23,9 @@ namespace {
 #define kOnePlusEpsUp __int_as_float(0x3f800347)
 #define kSlabScale (1.0f + 2.0f * gamma_n(3))
 
-constexpr int kStack = 40;
+// Per-thread traversal stack in shared memory, in 32-bit words (binary: one node per word; wide:
+// one node group per two words).
+constexpr int kStack = 48;
 constexpr int kBX = 16, kBY = 8, kThreads = kBX * kBY;
 
 enum BxdfType : uint32_t {
@@ -284,9 +286,9 @@ __device__ __forceinline__ bool slab(const TraceRay& r, float tmax_ray, float mn
 }
 
 template <bool ANY>
-__device__ __forceinline__ bool leaf_test(const SceneView& sv, int leaf, const TraceRay& r, float& tmax, int& best,
-                                          float& bu, float& bv, float& binv) {
-    const float4 a = __ldg(sv.leaf_v + 3 * leaf), b = __ldg(sv.leaf_v + 3 * leaf + 1), c = __ldg(sv.leaf_v + 3 * leaf + 2);
+__device__ __forceinline__ bool leaf_test(const float4* __restrict__ tv, int leaf, const TraceRay& r, float& tmax,
+                                          int& best, float& bu, float& bv, float& binv) {
+    const float4 a = __ldg(tv + 3 * leaf), b = __ldg(tv + 3 * leaf + 1), c = __ldg(tv + 3 * leaf + 2);
     if (ANY) return tri_test_shadow(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax);
     float t, u, v, inv;
     if (tri_test(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax, t, u, v, inv)) {
@@ -299,62 +301,189 @@ __device__ __forceinline__ bool leaf_test(const SceneView& sv, int leaf, const T
     return false;
 }
 
-// BVH::intersect / simpleIntersect (acceleration/BVH.cuh:331-398).  Returns the hit primitive
-// (closest) or 1/-1 (any), -1 for a miss.  `stack` is this thread's column of the shared stack.
+// Traversal work counters of one thread (node visits, triangle tests).
 struct Work {
     uint32_t nodes, tris;
 };
 
+// BVH traversal as a state machine: trav_begin sets a ray up, each trav_step opens one node, so a
+// thread can run one ray to completion (traverse) or a persistent warp can interleave steps with
+// fetching new rays for lanes whose ray has finished (the wavefront trace kernels).
+//
+// Binary LBVH (BVH::intersect / simpleIntersect, acceleration/BVH.cuh:331-398): both child
+// boxes per node, nearer child first, the other on the stack (one word per entry).
+// 8-wide compressed BVH: the same box test on the decoded (conservative) child boxes; children
+// are visited in the order slot ^ octant(ray direction), nearest octant first; a node's leaf
+// triangles are tested when it is opened; the stack holds (first child, remaining hit slots |
+// imask << 8) groups, two words per entry.  `stack` is the thread's column of a shared-memory
+// stack with row stride kThreads.
+struct Trav {
+    TraceRay r;
+    float tmax, bu, bv, binv;
+    int best;  // closest: primitive (-1 none); any: 1 on a hit
+    int node, sp;
+    uint32_t gbase, gbits;
+};
+
+// Returns true when the ray needs traversal steps; false when it is already resolved (missed
+// the scene bounds, or a one-triangle scene).
+template <bool ANY>
+__device__ __forceinline__ bool trav_begin(Trav& t, const SceneView& sv, int nleaf, V3 o, V3 d, float tmax, Work& wk) {
+    t.r = make_trace_ray(o, d);
+    t.tmax = tmax;
+    t.bu = t.bv = t.binv = 0.f;
+    t.best = -1;
+    t.node = 0;
+    t.sp = 0;
+    t.gbase = 0;
+    t.gbits = 0;
+    float te;
+    const float* rb = sv.root_bounds;
+    if (!slab(t.r, t.tmax, __ldg(rb), __ldg(rb + 1), __ldg(rb + 2), __ldg(rb + 3), __ldg(rb + 4), __ldg(rb + 5), te))
+        return false;
+    if (nleaf == 1) {
+        ++wk.tris;
+        if (leaf_test<ANY>(sv.leaf_v, 0, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) t.best = 1;
+        return false;
+    }
+    return true;
+}
+
+// One node; returns true when the traversal has finished.
+template <bool ANY>
+__device__ __forceinline__ bool trav_step_wide(Trav& t, const SceneView& sv, uint32_t* stack, uint32_t* err,
+                                               Work& wk) {
+    if ((unsigned)t.node >= (unsigned)sv.wcount) {
+        atomicOr(err, DEV_ERR_BAD_INDEX);
+        return true;
+    }
+    const uint32_t oct = (t.r.neg[0] ? 1u : 0u) | (t.r.neg[1] ? 2u : 0u) | (t.r.neg[2] ? 4u : 0u);
+    const WideNode* nd = sv.wnodes + t.node;
+    const float4 h = __ldg(&nd->h);
+    const uint4 m = __ldg(&nd->m), q0 = __ldg(&nd->q0), q1 = __ldg(&nd->q1), q2 = __ldg(&nd->q2);
+    ++wk.nodes;
+    const uint32_t hb = __float_as_uint(h.w);
+    const float sx = wide_scale(hb & 0xffu), sy = wide_scale((hb >> 8) & 0xffu), sz = wide_scale((hb >> 16) & 0xffu);
+    const uint32_t imask = hb >> 24, omask = m.z;
+    uint32_t hits = 0, leaves = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        if (!((omask >> s) & 1u)) continue;
+        const int sh = (s & 3) * 8;
+        const uint32_t lx = ((s < 4 ? q0.x : q0.y) >> sh) & 0xffu, ly = ((s < 4 ? q0.z : q0.w) >> sh) & 0xffu;
+        const uint32_t lz = ((s < 4 ? q1.x : q1.y) >> sh) & 0xffu, hx = ((s < 4 ? q1.z : q1.w) >> sh) & 0xffu;
+        const uint32_t hy = ((s < 4 ? q2.x : q2.y) >> sh) & 0xffu, hz = ((s < 4 ? q2.z : q2.w) >> sh) & 0xffu;
+        float te;
+        if (slab(t.r, t.tmax, wide_plane(h.x, lx, sx), wide_plane(h.y, ly, sy), wide_plane(h.z, lz, sz),
+                 wide_plane(h.x, hx, sx), wide_plane(h.y, hy, sy), wide_plane(h.z, hz, sz), te)) {
+            if ((imask >> s) & 1u) hits |= 1u << ((uint32_t)s ^ oct);
+            else leaves |= 1u << s;
+        }
+    }
+    const uint32_t lmask = omask & ~imask;
+    while (leaves) {
+        const int s = __ffs(leaves) - 1;
+        leaves &= leaves - 1u;
+        const int tri = (int)m.y + __popc(lmask & ((1u << s) - 1u));
+        if ((unsigned)tri >= (unsigned)sv.ntri) {
+            atomicOr(err, DEV_ERR_BAD_INDEX);
+            return true;
+        }
+        ++wk.tris;
+        if (leaf_test<ANY>(sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+            t.best = 1;
+            return true;
+        }
+    }
+    if (hits) {
+        if (t.gbits & 0xffu) {
+            if (2 * t.sp + 1 >= kStack) {
+                atomicOr(err, DEV_ERR_STACK_OVERFLOW);
+                return true;
+            }
+            stack[(2 * t.sp) * kThreads] = t.gbase;
+            stack[(2 * t.sp + 1) * kThreads] = t.gbits;
+            ++t.sp;
+        }
+        t.gbase = m.x;
+        t.gbits = hits | (imask << 8);
+    }
+    if (!(t.gbits & 0xffu)) {
+        if (t.sp == 0) return true;
+        --t.sp;
+        t.gbase = stack[(2 * t.sp) * kThreads];
+        t.gbits = stack[(2 * t.sp + 1) * kThreads];
+    }
+    const uint32_t p = (uint32_t)__ffs(t.gbits & 0xffu) - 1u;
+    t.gbits &= ~(1u << p);
+    const uint32_t s = p ^ oct;
+    t.node = (int)t.gbase + __popc((t.gbits >> 8) & ((1u << s) - 1u));
+    return false;
+}
+
+template <bool ANY>
+__device__ __forceinline__ bool trav_step_binary(Trav& t, const SceneView& sv, uint32_t* stack, uint32_t* err,
+                                                 Work& wk) {
+    const BvhNode* nd = sv.nodes + t.node;
+    const float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
+    const int4 lr = __ldg(&nd->d);
+    ++wk.nodes;
+    float tl, tr;
+    bool hl = slab(t.r, t.tmax, a.x, a.y, a.z, a.w, b.x, b.y, tl);
+    bool hr = slab(t.r, t.tmax, b.z, b.w, c.x, c.y, c.z, c.w, tr);
+    if (hl && lr.x < 0) {
+        ++wk.tris;
+        if (leaf_test<ANY>(sv.leaf_v, ~lr.x, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+            t.best = 1;
+            return true;
+        }
+        hl = false;
+    }
+    if (hr && lr.y < 0) {
+        ++wk.tris;
+        if (leaf_test<ANY>(sv.leaf_v, ~lr.y, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+            t.best = 1;
+            return true;
+        }
+        hr = false;
+    }
+    if (hl && hr) {
+        const bool left_first = tl <= tr;
+        if (t.sp >= kStack) {  // one word per entry
+            atomicOr(err, DEV_ERR_STACK_OVERFLOW);
+            return true;
+        }
+        stack[(t.sp++) * kThreads] = left_first ? lr.y : lr.x;
+        t.node = left_first ? lr.x : lr.y;
+    } else if (hl) {
+        t.node = lr.x;
+    } else if (hr) {
+        t.node = lr.y;
+    } else {
+        if (t.sp == 0) return true;
+        t.node = stack[(--t.sp) * kThreads];
+    }
+    return false;
+}
+
+template <bool ANY>
+__device__ __forceinline__ bool trav_step(Trav& t, const SceneView& sv, uint32_t* stack, uint32_t* err, Work& wk) {
+    return sv.wnodes ? trav_step_wide<ANY>(t, sv, stack, err, wk) : trav_step_binary<ANY>(t, sv, stack, err, wk);
+}
+
+// Whole traversal: the hit primitive (closest) or 1 / -1 (any), -1 for a miss.
 template <bool ANY>
 __device__ int traverse(const SceneView& sv, int nleaf, const TraceRay& r, float& tmax, float& bu, float& bv,
                         float& binv, uint32_t* stack, uint32_t* err, Work& wk) {
-    int best = -1;
-    float te;
-    const float* rb = sv.root_bounds;
-    if (!slab(r, tmax, __ldg(rb), __ldg(rb + 1), __ldg(rb + 2), __ldg(rb + 3), __ldg(rb + 4), __ldg(rb + 5), te))
-        return -1;
-    if (nleaf == 1) {
-        ++wk.tris;
-        if (leaf_test<ANY>(sv, 0, r, tmax, best, bu, bv, binv)) return 1;
-        return ANY ? -1 : best;
-    }
-    int node = 0, sp = 0;
-    for (;;) {
-        const BvhNode* nd = sv.nodes + node;
-        const float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
-        const int4 lr = __ldg(&nd->d);
-        ++wk.nodes;
-        float tl, tr;
-        bool hl = slab(r, tmax, a.x, a.y, a.z, a.w, b.x, b.y, tl);
-        bool hr = slab(r, tmax, b.z, b.w, c.x, c.y, c.z, c.w, tr);
-        if (hl && lr.x < 0) {
-            ++wk.tris;
-            if (leaf_test<ANY>(sv, ~lr.x, r, tmax, best, bu, bv, binv)) return 1;
-            hl = false;
+    Trav t;
+    if (trav_begin<ANY>(t, sv, nleaf, r.o, r.d, tmax, wk))
+        while (!trav_step<ANY>(t, sv, stack, err, wk)) {
         }
-        if (hr && lr.y < 0) {
-            ++wk.tris;
-            if (leaf_test<ANY>(sv, ~lr.y, r, tmax, best, bu, bv, binv)) return 1;
-            hr = false;
-        }
-        if (hl && hr) {
-            const bool left_first = tl <= tr;
-            if (sp >= kStack) {
-                atomicOr(err, DEV_ERR_STACK_OVERFLOW);
-                return ANY ? -1 : best;
-            }
-            stack[(sp++) * kThreads] = left_first ? lr.y : lr.x;
-            node = left_first ? lr.x : lr.y;
-        } else if (hl) {
-            node = lr.x;
-        } else if (hr) {
-            node = lr.y;
-        } else {
-            if (sp == 0) break;
-            node = stack[(--sp) * kThreads];
-        }
-    }
-    return ANY ? -1 : best;
+    tmax = t.tmax;
+    bu = t.bu;
+    bv = t.bv;
+    binv = t.binv;
+    return ANY ? (t.best == 1 ? 1 : -1) : t.best;
 }
 
 struct Hit {

@@ -126,88 +126,134 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, co
 }
 
 // Work counters: [0..2] all rays (rays, node visits, triangle tests), then the same three per
-// traversal kind (0 extend, 1 shadow, 2 MIS) at [3 + 3 * kind].
-__device__ __forceinline__ void count_work(const RenderParams& rp, const Work& wk, int kind) {
-    const unsigned mask = __activemask();
-    const unsigned tot = __popc(mask);
-    const unsigned tn = __reduce_add_sync(mask, wk.nodes), tt = __reduce_add_sync(mask, wk.tris);
-    const unsigned lane = threadIdx.x & 31u;
-    if ((mask & ((1u << lane) - 1u)) == 0u && rp.counters) {
+// traversal kind (0 extend, 1 shadow, 2 MIS) at [3 + 3 * kind].  Called by all 32 lanes.
+__device__ __forceinline__ void count_work(const RenderParams& rp, unsigned rays, const Work& wk, int kind) {
+    const unsigned tr = __reduce_add_sync(~0u, rays);
+    const unsigned tn = __reduce_add_sync(~0u, wk.nodes), tt = __reduce_add_sync(~0u, wk.tris);
+    if ((threadIdx.x & 31u) == 0u && rp.counters && tr) {
         unsigned long long* c = rp.counters;
         unsigned long long* k = rp.counters + 3 + 3 * kind;
-        atomicAdd(c, (unsigned long long)tot);
+        atomicAdd(c, (unsigned long long)tr);
         atomicAdd(c + 1, (unsigned long long)tn);
         atomicAdd(c + 2, (unsigned long long)tt);
-        atomicAdd(k, (unsigned long long)tot);
+        atomicAdd(k, (unsigned long long)tr);
         atomicAdd(k + 1, (unsigned long long)tn);
         atomicAdd(k + 2, (unsigned long long)tt);
     }
 }
 
-// extend: closest hit of each queued path ray (BVH::intersect, BVH.cuh:365-398).
-__global__ __launch_bounds__(kWfBlock) void k_wf_extend(const SceneView sv, const RenderParams rp, WfState st,
-                                                        const int32_t* __restrict__ q, const uint32_t* __restrict__ cnt,
-                                                        uint32_t* c_next, int nleaf) {
+enum : int { TR_EXTEND = 0, TR_SHADOW = 1, TR_MIS = 2 };
+
+// The ray of path slot p for each traversal kind.
+template <int KIND>
+__device__ __forceinline__ bool wf_ray_begin(Trav& t, const SceneView& sv, const WfState& st, int p, int nleaf,
+                                             Work& wk) {
+    if (KIND == TR_EXTEND) {  // path ray, closest hit (BVH::intersect, BVH.cuh:365-398)
+        const float4 o = st.ro[p], d = st.rd[p];
+        return trav_begin<false>(t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), INFINITY, wk);
+    } else if (KIND == TR_SHADOW) {  // VisibilityTester::unoccluded (VisibilityTester.cu:9-12), any hit
+        const float4 o = st.sh_o[p], d = st.sh_d[p];
+        return trav_begin<true>(t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), d.w, wk);
+    } else {  // MIS BSDF ray, closest hit
+        const float4 o = st.mis_o[p], d = st.mis_d[p];
+        return trav_begin<false>(t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), INFINITY, wk);
+    }
+}
+
+// Results of a finished traversal.  MIS: radiance of the sampled light where the BSDF ray lands
+// (IntegratorHelper.cuh:225-243).
+template <int KIND>
+__device__ __forceinline__ void wf_ray_end(const Trav& t, const SceneView& sv, WfState& st, int p) {
+    if (KIND == TR_EXTEND) {
+        st.hprim[p] = t.best;
+        st.huvi[p] = make_float4(t.bu, t.bv, t.binv, t.tmax);
+    } else if (KIND == TR_SHADOW) {
+        st.vis[p] = t.best == 1 ? 0u : 1u;
+    } else {
+        const float4 d = st.mis_d[p], fv = st.mis_fv[p], x = st.mis_x[p];
+        const V3 wi = v3(d.x, d.y, d.z);
+        const int off = __float_as_int(x.y);
+        const DevLight& Lt = sv.lights[off];
+        const bool found = t.best >= 0;
+        Spec Li = spec(0.0f);
+        if (found) {
+            SI lit;
+            V3 p0, p1, p2;
+            prim_tri(sv, t.best, p0, p1, p2);
+            make_si(sv, t.best, p0, p1, p2, wi, t.bu, t.bv, t.binv, lit);
+            if (__ldg(sv.prim_light + lit.prim) == off && Lt.kind == 0)
+                Li = dot(lit.n, -wi) > 0.f ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
+        } else {
+            Li = Lt.kind == 1 ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
+        }
+        Spec c = spec(0.0f);
+        const bool add = !is_black(Li);
+        if (add) c = Spec{fv.x, fv.y, fv.z} * Li * spec(1.0f) * fv.w / x.x;
+        st.ld_mis[p] = make_float4(c.r, c.g, c.b, add ? 1.f : 0.f);
+        st.mis_hit[p] = found ? t.best + 1 : 0;
+    }
+}
+
+// Lanes left idle before a warp fetches new rays (while the queue lasts).
+constexpr int kRefillIdle = 8;
+
+// Persistent traversal of one queue: each warp keeps up to 32 rays in flight; when at least
+// kRefillIdle lanes have finished, the warp claims that many queue entries with one atomic and
+// starts them, so lanes do not idle while the warp's longest ray finishes (dynamic ray fetch,
+// Aila and Laine, HPG 2009).  Launched with whole warps; `fetch` is zeroed before the launch.
+// WIDE: the 8-wide compressed BVH (sv.wnodes), else the binary LBVH.
+template <int KIND, bool WIDE>
+__global__ __launch_bounds__(kWfBlock) void k_wf_trace(const SceneView sv, const RenderParams rp, WfState st,
+                                                       const int32_t* __restrict__ q, const uint32_t* __restrict__ cnt,
+                                                       uint32_t* fetch, uint32_t* c_next, int nleaf) {
     __shared__ uint32_t s_stack[kStack * kWfBlock];
-    const int t = blockIdx.x * kWfBlock + threadIdx.x;
-    if (t == 0) {  // queues this iteration's shade and finalize push into
+    uint32_t* stack = s_stack + threadIdx.x;
+    if (KIND == TR_EXTEND && blockIdx.x == 0 && threadIdx.x == 0) {  // queues shade and finalize push into
         st.counts[2] = 0u;
         st.counts[3] = 0u;
         *c_next = 0u;
     }
-    if (t >= (int)*cnt) return;
-    const int p = q[t];
-    const float4 o = st.ro[p], d = st.rd[p];
-    const TraceRay r = make_trace_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z));
-    float tmax = INFINITY, bu = 0, bv = 0, binv = 0;
+    constexpr bool ANY = KIND == TR_SHADOW;
+    const uint32_t n = *cnt;
+    const unsigned lane = threadIdx.x & 31u;
+    Trav t;
+    int p = -1;
+    bool active = false, exhausted = false;
     Work wk{0u, 0u};
-    const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, s_stack + threadIdx.x, rp.err, wk);
-    st.hprim[p] = prim;
-    st.huvi[p] = make_float4(bu, bv, binv, tmax);
-    count_work(rp, wk, 0);
-}
-
-// shadow: any hit (VisibilityTester::unoccluded, VisibilityTester.cu:9-12).
-__global__ __launch_bounds__(kWfBlock) void k_wf_shadow(const SceneView sv, const RenderParams rp, WfState st,
-                                                        int nleaf) {
-    __shared__ uint32_t s_stack[kStack * kWfBlock];
-    const int t = blockIdx.x * kWfBlock + threadIdx.x;
-    if (t >= (int)st.counts[2]) return;
-    const int p = st.q_shadow[t];
-    const float4 o = st.sh_o[p], d = st.sh_d[p];
-    Work wk{0u, 0u};
-    const bool occ = scene_occluded(sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), d.w, s_stack + threadIdx.x, rp.err, wk);
-    st.vis[p] = occ ? 0u : 1u;
-    count_work(rp, wk, 1);
-}
-
-// mis: closest hit of the MIS BSDF ray; radiance of the sampled light where it lands
-// (IntegratorHelper.cuh:225-243).
-__global__ __launch_bounds__(kWfBlock) void k_wf_mis(const SceneView sv, const RenderParams rp, WfState st, int nleaf) {
-    __shared__ uint32_t s_stack[kStack * kWfBlock];
-    const int t = blockIdx.x * kWfBlock + threadIdx.x;
-    if (t >= (int)st.counts[3]) return;
-    const int p = st.q_mis[t];
-    const float4 o = st.mis_o[p], d = st.mis_d[p], fv = st.mis_fv[p], x = st.mis_x[p];
-    const V3 wi = v3(d.x, d.y, d.z);
-    const int off = __float_as_int(x.y);
-    const DevLight& Lt = sv.lights[off];
-    Work wk{0u, 0u};
-    SI lit;
-    const bool found = scene_intersect(sv, nleaf, v3(o.x, o.y, o.z), wi, INFINITY, lit, s_stack + threadIdx.x, rp.err, wk);
-    Spec Li = spec(0.0f);
-    if (found) {
-        if (__ldg(sv.prim_light + lit.prim) == off && Lt.kind == 0)
-            Li = dot(lit.n, -wi) > 0.f ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
-    } else {
-        Li = Lt.kind == 1 ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
+    unsigned rays = 0;
+    for (;;) {
+        const unsigned idle = __ballot_sync(~0u, !active);
+        if (!exhausted && __popc(idle) >= kRefillIdle) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(idle));
+            base = __shfl_sync(~0u, base, leader);
+            if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+            if (!active) {
+                const uint32_t idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (idx < n) {
+                    p = q[idx];
+                    ++rays;
+                    active = wf_ray_begin<KIND>(t, sv, st, p, nleaf, wk);
+                    if (!active) wf_ray_end<KIND>(t, sv, st, p);
+                }
+            }
+        }
+        if (__ballot_sync(~0u, active) == 0u) {
+            if (exhausted) break;
+            continue;
+        }
+        for (;;) {
+            if (active && (WIDE ? trav_step_wide<ANY>(t, sv, stack, rp.err, wk)
+                                : trav_step_binary<ANY>(t, sv, stack, rp.err, wk))) {
+                wf_ray_end<KIND>(t, sv, st, p);
+                active = false;
+            }
+            const unsigned act = __ballot_sync(~0u, active);
+            if (act == 0u || (!exhausted && 32 - __popc(act) >= kRefillIdle)) break;
+        }
     }
-    Spec c = spec(0.0f);
-    const bool add = !is_black(Li);
-    if (add) c = Spec{fv.x, fv.y, fv.z} * Li * spec(1.0f) * fv.w / x.x;
-    st.ld_mis[p] = make_float4(c.r, c.g, c.b, add ? 1.f : 0.f);
-    st.mis_hit[p] = found ? lit.prim + 1 : 0;
-    count_work(rp, wk, 2);
+    count_work(rp, rays, wk, KIND);
 }
 
 // shade: one bounce of PathTracingIntegrator::evaluate up to the next ray.

@@ -37,15 +37,19 @@ def ctx(built_lib):
 
 
 @pytest.mark.parametrize("kind", ["box_sphere", "materials"])
-@pytest.mark.parametrize("bvh_mode,integrator", [(0, 0), (1, 0), (1, 1)])
-def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator):
+@pytest.mark.parametrize("bvh_mode,integrator,width", [(0, 0, 2), (0, 1, 8), (1, 0, 8), (1, 1, 8), (1, 1, 2)])
+def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator, width):
     import lighttransportsimulation_gb300 as lts
     d, sc, sub = scene_dirs[kind]
     fx = np.load(os.path.join(GOLDEN, f"render_{kind}.npz"))
     w, h, spp, maxb, rr, seed, x0, y0, x1, y1 = (int(v) for v in fx["meta"])
     s = lts.Scene.parse(ctx, d, sc, sub, w, h)
     integ = lts.PathTracingIntegrator(maxb, rr, s, integrator=integrator, bvh_mode=bvh_mode)
-    r = integ.render(spp, seed, crop=(x0, y0, x1, y1), record=True, film=False)
+    ctx.set_option("bvh_width", width)
+    try:
+        r = integ.render(spp, seed, crop=(x0, y0, x1, y1), record=True, film=False)
+    finally:
+        ctx.set_option("bvh_width", 8)
     L = r["L"].reshape(-1, 3)
     sig = r["sig"].reshape(-1)
     Lr = fx["L"].reshape(-1, 3)
@@ -54,7 +58,7 @@ def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator):
     div = 1.0 - same.mean()
     ok = np.all(np.abs(L - Lr) <= RTOL * np.abs(Lr) + ATOL, axis=1)
     mism = 1.0 - ok[same].mean()
-    print(f"{kind} bvh={bvh_mode} integrator={integrator}: samples={len(sig)} divergent={div:.5f} mismatched={mism:.6f} "
+    print(f"{kind} bvh={bvh_mode} integrator={integrator} width={width}: samples={len(sig)} divergent={div:.5f} mismatched={mism:.6f} "
           f"maxrel={np.max(np.abs(L - Lr)[same] / (np.abs(Lr[same]) + 1e-6)):.3g}")
     assert np.isfinite(L).all()
     assert div <= MAX_DIVERGENT
@@ -129,3 +133,30 @@ def test_wavefront_film_reproducible(ctx, scene_dirs):
     f1 = integ.render(16, 3)["film"]
     f2 = integ.render(16, 3)["film"]
     assert np.array_equal(f1.view(np.uint32), f2.view(np.uint32))
+
+
+@pytest.mark.parametrize("kind", ["materials", "soup"])
+def test_wide_bvh_same_hits_as_binary(ctx, scene_dirs, tmp_path, kind):
+    """The 8-wide compressed BVH (conservative quantised boxes) finds the binary LBVH's closest
+    hits: identical event hashes and bit-identical radiance wherever no exact tie between two
+    triangles decided the hit."""
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    if kind == "soup":
+        d = str(tmp_path)
+        sc, sub = scenes.write_random_tris(d, 20000, seed=7)
+    else:
+        d, sc, sub = scene_dirs[kind]
+    s = lts.Scene.parse(ctx, d, sc, sub, 128, 96)
+    integ = lts.PathTracingIntegrator(6, 3, s, integrator=1)
+    out = {}
+    for width in (2, 8):
+        ctx.set_option("bvh_width", width)
+        out[width] = integ.render(4, 9, record=True, film=False)
+    ctx.set_option("bvh_width", 8)
+    a, b = out[2], out[8]
+    same = a["sig"].reshape(-1) == b["sig"].reshape(-1)
+    print(f"{kind}: hash-equal {same.mean():.6f}")
+    assert same.mean() >= 0.999
+    La, Lb = a["L"].reshape(-1, 3)[same], b["L"].reshape(-1, 3)[same]
+    assert np.array_equal(La.view(np.uint32), Lb.view(np.uint32))
