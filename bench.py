@@ -264,20 +264,19 @@ def run_gpu(args, wl):
         alg_bytes = 64.0 * r["node_visits"] + 48.0 * r["tri_tests"] + 32.0 * paths
         alg_text = "64 B per BVH node visit + 48 B per triangle test + 32 B film per path"
     else:
-        names = ["generate", "extend", "shade", "shadow", "mis", "finalize"]
+        names = ["generate", "trace", "finalize", "shade", "compact", "gather"]
         stages = {n: round(mr.render_stage_ms[k], 3) for k, n in enumerate(names)}
-        # per traversal kernel: nodes, triangles, plus the path-state bytes it reads and writes per ray
-        state = {"extend": 56.0, "shadow": 40.0, "mis": 88.0}
-        kinds = {"extend": 0, "shadow": 1, "mis": 2}
-        kernel = max(kinds, key=lambda n: mr.render_stage_ms[names.index(n)])
-        k = kinds[kernel]
-        kernel_ms = mr.render_stage_ms[names.index(kernel)]
-        kernel_launches = mr.render_iterations
+        # k_wf_trace (path, shadow and MIS rays in one launch): nodes, triangles, plus the path-state
+        # bytes each ray reads and writes
         node_b = 80.0 if args.bvh_width == 8 else 64.0
-        alg_bytes = (node_b * mr.kind_node_visits[k] + 48.0 * mr.kind_tri_tests[k] + state[kernel] * mr.kind_rays[k])
-        alg_text = (f"{int(node_b)} B per BVH node visit + 48 B per triangle test + {int(state[kernel])} B path state "
-                    f"per ray (k_wf_trace, {kernel} rays)")
-        kernel = f"k_wf_trace<{kernel}>"
+        state = [56.0, 40.0, 88.0]
+        alg_bytes = sum(node_b * mr.kind_node_visits[k] + 48.0 * mr.kind_tri_tests[k] + state[k] * mr.kind_rays[k]
+                        for k in range(3))
+        alg_text = (f"{int(node_b)} B per BVH node visit + 48 B per triangle test + path state per ray "
+                    f"(56 B path ray, 40 B shadow ray, 88 B MIS ray)")
+        kernel = "k_wf_trace"
+        kernel_ms = mr.render_stage_ms[1]
+        kernel_launches = mr.render_iterations
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
 
     # end to end through the public API: upload scene (H2D), build, render, read film (D2H)
@@ -318,7 +317,8 @@ def run_gpu(args, wl):
                          "kernel_ms_per_step": round(kernel_ms, 3), "peak_kind": peak_kind,
                          "algorithmic": alg_text, "algorithmic_bytes_per_step": alg_bytes},
             "stage_ms": stages,
-            "traversal": {"node_visits": r["node_visits"], "tri_tests": r["tri_tests"], "rays": r["rays"]},
+            "traversal": {"node_visits": r["node_visits"], "tri_tests": r["tri_tests"], "rays": r["rays"],
+                          "rays_by_kind": {"path": mr.kind_rays[0], "shadow": mr.kind_rays[1], "mis": mr.kind_rays[2]}},
             "lbvh": lbvh,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),

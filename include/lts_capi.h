@@ -200,9 +200,9 @@ typedef struct {
     int32_t kernel_launches; /* kernels launched by the last build + render */
     int32_t render_launches; /* kernels launched by the last render alone */
     int32_t render_iterations; /* wavefront: stage-loop iterations of the last render (1 for the megakernel) */
-    /* wavefront: device ms per stage (generate, extend, shade, shadow, mis, finalize) of the last
-     * render, and per traversal kind (extend, shadow, mis) its rays, node visits and triangle tests
-     * (filled by a synchronous lts_render); zero for the megakernel */
+    /* wavefront: device ms per stage (generate, trace, finalize, shade, compact, film gather) of
+     * the last render, and per traversal kind (path rays, shadow rays, MIS rays) its rays, node
+     * visits and triangle tests (filled by a synchronous lts_render); zero for the megakernel */
     double render_stage_ms[6];
     double kind_rays[3], kind_node_visits[3], kind_tri_tests[3];
 } lts_metrics;

@@ -669,93 +669,88 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
     st.q_a = (int32_t*)b[26]; st.q_b = (int32_t*)b[27]; st.q_shadow = (int32_t*)b[28]; st.q_mis = (int32_t*)b[29];
     st.q_free = (int32_t*)b[30]; st.counts = (uint32_t*)b[31]; st.wid = (int32_t*)b[32];
     st.fs_L = (float4*)b[33]; st.fs_y = (float*)b[34];
-    TRY(cudaMemsetAsync(st.counts, 0, 64, s));
     if (rp.sample_sig) {
         TRY(cudaMemsetAsync(st.ev_mis, 0, 8 * (size_t)P, s));
         TRY(cudaMemsetAsync(st.ev_main, 0, 8 * (size_t)P, s));
     }
     auto blocks = [](long n) { return (unsigned)((n + kWfBlock - 1) / kWfBlock); };
-    k_wf_init_free<<<blocks(P), kWfBlock, 0, s>>>(st.q_free, st.counts, (int)P);
     TRY(cudaEventRecord(ev0_, s));
-    int32_t *cur = st.q_a, *next = st.q_b;
-    uint32_t *c_cur = st.counts + 0, *c_next = st.counts + 1;
-    int i_cur = 0;
+    k_wf_init_free<<<blocks(P), kWfBlock, 0, s>>>(st.q_free, st.pix, (int)P);  // every slot free
     const bool rec = rp.sample_sig != nullptr;
+    const bool wide = sv.wnodes != nullptr;
     int iters = 0, launches = 1;
     for (cudaEvent_t& e : wf_ev_)
         if (!e) TRY(cudaEventCreate(&e));
     for (double& x : last_stage_ms) x = 0;
-    const dim3 gblock(32, 4);
-    // persistent trace grids: every SM filled with as many blocks as stay resident
-    const bool wide = sv.wnodes != nullptr;
+    // persistent trace grid: every SM filled with as many blocks as stay resident
     if (wf_trace_blocks_[0] == 0) {
-        int dev = 0, sms = 0;
+        int dev = 0, sms = 0, per_w = 0, per_b = 0;
         TRY(cudaGetDevice(&dev));
         TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        int per[6] = {0, 0, 0, 0, 0, 0};
-        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], k_wf_trace<TR_EXTEND, true>, kWfBlock, 0));
-        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], k_wf_trace<TR_SHADOW, true>, kWfBlock, 0));
-        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[2], k_wf_trace<TR_MIS, true>, kWfBlock, 0));
-        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[3], k_wf_trace<TR_EXTEND, false>, kWfBlock, 0));
-        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[4], k_wf_trace<TR_SHADOW, false>, kWfBlock, 0));
-        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[5], k_wf_trace<TR_MIS, false>, kWfBlock, 0));
-        for (int k = 0; k < 6; ++k) wf_trace_blocks_[k] = (unsigned)std::max(1, per[k] * sms);
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_w, k_wf_trace<true>, kWfBlock, 0));
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, k_wf_trace<false>, kWfBlock, 0));
+        wf_trace_blocks_[0] = (unsigned)std::max(1, per_w * sms);
+        wf_trace_blocks_[1] = (unsigned)std::max(1, per_b * sms);
     }
-    const unsigned* tb = wf_trace_blocks_ + (wide ? 0 : 3);
+    const unsigned tb = wf_trace_blocks_[wide ? 0 : 1];
+    const unsigned cgrid = (unsigned)((P + kCompactTile - 1) / kCompactTile);
+    const dim3 gblock(32, 4);
     for (int s0 = 0; s0 < d.spp; s0 += chunk) {
         const int nsc = std::min(chunk, d.spp - s0);
         const long ctot = npix * nsc;
         long generated = 0;
-        uint32_t nfree = (uint32_t)P, nnext = 0;
+        uint32_t nfree = (uint32_t)P, n_cont = 0, n_fin = 0, n_sh = 0, n_mis = 0;
+        int32_t *q_ext = st.q_a, *q_fin = st.q_b;
         for (;; ++iters) {
             const uint32_t take = (uint32_t)std::min<long>(nfree, ctot - generated);
-            const long ncur = (long)nnext + take;
-            if (ncur == 0) break;
+            const uint32_t n_ext = n_cont + take;
+            if (n_ext == 0 && n_fin == 0) break;
             if (iters > 1000000) return "wavefront did not converge";
+            TRY(cudaMemsetAsync(st.counts, 0, 64, s));
             TRY(cudaEventRecord(wf_ev_[0], s));
             if (take) {
-                k_wf_generate<<<blocks(take), kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, generated, nfree, take, s0, npix);
+                k_wf_generate<<<blocks(take), kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_cont, generated, take, s0, npix);
                 ++launches;
             }
             TRY(cudaEventRecord(wf_ev_[1], s));
-            const unsigned g = blocks(ncur);
-            TRY(cudaMemsetAsync(st.counts + 8, 0, 12, s));  // fetch counters of the three trace launches
-            if (wide) k_wf_trace<TR_EXTEND, true><<<std::min(g, tb[0]), kWfBlock, 0, s>>>(
-                    sv, rp, st, cur, c_cur, st.counts + 8, c_next, bvh.n);
-            else k_wf_trace<TR_EXTEND, false><<<std::min(g, tb[0]), kWfBlock, 0, s>>>(
-                    sv, rp, st, cur, c_cur, st.counts + 8, c_next, bvh.n);
+            const uint32_t nray = n_ext + n_sh + n_mis;
+            if (nray) {
+                const unsigned g = std::min(blocks(nray), tb);
+                if (wide) k_wf_trace<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_ext, n_sh, n_mis, st.counts + 8, bvh.n);
+                else k_wf_trace<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_ext, n_sh, n_mis, st.counts + 8, bvh.n);
+                ++launches;
+            }
             TRY(cudaEventRecord(wf_ev_[2], s));
-            if (rec) k_wf_shade<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur);
-            else k_wf_shade<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur);
+            if (n_fin) {
+                if (rec) k_wf_finalize<true><<<blocks(n_fin), kWfBlock, 0, s>>>(sv, rp, st, q_fin, n_fin);
+                else k_wf_finalize<false><<<blocks(n_fin), kWfBlock, 0, s>>>(sv, rp, st, q_fin, n_fin);
+                ++launches;
+            }
             TRY(cudaEventRecord(wf_ev_[3], s));
-            if (wide) k_wf_trace<TR_SHADOW, true><<<std::min(g, tb[1]), kWfBlock, 0, s>>>(
-                    sv, rp, st, st.q_shadow, st.counts + 2, st.counts + 9, nullptr, bvh.n);
-            else k_wf_trace<TR_SHADOW, false><<<std::min(g, tb[1]), kWfBlock, 0, s>>>(
-                    sv, rp, st, st.q_shadow, st.counts + 2, st.counts + 9, nullptr, bvh.n);
+            if (n_ext) {
+                if (rec) k_wf_shade<true><<<blocks(n_ext), kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_ext);
+                else k_wf_shade<false><<<blocks(n_ext), kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_ext);
+                ++launches;
+            }
             TRY(cudaEventRecord(wf_ev_[4], s));
-            if (wide) k_wf_trace<TR_MIS, true><<<std::min(g, tb[2]), kWfBlock, 0, s>>>(
-                    sv, rp, st, st.q_mis, st.counts + 3, st.counts + 10, nullptr, bvh.n);
-            else k_wf_trace<TR_MIS, false><<<std::min(g, tb[2]), kWfBlock, 0, s>>>(
-                    sv, rp, st, st.q_mis, st.counts + 3, st.counts + 10, nullptr, bvh.n);
+            k_wf_compact<<<cgrid, kCompactThreads, 0, s>>>(st, q_fin, (int)P);
+            ++launches;
             TRY(cudaEventRecord(wf_ev_[5], s));
-            if (rec) k_wf_finalize<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, next, c_next);
-            else k_wf_finalize<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, cur, c_cur, next, c_next);
-            TRY(cudaEventRecord(wf_ev_[6], s));
-            launches += 5;
             TRY(cudaGetLastError());
             TRY(cudaMemcpyAsync(wf_counts_host_, st.counts, 32, cudaMemcpyDeviceToHost, s));
             TRY(cudaStreamSynchronize(s));
-            for (int k = 0; k < 6; ++k) {
+            for (int k = 0; k < 5; ++k) {
                 float ms = 0;
                 TRY(cudaEventElapsedTime(&ms, wf_ev_[k], wf_ev_[k + 1]));
                 last_stage_ms[k] += ms;
             }
             generated += take;
-            nnext = wf_counts_host_[1 - i_cur];
+            n_fin = n_ext;
+            n_cont = wf_counts_host_[0];
+            n_sh = wf_counts_host_[2];
+            n_mis = wf_counts_host_[3];
             nfree = wf_counts_host_[4];
-            std::swap(cur, next);
-            std::swap(c_cur, c_next);
-            i_cur = 1 - i_cur;
+            std::swap(q_ext, q_fin);
         }
         if (nfree != (uint32_t)P) return "wavefront: path pool did not drain";
         TRY(cudaEventRecord(wf_ev_[0], s));

@@ -92,9 +92,9 @@ class Tracer {
     long trace_sample_ = -1;
     float* trace_ = nullptr;
     int last_launches = 0;
-    // Wavefront: device time per stage (generate, extend, shade, shadow, mis, finalize) summed over
-    // the loop's iterations, and rays / node visits / triangle tests per traversal kind (extend,
-    // shadow, mis).  Zero for the megakernel.
+    // Wavefront: device time per stage (generate, trace, finalize, shade, compact, film gather)
+    // summed over the loop's iterations, and rays / node visits / triangle tests per traversal kind
+    // (path rays, shadow rays, MIS rays).  Zero for the megakernel.
     double last_stage_ms[6] = {0, 0, 0, 0, 0, 0};
     double last_kind_work[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 
@@ -108,7 +108,7 @@ class Tracer {
     long wf_cap_ = 0, wf_fs_cap_ = 0;
     uint32_t* wf_counts_host_ = nullptr;
     cudaEvent_t wf_ev_[7] = {nullptr};
-    unsigned wf_trace_blocks_[6] = {0, 0, 0, 0, 0, 0};  // resident blocks of k_wf_trace (wide x3, binary x3)
+    unsigned wf_trace_blocks_[2] = {0, 0};  // resident blocks of k_wf_trace (wide, binary) on this device
     SceneView view_{};
     WideBvh wide_;
     void* bufs_[16] = {nullptr};

@@ -285,11 +285,10 @@ __device__ __forceinline__ bool slab(const TraceRay& r, float tmax_ray, float mn
     return (tMin < tmax_ray) && (tMax > 0);
 }
 
-template <bool ANY>
-__device__ __forceinline__ bool leaf_test(const float4* __restrict__ tv, int leaf, const TraceRay& r, float& tmax,
-                                          int& best, float& bu, float& bv, float& binv) {
+__device__ __forceinline__ bool leaf_test(const bool any, const float4* __restrict__ tv, int leaf, const TraceRay& r,
+                                          float& tmax, int& best, float& bu, float& bv, float& binv) {
     const float4 a = __ldg(tv + 3 * leaf), b = __ldg(tv + 3 * leaf + 1), c = __ldg(tv + 3 * leaf + 2);
-    if (ANY) return tri_test_shadow(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax);
+    if (any) return tri_test_shadow(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax);
     float t, u, v, inv;
     if (tri_test(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax, t, u, v, inv)) {
         tmax = t;
@@ -326,9 +325,9 @@ struct Trav {
 };
 
 // Returns true when the ray needs traversal steps; false when it is already resolved (missed
-// the scene bounds, or a one-triangle scene).
-template <bool ANY>
-__device__ __forceinline__ bool trav_begin(Trav& t, const SceneView& sv, int nleaf, V3 o, V3 d, float tmax, Work& wk) {
+// the scene bounds, or a one-triangle scene).  any: any hit (shadow rays), else closest hit.
+__device__ __forceinline__ bool trav_begin(const bool any, Trav& t, const SceneView& sv, int nleaf, V3 o, V3 d,
+                                           float tmax, Work& wk) {
     t.r = make_trace_ray(o, d);
     t.tmax = tmax;
     t.bu = t.bv = t.binv = 0.f;
@@ -343,16 +342,15 @@ __device__ __forceinline__ bool trav_begin(Trav& t, const SceneView& sv, int nle
         return false;
     if (nleaf == 1) {
         ++wk.tris;
-        if (leaf_test<ANY>(sv.leaf_v, 0, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) t.best = 1;
+        if (leaf_test(any, sv.leaf_v, 0, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) t.best = 1;
         return false;
     }
     return true;
 }
 
 // One node; returns true when the traversal has finished.
-template <bool ANY>
-__device__ __forceinline__ bool trav_step_wide(Trav& t, const SceneView& sv, uint32_t* stack, uint32_t* err,
-                                               Work& wk) {
+__device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const SceneView& sv, uint32_t* stack,
+                                               uint32_t* err, Work& wk) {
     if ((unsigned)t.node >= (unsigned)sv.wcount) {
         atomicOr(err, DEV_ERR_BAD_INDEX);
         return true;
@@ -390,7 +388,7 @@ __device__ __forceinline__ bool trav_step_wide(Trav& t, const SceneView& sv, uin
             return true;
         }
         ++wk.tris;
-        if (leaf_test<ANY>(sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+        if (leaf_test(any, sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
             t.best = 1;
             return true;
         }
@@ -421,9 +419,8 @@ __device__ __forceinline__ bool trav_step_wide(Trav& t, const SceneView& sv, uin
     return false;
 }
 
-template <bool ANY>
-__device__ __forceinline__ bool trav_step_binary(Trav& t, const SceneView& sv, uint32_t* stack, uint32_t* err,
-                                                 Work& wk) {
+__device__ __forceinline__ bool trav_step_binary(const bool any, Trav& t, const SceneView& sv, uint32_t* stack,
+                                                 uint32_t* err, Work& wk) {
     const BvhNode* nd = sv.nodes + t.node;
     const float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
     const int4 lr = __ldg(&nd->d);
@@ -433,7 +430,7 @@ __device__ __forceinline__ bool trav_step_binary(Trav& t, const SceneView& sv, u
     bool hr = slab(t.r, t.tmax, b.z, b.w, c.x, c.y, c.z, c.w, tr);
     if (hl && lr.x < 0) {
         ++wk.tris;
-        if (leaf_test<ANY>(sv.leaf_v, ~lr.x, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+        if (leaf_test(any, sv.leaf_v, ~lr.x, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
             t.best = 1;
             return true;
         }
@@ -441,7 +438,7 @@ __device__ __forceinline__ bool trav_step_binary(Trav& t, const SceneView& sv, u
     }
     if (hr && lr.y < 0) {
         ++wk.tris;
-        if (leaf_test<ANY>(sv.leaf_v, ~lr.y, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+        if (leaf_test(any, sv.leaf_v, ~lr.y, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
             t.best = 1;
             return true;
         }
@@ -466,9 +463,9 @@ __device__ __forceinline__ bool trav_step_binary(Trav& t, const SceneView& sv, u
     return false;
 }
 
-template <bool ANY>
-__device__ __forceinline__ bool trav_step(Trav& t, const SceneView& sv, uint32_t* stack, uint32_t* err, Work& wk) {
-    return sv.wnodes ? trav_step_wide<ANY>(t, sv, stack, err, wk) : trav_step_binary<ANY>(t, sv, stack, err, wk);
+__device__ __forceinline__ bool trav_step(const bool any, Trav& t, const SceneView& sv, uint32_t* stack, uint32_t* err,
+                                          Work& wk) {
+    return sv.wnodes ? trav_step_wide(any, t, sv, stack, err, wk) : trav_step_binary(any, t, sv, stack, err, wk);
 }
 
 // Whole traversal: the hit primitive (closest) or 1 / -1 (any), -1 for a miss.
@@ -476,8 +473,8 @@ template <bool ANY>
 __device__ int traverse(const SceneView& sv, int nleaf, const TraceRay& r, float& tmax, float& bu, float& bv,
                         float& binv, uint32_t* stack, uint32_t* err, Work& wk) {
     Trav t;
-    if (trav_begin<ANY>(t, sv, nleaf, r.o, r.d, tmax, wk))
-        while (!trav_step<ANY>(t, sv, stack, err, wk)) {
+    if (trav_begin(ANY, t, sv, nleaf, r.o, r.d, tmax, wk))
+        while (!trav_step(ANY, t, sv, stack, err, wk)) {
         }
     tmax = t.tmax;
     bu = t.bu;

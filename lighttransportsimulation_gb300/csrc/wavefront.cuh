@@ -1,16 +1,20 @@
 // Wavefront path tracer (sm_103a): the same integrator as k_pathtrace, split into stage kernels
-// over a pool of path states and index queues, so each stage runs with its own (small) register
-// budget and all lanes of a warp execute the same stage:
+// over a pool of path states, so each stage runs with its own (small) register budget and all
+// lanes of a warp execute the same stage.  One iteration of the host loop runs
 //
-//   generate  fill free pool slots with new (pixel, sample) work: film + lens draws, camera ray
-//   extend    closest-hit traversal of every queued path ray
-//   shade     emission, SurfaceInteraction, material, light sample (NEE) + MIS BSDF sample,
-//             path BSDF sample, throughput, Russian roulette; queues shadow and MIS rays
-//   shadow    any-hit traversal of the NEE shadow rays
-//   mis       closest-hit traversal of the MIS BSDF rays, light radiance where they land
-//   finalize  adds the bounce's direct light in the reference's order (Ld = light part + MIS
-//             part, L += beta * Ld / lightPdf), mixes the deferred parity events, then stores a
-//             finished sample (radiance, film position) and frees its slot, or requeues the path
+//   generate  start new (pixel, sample) paths in free slots: film + lens draws, camera ray
+//   trace     one persistent launch over three ray lists: this iteration's path rays (closest
+//             hit), and the previous shade's NEE shadow rays (any hit) and MIS BSDF rays
+//             (closest hit, light radiance where they land)
+//   finalize  for the paths shaded in the previous iteration: their bounce's direct light in the
+//             reference's order (Ld = light part + MIS part, L += beta * Ld / lightPdf) and the
+//             deferred parity events; a finished path stores its sample (radiance, film
+//             position) and frees its slot
+//   shade     this iteration's hits: emission, SurfaceInteraction, material, light sample (NEE)
+//             + MIS BSDF sample, path BSDF sample, throughput, Russian roulette
+//   compact   one pass over the slots builds the next iteration's lists in slot order (path
+//             rays, shadow rays, MIS rays, free slots), so every stage reads and writes the
+//             structure-of-arrays path state in near-contiguous runs
 //   gather    after a chunk of samples per pixel has finished: one thread per film pixel sums the
 //             filter-weighted samples of its 3x3 source pixels in a fixed order (compensated FP32,
 //             then added to the FP64 film), so the film has no atomics and is reproducible
@@ -41,7 +45,8 @@ struct WfState {
     uint64_t *ev_mis, *ev_main;
     int32_t* mis_hit;
     int32_t *q_a, *q_b, *q_shadow, *q_mis, *q_free;
-    uint32_t* counts;  // [0] q_a size, [1] q_b size, [2] shadow, [3] mis, [4] free
+    uint32_t* counts;  // written by compact: [0] next path rays, [2] shadow, [3] mis, [4] free;
+                       // [8] trace fetch counter
     float4* fs_L;      // finished samples of the chunk: radiance rgb, film x (chunk index order)
     float* fs_y;       // film y
 };
@@ -61,18 +66,6 @@ __device__ __forceinline__ void rng_resume(Rng& r) {
     }
 }
 
-__device__ __forceinline__ int warp_push(uint32_t* counter, bool pred) {
-    const unsigned mask = __activemask();
-    const unsigned vote = __ballot_sync(mask, pred);
-    if (!pred) return -1;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(vote) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(vote));
-    base = __shfl_sync(vote, base, leader);
-    return (int)(base + __popc(vote & ((1u << lane) - 1u)));
-}
-
 __device__ __forceinline__ void camera_ray(const SceneView& sv, float pfx, float pfy, V3& rd, V3& rxd, V3& ryd,
                                            float spp_scale) {
     const float* cam = sv.cam;
@@ -86,16 +79,16 @@ __device__ __forceinline__ void camera_ray(const SceneView& sv, float pfx, float
     ryd = rd + (dy0 - rd) * spp_scale;
 }
 
-// generate: pops `take` free slots and starts samples gen0 .. gen0 + take - 1 of the chunk
-// (sample-major over the crop's pixels: w = (s - s0) * npix + pixel).
+// generate: starts samples gen0 .. gen0 + take - 1 of the chunk (sample-major over the crop's
+// pixels: w = (s - s0) * npix + pixel) in the first `take` free slots, appending them to the
+// path-ray list after its `n_cont` continuing paths.
 __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, const RenderParams rp, WfState st,
-                                                          int32_t* q_cur, uint32_t* c_cur, long gen0, uint32_t nfree,
-                                                          uint32_t take, int s0, long npix) {
+                                                          int32_t* q_ext, uint32_t n_cont, long gen0, uint32_t take,
+                                                          int s0, long npix) {
     const long t = (long)blockIdx.x * kWfBlock + threadIdx.x;
-    if (t == 0) st.counts[4] = nfree - take;
     if (t >= (long)take) return;
     const long w = gen0 + t;
-    const int slot = st.q_free[nfree - 1 - t];
+    const int slot = st.q_free[t];
     const int cw = rp.x1 - rp.x0;
     const int s = s0 + (int)(w / npix);
     const long pc = w % npix;
@@ -115,14 +108,14 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, co
     st.wid[slot] = (int32_t)w;
     st.draw[slot] = rng.draw;
     st.flags[slot] = 0u;
+    st.pend[slot] = 0u;
     st.pf[slot] = make_float2(pfx, pfy);
     st.ro[slot] = make_float4(sv.cam[0], sv.cam[1], sv.cam[2], 0.f);
     st.rd[slot] = make_float4(rd.x, rd.y, rd.z, 0.f);
     st.beta[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
     st.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
     st.sig[slot] = kSigBasis;
-    const int pos = warp_push(c_cur, true);
-    q_cur[pos] = slot;
+    q_ext[n_cont + t] = slot;
 }
 
 // Work counters: [0..2] all rays (rays, node visits, triangle tests), then the same three per
@@ -144,30 +137,29 @@ __device__ __forceinline__ void count_work(const RenderParams& rp, unsigned rays
 
 enum : int { TR_EXTEND = 0, TR_SHADOW = 1, TR_MIS = 2 };
 
+
 // The ray of path slot p for each traversal kind.
-template <int KIND>
-__device__ __forceinline__ bool wf_ray_begin(Trav& t, const SceneView& sv, const WfState& st, int p, int nleaf,
-                                             Work& wk) {
-    if (KIND == TR_EXTEND) {  // path ray, closest hit (BVH::intersect, BVH.cuh:365-398)
+__device__ __forceinline__ bool wf_ray_begin(int kind, Trav& t, const SceneView& sv, const WfState& st, int p,
+                                             int nleaf, Work& wk) {
+    if (kind == TR_EXTEND) {  // path ray, closest hit (BVH::intersect, BVH.cuh:365-398)
         const float4 o = st.ro[p], d = st.rd[p];
-        return trav_begin<false>(t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), INFINITY, wk);
-    } else if (KIND == TR_SHADOW) {  // VisibilityTester::unoccluded (VisibilityTester.cu:9-12), any hit
+        return trav_begin(false, t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), INFINITY, wk);
+    } else if (kind == TR_SHADOW) {  // VisibilityTester::unoccluded (VisibilityTester.cu:9-12), any hit
         const float4 o = st.sh_o[p], d = st.sh_d[p];
-        return trav_begin<true>(t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), d.w, wk);
+        return trav_begin(true, t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), d.w, wk);
     } else {  // MIS BSDF ray, closest hit
         const float4 o = st.mis_o[p], d = st.mis_d[p];
-        return trav_begin<false>(t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), INFINITY, wk);
+        return trav_begin(false, t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), INFINITY, wk);
     }
 }
 
 // Results of a finished traversal.  MIS: radiance of the sampled light where the BSDF ray lands
 // (IntegratorHelper.cuh:225-243).
-template <int KIND>
-__device__ __forceinline__ void wf_ray_end(const Trav& t, const SceneView& sv, WfState& st, int p) {
-    if (KIND == TR_EXTEND) {
+__device__ __forceinline__ void wf_ray_end(int kind, const Trav& t, const SceneView& sv, WfState& st, int p) {
+    if (kind == TR_EXTEND) {
         st.hprim[p] = t.best;
         st.huvi[p] = make_float4(t.bu, t.bv, t.binv, t.tmax);
-    } else if (KIND == TR_SHADOW) {
+    } else if (kind == TR_SHADOW) {
         st.vis[p] = t.best == 1 ? 0u : 1u;
     } else {
         const float4 d = st.mis_d[p], fv = st.mis_fv[p], x = st.mis_x[p];
@@ -194,33 +186,28 @@ __device__ __forceinline__ void wf_ray_end(const Trav& t, const SceneView& sv, W
     }
 }
 
-// Lanes left idle before a warp fetches new rays (while the queue lasts).
+// Lanes left idle before a warp fetches new rays (while the lists last).
 constexpr int kRefillIdle = 8;
 
-// Persistent traversal of one queue: each warp keeps up to 32 rays in flight; when at least
-// kRefillIdle lanes have finished, the warp claims that many queue entries with one atomic and
-// starts them, so lanes do not idle while the warp's longest ray finishes (dynamic ray fetch,
-// Aila and Laine, HPG 2009).  Launched with whole warps; `fetch` is zeroed before the launch.
-// WIDE: the 8-wide compressed BVH (sv.wnodes), else the binary LBVH.
-template <int KIND, bool WIDE>
+// Persistent traversal of the three ray lists as one index space [path rays | shadow rays | MIS
+// rays]: each warp keeps up to 32 rays in flight; when at least kRefillIdle lanes have finished,
+// the warp claims that many entries with one atomic and starts them, so lanes do not idle while
+// the warp's longest ray finishes (dynamic ray fetch, Aila and Laine, HPG 2009), and the short
+// shadow and MIS lists share the launch's tail with the path rays.  Launched with whole warps;
+// `fetch` is zeroed before the launch.  WIDE: the 8-wide compressed BVH, else the binary LBVH.
+template <bool WIDE>
 __global__ __launch_bounds__(kWfBlock) void k_wf_trace(const SceneView sv, const RenderParams rp, WfState st,
-                                                       const int32_t* __restrict__ q, const uint32_t* __restrict__ cnt,
-                                                       uint32_t* fetch, uint32_t* c_next, int nleaf) {
+                                                       const int32_t* __restrict__ q_ext, uint32_t n_ext,
+                                                       uint32_t n_sh, uint32_t n_mis, uint32_t* fetch, int nleaf) {
     __shared__ uint32_t s_stack[kStack * kWfBlock];
     uint32_t* stack = s_stack + threadIdx.x;
-    if (KIND == TR_EXTEND && blockIdx.x == 0 && threadIdx.x == 0) {  // queues shade and finalize push into
-        st.counts[2] = 0u;
-        st.counts[3] = 0u;
-        *c_next = 0u;
-    }
-    constexpr bool ANY = KIND == TR_SHADOW;
-    const uint32_t n = *cnt;
+    const uint32_t e1 = n_ext, e2 = n_ext + n_sh, n = n_ext + n_sh + n_mis;
     const unsigned lane = threadIdx.x & 31u;
     Trav t;
-    int p = -1;
+    int p = -1, kind = 0;
     bool active = false, exhausted = false;
-    Work wk{0u, 0u};
-    unsigned rays = 0;
+    Work wk[3] = {{0u, 0u}, {0u, 0u}, {0u, 0u}};
+    unsigned rays[3] = {0u, 0u, 0u};
     for (;;) {
         const unsigned idle = __ballot_sync(~0u, !active);
         if (!exhausted && __popc(idle) >= kRefillIdle) {
@@ -232,10 +219,12 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_trace(const SceneView sv, const
             if (!active) {
                 const uint32_t idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
                 if (idx < n) {
-                    p = q[idx];
-                    ++rays;
-                    active = wf_ray_begin<KIND>(t, sv, st, p, nleaf, wk);
-                    if (!active) wf_ray_end<KIND>(t, sv, st, p);
+                    kind = idx < e1 ? TR_EXTEND : (idx < e2 ? TR_SHADOW : TR_MIS);
+                    p = kind == TR_EXTEND ? q_ext[idx] : (kind == TR_SHADOW ? st.q_shadow[idx - e1] : st.q_mis[idx - e2]);
+                    ++rays[kind];
+                    Work& w = wk[kind];
+                    active = wf_ray_begin(kind, t, sv, st, p, nleaf, w);
+                    if (!active) wf_ray_end(kind, t, sv, st, p);
                 }
             }
         }
@@ -244,24 +233,27 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_trace(const SceneView sv, const
             continue;
         }
         for (;;) {
-            if (active && (WIDE ? trav_step_wide<ANY>(t, sv, stack, rp.err, wk)
-                                : trav_step_binary<ANY>(t, sv, stack, rp.err, wk))) {
-                wf_ray_end<KIND>(t, sv, st, p);
-                active = false;
+            if (active) {
+                Work& w = wk[kind];
+                const bool any = kind == TR_SHADOW;
+                if (WIDE ? trav_step_wide(any, t, sv, stack, rp.err, w) : trav_step_binary(any, t, sv, stack, rp.err, w)) {
+                    wf_ray_end(kind, t, sv, st, p);
+                    active = false;
+                }
             }
             const unsigned act = __ballot_sync(~0u, active);
             if (act == 0u || (!exhausted && 32 - __popc(act) >= kRefillIdle)) break;
         }
     }
-    count_work(rp, rays, wk, KIND);
+    for (int k = 0; k < 3; ++k) count_work(rp, rays[k], wk[k], k);
 }
 
 // shade: one bounce of PathTracingIntegrator::evaluate up to the next ray.
 template <bool RECORD>
 __global__ __launch_bounds__(kWfBlock) void k_wf_shade(const SceneView sv, const RenderParams rp, WfState st,
-                                                       const int32_t* __restrict__ q, const uint32_t* __restrict__ cnt) {
+                                                       const int32_t* __restrict__ q, uint32_t cnt) {
     const int t = blockIdx.x * kWfBlock + threadIdx.x;
-    if (t >= (int)*cnt) return;
+    if (t >= (int)cnt) return;
     const int p = q[t];
     const uint32_t flags = st.flags[p];
     const int bounce = (int)(flags >> 8);
@@ -433,10 +425,6 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_shade(const SceneView sv, const
             if (bounce + 1 >= rp.max_bounce) done = true;
         }
     }
-    const int pos_s = warp_push(&st.counts[2], (pend & WF_VIS) != 0);
-    if (pos_s >= 0) st.q_shadow[pos_s] = p;
-    const int pos_m = warp_push(&st.counts[3], (pend & WF_MIS) != 0);
-    if (pos_m >= 0) st.q_mis[pos_m] = p;
     st.pend[p] = pend | (done ? WF_DONE : 0u);
     st.draw[p] = rng.draw;
     st.flags[p] = ((uint32_t)(bounce + 1) << 8) | (specular ? 1u : 0u);
@@ -449,13 +437,13 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_shade(const SceneView sv, const
     }
 }
 
-// finalize: direct light of the bounce, deferred parity events, film or requeue.
+// finalize: direct light of the bounce, deferred parity events; a finished path stores its
+// sample and frees its slot (pix = -1).
 template <bool RECORD>
 __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, const RenderParams rp, WfState st,
-                                                          const int32_t* __restrict__ q, const uint32_t* __restrict__ cnt,
-                                                          int32_t* q_next, uint32_t* c_next) {
+                                                          const int32_t* __restrict__ q, uint32_t cnt) {
     const int t = blockIdx.x * kWfBlock + threadIdx.x;
-    if (t >= (int)*cnt) return;
+    if (t >= (int)cnt) return;
     const int p = q[t];
     const uint32_t pend = st.pend[p];
     float4 l4 = st.L[p];
@@ -486,8 +474,6 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
     }
     if (!(pend & WF_DONE)) {
         st.L[p] = make_float4(L.r, L.g, L.b, 0.f);
-        const int pos = warp_push(c_next, true);
-        q_next[pos] = p;
         return;
     }
     // Camera::addSample (Camera.cu:192-218): the sample reaches film pixels [ceil(pf - 1),
@@ -526,15 +512,82 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
         rp.sample_sig[k] = sig;
     }
     st.pix[p] = -1;
-    const int pos = warp_push(&st.counts[4], true);
-    st.q_free[pos] = p;
 }
 
-// Every slot starts free; counts (zeroed by the host) get the free-list size.
-__global__ void k_wf_init_free(int32_t* q_free, uint32_t* counts, int n) {
+// Every slot starts free (pix = -1, in the free list in slot order).
+__global__ void k_wf_init_free(int32_t* q_free, int32_t* pix, int n) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) q_free[t] = n - 1 - t;
-    if (t == 0) counts[4] = (uint32_t)n;
+    if (t < n) {
+        q_free[t] = t;
+        pix[t] = -1;
+    }
+}
+
+// compact: one pass over the pool after shade.  Every live slot (pix >= 0) was shaded in this
+// iteration, so its pend flags say which lists it joins: path rays (not finished), shadow rays
+// (WF_VIS), MIS rays (WF_MIS); a slot with pix < 0 is free.  Each block scans its tile of
+// kCompactTile slots and reserves its runs with one atomic per list, so every list is in slot
+// order within a tile.
+constexpr int kCompactThreads = 256, kCompactItems = 4, kCompactTile = kCompactThreads * kCompactItems;
+__global__ __launch_bounds__(kCompactThreads) void k_wf_compact(WfState st, int32_t* __restrict__ q_ext_next, int P) {
+    __shared__ uint32_t s_warp[4][kCompactThreads / 32];
+    __shared__ uint32_t s_base[4];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int first = blockIdx.x * kCompactTile + tid * kCompactItems;
+    uint32_t flags[kCompactItems];
+    uint32_t cnt[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < kCompactItems; ++k) {
+        const int slot = first + k;
+        uint32_t f = 0;
+        if (slot < P) {
+            if (st.pix[slot] >= 0) {
+                const uint32_t pend = st.pend[slot];
+                f = ((pend & WF_DONE) ? 0u : 1u) | ((pend & WF_VIS) ? 2u : 0u) | ((pend & WF_MIS) ? 4u : 0u);
+            } else {
+                f = 8u;
+            }
+        }
+        flags[k] = f;
+#pragma unroll
+        for (int l = 0; l < 4; ++l) cnt[l] += (f >> l) & 1u;
+    }
+    // exclusive scan of the four counts over the block (warp shuffles, then the warps' totals)
+    uint32_t incl[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        uint32_t v = cnt[l];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(~0u, v, o);
+            if (lane >= o) v += u;
+        }
+        incl[l] = v;
+        if (lane == 31) s_warp[l][warp] = v;
+    }
+    __syncthreads();
+    if (tid < 4) {
+        uint32_t tot = 0;
+        for (int w = 0; w < kCompactThreads / 32; ++w) {
+            const uint32_t v = s_warp[tid][w];
+            s_warp[tid][w] = tot;
+            tot += v;
+        }
+        uint32_t* c = st.counts + (tid == 0 ? 0 : tid + 1);  // [0] path rays, [2] shadow, [3] mis, [4] free
+        s_base[tid] = tot ? atomicAdd(c, tot) : 0u;
+    }
+    __syncthreads();
+    int32_t* dst[4] = {q_ext_next, st.q_shadow, st.q_mis, st.q_free};
+    uint32_t pos[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) pos[l] = s_base[l] + s_warp[l][warp] + incl[l] - cnt[l];
+#pragma unroll
+    for (int k = 0; k < kCompactItems; ++k) {
+        const uint32_t f = flags[k];
+#pragma unroll
+        for (int l = 0; l < 4; ++l)
+            if ((f >> l) & 1u) dst[l][pos[l]++] = first + k;
+    }
 }
 
 // Film gather: thread (x, y) over the crop's film footprint [x0, x1 + 2) x [y0, y1 + 2) sums, in
