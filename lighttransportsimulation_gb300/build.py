@@ -16,6 +16,9 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "liblts_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Extra nvcc arguments for tuning builds (e.g. LTS_NVCC_EXTRA="-DLTS_TRACE_MIN_BLOCKS=5"); pass
+# force=True (or delete _lib/obj) when changing them.
+EXTRA = os.environ.get("LTS_NVCC_EXTRA", "").split()
 
 
 def _nvcc():
@@ -52,7 +55,7 @@ def build(verbose=False, force=False):
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                         "-Xptxas", "-warn-spills", "-c", src, "-o", obj])
+                         "-Xptxas", "-warn-spills", *EXTRA, "-c", src, "-o", obj])
     for f in cpp:
         src = os.path.join(CSRC, f)
         obj = os.path.join(LIBDIR, "obj", f + ".o")

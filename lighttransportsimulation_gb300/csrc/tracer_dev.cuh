@@ -348,6 +348,37 @@ __device__ __forceinline__ bool trav_begin(const bool any, Trav& t, const SceneV
     return true;
 }
 
+// Child-box test of a wide node in FMA form.  Per node and axis: A = scale * inv,
+// B = (p - o) * inv, so a plane's distance is q * A + B; both end planes are moved outwards by
+// E = 16 * 2^-24 * |inv| * (|p| + |o| + 255 scale), which bounds the rounding of this form and of
+// the reference's ((p + q scale) - o) * inv alike, so the interval contains the one the
+// reference's box test computes for the decoded box; the far planes then get the reference's
+// (1 + 2 gamma(3)) factor.  Needs finite inv (see trav_step_wide).
+struct WideAxis {
+    float A, Bn, Af, Bf;
+    uint32_t near_lo, near_hi, far_lo, far_hi;  // the 8 near / far plane bytes of the axis
+};
+__device__ __forceinline__ WideAxis wide_axis(float p, float o, float inv, uint32_t ebyte, bool neg, uint32_t lo0,
+                                              uint32_t lo1, uint32_t hi0, uint32_t hi1) {
+    WideAxis a;
+    const float sc = wide_scale(ebyte);
+    const float A = sc * inv;
+    const float B = (p - o) * inv;
+    const float E = (16.0f * 5.9604645e-8f) * fabsf(inv) * (fabsf(p) + fabsf(o) + 255.0f * sc);
+    a.A = A;
+    a.Bn = B - E;
+    a.Af = A * kSlabScale;
+    a.Bf = (B + E) * kSlabScale;
+    a.near_lo = neg ? hi0 : lo0;
+    a.near_hi = neg ? hi1 : lo1;
+    a.far_lo = neg ? lo0 : hi0;
+    a.far_hi = neg ? lo1 : hi1;
+    return a;
+}
+__device__ __forceinline__ float wide_byte(uint32_t lo, uint32_t hi, int s) {
+    return __uint2float_rn(((s < 4 ? lo : hi) >> ((s & 3) * 8)) & 0xffu);
+}
+
 // One node; returns true when the traversal has finished.
 __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const SceneView& sv, uint32_t* stack,
                                                uint32_t* err, Work& wk) {
@@ -361,21 +392,42 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
     const uint4 m = __ldg(&nd->m), q0 = __ldg(&nd->q0), q1 = __ldg(&nd->q1), q2 = __ldg(&nd->q2);
     ++wk.nodes;
     const uint32_t hb = __float_as_uint(h.w);
-    const float sx = wide_scale(hb & 0xffu), sy = wide_scale((hb >> 8) & 0xffu), sz = wide_scale((hb >> 16) & 0xffu);
     const uint32_t imask = hb >> 24, omask = m.z;
     uint32_t hits = 0, leaves = 0;
+    if (isfinite(t.r.inv.x) && isfinite(t.r.inv.y) && isfinite(t.r.inv.z)) {
+        const WideAxis ax = wide_axis(h.x, t.r.o.x, t.r.inv.x, hb & 0xffu, t.r.neg[0], q0.x, q0.y, q1.z, q1.w);
+        const WideAxis ay = wide_axis(h.y, t.r.o.y, t.r.inv.y, (hb >> 8) & 0xffu, t.r.neg[1], q0.z, q0.w, q2.x, q2.y);
+        const WideAxis az = wide_axis(h.z, t.r.o.z, t.r.inv.z, (hb >> 16) & 0xffu, t.r.neg[2], q1.x, q1.y, q2.z, q2.w);
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        if (!((omask >> s) & 1u)) continue;
-        const int sh = (s & 3) * 8;
-        const uint32_t lx = ((s < 4 ? q0.x : q0.y) >> sh) & 0xffu, ly = ((s < 4 ? q0.z : q0.w) >> sh) & 0xffu;
-        const uint32_t lz = ((s < 4 ? q1.x : q1.y) >> sh) & 0xffu, hx = ((s < 4 ? q1.z : q1.w) >> sh) & 0xffu;
-        const uint32_t hy = ((s < 4 ? q2.x : q2.y) >> sh) & 0xffu, hz = ((s < 4 ? q2.z : q2.w) >> sh) & 0xffu;
-        float te;
-        if (slab(t.r, t.tmax, wide_plane(h.x, lx, sx), wide_plane(h.y, ly, sy), wide_plane(h.z, lz, sz),
-                 wide_plane(h.x, hx, sx), wide_plane(h.y, hy, sy), wide_plane(h.z, hz, sz), te)) {
-            if ((imask >> s) & 1u) hits |= 1u << ((uint32_t)s ^ oct);
-            else leaves |= 1u << s;
+        for (int s = 0; s < 8; ++s) {
+            if (!((omask >> s) & 1u)) continue;
+            const float tnx = fmaf(wide_byte(ax.near_lo, ax.near_hi, s), ax.A, ax.Bn);
+            const float tny = fmaf(wide_byte(ay.near_lo, ay.near_hi, s), ay.A, ay.Bn);
+            const float tnz = fmaf(wide_byte(az.near_lo, az.near_hi, s), az.A, az.Bn);
+            const float tfx = fmaf(wide_byte(ax.far_lo, ax.far_hi, s), ax.Af, ax.Bf);
+            const float tfy = fmaf(wide_byte(ay.far_lo, ay.far_hi, s), ay.Af, ay.Bf);
+            const float tfz = fmaf(wide_byte(az.far_lo, az.far_hi, s), az.Af, az.Bf);
+            const float tn = fmaxf(fmaxf(tnx, tny), tnz), tf = fminf(fminf(tfx, tfy), tfz);
+            if (tn <= tf && tn < t.tmax && tf > 0.0f) {
+                if ((imask >> s) & 1u) hits |= 1u << ((uint32_t)s ^ oct);
+                else leaves |= 1u << s;
+            }
+        }
+    } else {  // an axis-parallel ray: the reference's slab test on the decoded planes
+        const float sx = wide_scale(hb & 0xffu), sy = wide_scale((hb >> 8) & 0xffu), sz = wide_scale((hb >> 16) & 0xffu);
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            if (!((omask >> s) & 1u)) continue;
+            const int sh = (s & 3) * 8;
+            const uint32_t lx = ((s < 4 ? q0.x : q0.y) >> sh) & 0xffu, ly = ((s < 4 ? q0.z : q0.w) >> sh) & 0xffu;
+            const uint32_t lz = ((s < 4 ? q1.x : q1.y) >> sh) & 0xffu, hx = ((s < 4 ? q1.z : q1.w) >> sh) & 0xffu;
+            const uint32_t hy = ((s < 4 ? q2.x : q2.y) >> sh) & 0xffu, hz = ((s < 4 ? q2.z : q2.w) >> sh) & 0xffu;
+            float te;
+            if (slab(t.r, t.tmax, wide_plane(h.x, lx, sx), wide_plane(h.y, ly, sy), wide_plane(h.z, lz, sz),
+                     wide_plane(h.x, hx, sx), wide_plane(h.y, hy, sy), wide_plane(h.z, hz, sz), te)) {
+                if ((imask >> s) & 1u) hits |= 1u << ((uint32_t)s ^ oct);
+                else leaves |= 1u << s;
+            }
         }
     }
     const uint32_t lmask = omask & ~imask;

@@ -188,6 +188,11 @@ __device__ __forceinline__ void wf_ray_end(int kind, const Trav& t, const SceneV
 
 // Lanes left idle before a warp fetches new rays (while the lists last).
 constexpr int kRefillIdle = 8;
+// Resident blocks per SM the trace kernel is compiled for (caps its registers).
+#ifndef LTS_TRACE_MIN_BLOCKS
+#define LTS_TRACE_MIN_BLOCKS 7
+#endif
+constexpr int kTraceMinBlocks = LTS_TRACE_MIN_BLOCKS;
 
 // Persistent traversal of the three ray lists as one index space [path rays | shadow rays | MIS
 // rays]: each warp keeps up to 32 rays in flight; when at least kRefillIdle lanes have finished,
@@ -196,7 +201,7 @@ constexpr int kRefillIdle = 8;
 // shadow and MIS lists share the launch's tail with the path rays.  Launched with whole warps;
 // `fetch` is zeroed before the launch.  WIDE: the 8-wide compressed BVH, else the binary LBVH.
 template <bool WIDE>
-__global__ __launch_bounds__(kWfBlock) void k_wf_trace(const SceneView sv, const RenderParams rp, WfState st,
+__global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const SceneView sv, const RenderParams rp, WfState st,
                                                        const int32_t* __restrict__ q_ext, uint32_t n_ext,
                                                        uint32_t n_sh, uint32_t n_mis, uint32_t* fetch, int nleaf) {
     __shared__ uint32_t s_stack[kStack * kWfBlock];
@@ -206,8 +211,25 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_trace(const SceneView sv, const
     Trav t;
     int p = -1, kind = 0;
     bool active = false, exhausted = false;
-    Work wk[3] = {{0u, 0u}, {0u, 0u}, {0u, 0u}};
-    unsigned rays[3] = {0u, 0u, 0u};
+    Work cur{0u, 0u};  // work of the ray in flight, credited to its kind when it finishes
+    Work w0{0u, 0u}, w1{0u, 0u}, w2{0u, 0u};
+    unsigned r0 = 0, r1 = 0, r2 = 0;
+    auto credit = [&]() {
+        if (kind == TR_EXTEND) {
+            w0.nodes += cur.nodes;
+            w0.tris += cur.tris;
+            ++r0;
+        } else if (kind == TR_SHADOW) {
+            w1.nodes += cur.nodes;
+            w1.tris += cur.tris;
+            ++r1;
+        } else {
+            w2.nodes += cur.nodes;
+            w2.tris += cur.tris;
+            ++r2;
+        }
+        cur.nodes = cur.tris = 0u;
+    };
     for (;;) {
         const unsigned idle = __ballot_sync(~0u, !active);
         if (!exhausted && __popc(idle) >= kRefillIdle) {
@@ -221,10 +243,11 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_trace(const SceneView sv, const
                 if (idx < n) {
                     kind = idx < e1 ? TR_EXTEND : (idx < e2 ? TR_SHADOW : TR_MIS);
                     p = kind == TR_EXTEND ? q_ext[idx] : (kind == TR_SHADOW ? st.q_shadow[idx - e1] : st.q_mis[idx - e2]);
-                    ++rays[kind];
-                    Work& w = wk[kind];
-                    active = wf_ray_begin(kind, t, sv, st, p, nleaf, w);
-                    if (!active) wf_ray_end(kind, t, sv, st, p);
+                    active = wf_ray_begin(kind, t, sv, st, p, nleaf, cur);
+                    if (!active) {
+                        wf_ray_end(kind, t, sv, st, p);
+                        credit();
+                    }
                 }
             }
         }
@@ -234,10 +257,11 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_trace(const SceneView sv, const
         }
         for (;;) {
             if (active) {
-                Work& w = wk[kind];
                 const bool any = kind == TR_SHADOW;
-                if (WIDE ? trav_step_wide(any, t, sv, stack, rp.err, w) : trav_step_binary(any, t, sv, stack, rp.err, w)) {
+                if (WIDE ? trav_step_wide(any, t, sv, stack, rp.err, cur)
+                         : trav_step_binary(any, t, sv, stack, rp.err, cur)) {
                     wf_ray_end(kind, t, sv, st, p);
+                    credit();
                     active = false;
                 }
             }
@@ -245,12 +269,18 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_trace(const SceneView sv, const
             if (act == 0u || (!exhausted && 32 - __popc(act) >= kRefillIdle)) break;
         }
     }
-    for (int k = 0; k < 3; ++k) count_work(rp, rays[k], wk[k], k);
+    count_work(rp, r0, w0, TR_EXTEND);
+    count_work(rp, r1, w1, TR_SHADOW);
+    count_work(rp, r2, w2, TR_MIS);
 }
 
 // shade: one bounce of PathTracingIntegrator::evaluate up to the next ray.
+// Resident blocks per SM the shade kernel is compiled for (caps its registers).
+#ifndef LTS_SHADE_MIN_BLOCKS
+#define LTS_SHADE_MIN_BLOCKS 4
+#endif
 template <bool RECORD>
-__global__ __launch_bounds__(kWfBlock) void k_wf_shade(const SceneView sv, const RenderParams rp, WfState st,
+__global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(const SceneView sv, const RenderParams rp, WfState st,
                                                        const int32_t* __restrict__ q, uint32_t cnt) {
     const int t = blockIdx.x * kWfBlock + threadIdx.x;
     if (t >= (int)cnt) return;
