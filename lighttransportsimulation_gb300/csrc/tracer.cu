@@ -444,6 +444,7 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
         puv[t] = make_int4(sc.tri_uv[3 * t], sc.tri_uv[3 * t + 1], sc.tri_uv[3 * t + 2], 0);
     }
     std::vector<DevMat> mats(sc.materials.size());
+    std::vector<int> class_keys;  // shade classes: distinct (kind, Oren-Nayar, texture kinds) in order of appearance
     for (size_t m = 0; m < mats.size(); ++m) {
         const HostMaterial& h = sc.materials[m];
         mats[m].kind = h.kind;
@@ -454,6 +455,15 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
             mats[m].tex[k].kind = h.tex[k].kind;
             for (int q = 0; q < 4; ++q) mats[m].tex[k].v[q] = h.tex[k].v[q];
         }
+        const int key = ((h.kind * 2 + (h.extra != 0.0f ? 1 : 0)) * 8 + h.tex[0].kind) * 8 + h.tex[1].kind;
+        int c = -1;
+        for (size_t u = 0; u < class_keys.size(); ++u)
+            if (class_keys[u] == key) c = (int)u;
+        if (c < 0) {
+            c = (int)class_keys.size();
+            class_keys.push_back(key);
+        }
+        mats[m].shade_class = 1 + c % (kShadeClasses - 1);
     }
     std::vector<DevLight> lights(sc.lights.size());
     for (size_t l = 0; l < lights.size(); ++l) {
@@ -633,7 +643,8 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
     const long P = std::max<long>(1, std::min<long>(chunk_total, wf_pool > 0 ? wf_pool : (1l << 21)));
     WfState st{};
     if (wf_cap_ < P) {
-        for (int k = 0; k < 33; ++k) {
+        for (int k : {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26,
+                      27, 28, 29, 30, 31, 32, 35}) {
             if (wf_bufs_[k]) dev_free(wf_bufs_[k]);
             wf_bufs_[k] = nullptr;
         }
@@ -642,9 +653,10 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
         const size_t sizes[] = {4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n,                       // pix smp draw flags pend vis
                                 16 * n, 16 * n, 16 * n, 16 * n, 8 * n, 8 * n, 4 * n, 16 * n,  // ro rd beta L pf sig hprim huvi
                                 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n, 16 * n,  // sh_* mis_* ld nee
-                                8 * n, 8 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 64,  // ev mis_hit queues counts
-                                4 * n};                                                          // wid
+                                8 * n, 8 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 256,  // ev mis_hit queues counts
+                                4 * n};                                                           // wid
         for (size_t k = 0; k < sizeof sizes / sizeof sizes[0]; ++k) TRY(dev_alloc(&wf_bufs_[k], sizes[k]));
+        TRY(dev_alloc(&wf_bufs_[35], 4 * (size_t)kShadeClasses * n));  // class-grouped shade lists
         wf_cap_ = P;
     }
     if (wf_fs_cap_ < chunk_total) {
@@ -669,6 +681,7 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
     st.q_a = (int32_t*)b[26]; st.q_b = (int32_t*)b[27]; st.q_shadow = (int32_t*)b[28]; st.q_mis = (int32_t*)b[29];
     st.q_free = (int32_t*)b[30]; st.counts = (uint32_t*)b[31]; st.wid = (int32_t*)b[32];
     st.fs_L = (float4*)b[33]; st.fs_y = (float*)b[34];
+    st.q_cls = (int32_t*)b[35];
     if (rp.sample_sig) {
         TRY(cudaMemsetAsync(st.ev_mis, 0, 8 * (size_t)P, s));
         TRY(cudaMemsetAsync(st.ev_main, 0, 8 * (size_t)P, s));
@@ -706,7 +719,7 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
             const uint32_t n_ext = n_cont + take;
             if (n_ext == 0 && n_fin == 0) break;
             if (iters > 1000000) return "wavefront did not converge";
-            TRY(cudaMemsetAsync(st.counts, 0, 64, s));
+            TRY(cudaMemsetAsync(st.counts, 0, 256, s));
             TRY(cudaEventRecord(wf_ev_[0], s));
             if (take) {
                 k_wf_generate<<<blocks(take), kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_cont, generated, take, s0, npix);
@@ -728,9 +741,11 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
             }
             TRY(cudaEventRecord(wf_ev_[3], s));
             if (n_ext) {
-                if (rec) k_wf_shade<true><<<blocks(n_ext), kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_ext);
-                else k_wf_shade<false><<<blocks(n_ext), kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_ext);
-                ++launches;
+                k_wf_classify<<<blocks(n_ext), kWfBlock, 0, s>>>(sv, st, q_ext, n_ext, (int)P);
+                const unsigned g = blocks(n_ext) + kShadeClasses;
+                if (rec) k_wf_shade<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, (int)P);
+                else k_wf_shade<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, (int)P);
+                launches += 2;
             }
             TRY(cudaEventRecord(wf_ev_[4], s));
             k_wf_compact<<<cgrid, kCompactThreads, 0, s>>>(st, q_fin, (int)P);

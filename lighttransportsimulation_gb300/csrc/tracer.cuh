@@ -21,7 +21,9 @@ struct DevMat {
     int32_t kind;
     float extra, on_a, on_b;
     DevTex tex[2];
+    int32_t shade_class;  // 1..15: materials with the same BSDF and texture kinds share a class
 };
+constexpr int kShadeClasses = 16;  // class 0: rays that left the scene
 struct DevLight {
     int32_t kind, prim;
     float L[3], p[3], radius, area;

@@ -46,7 +46,8 @@ struct WfState {
     int32_t* mis_hit;
     int32_t *q_a, *q_b, *q_shadow, *q_mis, *q_free;
     uint32_t* counts;  // written by compact: [0] next path rays, [2] shadow, [3] mis, [4] free;
-                       // [8] trace fetch counter
+                       // [8] trace fetch counter; [16 + c] paths of shade class c (classify)
+    int32_t* q_cls;    // [kShadeClasses][pool] this iteration's paths grouped by shade class
     float4* fs_L;      // finished samples of the chunk: radiance rgb, film x (chunk index order)
     float* fs_y;       // film y
 };
@@ -275,16 +276,50 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
 }
 
 // shade: one bounce of PathTracingIntegrator::evaluate up to the next ray.
-// Resident blocks per SM the shade kernel is compiled for (caps its registers).
-#ifndef LTS_SHADE_MIN_BLOCKS
-#define LTS_SHADE_MIN_BLOCKS 4
-#endif
-template <bool RECORD>
-__global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(const SceneView sv, const RenderParams rp, WfState st,
-                                                       const int32_t* __restrict__ q, uint32_t cnt) {
+// classify: groups this iteration's paths by the shade class of what they hit (0: left the
+// scene), so that shade runs warps over one material kind at a time.
+__global__ __launch_bounds__(kWfBlock) void k_wf_classify(const SceneView sv, WfState st, const int32_t* __restrict__ q,
+                                                          uint32_t cnt, int pool) {
     const int t = blockIdx.x * kWfBlock + threadIdx.x;
     if (t >= (int)cnt) return;
     const int p = q[t];
+    const int prim = st.hprim[p];
+    const int c = prim < 0 ? 0 : sv.mats[__ldg(&sv.prim_n[prim].w)].shade_class;
+    const unsigned grp = __match_any_sync(__activemask(), c);
+    const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(st.counts + 16 + c, (uint32_t)__popc(grp));
+    base = __shfl_sync(grp, base, leader);
+    st.q_cls[(size_t)c * pool + base + __popc(grp & ((1u << lane) - 1u))] = p;
+}
+
+// Block b of shade -> (class, entry): classes take consecutive runs of blocks.
+__device__ __forceinline__ int shade_entry(const WfState& st, int pool) {
+    __shared__ uint32_t s_cnt[kShadeClasses];
+    if (threadIdx.x < kShadeClasses) s_cnt[threadIdx.x] = st.counts[16 + threadIdx.x];
+    __syncthreads();
+    uint32_t b = blockIdx.x;
+    for (int c = 0; c < kShadeClasses; ++c) {
+        const uint32_t nb = (s_cnt[c] + kWfBlock - 1) / kWfBlock;
+        if (b < nb) {
+            const uint32_t i = b * kWfBlock + threadIdx.x;
+            return i < s_cnt[c] ? st.q_cls[(size_t)c * pool + i] : -1;
+        }
+        b -= nb;
+    }
+    return -1;
+}
+
+// Resident blocks per SM the shade kernel is compiled for (caps its registers).
+#ifndef LTS_SHADE_MIN_BLOCKS
+#define LTS_SHADE_MIN_BLOCKS 5
+#endif
+// Launched with ceil(paths / kWfBlock) + kShadeClasses blocks over the class-grouped lists.
+template <bool RECORD>
+__global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(const SceneView sv, const RenderParams rp,
+                                                                              WfState st, int pool) {
+    const int p = shade_entry(st, pool);
+    if (p < 0) return;
     const uint32_t flags = st.flags[p];
     const int bounce = (int)(flags >> 8);
     bool specular = (flags & 1u) != 0;
