@@ -25,6 +25,7 @@ Inputs (BVH + triangles, ~150 MB) exceed the 129 MB L2, so no flush runs between
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -212,6 +213,22 @@ def lbvh_bench(ctx, n, steps, warmup, mode, peaks):
             "frac_of_hbm": round(gbs / peaks["hbm_gbs"], 4)}
 
 
+def profiled_traffic(kernel, workload, bvh_width):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary (dram__bytes_read.sum +
+    dram__bytes_write.sum over every launch of one render, divided by the launches), or None."""
+    path = os.path.join(ROOT, "profiles", "trace_wavefront_bench.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        m = re.search(r"<!-- traffic: (.*) -->", line)
+        if not m:
+            continue
+        kv = dict(x.split("=", 1) for x in m.group(1).split())
+        if kv.get("kernel") == kernel and kv.get("workload") == workload and kv.get("bvh_width") == str(bvh_width):
+            return int(kv["bytes_per_launch"])
+    return None
+
+
 def run_gpu(args, wl):
     import ctypes
 
@@ -278,6 +295,7 @@ def run_gpu(args, wl):
         kernel_ms = mr.render_stage_ms[1]
         kernel_launches = mr.render_iterations
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
+    traffic = profiled_traffic(kernel, wl["name"], args.bvh_width)
 
     # end to end through the public API: upload scene (H2D), build, render, read film (D2H)
     h2d = scene.info["triangles"] * 48 + scene.info["triangles"] * 16 * 2
@@ -312,7 +330,8 @@ def run_gpu(args, wl):
             "e2e": {"value": round(e2e, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "seconds_per_step": round(e2e_s, 4)},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                         "frac": round(achieved / peaks["hbm_gbs"], 4),
+                         "traffic": traffic, "traffic_source": "profiles/trace_wavefront_bench.md" if traffic else None,
                          "kernel": kernel, "launches_per_step": kernel_launches,
                          "kernel_ms_per_step": round(kernel_ms, 3), "peak_kind": peak_kind,
                          "algorithmic": alg_text, "algorithmic_bytes_per_step": alg_bytes},
