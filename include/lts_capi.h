@@ -135,6 +135,7 @@ int lts_bvh_build_noalloc(const float* d_tri_p9, int32_t n, int32_t mode, int32_
 /* ---------------------------------------------------------------- rendering */
 #define LTS_INTEGRATOR_MEGAKERNEL 0 /* one thread per pixel, all spp and bounces        */
 #define LTS_INTEGRATOR_WAVEFRONT 1  /* generate / extend / shade / shadow / film queues  */
+#define LTS_INTEGRATOR_FP64 2       /* the megakernel in double: FP64 oracle renders      */
 
 typedef struct {
     int32_t spp, max_bounce, rr_start;

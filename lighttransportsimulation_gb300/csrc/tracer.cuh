@@ -67,6 +67,13 @@ struct RenderParams {
     long trace_sample;               // crop sample index traced (-1: none)
 };
 
+// The procedural textures' tables (host copies): the 512-entry Perlin permutation and the
+// 10 x 3 marble colours; each translation unit with device textures uploads its own.
+void texture_tables(unsigned char perm512[512], const float** marble30);
+
+// FP64 oracle renderer (render64.cu): the megakernel integrator in double on the binary LBVH.
+std::string render64_launch(const SceneView& sv, const RenderParams& rp, int nleaf, bool record, cudaStream_t s);
+
 class Tracer {
    public:
     Tracer() = default;

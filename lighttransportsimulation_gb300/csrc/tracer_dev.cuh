@@ -18,10 +18,18 @@ namespace {
 //   u > 1.0 + SHADOW_EPSILON  <=>  u >= kOnePlusEpsUp    (Triangle.cu:72,78)
 //   x > 1e-4                  <=>  x >= 0.0001f          (models/Microfacet.cuh:32)
 //   cosT > .9999              <=>  cosT >= kOneMinusEpsUp (models/Microfacet.cuh:56)
+// (the FP64 build compares in double: the next double above 1 -+ 1e-4)
+#if LTS_FP64
+#define kShadowEps 1e-4
+#define kOneMinusEpsUp __longlong_as_double(__double_as_longlong(1.0 - 1e-4) + 1)
+#define kOnePlusEpsUp __longlong_as_double(__double_as_longlong(1.0 + 1e-4) + 1)
+#define kSlabScale (1.0 + 2.0 * gamma_n(3))
+#else
 #define kShadowEps 0.0001f
 #define kOneMinusEpsUp __int_as_float(0x3f7ff973)
 #define kOnePlusEpsUp __int_as_float(0x3f800347)
 #define kSlabScale (1.0f + 2.0f * gamma_n(3))
+#endif
 
 // Per-thread traversal stack in shared memory, in 32-bit words (binary: one node per word; wide:
 // one node group per two words).
@@ -137,20 +145,20 @@ __device__ __forceinline__ V3 normal_at(const SceneView& sv, int idx) {
 
 // ------------------------------------------------------------------ triangle tests
 // Triangle::intersect test part (shapes/Triangle.cu:94-128).
-__device__ __forceinline__ bool tri_test(V3 p0, V3 p1, V3 p2, V3 o, V3 d, float tmax, float& t_out, float& u_out,
-                                         float& v_out, float& inv_out) {
+__device__ __forceinline__ bool tri_test(V3 p0, V3 p1, V3 p2, V3 o, V3 d, real tmax, real& t_out, real& u_out,
+                                         real& v_out, real& inv_out) {
     const V3 e1 = p1 - p0, e2 = p2 - p0;
     const V3 pv = cross(d, e2);
-    const float det = dot(e1, pv);
+    const real det = dot(e1, pv);
     if (det == 0) return false;
-    const float inv = __frcp_rn(det);  // == (float)(1.0 / (double)det)
+    const real inv = xrcp(det);  // == (real)(1.0 / (double)det)
     const V3 tv = o - p0;
-    const float u = inv * dot(tv, pv);
+    const real u = inv * dot(tv, pv);
     if (u < kShadowEps || u >= kOneMinusEpsUp) return false;
     const V3 qv = cross(tv, e1);
-    const float v = inv * dot(d, qv);
+    const real v = inv * dot(d, qv);
     if (v < kShadowEps || u + v >= kOneMinusEpsUp) return false;
-    const float t = inv * dot(e2, qv);
+    const real t = inv * dot(e2, qv);
     if (!(t > 0 && t < tmax)) return false;
     t_out = t;
     u_out = u;
@@ -159,19 +167,19 @@ __device__ __forceinline__ bool tri_test(V3 p0, V3 p1, V3 p2, V3 o, V3 d, float 
     return true;
 }
 // Triangle::simpleIntersect (shapes/Triangle.cu:50-84): swapped edges, grown bound.
-__device__ __forceinline__ bool tri_test_shadow(V3 p0, V3 p1, V3 p2, V3 o, V3 d, float tmax) {
+__device__ __forceinline__ bool tri_test_shadow(V3 p0, V3 p1, V3 p2, V3 o, V3 d, real tmax) {
     const V3 e1 = p1 - p0, e2 = p2 - p0;
     const V3 pv = cross(d, e1);
-    const float det = dot(e2, pv);
+    const real det = dot(e2, pv);
     if (det == 0) return false;
-    const float inv = __frcp_rn(det);
+    const real inv = xrcp(det);
     const V3 tv = o - p0;
-    const float u = inv * dot(tv, pv);
+    const real u = inv * dot(tv, pv);
     if (u < kShadowEps || u >= kOnePlusEpsUp) return false;
     const V3 qv = cross(tv, e2);
-    const float v = inv * dot(d, qv);
+    const real v = inv * dot(d, qv);
     if (v < kShadowEps || u + v >= kOnePlusEpsUp) return false;
-    const float t = inv * dot(e1, qv);
+    const real t = inv * dot(e1, qv);
     return t > 0 && t < tmax;
 }
 
@@ -186,7 +194,7 @@ struct SI {
 
 __device__ __forceinline__ void coordinate_system(V3 v1, V3& v2, V3& v3o) {
     // Geometry.cuh:250-258
-    if (fabsf(v1.x) > fabsf(v1.y))
+    if (xabs(v1.x) > xabs(v1.y))
         v2 = v3(-v1.z, 0, v1.x) * rsqrt_q3(v1.x * v1.x + v1.z * v1.z);
     else
         v2 = v3(0, v1.z, -v1.y) * rsqrt_q3(v1.y * v1.y + v1.z * v1.z);
@@ -195,20 +203,20 @@ __device__ __forceinline__ void coordinate_system(V3 v1, V3& v2, V3& v3o) {
 
 // Builds the SurfaceInteraction of a hit (Triangle.cu:128-199 and the SurfaceInteraction
 // constructor, geometry/Interaction.cuh:85-116).
-__device__ void make_si(const SceneView& sv, int prim, V3 p0, V3 p1, V3 p2, V3 d, float u, float v, float inv,
+__device__ void make_si(const SceneView& sv, int prim, V3 p0, V3 p1, V3 p2, V3 d, real u, real v, real inv,
                         SI& si) {
-    const float w = 1 - u - v;
+    const real w = 1 - u - v;
     const V3 e1 = p1 - p0, e2 = p2 - p0;
     const int4 uvi = __ldg(sv.prim_uv + prim);
-    float uv0x = 0, uv0y = 0, uv1x = 1, uv1y = 0, uv2x = 1, uv2y = 1;
+    real uv0x = 0, uv0y = 0, uv1x = 1, uv1y = 0, uv2x = 1, uv2y = 1;
     if (uvi.x >= 0) {
         uv0x = __ldg(sv.uvs + 2 * uvi.x); uv0y = __ldg(sv.uvs + 2 * uvi.x + 1);
         uv1x = __ldg(sv.uvs + 2 * uvi.y); uv1y = __ldg(sv.uvs + 2 * uvi.y + 1);
         uv2x = __ldg(sv.uvs + 2 * uvi.z); uv2y = __ldg(sv.uvs + 2 * uvi.z + 1);
     }
-    const float d02x = uv0x - uv2x, d02y = uv0y - uv2y, d12x = uv1x - uv2x, d12y = uv1y - uv2y;
+    const real d02x = uv0x - uv2x, d02y = uv0y - uv2y, d12x = uv1x - uv2x, d12y = uv1y - uv2y;
     const V3 dp02 = p0 - p2, dp12 = p1 - p2;
-    const float determinant = d02x * d12y - d02y * d12x;
+    const real determinant = d02x * d12y - d02y * d12x;
     V3 dpdu, dpdv;
     if (determinant == 0) {
         coordinate_system(normalize(cross(e2, e1)), dpdu, dpdv);
@@ -217,9 +225,9 @@ __device__ void make_si(const SceneView& sv, int prim, V3 p0, V3 p1, V3 p2, V3 d
         dpdu = (dp02 * d12y - dp12 * d02y) * inv;
         dpdv = (dp02 * -d12x + dp12 * d02x) * inv;
     }
-    const float xs = fabsf(w * p0.x) + fabsf(u * p1.x) + fabsf(v * p2.x);
-    const float ys = fabsf(w * p0.y) + fabsf(u * p1.y) + fabsf(v * p2.y);
-    const float zs = fabsf(w * p0.z) + fabsf(u * p1.z) + fabsf(v * p2.z);
+    const real xs = xabs(w * p0.x) + xabs(u * p1.x) + xabs(v * p2.x);
+    const real ys = xabs(w * p0.y) + xabs(u * p1.y) + xabs(v * p2.y);
+    const real zs = xabs(w * p0.z) + xabs(u * p1.z) + xabs(v * p2.z);
     si.perr = v3(xs, ys, zs) * gamma_n(7);
     si.p = p0 * w + p1 * u + p2 * v;
     si.wo = -d;
@@ -257,26 +265,26 @@ __device__ __forceinline__ TraceRay make_trace_ray(V3 o, V3 d) {
     TraceRay r;
     r.o = o;
     r.d = d;
-    r.inv = v3(__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z));
+    r.inv = v3(xdiv(1.0f, d.x), xdiv(1.0f, d.y), xdiv(1.0f, d.z));
     r.neg[0] = r.inv.x < 0;
     r.neg[1] = r.inv.y < 0;
     r.neg[2] = r.inv.z < 0;
     return r;
 }
 // Bounds3::simpleIntersect (geometry/Bound.cuh:199-227), returning the entry distance.
-__device__ __forceinline__ bool slab(const TraceRay& r, float tmax_ray, float mnx, float mny, float mnz, float mxx,
-                                     float mxy, float mxz, float& tentry) {
-    float tMin = ((r.neg[0] ? mxx : mnx) - r.o.x) * r.inv.x;
-    float tMax = ((r.neg[0] ? mnx : mxx) - r.o.x) * r.inv.x;
-    const float tyMin = ((r.neg[1] ? mxy : mny) - r.o.y) * r.inv.y;
-    float tyMax = ((r.neg[1] ? mny : mxy) - r.o.y) * r.inv.y;
+__device__ __forceinline__ bool slab(const TraceRay& r, real tmax_ray, real mnx, real mny, real mnz, real mxx,
+                                     real mxy, real mxz, real& tentry) {
+    real tMin = ((r.neg[0] ? mxx : mnx) - r.o.x) * r.inv.x;
+    real tMax = ((r.neg[0] ? mnx : mxx) - r.o.x) * r.inv.x;
+    const real tyMin = ((r.neg[1] ? mxy : mny) - r.o.y) * r.inv.y;
+    real tyMax = ((r.neg[1] ? mny : mxy) - r.o.y) * r.inv.y;
     tMax *= kSlabScale;
     tyMax *= kSlabScale;
     if (tMin > tyMax || tyMin > tMax) return false;
     if (tyMin > tMin) tMin = tyMin;
     if (tyMax < tMax) tMax = tyMax;
-    const float tzMin = ((r.neg[2] ? mxz : mnz) - r.o.z) * r.inv.z;
-    float tzMax = ((r.neg[2] ? mnz : mxz) - r.o.z) * r.inv.z;
+    const real tzMin = ((r.neg[2] ? mxz : mnz) - r.o.z) * r.inv.z;
+    real tzMax = ((r.neg[2] ? mnz : mxz) - r.o.z) * r.inv.z;
     tzMax *= kSlabScale;
     if (tMin > tzMax || tzMin > tMax) return false;
     if (tzMin > tMin) tMin = tzMin;
@@ -286,10 +294,10 @@ __device__ __forceinline__ bool slab(const TraceRay& r, float tmax_ray, float mn
 }
 
 __device__ __forceinline__ bool leaf_test(const bool any, const float4* __restrict__ tv, int leaf, const TraceRay& r,
-                                          float& tmax, int& best, float& bu, float& bv, float& binv) {
+                                          real& tmax, int& best, real& bu, real& bv, real& binv) {
     const float4 a = __ldg(tv + 3 * leaf), b = __ldg(tv + 3 * leaf + 1), c = __ldg(tv + 3 * leaf + 2);
     if (any) return tri_test_shadow(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax);
-    float t, u, v, inv;
+    real t, u, v, inv;
     if (tri_test(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax, t, u, v, inv)) {
         tmax = t;
         best = __float_as_int(a.w);
@@ -318,7 +326,7 @@ struct Work {
 // stack with row stride kThreads.
 struct Trav {
     TraceRay r;
-    float tmax, bu, bv, binv;
+    real tmax, bu, bv, binv;
     int best;  // closest: primitive (-1 none); any: 1 on a hit
     int node, sp;
     uint32_t gbase, gbits;
@@ -327,7 +335,7 @@ struct Trav {
 // Returns true when the ray needs traversal steps; false when it is already resolved (missed
 // the scene bounds, or a one-triangle scene).  any: any hit (shadow rays), else closest hit.
 __device__ __forceinline__ bool trav_begin(const bool any, Trav& t, const SceneView& sv, int nleaf, V3 o, V3 d,
-                                           float tmax, Work& wk) {
+                                           real tmax, Work& wk) {
     t.r = make_trace_ray(o, d);
     t.tmax = tmax;
     t.bu = t.bv = t.binv = 0.f;
@@ -336,7 +344,7 @@ __device__ __forceinline__ bool trav_begin(const bool any, Trav& t, const SceneV
     t.sp = 0;
     t.gbase = 0;
     t.gbits = 0;
-    float te;
+    real te;
     const float* rb = sv.root_bounds;
     if (!slab(t.r, t.tmax, __ldg(rb), __ldg(rb + 1), __ldg(rb + 2), __ldg(rb + 3), __ldg(rb + 4), __ldg(rb + 5), te))
         return false;
@@ -348,6 +356,7 @@ __device__ __forceinline__ bool trav_begin(const bool any, Trav& t, const SceneV
     return true;
 }
 
+#if !LTS_FP64  // the wide BVH is traversed in float only; the FP64 build uses the binary LBVH
 // Child-box test of a wide node in FMA form.  Per node and axis: A = scale * inv,
 // B = (p - o) * inv, so a plane's distance is q * A + B; both end planes are moved outwards by
 // E = 16 * 2^-24 * |inv| * (|p| + |o| + 255 scale), which bounds the rounding of this form and of
@@ -355,16 +364,16 @@ __device__ __forceinline__ bool trav_begin(const bool any, Trav& t, const SceneV
 // reference's box test computes for the decoded box; the far planes then get the reference's
 // (1 + 2 gamma(3)) factor.  Needs finite inv (see trav_step_wide).
 struct WideAxis {
-    float A, Bn, Af, Bf;
+    real A, Bn, Af, Bf;
     uint32_t near_lo, near_hi, far_lo, far_hi;  // the 8 near / far plane bytes of the axis
 };
-__device__ __forceinline__ WideAxis wide_axis(float p, float o, float inv, uint32_t ebyte, bool neg, uint32_t lo0,
+__device__ __forceinline__ WideAxis wide_axis(real p, real o, real inv, uint32_t ebyte, bool neg, uint32_t lo0,
                                               uint32_t lo1, uint32_t hi0, uint32_t hi1) {
     WideAxis a;
-    const float sc = wide_scale(ebyte);
-    const float A = sc * inv;
-    const float B = (p - o) * inv;
-    const float E = (16.0f * 5.9604645e-8f) * fabsf(inv) * (fabsf(p) + fabsf(o) + 255.0f * sc);
+    const real sc = wide_scale(ebyte);
+    const real A = sc * inv;
+    const real B = (p - o) * inv;
+    const real E = (16.0f * 5.9604645e-8f) * xabs(inv) * (xabs(p) + xabs(o) + 255.0f * sc);
     a.A = A;
     a.Bn = B - E;
     a.Af = A * kSlabScale;
@@ -375,7 +384,7 @@ __device__ __forceinline__ WideAxis wide_axis(float p, float o, float inv, uint3
     a.far_hi = neg ? lo1 : hi1;
     return a;
 }
-__device__ __forceinline__ float wide_byte(uint32_t lo, uint32_t hi, int s) {
+__device__ __forceinline__ real wide_byte(uint32_t lo, uint32_t hi, int s) {
     return __uint2float_rn(((s < 4 ? lo : hi) >> ((s & 3) * 8)) & 0xffu);
 }
 
@@ -401,20 +410,20 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
 #pragma unroll
         for (int s = 0; s < 8; ++s) {
             if (!((omask >> s) & 1u)) continue;
-            const float tnx = fmaf(wide_byte(ax.near_lo, ax.near_hi, s), ax.A, ax.Bn);
-            const float tny = fmaf(wide_byte(ay.near_lo, ay.near_hi, s), ay.A, ay.Bn);
-            const float tnz = fmaf(wide_byte(az.near_lo, az.near_hi, s), az.A, az.Bn);
-            const float tfx = fmaf(wide_byte(ax.far_lo, ax.far_hi, s), ax.Af, ax.Bf);
-            const float tfy = fmaf(wide_byte(ay.far_lo, ay.far_hi, s), ay.Af, ay.Bf);
-            const float tfz = fmaf(wide_byte(az.far_lo, az.far_hi, s), az.Af, az.Bf);
-            const float tn = fmaxf(fmaxf(tnx, tny), tnz), tf = fminf(fminf(tfx, tfy), tfz);
+            const real tnx = xfma(wide_byte(ax.near_lo, ax.near_hi, s), ax.A, ax.Bn);
+            const real tny = xfma(wide_byte(ay.near_lo, ay.near_hi, s), ay.A, ay.Bn);
+            const real tnz = xfma(wide_byte(az.near_lo, az.near_hi, s), az.A, az.Bn);
+            const real tfx = xfma(wide_byte(ax.far_lo, ax.far_hi, s), ax.Af, ax.Bf);
+            const real tfy = xfma(wide_byte(ay.far_lo, ay.far_hi, s), ay.Af, ay.Bf);
+            const real tfz = xfma(wide_byte(az.far_lo, az.far_hi, s), az.Af, az.Bf);
+            const real tn = xmax(xmax(tnx, tny), tnz), tf = xmin(xmin(tfx, tfy), tfz);
             if (tn <= tf && tn < t.tmax && tf > 0.0f) {
                 if ((imask >> s) & 1u) hits |= 1u << ((uint32_t)s ^ oct);
                 else leaves |= 1u << s;
             }
         }
     } else {  // an axis-parallel ray: the reference's slab test on the decoded planes
-        const float sx = wide_scale(hb & 0xffu), sy = wide_scale((hb >> 8) & 0xffu), sz = wide_scale((hb >> 16) & 0xffu);
+        const real sx = wide_scale(hb & 0xffu), sy = wide_scale((hb >> 8) & 0xffu), sz = wide_scale((hb >> 16) & 0xffu);
 #pragma unroll
         for (int s = 0; s < 8; ++s) {
             if (!((omask >> s) & 1u)) continue;
@@ -422,7 +431,7 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
             const uint32_t lx = ((s < 4 ? q0.x : q0.y) >> sh) & 0xffu, ly = ((s < 4 ? q0.z : q0.w) >> sh) & 0xffu;
             const uint32_t lz = ((s < 4 ? q1.x : q1.y) >> sh) & 0xffu, hx = ((s < 4 ? q1.z : q1.w) >> sh) & 0xffu;
             const uint32_t hy = ((s < 4 ? q2.x : q2.y) >> sh) & 0xffu, hz = ((s < 4 ? q2.z : q2.w) >> sh) & 0xffu;
-            float te;
+            real te;
             if (slab(t.r, t.tmax, wide_plane(h.x, lx, sx), wide_plane(h.y, ly, sy), wide_plane(h.z, lz, sz),
                      wide_plane(h.x, hx, sx), wide_plane(h.y, hy, sy), wide_plane(h.z, hz, sz), te)) {
                 if ((imask >> s) & 1u) hits |= 1u << ((uint32_t)s ^ oct);
@@ -471,13 +480,15 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
     return false;
 }
 
+#endif  // !LTS_FP64
+
 __device__ __forceinline__ bool trav_step_binary(const bool any, Trav& t, const SceneView& sv, uint32_t* stack,
                                                  uint32_t* err, Work& wk) {
     const BvhNode* nd = sv.nodes + t.node;
     const float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
     const int4 lr = __ldg(&nd->d);
     ++wk.nodes;
-    float tl, tr;
+    real tl, tr;
     bool hl = slab(t.r, t.tmax, a.x, a.y, a.z, a.w, b.x, b.y, tl);
     bool hr = slab(t.r, t.tmax, b.z, b.w, c.x, c.y, c.z, c.w, tr);
     if (hl && lr.x < 0) {
@@ -517,13 +528,17 @@ __device__ __forceinline__ bool trav_step_binary(const bool any, Trav& t, const 
 
 __device__ __forceinline__ bool trav_step(const bool any, Trav& t, const SceneView& sv, uint32_t* stack, uint32_t* err,
                                           Work& wk) {
+#if LTS_FP64
+    return trav_step_binary(any, t, sv, stack, err, wk);
+#else
     return sv.wnodes ? trav_step_wide(any, t, sv, stack, err, wk) : trav_step_binary(any, t, sv, stack, err, wk);
+#endif
 }
 
 // Whole traversal: the hit primitive (closest) or 1 / -1 (any), -1 for a miss.
 template <bool ANY>
-__device__ int traverse(const SceneView& sv, int nleaf, const TraceRay& r, float& tmax, float& bu, float& bv,
-                        float& binv, uint32_t* stack, uint32_t* err, Work& wk) {
+__device__ int traverse(const SceneView& sv, int nleaf, const TraceRay& r, real& tmax, real& bu, real& bv,
+                        real& binv, uint32_t* stack, uint32_t* err, Work& wk) {
     Trav t;
     if (trav_begin(ANY, t, sv, nleaf, r.o, r.d, tmax, wk))
         while (!trav_step(ANY, t, sv, stack, err, wk)) {
@@ -540,10 +555,10 @@ struct Hit {
     SI si;
 };
 
-__device__ __forceinline__ bool scene_intersect(const SceneView& sv, int nleaf, V3 o, V3 d, float tmax, SI& si,
+__device__ __forceinline__ bool scene_intersect(const SceneView& sv, int nleaf, V3 o, V3 d, real tmax, SI& si,
                                                 uint32_t* stack, uint32_t* err, Work& wk) {
     const TraceRay r = make_trace_ray(o, d);
-    float bu = 0, bv = 0, binv = 0;
+    real bu = 0, bv = 0, binv = 0;
     const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk);
     if (prim < 0) return false;
     V3 p0, p1, p2;
@@ -551,17 +566,17 @@ __device__ __forceinline__ bool scene_intersect(const SceneView& sv, int nleaf, 
     make_si(sv, prim, p0, p1, p2, d, bu, bv, binv, si);
     return true;
 }
-__device__ __forceinline__ bool scene_occluded(const SceneView& sv, int nleaf, V3 o, V3 d, float tmax, uint32_t* stack,
+__device__ __forceinline__ bool scene_occluded(const SceneView& sv, int nleaf, V3 o, V3 d, real tmax, uint32_t* stack,
                                                uint32_t* err, Work& wk) {
     const TraceRay r = make_trace_ray(o, d);
-    float bu, bv, binv;
+    real bu, bv, binv;
     return traverse<true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk) > 0;
 }
 
 // ------------------------------------------------------------------ rays from interactions
 // offsetRayOrigin (Geometry.cuh:782-797)
 __device__ __forceinline__ V3 offset_origin(V3 p, V3 perr, V3 n, V3 w) {
-    const float dd = dot(vabs(n), perr);
+    const real dd = dot(vabs(n), perr);
     V3 off = n * dd;
     if (dot(w, n) < 0) off = -off;
     V3 po = p + off;
@@ -575,75 +590,75 @@ __device__ __forceinline__ V3 offset_origin(V3 p, V3 perr, V3 n, V3 w) {
 __constant__ unsigned char c_perm[512];
 __constant__ float c_marble[10][3];
 
-__device__ __forceinline__ float noise_weight(float t) {
-    const float t3 = t * t * t, t4 = t3 * t;
+__device__ __forceinline__ real noise_weight(real t) {
+    const real t3 = t * t * t, t4 = t3 * t;
     return 6 * t4 * t - 15 * t4 + 10 * t3;
 }
-__device__ __forceinline__ float lerpf(float t, float a, float b) { return (1 - t) * a + t * b; }
-__device__ __forceinline__ float grad(int x, int y, int z, float dx, float dy, float dz) {
+__device__ __forceinline__ real lerpf(real t, real a, real b) { return (1 - t) * a + t * b; }
+__device__ __forceinline__ real grad(int x, int y, int z, real dx, real dy, real dz) {
     int h = c_perm[c_perm[c_perm[x] + y] + z];
     h &= 15;
-    const float u = h < 8 || h == 12 || h == 13 ? dx : dy;
-    const float v = h < 4 || h == 12 || h == 13 ? dy : dz;
+    const real u = h < 8 || h == 12 || h == 13 ? dx : dy;
+    const real v = h < 4 || h == 12 || h == 13 ? dy : dz;
     return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
 }
 // textures/Procedural.cuh:130-155 (improved Perlin noise)
-__device__ float perlin(float x, float y, float z) {
-    int ix = (int)floorf(x), iy = (int)floorf(y), iz = (int)floorf(z);
-    const float dx = x - ix, dy = y - iy, dz = z - iz;
+__device__ real perlin(real x, real y, real z) {
+    int ix = (int)xfloor(x), iy = (int)xfloor(y), iz = (int)xfloor(z);
+    const real dx = x - ix, dy = y - iy, dz = z - iz;
     ix &= 255;
     iy &= 255;
     iz &= 255;
-    const float w000 = grad(ix, iy, iz, dx, dy, dz);
-    const float w100 = grad(ix + 1, iy, iz, dx - 1, dy, dz);
-    const float w010 = grad(ix, iy + 1, iz, dx, dy - 1, dz);
-    const float w001 = grad(ix, iy, iz + 1, dx, dy, dz - 1);
-    const float w110 = grad(ix + 1, iy + 1, iz, dx - 1, dy - 1, dz);
-    const float w011 = grad(ix, iy + 1, iz + 1, dx, dy - 1, dz - 1);
-    const float w101 = grad(ix + 1, iy, iz + 1, dx - 1, dy, dz - 1);
-    const float w111 = grad(ix + 1, iy + 1, iz + 1, dx - 1, dy - 1, dz - 1);
-    const float wx = noise_weight(dx), wy = noise_weight(dy), wz = noise_weight(dz);
-    const float x00 = lerpf(wx, w000, w100), x10 = lerpf(wx, w010, w110);
-    const float x01 = lerpf(wx, w001, w101), x11 = lerpf(wx, w011, w111);
-    const float y0 = lerpf(wy, x00, x10), y1 = lerpf(wy, x01, x11);
+    const real w000 = grad(ix, iy, iz, dx, dy, dz);
+    const real w100 = grad(ix + 1, iy, iz, dx - 1, dy, dz);
+    const real w010 = grad(ix, iy + 1, iz, dx, dy - 1, dz);
+    const real w001 = grad(ix, iy, iz + 1, dx, dy, dz - 1);
+    const real w110 = grad(ix + 1, iy + 1, iz, dx - 1, dy - 1, dz);
+    const real w011 = grad(ix, iy + 1, iz + 1, dx, dy - 1, dz - 1);
+    const real w101 = grad(ix + 1, iy, iz + 1, dx - 1, dy, dz - 1);
+    const real w111 = grad(ix + 1, iy + 1, iz + 1, dx - 1, dy - 1, dz - 1);
+    const real wx = noise_weight(dx), wy = noise_weight(dy), wz = noise_weight(dz);
+    const real x00 = lerpf(wx, w000, w100), x10 = lerpf(wx, w010, w110);
+    const real x01 = lerpf(wx, w001, w101), x11 = lerpf(wx, w011, w111);
+    const real y0 = lerpf(wy, x00, x10), y1 = lerpf(wy, x01, x11);
     return lerpf(wz, y0, y1);
 }
-__device__ __forceinline__ float smooth_step(float mn, float mx, float val) {
-    const float v = clampf((val - mn) / (mx - mn), 0, 1);
+__device__ __forceinline__ real smooth_step(real mn, real mx, real val) {
+    const real v = clampf((val - mn) / (mx - mn), 0, 1);
     return v * v * (-2 * v + 3);
 }
-__device__ __forceinline__ float octaves_of(V3 dpdx, V3 dpdy, int max_oct) {
-    const float l2 = fmaxf(len2(dpdx), len2(dpdy));
-    return clampf(-1 - 0.5f * log2f(l2), 0, (float)max_oct);
+__device__ __forceinline__ real octaves_of(V3 dpdx, V3 dpdy, int max_oct) {
+    const real l2 = xmax(len2(dpdx), len2(dpdy));
+    return clampf(-1 - 0.5f * xlog2(l2), 0, (real)max_oct);
 }
 // Procedural.cuh:161-179
-__device__ float fbm(V3 p, V3 dpdx, V3 dpdy, float omega, int max_oct, EvSink* sig) {
-    const float n = octaves_of(dpdx, dpdy, max_oct);
-    const int ni = (int)floorf(n);
+__device__ real fbm(V3 p, V3 dpdx, V3 dpdy, real omega, int max_oct, EvSink* sig) {
+    const real n = octaves_of(dpdx, dpdy, max_oct);
+    const int ni = (int)xfloor(n);
     if (sig) sig->put(0x400000000ull + (unsigned)ni);
-    float sum = 0, lambda = 1, o = 1;
+    real sum = 0, lambda = 1, o = 1;
     for (int i = 0; i < ni; ++i) {
         sum += o * perlin(p.x * lambda, p.y * lambda, p.z * lambda);
         lambda *= 1.99f;
         o *= omega;
     }
-    const float np = n - ni;
+    const real np = n - ni;
     sum += o * smooth_step(0.3f, 0.7f, np) * perlin(p.x * lambda, p.y * lambda, p.z * lambda);
     return sum;
 }
 // Procedural.cuh:181-205
-__device__ float turbulence(V3 p, V3 dpdx, V3 dpdy, float omega, int max_oct, EvSink* sig) {
-    const float n = octaves_of(dpdx, dpdy, max_oct);
-    const int ni = (int)floorf(n);
+__device__ real turbulence(V3 p, V3 dpdx, V3 dpdy, real omega, int max_oct, EvSink* sig) {
+    const real n = octaves_of(dpdx, dpdy, max_oct);
+    const int ni = (int)xfloor(n);
     if (sig) sig->put(0x400000000ull + (unsigned)ni);
-    float sum = 0, lambda = 1, o = 1;
+    real sum = 0, lambda = 1, o = 1;
     for (int i = 0; i < ni; ++i) {
-        sum += o * fabsf(perlin(p.x * lambda, p.y * lambda, p.z * lambda));
+        sum += o * xabs(perlin(p.x * lambda, p.y * lambda, p.z * lambda));
         lambda *= 1.99f;
         o *= omega;
     }
-    const float np = n - ni;
-    sum += o * lerpf(smooth_step(0.3f, 0.7f, np), 0.2f, fabsf(perlin(p.x * lambda, p.y * lambda, p.z * lambda)));
+    const real np = n - ni;
+    sum += o * lerpf(smooth_step(0.3f, 0.7f, np), 0.2f, xabs(perlin(p.x * lambda, p.y * lambda, p.z * lambda)));
     for (int i = ni; i < max_oct; ++i) {
         sum += o * 0.2f;
         o *= omega;
@@ -658,11 +673,11 @@ __device__ Spec eval_texture(const DevTex& t, const SI& si, EvSink* sig) {
         case 2:  // WrinkledTexture (Procedural.cuh:227-245)
             return spec(turbulence(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0], sig));
         case 3: {  // MarbleTexture (Procedural.cuh:267-311)
-            const float scale = t.v[2], var = t.v[3];
+            const real scale = t.v[2], var = t.v[3];
             const V3 p = si.p * scale;
-            const float marble = p.y + var * fbm(p, si.dpdx * scale, si.dpdy * scale, t.v[1], (int)t.v[0], sig);
-            float tt = 0.5f + 0.5f * sinf(marble);
-            const int first = (int)floorf(tt * 6.0f);
+            const real marble = p.y + var * fbm(p, si.dpdx * scale, si.dpdy * scale, t.v[1], (int)t.v[0], sig);
+            real tt = 0.5f + 0.5f * xsin(marble);
+            const int first = (int)xfloor(tt * 6.0f);
             if (sig) sig->put(0x500000000ull + (unsigned)first);
             tt = (tt * 6.0f - first);
             Spec c[4];
@@ -676,9 +691,9 @@ __device__ Spec eval_texture(const DevTex& t, const SI& si, EvSink* sig) {
             return (s0 * (1.0f - tt) + s1 * tt) * 1.5f;
         }
         case 4: {  // WindyTexture (Procedural.cuh:247-265)
-            const float wind = fbm(si.p * 0.1f, si.dpdx * 0.1f, si.dpdy * 0.1f, 0.5f, 3, sig);
-            const float wave = fbm(si.p, si.dpdx, si.dpdy, 0.5f, 6, sig);
-            return spec(fabsf(wind) * wave);
+            const real wind = fbm(si.p * 0.1f, si.dpdx * 0.1f, si.dpdy * 0.1f, 0.5f, 3, sig);
+            const real wave = fbm(si.p, si.dpdx, si.dpdy, 0.5f, 6, sig);
+            return spec(xabs(wind) * wave);
         }
         default:
             return Spec{t.v[0], t.v[1], t.v[2]};
@@ -686,15 +701,15 @@ __device__ Spec eval_texture(const DevTex& t, const SI& si, EvSink* sig) {
 }
 
 // ------------------------------------------------------------------ BxDFs
-__device__ __forceinline__ float cos2t(V3 w) { return w.z * w.z; }
-__device__ __forceinline__ float sin2t(V3 w) { return fmaxf(1 - cos2t(w), 0.0f); }
-__device__ __forceinline__ float sint(V3 w) { return sqrtf(sin2t(w)); }
-__device__ __forceinline__ float tant(V3 w) { return sint(w) / w.z; }
-__device__ __forceinline__ float tan2t(V3 w) { return sin2t(w) / cos2t(w); }
+__device__ __forceinline__ real cos2t(V3 w) { return w.z * w.z; }
+__device__ __forceinline__ real sin2t(V3 w) { return xmax(1 - cos2t(w), 0.0f); }
+__device__ __forceinline__ real sint(V3 w) { return xsqrt(sin2t(w)); }
+__device__ __forceinline__ real tant(V3 w) { return sint(w) / w.z; }
+__device__ __forceinline__ real tan2t(V3 w) { return sin2t(w) / cos2t(w); }
 // cosPhi/sinPhi compare the function sinTheta (not its value) with 0, so they never take the
 // sin == 0 branch (models/BxDF.cuh:144-153).
-__device__ __forceinline__ float cosphi(V3 w) { return clampf(w.x / sint(w), -1, 1); }
-__device__ __forceinline__ float sinphi(V3 w) { return clampf(w.y / sint(w), -1, 1); }
+__device__ __forceinline__ real cosphi(V3 w) { return clampf(w.x / sint(w), -1, 1); }
+__device__ __forceinline__ real sinphi(V3 w) { return clampf(w.y / sint(w), -1, 1); }
 __device__ __forceinline__ bool same_hemi(V3 a, V3 b, EvSink* sig) {  // sameHemisphere, recorded
     const bool v = a.z * b.z > 0;
     if (sig) sig->put(0x700000000ull + (v ? 1u : 0u));
@@ -702,28 +717,28 @@ __device__ __forceinline__ bool same_hemi(V3 a, V3 b, EvSink* sig) {  // sameHem
 }
 
 // models/BxDF.cuh:16-37 with the swapped clamp bounds of line 17.
-__device__ float fresnel_dielectric(float cos_i, float eta_i, float eta_t) {
+__device__ real fresnel_dielectric(real cos_i, real eta_i, real eta_t) {
     cos_i = clampf(cos_i, 1, -1);
     const bool entering = cos_i > 0.0f;
     if (!entering) {
-        const float tmp = eta_i;
+        const real tmp = eta_i;
         eta_i = eta_t;
         eta_t = tmp;
-        cos_i = fabsf(cos_i);
+        cos_i = xabs(cos_i);
     }
-    const float sin_i = sqrtf(fmaxf(0.0f, 1 - cos_i * cos_i));
-    const float sin_t = eta_i / eta_t * sin_i;
+    const real sin_i = xsqrt(xmax(0.0f, 1 - cos_i * cos_i));
+    const real sin_t = eta_i / eta_t * sin_i;
     if (sin_t >= 1) return 1;
-    const float cos_t = sqrtf(fmaxf(0.0f, 1 - sin_t * sin_t));
-    const float rpar = ((eta_t * cos_i) - (eta_i * cos_t)) / ((eta_t * cos_i) + (eta_i * cos_t));
-    const float rperp = ((eta_i * cos_i) - (eta_t * cos_t)) / ((eta_i * cos_i) + (eta_t * cos_t));
+    const real cos_t = xsqrt(xmax(0.0f, 1 - sin_t * sin_t));
+    const real rpar = ((eta_t * cos_i) - (eta_i * cos_t)) / ((eta_t * cos_i) + (eta_i * cos_t));
+    const real rperp = ((eta_i * cos_i) - (eta_t * cos_t)) / ((eta_i * cos_i) + (eta_t * cos_t));
     return (rpar * rpar + rperp * rperp) / 2;
 }
 // models/BxDF.cuh:44-67 (etaI = 1)
-__device__ Spec fresnel_conductor(float cos_i, Spec eta_t, Spec k) {
+__device__ Spec fresnel_conductor(real cos_i, Spec eta_t, Spec k) {
     cos_i = clampf(cos_i, -1, 1);
     const Spec eta = eta_t / 1.0f, etak = k / 1.0f;
-    const float c2 = cos_i * cos_i, s2 = 1.0f - c2;
+    const real c2 = cos_i * cos_i, s2 = 1.0f - c2;
     const Spec eta2 = eta * eta, etak2 = etak * etak;
     const Spec t0 = eta2 - etak2 - spec(s2);
     const Spec a2b2 = ssqrt(t0 * t0 + eta2 * 4.0f * etak2);
@@ -737,57 +752,57 @@ __device__ Spec fresnel_conductor(float cos_i, Spec eta_t, Spec k) {
     return (rp + rs) * 0.5f;
 }
 // models/BxDF.cuh:156-166
-__device__ __forceinline__ bool refract(V3 wi, V3 n, float eta, V3& wt) {
-    const float ci = dot(n, wi);
-    const float s2i = fmaxf(0.0f, 1.0f - ci * ci);
-    const float s2t = eta * eta * s2i;
+__device__ __forceinline__ bool refract(V3 wi, V3 n, real eta, V3& wt) {
+    const real ci = dot(n, wi);
+    const real s2i = xmax(0.0f, 1.0f - ci * ci);
+    const real s2t = eta * eta * s2i;
     if (s2t >= 1) return false;
-    const float ct = sqrtf(1 - s2t);
+    const real ct = xsqrt(1 - s2t);
     wt = -wi * eta + n * (eta * ci - ct);
     return true;
 }
 
 // Trowbridge-Reitz (models/Microfacet.cuh:53-181)
-__device__ float tr_lambda(V3 w, float ax, float ay) {
-    const float at = fabsf(tant(w));
+__device__ real tr_lambda(V3 w, real ax, real ay) {
+    const real at = xabs(tant(w));
     if (isinf(at)) return 0.0f;
-    const float cp = cosphi(w), sp = sinphi(w);
-    const float alpha = sqrtf(cp * cp * ax * ax + sp * sp * ay * ay);
-    const float a2t2 = (alpha * at) * (alpha * at);
-    return (-1 + sqrtf(1.0f + a2t2)) / 2;
+    const real cp = cosphi(w), sp = sinphi(w);
+    const real alpha = xsqrt(cp * cp * ax * ax + sp * sp * ay * ay);
+    const real a2t2 = (alpha * at) * (alpha * at);
+    return (-1 + xsqrt(1.0f + a2t2)) / 2;
 }
-__device__ float tr_d(V3 wh, float ax, float ay) {
-    const float t2 = tan2t(wh);
+__device__ real tr_d(V3 wh, real ax, real ay) {
+    const real t2 = tan2t(wh);
     if (isinf(t2)) return 0;
-    const float c4 = cos2t(wh) * cos2t(wh);
-    const float cp = cosphi(wh), sp = sinphi(wh);
-    const float e = (cp * cp / (ax * ax) + sp * sp / (ay * ay)) * t2;
+    const real c4 = cos2t(wh) * cos2t(wh);
+    const real cp = cosphi(wh), sp = sinphi(wh);
+    const real e = (cp * cp / (ax * ax) + sp * sp / (ay * ay)) * t2;
     return 1 / (3.14159265358979f * ax * ay * c4 * (1 + e) * (1 + e));
 }
-__device__ __forceinline__ float tr_g1(V3 w, float ax, float ay) { return 1 / (1 + tr_lambda(w, ax, ay)); }
-__device__ __forceinline__ float tr_g(V3 wo, V3 wi, float ax, float ay) {
+__device__ __forceinline__ real tr_g1(V3 w, real ax, real ay) { return 1 / (1 + tr_lambda(w, ax, ay)); }
+__device__ __forceinline__ real tr_g(V3 wo, V3 wi, real ax, real ay) {
     return 1 / (1 + tr_lambda(wo, ax, ay) + tr_lambda(wi, ax, ay));
 }
-__device__ void tr_sample11(float cosT, float U1, float U2, float& sx, float& sy) {
+__device__ void tr_sample11(real cosT, real U1, real U2, real& sx, real& sy) {
     if (cosT >= kOneMinusEpsUp) {
-        const float r = sqrtf(U1 / (1 - U1));
-        const float phi = mul_dc(U2, LTS_2PI_HI, LTS_2PI_LO);
-        sx = r * cosf(phi);
-        sy = r * sinf(phi);
+        const real r = xsqrt(U1 / (1 - U1));
+        const real phi = mul_dc(U2, LTS_2PI);
+        sx = r * xcos(phi);
+        sy = r * xsin(phi);
         return;
     }
-    const float sinT = sqrtf(fmaxf(0.0f, 1.0f - cosT * cosT));
-    const float tanT = sinT / cosT;
-    const float a = 1 / tanT;
-    const float G1 = 2 / (1 + sqrtf(1.f + 1.f / (a * a)));
-    const float A = 2 * U1 / G1 - 1;
-    float tmp = 1.f / (A * A - 1.f);
+    const real sinT = xsqrt(xmax(0.0f, 1.0f - cosT * cosT));
+    const real tanT = sinT / cosT;
+    const real a = 1 / tanT;
+    const real G1 = 2 / (1 + xsqrt(1.f + 1.f / (a * a)));
+    const real A = 2 * U1 / G1 - 1;
+    real tmp = 1.f / (A * A - 1.f);
     if (tmp > 1e10f) tmp = 1e10f;
-    const float B = tanT;
-    const float D = sqrtf(fmaxf(float(B * B * tmp * tmp - (A * A - B * B) * tmp), 0.0f));
-    const float s1 = B * tmp - D, s2 = B * tmp + D;
+    const real B = tanT;
+    const real D = xsqrt(xmax(real(B * B * tmp * tmp - (A * A - B * B) * tmp), 0.0f));
+    const real s1 = B * tmp - D, s2 = B * tmp + D;
     sx = (A < 0 || s2 > 1.f / tanT) ? s1 : s2;
-    float S;
+    real S;
     if (U2 > 0.5f) {
         S = 1.f;
         U2 = 2.f * (U2 - .5f);
@@ -795,15 +810,15 @@ __device__ void tr_sample11(float cosT, float U1, float U2, float& sx, float& sy
         S = -1.f;
         U2 = 2.f * (.5f - U2);
     }
-    const float z = (U2 * (U2 * (U2 * 0.27385f - 0.73369f) + 0.46341f)) /
+    const real z = (U2 * (U2 * (U2 * 0.27385f - 0.73369f) + 0.46341f)) /
                     (U2 * (U2 * (U2 * 0.093073f + 0.309420f) - 1.000000f) + 0.597999f);
-    sy = S * z * sqrtf(1.f + sx * sx);
+    sy = S * z * xsqrt(1.f + sx * sx);
 }
-__device__ V3 tr_sample(V3 wi, float ax, float ay, float U1, float U2) {
+__device__ V3 tr_sample(V3 wi, real ax, real ay, real U1, real U2) {
     const V3 ws = normalize(v3(ax * wi.x, ay * wi.y, wi.z));
-    float sx, sy;
+    real sx, sy;
     tr_sample11(ws.z, U1, U2, sx, sy);
-    const float tmp = cosphi(ws) * sx - sinphi(ws) * sy;
+    const real tmp = cosphi(ws) * sx - sinphi(ws) * sy;
     sy = sinphi(ws) * sx + cosphi(ws) * sy;
     sx = tmp;
     sx = ax * sx;
@@ -816,7 +831,7 @@ struct Bsdf {
     uint32_t type;      // BxDF type bits of the lobe
     V3 ns, ng, ss, ts;
     Spec R, T, k, eta3;
-    float eta, a, b, alpha;
+    real eta, a, b, alpha;
 };
 
 __device__ __forceinline__ V3 to_local(const Bsdf& f, V3 v) { return v3(dot(v, f.ss), dot(v, f.ts), dot(v, f.ns)); }
@@ -829,47 +844,47 @@ __device__ __forceinline__ bool matches(uint32_t type, uint32_t flags) { return 
 // BxDF::f
 __device__ Spec lobe_f(const Bsdf& f, V3 wo, V3 wi) {
     switch (f.lobe) {
-        case LOBE_LAMBERT: return f.R * LTS_1_PI_HI;
+        case LOBE_LAMBERT: return f.R * LTS_INV_PI_F;
         case LOBE_OREN_NAYAR: {  // Microfacet.cuh:27-50
-            const float so = sint(wo), si_ = sint(wi);
-            float maxcos = 0.0f;
+            const real so = sint(wo), si_ = sint(wi);
+            real maxcos = 0.0f;
             if (si_ >= 0.0001f && so >= 0.0001f) {
-                const float spo = sinphi(wo), cpo = cosphi(wo), spi = sinphi(wi), cpi = cosphi(wi);
-                const float dcos = cpi * cpo + spi * spo;
-                maxcos = fmaxf(0.0f, dcos);
+                const real spo = sinphi(wo), cpo = cosphi(wo), spi = sinphi(wi), cpi = cosphi(wi);
+                const real dcos = cpi * cpo + spi * spo;
+                maxcos = xmax(0.0f, dcos);
             }
-            float sin_a, tan_b;
-            if (fabsf(wi.z) > fabsf(wo.z)) {
+            real sin_a, tan_b;
+            if (xabs(wi.z) > xabs(wo.z)) {
                 sin_a = so;
-                tan_b = si_ / fabsf(wi.z);
+                tan_b = si_ / xabs(wi.z);
             } else {
                 sin_a = si_;
-                tan_b = so / fabsf(wo.z);
+                tan_b = so / xabs(wo.z);
             }
-            return f.R * LTS_1_PI_HI * (f.a + f.b * maxcos * sin_a * tan_b);
+            return f.R * LTS_INV_PI_F * (f.a + f.b * maxcos * sin_a * tan_b);
         }
         case LOBE_MICROFACET: {  // Microfacet.cuh:200-209
-            const float co = fabsf(wo.z), ci = fabsf(wi.z);
+            const real co = xabs(wo.z), ci = xabs(wi.z);
             V3 wh = wi + wo;
             if (ci == 0 || co == 0) return spec(0.0f);
             if (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) return spec(0.0f);
             wh = normalize(wh);
-            const Spec F = fresnel_conductor(fabsf(dot(wi, wh)), f.eta3, f.k);
+            const Spec F = fresnel_conductor(xabs(dot(wi, wh)), f.eta3, f.k);
             return f.R * tr_d(wh, f.alpha, f.alpha) * tr_g(wo, wi, f.alpha, f.alpha) * F / (4 * ci * co);
         }
         default: return spec(0.0f);  // specular lobes
     }
 }
 // BxDF::Pdf
-__device__ float lobe_pdf(const Bsdf& f, V3 wo, V3 wi, EvSink* sig) {
+__device__ real lobe_pdf(const Bsdf& f, V3 wo, V3 wi, EvSink* sig) {
     switch (f.lobe) {
         case LOBE_LAMBERT:
         case LOBE_OREN_NAYAR:
-            return same_hemi(wo, wi, sig) ? mul_dc(fabsf(wi.z), LTS_1_PI_HI, LTS_1_PI_LO) : 0.0f;
+            return same_hemi(wo, wi, sig) ? mul_dc(xabs(wi.z), LTS_1_PI) : 0.0f;
         case LOBE_MICROFACET: {
             if (!same_hemi(wo, wi, sig)) return 0;
             const V3 wh = normalize(wo + wi);
-            const float pd = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha, f.alpha) * absdot(wo, wh) / fabsf(wo.z);
+            const real pd = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha, f.alpha) * absdot(wo, wh) / xabs(wo.z);
             return pd / (4 * dot(wo, wh));
         }
         default: return 0.0f;
@@ -886,22 +901,22 @@ __device__ Spec bsdf_f(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags, EvSink* si
     return spec(0.0f);
 }
 // BSDF::Pdf (BSDF.cuh:261-276)
-__device__ float bsdf_pdf(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags, EvSink* sig) {
+__device__ real bsdf_pdf(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags, EvSink* sig) {
     if (f.lobe == LOBE_NONE) return 0.0f;
     const V3 wo = to_local(f, woW), wi = to_local(f, wiW);
     if (wo.z == 0) return 0.0f;
     if (!matches(f.type, flags)) return 0.0f;
-    const float pdf = 0.0f + lobe_pdf(f, wo, wi, sig);
+    const real pdf = 0.0f + lobe_pdf(f, wo, wi, sig);
     return pdf / 1;
 }
 // BSDF::sampleF with a single matching lobe (BSDF.cuh:206-259) and the lobes' sampleF.
-__device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, uint32_t flags, uint32_t& sampled,
+__device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, real& pdf, uint32_t flags, uint32_t& sampled,
                             EvSink* sig) {
     if (f.lobe == LOBE_NONE || !matches(f.type, flags)) {
         pdf = 0;
         return spec(0.0f);
     }
-    // comp = min((int)floorf(u.x * 1), 0) = 0; the remapped sample is u itself
+    // comp = min((int)xfloor(u.x * 1), 0) = 0; the remapped sample is u itself
     const V3 wo = to_local(f, woW);
     V3 wi = v3(0, 0, 0);
     pdf = 0;
@@ -910,10 +925,10 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, ui
     switch (f.lobe) {
         case LOBE_LAMBERT:
         case LOBE_OREN_NAYAR: {  // BxDF::sampleF (BxDF.cuh:196-204)
-            const float r = sqrtf(u.x);
-            const float th = mul_dc(u.y, LTS_2PI_HI, LTS_2PI_LO);
-            const float dx = r * cosf(th), dy = r * sinf(th);
-            wi = v3(dx, dy, sqrtf(fmaxf(0.0f, 1 - dx * dx - dy * dy)));
+            const real r = xsqrt(u.x);
+            const real th = mul_dc(u.y, LTS_2PI);
+            const real dx = r * xcos(th), dy = r * xsin(th);
+            wi = v3(dx, dy, xsqrt(xmax(0.0f, 1 - dx * dx - dy * dy)));
             if (wo.z < 0) wi.z *= -1;
             pdf = lobe_pdf(f, wo, wi, sig);
             val = lobe_f(f, wo, wi);
@@ -922,19 +937,19 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, ui
         case LOBE_SPECULAR_REFL: {  // Specular.cuh:30-39, FresnelNoOp
             wi = v3(-wo.x, -wo.y, wo.z);
             pdf = 1.0f;
-            val = (spec(1.0f) * f.R) / fabsf(wi.z);
+            val = (spec(1.0f) * f.R) / xabs(wi.z);
             break;
         }
         case LOBE_FRESNEL_SPECULAR: {  // Specular.cuh:107-135
-            const float F = fresnel_dielectric(wo.z, 1.0f, f.eta);
+            const real F = fresnel_dielectric(wo.z, 1.0f, f.eta);
             if (u.x < F) {
                 wi = v3(-wo.x, -wo.y, -wo.z);  // the reference's "reflection" keeps going straight
                 sampled = BSDF_SPECULAR | BSDF_REFLECTION;
                 pdf = F;
-                val = (f.R * F) / fabsf(wi.z);
+                val = (f.R * F) / xabs(wi.z);
             } else {
                 const bool entering = wo.z > 0;
-                const float ei = entering ? 1.0f : f.eta, et = entering ? f.eta : 1.0f;
+                const real ei = entering ? 1.0f : f.eta, et = entering ? f.eta : 1.0f;
                 const V3 n = face_towards(v3(0, 0, 1), wo);
                 if (!refract(wo, n, ei / et, wi)) {
                     pdf = 0;
@@ -944,7 +959,7 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, ui
                 ft = ft * ((ei * ei) / (et * et));
                 sampled = BSDF_SPECULAR | BSDF_TRANSMISSION;
                 pdf = 1.0f - F;
-                val = ft / fabsf(wi.z);
+                val = ft / xabs(wi.z);
             }
             break;
         }
@@ -956,7 +971,7 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, float& pdf, ui
             if (dot(wo, wh) < 0) return spec(0.0f);
             wi = -wo + wh * (2 * dot(wo, wh));
             if (!same_hemi(wo, wi, sig)) return spec(0.0f);
-            const float pd = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha, f.alpha) * absdot(wo, wh) / fabsf(wo.z);
+            const real pd = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha, f.alpha) * absdot(wo, wh) / xabs(wo.z);
             pdf = pd / (4 * dot(wo, wh));
             val = lobe_f(f, wo, wi);
             break;
@@ -1031,21 +1046,21 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* si
 struct LightSample {
     Spec Li;
     V3 wi;
-    float pdf;
+    real pdf;
     V3 p1, perr1, n1;  // visibility target interaction
 };
-__device__ __forceinline__ float sph_pdf_infinite(V3 w) {
-    // uniformSampleHemispherePDF() / (2 * M_PI * M_PI * sinf(sphericalTheta(w)))
-    const float s = sinf(acosf(clampf(w.z, -1.0f, 1.0f)));
+__device__ __forceinline__ real sph_pdf_infinite(V3 w) {
+    // uniformSampleHemispherePDF() / (2 * M_PI * M_PI * xsin(sphericalTheta(w)))
+    const real s = xsin(xacos(clampf(w.z, -1.0f, 1.0f)));
     return 0.159154937f / (19.7392088f * s);
 }
 
 // Triangle::Pdf(it, wi) (shapes/Triangle.cu:211-225): re-intersects the light triangle.
-__device__ float area_pdf(const SceneView& sv, const DevLight& L, V3 p, V3 perr, V3 n, V3 wi) {
+__device__ real area_pdf(const SceneView& sv, const DevLight& L, V3 p, V3 perr, V3 n, V3 wi) {
     const V3 o = offset_origin(p, perr, n, wi);
     V3 p0, p1, p2;
     prim_tri(sv, L.prim, p0, p1, p2);
-    float t, u, v, inv;
+    real t, u, v, inv;
     if (!tri_test(p0, p1, p2, o, wi, INFINITY, t, u, v, inv)) return 0;
     SI is;
     make_si(sv, L.prim, p0, p1, p2, wi, u, v, inv, is);
@@ -1059,11 +1074,11 @@ __device__ bool sample_li(const SceneView& sv, const DevLight& L, const SI& si, 
     ls.perr1 = v3(0, 0, 0);
     ls.n1 = v3(0, 0, 0);
     if (L.kind == 0) {  // AreaLight::sampleLi (Light.cu:28-37) + Triangle::sample (Triangle.cu:232-259)
-        const float su = sqrtf(u.x);
-        const float b0 = 1 - su, b1 = u.y * su;
+        const real su = xsqrt(u.x);
+        const real b0 = 1 - su, b1 = u.y * su;
         V3 p0, p1, p2;
         prim_tri(sv, L.prim, p0, p1, p2);
-        const float b2 = 1 - b0 - b1;
+        const real b2 = 1 - b0 - b1;
         const V3 ps = p0 * b0 + p1 * b1 + p2 * b2;
         V3 ns;
         const int4 ni = __ldg(sv.prim_n + L.prim);
@@ -1081,10 +1096,10 @@ __device__ bool sample_li(const SceneView& sv, const DevLight& L, const SI& si, 
         return false;
     }
     if (L.kind == 1) {  // InfiniteLight::sampleLi (Light.cu:68-90)
-        const float z = u.x;
-        const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
-        const float phi = mul_dc(u.y, LTS_2PI_HI, LTS_2PI_LO);
-        const V3 w0 = v3(r * cosf(phi), r * sinf(phi), z);
+        const real z = u.x;
+        const real r = xsqrt(xmax(0.0f, 1.0f - z * z));
+        const real phi = mul_dc(u.y, LTS_2PI);
+        const V3 w0 = v3(r * xcos(phi), r * xsin(phi), z);
         const V3 ref = v3(0, 1, 0);
         V3 a, b;
         coordinate_system(ref, a, b);

@@ -37,7 +37,7 @@ def ctx(built_lib):
 
 
 @pytest.mark.parametrize("kind", ["box_sphere", "materials"])
-@pytest.mark.parametrize("bvh_mode,integrator,width", [(0, 0, 2), (0, 1, 8), (1, 0, 8), (1, 1, 8), (1, 1, 2)])
+@pytest.mark.parametrize("bvh_mode,integrator,width", [(0, 0, 2), (0, 1, 8), (1, 0, 8), (1, 1, 8), (1, 1, 2), (1, 2, 2)])
 def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator, width):
     import lighttransportsimulation_gb300 as lts
     d, sc, sub = scene_dirs[kind]
@@ -56,8 +56,13 @@ def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator, width)
     sr = fx["sig"].reshape(-1)
     same = sig == sr
     div = 1.0 - same.mean()
-    ok = np.all(np.abs(L - Lr) <= RTOL * np.abs(Lr) + ATOL, axis=1)
+    # the FP64 oracle renderer evaluates the same samples without the reference's float rounding:
+    # its per-sample values are checked at 1e-2, the float renderers' at 1e-4
+    rtol = RTOL if integrator != 2 else 1e-2
+    ok = np.all(np.abs(L - Lr) <= rtol * np.abs(Lr) + ATOL, axis=1)
     mism = 1.0 - ok[same].mean()
+    ok4 = np.all(np.abs(L - Lr) <= RTOL * np.abs(Lr) + ATOL, axis=1)
+    print(f"  within 1e-4: {ok4[same].mean():.6f}")
     print(f"{kind} bvh={bvh_mode} integrator={integrator} width={width}: samples={len(sig)} divergent={div:.5f} mismatched={mism:.6f} "
           f"maxrel={np.max(np.abs(L - Lr)[same] / (np.abs(Lr[same]) + 1e-6)):.3g}")
     assert np.isfinite(L).all()
@@ -68,7 +73,7 @@ def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator, width)
 
 
 @pytest.mark.parametrize("kind", ["box_sphere", "materials"])
-@pytest.mark.parametrize("integrator", [0, 1])
+@pytest.mark.parametrize("integrator", [0, 1, 2])
 def test_film_matches_reference(ctx, scene_dirs, kind, integrator):
     """Full-frame film (Kahan FP32 + FP64 resolve) against the reference's single-thread film."""
     import lighttransportsimulation_gb300 as lts
@@ -160,3 +165,23 @@ def test_wide_bvh_same_hits_as_binary(ctx, scene_dirs, tmp_path, kind):
     assert same.mean() >= 0.999
     La, Lb = a["L"].reshape(-1, 3)[same], b["L"].reshape(-1, 3)[same]
     assert np.array_equal(La.view(np.uint32), Lb.view(np.uint32))
+
+
+def test_fp64_oracle_converges_to_fp32_estimator(ctx, scene_dirs):
+    """The FP64 renderer computes the same estimator: a 256-spp FP64 film and a 256-spp FP32
+    wavefront film of the same seed agree far below their Monte Carlo noise, and the RMSE of 16-spp
+    FP32 films against the FP64 film falls as more samples are taken."""
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs["box_sphere"]
+    s = lts.Scene.parse(ctx, d, sc, sub, 64, 64)
+    ref = lts.PathTracingIntegrator(5, 3, s, integrator=lts.INTEGRATOR_FP64).render(256, 1)["film"]
+    same = lts.PathTracingIntegrator(5, 3, s, integrator=1).render(256, 1)["film"]
+    rel = np.sqrt(np.mean((same - ref) ** 2)) / np.sqrt(np.mean(ref ** 2))
+    print(f"fp32 vs fp64, same samples: rel-RMSE {rel:.2e}")
+    assert rel < 1e-3
+    errs = []
+    for spp in (4, 16, 64):
+        f = lts.PathTracingIntegrator(5, 3, s, integrator=1).render(spp, 7)["film"]
+        errs.append(np.sqrt(np.mean((f - ref) ** 2)))
+    print("RMSE vs FP64 at 4/16/64 spp:", errs)
+    assert errs[0] > errs[1] > errs[2]
