@@ -40,6 +40,10 @@ WORKLOAD = dict(name="displaced_icosphere_box", width=1024, height=1024, spp=64,
                 seed=0, level=8)
 SMALL = dict(name="displaced_icosphere_box_small", width=256, height=256, spp=16, max_bounce=8, rr_start=3,
              seed=0, level=6)
+# material and divergence stress: glass + 8 rough conductor spheres of 261,120 tris each, marble floor,
+# area + infinite light
+STRESS = dict(name="stress_glass_conductors", width=1920, height=1080, spp=256, max_bounce=16, rr_start=4,
+              seed=0, level=0)
 
 
 def scene_dir(wl):
@@ -48,8 +52,13 @@ def scene_dir(wl):
     marker = os.path.join(d, "done")
     if not os.path.exists(marker):
         os.makedirs(d, exist_ok=True)
-        scenes.write_displaced(d, level=wl["level"])
+        if wl is STRESS:
+            scenes.write_stress_scene(d)
+        else:
+            scenes.write_displaced(d, level=wl["level"])
         open(marker, "w").write("ok")
+    if wl is STRESS:
+        return d, "stress", "stress"
     return d, "box", "displaced"
 
 
@@ -175,7 +184,7 @@ def run_reference(args, wl):
             "impl": "reference",
             "config": {"workload": wl["name"], "width": wl["width"], "height": wl["height"], "spp": wl["spp"],
                        "max_bounce": wl["max_bounce"], "rr_start": wl["rr_start"], "seed": wl["seed"],
-                       "triangles": 20 * 4 ** wl["level"] + 12},
+                       "triangles": (20 * 4 ** wl["level"] + 12) if wl is not STRESS else 9 * 261120 + 12},
             "cpu_baseline": {**res, "value": v},
             "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -358,6 +367,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--small", action="store_true", help="256x256x16 spp level-6 sphere (quick check)")
+    ap.add_argument("--stress", action="store_true",
+                    help="the glass + rough-conductor stress scene (1920x1080, 256 spp, 16 bounces)")
     ap.add_argument("--skip-lbvh", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--integrator", type=int, default=1, choices=[0, 1], help="0 megakernel, 1 wavefront")
@@ -366,7 +377,7 @@ def main():
     ap.add_argument("--lbvh-only", type=int, default=0, metavar="N",
                     help="only time the LBVH build over N random triangles (seed 1)")
     args = ap.parse_args()
-    wl = SMALL if args.small else WORKLOAD
+    wl = SMALL if args.small else (STRESS if args.stress else WORKLOAD)
     if args.lbvh_only:
         import lighttransportsimulation_gb300 as lts
         ctx = lts.Context(0)

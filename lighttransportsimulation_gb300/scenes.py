@@ -15,6 +15,12 @@ Workloads (sizes are the ones the benchmarks are quoted on):
                (8 octaves, omega 0.5); 1024x1024, 64 spp, 8 bounces.
   random_tris  N triangles with centroids U[0,1)^3 and vertices centroid + N(0, 1e-3)^3, FP32,
                seed 1 (the LBVH build benchmark, 1M and 16M).
+  stress       material and divergence stress: in the same box, a glass (IOR 1.5) lat-long sphere
+               of 512 x 256 segments (261,120 tris) displaced by 0.1 * fbm(8, 0.5); eight rough
+               conductor spheres of the same tessellation (Trowbridge-Reitz, alpha U[0.05, 0.5]
+               per copy, positions seeded with 2) written as eight pre-transformed meshes; a
+               marble Lambertian floor (8 octaves, omega 0.5, scale 4); the ceiling area light and
+               a constant infinite light of 0.5.  1920x1080, 256 spp, 16 bounces, roulette from 4.
 """
 import os
 
@@ -244,6 +250,77 @@ def write_displaced(d, level=8, amplitude=0.1, radius=0.5):
     with open(os.path.join(d, "displaced.subject"), "w") as fh:
         fh.write("0\n1\tdisplaced\n1\nL\tw\t8 0.5\t0\n")
     return "box", "displaced"
+
+
+def uv_sphere(rings, segs):
+    """Unit lat-long sphere: vertices (float64) and triangles; fans at the poles, two triangles
+    per quad elsewhere: 2 * segs * (rings - 1) triangles, counter-clockwise seen from outside."""
+    th = np.pi * np.arange(1, rings) / rings                      # interior rings
+    ph = 2 * np.pi * np.arange(segs) / segs
+    st, ct = np.sin(th)[:, None], np.cos(th)[:, None]
+    ring = np.stack([st * np.cos(ph)[None, :], np.broadcast_to(ct, (rings - 1, segs)),
+                     st * np.sin(ph)[None, :]], axis=-1).reshape(-1, 3)
+    v = np.concatenate([[[0.0, 1.0, 0.0]], ring, [[0.0, -1.0, 0.0]]])
+    top, bot = 0, v.shape[0] - 1
+    idx = 1 + np.arange((rings - 1) * segs).reshape(rings - 1, segs)
+    nxt = np.roll(idx, -1, axis=1)
+    f = [np.stack([np.full(segs, top), nxt[0], idx[0]], axis=1)]
+    a, b, c, d = idx[:-1], nxt[:-1], nxt[1:], idx[1:]
+    f.append(np.stack([a, b, c], axis=-1).reshape(-1, 3))
+    f.append(np.stack([a, c, d], axis=-1).reshape(-1, 3))
+    f.append(np.stack([np.full(segs, bot), idx[-1], nxt[-1]], axis=1))
+    return v, np.concatenate(f).astype(np.int64)
+
+
+STRESS_SPHERE = (256, 512)   # rings, segments: 261,120 triangles per sphere
+
+
+def write_stress_scene(d, rings=STRESS_SPHERE[0], segs=STRESS_SPHERE[1], copies=8, seed=2, amplitude=0.1):
+    """The material and divergence stress scene (see the module docstring); smaller `rings` and
+    `segs` give the same layout with coarser spheres (parity cases)."""
+    os.makedirs(d, exist_ok=True)
+    write_quads(os.path.join(d, "s_back.bin"), [((-1, -1, -1), (2, 0, 0), (0, 2, 0)),
+                                                  ((-1, 1, -1), (2, 0, 0), (0, 0, 2))])
+    write_quads(os.path.join(d, "s_floor.bin"), [((-1, -1, -1), (0, 0, 2), (2, 0, 0))])
+    write_quads(os.path.join(d, "box_red.bin"), [((-1, -1, -1), (0, 2, 0), (0, 0, 2))])
+    write_quads(os.path.join(d, "box_green.bin"), [((1, -1, -1), (0, 0, 2), (0, 2, 0))])
+    write_quads(os.path.join(d, "box_light.bin"), [((-0.25, 0.999, -0.25), (0.5, 0, 0), (0, 0, 0.5))])
+    v, f = uv_sphere(rings, segs)
+    glass_c, glass_r = np.array([0.0, -0.55, 0.0]), 0.35
+    disp = fbm_full((v * glass_r).astype(np.float32) * np.float32(4.0), 0.5, 8).astype(np.float64)
+    write_bin(os.path.join(d, "glass.bin"), glass_c + v * (glass_r + amplitude * disp)[:, None], v, f, f)
+    rng = np.random.default_rng(seed)
+    r = 0.14
+    centres, alphas = [], []
+    while len(centres) < copies:
+        c = rng.uniform([-0.8, -0.85, -0.8], [0.8, 0.7, 0.6])
+        if np.linalg.norm(c - glass_c) < glass_r + amplitude + r + 0.02:
+            continue
+        if any(np.linalg.norm(c - o) < 2 * r + 0.02 for o in centres):
+            continue
+        centres.append(c)
+        alphas.append(float(rng.uniform(0.05, 0.5)))
+    names = []
+    for k, c in enumerate(centres):
+        names.append(f"metal{k}")
+        write_bin(os.path.join(d, f"metal{k}.bin"), c + v * r, v, f, f)
+    with open(os.path.join(d, "stress.scene"), "w") as fh:
+        fh.write(CAMERA_BOX + IDENTITY_SUBJECT + "0\n"
+                 "5\ts_back\ts_floor\tbox_red\tbox_green\tbox_light\n"
+                 "5\n"
+                 "L\tc\t0.7 0.7 0.7\t0\n"
+                 "L\tm\t8 0.5 4 1\t0\n"
+                 "L\tc\t0.7 0.1 0.1\t0\n"
+                 "L\tc\t0.1 0.7 0.1\t0\n"
+                 "L\tc\t0 0 0\t0\n"
+                 "1\t10 10 10\n"
+                 "1\t0.5 0.5 0.5\n")
+    with open(os.path.join(d, "stress.subject"), "w") as fh:
+        fh.write("0\n%d\tglass\t%s\n%d\n" % (1 + copies, "\t".join(names), 1 + copies))
+        fh.write("G\tc\t1 1 1\tc\t1 1 1\t1.5\n")
+        for a in alphas:
+            fh.write("C\tc\t3.9 2.4 1.8\tc\t0.2 0.4 1.4\t%.6f\n" % a)
+    return "stress", "stress"
 
 
 def random_triangles(n, seed=1):

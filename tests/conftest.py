@@ -24,6 +24,8 @@ def built_lib():
 
 def write_scene(kind, d):
     from lighttransportsimulation_gb300 import scenes
+    if kind == "stress_small":  # the stress scene with 16 x 32 spheres (tests/golden/make_golden_port.py)
+        return scenes.write_stress_scene(d, rings=16, segs=32)
     return {"box_sphere": scenes.write_box_sphere, "materials": scenes.write_materials_scene}[kind](d)
 
 
@@ -40,10 +42,10 @@ def scene_digest(d):
 def scene_dirs(tmp_path_factory):
     """Generated parity scenes, checked against the digests recorded in the fixtures."""
     out = {}
-    for kind in ("box_sphere", "materials"):
+    for kind in ("box_sphere", "materials", "stress_small"):
         d = str(tmp_path_factory.mktemp(kind))
         sc, sub = write_scene(kind, d)
-        fx = np.load(os.path.join(GOLDEN, f"lbvh_{kind}.npz"))
+        fx = np.load(os.path.join(GOLDEN, f"lbvh_{kind}.npz" if kind != "stress_small" else f"render_{kind}.npz"))
         assert list(fx["scene_digest"]) == scene_digest(d), f"scene generator drifted for {kind}"
         out[kind] = (d, sc, sub)
     return out

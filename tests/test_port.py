@@ -34,7 +34,7 @@ def test_port_lbvh_bit_exact(port_exe, scene_dirs, kind, tmp_path):
         assert np.array_equal(b[k].view(np.uint32), fx[k].view(np.uint32)), k
 
 
-@pytest.mark.parametrize("kind", ["box_sphere", "materials"])
+@pytest.mark.parametrize("kind", ["box_sphere", "materials", "stress_small"])
 def test_port_per_sample_radiance_bit_exact(port_exe, scene_dirs, kind, tmp_path):
     from oracle import ltsd
     d, sc, sub = scene_dirs[kind]
@@ -46,7 +46,7 @@ def test_port_per_sample_radiance_bit_exact(port_exe, scene_dirs, kind, tmp_path
     assert np.array_equal(r["sig"], fx["sig"].reshape(-1))
 
 
-@pytest.mark.parametrize("kind", ["box_sphere", "materials"])
+@pytest.mark.parametrize("kind", ["box_sphere", "materials", "stress_small"])
 def test_port_film_bit_exact(port_exe, scene_dirs, kind, tmp_path):
     from oracle import ltsd
     d, sc, sub = scene_dirs[kind]
