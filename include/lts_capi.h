@@ -191,6 +191,13 @@ int lts_debug_trace_get(lts_ctx* ctx, float* out_64x16);
  * Unknown keys and negative values return LTS_ERR_ARG. */
 int lts_set_option(lts_ctx* ctx, const char* key, int64_t value);
 
+/* Tensor-core layout check (no counterpart in the reference): one 5th-generation tensor-core
+ * product of bf16 operands with FP32 accumulation, in one of the three operand arrangements the
+ * radiance-cache MLP uses.  mode 0: a 128x64, b 64x64, d = a b^T (128x64); mode 1: a 128x64,
+ * b 64x96, d = a b (128x96); mode 2: a 128x96, b 128x64, d = a^T b (rows 0..95 of a 128x64 d).
+ * a, b: host arrays of bf16 bit patterns, row-major; d: host FP32. */
+int lts_debug_umma_probe(lts_ctx* ctx, int32_t mode, int32_t swap, const uint16_t* a, const uint16_t* b, float* d);
+
 /* ---------------------------------------------------------------- metrics */
 typedef struct {
     double bvh_build_ms;  /* device time of the last LBVH build */

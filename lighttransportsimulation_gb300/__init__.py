@@ -36,7 +36,7 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_scene_get_light_distribution", "lts_bvh_build", "lts_bvh_build_triangles",
            "lts_bvh_build_device_async", "lts_bvh_dump_get", "lts_render", "lts_render_async", "lts_film_get",
            "lts_write_image", "lts_get_metrics", "lts_bvh_build_noalloc", "lts_debug_trace_sample",
-           "lts_debug_trace_get", "lts_set_option"]
+           "lts_debug_trace_get", "lts_set_option", "lts_debug_umma_probe"]
 
 
 class LtsError(RuntimeError):
@@ -116,6 +116,7 @@ def library():
             "lts_debug_trace_sample": (I, [P, ctypes.c_int64]),
             "lts_debug_trace_get": (I, [P, P]),
             "lts_set_option": (I, [P, ctypes.c_char_p, ctypes.c_int64]),
+            "lts_debug_umma_probe": (I, [P, I, I, P, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)

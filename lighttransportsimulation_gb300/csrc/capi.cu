@@ -17,6 +17,7 @@
 #include "dev_common.cuh"
 #include "host_scene.hpp"
 #include "lbvh.cuh"
+#include "mlp.cuh"
 #include "tracer.cuh"
 
 namespace lts {
@@ -425,6 +426,14 @@ int lts_write_image(const char* path, const float* rgb, int32_t w, int32_t h, in
     }
     fclose(f);
     return LTS_OK;
+}
+
+int lts_debug_umma_probe(lts_ctx* ctx, int32_t mode, int32_t swap, const uint16_t* a, const uint16_t* b, float* d) {
+    if (!ctx || !a || !b || !d) return LTS_ERR_ARG;
+    if (ctx->device < 0) return fail(ctx, LTS_ERR_STATE, "host-only context");
+    const std::string e = umma_probe(mode, swap, a, b, d, ctx->d_error, ctx->stream);
+    if (!e.empty()) return fail(ctx, LTS_ERR_ARG, e);
+    return check_device_error(ctx);
 }
 
 int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {

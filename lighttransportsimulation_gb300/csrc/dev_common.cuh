@@ -37,6 +37,7 @@ enum DeviceError : uint32_t {
     DEV_ERR_QUEUE_OVERFLOW = 4u,
     DEV_ERR_BAD_INDEX = 8u,
     DEV_ERR_CAPACITY = 16u,
+    DEV_ERR_MMA_TIMEOUT = 32u,
 };
 
 // Upper bound of spin iterations of any wait on another block's flag.  A tile's predecessor
