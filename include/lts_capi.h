@@ -198,6 +198,23 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value);
  * a, b: host arrays of bf16 bit patterns, row-major; d: host FP32. */
 int lts_debug_umma_probe(lts_ctx* ctx, int32_t mode, int32_t swap, const uint16_t* a, const uint16_t* b, float* d);
 
+/* ---------------------------------------------------------------- radiance-cache MLP
+ * No counterpart in the reference.  A 96 -> 5 x 64 (ReLU) -> 3 (exp) network without biases,
+ * BF16 weights and activations on the tensor cores, FP32 master weights and Adam state, trained
+ * with the relative L2 loss mean((pred - target)^2 / (pred^2 + 0.01)).  Parameters: FP32, the
+ * row-major [out][in] matrices W0 (64x96), W1..W4 (64x64), W5 (16x64, rows 3..15 unused)
+ * concatenated (LTS_MLP_PARAMS values).  Features: n x 96 bf16 bit patterns per sample. */
+#define LTS_MLP_PARAMS 23552
+#define LTS_MLP_FEATURES 96
+int lts_mlp_init(lts_ctx* ctx, uint32_t seed);
+int lts_mlp_set_params(lts_ctx* ctx, const float* params);
+int lts_mlp_get_params(lts_ctx* ctx, float* params);
+int lts_mlp_forward(lts_ctx* ctx, const uint16_t* features, int32_t n, float* out_rgb);
+/* Gradient of the loss over the n samples; *loss receives the loss; grad (may be NULL) the
+ * gradient before the update; then one Adam step (beta1 0.9, beta2 0.99, eps 1e-8) when lr > 0. */
+int lts_mlp_train_step(lts_ctx* ctx, const uint16_t* features, const float* targets, int32_t n, float lr,
+                       float* loss, float* grad);
+
 /* ---------------------------------------------------------------- metrics */
 typedef struct {
     double bvh_build_ms;  /* device time of the last LBVH build */

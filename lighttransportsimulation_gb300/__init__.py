@@ -36,7 +36,8 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_scene_get_light_distribution", "lts_bvh_build", "lts_bvh_build_triangles",
            "lts_bvh_build_device_async", "lts_bvh_dump_get", "lts_render", "lts_render_async", "lts_film_get",
            "lts_write_image", "lts_get_metrics", "lts_bvh_build_noalloc", "lts_debug_trace_sample",
-           "lts_debug_trace_get", "lts_set_option", "lts_debug_umma_probe"]
+           "lts_debug_trace_get", "lts_set_option", "lts_debug_umma_probe", "lts_mlp_init", "lts_mlp_set_params",
+           "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step"]
 
 
 class LtsError(RuntimeError):
@@ -117,6 +118,11 @@ def library():
             "lts_debug_trace_get": (I, [P, P]),
             "lts_set_option": (I, [P, ctypes.c_char_p, ctypes.c_int64]),
             "lts_debug_umma_probe": (I, [P, I, I, P, P, P]),
+            "lts_mlp_init": (I, [P, ctypes.c_uint32]),
+            "lts_mlp_set_params": (I, [P, P]),
+            "lts_mlp_get_params": (I, [P, P]),
+            "lts_mlp_forward": (I, [P, P, I, P]),
+            "lts_mlp_train_step": (I, [P, P, P, I, ctypes.c_float, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -298,3 +304,46 @@ def write_image(path, rgb, fmt):
     rc = library().lts_write_image(path.encode(), _ptr(rgb), w, h, fmt)
     if rc != LTS_OK:
         raise LtsError(rc, path)
+
+
+class RadianceCacheMLP:
+    """The radiance-cache network of a context (lts_mlp_*): 96 bf16 features -> RGB."""
+
+    PARAMS = 23552
+    FEATURES = 96
+
+    def __init__(self, ctx, seed=1):
+        self.ctx = ctx
+        ctx.check(ctx.lib.lts_mlp_init(ctx.h, seed))
+
+    def params(self):
+        import numpy as np
+        out = np.zeros(self.PARAMS, np.float32)
+        self.ctx.check(self.ctx.lib.lts_mlp_get_params(self.ctx.h, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def set_params(self, p):
+        import numpy as np
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.PARAMS
+        self.ctx.check(self.ctx.lib.lts_mlp_set_params(self.ctx.h, p.ctypes.data_as(ctypes.c_void_p)))
+
+    def forward(self, feat_bits):
+        import numpy as np
+        f = np.ascontiguousarray(feat_bits, np.uint16).reshape(-1, self.FEATURES)
+        out = np.zeros((f.shape[0], 3), np.float32)
+        self.ctx.check(self.ctx.lib.lts_mlp_forward(self.ctx.h, f.ctypes.data_as(ctypes.c_void_p), f.shape[0],
+                                                    out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def train_step(self, feat_bits, targets, lr, want_grad=False):
+        """Returns (loss, gradient before the update or None)."""
+        import numpy as np
+        f = np.ascontiguousarray(feat_bits, np.uint16).reshape(-1, self.FEATURES)
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, 3)
+        loss = ctypes.c_float()
+        g = np.zeros(self.PARAMS, np.float32) if want_grad else None
+        self.ctx.check(self.ctx.lib.lts_mlp_train_step(
+            self.ctx.h, f.ctypes.data_as(ctypes.c_void_p), t.ctypes.data_as(ctypes.c_void_p), f.shape[0],
+            ctypes.c_float(lr), ctypes.byref(loss), g.ctypes.data_as(ctypes.c_void_p) if want_grad else None))
+        return loss.value, g

@@ -77,6 +77,7 @@ struct lts_ctx {
     float* d_tri = nullptr;  // scene triangle soup, 9 floats per triangle (scene order)
     size_t d_tri_cap = 0;
     std::unique_ptr<Lbvh> bvh;
+    std::unique_ptr<Mlp> mlp;
     int bvh_mode = -1;        // mode of the BVH currently held (-1: none)
     bool bvh_is_scene = false;
     std::unique_ptr<Tracer> tracer;
@@ -434,6 +435,88 @@ int lts_debug_umma_probe(lts_ctx* ctx, int32_t mode, int32_t swap, const uint16_
     const std::string e = umma_probe(mode, swap, a, b, d, ctx->d_error, ctx->stream);
     if (!e.empty()) return fail(ctx, LTS_ERR_ARG, e);
     return check_device_error(ctx);
+}
+
+namespace {
+int mlp_ready(lts_ctx* ctx) {
+    if (!ctx) return LTS_ERR_ARG;
+    if (ctx->device < 0) return fail(ctx, LTS_ERR_STATE, "host-only context");
+    if (!ctx->mlp || !ctx->mlp->ready()) return fail(ctx, LTS_ERR_STATE, "MLP not initialised (lts_mlp_init)");
+    return LTS_OK;
+}
+}  // namespace
+
+int lts_mlp_init(lts_ctx* ctx, uint32_t seed) {
+    if (!ctx) return LTS_ERR_ARG;
+    if (ctx->device < 0) return fail(ctx, LTS_ERR_STATE, "host-only context");
+    if (!ctx->mlp) ctx->mlp.reset(new Mlp());
+    const std::string e = ctx->mlp->init(seed, ctx->stream);
+    return e.empty() ? LTS_OK : fail(ctx, LTS_ERR_DEVICE, e);
+}
+
+int lts_mlp_set_params(lts_ctx* ctx, const float* params) {
+    if (int r = mlp_ready(ctx)) return r;
+    if (!params) return LTS_ERR_ARG;
+    const std::string e = ctx->mlp->set_params(params, ctx->stream);
+    return e.empty() ? LTS_OK : fail(ctx, LTS_ERR_DEVICE, e);
+}
+
+int lts_mlp_get_params(lts_ctx* ctx, float* params) {
+    if (int r = mlp_ready(ctx)) return r;
+    if (!params) return LTS_ERR_ARG;
+    const std::string e = ctx->mlp->get_params(params, ctx->stream);
+    return e.empty() ? LTS_OK : fail(ctx, LTS_ERR_DEVICE, e);
+}
+
+int lts_mlp_forward(lts_ctx* ctx, const uint16_t* features, int32_t n, float* out_rgb) {
+    if (int r = mlp_ready(ctx)) return r;
+    if (!features || !out_rgb || n < 0) return LTS_ERR_ARG;
+    if (n == 0) return LTS_OK;
+    void *df = nullptr, *dout = nullptr;
+    int rc = LTS_OK;
+    if (dev_alloc(&df, 2 * (size_t)n * kMlpIn) != cudaSuccess || dev_alloc(&dout, 12 * (size_t)n) != cudaSuccess) {
+        rc = fail(ctx, LTS_ERR_DEVICE, "MLP buffers: allocation failed");
+    } else {
+        std::string e;
+        cudaError_t c = cudaMemcpyAsync(df, features, 2 * (size_t)n * kMlpIn, cudaMemcpyHostToDevice, ctx->stream);
+        if (c == cudaSuccess) e = ctx->mlp->forward((const uint16_t*)df, n, (float*)dout, ctx->d_error, ctx->stream);
+        if (c == cudaSuccess && e.empty())
+            c = cudaMemcpyAsync(out_rgb, dout, 12 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
+        if (c != cudaSuccess) e = cudaGetErrorString(c);
+        rc = e.empty() ? check_device_error(ctx) : fail(ctx, LTS_ERR_DEVICE, e);
+    }
+    dev_free(df);
+    dev_free(dout);
+    return rc;
+}
+
+int lts_mlp_train_step(lts_ctx* ctx, const uint16_t* features, const float* targets, int32_t n, float lr,
+                       float* loss, float* grad) {
+    if (int r = mlp_ready(ctx)) return r;
+    if (!features || !targets || n <= 0) return LTS_ERR_ARG;
+    void *df = nullptr, *dt = nullptr, *dl = nullptr;
+    int rc = LTS_OK;
+    if (dev_alloc(&df, 2 * (size_t)n * kMlpIn) != cudaSuccess || dev_alloc(&dt, 12 * (size_t)n) != cudaSuccess ||
+        dev_alloc(&dl, 4) != cudaSuccess) {
+        rc = fail(ctx, LTS_ERR_DEVICE, "MLP buffers: allocation failed");
+    } else {
+        std::string e;
+        cudaError_t c = cudaMemcpyAsync(df, features, 2 * (size_t)n * kMlpIn, cudaMemcpyHostToDevice, ctx->stream);
+        if (c == cudaSuccess) c = cudaMemcpyAsync(dt, targets, 12 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+        if (c == cudaSuccess)
+            e = ctx->mlp->train_step((const uint16_t*)df, (const float*)dt, n, 0.0f, (float*)dl, ctx->d_error,
+                                     ctx->stream);
+        if (c == cudaSuccess && e.empty() && grad) e = ctx->mlp->get_grad(grad, ctx->stream);
+        if (c == cudaSuccess && e.empty() && loss) c = cudaMemcpyAsync(loss, dl, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (c == cudaSuccess && e.empty() && lr > 0) e = ctx->mlp->adam(lr, ctx->stream);
+        if (c == cudaSuccess && e.empty()) c = cudaStreamSynchronize(ctx->stream);
+        if (c != cudaSuccess) e = cudaGetErrorString(c);
+        rc = e.empty() ? check_device_error(ctx) : fail(ctx, LTS_ERR_DEVICE, e);
+    }
+    dev_free(df);
+    dev_free(dt);
+    dev_free(dl);
+    return rc;
 }
 
 int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
