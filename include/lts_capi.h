@@ -183,6 +183,16 @@ int lts_debug_trace_sample(lts_ctx* ctx, int64_t crop_sample_index);
 int lts_debug_trace_get(lts_ctx* ctx, float* out_64x16);
 
 /* Tuning knobs of the renderer (no counterpart in the reference).  Keys:
+ *   "radiance_cache"          1: wavefront paths end at the vertex after their first rough vertex
+ *                             (roughness > 0.3) with the MLP's radiance there; a share of paths is
+ *                             traced in full, supervises the MLP (one record per path at that
+ *                             vertex) and measures its bias; after each render the MLP takes Adam
+ *                             steps on the records.  Needs lts_mlp_init.
+ *   "radiance_cache_unbiased_permille" share of full paths (default 30 = 3 %)
+ *   "radiance_cache_train_samples"     training records per render (default 65536)
+ *   "radiance_cache_train_steps"       Adam steps per render (default 4)
+ *   "radiance_cache_lr_micro"          learning rate in 1e-6 (default 1000 = 1e-3)
+ *   "film_accumulate"         1: renders add to the film's sums instead of clearing them
  *   "bvh_width"               traversal structure: 8 (default) the 8-wide compressed BVH collapsed
  *                             from the LBVH, 2 the binary LBVH itself; both give the same hits
  *   "wavefront_pool"          path-state pool capacity in paths (0: automatic, 2^21)
@@ -230,6 +240,13 @@ typedef struct {
      * visits and triangle tests (filled by a synchronous lts_render); zero for the megakernel */
     double render_stage_ms[6];
     double kind_rays[3], kind_node_visits[3], kind_tri_tests[3];
+    /* radiance cache (wavefront with the option radiance_cache = 1): queries answered by the
+     * network, training records taken from the unbiased paths, the last Adam step's loss, the
+     * relative bias of the cache's mean against those records before the update, and the time of
+     * the bias check and training after the render */
+    double cache_queries;
+    int32_t cache_train_samples;
+    double cache_train_loss, cache_bias, cache_train_ms;
 } lts_metrics;
 int lts_get_metrics(lts_ctx* ctx, lts_metrics* out);
 

@@ -82,7 +82,10 @@ class Metrics(ctypes.Structure):
                 ("device_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int32),
                 ("render_launches", ctypes.c_int32), ("render_iterations", ctypes.c_int32),
                 ("render_stage_ms", ctypes.c_double * 6), ("kind_rays", ctypes.c_double * 3),
-                ("kind_node_visits", ctypes.c_double * 3), ("kind_tri_tests", ctypes.c_double * 3)]
+                ("kind_node_visits", ctypes.c_double * 3), ("kind_tri_tests", ctypes.c_double * 3),
+                ("cache_queries", ctypes.c_double), ("cache_train_samples", ctypes.c_int32),
+                ("cache_train_loss", ctypes.c_double), ("cache_bias", ctypes.c_double),
+                ("cache_train_ms", ctypes.c_double)]
 
 
 _lib = None

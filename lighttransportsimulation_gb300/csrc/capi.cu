@@ -526,6 +526,24 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
     if (!strcmp(key, "wavefront_pool")) {
         if (value >= (1ll << 30)) return fail(ctx, LTS_ERR_ARG, "wavefront_pool too large");
         ctx->tracer->wf_pool = (long)value;
+    } else if (!strcmp(key, "radiance_cache")) {
+        if (value && (!ctx->mlp || !ctx->mlp->ready()))
+            return fail(ctx, LTS_ERR_STATE, "radiance_cache needs an initialised MLP (lts_mlp_init)");
+        ctx->tracer->cache_mode = value ? 1 : 0;
+        ctx->tracer->mlp = ctx->mlp.get();
+    } else if (!strcmp(key, "radiance_cache_unbiased_permille")) {
+        if (value > 1000) return fail(ctx, LTS_ERR_ARG, "radiance_cache_unbiased_permille must be <= 1000");
+        ctx->tracer->cache_unbiased_permille = (int)value;
+    } else if (!strcmp(key, "radiance_cache_train_samples")) {
+        if (value > (1 << 22)) return fail(ctx, LTS_ERR_ARG, "radiance_cache_train_samples too large");
+        ctx->tracer->cache_train_cap = (int)value;
+    } else if (!strcmp(key, "radiance_cache_train_steps")) {
+        if (value < 1 || value > 64) return fail(ctx, LTS_ERR_ARG, "radiance_cache_train_steps must be 1..64");
+        ctx->tracer->cache_train_steps = (int)value;
+    } else if (!strcmp(key, "radiance_cache_lr_micro")) {
+        ctx->tracer->cache_lr = (float)value * 1e-6f;
+    } else if (!strcmp(key, "film_accumulate")) {
+        ctx->tracer->film_accumulate = value != 0;
     } else if (!strcmp(key, "bvh_width")) {
         if (value != 2 && value != 8) return fail(ctx, LTS_ERR_ARG, "bvh_width must be 2 or 8");
         ctx->tracer->bvh_width = (int)value;
@@ -559,6 +577,11 @@ int lts_get_metrics(lts_ctx* ctx, lts_metrics* out) {
     out->render_launches = ctx->tracer ? ctx->tracer->last_launches : 0;
     out->render_iterations = ctx->tracer ? ctx->tracer->last_iterations : 0;
     for (int k = 0; k < 6; ++k) out->render_stage_ms[k] = ctx->tracer ? ctx->tracer->last_stage_ms[k] : 0.0;
+    out->cache_queries = ctx->tracer ? ctx->tracer->last_cache_queries : 0.0;
+    out->cache_train_samples = ctx->tracer ? ctx->tracer->last_train_samples : 0;
+    out->cache_train_loss = ctx->tracer ? ctx->tracer->last_train_loss : 0.0;
+    out->cache_bias = ctx->tracer ? ctx->tracer->last_cache_bias : 0.0;
+    out->cache_train_ms = ctx->tracer ? ctx->tracer->last_train_ms : 0.0;
     for (int k = 0; k < 3; ++k) {
         out->kind_rays[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k] : 0.0;
         out->kind_node_visits[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k + 1] : 0.0;

@@ -202,9 +202,11 @@ __device__ __forceinline__ void load_feature_row(unsigned char* smem, const uint
     }
 }
 
-// Inference: out[n][3] = exp(z[0..2]).  Persistent CTAs of 128 threads, one row per thread.
+// Inference: out[r * stride + c] = exp(z_c), c < 3, for the feature rows r = rows[i] (rows null:
+// r = i), i < n.  Persistent CTAs of 128 threads, one row per thread.
 __global__ __launch_bounds__(128) void k_mlp_forward(const uint16_t* __restrict__ w16, const uint16_t* __restrict__ feat,
-                                                     int n, float* __restrict__ out, uint32_t* err) {
+                                                     const int32_t* __restrict__ rows, int n, float* __restrict__ out,
+                                                     int stride, uint32_t* err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     uint64_t* mbar = (uint64_t*)(smem + kFwdBar);
     uint32_t* tslot = (uint32_t*)(smem + kFwdBar + 16);
@@ -216,14 +218,15 @@ __global__ __launch_bounds__(128) void k_mlp_forward(const uint16_t* __restrict_
     uint32_t phase = 0;
     const int ntiles = (n + 127) / 128;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long grow = (long)tile * 128 + threadIdx.x;
-        const bool valid = grow < n;
-        load_feature_row(smem, feat, grow, valid);
+        const long i = (long)tile * 128 + threadIdx.x;
+        const bool valid = i < n;
+        const long r = valid ? (rows ? (long)__ldg(rows + i) : i) : 0;
+        load_feature_row(smem, feat, r, valid);
         publish_smem();
         float z[16];
         if (!mlp_forward_tile<false>(smem, tmem, mbar, phase, err, z)) break;
         if (valid)
-            for (int c = 0; c < kMlpOut; ++c) out[grow * 3 + c] = expf(z[c]);
+            for (int c = 0; c < kMlpOut; ++c) out[r * stride + c] = expf(z[c]);
         tc_fence_before();
         __syncthreads();  // every row read the output before the next tile's products
         tc_fence_after();
@@ -477,11 +480,12 @@ std::string Mlp::get_grad(float* host, cudaStream_t s) {
     return "";
 }
 
-std::string Mlp::forward(const uint16_t* d_feat, int n, float* d_out, uint32_t* d_err, cudaStream_t s) {
+std::string Mlp::forward(const uint16_t* d_feat, int n, float* d_out, uint32_t* d_err, cudaStream_t s,
+                         const int32_t* d_rows, int out_stride) {
     if (!w32_) return "MLP not initialised";
     if (n <= 0) return "";
     const int tiles = (n + 127) / 128;
-    k_mlp_forward<<<std::min(tiles, blocks_fwd_), 128, kFwdSmem, s>>>(w16_, d_feat, n, d_out, d_err);
+    k_mlp_forward<<<std::min(tiles, blocks_fwd_), 128, kFwdSmem, s>>>(w16_, d_feat, d_rows, n, d_out, out_stride, d_err);
     TRY(cudaGetLastError());
     return "";
 }

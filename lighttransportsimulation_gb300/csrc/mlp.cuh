@@ -41,8 +41,10 @@ class Mlp {
     std::string set_params(const float* host, cudaStream_t s);  // kMlpParams FP32 values
     std::string get_params(float* host, cudaStream_t s);
 
-    // out[n][3] = network(features[n][96]) (device pointers; features are bf16 bits).
-    std::string forward(const uint16_t* d_feat, int n, float* d_out, uint32_t* d_err, cudaStream_t s);
+    // out[r * out_stride + c] = network(features[r][96])_c for r = rows[i] (rows null: r = i),
+    // i < n (device pointers; features are bf16 bits).
+    std::string forward(const uint16_t* d_feat, int n, float* d_out, uint32_t* d_err, cudaStream_t s,
+                        const int32_t* d_rows = nullptr, int out_stride = 3);
     // Gradient of the relative L2 loss mean((pred - t)^2 / (pred^2 + 0.01)) over the n samples
     // into the gradient buffer (zeroed first), the loss into *d_loss (device), then, if lr > 0,
     // one Adam step (beta 0.9 / 0.99, eps 1e-8) that also zeroes the gradient.

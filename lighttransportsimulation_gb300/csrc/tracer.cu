@@ -14,6 +14,7 @@
 //  - the film accumulates each pixel's own 2x2 splat footprint in compensated FP32 (Kahan) in
 //    shared memory and flushes it once per pixel to FP64 sums; the rare wider splats go straight
 //    to FP64 atomics.  The resolve divides in FP64.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +27,7 @@
 #include "dev_math.cuh"
 #include "tracer.cuh"
 #include "tracer_dev.cuh"
+#include "mlp.cuh"
 
 namespace lts {
 namespace {
@@ -118,6 +120,7 @@ void Tracer::free_all() {
         p = nullptr;
     }
     wf_cap_ = wf_fs_cap_ = 0;
+    wf_cache_cap_ = wf_train_cap_ = 0;
     film_cap_ = rec_cap_ = 0;
     leaf_serial_ = 0;
 }
@@ -293,7 +296,7 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
         TRY(dev_alloc((void**)&rgb_, 12 * (size_t)sc.width * sc.height));
         film_cap_ = film_bytes;
     }
-    TRY(cudaMemsetAsync(film_, 0, film_bytes, s));
+    if (!film_accumulate) TRY(cudaMemsetAsync(film_, 0, film_bytes, s));
     TRY(cudaMemsetAsync(counters_, 0, 128, s));
     const long ns = (long)(x1 - x0) * (y1 - y0) * d.spp;
     *crop_samples = ns;
@@ -425,6 +428,33 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
     st.q_free = (int32_t*)b[30]; st.counts = (uint32_t*)b[31]; st.wid = (int32_t*)b[32];
     st.fs_L = (float4*)b[33]; st.fs_y = (float*)b[34];
     st.q_cls = (int32_t*)b[35];
+    // radiance cache buffers (allocated on first use with the cache on)
+    const bool cache = cache_mode != 0 && mlp != nullptr && mlp->ready();
+    st.cache = cache ? 1 : 0;
+    st.unb_permille = (uint32_t)std::max(0, std::min(1000, cache_unbiased_permille));
+    st.tr_cap = (uint32_t)std::max(0, cache_train_cap);
+    st.bounds = sv.root_bounds;
+    if (cache) {
+        if (wf_cache_cap_ < P || wf_train_cap_ < (long)st.tr_cap) {
+            for (int k = 36; k < 45; ++k) {
+                dev_free(wf_bufs_[k]);
+                wf_bufs_[k] = nullptr;
+            }
+            wf_cache_cap_ = wf_train_cap_ = 0;
+            const size_t n = (size_t)P, m = std::max<size_t>(1, st.tr_cap);
+            const size_t sz[7] = {2 * 96 * n, 16 * n, 4 * n, 16 * n, 16 * n, 4 * n, 2 * 96 * m};
+            for (int k = 0; k < 7; ++k) TRY(dev_alloc(&wf_bufs_[36 + k], sz[k]));
+            TRY(dev_alloc(&wf_bufs_[43], 12 * m + 16));  // targets, then the loss word
+            TRY(dev_alloc(&wf_bufs_[44], 12 * m));       // the cache's predictions for the records
+            wf_cache_cap_ = P;
+            wf_train_cap_ = (long)st.tr_cap;
+        }
+        st.feat = (uint16_t*)b[36]; st.cache_L = (float4*)b[37]; st.q_cache = (int32_t*)b[38];
+        st.tr_beta = (float4*)b[39]; st.tr_L0 = (float4*)b[40]; st.tr_idx = (int32_t*)b[41];
+        st.tr_feat = (uint16_t*)b[42]; st.tr_target = (float*)b[43];
+    }
+    last_cache_queries = 0;
+    last_train_samples = 0;
     if (rp.sample_sig) {
         TRY(cudaMemsetAsync(st.ev_mis, 0, 8 * (size_t)P, s));
         TRY(cudaMemsetAsync(st.ev_main, 0, 8 * (size_t)P, s));
@@ -432,6 +462,7 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
     auto blocks = [](long n) { return (unsigned)((n + kWfBlock - 1) / kWfBlock); };
     TRY(cudaEventRecord(ev0_, s));
     k_wf_init_free<<<blocks(P), kWfBlock, 0, s>>>(st.q_free, st.pix, (int)P);  // every slot free
+    TRY(cudaMemsetAsync(st.counts + 32, 0, 4, s));  // training records of this render
     const bool rec = rp.sample_sig != nullptr;
     const bool wide = sv.wnodes != nullptr;
     int iters = 0, launches = 1;
@@ -455,14 +486,14 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
         const int nsc = std::min(chunk, d.spp - s0);
         const long ctot = npix * nsc;
         long generated = 0;
-        uint32_t nfree = (uint32_t)P, n_cont = 0, n_fin = 0, n_sh = 0, n_mis = 0;
+        uint32_t nfree = (uint32_t)P, n_cont = 0, n_fin = 0, n_sh = 0, n_mis = 0, n_query = 0;
         int32_t *q_ext = st.q_a, *q_fin = st.q_b;
         for (;; ++iters) {
             const uint32_t take = (uint32_t)std::min<long>(nfree, ctot - generated);
             const uint32_t n_ext = n_cont + take;
             if (n_ext == 0 && n_fin == 0) break;
             if (iters > 1000000) return "wavefront did not converge";
-            TRY(cudaMemsetAsync(st.counts, 0, 256, s));
+            TRY(cudaMemsetAsync(st.counts, 0, 128, s));  // per-iteration counters (words 0..31)
             TRY(cudaEventRecord(wf_ev_[0], s));
             if (take) {
                 k_wf_generate<<<blocks(take), kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_cont, generated, take, s0, npix);
@@ -475,6 +506,12 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
                 if (wide) k_wf_trace<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_ext, n_sh, n_mis, st.counts + 8, bvh.n);
                 else k_wf_trace<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_ext, n_sh, n_mis, st.counts + 8, bvh.n);
                 ++launches;
+            }
+            if (n_query) {  // the previous shade's cache queries, before finalize adds them
+                const std::string me = mlp->forward(st.feat, (int)n_query, (float*)st.cache_L, rp.err, s, st.q_cache, 4);
+                if (!me.empty()) return me;
+                ++launches;
+                last_cache_queries += n_query;
             }
             TRY(cudaEventRecord(wf_ev_[2], s));
             if (n_fin) {
@@ -495,7 +532,7 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
             ++launches;
             TRY(cudaEventRecord(wf_ev_[5], s));
             TRY(cudaGetLastError());
-            TRY(cudaMemcpyAsync(wf_counts_host_, st.counts, 32, cudaMemcpyDeviceToHost, s));
+            TRY(cudaMemcpyAsync(wf_counts_host_, st.counts, 64, cudaMemcpyDeviceToHost, s));
             TRY(cudaStreamSynchronize(s));
             for (int k = 0; k < 5; ++k) {
                 float ms = 0;
@@ -508,6 +545,7 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
             n_sh = wf_counts_host_[2];
             n_mis = wf_counts_host_[3];
             nfree = wf_counts_host_[4];
+            n_query = wf_counts_host_[12];
             std::swap(q_ext, q_fin);
         }
         if (nfree != (uint32_t)P) return "wavefront: path pool did not drain";
@@ -523,9 +561,63 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
         TRY(cudaEventElapsedTime(&ms, wf_ev_[0], wf_ev_[6]));
         last_stage_ms[5] += ms;
     }
+    if (cache) {  // train the cache on this render's unbiased suffixes
+        const std::string te = train_cache(st.counts, st.tr_feat, st.tr_target, st.tr_cap, s, rp.err);
+        if (!te.empty()) return te;
+        launches += 1 + cache_train_steps;
+    }
     TRY(cudaEventRecord(ev1_, s));
     last_launches = launches;
     last_iterations = iters;
+    return "";
+}
+
+// After a render with the radiance cache: the cache's bias on this render's training records
+// (its prediction against the unbiased suffix radiance), then `cache_train_steps` Adam steps over
+// the records in equal mini-batches.
+std::string Tracer::train_cache(uint32_t* d_counts, uint16_t* tr_feat, float* tr_target, uint32_t tr_cap,
+                                cudaStream_t s, uint32_t* d_err) {
+    uint32_t nrec = 0;
+    TRY(cudaMemcpyAsync(&nrec, d_counts + 32, 4, cudaMemcpyDeviceToHost, s));
+    TRY(cudaStreamSynchronize(s));
+    const int n = (int)std::min<uint32_t>(nrec, tr_cap);
+    last_train_samples = n;
+    if (n <= 0) return "";
+    cudaEvent_t a, b;
+    TRY(cudaEventCreate(&a));
+    TRY(cudaEventCreate(&b));
+    TRY(cudaEventRecord(a, s));
+    // bias of the cache before this frame's update, on the same vertices
+    float* pred = (float*)wf_bufs_[44];
+    std::string e = mlp->forward(tr_feat, n, pred, d_err, s);
+    if (!e.empty()) return e;
+    std::vector<float> hp(3 * (size_t)n), ht(3 * (size_t)n);
+    TRY(cudaMemcpyAsync(hp.data(), pred, 12 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    TRY(cudaMemcpyAsync(ht.data(), tr_target, 12 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    TRY(cudaStreamSynchronize(s));
+    double num = 0, den = 0;
+    for (size_t k = 0; k < hp.size(); ++k) {
+        num += (double)hp[k] - (double)ht[k];
+        den += (double)ht[k];
+    }
+    last_cache_bias = den != 0 ? num / den : 0.0;  // relative bias of the mean
+    float* d_loss = tr_target + 3 * (size_t)tr_cap;
+    const int steps = std::max(1, cache_train_steps);
+    const int nb = std::max(1, n / steps);
+    for (int k = 0; k < steps && k * nb < n; ++k) {
+        const int cnt = std::min(nb, n - k * nb);
+        e = mlp->train_step(tr_feat + (size_t)k * nb * 96, tr_target + 3 * (size_t)k * nb, cnt, cache_lr, d_loss, d_err,
+                            s);
+        if (!e.empty()) return e;
+    }
+    TRY(cudaEventRecord(b, s));
+    TRY(cudaMemcpyAsync(&last_train_loss, d_loss, 4, cudaMemcpyDeviceToHost, s));
+    TRY(cudaEventSynchronize(b));
+    float ms = 0;
+    TRY(cudaEventElapsedTime(&ms, a, b));
+    last_train_ms = ms;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
     return "";
 }
 

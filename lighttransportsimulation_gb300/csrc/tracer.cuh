@@ -93,6 +93,18 @@ class Tracer {
     long wf_pool = 0;
     // Traversal structure: 8 = the collapsed 8-wide compressed BVH, 2 = the binary LBVH.
     int bvh_width = 8;
+    // Radiance cache (wavefront integrator): on/off, the MLP it queries and trains (owned by the
+    // context), the share of paths traced in full (per mille), training records per render, Adam
+    // steps per render and learning rate; statistics of the last render.
+    int cache_mode = 0;
+    class Mlp* mlp = nullptr;
+    int cache_unbiased_permille = 30, cache_train_cap = 65536, cache_train_steps = 4;
+    float cache_lr = 1e-3f;
+    double last_cache_queries = 0, last_cache_bias = 0;
+    int last_train_samples = 0;
+    float last_train_loss = 0, last_train_ms = 0;
+    // Keep the film's sums across renders (progressive rendering) instead of clearing them.
+    bool film_accumulate = false;
     bool last_wide = false;  // the last render traversed the wide BVH
     // Finished-sample buffer capacity of the wavefront film gather, in samples (0: 2^27).
     long wf_sample_cap = 0;
@@ -113,7 +125,10 @@ class Tracer {
     void free_all();
     std::string render_wavefront(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                                  uint32_t* d_err, const RenderParams& rp, const SceneView& sv, long total);
-    void* wf_bufs_[40] = {nullptr};
+    void* wf_bufs_[48] = {nullptr};
+    long wf_cache_cap_ = 0, wf_train_cap_ = 0;
+    std::string train_cache(uint32_t* d_counts, uint16_t* tr_feat, float* tr_target, uint32_t tr_cap, cudaStream_t s,
+                            uint32_t* d_err);
     long wf_cap_ = 0, wf_fs_cap_ = 0;
     uint32_t* wf_counts_host_ = nullptr;
     cudaEvent_t wf_ev_[7] = {nullptr};

@@ -27,7 +27,9 @@
 namespace lts {
 namespace {
 
-enum : uint32_t { WF_VIS = 1u, WF_MIS = 2u, WF_NEE = 4u, WF_DONE = 8u };
+enum : uint32_t { WF_VIS = 1u, WF_MIS = 2u, WF_NEE = 4u, WF_DONE = 8u, WF_CACHE = 16u };
+// path flags (low byte; the bounce count sits above bit 8)
+enum : uint32_t { FL_SPECULAR = 1u, FL_ROUGH = 2u, FL_UNBIASED = 4u, FL_RECORDED = 8u };
 constexpr int kWfBlock = 128;
 constexpr uint64_t kSigBasis = 0xcbf29ce484222325ull;
 
@@ -50,7 +52,67 @@ struct WfState {
     int32_t* q_cls;    // [kShadeClasses][pool] this iteration's paths grouped by shade class
     float4* fs_L;      // finished samples of the chunk: radiance rgb, film x (chunk index order)
     float* fs_y;       // film y
+    // radiance cache (cache == 0: off, pointers unused)
+    int cache;
+    uint32_t unb_permille;  // share of paths traced in full (unbiased), per mille
+    uint32_t tr_cap;        // training records per render
+    const float* bounds;    // scene bounds: position features are normalised to the unit cube
+    uint16_t* feat;         // [pool][96] features of the vertex a path queries
+    float4* cache_L;        // [pool] the cache's radiance for that vertex
+    int32_t* q_cache;       // this iteration's queries (count in counts[12])
+    float4 *tr_beta, *tr_L0;  // an unbiased path's throughput and radiance at its recorded vertex
+    int32_t* tr_idx;        // its training record
+    uint16_t* tr_feat;      // [tr_cap][96] training features (count in counts[32])
+    float* tr_target;       // [tr_cap][3] training targets
 };
+
+// Radiance-cache features of a shading point (the layout oracle/mlp_np.py's encode states):
+// 12-frequency sin/cos of the position in the unit cube of the scene bounds, the direction
+// towards the previous vertex, the shading normal, roughness, diffuse and specular albedo, 1.
+__device__ __forceinline__ float bsdf_roughness(const Bsdf& f) {
+    return (f.lobe == LOBE_LAMBERT || f.lobe == LOBE_OREN_NAYAR) ? 1.0f : (f.lobe == LOBE_MICROFACET ? f.alpha : 0.0f);
+}
+__device__ void write_features(const WfState& st, const SI& si, const Bsdf& f, uint16_t* out) {
+    float v[96];
+#pragma unroll
+    for (int k = 0; k < 96; ++k) v[k] = 0.0f;
+    const float pc[3] = {si.p.x, si.p.y, si.p.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float lo = __ldg(st.bounds + a), ext = __ldg(st.bounds + 3 + a) - lo;
+        const float u = ext > 0.0f ? (pc[a] - lo) / ext : 0.5f;
+        float fr = 3.14159265358979f;
+#pragma unroll
+        for (int j = 0; j < 12; ++j) {
+            float sn, cs;
+            sincosf(u * fr, &sn, &cs);
+            v[a * 12 + j] = sn;
+            v[36 + a * 12 + j] = cs;
+            fr *= 2.0f;
+        }
+    }
+    v[72] = si.wo.x; v[73] = si.wo.y; v[74] = si.wo.z;
+    v[75] = si.sn.x; v[76] = si.sn.y; v[77] = si.sn.z;
+    v[78] = bsdf_roughness(f);
+    const bool diffuse = f.lobe == LOBE_LAMBERT || f.lobe == LOBE_OREN_NAYAR;
+    const Spec ks = f.lobe == LOBE_MICROFACET ? spec(1.0f) : f.R;
+    if (diffuse) {
+        v[79] = f.R.r; v[80] = f.R.g; v[81] = f.R.b;
+    } else {
+        v[82] = ks.r; v[83] = ks.g; v[84] = ks.b;
+    }
+    v[85] = 1.0f;
+    uint4* o = (uint4*)out;
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+        uint32_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            w[q] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[8 * j + 2 * q])) |
+                   ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[8 * j + 2 * q + 1])) << 16);
+        o[j] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
 
 // Resume a (pixel, sample) stream at draw `draw` (regenerates the current Philox block).
 __device__ __forceinline__ void rng_resume(Rng& r) {
@@ -108,7 +170,8 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, co
     st.smp[slot] = s;
     st.wid[slot] = (int32_t)w;
     st.draw[slot] = rng.draw;
-    st.flags[slot] = 0u;
+    st.flags[slot] = (st.cache && wang_hash((uint32_t)id ^ ((uint32_t)s * 0x9E3779B9u)) % 1000u < st.unb_permille)
+                         ? FL_UNBIASED : 0u;
     st.pend[slot] = 0u;
     st.pf[slot] = make_float2(pfx, pfy);
     st.ro[slot] = make_float4(sv.cam[0], sv.cam[1], sv.cam[2], 0.f);
@@ -381,6 +444,27 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
         }
         if (!make_bsdf(sv, si, f, RECORD ? &evs : nullptr)) done = true;
     }
+    bool recorded = (flags & FL_RECORDED) != 0, rough_seen = (flags & FL_ROUGH) != 0;
+    if (st.cache && !done && rough_seen) {
+        // the vertex after the first rough one: cached paths end here with the cache's radiance,
+        // unbiased paths record a training sample once and go on
+        if (!(flags & FL_UNBIASED)) {
+            write_features(st, si, f, st.feat + (size_t)p * 96);
+            st.q_cache[atomicAdd(&st.counts[12], 1u)] = p;
+            pend |= WF_CACHE;
+            done = true;
+        } else if (!recorded) {
+            const uint32_t r = atomicAdd(&st.counts[32], 1u);
+            if (r < st.tr_cap) {
+                write_features(st, si, f, st.tr_feat + (size_t)r * 96);
+                st.tr_idx[p] = (int32_t)r;
+                st.tr_beta[p] = make_float4(beta.r, beta.g, beta.b, 0.f);
+                st.tr_L0[p] = make_float4(L.r, L.g, L.b, 0.f);
+                recorded = true;
+            }
+        }
+    }
+    if (!done && bsdf_roughness(f) > 0.3f) rough_seen = true;
     uint64_t ev_mis = 0, ev_main = 0;
     if (!done) {
         if (sv.nlight > 0) {
@@ -492,7 +576,8 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
     }
     st.pend[p] = pend | (done ? WF_DONE : 0u);
     st.draw[p] = rng.draw;
-    st.flags[p] = ((uint32_t)(bounce + 1) << 8) | (specular ? 1u : 0u);
+    st.flags[p] = ((uint32_t)(bounce + 1) << 8) | (specular ? FL_SPECULAR : 0u) | (rough_seen ? FL_ROUGH : 0u) |
+                  (flags & FL_UNBIASED) | (recorded ? FL_RECORDED : 0u);
     st.beta[p] = make_float4(beta.r, beta.g, beta.b, 0.f);
     st.L[p] = make_float4(L.r, L.g, L.b, 0.f);
     if (RECORD) {
@@ -531,6 +616,10 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
         const float4 nb = st.nee_beta[p];
         L = L + Spec{nb.x, nb.y, nb.z} * (Ld / nb.w);
     }
+    if (pend & WF_CACHE) {  // the path ends in the cache: beta * cached radiance of the vertex
+        const float4 c = st.cache_L[p], b = st.beta[p];
+        L = L + Spec{b.x, b.y, b.z} * Spec{c.x, c.y, c.z};
+    }
     if (RECORD && st.ev_main[p]) fnv_mix(sig, st.ev_main[p]);
     if (RECORD) {
         st.sig[p] = sig;
@@ -540,6 +629,14 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
     if (!(pend & WF_DONE)) {
         st.L[p] = make_float4(L.r, L.g, L.b, 0.f);
         return;
+    }
+    if (st.cache && (st.flags[p] & FL_RECORDED)) {  // training target: radiance after the vertex / beta there
+        const int r = st.tr_idx[p];
+        const float4 tb = st.tr_beta[p], l0 = st.tr_L0[p];
+        float* tg = st.tr_target + 3 * (size_t)r;
+        tg[0] = tb.x > 0.f ? (L.r - l0.x) / tb.x : 0.f;
+        tg[1] = tb.y > 0.f ? (L.g - l0.y) / tb.y : 0.f;
+        tg[2] = tb.z > 0.f ? (L.b - l0.z) / tb.z : 0.f;
     }
     // Camera::addSample (Camera.cu:192-218): the sample reaches film pixels [ceil(pf - 1),
     // floor(pf + 1)] per axis.  With pf in [i, i + 1] that is i .. i + 2, gathered later, plus
