@@ -360,6 +360,95 @@ def run_gpu(args, wl):
         dist.destroy_process_group()
 
 
+def time_to_rmse(args):
+    """Time for the cached wavefront renderer and for the plain megakernel to bring the stress scene
+    (1920x1080, 16 bounces, roulette from 4) to an RMSE <= target against an FP64 oracle render.
+    The oracle is the FP64 megakernel on a centred crop at high spp; RMSE is taken over the crop's
+    interior (2 pixels in from its edge: border pixels of a crop render miss splats from outside).
+    Both renderers accumulate full frames (film_accumulate); time = summed device time of the
+    renders (for the cached renderer this includes the bias check and the Adam steps after each
+    frame, and its warm-up frames)."""
+    import numpy as np
+
+    import lighttransportsimulation_gb300 as lts
+    wl = STRESS
+    W, H = wl["width"], wl["height"]
+    cw, ch = args.ttr_crop
+    x0, y0 = (W - cw) // 2, (H - ch) // 2
+    x1, y1 = x0 + cw, y0 + ch
+    ctx = lts.Context(0)
+    d, sc, sub = scene_dir(wl)
+    scene = lts.Scene.parse(ctx, d, sc, sub, W, H)
+    maxb, rr = wl["max_bounce"], wl["rr_start"]
+
+    def interior(film):
+        img = film.reshape(H, W, 3)[::-1]  # the resolve flips rows; undo to index by pixel row
+        return img[y0 + 2:y1 - 2, x0 + 2:x1 - 2].astype(np.float64)
+
+    # FP64 oracle on the crop, in passes of at most 256 spp
+    t0 = time.time()
+    oracle_ms = 0.0
+    o = lts.PathTracingIntegrator(maxb, rr, scene, integrator=lts.INTEGRATOR_FP64)
+    spp_pass = min(args.ttr_oracle_spp, 256)
+    npass = max(1, args.ttr_oracle_spp // spp_pass)
+    half = None
+    for k in range(npass):
+        ctx.set_option("film_accumulate", 0 if k == 0 else 1)
+        r = o.render(spp_pass, 50_000 + k, crop=(x0, y0, x1, y1))
+        oracle_ms += r["render_ms"]
+        if k == npass // 2 - 1:
+            half = interior(r["film"])
+    oracle = interior(r["film"])
+    ctx.set_option("film_accumulate", 0)
+    # the oracle's own error, estimated from its first half against the whole
+    oracle_err = float(np.sqrt(np.mean((half - oracle) ** 2))) if half is not None else None
+
+    def run(kind):
+        integ = lts.PathTracingIntegrator(maxb, rr, scene, integrator=0 if kind == "plain" else 1)
+        spp = args.ttr_spp_plain if kind == "plain" else args.ttr_spp_cached
+        dev_ms, curve, reached = 0.0, [], None
+        if kind == "cached":
+            lts.RadianceCacheMLP(ctx, seed=7)
+            ctx.set_option("radiance_cache", 1)
+            for k in range(args.ttr_warmup):
+                ctx.set_option("film_accumulate", 0)
+                dev_ms += integ.render(1, 90_000 + k, film=False)["render_ms"]
+        frame = 0
+        while dev_ms < 1000 * args.ttr_max_seconds:
+            ctx.set_option("film_accumulate", 0 if frame == 0 else 1)
+            r = integ.render(spp, 1_000 + frame)
+            dev_ms += r["render_ms"]
+            frame += 1
+            e = float(np.sqrt(np.mean((interior(r["film"]) - oracle) ** 2)))
+            curve.append((frame * spp, round(dev_ms / 1000, 3), round(e, 5)))
+            if e <= args.ttr_target:
+                reached = dev_ms / 1000
+                break
+        m = ctx.metrics()
+        ctx.set_option("radiance_cache", 0)
+        ctx.set_option("film_accumulate", 0)
+        out = {"seconds_to_target": reached, "seconds_run": round(dev_ms / 1000, 3), "spp": frame * spp,
+               "final_rmse": curve[-1][2], "curve": curve[:: max(1, len(curve) // 12)] + curve[-1:]}
+        if kind == "cached":
+            out.update(cache_bias=round(m.cache_bias, 4), train_loss=round(m.cache_train_loss, 4),
+                       warmup_frames=args.ttr_warmup)
+        return out
+
+    plain = run("plain")
+    cached = run("cached")
+    line = {"metric": "time-to-RMSE", "target_rmse": args.ttr_target, "unit": "s", "higher_is_better": False,
+            "config": {"workload": wl["name"], "width": W, "height": H, "max_bounce": maxb, "rr_start": rr,
+                       "crop": [x0, y0, x1, y1], "oracle_spp": npass * spp_pass,
+                       "oracle_seconds": round(oracle_ms / 1000, 2), "oracle_rmse_estimate": oracle_err,
+                       "frame_spp": {"plain": args.ttr_spp_plain, "cached": args.ttr_spp_cached}},
+            "plain_megakernel": plain, "cached_wavefront": cached,
+            "speedup": (plain["seconds_to_target"] / cached["seconds_to_target"])
+            if plain["seconds_to_target"] and cached["seconds_to_target"] else None,
+            "wall_s": round(time.time() - t0, 1)}
+    print(json.dumps(line))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -376,8 +465,20 @@ def main():
                     help="traversal structure: 8-wide compressed BVH or the binary LBVH")
     ap.add_argument("--lbvh-only", type=int, default=0, metavar="N",
                     help="only time the LBVH build over N random triangles (seed 1)")
+    ap.add_argument("--time-to-rmse", action="store_true",
+                    help="time for the cached wavefront and the plain megakernel to reach --ttr-target RMSE")
+    ap.add_argument("--ttr-target", type=float, default=1e-2)
+    ap.add_argument("--ttr-crop", type=int, nargs=2, default=[192, 108])
+    ap.add_argument("--ttr-oracle-spp", type=int, default=16384)
+    ap.add_argument("--ttr-spp-plain", type=int, default=8)
+    ap.add_argument("--ttr-spp-cached", type=int, default=4)
+    ap.add_argument("--ttr-warmup", type=int, default=8)
+    ap.add_argument("--ttr-max-seconds", type=float, default=60.0)
     args = ap.parse_args()
     wl = SMALL if args.small else (STRESS if args.stress else WORKLOAD)
+    if args.time_to_rmse:
+        time_to_rmse(args)
+        return
     if args.lbvh_only:
         import lighttransportsimulation_gb300 as lts
         ctx = lts.Context(0)
