@@ -360,6 +360,9 @@ def run_gpu(args, wl):
         dist.destroy_process_group()
 
 
+TTR_LEVELS = (0.05, 0.03, 0.02, 0.015, 0.0125, 0.01)
+
+
 def time_to_rmse(args):
     """Time for the cached wavefront renderer and for the plain megakernel to bring the stress scene
     (1920x1080, 16 bounces, roulette from 4) to an RMSE <= target against an FP64 oracle render.
@@ -427,8 +430,13 @@ def time_to_rmse(args):
         m = ctx.metrics()
         ctx.set_option("radiance_cache", 0)
         ctx.set_option("film_accumulate", 0)
+        levels = {}
+        for lv in TTR_LEVELS:
+            hit = next((c for c in curve if c[2] <= lv), None)
+            levels[str(lv)] = hit[1] if hit else None
         out = {"seconds_to_target": reached, "seconds_run": round(dev_ms / 1000, 3), "spp": frame * spp,
-               "final_rmse": curve[-1][2], "curve": curve[:: max(1, len(curve) // 12)] + curve[-1:]}
+               "final_rmse": curve[-1][2], "seconds_to_rmse": levels,
+               "curve": curve[:: max(1, len(curve) // 12)] + curve[-1:]}
         if kind == "cached":
             out.update(cache_bias=round(m.cache_bias, 4), train_loss=round(m.cache_train_loss, 4),
                        warmup_frames=args.ttr_warmup)
@@ -444,6 +452,8 @@ def time_to_rmse(args):
             "plain_megakernel": plain, "cached_wavefront": cached,
             "speedup": (plain["seconds_to_target"] / cached["seconds_to_target"])
             if plain["seconds_to_target"] and cached["seconds_to_target"] else None,
+            "speedup_by_rmse": {k: (round(plain["seconds_to_rmse"][k] / v, 2) if v and plain["seconds_to_rmse"][k] else None)
+                                for k, v in cached["seconds_to_rmse"].items()},
             "wall_s": round(time.time() - t0, 1)}
     print(json.dumps(line))
     ctx.close()
