@@ -182,6 +182,23 @@ int lts_write_image(const char* path, const float* rgb, int32_t width, int32_t h
 int lts_debug_trace_sample(lts_ctx* ctx, int64_t crop_sample_index);
 int lts_debug_trace_get(lts_ctx* ctx, float* out_64x16);
 
+/* Batched views (no counterpart in the reference: it renders the one camera of its scene file).
+ * Camera records like the scene file's (from, at, up, vertical field of view in degrees, focus
+ * distance), each with its own film size, samples per pixel and seed.  lts_render_views renders
+ * all of them in batched wavefront launches that share the scene, its BVH and (when on) the
+ * radiance cache: small views fill the GPU together.  desc gives max_bounce, rr_start and
+ * bvh_mode (its integrator must be LTS_INTEGRATOR_WAVEFRONT; spp, seed and crop are ignored).
+ * films_rgb[v] (host, width*height*3 floats) receives view v's resolved image like lts_render's
+ * film_rgb; out (may be NULL) gets the total device time and ray counts. */
+typedef struct {
+    float from[3], at[3], up[3];
+    float vfov, focus;
+    int32_t width, height, spp;
+    uint32_t seed;
+} lts_view;
+int lts_render_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts_render_desc* desc,
+                     float* const* films_rgb, lts_render_out* out);
+
 /* Tuning knobs of the renderer (no counterpart in the reference).  Keys:
  *   "radiance_cache"          1: wavefront paths end at the vertex after their first rough vertex
  *                             (roughness > 0.3) with the MLP's radiance there; a share of paths is

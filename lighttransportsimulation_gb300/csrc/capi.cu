@@ -378,6 +378,28 @@ int lts_render(lts_ctx* ctx, const lts_render_desc* desc, lts_render_out* out) {
     return LTS_OK;
 }
 
+int lts_render_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts_render_desc* desc,
+                     float* const* films_rgb, lts_render_out* out) {
+    if (!ctx || !desc || !views || !films_rgb || n <= 0) return fail(ctx, LTS_ERR_ARG, "null argument");
+    if (ctx->device == -1) return fail(ctx, LTS_ERR_STATE, "host-only context (device -1) cannot run kernels");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    CK(cudaSetDevice(ctx->device));
+    const int mode = desc->bvh_mode == LTS_BVH_REFERENCE ? LTS_BVH_REFERENCE : LTS_BVH_SORTED;
+    if (!(ctx->bvh_is_scene && ctx->bvh_mode == mode)) {
+        int rc = lts_bvh_build(ctx, mode, nullptr);
+        if (rc) return rc;
+    }
+    std::string e = ctx->tracer->render_views(ctx->scene, *ctx->bvh, views, n, *desc, films_rgb, out, ctx->stream,
+                                              ctx->d_error);
+    if (!e.empty()) return fail(ctx, e.find("argument") != std::string::npos ? LTS_ERR_ARG : LTS_ERR_CUDA, e);
+    int rc = check_device_error(ctx);
+    if (rc) return rc;
+    ctx->metrics.render_ms = ctx->tracer->last_ms;
+    ctx->metrics.paths = ctx->tracer->last_paths;
+    ctx->metrics.rays = ctx->tracer->last_rays;
+    return LTS_OK;
+}
+
 int lts_render_async(lts_ctx* ctx, const lts_render_desc* desc) {
     if (!ctx || !desc) return fail(ctx, LTS_ERR_ARG, "null argument");
     if (ctx->device == -1) return fail(ctx, LTS_ERR_STATE, "host-only context (device -1) cannot run kernels");

@@ -199,6 +199,26 @@ HostTexture read_texture(Tokens& s, bool scene_stream, int subject_images) {
 
 }  // namespace
 
+// Camera (rendering/Camera.cu:9-43) with aperture 0 (LightTransportSimulation.cu:70) from the
+// scene file's camera record cf = from(3), at(3), up(3), vfov (degrees), focus distance.
+void build_camera(const float cf[11], int width, int height, float cam[23]) {
+    const V3 from{cf[0], cf[1], cf[2]}, at{cf[3], cf[4], cf[5]}, vup{cf[6], cf[7], cf[8]};
+    const float vfov = cf[9], focus = cf[10];
+    const float aspect = (float)width / (float)height;
+    const float theta = (float)((double)vfov * kPi / 180.0f);
+    const float h = tanf(theta / 2);
+    const float vh = 2 * h, vw = aspect * vh;
+    const V3 w = normalize_q(sub(from, at));
+    const V3 u = normalize_q(cross_d(vup, w));
+    const V3 v = cross_d(w, u);
+    const V3 right = scale(u, focus * vw), up = scale(v, focus * vh);
+    const V3 llc = sub(sub(sub(from, scale(right, 0.5f)), scale(up, 0.5f)), scale(w, focus));
+    const float camv[23] = {from.x, from.y, from.z, right.x, right.y, right.z, up.x, up.y, up.z,
+                            llc.x,  llc.y,  llc.z,  u.x,     u.y,     u.z,     v.x,  v.y,  v.z,
+                            w.x,    w.y,    w.z,    0.0f / 2, focus};
+    memcpy(cam, camv, sizeof camv);
+}
+
 // geometry/Geometry.cuh:15-29 with the 32-bit integer read of the Windows (LLP64) build.
 float quake_rsqrt(float f) {
     const float threehalfs = 1.5f;
@@ -448,23 +468,7 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
         // Camera (rendering/Camera.cu:9-43), aperture 0 (LightTransportSimulation.cu:70).
         sc->width = width;
         sc->height = height;
-        {
-            const V3 from{cf[0], cf[1], cf[2]}, at{cf[3], cf[4], cf[5]}, vup{cf[6], cf[7], cf[8]};
-            const float vfov = cf[9], focus = cf[10];
-            const float aspect = (float)width / (float)height;
-            const float theta = (float)((double)vfov * kPi / 180.0f);
-            const float h = tanf(theta / 2);
-            const float vh = 2 * h, vw = aspect * vh;
-            const V3 w = normalize_q(sub(from, at));
-            const V3 u = normalize_q(cross_d(vup, w));
-            const V3 v = cross_d(w, u);
-            const V3 right = scale(u, focus * vw), up = scale(v, focus * vh);
-            const V3 llc = sub(sub(sub(from, scale(right, 0.5f)), scale(up, 0.5f)), scale(w, focus));
-            const float camv[23] = {from.x, from.y, from.z, right.x, right.y, right.z, up.x, up.y, up.z,
-                                    llc.x,  llc.y,  llc.z,  u.x,     u.y,     u.z,     v.x,  v.y,  v.z,
-                                    w.x,    w.y,    w.z,    0.0f / 2, focus};
-            memcpy(sc->cam, camv, sizeof camv);
-        }
+        build_camera(cf, width, height, sc->cam);
         // Gaussian filter table (Filter.cuh:32-50,82-99): radius (1,1), alpha 1.
         {
             const float alpha = 1.0f, rx = 1.0f, ry = 1.0f;

@@ -86,4 +86,8 @@ std::string load_scene(const std::string& root, const std::string& scene, const 
 // Reference float helpers shared by loader code paths (host, no FMA contraction).
 float quake_rsqrt(float f);
 
+// The reference camera (rendering/Camera.cu:9-43, aperture 0) from a camera record
+// cf = from(3), at(3), up(3), vfov in degrees, focus distance: cam[23] as HostScene::cam.
+void build_camera(const float cf[11], int width, int height, float cam[23]);
+
 }  // namespace lts

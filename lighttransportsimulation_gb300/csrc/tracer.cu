@@ -115,6 +115,9 @@ void Tracer::free_all() {
     rgb_ = nullptr;
     dev_free(trace_);
     trace_ = nullptr;
+    dev_free(views_film_);
+    views_film_ = nullptr;
+    views_film_cap_ = 0;
     for (void*& p : wf_bufs_) {
         if (p) dev_free(p);
         p = nullptr;
@@ -377,20 +380,53 @@ std::string Tracer::render_async(const HostScene& sc, const Lbvh& bvh, const lts
 std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                                      uint32_t* d_err, const RenderParams& rp, const SceneView& sv, long total) {
     (void)sc;
-    (void)d_err;
     (void)total;
     // Samples per pixel are rendered in chunks whose finished samples fit the sample buffer; the
-    // path pool drains at the end of each chunk and the chunk is gathered into the film.
+    // path pool drains at the end of each chunk and the chunk is gathered into the film.  Each
+    // chunk is a batch of one view slice.
     const long npix = (long)(rp.x1 - rp.x0) * (rp.y1 - rp.y0);
     const long cap = wf_sample_cap > 0 ? wf_sample_cap : (1l << 27);
     const int chunk = (int)std::max<long>(1, std::min<long>(d.spp, cap / npix));
-    const long chunk_total = npix * chunk;
-    if (chunk_total >= (1l << 31)) return "wavefront: crop too large for one sample chunk";
+    if (npix * chunk >= (1l << 31)) return "wavefront: crop too large for one sample chunk";
+    std::vector<std::vector<WfView>> batches;
+    for (int s0 = 0; s0 < d.spp; s0 += chunk) {
+        WfView v{};
+        for (int k = 0; k < 12; ++k) v.cam[k] = sv.cam[k];
+        v.W = sv.width;
+        v.H = sv.height;
+        v.x0 = rp.x0; v.y0 = rp.y0; v.x1 = rp.x1; v.y1 = rp.y1;
+        v.spp = d.spp;
+        v.s_first = s0;
+        v.nsc = std::min(chunk, d.spp - s0);
+        v.seed = rp.seed;
+        v.spp_scale = rp.spp_scale;
+        v.base = 0;
+        v.npix = npix;
+        v.film_off = 0;
+        batches.push_back({v});
+    }
+    return run_wavefront(batches, bvh, s, d_err, rp, sv);
+}
+
+// The wavefront loop over batches of view slices (see WfView): per batch, the path pool runs
+// until it drains, then every slice is gathered into its view's film.
+std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batches, const Lbvh& bvh, cudaStream_t s,
+                                  uint32_t* d_err, const RenderParams& rp, const SceneView& sv) {
+    (void)d_err;
+    long batch_max = 1;
+    for (const auto& bt : batches) {
+        long t = 0;
+        for (const WfView& v : bt) t += v.npix * v.nsc;
+        batch_max = std::max(batch_max, t);
+        if (bt.size() > (size_t)kMaxViews) return "wavefront: too many views in one batch";
+    }
+    if (batch_max >= (1l << 31)) return "wavefront: batch too large";
+    const long chunk_total = batch_max;
     const long P = std::max<long>(1, std::min<long>(chunk_total, wf_pool > 0 ? wf_pool : (1l << 21)));
     WfState st{};
     if (wf_cap_ < P) {
         for (int k : {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26,
-                      27, 28, 29, 30, 31, 32, 35}) {
+                      27, 28, 29, 30, 31, 32, 35, 45}) {
             if (wf_bufs_[k]) dev_free(wf_bufs_[k]);
             wf_bufs_[k] = nullptr;
         }
@@ -403,6 +439,7 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
                                 4 * n};                                                           // wid
         for (size_t k = 0; k < sizeof sizes / sizeof sizes[0]; ++k) TRY(dev_alloc(&wf_bufs_[k], sizes[k]));
         TRY(dev_alloc(&wf_bufs_[35], 4 * (size_t)kShadeClasses * n));  // class-grouped shade lists
+        TRY(dev_alloc(&wf_bufs_[45], 4 * n));                             // view slice of each path
         wf_cap_ = P;
     }
     if (wf_fs_cap_ < chunk_total) {
@@ -428,6 +465,9 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
     st.q_free = (int32_t*)b[30]; st.counts = (uint32_t*)b[31]; st.wid = (int32_t*)b[32];
     st.fs_L = (float4*)b[33]; st.fs_y = (float*)b[34];
     st.q_cls = (int32_t*)b[35];
+    st.view = (int32_t*)b[45];
+    if (!wf_bufs_[46]) TRY(dev_alloc(&wf_bufs_[46], sizeof(WfView) * kMaxViews));
+    st.views = (const WfView*)b[46];
     // radiance cache buffers (allocated on first use with the cache on)
     const bool cache = cache_mode != 0 && mlp != nullptr && mlp->ready();
     st.cache = cache ? 1 : 0;
@@ -482,9 +522,15 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
     const unsigned tb = wf_trace_blocks_[wide ? 0 : 1];
     const unsigned cgrid = (unsigned)((P + kCompactTile - 1) / kCompactTile);
     const dim3 gblock(32, 4);
-    for (int s0 = 0; s0 < d.spp; s0 += chunk) {
-        const int nsc = std::min(chunk, d.spp - s0);
-        const long ctot = npix * nsc;
+    for (const auto& batch : batches) {
+        std::vector<WfView> vv = batch;
+        long ctot = 0;
+        for (WfView& v : vv) {
+            v.base = ctot;
+            ctot += v.npix * v.nsc;
+        }
+        st.nviews = (int)vv.size();
+        TRY(cudaMemcpyAsync(wf_bufs_[46], vv.data(), sizeof(WfView) * vv.size(), cudaMemcpyHostToDevice, s));
         long generated = 0;
         uint32_t nfree = (uint32_t)P, n_cont = 0, n_fin = 0, n_sh = 0, n_mis = 0, n_query = 0;
         int32_t *q_ext = st.q_a, *q_fin = st.q_b;
@@ -496,7 +542,7 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
             TRY(cudaMemsetAsync(st.counts, 0, 128, s));  // per-iteration counters (words 0..31)
             TRY(cudaEventRecord(wf_ev_[0], s));
             if (take) {
-                k_wf_generate<<<blocks(take), kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_cont, generated, take, s0, npix);
+                k_wf_generate<<<blocks(take), kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_cont, generated, take);
                 ++launches;
             }
             TRY(cudaEventRecord(wf_ev_[1], s));
@@ -550,11 +596,13 @@ std::string Tracer::render_wavefront(const HostScene& sc, const Lbvh& bvh, const
         }
         if (nfree != (uint32_t)P) return "wavefront: path pool did not drain";
         TRY(cudaEventRecord(wf_ev_[0], s));
-        const dim3 ggrid((unsigned)((std::min(rp.x1 + 2, sv.width) - rp.x0 + 31) / 32),
-                         (unsigned)((std::min(rp.y1 + 2, sv.height) - rp.y0 + 3) / 4));
-        k_film_gather<<<ggrid, gblock, 0, s>>>(sv, rp, st.fs_L, st.fs_y, nsc, npix);
+        for (const WfView& v : vv) {
+            const dim3 ggrid((unsigned)((std::min(v.x1 + 2, v.W) - v.x0 + 31) / 32),
+                             (unsigned)((std::min(v.y1 + 2, v.H) - v.y0 + 3) / 4));
+            k_film_gather<<<ggrid, gblock, 0, s>>>(sv, rp.film, v, st.fs_L, st.fs_y);
+            ++launches;
+        }
         TRY(cudaEventRecord(wf_ev_[6], s));
-        ++launches;
         TRY(cudaGetLastError());
         TRY(cudaEventSynchronize(wf_ev_[6]));
         float ms = 0;
@@ -664,6 +712,116 @@ std::string Tracer::film_get(const HostScene& sc, float* rgb, double* sums, cuda
     }
     if (sums) TRY(cudaMemcpyAsync(sums, film_, 32 * (size_t)W * H, cudaMemcpyDeviceToHost, s));
     TRY(cudaStreamSynchronize(s));
+    return "";
+}
+
+
+std::string Tracer::render_views(const HostScene& sc, const Lbvh& bvh, const lts_view* views, int n,
+                                 const lts_render_desc& d, float* const* films, lts_render_out* out, cudaStream_t s,
+                                 uint32_t* d_err) {
+    if (n <= 0 || !views || !films) return "bad argument: no views";
+    if (d.integrator != LTS_INTEGRATOR_WAVEFRONT) return "bad argument: batched views need the wavefront integrator";
+    lts_render_desc d0 = d;  // scene-wide set-up (BVH views, counters) through the one-view path
+    d0.spp = 1;
+    d0.x0 = d0.y0 = d0.x1 = d0.y1 = 0;
+    d0.record_samples = 0;
+    RenderParams rp;
+    SceneView sv;
+    long ns = 0;
+    std::string e = prepare(sc, bvh, d0, s, d_err, &rp, &sv, &ns);
+    if (!e.empty()) return e;
+    // the views' films, one after another
+    std::vector<WfView> slices;
+    long pixels = 0, paths = 0, max_pix = 0;
+    const long cap = wf_sample_cap > 0 ? wf_sample_cap : (1l << 27);
+    for (int v = 0; v < n; ++v) {
+        const lts_view& lv = views[v];
+        if (lv.width < 2 || lv.height < 2 || lv.spp < 1) return "bad argument: view size or spp";
+        const long npix = (long)lv.width * lv.height;
+        if (npix > cap) return "bad argument: view larger than the sample buffer";
+        WfView w{};
+        const float cf[11] = {lv.from[0], lv.from[1], lv.from[2], lv.at[0], lv.at[1], lv.at[2],
+                              lv.up[0],   lv.up[1],   lv.up[2],   lv.vfov,  lv.focus};
+        float cam[23];
+        build_camera(cf, lv.width, lv.height, cam);
+        for (int k = 0; k < 12; ++k) w.cam[k] = cam[k];
+        w.W = lv.width;
+        w.H = lv.height;
+        w.x0 = w.y0 = 0;
+        w.x1 = lv.width;
+        w.y1 = lv.height;
+        w.spp = lv.spp;
+        w.seed = lv.seed;
+        w.spp_scale = quake_host((float)lv.spp);
+        w.npix = npix;
+        w.film_off = pixels;
+        const int chunk = (int)std::max<long>(1, std::min<long>(lv.spp, cap / npix));
+        for (int s0 = 0; s0 < lv.spp; s0 += chunk) {
+            w.s_first = s0;
+            w.nsc = std::min(chunk, lv.spp - s0);
+            slices.push_back(w);
+        }
+        pixels += npix;
+        paths += npix * lv.spp;
+        max_pix = std::max(max_pix, npix);
+    }
+    // greedy batches of whole slices within the sample buffer
+    std::vector<std::vector<WfView>> batches(1);
+    long acc = 0;
+    for (const WfView& w : slices) {
+        const long t = w.npix * w.nsc;
+        if (!batches.back().empty() && (acc + t > cap || (int)batches.back().size() >= kMaxViews)) {
+            batches.emplace_back();
+            acc = 0;
+        }
+        batches.back().push_back(w);
+        acc += t;
+    }
+    if ((size_t)pixels * 32 > views_film_cap_) {
+        dev_free(views_film_);
+        views_film_ = nullptr;
+        views_film_cap_ = 0;
+        TRY(dev_alloc((void**)&views_film_, (size_t)pixels * 32));
+        views_film_cap_ = (size_t)pixels * 32;
+    }
+    if (!film_accumulate) TRY(cudaMemsetAsync(views_film_, 0, (size_t)pixels * 32, s));
+    rp.film = views_film_;
+    last_paths = (double)paths;
+    e = run_wavefront(batches, bvh, s, d_err, rp, sv);
+    if (!e.empty()) return e;
+    TRY(cudaStreamSynchronize(s));
+    float ms = 0;
+    TRY(cudaEventElapsedTime(&ms, ev0_, ev1_));
+    last_ms = ms;
+    unsigned long long cnt[12] = {0};
+    TRY(cudaMemcpy(cnt, counters_, sizeof cnt, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 9; ++k) last_kind_work[k] = (double)cnt[3 + k];
+    last_rays = (double)cnt[0];
+    last_node_visits = (double)cnt[1];
+    last_tri_tests = (double)cnt[2];
+    // resolve each view
+    float* rgb = nullptr;
+    TRY(dev_alloc((void**)&rgb, 12 * (size_t)max_pix));
+    long off = 0;
+    for (int v = 0; v < n; ++v) {
+        const int W = views[v].width, H = views[v].height;
+        k_resolve<<<(W * H + 255) / 256, 256, 0, s>>>(views_film_ + 4 * off, rgb, W, H);
+        cudaError_t c = cudaGetLastError();
+        if (c == cudaSuccess && films[v]) c = cudaMemcpyAsync(films[v], rgb, 12 * (size_t)W * H, cudaMemcpyDeviceToHost, s);
+        if (c == cudaSuccess) c = cudaStreamSynchronize(s);
+        if (c != cudaSuccess) {
+            dev_free(rgb);
+            return std::string("resolve views: ") + cudaGetErrorString(c);
+        }
+        off += (long)W * H;
+    }
+    dev_free(rgb);
+    if (out) {
+        out->render_ms = ms;
+        out->rays = last_rays;
+        out->node_visits = last_node_visits;
+        out->tri_tests = last_tri_tests;
+    }
     return "";
 }
 

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/lts_capi.h"
 #include "host_scene.hpp"
@@ -67,6 +68,21 @@ struct RenderParams {
     long trace_sample;               // crop sample index traced (-1: none)
 };
 
+// One slice of a batched wavefront render: samples s_first .. s_first + nsc - 1 per pixel of a
+// view's crop.  Batch sample index w in [base, base + nsc * npix) maps to sample
+// s_first + (w - base) / npix of crop pixel (w - base) % npix (sample-major).  Plain data shared
+// by the host and the kernels.
+constexpr int kMaxViews = 256;  // view slices per wavefront batch
+struct WfView {
+    float cam[12];                 // origin, right, up, lower-left corner (HostScene::cam[0..11])
+    int32_t W, H, x0, y0, x1, y1;  // film size and crop
+    int32_t spp, s_first, nsc;     // the view's samples per pixel; the slice's first sample and count
+    uint32_t seed;
+    float spp_scale;               // quake_rsqrt(spp) for ray differentials
+    int32_t pad;
+    int64_t base, npix, film_off;  // first batch sample index; crop pixels; first film pixel
+};
+
 // The procedural textures' tables (host copies): the 512-entry Perlin permutation and the
 // 10 x 3 marble colours; each translation unit with device textures uploads its own.
 void texture_tables(unsigned char perm512[512], const float** marble30);
@@ -87,6 +103,10 @@ class Tracer {
     std::string render_async(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                              uint32_t* d_err);
     std::string film_get(const HostScene& sc, float* rgb, double* sums, cudaStream_t s);
+    // Batched views (lts_render_views): every view's full frame through the wavefront loop.
+    std::string render_views(const HostScene& sc, const Lbvh& bvh, const lts_view* views, int n,
+                             const lts_render_desc& d, float* const* films, lts_render_out* out, cudaStream_t s,
+                             uint32_t* d_err);
 
     double last_ms = 0, last_paths = 0, last_rays = 0, last_node_visits = 0, last_tri_tests = 0;
     // Path-pool capacity of the wavefront integrator (0: automatic).
@@ -125,6 +145,8 @@ class Tracer {
     void free_all();
     std::string render_wavefront(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                                  uint32_t* d_err, const RenderParams& rp, const SceneView& sv, long total);
+    std::string run_wavefront(const std::vector<std::vector<WfView>>& batches, const Lbvh& bvh, cudaStream_t s,
+                              uint32_t* d_err, const RenderParams& rp, const SceneView& sv);
     void* wf_bufs_[48] = {nullptr};
     long wf_cache_cap_ = 0, wf_train_cap_ = 0;
     std::string train_cache(uint32_t* d_counts, uint16_t* tr_feat, float* tr_target, uint32_t tr_cap, cudaStream_t s,
@@ -140,6 +162,8 @@ class Tracer {
     int leaf_n_ = 0;
     uint64_t leaf_serial_ = 0;  // Lbvh::serial the leaf_v_ copy was gathered for
     double* film_ = nullptr;
+    double* views_film_ = nullptr;
+    size_t views_film_cap_ = 0;
     size_t film_cap_ = 0;
     float* rec_L_ = nullptr;
     uint64_t* rec_sig_ = nullptr;

@@ -34,7 +34,10 @@ constexpr int kWfBlock = 128;
 constexpr uint64_t kSigBasis = 0xcbf29ce484222325ull;
 
 struct WfState {
-    int32_t *pix, *smp, *wid;  // pixel, sample, index of the sample within its chunk
+    int32_t *pix, *smp, *wid;  // pixel (within its view's film), sample, index within the batch
+    int32_t* view;             // slice of the batch the path belongs to
+    const WfView* views;       // the batch's slices
+    int nviews;
     uint32_t *draw, *flags, *pend, *vis;
     float4 *ro, *rd, *beta, *L;
     float2* pf;
@@ -129,12 +132,12 @@ __device__ __forceinline__ void rng_resume(Rng& r) {
     }
 }
 
-__device__ __forceinline__ void camera_ray(const SceneView& sv, float pfx, float pfy, V3& rd, V3& rxd, V3& ryd,
-                                           float spp_scale) {
-    const float* cam = sv.cam;
+__device__ __forceinline__ void camera_ray(const WfView& vw, float pfx, float pfy, V3& rd, V3& rxd, V3& ryd) {
+    const float* cam = vw.cam;
+    const float spp_scale = vw.spp_scale;
     const V3 co = v3(cam[0], cam[1], cam[2]), cright = v3(cam[3], cam[4], cam[5]), cup = v3(cam[6], cam[7], cam[8]),
              cllc = v3(cam[9], cam[10], cam[11]);
-    const float rx = (float)(sv.width - 1), ry = (float)(sv.height - 1);
+    const float rx = (float)(vw.W - 1), ry = (float)(vw.H - 1);
     rd = normalize(cllc + cright * (pfx / rx) + cup * (pfy / ry) - co);
     const V3 dx0 = normalize(cllc + cright * ((pfx + 1) / rx) + cup * (pfy / ry) - co);
     const V3 dy0 = normalize(cllc + cright * (pfx / rx) + cup * ((pfy + 1) / ry) - co);
@@ -142,30 +145,33 @@ __device__ __forceinline__ void camera_ray(const SceneView& sv, float pfx, float
     ryd = rd + (dy0 - rd) * spp_scale;
 }
 
-// generate: starts samples gen0 .. gen0 + take - 1 of the chunk (sample-major over the crop's
-// pixels: w = (s - s0) * npix + pixel) in the first `take` free slots, appending them to the
-// path-ray list after its `n_cont` continuing paths.
+// generate: starts batch samples gen0 .. gen0 + take - 1 in the first `take` free slots,
+// appending them to the path-ray list after its `n_cont` continuing paths.
 __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, const RenderParams rp, WfState st,
-                                                          int32_t* q_ext, uint32_t n_cont, long gen0, uint32_t take,
-                                                          int s0, long npix) {
+                                                          int32_t* q_ext, uint32_t n_cont, long gen0, uint32_t take) {
     const long t = (long)blockIdx.x * kWfBlock + threadIdx.x;
     if (t >= (long)take) return;
     const long w = gen0 + t;
     const int slot = st.q_free[t];
-    const int cw = rp.x1 - rp.x0;
-    const int s = s0 + (int)(w / npix);
-    const long pc = w % npix;
-    const int i = rp.x0 + (int)(pc % cw), j = rp.y0 + (int)(pc / cw);
-    const int id = j * sv.width + i;
+    int v = 0;
+    while (v + 1 < st.nviews && st.views[v + 1].base <= w) ++v;
+    const WfView& vw = st.views[v];
+    const long local = w - vw.base;
+    const int cw = vw.x1 - vw.x0;
+    const int s = vw.s_first + (int)(local / vw.npix);
+    const long pc = local % vw.npix;
+    const int i = vw.x0 + (int)(pc % cw), j = vw.y0 + (int)(pc / cw);
+    const int id = j * vw.W + i;
     Rng rng;
-    rng.key = rp.seed + wang_hash((uint32_t)id);
+    rng.key = vw.seed + wang_hash((uint32_t)id);
     rng.sample = (uint32_t)s;
     rng.draw = 0;
     const F2 fs = rng_2d(rng);
     (void)rng_2d(rng);
     const float pfx = (float)(i + fs.x), pfy = (float)(j + fs.y);
     V3 rd, rxd, ryd;
-    camera_ray(sv, pfx, pfy, rd, rxd, ryd, rp.spp_scale);
+    camera_ray(vw, pfx, pfy, rd, rxd, ryd);
+    st.view[slot] = v;
     st.pix[slot] = id;
     st.smp[slot] = s;
     st.wid[slot] = (int32_t)w;
@@ -174,7 +180,7 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, co
                          ? FL_UNBIASED : 0u;
     st.pend[slot] = 0u;
     st.pf[slot] = make_float2(pfx, pfy);
-    st.ro[slot] = make_float4(sv.cam[0], sv.cam[1], sv.cam[2], 0.f);
+    st.ro[slot] = make_float4(vw.cam[0], vw.cam[1], vw.cam[2], 0.f);
     st.rd[slot] = make_float4(rd.x, rd.y, rd.z, 0.f);
     st.beta[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
     st.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -421,7 +427,8 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
         }
     }
     Rng rng;
-    rng.key = rp.seed + wang_hash((uint32_t)st.pix[p]);
+    const WfView& vw = st.views[st.view[p]];
+    rng.key = vw.seed + wang_hash((uint32_t)st.pix[p]);
     rng.sample = (uint32_t)st.smp[p];
     rng.draw = st.draw[p];
     rng_resume(rng);
@@ -431,7 +438,7 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
         if (bounce == 0) {  // camera-ray differentials (Interaction.cuh:118-160)
             const float2 pf = st.pf[p];
             V3 rd0, rxd, ryd;
-            camera_ray(sv, pf.x, pf.y, rd0, rxd, ryd, rp.spp_scale);
+            camera_ray(vw, pf.x, pf.y, rd0, rxd, ryd);
             const V3 n = si.n;
             const float dd = -dot(n, si.p);
             const float tx = (-dot(n, ro) - dd) / dot(n, rxd);
@@ -643,8 +650,10 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
     // the column i - 1 (row j - 1) when pf rounds to exactly i (j), added here.
     const float2 pf = st.pf[p];
     const int id = st.pix[p];
-    const int W = sv.width, H = sv.height;
+    const WfView& vw = st.views[st.view[p]];
+    const int W = vw.W, H = vw.H;
     const int i = id % W, j = id / W;
+    double* const film = rp.film + 4 * (size_t)vw.film_off;
     const int px0 = max((int)ceilf(pf.x - 1.0f), 0), py0 = max((int)ceilf(pf.y - 1.0f), 0);
     if (px0 < i || py0 < j) {
         const int px1 = min((int)floorf(pf.x + 1.0f) + 1, W), py1 = min((int)floorf(pf.y + 1.0f) + 1, H);
@@ -656,7 +665,7 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
                 const int ix = min((int)floorf(fdx), 15), iy = min((int)floorf(fdy), 15);
                 const float wgt = __ldg(sv.filter + iy * 16 + ix);
                 const Spec c = L * wgt;
-                double* fp = rp.film + 4 * ((size_t)y * W + x);
+                double* fp = film + 4 * ((size_t)y * W + x);
                 atomicAdd(fp + 0, (double)c.r);
                 atomicAdd(fp + 1, (double)c.g);
                 atomicAdd(fp + 2, (double)c.b);
@@ -667,7 +676,7 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
     st.fs_L[w] = make_float4(L.r, L.g, L.b, pf.x);
     st.fs_y[w] = pf.y;
     if (RECORD) {
-        const size_t k = ((size_t)(j - rp.y0) * (rp.x1 - rp.x0) + (i - rp.x0)) * rp.spp + st.smp[p];
+        const size_t k = ((size_t)(j - vw.y0) * (vw.x1 - vw.x0) + (i - vw.x0)) * vw.spp + st.smp[p];
         rp.sample_L[3 * k + 0] = L.r;
         rp.sample_L[3 * k + 1] = L.g;
         rp.sample_L[3 * k + 2] = L.b;
@@ -757,24 +766,27 @@ __global__ __launch_bounds__(kCompactThreads) void k_wf_compact(WfState st, int3
 // filter footprint covers it from source pixels x - 2 .. x (y - 2 .. y): the pixels i .. i + 2
 // that k_wf_finalize left to this kernel.  Kahan-compensated FP32 per channel, then one
 // non-atomic FP64 add per channel (each film pixel has exactly one thread).
-__global__ __launch_bounds__(128) void k_film_gather(const SceneView sv, const RenderParams rp,
-                                                     const float4* __restrict__ fs_L, const float* __restrict__ fs_y,
-                                                     int nsc, long npix) {
+__global__ __launch_bounds__(128) void k_film_gather(const SceneView sv, double* __restrict__ film_all, const WfView vw,
+                                                     const float4* __restrict__ fs_L, const float* __restrict__ fs_y) {
     __shared__ float s_filter[256];
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     for (int k = tid; k < 256; k += blockDim.x * blockDim.y) s_filter[k] = sv.filter[k];
     __syncthreads();
-    const int W = sv.width, H = sv.height;
-    const int x = rp.x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int y = rp.y0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    if (x >= min(rp.x1 + 2, W) || y >= min(rp.y1 + 2, H)) return;
-    const int cw = rp.x1 - rp.x0;
+    const int W = vw.W, H = vw.H;
+    const int x = vw.x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = vw.y0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (x >= min(vw.x1 + 2, W) || y >= min(vw.y1 + 2, H)) return;
+    const int cw = vw.x1 - vw.x0;
+    const long npix = vw.npix;
+    const int nsc = vw.nsc;
+    fs_L += vw.base;
+    fs_y += vw.base;
     float sum[4] = {0, 0, 0, 0}, cmp[4] = {0, 0, 0, 0};
-    const int j0 = max(y - 2, rp.y0), j1 = min(y, rp.y1 - 1);
-    const int i0 = max(x - 2, rp.x0), i1 = min(x, rp.x1 - 1);
+    const int j0 = max(y - 2, vw.y0), j1 = min(y, vw.y1 - 1);
+    const int i0 = max(x - 2, vw.x0), i1 = min(x, vw.x1 - 1);
     for (int j = j0; j <= j1; ++j)
         for (int i = i0; i <= i1; ++i) {
-            const long pc = (long)(j - rp.y0) * cw + (i - rp.x0);
+            const long pc = (long)(j - vw.y0) * cw + (i - vw.x0);
             for (int s = 0; s < nsc; ++s) {
                 const long k = (long)s * npix + pc;
                 const float4 v = __ldg(fs_L + k);
@@ -796,7 +808,7 @@ __global__ __launch_bounds__(128) void k_film_gather(const SceneView sv, const R
             }
         }
     if (sum[3] == 0.f && cmp[3] == 0.f) return;
-    double* fp = rp.film + 4 * ((size_t)y * W + x);
+    double* fp = film_all + 4 * ((size_t)vw.film_off + (size_t)y * W + x);
 #pragma unroll
     for (int q = 0; q < 4; ++q) fp[q] += (double)sum[q] - (double)cmp[q];
 }
