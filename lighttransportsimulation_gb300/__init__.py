@@ -37,7 +37,7 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_bvh_build_device_async", "lts_bvh_dump_get", "lts_render", "lts_render_async", "lts_film_get",
            "lts_write_image", "lts_get_metrics", "lts_bvh_build_noalloc", "lts_debug_trace_sample",
            "lts_debug_trace_get", "lts_set_option", "lts_debug_umma_probe", "lts_mlp_init", "lts_mlp_set_params",
-           "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step"]
+           "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step", "lts_render_views"]
 
 
 class LtsError(RuntimeError):
@@ -126,6 +126,7 @@ def library():
             "lts_mlp_get_params": (I, [P, P]),
             "lts_mlp_forward": (I, [P, P, I, P]),
             "lts_mlp_train_step": (I, [P, P, P, I, ctypes.c_float, P, P]),
+            "lts_render_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P, ctypes.POINTER(RenderOut)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -350,3 +351,35 @@ class RadianceCacheMLP:
             self.ctx.h, f.ctypes.data_as(ctypes.c_void_p), t.ctypes.data_as(ctypes.c_void_p), f.shape[0],
             ctypes.c_float(lr), ctypes.byref(loss), g.ctypes.data_as(ctypes.c_void_p) if want_grad else None))
         return loss.value, g
+
+
+class View(ctypes.Structure):
+    """One camera of a batched render (lts_view): the scene file's camera record fields plus film
+    size, samples per pixel and seed."""
+    _fields_ = [("frm", ctypes.c_float * 3), ("at", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("vfov", ctypes.c_float), ("focus", ctypes.c_float), ("width", ctypes.c_int32),
+                ("height", ctypes.c_int32), ("spp", ctypes.c_int32), ("seed", ctypes.c_uint32)]
+
+
+def render_views(scene, views, max_bounce, rr_start, bvh_mode=1):
+    """Renders every view (dicts with frm, at, up, vfov, focus, width, height, spp, seed) of the
+    loaded scene in batched wavefront launches; returns ([H x W x 3 images, flipped like
+    lts_render's film], render_ms)."""
+    import numpy as np
+    ctx = scene.ctx
+    n = len(views)
+    arr = (View * n)()
+    for k, v in enumerate(views):
+        arr[k].frm[:] = v["frm"]
+        arr[k].at[:] = v["at"]
+        arr[k].up[:] = v.get("up", (0, 1, 0))
+        arr[k].vfov = v["vfov"]
+        arr[k].focus = v.get("focus", 1.0)
+        arr[k].width, arr[k].height, arr[k].spp, arr[k].seed = v["width"], v["height"], v["spp"], v["seed"]
+    films = [np.zeros(v["width"] * v["height"] * 3, np.float32) for v in views]
+    ptrs = (ctypes.c_void_p * n)(*[f.ctypes.data for f in films])
+    desc = RenderDesc()
+    desc.spp, desc.max_bounce, desc.rr_start, desc.integrator, desc.bvh_mode = 1, max_bounce, rr_start, 1, bvh_mode
+    out = RenderOut()
+    ctx.check(ctx.lib.lts_render_views(ctx.h, arr, n, ctypes.byref(desc), ptrs, ctypes.byref(out)))
+    return [f.reshape(v["height"], v["width"], 3) for f, v in zip(films, views)], out.render_ms
