@@ -281,9 +281,12 @@ def run_gpu(args, wl):
     ms = barrier_max(dist, ms)
     value = world * paths / (ms * 1e-3) / 1e6
 
-    # one counted render for the roofline's algorithmic bytes (same kernels, same launches)
+    # one counted render for the roofline's algorithmic bytes and the per-stage device times (the
+    # same kernels, launched one by one instead of as graphs so that each stage can be timed)
+    ctx.set_option("wavefront_graph", 0)
     r = integ.render(wl["spp"], wl["seed"], film=False)
     mr = ctx.metrics()
+    ctx.set_option("wavefront_graph", 1)
     stages = None
     if args.integrator == 0:
         kernel, kernel_ms, kernel_launches = "k_pathtrace", r["render_ms"], 1

@@ -210,6 +210,9 @@ int lts_render_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts_r
  *   "radiance_cache_train_steps"       Adam steps per render (default 4)
  *   "radiance_cache_lr_micro"          learning rate in 1e-6 (default 1000 = 1e-3)
  *   "film_accumulate"         1: renders add to the film's sums instead of clearing them
+ *   "wavefront_graph"         1 (default): each wavefront iteration runs as a captured CUDA graph,
+ *                             launched in groups with one host check per group; 0: kernel by
+ *                             kernel with host-sized grids and per-stage timing (lts_metrics)
  *   "bvh_width"               traversal structure: 8 (default) the 8-wide compressed BVH collapsed
  *                             from the LBVH, 2 the binary LBVH itself; both give the same hits
  *   "wavefront_pool"          path-state pool capacity in paths (0: automatic, 2^21)

@@ -564,6 +564,8 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
         ctx->tracer->cache_train_steps = (int)value;
     } else if (!strcmp(key, "radiance_cache_lr_micro")) {
         ctx->tracer->cache_lr = (float)value * 1e-6f;
+    } else if (!strcmp(key, "wavefront_graph")) {
+        ctx->tracer->wf_graph = value ? 1 : 0;
     } else if (!strcmp(key, "film_accumulate")) {
         ctx->tracer->film_accumulate = value != 0;
     } else if (!strcmp(key, "bvh_width")) {

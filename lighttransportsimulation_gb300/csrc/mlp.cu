@@ -205,8 +205,9 @@ __device__ __forceinline__ void load_feature_row(unsigned char* smem, const uint
 // Inference: out[r * stride + c] = exp(z_c), c < 3, for the feature rows r = rows[i] (rows null:
 // r = i), i < n.  Persistent CTAs of 128 threads, one row per thread.
 __global__ __launch_bounds__(128) void k_mlp_forward(const uint16_t* __restrict__ w16, const uint16_t* __restrict__ feat,
-                                                     const int32_t* __restrict__ rows, int n, float* __restrict__ out,
-                                                     int stride, uint32_t* err) {
+                                                     const int32_t* __restrict__ rows, int n, const uint32_t* d_n,
+                                                     float* __restrict__ out, int stride, uint32_t* err) {
+    if (d_n) n = min(n, (int)*d_n);  // a count produced on the device (at most n)
     extern __shared__ __align__(1024) unsigned char smem[];
     uint64_t* mbar = (uint64_t*)(smem + kFwdBar);
     uint32_t* tslot = (uint32_t*)(smem + kFwdBar + 16);
@@ -481,11 +482,12 @@ std::string Mlp::get_grad(float* host, cudaStream_t s) {
 }
 
 std::string Mlp::forward(const uint16_t* d_feat, int n, float* d_out, uint32_t* d_err, cudaStream_t s,
-                         const int32_t* d_rows, int out_stride) {
+                         const int32_t* d_rows, int out_stride, const uint32_t* d_n) {
     if (!w32_) return "MLP not initialised";
     if (n <= 0) return "";
     const int tiles = (n + 127) / 128;
-    k_mlp_forward<<<std::min(tiles, blocks_fwd_), 128, kFwdSmem, s>>>(w16_, d_feat, d_rows, n, d_out, out_stride, d_err);
+    k_mlp_forward<<<std::min(tiles, blocks_fwd_), 128, kFwdSmem, s>>>(w16_, d_feat, d_rows, n, d_n, d_out, out_stride,
+                                                                     d_err);
     TRY(cudaGetLastError());
     return "";
 }

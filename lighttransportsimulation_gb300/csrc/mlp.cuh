@@ -43,8 +43,9 @@ class Mlp {
 
     // out[r * out_stride + c] = network(features[r][96])_c for r = rows[i] (rows null: r = i),
     // i < n (device pointers; features are bf16 bits).
+    // d_n (device, may be null): the row count to use, at most n (the grid is sized for n).
     std::string forward(const uint16_t* d_feat, int n, float* d_out, uint32_t* d_err, cudaStream_t s,
-                        const int32_t* d_rows = nullptr, int out_stride = 3);
+                        const int32_t* d_rows = nullptr, int out_stride = 3, const uint32_t* d_n = nullptr);
     // Gradient of the relative L2 loss mean((pred - t)^2 / (pred^2 + 0.01)) over the n samples
     // into the gradient buffer (zeroed first), the loss into *d_loss (device), then, if lr > 0,
     // one Adam step (beta 0.9 / 0.99, eps 1e-8) that also zeroes the gradient.

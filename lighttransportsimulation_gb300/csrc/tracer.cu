@@ -155,6 +155,7 @@ void texture_tables(unsigned char perm512[512], const float** marble30) {
 Tracer::~Tracer() {
     free_all();
     if (wf_counts_host_) cudaFreeHost(wf_counts_host_);
+    if (wf_ctl_host_) cudaFreeHost(wf_ctl_host_);
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
     for (cudaEvent_t e : wf_ev_)
@@ -501,7 +502,8 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
     }
     auto blocks = [](long n) { return (unsigned)((n + kWfBlock - 1) / kWfBlock); };
     TRY(cudaEventRecord(ev0_, s));
-    k_wf_init_free<<<blocks(P), kWfBlock, 0, s>>>(st.q_free, st.pix, (int)P);  // every slot free
+    TRY(cudaMemsetAsync(st.counts, 0, 128, s));
+    k_wf_init_free<<<blocks(P), kWfBlock, 0, s>>>(st.q_free, st.pix, st.counts, (int)P);  // every slot free
     TRY(cudaMemsetAsync(st.counts + 32, 0, 4, s));  // training records of this render
     const bool rec = rp.sample_sig != nullptr;
     const bool wide = sv.wnodes != nullptr;
@@ -522,6 +524,75 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
     const unsigned tb = wf_trace_blocks_[wide ? 0 : 1];
     const unsigned cgrid = (unsigned)((P + kCompactTile - 1) / kCompactTile);
     const dim3 gblock(32, 4);
+    // control block (device) and its host mirror
+    if (!wf_bufs_[47]) TRY(dev_alloc(&wf_bufs_[47], sizeof(WfCtl)));
+    WfCtl* d_ctl = (WfCtl*)wf_bufs_[47];
+    if (!wf_ctl_host_) TRY(cudaMallocHost((void**)&wf_ctl_host_, sizeof(WfCtl)));
+    WfCtl* h_ctl = (WfCtl*)wf_ctl_host_;
+    // graph mode: one iteration captured twice (path-ray list in q_a or in q_b), launched in groups
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    auto free_graphs = [&]() {
+        for (cudaGraphExec_t& g : gexec)
+            if (g) cudaGraphExecDestroy(g);
+    };
+    auto launch_iteration = [&](int32_t* q_ext, int32_t* q_fin, bool full, uint32_t take, uint32_t n_ext,
+                                uint32_t n_fin, uint32_t nray, uint32_t n_query) -> std::string {
+        // full: grids for the largest lists (graph mode); else sized to the host's counts
+        k_wf_control<<<1, 32, 0, s>>>(st, d_ctl);
+        if (!full) TRY(cudaEventRecord(wf_ev_[0], s));
+        if (full || take) k_wf_generate<<<full ? blocks(P) : blocks(take), kWfBlock, 0, s>>>(sv, rp, st, q_ext, d_ctl);
+        if (!full) TRY(cudaEventRecord(wf_ev_[1], s));
+        if (full || nray) {
+            const unsigned g = full ? tb : std::min(blocks(nray), tb);
+            if (wide) k_wf_trace<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, d_ctl, st.counts + 8, bvh.n);
+            else k_wf_trace<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, d_ctl, st.counts + 8, bvh.n);
+        }
+        if (st.cache && (full || n_query)) {  // the previous shade's cache queries, before finalize adds them
+            const std::string me = mlp->forward(st.feat, full ? (int)P : (int)n_query, (float*)st.cache_L, rp.err, s,
+                                                st.q_cache, 4, &d_ctl->n_query);
+            if (!me.empty()) return me;
+        }
+        if (!full) TRY(cudaEventRecord(wf_ev_[2], s));
+        if (full || n_fin) {
+            const unsigned g = full ? blocks(P) : blocks(n_fin);
+            if (rec) k_wf_finalize<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_fin, d_ctl);
+            else k_wf_finalize<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_fin, d_ctl);
+        }
+        if (!full) TRY(cudaEventRecord(wf_ev_[3], s));
+        if (full || n_ext) {
+            const unsigned g = full ? blocks(P) : blocks(n_ext);
+            k_wf_classify<<<g, kWfBlock, 0, s>>>(sv, st, q_ext, d_ctl, (int)P);
+            if (rec) k_wf_shade<true><<<g + kShadeClasses, kWfBlock, 0, s>>>(sv, rp, st, (int)P);
+            else k_wf_shade<false><<<g + kShadeClasses, kWfBlock, 0, s>>>(sv, rp, st, (int)P);
+        }
+        if (!full) TRY(cudaEventRecord(wf_ev_[4], s));
+        k_wf_compact<<<cgrid, kCompactThreads, 0, s>>>(st, q_fin, (int)P);
+        if (!full) TRY(cudaEventRecord(wf_ev_[5], s));
+        TRY(cudaGetLastError());
+        return "";
+    };
+    const bool graph = wf_graph != 0;
+    if (graph) {
+        for (int k = 0; k < 2; ++k) {
+            cudaGraph_t g = nullptr;
+            TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            const std::string ce = launch_iteration(k ? st.q_b : st.q_a, k ? st.q_a : st.q_b, true, 0, 0, 0, 0, 0);
+            cudaGraph_t gg = nullptr;
+            const cudaError_t ee = cudaStreamEndCapture(s, &gg);
+            g = gg;
+            if (!ce.empty() || ee != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                free_graphs();
+                return ce.empty() ? std::string("graph capture: ") + cudaGetErrorString(ee) : ce;
+            }
+            const cudaError_t ie = cudaGraphInstantiate(&gexec[k], g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess) {
+                free_graphs();
+                return std::string("graph instantiate: ") + cudaGetErrorString(ie);
+            }
+        }
+    }
     for (const auto& batch : batches) {
         std::vector<WfView> vv = batch;
         long ctot = 0;
@@ -529,72 +600,66 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
             v.base = ctot;
             ctot += v.npix * v.nsc;
         }
-        st.nviews = (int)vv.size();
         TRY(cudaMemcpyAsync(wf_bufs_[46], vv.data(), sizeof(WfView) * vv.size(), cudaMemcpyHostToDevice, s));
-        long generated = 0;
-        uint32_t nfree = (uint32_t)P, n_cont = 0, n_fin = 0, n_sh = 0, n_mis = 0, n_query = 0;
-        int32_t *q_ext = st.q_a, *q_fin = st.q_b;
-        for (;; ++iters) {
-            const uint32_t take = (uint32_t)std::min<long>(nfree, ctot - generated);
-            const uint32_t n_ext = n_cont + take;
-            if (n_ext == 0 && n_fin == 0) break;
-            if (iters > 1000000) return "wavefront did not converge";
-            TRY(cudaMemsetAsync(st.counts, 0, 128, s));  // per-iteration counters (words 0..31)
-            TRY(cudaEventRecord(wf_ev_[0], s));
-            if (take) {
-                k_wf_generate<<<blocks(take), kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_cont, generated, take);
-                ++launches;
+        WfCtl c0{};
+        c0.ctot = ctot;
+        c0.nviews = (uint32_t)vv.size();
+        *h_ctl = c0;
+        TRY(cudaMemcpyAsync(d_ctl, h_ctl, sizeof(WfCtl), cudaMemcpyHostToDevice, s));
+        uint32_t nfree = (uint32_t)P;
+        if (graph) {
+            int par = 0, group = 4;
+            for (;;) {
+                for (int k = 0; k < group; ++k, par ^= 1) TRY(cudaGraphLaunch(gexec[par], s));
+                launches += group * (st.cache ? 8 : 7);
+                TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(WfCtl), cudaMemcpyDeviceToHost, s));
+                TRY(cudaStreamSynchronize(s));
+                if (!h_ctl->active) break;
+                if (h_ctl->iters > 1000000) {
+                    free_graphs();
+                    return "wavefront did not converge";
+                }
+                group = std::min(group * 2, 16);
             }
-            TRY(cudaEventRecord(wf_ev_[1], s));
-            const uint32_t nray = n_ext + n_sh + n_mis;
-            if (nray) {
-                const unsigned g = std::min(blocks(nray), tb);
-                if (wide) k_wf_trace<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_ext, n_sh, n_mis, st.counts + 8, bvh.n);
-                else k_wf_trace<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, n_ext, n_sh, n_mis, st.counts + 8, bvh.n);
-                ++launches;
-            }
-            if (n_query) {  // the previous shade's cache queries, before finalize adds them
-                const std::string me = mlp->forward(st.feat, (int)n_query, (float*)st.cache_L, rp.err, s, st.q_cache, 4);
-                if (!me.empty()) return me;
-                ++launches;
+            iters += (int)h_ctl->iters;
+            last_cache_queries += (double)h_ctl->queries;
+            nfree = h_ctl->nfree;
+        } else {
+            long generated = 0;
+            uint32_t n_cont = 0, n_fin = 0, n_sh = 0, n_mis = 0, n_query = 0;
+            int32_t *q_ext = st.q_a, *q_fin = st.q_b;
+            for (;; ++iters) {
+                const uint32_t take = (uint32_t)std::min<long>(nfree, ctot - generated);
+                const uint32_t n_ext = n_cont + take;
+                if (n_ext == 0 && n_fin == 0) break;
+                if (iters > 1000000) return "wavefront did not converge";
+                const std::string ie = launch_iteration(q_ext, q_fin, false, take, n_ext, n_fin, n_ext + n_sh + n_mis,
+                                                        n_query);
+                if (!ie.empty()) return ie;
+                launches += 7 + (n_query ? 1 : 0);
                 last_cache_queries += n_query;
+                TRY(cudaMemcpyAsync(wf_counts_host_, st.counts, 64, cudaMemcpyDeviceToHost, s));
+                TRY(cudaStreamSynchronize(s));
+                for (int k = 0; k < 5; ++k) {
+                    float ms = 0;
+                    TRY(cudaEventElapsedTime(&ms, wf_ev_[k], wf_ev_[k + 1]));
+                    last_stage_ms[k] += ms;
+                }
+                generated += take;
+                n_fin = n_ext;
+                n_cont = wf_counts_host_[0];
+                n_sh = wf_counts_host_[2];
+                n_mis = wf_counts_host_[3];
+                nfree = wf_counts_host_[4];
+                n_query = wf_counts_host_[12];
+                std::swap(q_ext, q_fin);
             }
-            TRY(cudaEventRecord(wf_ev_[2], s));
-            if (n_fin) {
-                if (rec) k_wf_finalize<true><<<blocks(n_fin), kWfBlock, 0, s>>>(sv, rp, st, q_fin, n_fin);
-                else k_wf_finalize<false><<<blocks(n_fin), kWfBlock, 0, s>>>(sv, rp, st, q_fin, n_fin);
-                ++launches;
-            }
-            TRY(cudaEventRecord(wf_ev_[3], s));
-            if (n_ext) {
-                k_wf_classify<<<blocks(n_ext), kWfBlock, 0, s>>>(sv, st, q_ext, n_ext, (int)P);
-                const unsigned g = blocks(n_ext) + kShadeClasses;
-                if (rec) k_wf_shade<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, (int)P);
-                else k_wf_shade<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, (int)P);
-                launches += 2;
-            }
-            TRY(cudaEventRecord(wf_ev_[4], s));
-            k_wf_compact<<<cgrid, kCompactThreads, 0, s>>>(st, q_fin, (int)P);
-            ++launches;
-            TRY(cudaEventRecord(wf_ev_[5], s));
-            TRY(cudaGetLastError());
-            TRY(cudaMemcpyAsync(wf_counts_host_, st.counts, 64, cudaMemcpyDeviceToHost, s));
-            TRY(cudaStreamSynchronize(s));
-            for (int k = 0; k < 5; ++k) {
-                float ms = 0;
-                TRY(cudaEventElapsedTime(&ms, wf_ev_[k], wf_ev_[k + 1]));
-                last_stage_ms[k] += ms;
-            }
-            generated += take;
-            n_fin = n_ext;
-            n_cont = wf_counts_host_[0];
-            n_sh = wf_counts_host_[2];
-            n_mis = wf_counts_host_[3];
-            nfree = wf_counts_host_[4];
-            n_query = wf_counts_host_[12];
-            std::swap(q_ext, q_fin);
+            // the last compaction left the counts of an empty pool; the control block follows them
         }
-        if (nfree != (uint32_t)P) return "wavefront: path pool did not drain";
+        if (nfree != (uint32_t)P) {
+            free_graphs();
+            return "wavefront: path pool did not drain";
+        }
         TRY(cudaEventRecord(wf_ev_[0], s));
         for (const WfView& v : vv) {
             const dim3 ggrid((unsigned)((std::min(v.x1 + 2, v.W) - v.x0 + 31) / 32),
@@ -609,6 +674,7 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
         TRY(cudaEventElapsedTime(&ms, wf_ev_[0], wf_ev_[6]));
         last_stage_ms[5] += ms;
     }
+    free_graphs();
     if (cache) {  // train the cache on this render's unbiased suffixes
         const std::string te = train_cache(st.counts, st.tr_feat, st.tr_target, st.tr_cap, s, rp.err);
         if (!te.empty()) return te;

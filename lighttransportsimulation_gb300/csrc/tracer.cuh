@@ -126,6 +126,9 @@ class Tracer {
     // Keep the film's sums across renders (progressive rendering) instead of clearing them.
     bool film_accumulate = false;
     bool last_wide = false;  // the last render traversed the wide BVH
+    // Wavefront iterations as CUDA graphs launched in groups (1), or launched one by one with
+    // host-sized grids and per-stage timing (0).
+    int wf_graph = 1;
     // Finished-sample buffer capacity of the wavefront film gather, in samples (0: 2^27).
     long wf_sample_cap = 0;
     int last_iterations = 0;
@@ -153,6 +156,7 @@ class Tracer {
                             uint32_t* d_err);
     long wf_cap_ = 0, wf_fs_cap_ = 0;
     uint32_t* wf_counts_host_ = nullptr;
+    void* wf_ctl_host_ = nullptr;  // pinned mirror of the wavefront control block
     cudaEvent_t wf_ev_[7] = {nullptr};
     unsigned wf_trace_blocks_[2] = {0, 0};  // resident blocks of k_wf_trace (wide, binary) on this device
     SceneView view_{};

@@ -36,8 +36,7 @@ constexpr uint64_t kSigBasis = 0xcbf29ce484222325ull;
 struct WfState {
     int32_t *pix, *smp, *wid;  // pixel (within its view's film), sample, index within the batch
     int32_t* view;             // slice of the batch the path belongs to
-    const WfView* views;       // the batch's slices
-    int nviews;
+    const WfView* views;       // the batch's slices (count in WfCtl::nviews)
     uint32_t *draw, *flags, *pend, *vis;
     float4 *ro, *rd, *beta, *L;
     float2* pf;
@@ -67,6 +66,14 @@ struct WfState {
     int32_t* tr_idx;        // its training record
     uint16_t* tr_feat;      // [tr_cap][96] training features (count in counts[32])
     float* tr_target;       // [tr_cap][3] training targets
+};
+
+// Per-iteration bookkeeping on the device (so an iteration can run as a CUDA graph): k_wf_control
+// turns the previous compaction's counts into this iteration's list sizes and new samples.
+struct WfCtl {
+    uint32_t take, n_cont, n_ext, n_fin, n_sh, n_mis, n_query, nfree, active, iters, nviews, pad;
+    long long gen0, generated, ctot;
+    unsigned long long queries;  // cache queries answered in the batch
 };
 
 // Radiance-cache features of a shading point (the layout oracle/mlp_np.py's encode states):
@@ -148,13 +155,15 @@ __device__ __forceinline__ void camera_ray(const WfView& vw, float pfx, float pf
 // generate: starts batch samples gen0 .. gen0 + take - 1 in the first `take` free slots,
 // appending them to the path-ray list after its `n_cont` continuing paths.
 __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, const RenderParams rp, WfState st,
-                                                          int32_t* q_ext, uint32_t n_cont, long gen0, uint32_t take) {
+                                                          int32_t* q_ext, const WfCtl* __restrict__ ctl) {
     const long t = (long)blockIdx.x * kWfBlock + threadIdx.x;
-    if (t >= (long)take) return;
-    const long w = gen0 + t;
+    if (t >= (long)ctl->take) return;
+    const long w = ctl->gen0 + t;
+    const uint32_t n_cont = ctl->n_cont;
+    const int nviews = (int)ctl->nviews;
     const int slot = st.q_free[t];
     int v = 0;
-    while (v + 1 < st.nviews && st.views[v + 1].base <= w) ++v;
+    while (v + 1 < nviews && st.views[v + 1].base <= w) ++v;
     const WfView& vw = st.views[v];
     const long local = w - vw.base;
     const int cw = vw.x1 - vw.x0;
@@ -272,10 +281,11 @@ constexpr int kTraceMinBlocks = LTS_TRACE_MIN_BLOCKS;
 // `fetch` is zeroed before the launch.  WIDE: the 8-wide compressed BVH, else the binary LBVH.
 template <bool WIDE>
 __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const SceneView sv, const RenderParams rp, WfState st,
-                                                       const int32_t* __restrict__ q_ext, uint32_t n_ext,
-                                                       uint32_t n_sh, uint32_t n_mis, uint32_t* fetch, int nleaf) {
+                                                       const int32_t* __restrict__ q_ext,
+                                                       const WfCtl* __restrict__ ctl, uint32_t* fetch, int nleaf) {
     __shared__ uint32_t s_stack[kStack * kWfBlock];
     uint32_t* stack = s_stack + threadIdx.x;
+    const uint32_t n_ext = ctl->n_ext, n_sh = ctl->n_sh, n_mis = ctl->n_mis;
     const uint32_t e1 = n_ext, e2 = n_ext + n_sh, n = n_ext + n_sh + n_mis;
     const unsigned lane = threadIdx.x & 31u;
     Trav t;
@@ -348,9 +358,9 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
 // classify: groups this iteration's paths by the shade class of what they hit (0: left the
 // scene), so that shade runs warps over one material kind at a time.
 __global__ __launch_bounds__(kWfBlock) void k_wf_classify(const SceneView sv, WfState st, const int32_t* __restrict__ q,
-                                                          uint32_t cnt, int pool) {
+                                                          const WfCtl* __restrict__ ctl, int pool) {
     const int t = blockIdx.x * kWfBlock + threadIdx.x;
-    if (t >= (int)cnt) return;
+    if (t >= (int)ctl->n_ext) return;
     const int p = q[t];
     const int prim = st.hprim[p];
     const int c = prim < 0 ? 0 : sv.mats[__ldg(&sv.prim_n[prim].w)].shade_class;
@@ -598,9 +608,9 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
 // sample and frees its slot (pix = -1).
 template <bool RECORD>
 __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, const RenderParams rp, WfState st,
-                                                          const int32_t* __restrict__ q, uint32_t cnt) {
+                                                          const int32_t* __restrict__ q, const WfCtl* __restrict__ ctl) {
     const int t = blockIdx.x * kWfBlock + threadIdx.x;
-    if (t >= (int)cnt) return;
+    if (t >= (int)ctl->n_fin) return;
     const int p = q[t];
     const uint32_t pend = st.pend[p];
     float4 l4 = st.L[p];
@@ -685,13 +695,45 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
     st.pix[p] = -1;
 }
 
-// Every slot starts free (pix = -1, in the free list in slot order).
-__global__ void k_wf_init_free(int32_t* q_free, int32_t* pix, int n) {
+// Every slot starts free (pix = -1, in the free list in slot order); the counts read as after a
+// compaction of an empty pool (counts zeroed by the host first).
+__global__ void k_wf_init_free(int32_t* q_free, int32_t* pix, uint32_t* counts, int n) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) {
         q_free[t] = t;
         pix[t] = -1;
     }
+    if (t == 0) counts[4] = (uint32_t)n;
+}
+
+// control: one iteration's sizes from the previous compaction (path rays continuing, shadow and
+// MIS rays, free slots, cache queries) and the batch's remaining samples; then clears the
+// per-iteration counters (words 0..31).  `active` is 0 once nothing is left to do, and every
+// kernel of such an iteration finds empty lists.
+__global__ void k_wf_control(WfState st, WfCtl* ctl) {
+    __shared__ uint32_t c[16];
+    if (threadIdx.x < 16) c[threadIdx.x] = st.counts[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        WfCtl x = *ctl;
+        x.n_fin = x.n_ext;  // paths shaded in the previous iteration
+        x.n_cont = c[0];
+        x.n_sh = c[2];
+        x.n_mis = c[3];
+        x.nfree = c[4];
+        x.n_query = c[12];
+        const long long rem = x.ctot - x.generated;
+        x.take = (uint32_t)min((long long)x.nfree, rem);
+        x.n_ext = x.n_cont + x.take;
+        x.gen0 = x.generated;
+        x.generated += x.take;
+        x.active = (x.n_ext | x.n_fin | x.n_sh | x.n_mis | x.n_query) ? 1u : 0u;
+        x.queries += x.n_query;
+        if (x.active) ++x.iters;
+        *ctl = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) st.counts[threadIdx.x] = 0u;
 }
 
 // compact: one pass over the pool after shade.  Every live slot (pix >= 0) was shaded in this

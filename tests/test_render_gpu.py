@@ -198,3 +198,20 @@ def test_fp64_oracle_converges_to_fp32_estimator(ctx, scene_dirs):
         errs.append(np.sqrt(np.mean((f - ref) ** 2)))
     print("RMSE vs FP64 at 4/16/64 spp:", errs)
     assert errs[0] > errs[1] > errs[2]
+
+
+def test_graph_and_kernel_by_kernel_iterations_agree(ctx, scene_dirs):
+    """The wavefront iteration launched as captured CUDA graphs (grids for the largest lists,
+    control on the device) renders exactly what the kernel-by-kernel loop renders."""
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs["materials"]
+    s = lts.Scene.parse(ctx, d, sc, sub, 80, 64)
+    integ = lts.PathTracingIntegrator(8, 3, s, integrator=1)
+    out = {}
+    for g in (1, 0):
+        ctx.set_option("wavefront_graph", g)
+        out[g] = integ.render(8, 21, record=True)
+    ctx.set_option("wavefront_graph", 1)
+    assert np.array_equal(out[0]["sig"], out[1]["sig"])
+    assert np.array_equal(out[0]["L"].view(np.uint32), out[1]["L"].view(np.uint32))
+    assert np.array_equal(out[0]["film"].view(np.uint32), out[1]["film"].view(np.uint32))
