@@ -363,6 +363,63 @@ def run_gpu(args, wl):
         dist.destroy_process_group()
 
 
+def views64(args):
+    """Batched uneven views (the scene of the main workload, 8 bounces): 64 cameras at radius 3.5
+    looking at the origin through the box's open front (directions drawn on the cap z >= 0.5 of
+    the sphere, seed 4), resolutions drawn from {128^2, 256^2, 512x384, 1024^2}, spp from
+    {4, 16, 64}.  Aggregate Mpaths/s of: each view rendered alone; all views batched; batched
+    after the autotuner; batched with the radiance cache shared by all views."""
+    import numpy as np
+
+    import lighttransportsimulation_gb300 as lts
+    wl = WORKLOAD
+    rng = np.random.default_rng(4)
+    sizes = [(128, 128), (256, 256), (512, 384), (1024, 1024)]
+    views = []
+    while len(views) < 64:
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        if d[2] < 0.5:
+            continue
+        w, h = sizes[rng.integers(0, 4)]
+        views.append(dict(frm=tuple(float(x) for x in 3.5 * d), at=(0.0, 0.0, 0.0), up=(0, 1, 0), vfov=40.0, focus=3.5,
+                          width=w, height=h, spp=int(rng.choice([4, 16, 64])), seed=len(views)))
+    paths = sum(v["width"] * v["height"] * v["spp"] for v in views)
+    ctx = lts.Context(0)
+    d, sc, sub = scene_dir(wl)
+    scene = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
+    maxb, rr = wl["max_bounce"], wl["rr_start"]
+    lts.render_views(scene, views[:2], maxb, rr)  # warm-up: BVH, buffers
+    t_alone = sum(lts.render_views(scene, [v], maxb, rr)[1] for v in views)
+    _, t_batch = lts.render_views(scene, views, maxb, rr)
+    tuned = lts.autotune_views(scene, views, maxb, rr)
+    _, t_tuned = lts.render_views(scene, views, maxb, rr)
+    lts.RadianceCacheMLP(ctx, seed=7)
+    ctx.set_option("radiance_cache", 1)
+    biases = []
+    for _ in range(12):  # the cache trains on each render; the last render is the timed one
+        _, t_cached = lts.render_views(scene, views, maxb, rr)
+        biases.append(round(ctx.metrics().cache_bias, 4))
+    m = ctx.metrics()
+    ctx.set_option("radiance_cache", 0)
+    line = {"metric": "Mpaths/s", "unit": "Mpaths/s", "higher_is_better": True, "data": "synthetic",
+            "config": {"workload": "64_uneven_views_displaced_icosphere_box", "views": 64, "paths": paths,
+                       "max_bounce": maxb, "rr_start": rr,
+                       "sizes": {f"{w}x{h}": sum(1 for v in views if (v["width"], v["height"]) == (w, h))
+                                 for w, h in sizes},
+                       "spp": {str(k): sum(1 for v in views if v["spp"] == k) for k in (4, 16, 64)}},
+            "one_by_one": round(paths / (t_alone * 1e-3) / 1e6, 2),
+            "batched": round(paths / (t_batch * 1e-3) / 1e6, 2),
+            "batched_autotuned": round(paths / (t_tuned * 1e-3) / 1e6, 2), "autotune": tuned,
+            "batched_autotuned_cached": round(paths / (t_cached * 1e-3) / 1e6, 2),
+            "cache": {"bias": round(m.cache_bias, 4), "bias_by_render": biases, "train_samples": m.cache_train_samples,
+                      "train_ms": round(m.cache_train_ms, 3)},
+            "ms": {"one_by_one": round(t_alone, 2), "batched": round(t_batch, 2), "autotuned": round(t_tuned, 2),
+                   "cached": round(t_cached, 2)}}
+    print(json.dumps(line))
+    ctx.close()
+
+
 TTR_LEVELS = (0.05, 0.03, 0.02, 0.015, 0.0125, 0.01)
 
 
@@ -478,6 +535,7 @@ def main():
                     help="traversal structure: 8-wide compressed BVH or the binary LBVH")
     ap.add_argument("--lbvh-only", type=int, default=0, metavar="N",
                     help="only time the LBVH build over N random triangles (seed 1)")
+    ap.add_argument("--views64", action="store_true", help="64 batched uneven views (autotuned, with the cache)")
     ap.add_argument("--time-to-rmse", action="store_true",
                     help="time for the cached wavefront and the plain megakernel to reach --ttr-target RMSE")
     ap.add_argument("--ttr-target", type=float, default=1e-2)
@@ -491,6 +549,9 @@ def main():
     wl = SMALL if args.small else (STRESS if args.stress else WORKLOAD)
     if args.time_to_rmse:
         time_to_rmse(args)
+        return
+    if args.views64:
+        views64(args)
         return
     if args.lbvh_only:
         import lighttransportsimulation_gb300 as lts

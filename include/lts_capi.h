@@ -199,6 +199,18 @@ typedef struct {
 int lts_render_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts_render_desc* desc,
                      float* const* films_rgb, lts_render_out* out);
 
+/* Autotuner (no counterpart in the reference): renders the views at 1/8 of their spp under each
+ * candidate shape of the wavefront -- path-pool capacity 2^18 .. 2^22 (queue size), persistent
+ * trace blocks per SM 2 / 4 / all resident (block shape), graph or kernel-by-kernel iterations --
+ * one knob at a time from the current settings, keeps the fastest and leaves it set on the
+ * context (the options wavefront_pool, trace_blocks_per_sm, wavefront_graph). */
+typedef struct {
+    int32_t pool_log2, trace_blocks_per_sm, graph;
+    double ms_default, ms_best; /* device ms of one tuning render before and after */
+} lts_autotune_result;
+int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts_render_desc* desc,
+                       lts_autotune_result* result);
+
 /* Tuning knobs of the renderer (no counterpart in the reference).  Keys:
  *   "radiance_cache"          1: wavefront paths end at the vertex after their first rough vertex
  *                             (roughness > 0.3) with the MLP's radiance there; a share of paths is
@@ -210,6 +222,7 @@ int lts_render_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts_r
  *   "radiance_cache_train_steps"       Adam steps per render (default 4)
  *   "radiance_cache_lr_micro"          learning rate in 1e-6 (default 1000 = 1e-3)
  *   "film_accumulate"         1: renders add to the film's sums instead of clearing them
+ *   "trace_blocks_per_sm"     persistent trace blocks per SM (0, default: all that stay resident)
  *   "wavefront_graph"         1 (default): each wavefront iteration runs as a captured CUDA graph,
  *                             launched in groups with one host check per group; 0: kernel by
  *                             kernel with host-sized grids and per-stage timing (lts_metrics)

@@ -37,7 +37,8 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_bvh_build_device_async", "lts_bvh_dump_get", "lts_render", "lts_render_async", "lts_film_get",
            "lts_write_image", "lts_get_metrics", "lts_bvh_build_noalloc", "lts_debug_trace_sample",
            "lts_debug_trace_get", "lts_set_option", "lts_debug_umma_probe", "lts_mlp_init", "lts_mlp_set_params",
-           "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step", "lts_render_views"]
+           "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step", "lts_render_views",
+           "lts_autotune_views"]
 
 
 class LtsError(RuntimeError):
@@ -127,6 +128,7 @@ def library():
             "lts_mlp_forward": (I, [P, P, I, P]),
             "lts_mlp_train_step": (I, [P, P, P, I, ctypes.c_float, P, P]),
             "lts_render_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P, ctypes.POINTER(RenderOut)]),
+            "lts_autotune_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -361,14 +363,13 @@ class View(ctypes.Structure):
                 ("height", ctypes.c_int32), ("spp", ctypes.c_int32), ("seed", ctypes.c_uint32)]
 
 
-def render_views(scene, views, max_bounce, rr_start, bvh_mode=1):
-    """Renders every view (dicts with frm, at, up, vfov, focus, width, height, spp, seed) of the
-    loaded scene in batched wavefront launches; returns ([H x W x 3 images, flipped like
-    lts_render's film], render_ms)."""
-    import numpy as np
-    ctx = scene.ctx
-    n = len(views)
-    arr = (View * n)()
+class AutotuneResult(ctypes.Structure):
+    _fields_ = [("pool_log2", ctypes.c_int32), ("trace_blocks_per_sm", ctypes.c_int32), ("graph", ctypes.c_int32),
+                ("ms_default", ctypes.c_double), ("ms_best", ctypes.c_double)]
+
+
+def _view_array(views):
+    arr = (View * len(views))()
     for k, v in enumerate(views):
         arr[k].frm[:] = v["frm"]
         arr[k].at[:] = v["at"]
@@ -376,6 +377,29 @@ def render_views(scene, views, max_bounce, rr_start, bvh_mode=1):
         arr[k].vfov = v["vfov"]
         arr[k].focus = v.get("focus", 1.0)
         arr[k].width, arr[k].height, arr[k].spp, arr[k].seed = v["width"], v["height"], v["spp"], v["seed"]
+    return arr
+
+
+def autotune_views(scene, views, max_bounce, rr_start, bvh_mode=1):
+    """lts_autotune_views: picks and sets the wavefront's pool size, trace grid and graph mode for
+    this batch of views; returns the choice as a dict."""
+    ctx = scene.ctx
+    desc = RenderDesc()
+    desc.spp, desc.max_bounce, desc.rr_start, desc.integrator, desc.bvh_mode = 1, max_bounce, rr_start, 1, bvh_mode
+    res = AutotuneResult()
+    ctx.check(ctx.lib.lts_autotune_views(ctx.h, _view_array(views), len(views), ctypes.byref(desc), ctypes.byref(res)))
+    return {"pool_log2": res.pool_log2, "trace_blocks_per_sm": res.trace_blocks_per_sm, "graph": res.graph,
+            "ms_default": res.ms_default, "ms_best": res.ms_best}
+
+
+def render_views(scene, views, max_bounce, rr_start, bvh_mode=1):
+    """Renders every view (dicts with frm, at, up, vfov, focus, width, height, spp, seed) of the
+    loaded scene in batched wavefront launches; returns ([H x W x 3 images, flipped like
+    lts_render's film], render_ms)."""
+    import numpy as np
+    ctx = scene.ctx
+    n = len(views)
+    arr = _view_array(views)
     films = [np.zeros(v["width"] * v["height"] * 3, np.float32) for v in views]
     ptrs = (ctypes.c_void_p * n)(*[f.ctypes.data for f in films])
     desc = RenderDesc()

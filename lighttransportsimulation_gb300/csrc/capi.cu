@@ -400,6 +400,23 @@ int lts_render_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts_r
     return LTS_OK;
 }
 
+int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts_render_desc* desc,
+                       lts_autotune_result* result) {
+    if (!ctx || !desc || !views || n <= 0) return fail(ctx, LTS_ERR_ARG, "null argument");
+    if (ctx->device == -1) return fail(ctx, LTS_ERR_STATE, "host-only context (device -1) cannot run kernels");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    CK(cudaSetDevice(ctx->device));
+    const int mode = desc->bvh_mode == LTS_BVH_REFERENCE ? LTS_BVH_REFERENCE : LTS_BVH_SORTED;
+    if (!(ctx->bvh_is_scene && ctx->bvh_mode == mode)) {
+        int rc = lts_bvh_build(ctx, mode, nullptr);
+        if (rc) return rc;
+    }
+    std::string e = ctx->tracer->autotune_views(ctx->scene, *ctx->bvh, views, n, *desc, result, ctx->stream,
+                                                ctx->d_error);
+    if (!e.empty()) return fail(ctx, e.find("argument") != std::string::npos ? LTS_ERR_ARG : LTS_ERR_CUDA, e);
+    return check_device_error(ctx);
+}
+
 int lts_render_async(lts_ctx* ctx, const lts_render_desc* desc) {
     if (!ctx || !desc) return fail(ctx, LTS_ERR_ARG, "null argument");
     if (ctx->device == -1) return fail(ctx, LTS_ERR_STATE, "host-only context (device -1) cannot run kernels");
@@ -564,6 +581,9 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
         ctx->tracer->cache_train_steps = (int)value;
     } else if (!strcmp(key, "radiance_cache_lr_micro")) {
         ctx->tracer->cache_lr = (float)value * 1e-6f;
+    } else if (!strcmp(key, "trace_blocks_per_sm")) {
+        if (value > 64) return fail(ctx, LTS_ERR_ARG, "trace_blocks_per_sm must be 0..64");
+        ctx->tracer->trace_blocks_per_sm = (int)value;
     } else if (!strcmp(key, "wavefront_graph")) {
         ctx->tracer->wf_graph = value ? 1 : 0;
     } else if (!strcmp(key, "film_accumulate")) {

@@ -520,8 +520,10 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
         TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, k_wf_trace<false>, kWfBlock, 0));
         wf_trace_blocks_[0] = (unsigned)std::max(1, per_w * sms);
         wf_trace_blocks_[1] = (unsigned)std::max(1, per_b * sms);
+        wf_sms_ = (unsigned)sms;
     }
-    const unsigned tb = wf_trace_blocks_[wide ? 0 : 1];
+    unsigned tb = wf_trace_blocks_[wide ? 0 : 1];
+    if (trace_blocks_per_sm > 0) tb = std::min(tb, (unsigned)trace_blocks_per_sm * wf_sms_);
     const unsigned cgrid = (unsigned)((P + kCompactTile - 1) / kCompactTile);
     const dim3 gblock(32, 4);
     // control block (device) and its host mirror
@@ -887,6 +889,83 @@ std::string Tracer::render_views(const HostScene& sc, const Lbvh& bvh, const lts
         out->rays = last_rays;
         out->node_visits = last_node_visits;
         out->tri_tests = last_tri_tests;
+    }
+    return "";
+}
+
+
+// Autotuner: renders the views at reduced spp under each candidate of the wavefront's runtime
+// shape -- path-pool capacity (queue size), persistent trace blocks per SM, graph or
+// kernel-by-kernel iterations -- one knob at a time from the defaults, keeps the fastest and leaves
+// it set.
+std::string Tracer::autotune_views(const HostScene& sc, const Lbvh& bvh, const lts_view* views, int n,
+                                   const lts_render_desc& d, lts_autotune_result* res, cudaStream_t s,
+                                   uint32_t* d_err) {
+    std::vector<lts_view> tv(views, views + n);
+    long max_pix = 0;
+    for (lts_view& v : tv) {
+        v.spp = std::max(1, v.spp / 8);
+        max_pix = std::max(max_pix, (long)v.width * v.height);
+    }
+    std::vector<float> scratch(3 * (size_t)max_pix);
+    std::vector<float*> films(n, scratch.data());  // every view resolves into the same host buffer
+    const bool accum = film_accumulate;
+    film_accumulate = false;
+    auto trial = [&](double* ms) -> std::string {
+        double best = 1e30;
+        for (int rep = 0; rep < 2; ++rep) {  // first run may allocate; keep the faster of two
+            const std::string e = render_views(sc, bvh, tv.data(), n, d, films.data(), nullptr, s, d_err);
+            if (!e.empty()) return e;
+            best = std::min(best, (double)last_ms);
+        }
+        *ms = best;
+        return "";
+    };
+    long pool = wf_pool > 0 ? wf_pool : (1l << 21);
+    int bps = trace_blocks_per_sm, graph = wf_graph;
+    double t0 = 0;
+    std::string e = trial(&t0);
+    if (!e.empty()) return e;
+    double best = t0;
+    for (int lg = 18; lg <= 22; ++lg) {
+        wf_pool = 1l << lg;
+        double t;
+        if (!(e = trial(&t)).empty()) return e;
+        if (t < best) {
+            best = t;
+            pool = wf_pool;
+        }
+    }
+    wf_pool = pool;
+    for (int b : {2, 4, 0}) {  // 0: as many as stay resident
+        trace_blocks_per_sm = b;
+        double t;
+        if (!(e = trial(&t)).empty()) return e;
+        if (t < best) {
+            best = t;
+            bps = b;
+        }
+    }
+    trace_blocks_per_sm = bps;
+    wf_graph = 1 - graph;
+    {
+        double t;
+        if (!(e = trial(&t)).empty()) return e;
+        if (t < best) {
+            best = t;
+            graph = wf_graph;
+        }
+    }
+    wf_graph = graph;
+    film_accumulate = accum;
+    if (res) {
+        int lg = 0;
+        while ((1l << lg) < pool) ++lg;
+        res->pool_log2 = lg;
+        res->trace_blocks_per_sm = bps;
+        res->graph = graph;
+        res->ms_default = t0;
+        res->ms_best = best;
     }
     return "";
 }

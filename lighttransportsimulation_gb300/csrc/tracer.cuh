@@ -103,6 +103,8 @@ class Tracer {
     std::string render_async(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                              uint32_t* d_err);
     std::string film_get(const HostScene& sc, float* rgb, double* sums, cudaStream_t s);
+    std::string autotune_views(const HostScene& sc, const Lbvh& bvh, const lts_view* views, int n,
+                               const lts_render_desc& d, lts_autotune_result* res, cudaStream_t s, uint32_t* d_err);
     // Batched views (lts_render_views): every view's full frame through the wavefront loop.
     std::string render_views(const HostScene& sc, const Lbvh& bvh, const lts_view* views, int n,
                              const lts_render_desc& d, float* const* films, lts_render_out* out, cudaStream_t s,
@@ -129,6 +131,8 @@ class Tracer {
     // Wavefront iterations as CUDA graphs launched in groups (1), or launched one by one with
     // host-sized grids and per-stage timing (0).
     int wf_graph = 1;
+    // Persistent trace blocks per SM (0: as many as stay resident).
+    int trace_blocks_per_sm = 0;
     // Finished-sample buffer capacity of the wavefront film gather, in samples (0: 2^27).
     long wf_sample_cap = 0;
     int last_iterations = 0;
@@ -158,7 +162,8 @@ class Tracer {
     uint32_t* wf_counts_host_ = nullptr;
     void* wf_ctl_host_ = nullptr;  // pinned mirror of the wavefront control block
     cudaEvent_t wf_ev_[7] = {nullptr};
-    unsigned wf_trace_blocks_[2] = {0, 0};  // resident blocks of k_wf_trace (wide, binary) on this device
+    unsigned wf_trace_blocks_[2] = {0, 0};
+    unsigned wf_sms_ = 0;  // resident blocks of k_wf_trace (wide, binary) on this device
     SceneView view_{};
     WideBvh wide_;
     void* bufs_[16] = {nullptr};

@@ -47,3 +47,21 @@ def test_batching_does_not_change_a_view(ctx, scene_dirs):
         ctx.set_option("wavefront_sample_chunk", 0)
     for a, b in zip(sliced, together):
         assert np.allclose(a, b, rtol=1e-5, atol=1e-7)
+
+
+def test_autotuner_picks_a_setting_and_keeps_results(ctx, scene_dirs):
+    """The autotuner returns one of its candidates, no slower than the defaults it started from,
+    and rendering after it gives the same images (the knobs change speed, not samples)."""
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs["box_sphere"]
+    s = lts.Scene.parse(ctx, d, sc, sub, 64, 64)
+    before, _ = lts.render_views(s, VIEWS, 5, 3)
+    res = lts.autotune_views(s, VIEWS, 5, 3)
+    print(res)
+    assert 18 <= res["pool_log2"] <= 22 and res["trace_blocks_per_sm"] in (0, 2, 4) and res["graph"] in (0, 1)
+    assert res["ms_best"] <= res["ms_default"]
+    after, _ = lts.render_views(s, VIEWS, 5, 3)
+    for a, b in zip(before, after):
+        assert np.allclose(a, b, rtol=1e-5, atol=1e-7)
+    for k, v in (("wavefront_pool", 0), ("trace_blocks_per_sm", 0), ("wavefront_graph", 1)):
+        ctx.set_option(k, v)
