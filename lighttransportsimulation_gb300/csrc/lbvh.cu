@@ -5,8 +5,8 @@
 //                                                                 BVH.cuh:101-116,134-137, Bound.cuh:169-175
 //   3 k_digit_prefix + 4 x k_onesweep   stable LSD radix sort of (code, id), 8-bit digits,
 //                      decoupled look-back (replaces thrust::stable_sort_by_key, BVH.cuh:140-146)
-//   4 k_topology       Karras split per interior node             BVH.cuh:173-236
-//   5 k_refit          bottom-up AABBs, second arrival unions     BVH.cuh:238-262
+//   4 k_tree           Karras topology and bottom-up AABBs in one climb
+//                                                                 BVH.cuh:173-262
 // Output layout: one 64-byte node per interior node carrying both child boxes (see lbvh.cuh).
 #include <cuda/atomic>
 #include <cuda_runtime.h>
@@ -145,7 +145,7 @@ __global__ __launch_bounds__(kBlock) void k_morton(const float* __restrict__ tri
                 id = (int32_t)i;
             }
             codes[i] = code;
-            ids[i] = id;
+            if (ids) ids[i] = id;  // null: every id is its position, generated by the first sort pass
 #pragma unroll
             for (int p = 0; p < 4; ++p) atomicAdd(&s_hist[p * 256 + ((code >> (8 * p)) & 255u)], 1u);
         }
@@ -178,7 +178,32 @@ __global__ void k_digit_prefix(const uint32_t* __restrict__ hist, uint32_t* __re
     prefix[blockIdx.x * 256 + threadIdx.x] = block_excl_scan256(v, s_warp);
 }
 
-__global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __restrict__ kin, const int32_t* __restrict__ vin,
+#ifndef LTS_SORT_MIN_BLOCKS
+#define LTS_SORT_MIN_BLOCKS 4  // resident sort tiles per SM the register budget is cut for
+#endif
+#ifndef LTS_SORT_BALLOT_MATCH
+#define LTS_SORT_BALLOT_MATCH 1  // 0: __match_any_sync
+#endif
+// Lanes of the warp whose valid key has the same 8-bit digit d (only valid lanes: `valid`).  One
+// ballot per digit bit: a lane keeps the lanes that agree with it on every bit.  MATCH.ANY is
+// issued on the slow ADU pipe; the ballots are not.
+__device__ __forceinline__ uint32_t digit_peers(uint32_t d, bool valid) {
+#if LTS_SORT_BALLOT_MATCH
+    uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const bool bit = (d >> b) & 1u;
+        const uint32_t m = __ballot_sync(0xffffffffu, bit);
+        peers &= bit ? m : ~m;
+    }
+    return valid ? peers : (1u << (threadIdx.x & 31));  // an invalid lane ranks alone (unused)
+#else
+    return __match_any_sync(0xffffffffu, valid ? d : 256u);
+#endif
+}
+
+// vin null: every value is its key's position (the identity ids of the first pass).
+__global__ __launch_bounds__(kSortThreads, LTS_SORT_MIN_BLOCKS) void k_onesweep(const uint32_t* __restrict__ kin, const int32_t* __restrict__ vin,
                                                            uint32_t* __restrict__ kout, int32_t* __restrict__ vout,
                                                            int n, int shift, const uint32_t* __restrict__ gprefix,
                                                            uint32_t* __restrict__ status, uint32_t* __restrict__ tile_counter,
@@ -207,7 +232,7 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
         const long idx = wbase + i * 32 + lane;
         if (idx < n) {
             key[i] = __ldg(kin + idx);
-            val[i] = __ldg(vin + idx);
+            val[i] = vin ? __ldg(vin + idx) : (int32_t)idx;
         } else {
             key[i] = 0;
             val[i] = 0;
@@ -219,7 +244,7 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
         const long idx = wbase + i * 32 + lane;
         const bool valid = idx < n;
         const uint32_t d = (key[i] >> shift) & 255u;
-        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u);
+        const uint32_t peers = digit_peers(d, valid);
         const int leader = __ffs(peers) - 1;
         uint32_t b = 0;
         if (valid && lane == leader) {
@@ -285,11 +310,11 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
     }
 }
 
-// ------------------------------------------------------------------ 4. Karras topology
-__device__ __forceinline__ int delta(const uint32_t* __restrict__ c, int n, int a, int b) {
-    // BVH.cuh:173-190 (a is always in range)
-    if (b < 0 || b >= n) return -1;
-    uint32_t x = __ldg(c + a) ^ __ldg(c + b);
+// ------------------------------------------------------------------ 4+5. tree: topology and refit
+// delta (BVH.cuh:173-190): common-prefix length of the Morton codes at sorted positions a and b;
+// for equal codes 40 + the common prefix of the positions; -1 when b lies outside [0, n).
+__device__ __forceinline__ int delta_codes(uint32_t ca, uint32_t cb, int a, int b) {
+    uint32_t x = ca ^ cb;
     int extra = 0;
     if (x == 0) {
         extra = 40;
@@ -297,80 +322,238 @@ __device__ __forceinline__ int delta(const uint32_t* __restrict__ c, int n, int 
     }
     return __clz((int)x) + extra;
 }
-
-__global__ __launch_bounds__(kBlock) void k_topology(const uint32_t* __restrict__ codes, int n, BvhNode* __restrict__ nodes,
-                                                     int32_t* __restrict__ parent) {
-    const int i = blockIdx.x * kBlock + threadIdx.x;
-    if (i >= n - 1) return;
-    // BVH.cuh:192-236
-    const int d = (delta(codes, n, i, i + 1) - delta(codes, n, i, i - 1)) > 0 ? 1 : -1;
-    const int dmin = delta(codes, n, i, i - d);
-    long lmax = 128;
-    while (delta(codes, n, i, (int)(i + lmax * d)) > dmin) lmax *= 4;
-    int l = 0;
-    for (long t = lmax / 2; t >= 1; t /= 2)
-        if (delta(codes, n, i, (int)(i + (l + t) * d)) > dmin) l += (int)t;
-    const int j = i + l * d;
-    const int dnode = delta(codes, n, i, j);
-    int s = 0;
-    for (int t = (l + 1) / 2; t >= 1; t = (t == 1) ? 0 : (t + 1) / 2)
-        if (delta(codes, n, i, i + (s + t) * d) > dnode) s += t;
-    const int gamma = i + s * d + min(d, 0);
-    const int lo = min(i, j), hi = max(i, j);
-    const int left = (lo == gamma) ? ~gamma : gamma;
-    const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
-    nodes[i].d = make_int4(left, right, -1, 0);
-    const int lc = left < 0 ? (n - 1) + ~left : left;
-    const int rc = right < 0 ? (n - 1) + ~right : right;
-    parent[lc] = i << 1;
-    parent[rc] = (i << 1) | 1;
+__device__ __forceinline__ int delta(const uint32_t* __restrict__ c, int n, int a, int b) {
+    if (b < 0 || b >= n) return -1;
+    return delta_codes(__ldg(c + a), __ldg(c + b), a, b);
 }
 
-// ------------------------------------------------------------------ 5. refit
-__global__ __launch_bounds__(kBlock) void k_refit(const float* __restrict__ tri, int n, int mode, const int32_t* __restrict__ ids,
-                                                  const int32_t* __restrict__ parent, BvhNode* __restrict__ nodes,
-                                                  uint32_t* __restrict__ flags, int32_t* __restrict__ leaf_prim,
-                                                  float* __restrict__ root_bounds) {
-    const int l = blockIdx.x * kBlock + threadIdx.x;
-    if (l >= n) return;
-    const int prim = (mode == BVH_MODE_REFERENCE) ? l : __ldg(ids + l);
-    leaf_prim[l] = prim;
-    float t[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9L * prim + k);
-    float mn[3], mx[3];
-    tri_bounds(t, mn, mx);
-    if (n == 1) {
-        for (int k = 0; k < 3; ++k) {
-            root_bounds[k] = mn[k];
-            root_bounds[3 + k] = mx[k];
-        }
-        return;
+// The reference builds the tree in two passes: every interior node i finds its leaf range and
+// split by binary searches over delta (BVH.cuh:192-236), then every leaf climbs to the root
+// through parent links, the second child to arrive forming the union (BVH.cuh:238-262).  The
+// result is the binary radix tree of the sorted codes: node [lo, hi] with split g has children
+// [lo, g] and [g+1, hi]; an interior child sits at index g when it is a left child (its last
+// position) and at g+1 when it is a right child (its first position); the root, [0, n-1], at 0.
+// The same tree is built here in ONE bottom-up pass (the agglomerative order of Apetrei, "Fast
+// and Simple Agglomerative LBVH Construction", 2014, with the indices above): node [L, R] is the
+// left child of a parent split at R when delta(R, R+1) > delta(L-1, L) and the right child of a
+// parent split at L-1 otherwise (the two deltas differ for distinct augmented keys), which also
+// gives the node's own index (R or L).  Each thread climbs from one leaf; the two children of a
+// parent meet at the parent's split g, the first to arrive stops, the second forms the union,
+// writes the parent's whole 64-byte record (both child boxes, children, range) and climbs on:
+//  * a block of kTreeBlock threads owns kTreeBlock consecutive leaves; when g and g+1 both lie in
+//    the block the children meet in a shared-memory slot of g (box, child reference, far range
+//    end; a block-scope fence and a shared arrival bitmask), without barriers;
+//  * otherwise they meet in device memory, in a second kernel (k_tree_top), so that no block of
+//    k_tree waits on another: k_tree lists such a child (its reference; its record is written),
+//    and also a child left alone in a shared slot after the block's climbs (its sibling reaches
+//    into another block).  k_tree_top climbs from every listed child: both children of a parent
+//    swap the build's epoch into the arrival word of g with acq_rel order, and the second reads
+//    its sibling back -- the sibling's node record, or its triangle for a leaf.  Only the
+//    ~log2(n / kTreeBlock) ancestors of each block edge meet there.
+constexpr int kTreeBlock = 512;
+#ifndef LTS_TREE_MIN_BLOCKS
+#define LTS_TREE_MIN_BLOCKS 4  // resident blocks per SM the register budget is cut for
+#endif
+
+__device__ __forceinline__ void put_node(BvhNode* __restrict__ nodes, int idx, const float* cb, int lref, int rref, int lo,
+                                         int hi) {
+    float4* P = reinterpret_cast<float4*>(nodes + idx);
+    P[0] = make_float4(cb[0], cb[1], cb[2], cb[3]);
+    P[1] = make_float4(cb[4], cb[5], cb[6], cb[7]);
+    P[2] = make_float4(cb[8], cb[9], cb[10], cb[11]);
+    reinterpret_cast<int4*>(P)[3] = make_int4(lref, rref, lo, hi);
+}
+__device__ __forceinline__ void put_root(float* __restrict__ root_bounds, const float* mn, const float* mx) {
+    for (int k = 0; k < 3; ++k) {
+        root_bounds[k] = mn[k];
+        root_bounds[3 + k] = mx[k];
     }
-    int node = (n - 1) + l;
+}
+
+// Children (own box / ref, sibling box / ref) of the parent in left-right order, and the union.
+__device__ __forceinline__ void pair_up(bool left, float* mn, float* mx, const float* smn, const float* smx, float* cb) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        cb[k] = left ? mn[k] : smn[k];
+        cb[3 + k] = left ? mx[k] : smx[k];
+        cb[6 + k] = left ? smn[k] : mn[k];
+        cb[9 + k] = left ? smx[k] : mx[k];
+        mn[k] = fminf(cb[k], cb[6 + k]);  // bUnion(left, right)
+        mx[k] = fmaxf(cb[3 + k], cb[9 + k]);
+    }
+}
+
+// Arrival word of a split: the build's epoch (kEpochBits) above a leaf flag and the far range end
+// of the child that arrived (its first leaf for a left child, its last for a right child), so
+// that the second arrival learns its sibling's shape from the exchange itself.
+constexpr int kEpochBits = 7;
+constexpr uint32_t kEpochMax = (1u << kEpochBits) - 1u;
+constexpr uint32_t kArrivalLeaf = 1u << 24, kArrivalEnd = kArrivalLeaf - 1u;
+static_assert(32 - kEpochBits == 25, "epoch above the leaf flag and a 24-bit position");
+
+// The climb through device memory from node [L, R] (reference ref, box mn/mx, its record already
+// written), the `left` child of the parent split at g.
+__device__ void climb_global(const float* __restrict__ tri, int n, int mode, const int32_t* __restrict__ ids,
+                             const uint32_t* __restrict__ codes, BvhNode* __restrict__ nodes,
+                             uint32_t* __restrict__ arrivals, uint32_t epoch, float* __restrict__ root_bounds, int L,
+                             int R, int ref, int g, bool left, float* mn, float* mx) {
     for (;;) {
-        const int pe = __ldg(parent + node);
-        const int p = pe >> 1;
-        float* P = reinterpret_cast<float*>(nodes + p);
-        if ((pe & 1) == 0) {  // left slot: a.xyz = min, a.w, b.x, b.y = max
-            P[0] = mn[0]; P[1] = mn[1]; P[2] = mn[2]; P[3] = mx[0]; P[4] = mx[1]; P[5] = mx[2];
-        } else {              // right slot: b.z, b.w, c.x = min, c.yzw = max
-            P[6] = mn[0]; P[7] = mn[1]; P[8] = mn[2]; P[9] = mx[0]; P[10] = mx[1]; P[11] = mx[2];
+        cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrival(arrivals[g]);
+        const uint32_t mine = (epoch << 25) | (L == R ? kArrivalLeaf : 0u) | (uint32_t)(left ? L : R);
+        const uint32_t other = arrival.exchange(mine, cuda::memory_order_acq_rel);
+        if ((other >> 25) != epoch) return;  // first arrival stops
+        const int sp = left ? g + 1 : g;     // the sibling's position next to the split
+        const int send = (int)(other & kArrivalEnd);
+        if (left) R = send;
+        else L = send;
+        const bool root = (L == 0 && R == n - 1);
+        // the parent's side, read alongside the sibling's box
+        const bool pleft = !root && delta(codes, n, R, R + 1) > delta(codes, n, L, L - 1);
+        float smn[3], smx[3];
+        int sref;
+        if (other & kArrivalLeaf) {
+            const int prim = (mode == BVH_MODE_REFERENCE) ? sp : __ldg(ids + sp);
+            float t[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9L * prim + k);
+            tri_bounds(t, smn, smx);
+            sref = ~sp;
+        } else {
+            const float4 a = __ldcg(&nodes[sp].a), b = __ldcg(&nodes[sp].b), c = __ldcg(&nodes[sp].c);
+            smn[0] = fminf(a.x, b.z); smn[1] = fminf(a.y, b.w); smn[2] = fminf(a.z, c.x);
+            smx[0] = fmaxf(a.w, c.y); smx[1] = fmaxf(b.x, c.z); smx[2] = fmaxf(b.y, c.w);
+            sref = sp;
         }
-        // acq_rel: the first arrival releases its child box, the second acquires it
-        cuda::atomic_ref<uint32_t, cuda::thread_scope_device> flag(flags[p]);
-        if (flag.fetch_add(1u, cuda::memory_order_acq_rel) == 0u) return;  // first arrival stops (BVH.cuh:251-255)
-        const float4 a = __ldcg(&nodes[p].a), b = __ldcg(&nodes[p].b), c = __ldcg(&nodes[p].c);
-        mn[0] = fminf(a.x, b.z); mn[1] = fminf(a.y, b.w); mn[2] = fminf(a.z, c.x);  // bUnion(left, right)
-        mx[0] = fmaxf(a.w, c.y); mx[1] = fmaxf(b.x, c.z); mx[2] = fmaxf(b.y, c.w);
-        if (p == 0) {
-            for (int k = 0; k < 3; ++k) {
-                root_bounds[k] = mn[k];
-                root_bounds[3 + k] = mx[k];
-            }
+        float cb[12];
+        pair_up(left, mn, mx, smn, smx, cb);
+        const int lref = left ? ref : sref, rref = left ? sref : ref;
+        if (root) {
+            put_node(nodes, 0, cb, lref, rref, L, R);
+            put_root(root_bounds, mn, mx);
             return;
         }
-        node = p;
+        left = pleft;
+        ref = left ? R : L;
+        put_node(nodes, ref, cb, lref, rref, L, R);
+        g = left ? R : L - 1;
+    }
+}
+
+__global__ __launch_bounds__(kTreeBlock, LTS_TREE_MIN_BLOCKS) void k_tree(const float* __restrict__ tri, int n, int mode,
+                                                     const int32_t* __restrict__ ids, const uint32_t* __restrict__ codes,
+                                                     BvhNode* __restrict__ nodes, int32_t* __restrict__ pending,
+                                                     uint32_t* __restrict__ pending_count, int32_t* __restrict__ leaf_prim,
+                                                     float* __restrict__ root_bounds) {
+    __shared__ uint32_t s_code[kTreeBlock + 2];      // codes of positions b0-1 .. b0+kTreeBlock
+    __shared__ float s_box[2][6][kTreeBlock];        // [left/right child][min xyz, max xyz][g - b0]
+    __shared__ int s_ref[2][kTreeBlock], s_end[2][kTreeBlock];
+    __shared__ uint32_t s_have[kTreeBlock];          // bit 0 / 1: left / right child arrived
+    const int b0 = blockIdx.x * kTreeBlock, b1 = min(b0 + kTreeBlock, n) - 1;
+    for (int k = threadIdx.x; k < kTreeBlock + 2; k += kTreeBlock) {
+        const int pos = b0 - 1 + k;
+        s_code[k] = (pos >= 0 && pos < n) ? __ldg(codes + pos) : 0u;
+    }
+    s_have[threadIdx.x] = 0u;
+    __syncthreads();
+    auto sdelta = [&](int a, int b) -> int {  // delta of positions within [b0-1, b1+1]
+        if (b < 0 || b >= n) return -1;
+        return delta_codes(s_code[a - b0 + 1], s_code[b - b0 + 1], a, b);
+    };
+
+    const int l = b0 + threadIdx.x;
+    if (l <= b1) {
+        const int prim = (mode == BVH_MODE_REFERENCE) ? l : __ldg(ids + l);
+        leaf_prim[l] = prim;
+        float t[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9L * prim + k);
+        float mn[3], mx[3];
+        tri_bounds(t, mn, mx);
+        if (n == 1) {
+            put_root(root_bounds, mn, mx);
+        } else {
+            int L = l, R = l, ref = ~l;
+            bool left = sdelta(l, l + 1) > sdelta(l, l - 1);
+            int g = left ? l : l - 1;
+            // block-local climb
+            for (;;) {
+                if (g < b0 || g + 1 > b1) {  // the parent reaches into another block
+                    pending[atomicAdd(pending_count, 1u)] = ref;
+                    break;
+                }
+                const int side = left ? 0 : 1, slot = g - b0;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    s_box[side][k][slot] = mn[k];
+                    s_box[side][3 + k][slot] = mx[k];
+                }
+                s_ref[side][slot] = ref;
+                s_end[side][slot] = left ? L : R;
+                __threadfence_block();
+                if (!(atomicOr(&s_have[slot], 1u << side) & (2u >> side))) break;  // first arrival stops
+                __threadfence_block();
+                float smn[3], smx[3], cb[12];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    smn[k] = s_box[side ^ 1][k][slot];
+                    smx[k] = s_box[side ^ 1][3 + k][slot];
+                }
+                const int sref = s_ref[side ^ 1][slot], send = s_end[side ^ 1][slot];
+                pair_up(left, mn, mx, smn, smx, cb);
+                const int lref = left ? ref : sref, rref = left ? sref : ref;
+                if (left) R = send;
+                else L = send;
+                if (L == 0 && R == n - 1) {
+                    put_node(nodes, 0, cb, lref, rref, L, R);
+                    put_root(root_bounds, mn, mx);
+                    break;
+                }
+                left = sdelta(R, R + 1) > sdelta(L, L - 1);
+                ref = left ? R : L;
+                put_node(nodes, ref, cb, lref, rref, L, R);
+                g = left ? R : L - 1;
+            }
+        }
+    }
+    __syncthreads();
+    // a child alone in its slot: the sibling reaches into another block
+    const int slot = threadIdx.x;
+    if (b0 + slot + 1 <= b1) {
+        const uint32_t have = s_have[slot];
+        if (have == 1u || have == 2u) pending[atomicAdd(pending_count, 1u)] = s_ref[have == 1u ? 0 : 1][slot];
+    }
+}
+
+// Climbs from every child k_tree listed (at most 2n - 2 of them), grid-stride.
+__global__ __launch_bounds__(kBlock) void k_tree_top(const float* __restrict__ tri, int n, int mode,
+                                                     const int32_t* __restrict__ ids, const uint32_t* __restrict__ codes,
+                                                     BvhNode* __restrict__ nodes, uint32_t* __restrict__ arrivals,
+                                                     uint32_t epoch, const int32_t* __restrict__ pending,
+                                                     const uint32_t* __restrict__ pending_count,
+                                                     float* __restrict__ root_bounds) {
+    const int count = (int)*pending_count;
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < count; i += gridDim.x * kBlock) {
+        const int ref = pending[i];
+        int L, R;
+        float mn[3], mx[3];
+        if (ref < 0) {  // leaf ~ref
+            L = R = ~ref;
+            const int prim = (mode == BVH_MODE_REFERENCE) ? L : __ldg(ids + L);
+            float t[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9L * prim + k);
+            tri_bounds(t, mn, mx);
+        } else {        // interior node: its record holds both child boxes and its range
+            const float4 a = __ldcg(&nodes[ref].a), b = __ldcg(&nodes[ref].b), c = __ldcg(&nodes[ref].c);
+            const int4 d = __ldcg(&nodes[ref].d);
+            mn[0] = fminf(a.x, b.z); mn[1] = fminf(a.y, b.w); mn[2] = fminf(a.z, c.x);
+            mx[0] = fmaxf(a.w, c.y); mx[1] = fmaxf(b.x, c.z); mx[2] = fmaxf(b.y, c.w);
+            L = d.z;
+            R = d.w;
+        }
+        const bool left = delta(codes, n, R, R + 1) > delta(codes, n, L, L - 1);
+        climb_global(tri, n, mode, ids, codes, nodes, arrivals, epoch, root_bounds, L, R, ref, left ? R : L - 1, left,
+                     mn, mx);
     }
 }
 
@@ -385,7 +568,7 @@ inline int grid_for(long items, int per_block) { return (int)((items + per_block
     } while (0)
 
 Lbvh::~Lbvh() {
-    void* ptrs[] = {nodes, root_bounds, leaf_prim, codes, ids, codes_alt_, hist_, status_, counters_, gbounds_, flags_, ids_alt_, parent_};
+    void* ptrs[] = {nodes, root_bounds, leaf_prim, codes, ids, codes_alt_, hist_, status_, counters_, gbounds_, flags_};
     for (void* p : ptrs)
         if (p) dev_free(p);
     for (auto& e : ev_)
@@ -396,7 +579,7 @@ std::string Lbvh::reserve(int nn) {
     if (!ev_[0])
         for (auto& e : ev_) LTS_TRY(cudaEventCreate(&e));
     if (nn <= cap_) return "";
-    void* ptrs[] = {nodes, root_bounds, leaf_prim, codes, ids, codes_alt_, hist_, status_, counters_, gbounds_, flags_, ids_alt_, parent_};
+    void* ptrs[] = {nodes, root_bounds, leaf_prim, codes, ids, codes_alt_, hist_, status_, counters_, gbounds_, flags_};
     for (void* p : ptrs)
         if (p) dev_free(p);
     const size_t N = (size_t)nn, tiles = (N + kSortTile - 1) / kSortTile;
@@ -410,14 +593,16 @@ std::string Lbvh::reserve(int nn) {
     LTS_TRY(al((void**)&leaf_prim, 4 * N));
     LTS_TRY(al((void**)&codes, 4 * N));
     LTS_TRY(al((void**)&ids, 4 * N));
-    LTS_TRY(al((void**)&codes_alt_, 4 * N));
-    LTS_TRY(al((void**)&ids_alt_, 4 * N));
+    // the sort's ping-pong keys and ids, one allocation: after the sort it holds the tree's list
+    // of up to 2n - 2 children that meet across blocks
+    LTS_TRY(al((void**)&codes_alt_, 8 * N));
+    ids_alt_ = reinterpret_cast<int32_t*>(codes_alt_ + N);
     LTS_TRY(al((void**)&hist_, 4 * 2 * 4 * 256));  // histograms then prefixes
     LTS_TRY(al((void**)&status_, 4 * 4 * 256 * tiles));
     LTS_TRY(al((void**)&counters_, 4 * 8));
     LTS_TRY(al((void**)&gbounds_, 4 * 6));
     LTS_TRY(al((void**)&flags_, 4 * (N > 1 ? N - 1 : 1)));
-    LTS_TRY(al((void**)&parent_, 4 * (2 * N - 1)));
+    clear_arrivals_ = true;  // arrival words of fresh memory are zeroed before the first build
     cap_ = nn;
     return "";
 }
@@ -444,7 +629,8 @@ std::string Lbvh::build(const float* d_tri, int nn, int md, int code_limit, cuda
     ++launches;
     LTS_TRY(cudaEventRecord(ev_[1], s));
     LTS_TRY(cudaMemsetAsync(hist_, 0, 4 * 4 * 256, s));
-    k_morton<<<stream_grid, kBlock, 0, s>>>(d_tri, nn, gbounds_, code_limit, codes, ids, hist_);
+    const bool identity = code_limit < 0 || code_limit >= nn;  // every id is its position
+    k_morton<<<stream_grid, kBlock, 0, s>>>(d_tri, nn, gbounds_, code_limit, codes, identity ? nullptr : ids, hist_);
     ++launches;
     LTS_TRY(cudaEventRecord(ev_[2], s));
     LTS_TRY(cudaMemsetAsync(status_, 0, 4 * 4 * 256 * tiles, s));
@@ -456,22 +642,34 @@ std::string Lbvh::build(const float* d_tri, int nn, int md, int code_limit, cuda
     uint32_t* kout = codes_alt_;
     int32_t* vout = ids_alt_;
     for (int p = 0; p < 4; ++p) {
-        k_onesweep<<<(int)tiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, nn, 8 * p, hist_ + 4 * 256 + 256 * p,
-                                                        status_ + (size_t)p * 256 * tiles, counters_ + p, d_error);
+        k_onesweep<<<(int)tiles, kSortThreads, 0, s>>>(kin, (p == 0 && identity) ? nullptr : vin, kout, vout, nn, 8 * p,
+                                                        hist_ + 4 * 256 + 256 * p, status_ + (size_t)p * 256 * tiles,
+                                                        counters_ + p, d_error);
         ++launches;
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
     LTS_TRY(cudaEventRecord(ev_[3], s));
+    // the arrival words keep the epoch of the build that last touched them, so a new epoch per
+    // build replaces clearing them; they are cleared only when fresh or when the epoch wraps
+    if (++epoch_ > kEpochMax) {
+        clear_arrivals_ = true;
+        epoch_ = 1u;
+    }
+    if (clear_arrivals_) {
+        LTS_TRY(cudaMemsetAsync(flags_, 0, 4 * (N > 1 ? N - 1 : 1), s));
+        clear_arrivals_ = false;
+    }
+    LTS_TRY(cudaEventRecord(ev_[4], s));  // topology and refit run as one kernel, timed as the refit stage
+    int32_t* pending = reinterpret_cast<int32_t*>(codes_alt_);
+    k_tree<<<grid_for((long)N, kTreeBlock), kTreeBlock, 0, s>>>(d_tri, nn, md, ids, codes, nodes, pending, counters_ + 4,
+                                                                leaf_prim, root_bounds);
+    ++launches;
     if (nn > 1) {
-        LTS_TRY(cudaMemsetAsync(parent_, 0xff, 4 * (2 * N - 1), s));
-        k_topology<<<grid_for((long)N - 1, kBlock), kBlock, 0, s>>>(codes, nn, nodes, parent_);
+        k_tree_top<<<sms * 4, kBlock, 0, s>>>(d_tri, nn, md, ids, codes, nodes, flags_, epoch_, pending, counters_ + 4,
+                                              root_bounds);
         ++launches;
     }
-    LTS_TRY(cudaEventRecord(ev_[4], s));
-    if (nn > 1) LTS_TRY(cudaMemsetAsync(flags_, 0, 4 * (N - 1), s));
-    k_refit<<<grid_for((long)N, kBlock), kBlock, 0, s>>>(d_tri, nn, md, ids, parent_, nodes, flags_, leaf_prim, root_bounds);
-    ++launches;
     LTS_TRY(cudaEventRecord(ev_[5], s));
     LTS_TRY(cudaGetLastError());
     return "";
@@ -496,11 +694,11 @@ void Lbvh::stage_ms(float out[5]) const {
 // memory-pool callback, real-time render loops that forbid cudaMalloc/cudaFree (both can
 // synchronise the whole device), and plugins whose host application owns every device
 // allocation.  This variant keeps all of the build's scratch (the sort's ping-pong buffers and
-// look-back table, histograms, parent links, refit counters, the scene box and an error word) in
+// look-back table, histograms, the tree's arrival words, the scene box and an error word) in
 // one file-scope device array of fixed size, so a call allocates nothing; the caller supplies the
 // triangles and every output buffer.
 //
-// Limits and sharing: at most kNoAllocMaxPrims primitives (about 5.3 MiB of device memory that
+// Limits and sharing: at most kNoAllocMaxPrims primitives (about 3.3 MiB of device memory that
 // every GPU which loads the library keeps until process exit).  All calls share the one array and
 // it keeps the previous call's contents, so everything that must start at zero is cleared at the
 // start of each call, and two calls that overlap on the GPU (different streams, or different host
@@ -517,13 +715,13 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kOffCodes = 0;
 constexpr size_t kOffIds = kOffCodes + align256(4ull * kNoAllocMaxPrims);
 constexpr size_t kOffHist = kOffIds + align256(4ull * kNoAllocMaxPrims);
+static_assert(kOffIds == kOffCodes + 4ull * kNoAllocMaxPrims, "the tree's list of 2n ints spans both sort buffers");
 constexpr size_t kOffStatus = kOffHist + align256(4ull * 2 * 4 * 256);
 constexpr size_t kOffCounters = kOffStatus + align256(4ull * 4 * 256 * kNoAllocTiles);
 constexpr size_t kOffBounds = kOffCounters + 256;
 constexpr size_t kOffError = kOffBounds + 256;
 constexpr size_t kOffFlags = kOffError + 256;
-constexpr size_t kOffParent = kOffFlags + align256(4ull * kNoAllocMaxPrims);
-constexpr size_t kNoAllocBytes = kOffParent + align256(4ull * (2ull * kNoAllocMaxPrims - 1));
+constexpr size_t kNoAllocBytes = kOffFlags + align256(4ull * kNoAllocMaxPrims);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -571,7 +769,6 @@ extern "C" int lts_bvh_build_noalloc(const float* d_tri, int32_t n, int32_t mode
     uint32_t* gbounds = reinterpret_cast<uint32_t*>(base + kOffBounds);
     uint32_t* err = reinterpret_cast<uint32_t*>(base + kOffError);
     uint32_t* flags = reinterpret_cast<uint32_t*>(base + kOffFlags);
-    int32_t* parent = reinterpret_cast<int32_t*>(base + kOffParent);
     BvhNode* nodes = static_cast<BvhNode*>(d_nodes);
     const size_t N = (size_t)n, tiles = (N + kSortTile - 1) / kSortTile;
     int sms = 0;
@@ -585,25 +782,27 @@ extern "C" int lts_bvh_build_noalloc(const float* d_tri, int32_t n, int32_t mode
     cudaMemsetAsync(status, 0, 4 * 4 * 256 * tiles, s);
     cudaMemsetAsync(counters, 0, 4 * 8, s);
     k_scene_bounds<<<stream_grid, kBlock, 0, s>>>(d_tri, n, gbounds);
-    k_morton<<<stream_grid, kBlock, 0, s>>>(d_tri, n, gbounds, code_limit, d_codes, d_ids, hist);
+    const bool identity = code_limit < 0 || code_limit >= n;  // every id is its position
+    k_morton<<<stream_grid, kBlock, 0, s>>>(d_tri, n, gbounds, code_limit, d_codes, identity ? nullptr : d_ids, hist);
     k_digit_prefix<<<4, 256, 0, s>>>(hist, hist + 4 * 256);
     uint32_t* kin = d_codes;
     int32_t* vin = d_ids;
     uint32_t* kout = codes_alt;
     int32_t* vout = ids_alt;
     for (int p = 0; p < 4; ++p) {
-        k_onesweep<<<(int)tiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, 8 * p, hist + 4 * 256 + 256 * p,
-                                                        status + (size_t)p * 256 * tiles, counters + p, err);
+        k_onesweep<<<(int)tiles, kSortThreads, 0, s>>>(kin, (p == 0 && identity) ? nullptr : vin, kout, vout, n, 8 * p,
+                                                        hist + 4 * 256 + 256 * p, status + (size_t)p * 256 * tiles,
+                                                        counters + p, err);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
-    if (n > 1) {
-        cudaMemsetAsync(parent, 0xff, 4 * (2 * N - 1), s);
-        k_topology<<<grid_for((long)N - 1, kBlock), kBlock, 0, s>>>(d_codes, n, nodes, parent);
-        cudaMemsetAsync(flags, 0, 4 * (N - 1), s);
-    }
-    k_refit<<<grid_for((long)N, kBlock), kBlock, 0, s>>>(d_tri, n, mode, d_ids, parent, nodes, flags, d_leaf_prim,
-                                                        d_root_bounds);
+    if (n > 1) cudaMemsetAsync(flags, 0, 4 * (N - 1), s);  // arrival words, epoch 1
+    int32_t* pending = reinterpret_cast<int32_t*>(codes_alt);  // codes_alt and ids_alt: 2n ints
+    k_tree<<<grid_for((long)N, kTreeBlock), kTreeBlock, 0, s>>>(d_tri, n, mode, d_ids, d_codes, nodes, pending,
+                                                                counters + 4, d_leaf_prim, d_root_bounds);
+    if (n > 1)
+        k_tree_top<<<sms * 4, kBlock, 0, s>>>(d_tri, n, mode, d_ids, d_codes, nodes, flags, 1u, pending, counters + 4,
+                                              d_root_bounds);
     if (cudaGetLastError() != cudaSuccess) return LTS_ERR_CUDA;
     uint32_t h_err = 0;
     if (cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return LTS_ERR_CUDA;

@@ -15,7 +15,7 @@ struct alignas(16) BvhNode {
     float4 a;  // left  min.xyz, left  max.x
     float4 b;  // left  max.yz,  right min.xy
     float4 c;  // right min.z,   right max.xyz
-    int4 d;    // left child, right child, parent (-1 for the root), unused
+    int4 d;    // left child, right child, first and last leaf (Morton position) of the node's range
 };
 
 enum { BVH_MODE_REFERENCE = 0, BVH_MODE_SORTED = 1 };
@@ -33,7 +33,8 @@ class Lbvh {
     // Returns "" or an error message (allocation failure).
     std::string build(const float* d_tri, int n, int mode, int code_limit, cudaStream_t s, uint32_t* d_error);
 
-    // Elapsed device milliseconds of the 5 stages of the last build (synchronises on events).
+    // Elapsed device milliseconds of the 5 stages of the last build (synchronises on events);
+    // topology and refit run as one kernel, reported as the refit stage (topology ~0).
     void stage_ms(float out[5]) const;
 
     int n = 0;
@@ -54,14 +55,18 @@ class Lbvh {
     size_t bytes_ = 0;
     uint32_t *codes_alt_ = nullptr, *hist_ = nullptr, *status_ = nullptr, *counters_ = nullptr,
              *gbounds_ = nullptr, *flags_ = nullptr;
-    int32_t* ids_alt_ = nullptr;
-    int32_t* parent_ = nullptr;  // [2n-1] (parent << 1) | is_right, combined index space
+    int32_t* ids_alt_ = nullptr;  // second half of codes_alt_'s allocation
+    uint32_t epoch_ = 0;            // tree-build epoch written into the arrival words (flags_)
+    bool clear_arrivals_ = false;   // flags_ is fresh memory and must be zeroed once
     cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
 // Radix-sort tile geometry (exposed for the byte model and tests).
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 15;
+#ifndef LTS_SORT_ITEMS
+#define LTS_SORT_ITEMS 15  // keys per thread of one sort tile
+#endif
+constexpr int kSortItems = LTS_SORT_ITEMS;
 constexpr int kSortTile = kSortThreads * kSortItems;
 
 }  // namespace lts

@@ -57,9 +57,10 @@ def test_sorted_mode_is_the_textbook_lbvh(ctx, scene_dirs, kind):
     lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"], np.concatenate([mn, mx], 1)[ids])
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 17, 3841, 100_003])
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 511, 512, 513, 1025, 3841, 100_003])
 def test_edge_sizes(ctx, n):
-    """Single primitive, tiny trees and sizes straddling the sort tile (3840 keys)."""
+    """Single primitive, tiny trees, sizes at the tree kernel's 512-leaf blocks and straddling the
+    sort tile (3840 keys)."""
     import lighttransportsimulation_gb300 as lts
     from lighttransportsimulation_gb300 import scenes
     from oracle import lbvh_np
@@ -90,6 +91,22 @@ def test_duplicate_codes_keep_stable_order(ctx):
     left, right = lbvh_np.karras_topology(codes)
     n = len(tris)
     assert np.array_equal(out["node_left"][: n - 1], left) and np.array_equal(out["node_right"][: n - 1], right)
+
+
+def test_rebuilds_reuse_the_arrival_words(ctx):
+    """Builds of different sizes in one context (the tree's arrival words are reused across builds
+    without clearing): every build's topology and boxes are those of a fresh build."""
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    from oracle import lbvh_np
+    for n, seed in ((70_001, 4), (4_097, 5), (70_001, 6), (70_001, 4)):
+        tris = scenes.random_triangles(n, seed=seed)
+        out = lts.build_bvh_triangles(ctx, tris, lts.BVH_SORTED)
+        codes, ids = lbvh_np.stable_sort(*lbvh_np.morton_codes(tris))
+        left, right = lbvh_np.karras_topology(codes)
+        assert np.array_equal(out["node_left"][: n - 1], left) and np.array_equal(out["node_right"][: n - 1], right)
+        mn, mx = lbvh_np.tri_bounds(tris)
+        lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"], np.concatenate([mn, mx], 1)[ids])
 
 
 def test_one_million_random_triangles(ctx):
