@@ -61,6 +61,28 @@ __device__ __forceinline__ void tri_bounds(const float* t, float mn[3], float mx
     }
 }
 
+// Box of triangle `prim` gathered from an array of n triangles (9 floats each).  With a 16-byte
+// aligned array, the 48-byte aligned window [floor16(36 prim), +48) always holds the triangle and
+// lies inside the array for prim <= n - 2, so three 16-byte loads replace nine 4-byte ones (a third
+// of the L1 wavefronts of a random gather); the last triangle and unaligned arrays load floats.
+__device__ __forceinline__ void gather_tri_bounds(const float* __restrict__ tri, int n, bool aligned16, int prim,
+                                                  float mn[3], float mx[3]) {
+    float t[9];
+    if (aligned16 && prim <= n - 2) {
+        const long f = 9L * prim;
+        const float4* w = reinterpret_cast<const float4*>(tri + (f & ~3L));
+        const float4 w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2);
+        const float v[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
+        const int sh = (int)(f & 3L);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) t[k] = sh == 0 ? v[k] : sh == 1 ? v[k + 1] : sh == 2 ? v[k + 2] : v[k + 3];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9L * prim + k);
+    }
+    tri_bounds(t, mn, mx);
+}
+
 // ------------------------------------------------------------------ 1. scene bounds
 __global__ __launch_bounds__(kBlock) void k_scene_bounds(const float* __restrict__ tri, int n,
                                                          uint32_t* __restrict__ gb) {
@@ -81,6 +103,8 @@ __global__ __launch_bounds__(kBlock) void k_scene_bounds(const float* __restrict
             }
         }
     }
+    // warp, then block reduction: one atomic per block and bound (same-address atomics serialise)
+    __shared__ uint32_t s_red[kBlock / 32][6];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         for (int o = 16; o > 0; o >>= 1) {
@@ -91,9 +115,17 @@ __global__ __launch_bounds__(kBlock) void k_scene_bounds(const float* __restrict
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            atomicMin(gb + k, kmn[k]);
-            atomicMax(gb + 3 + k, kmx[k]);
+            s_red[threadIdx.x >> 5][k] = kmn[k];
+            s_red[threadIdx.x >> 5][3 + k] = kmx[k];
         }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        uint32_t v = s_red[0][threadIdx.x];
+        for (int w = 1; w < kBlock / 32; ++w)
+            v = threadIdx.x < 3 ? min(v, s_red[w][threadIdx.x]) : max(v, s_red[w][threadIdx.x]);
+        if (threadIdx.x < 3) atomicMin(gb + threadIdx.x, v);
+        else atomicMax(gb + threadIdx.x, v);
     }
 }
 
@@ -444,31 +476,49 @@ __global__ __launch_bounds__(kTreeBlock, LTS_TREE_MIN_BLOCKS) void k_tree(const 
                                                      BvhNode* __restrict__ nodes, int32_t* __restrict__ pending,
                                                      uint32_t* __restrict__ pending_count, int32_t* __restrict__ leaf_prim,
                                                      float* __restrict__ root_bounds) {
+    // Slot g - b0 of a split g inside the block holds what its parent's record needs: both child
+    // boxes, both child references, the parent's range [far end of the left child, far end of the
+    // right child] and, once both children arrived, the parent's node index.  The climbs touch
+    // only shared memory (so the block-scope fences wait on nothing in flight to device memory);
+    // the records go out after the block's barrier, one 64-byte line per thread.
+    //   s_slot[slot][2 side + 0] = (min.x, min.y, min.z, max.x)      side 0: left child, 1: right
+    //   s_slot[slot][2 side + 1] = (max.y, max.z, reference, far end)
+    //   s_slot[slot][4]          = (parent index, arrival bits: 1 left, 2 right, -, -)
+    // Five 16-byte words per slot put eight consecutive slots in distinct bank groups.
+    // Children that meet across blocks are listed in shared memory first and appended to the
+    // device list with one atomic per block (a same-address atomic per child serialises): the
+    // climbs list at most two (the one node ending at the block's last leaf whose parent lies
+    // beyond, and the one starting at its first), the lone slots at most one each.
     __shared__ uint32_t s_code[kTreeBlock + 2];      // codes of positions b0-1 .. b0+kTreeBlock
-    __shared__ float s_box[2][6][kTreeBlock];        // [left/right child][min xyz, max xyz][g - b0]
-    __shared__ int s_ref[2][kTreeBlock], s_end[2][kTreeBlock];
-    __shared__ uint32_t s_have[kTreeBlock];          // bit 0 / 1: left / right child arrived
+    __shared__ float4 s_slot[kTreeBlock][5];
+    constexpr uint32_t kPendCap = kTreeBlock + 2;
+    __shared__ int32_t s_pend[kPendCap];
+    __shared__ uint32_t s_npend, s_pbase;
+    auto push = [&](int32_t r) {  // past the bound above (never, by the count) straight to the device list
+        const uint32_t i = atomicAdd(&s_npend, 1u);
+        if (i < kPendCap) s_pend[i] = r;
+        else pending[atomicAdd(pending_count, 1u)] = r;
+    };
     const int b0 = blockIdx.x * kTreeBlock, b1 = min(b0 + kTreeBlock, n) - 1;
     for (int k = threadIdx.x; k < kTreeBlock + 2; k += kTreeBlock) {
         const int pos = b0 - 1 + k;
         s_code[k] = (pos >= 0 && pos < n) ? __ldg(codes + pos) : 0u;
     }
-    s_have[threadIdx.x] = 0u;
+    s_slot[threadIdx.x][4] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (threadIdx.x == 0) s_npend = 0u;
     __syncthreads();
     auto sdelta = [&](int a, int b) -> int {  // delta of positions within [b0-1, b1+1]
         if (b < 0 || b >= n) return -1;
         return delta_codes(s_code[a - b0 + 1], s_code[b - b0 + 1], a, b);
     };
+    auto have_of = [&](int slot) -> uint32_t* { return reinterpret_cast<uint32_t*>(&s_slot[slot][4]) + 1; };
 
     const int l = b0 + threadIdx.x;
+    int prim = 0;
     if (l <= b1) {
-        const int prim = (mode == BVH_MODE_REFERENCE) ? l : __ldg(ids + l);
-        leaf_prim[l] = prim;
-        float t[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9L * prim + k);
+        prim = (mode == BVH_MODE_REFERENCE) ? l : __ldg(ids + l);
         float mn[3], mx[3];
-        tri_bounds(t, mn, mx);
+        gather_tri_bounds(tri, n, (reinterpret_cast<uintptr_t>(tri) & 15u) == 0, prim, mn, mx);
         if (n == 1) {
             put_root(root_bounds, mn, mx);
         } else {
@@ -478,50 +528,61 @@ __global__ __launch_bounds__(kTreeBlock, LTS_TREE_MIN_BLOCKS) void k_tree(const 
             // block-local climb
             for (;;) {
                 if (g < b0 || g + 1 > b1) {  // the parent reaches into another block
-                    pending[atomicAdd(pending_count, 1u)] = ref;
+                    push(ref);
                     break;
                 }
                 const int side = left ? 0 : 1, slot = g - b0;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    s_box[side][k][slot] = mn[k];
-                    s_box[side][3 + k][slot] = mx[k];
-                }
-                s_ref[side][slot] = ref;
-                s_end[side][slot] = left ? L : R;
+                s_slot[slot][2 * side] = make_float4(mn[0], mn[1], mn[2], mx[0]);
+                s_slot[slot][2 * side + 1] = make_float4(mx[1], mx[2], __int_as_float(ref), __int_as_float(left ? L : R));
                 __threadfence_block();
-                if (!(atomicOr(&s_have[slot], 1u << side) & (2u >> side))) break;  // first arrival stops
+                if (!(atomicOr(have_of(slot), 1u << side) & (2u >> side))) break;  // first arrival stops
                 __threadfence_block();
-                float smn[3], smx[3], cb[12];
+                const float4 e0 = s_slot[slot][2 * (side ^ 1)], e1 = s_slot[slot][2 * (side ^ 1) + 1];
+                const float smn[3] = {e0.x, e0.y, e0.z}, smx[3] = {e0.w, e1.x, e1.y};
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    smn[k] = s_box[side ^ 1][k][slot];
-                    smx[k] = s_box[side ^ 1][3 + k][slot];
+                for (int k = 0; k < 3; ++k) {  // bUnion(left, right), operands in that order
+                    mn[k] = left ? fminf(mn[k], smn[k]) : fminf(smn[k], mn[k]);
+                    mx[k] = left ? fmaxf(mx[k], smx[k]) : fmaxf(smx[k], mx[k]);
                 }
-                const int sref = s_ref[side ^ 1][slot], send = s_end[side ^ 1][slot];
-                pair_up(left, mn, mx, smn, smx, cb);
-                const int lref = left ? ref : sref, rref = left ? sref : ref;
-                if (left) R = send;
-                else L = send;
+                if (left) R = __float_as_int(e1.w);
+                else L = __float_as_int(e1.w);
+                int* idx = reinterpret_cast<int*>(&s_slot[slot][4]);
                 if (L == 0 && R == n - 1) {
-                    put_node(nodes, 0, cb, lref, rref, L, R);
+                    *idx = 0;
                     put_root(root_bounds, mn, mx);
                     break;
                 }
                 left = sdelta(R, R + 1) > sdelta(L, L - 1);
                 ref = left ? R : L;
-                put_node(nodes, ref, cb, lref, rref, L, R);
+                *idx = ref;
                 g = left ? R : L - 1;
             }
         }
     }
     __syncthreads();
-    // a child alone in its slot: the sibling reaches into another block
+    if (l <= b1) leaf_prim[l] = prim;
     const int slot = threadIdx.x;
     if (b0 + slot + 1 <= b1) {
-        const uint32_t have = s_have[slot];
-        if (have == 1u || have == 2u) pending[atomicAdd(pending_count, 1u)] = s_ref[have == 1u ? 0 : 1][slot];
+        const float4 w = s_slot[slot][4];
+        const uint32_t have = __float_as_uint(w.y);
+        if (have == 3u) {  // the record of the parent formed here
+            const float4 a0 = s_slot[slot][0], a1 = s_slot[slot][1], c0 = s_slot[slot][2], c1 = s_slot[slot][3];
+            float4* P = reinterpret_cast<float4*>(nodes + __float_as_int(w.x));
+            P[0] = a0;
+            P[1] = make_float4(a1.x, a1.y, c0.x, c0.y);
+            P[2] = make_float4(c0.z, c0.w, c1.x, c1.y);
+            reinterpret_cast<int4*>(P)[3] = make_int4(__float_as_int(a1.z), __float_as_int(c1.z), __float_as_int(a1.w),
+                                                      __float_as_int(c1.w));  // (left ref, right ref, lo, hi)
+        } else if (have != 0u) {  // a child alone: its sibling reaches into another block
+            push(__float_as_int(s_slot[slot][have == 1u ? 1 : 3].z));
+        }
     }
+    __syncthreads();
+    const uint32_t np = min(s_npend, kPendCap);
+    if (np == 0u) return;
+    if (threadIdx.x == 0) s_pbase = atomicAdd(pending_count, np);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < np; i += kTreeBlock) pending[s_pbase + i] = s_pend[i];
 }
 
 // Climbs from every child k_tree listed (at most 2n - 2 of them), grid-stride.
