@@ -222,6 +222,49 @@ def lbvh_bench(ctx, n, steps, warmup, mode, peaks):
             "frac_of_hbm": round(gbs / peaks["hbm_gbs"], 4)}
 
 
+MLP_FWD_FLOP = 2 * (96 * 64 + 4 * 64 * 64 + 64 * 3)  # per query: the six layers' products (3 outputs)
+MLP_TRAIN_FLOP = MLP_FWD_FLOP + 2 * (3 * 64 + 4 * 64 * 64) + MLP_FWD_FLOP  # + activation and weight gradients
+
+
+def mlp_bench(ctx, steps, warmup, peaks, queries=1920 * 1080, train_rows=65536):
+    """Device time of the radiance-cache network's inference over one film of queries (1920x1080,
+    the cache workload's resolution) and of one training step on 65,536 path-suffix samples (the
+    per-frame training set), through the device-pointer C-ABI on the context's stream.  Features:
+    seeded uniform [-1, 1) bf16 values; targets uniform (0, 1]."""
+    import torch
+
+    import lighttransportsimulation_gb300 as lts
+    g = torch.Generator(device="cuda").manual_seed(5)
+    feat = (torch.rand((queries, 96), generator=g, device="cuda") * 2 - 1).to(torch.bfloat16).view(torch.int16)
+    tfeat = feat[:train_rows].contiguous()
+    targ = torch.rand((train_rows, 3), generator=g, device="cuda") * 0.999 + 0.001
+    out = torch.empty((queries, 3), device="cuda")
+    loss = torch.zeros(1, device="cuda")
+    net = lts.RadianceCacheMLP(ctx, seed=7)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    torch.cuda.synchronize()
+    res = {}
+    for name, call, rows, flop in (
+            ("forward", lambda: net.forward_device_async(feat.data_ptr(), queries, out.data_ptr()), queries,
+             MLP_FWD_FLOP),
+            ("train", lambda: net.train_step_device_async(tfeat.data_ptr(), targ.data_ptr(), train_rows, 1e-3,
+                                                           loss.data_ptr()), train_rows, MLP_TRAIN_FLOP)):
+        for _ in range(warmup):
+            call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            call()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        tf = rows * flop / (ms * 1e-3) / 1e12
+        res[name] = {"rows": rows, "ms": round(ms, 4), "mrows_s": round(rows / (ms * 1e-3) / 1e6, 1),
+                     "flop_per_row": flop, "tflops": round(tf, 2), "frac_of_bf16": round(tf / peaks["bf16_tflops"], 4)}
+    res["train"]["loss"] = round(float(loss.item()), 6)
+    return res
+
+
 def profiled_traffic(kernel, workload, bvh_width):
     """DRAM bytes per launch of `kernel` from the committed ncu summary (dram__bytes_read.sum +
     dram__bytes_write.sum over every launch of one render, divided by the launches), or None."""
@@ -536,6 +579,8 @@ def main():
     ap.add_argument("--lbvh-only", type=int, default=0, metavar="N",
                     help="only time the LBVH build over N random triangles (seed 1)")
     ap.add_argument("--views64", action="store_true", help="64 batched uneven views (autotuned, with the cache)")
+    ap.add_argument("--mlp-only", action="store_true",
+                    help="radiance-cache network alone: inference over 1920x1080 queries, one 65,536-sample training step")
     ap.add_argument("--time-to-rmse", action="store_true",
                     help="time for the cached wavefront and the plain megakernel to reach --ttr-target RMSE")
     ap.add_argument("--ttr-target", type=float, default=1e-2)
@@ -557,6 +602,12 @@ def main():
         import lighttransportsimulation_gb300 as lts
         ctx = lts.Context(0)
         print(json.dumps(lbvh_bench(ctx, args.lbvh_only, args.steps, args.warmup, lts.BVH_SORTED, measured_peaks()[0])))
+        ctx.close()
+        return
+    if args.mlp_only:
+        import lighttransportsimulation_gb300 as lts
+        ctx = lts.Context(0)
+        print(json.dumps({"mlp": mlp_bench(ctx, args.steps, args.warmup, measured_peaks()[0])}))
         ctx.close()
         return
     if args.impl == "reference":

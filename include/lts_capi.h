@@ -257,6 +257,12 @@ int lts_mlp_forward(lts_ctx* ctx, const uint16_t* features, int32_t n, float* ou
  * gradient before the update; then one Adam step (beta1 0.9, beta2 0.99, eps 1e-8) when lr > 0. */
 int lts_mlp_train_step(lts_ctx* ctx, const uint16_t* features, const float* targets, int32_t n, float lr,
                        float* loss, float* grad);
+/* Device-pointer variants, enqueued on the context's stream (lts_stream) without synchronising:
+ * the inference and training passes the renderer runs on its own buffers, for callers whose
+ * features already live on the device.  d_loss: one device float (may be NULL for none). */
+int lts_mlp_forward_device_async(lts_ctx* ctx, const uint16_t* d_features, int32_t n, float* d_out_rgb);
+int lts_mlp_train_step_device_async(lts_ctx* ctx, const uint16_t* d_features, const float* d_targets, int32_t n,
+                                    float lr, float* d_loss);
 
 /* ---------------------------------------------------------------- metrics */
 typedef struct {

@@ -37,8 +37,8 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_bvh_build_device_async", "lts_bvh_dump_get", "lts_render", "lts_render_async", "lts_film_get",
            "lts_write_image", "lts_get_metrics", "lts_bvh_build_noalloc", "lts_debug_trace_sample",
            "lts_debug_trace_get", "lts_set_option", "lts_debug_umma_probe", "lts_mlp_init", "lts_mlp_set_params",
-           "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step", "lts_render_views",
-           "lts_autotune_views"]
+           "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step", "lts_mlp_forward_device_async",
+           "lts_mlp_train_step_device_async", "lts_render_views", "lts_autotune_views"]
 
 
 class LtsError(RuntimeError):
@@ -127,6 +127,8 @@ def library():
             "lts_mlp_get_params": (I, [P, P]),
             "lts_mlp_forward": (I, [P, P, I, P]),
             "lts_mlp_train_step": (I, [P, P, P, I, ctypes.c_float, P, P]),
+            "lts_mlp_forward_device_async": (I, [P, P, I, P]),
+            "lts_mlp_train_step_device_async": (I, [P, P, P, I, ctypes.c_float, P]),
             "lts_render_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P, ctypes.POINTER(RenderOut)]),
             "lts_autotune_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P]),
         }
@@ -353,6 +355,18 @@ class RadianceCacheMLP:
             self.ctx.h, f.ctypes.data_as(ctypes.c_void_p), t.ctypes.data_as(ctypes.c_void_p), f.shape[0],
             ctypes.c_float(lr), ctypes.byref(loss), g.ctypes.data_as(ctypes.c_void_p) if want_grad else None))
         return loss.value, g
+
+
+    def forward_device_async(self, d_features, n, d_out):
+        """Inference on device buffers (bf16 feature bits, FP32 RGB out), on the context's stream."""
+        self.ctx.check(self.ctx.lib.lts_mlp_forward_device_async(self.ctx.h, ctypes.c_void_p(d_features), int(n),
+                                                                 ctypes.c_void_p(d_out)))
+
+    def train_step_device_async(self, d_features, d_targets, n, lr, d_loss=None):
+        """One training pass (and Adam step when lr > 0) on device buffers, on the context's stream."""
+        self.ctx.check(self.ctx.lib.lts_mlp_train_step_device_async(
+            self.ctx.h, ctypes.c_void_p(d_features), ctypes.c_void_p(d_targets), int(n), ctypes.c_float(lr),
+            ctypes.c_void_p(d_loss) if d_loss else None))
 
 
 class View(ctypes.Structure):

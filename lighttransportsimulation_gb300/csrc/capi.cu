@@ -558,6 +558,23 @@ int lts_mlp_train_step(lts_ctx* ctx, const uint16_t* features, const float* targ
     return rc;
 }
 
+int lts_mlp_forward_device_async(lts_ctx* ctx, const uint16_t* d_features, int32_t n, float* d_out_rgb) {
+    if (int r = mlp_ready(ctx)) return r;
+    if (!d_features || !d_out_rgb || n < 0) return LTS_ERR_ARG;
+    if (n == 0) return LTS_OK;
+    const std::string e = ctx->mlp->forward(d_features, n, d_out_rgb, ctx->d_error, ctx->stream);
+    return e.empty() ? LTS_OK : fail(ctx, LTS_ERR_DEVICE, e);
+}
+
+int lts_mlp_train_step_device_async(lts_ctx* ctx, const uint16_t* d_features, const float* d_targets, int32_t n,
+                                    float lr, float* d_loss) {
+    if (int r = mlp_ready(ctx)) return r;
+    if (!d_features || !d_targets || n <= 0) return LTS_ERR_ARG;
+    float* dl = d_loss ? d_loss : ctx->mlp->scratch_loss();
+    const std::string e = ctx->mlp->train_step(d_features, d_targets, n, lr, dl, ctx->d_error, ctx->stream);
+    return e.empty() ? LTS_OK : fail(ctx, LTS_ERR_DEVICE, e);
+}
+
 int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
     if (!ctx || !key) return LTS_ERR_ARG;
     if (value < 0) return fail(ctx, LTS_ERR_ARG, "option value must be >= 0");

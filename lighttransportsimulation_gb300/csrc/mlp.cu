@@ -413,6 +413,7 @@ Mlp::~Mlp() {
     dev_free(m_);
     dev_free(v_);
     dev_free(w16_);
+    dev_free(loss_);
 }
 
 std::string Mlp::init(uint32_t seed, cudaStream_t s) {
@@ -422,6 +423,7 @@ std::string Mlp::init(uint32_t seed, cudaStream_t s) {
         TRY(dev_alloc((void**)&m_, 4 * kMlpParams));
         TRY(dev_alloc((void**)&v_, 4 * kMlpParams));
         TRY(dev_alloc((void**)&w16_, 2 * kMlpParams));
+        TRY(dev_alloc((void**)&loss_, 4));
         int dev = 0, sms = 0;
         TRY(cudaGetDevice(&dev));
         TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

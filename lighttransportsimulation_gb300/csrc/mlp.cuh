@@ -56,10 +56,11 @@ class Mlp {
     std::string adam(float lr, cudaStream_t s);
 
     bool ready() const { return w32_ != nullptr; }
+    float* scratch_loss() const { return loss_; }  // one device float for callers that drop the loss
     int steps = 0;
 
    private:
-    float *w32_ = nullptr, *grad_ = nullptr, *m_ = nullptr, *v_ = nullptr;
+    float *w32_ = nullptr, *grad_ = nullptr, *m_ = nullptr, *v_ = nullptr, *loss_ = nullptr;
     uint16_t* w16_ = nullptr;
     int blocks_train_ = 0, blocks_fwd_ = 0;
     std::string sync_bf16(cudaStream_t s);

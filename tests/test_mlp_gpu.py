@@ -114,3 +114,37 @@ def test_mlp_learns(ctx):
     print(f"loss {losses[0]:.4f} -> {losses[-1]:.5f}, held-out {held:.5f}")
     assert losses[-1] < losses[0] / 10
     assert held < 3 * losses[-1] + 1e-3
+
+
+def test_device_pointer_entry_points_match_host_ones(ctx):
+    """lts_mlp_forward_device_async / lts_mlp_train_step_device_async give the host entry points'
+    outputs, loss and updated parameters on the same data."""
+    import torch
+
+    import lighttransportsimulation_gb300 as lts
+    rng = np.random.default_rng(11)
+    n = 3000
+    feat = to_bf16_bits(rng.uniform(-1, 1, (n, 96)).astype(np.float32))
+    targ = rng.uniform(0.01, 1.0, (n, 3)).astype(np.float32)
+    net = lts.RadianceCacheMLP(ctx, seed=3)
+    p0 = net.params()
+    ref_out = net.forward(feat)
+    ref_loss, _ = net.train_step(feat, targ, 1e-3)
+    p_host = net.params()
+    net.set_params(p0)  # same weights, fresh Adam state
+    d_feat = torch.from_numpy(feat.view(np.int16)).cuda()
+    d_targ = torch.from_numpy(targ).cuda()
+    d_out = torch.empty((n, 3), device="cuda")
+    d_loss = torch.zeros(1, device="cuda")
+    torch.cuda.synchronize()
+    net.forward_device_async(d_feat.data_ptr(), n, d_out.data_ptr())
+    net.train_step_device_async(d_feat.data_ptr(), d_targ.data_ptr(), n, 1e-3, d_loss.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(d_out.cpu().numpy(), ref_out)  # inference: no atomics, bit-exact
+    # training sums the per-CTA gradients and losses with float atomics (order varies): the loss to
+    # 1e-5; Adam's first step moves each weight by ~lr * sign(g), so weights agree to float
+    # rounding except where a gradient is ~0 and its sign may differ (at most 2 lr apart)
+    assert d_loss.item() == pytest.approx(ref_loss, rel=1e-5)
+    p_dev = net.params()
+    assert np.mean(np.abs(p_dev - p_host) <= 1e-6) >= 0.999
+    assert np.max(np.abs(p_dev - p_host)) <= 2.1e-3
