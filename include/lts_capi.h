@@ -119,10 +119,11 @@ int lts_bvh_dump_get(lts_ctx* ctx, lts_bvh_dump* dump);
 /* No counterpart in the reference.  The same LBVH build for callers that may not allocate
  * device memory (memory-pool or allocator callbacks, real-time loops that forbid cudaMalloc,
  * plugins whose host owns every allocation): no context, no cudaMalloc/cudaFree, all scratch in
- * one fixed file-scope device array of about 5.3 MiB that each GPU loading the library keeps
+ * one fixed file-scope device array of about 3.3 MiB that each GPU loading the library keeps
  * until exit.  n <= LTS_NOALLOC_MAX_PRIMITIVES, else LTS_ERR_ARG.  The caller passes device
  * buffers: d_tri_p9 [9n floats], outputs d_sorted_codes [n], d_sorted_ids [n], d_nodes
- * [(n-1) x 64 bytes: left box, right box, children (>= 0 interior, < 0 leaf ~l)], d_leaf_prim
+ * [(n-1) x 64 bytes: left box, right box, children (>= 0 interior, < 0 leaf ~l), first and last
+ * leaf of the node's range], d_leaf_prim
  * [n], d_root_bounds [6].  Runs on `stream` (a cudaStream_t, NULL for the default stream) and
  * waits for it before returning.  The first call on a device looks up the array's address
  * (may load the module): make it before any stream capture.  Calls share the array, so calls
