@@ -54,8 +54,16 @@ typedef struct {
  * Replaces readApplicationParameters (core/FileIO.cuh:234-257). */
 int lts_read_app_params(const char* path, lts_app_params* out);
 
+/* Converts mesh_name + ".obj" to mesh_name + ".bin" (the loader's binary mesh layout).
+ * Replaces parseMeshFile + binMeshWrite (core/FileIO.cuh:20-45, 73-164): whitespace tokens,
+ * "v"/"vn" three floats, "vt" two, "f" three "p/uv/n" corners (uv index 0 until a "vt" has been
+ * read).  LTS_ERR_IO when a file cannot be opened or written, LTS_ERR_PARSE on input the
+ * reference's reader has no defined result for. */
+int lts_obj_to_bin(const char* mesh_name);
+
 /* Loads `root + scene + ".scene"` and optionally `root + subject + ".subject"` with their
- * `.bin` meshes, transforms subject meshes, builds the camera for a width x height film and
+ * meshes (`name.bin`, else `name.obj`, converted and also written to `name.bin` as the
+ * reference's parseMesh does, core/FileIO.cuh:213-232), transforms subject meshes, builds the camera for a width x height film and
  * the light table, and uploads SoA tables to the device.  subject may be NULL or "".
  * Replaces parseScene (core/SceneLoader.cuh:195-360) and the init kernels of
  * core/SceneLoader_kernels.cu:8-111.  Image textures ('i') are rejected with

@@ -38,7 +38,7 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_write_image", "lts_get_metrics", "lts_bvh_build_noalloc", "lts_debug_trace_sample",
            "lts_debug_trace_get", "lts_set_option", "lts_debug_umma_probe", "lts_mlp_init", "lts_mlp_set_params",
            "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step", "lts_mlp_forward_device_async",
-           "lts_mlp_train_step_device_async", "lts_render_views", "lts_autotune_views"]
+           "lts_mlp_train_step_device_async", "lts_render_views", "lts_autotune_views", "lts_obj_to_bin"]
 
 
 class LtsError(RuntimeError):
@@ -128,6 +128,7 @@ def library():
             "lts_mlp_forward": (I, [P, P, I, P]),
             "lts_mlp_train_step": (I, [P, P, P, I, ctypes.c_float, P, P]),
             "lts_mlp_forward_device_async": (I, [P, P, I, P]),
+            "lts_obj_to_bin": (I, [ctypes.c_char_p]),
             "lts_mlp_train_step_device_async": (I, [P, P, P, I, ctypes.c_float, P]),
             "lts_render_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P, ctypes.POINTER(RenderOut)]),
             "lts_autotune_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P]),
@@ -304,6 +305,13 @@ class PathTracingIntegrator:
         res["node_visits"] = o.node_visits
         res["tri_tests"] = o.tri_tests
         return res
+
+
+def obj_to_bin(mesh_name):
+    """mesh_name.obj -> mesh_name.bin in the reference's binary mesh layout (lts_obj_to_bin)."""
+    rc = library().lts_obj_to_bin(str(mesh_name).encode())
+    if rc != LTS_OK:
+        raise LtsError(rc, str(mesh_name))
 
 
 def write_image(path, rgb, fmt):

@@ -245,6 +245,13 @@ int lts_read_app_params(const char* path, lts_app_params* out) {
     return LTS_OK;
 }
 
+int lts_obj_to_bin(const char* mesh_name) {
+    if (!mesh_name) return LTS_ERR_ARG;
+    int code = LTS_OK;
+    obj_to_bin(mesh_name, &code);
+    return code;
+}
+
 int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char* subject, int32_t width,
                    int32_t height) {
     if (!ctx || !root || !scene) return fail(ctx, LTS_ERR_ARG, "null argument");

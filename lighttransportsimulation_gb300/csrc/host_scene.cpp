@@ -4,10 +4,15 @@
 // rendering/Filter.cuh, intergrators/IntegratorHelper.cuh, sampling/Sampling.cuh).
 #include "host_scene.hpp"
 
+#include <cctype>
+#include <cerrno>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <utility>
+#include <vector>
 
 #include "../../include/lts_capi.h"
 
@@ -136,7 +141,7 @@ struct MeshData {
 // core/FileIO.cuh:170-206 (binMeshRead), with size checks the reference does not make.
 MeshData read_bin(const std::string& path) {
     std::ifstream f(path, std::ios::binary);
-    if (!f.good()) throw ParseError{LTS_ERR_IO, "cannot open mesh " + path + " (.obj input is not supported)"};
+    if (!f.good()) throw ParseError{LTS_ERR_IO, "cannot open mesh " + path};
     f.seekg(0, std::ios::end);
     const long long size = (long long)f.tellg();
     f.seekg(0, std::ios::beg);
@@ -159,12 +164,142 @@ MeshData read_bin(const std::string& path) {
     f.read((char*)m.uv.data(), 8LL * m.nuv);
     f.read((char*)m.n.data(), 12LL * m.nn);
     f.read((char*)m.idx.data(), 36LL * m.ntri);
+    return m;
+}
+
+// Every corner's position index, and its uv / normal index when the mesh has any, in range (the
+// reference reads out of bounds otherwise).
+void check_indices(const MeshData& m, const std::string& name) {
     for (int32_t t = 0; t < m.ntri; ++t)
         for (int c = 0; c < 3; ++c) {
             const int32_t ip = m.idx[9 * t + 3 * c], iu = m.idx[9 * t + 3 * c + 1], in = m.idx[9 * t + 3 * c + 2];
             if (ip < 0 || ip >= m.np || (m.nuv > 0 && (iu < 0 || iu >= m.nuv)) || (m.nn > 0 && (in < 0 || in >= m.nn)))
-                throw ParseError{LTS_ERR_PARSE, "vertex index out of range in " + path};
+                throw ParseError{LTS_ERR_PARSE, "vertex index out of range in mesh " + name};
         }
+}
+
+// core/FileIO.cuh:73-164 (parseMeshFile): the whole file is read as whitespace-separated tokens
+// (no comment handling: a token of a comment or of an unknown statement is skipped like any other
+// token, so a "v" inside a comment still reads a vertex); "v" / "vn" take the next three tokens
+// and "vt" the next two as floats (std::stof: leading number of the token); "f" takes the next
+// three tokens as "p/uv/n" 1-based indices.  The uv index is read only once some "vt" has been
+// seen (0 before); an index field that does not start with a number keeps the value read last in
+// the same face corner (std::from_chars leaves its output unchanged on failure).  Where the
+// reference's behaviour is undefined (no number at all before the first field, fewer than three
+// fields, a token that stof rejects, missing tokens at the end) this reader raises a parse error.
+MeshData parse_obj(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f.good()) throw ParseError{LTS_ERR_IO, "cannot open mesh " + path + " (neither .bin nor .obj)"};
+    std::ostringstream ss;
+    ss << f.rdbuf();
+    const std::string text = ss.str();
+    size_t pos = 0;
+    auto next = [&](std::string& t) -> bool {  // operator>>(istream&, string&)
+        while (pos < text.size() && std::isspace((unsigned char)text[pos])) ++pos;
+        if (pos >= text.size()) return false;
+        const size_t b = pos;
+        while (pos < text.size() && !std::isspace((unsigned char)text[pos])) ++pos;
+        t.assign(text, b, pos - b);
+        return true;
+    };
+    auto num = [&](const char* what) -> float {
+        std::string t;
+        if (!next(t)) throw ParseError{LTS_ERR_PARSE, std::string("missing ") + what + " in " + path};
+        errno = 0;
+        char* end = nullptr;
+        const float v = std::strtof(t.c_str(), &end);
+        if (end == t.c_str() || errno == ERANGE)  // std::stof throws on both
+            throw ParseError{LTS_ERR_PARSE, "bad number '" + t + "' for " + what + " in " + path};
+        return v;
+    };
+    // std::from_chars(int) over [b, e): leading digits with an optional '-'; false leaves i as is
+    auto field = [](const char* b, const char* e, int& i) -> bool {
+        const char* q = b;
+        bool neg = false;
+        if (q < e && *q == '-') {
+            neg = true;
+            ++q;
+        }
+        if (q >= e || *q < '0' || *q > '9') return false;
+        long long v = 0;
+        for (; q < e && *q >= '0' && *q <= '9'; ++q) {
+            v = v * 10 + (*q - '0');
+            if (v > 2147483648LL) return false;  // out of range: from_chars reports an error
+        }
+        v = neg ? -v : v;
+        if (v > 2147483647LL || v < -2147483648LL) return false;
+        i = (int)v;
+        return true;
+    };
+    MeshData m;
+    std::string t;
+    while (next(t)) {
+        if (t == "v") {
+            for (int k = 0; k < 3; ++k) m.p.push_back(num("vertex"));
+        } else if (t == "vt") {
+            for (int k = 0; k < 2; ++k) m.uv.push_back(num("texture coordinate"));
+        } else if (t == "vn") {
+            for (int k = 0; k < 3; ++k) m.n.push_back(num("normal"));
+        } else if (t == "f") {
+            for (int c = 0; c < 3; ++c) {
+                std::string corner;
+                if (!next(corner)) throw ParseError{LTS_ERR_PARSE, "missing face corner in " + path};
+                std::vector<std::pair<size_t, size_t>> parts;  // FileIO.cuh:50-66 split on '/'
+                size_t b = 0;
+                for (;;) {
+                    const size_t e = corner.find('/', b);
+                    parts.emplace_back(b, (e == std::string::npos ? corner.size() : e) - b);
+                    if (e == std::string::npos) break;
+                    b = e + 1;
+                }
+                const bool with_uv = !m.uv.empty();
+                if (parts.size() < 3)
+                    throw ParseError{LTS_ERR_PARSE, "face corner '" + corner + "' is not p/uv/n in " + path};
+                const char* base = corner.data();
+                int i = 0;
+                if (!field(base + parts[0].first, base + parts[0].first + parts[0].second, i))
+                    throw ParseError{LTS_ERR_PARSE, "face corner '" + corner + "' has no vertex index in " + path};
+                m.idx.push_back(i - 1);
+                if (with_uv) {
+                    field(base + parts[1].first, base + parts[1].first + parts[1].second, i);
+                    m.idx.push_back(i - 1);
+                } else {
+                    m.idx.push_back(0);
+                }
+                field(base + parts[2].first, base + parts[2].first + parts[2].second, i);
+                m.idx.push_back(i - 1);
+            }
+            ++m.ntri;
+        }
+    }
+    m.np = (int32_t)(m.p.size() / 3);
+    m.nuv = (int32_t)(m.uv.size() / 2);
+    m.nn = (int32_t)(m.n.size() / 3);
+    return m;
+}
+
+// core/FileIO.cuh:20-45 (binMeshWrite): header nTri nP nUV nN, then P, UV, N, indices.
+bool write_bin(const std::string& path, const MeshData& m) {
+    std::ofstream f(path, std::ios::binary | std::ios::trunc);
+    if (!f.good()) return false;
+    const int32_t hdr[4] = {m.ntri, m.np, m.nuv, m.nn};
+    f.write((const char*)hdr, 16);
+    f.write((const char*)m.p.data(), 12LL * m.np);
+    f.write((const char*)m.uv.data(), 8LL * m.nuv);
+    f.write((const char*)m.n.data(), 12LL * m.nn);
+    f.write((const char*)m.idx.data(), 36LL * m.ntri);
+    return f.good();
+}
+
+// core/FileIO.cuh:213-232 (parseMesh): meshName.bin when it opens, else meshName.obj, whose
+// conversion is also written to meshName.bin (as the reference does; a failed write is ignored).
+MeshData read_mesh(const std::string& name) {
+    {
+        std::ifstream probe(name + ".bin", std::ios::binary);
+        if (probe.good()) return read_bin(name + ".bin");
+    }
+    MeshData m = parse_obj(name + ".obj");
+    write_bin(name + ".bin", m);
     return m;
 }
 
@@ -244,6 +379,21 @@ void HostScene::triangle_soup(std::vector<float>& out) const {
     for (int32_t t = 0; t < nt; ++t)
         for (int c = 0; c < 3; ++c)
             for (int k = 0; k < 3; ++k) out[9 * (size_t)t + 3 * c + k] = p[3 * (size_t)tri_p[3 * t + c] + k];
+}
+
+std::string obj_to_bin(const std::string& mesh_name, int* code) {
+    try {
+        const MeshData m = parse_obj(mesh_name + ".obj");
+        if (!write_bin(mesh_name + ".bin", m)) {
+            *code = LTS_ERR_IO;
+            return "cannot write " + mesh_name + ".bin";
+        }
+    } catch (const ParseError& e) {
+        *code = e.code;
+        return e.msg;
+    }
+    *code = LTS_OK;
+    return "";
 }
 
 std::string read_app_params(const std::string& path, AppParams* out, int* code) {
@@ -368,7 +518,8 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
         sc->mesh_first_tri.clear(); sc->mesh_tri_count.clear();
         const Xform ident;  // Transform(1)
         for (int m = 0; m < meshes; ++m) {
-            MeshData md = read_bin(files[m] + ".bin");
+            MeshData md = read_mesh(files[m]);
+            check_indices(md, files[m]);
             const Xform& X = m >= sub_meshes ? ident : subject_xf;
             const int32_t pbase = (int32_t)(sc->p.size() / 3), nbase = (int32_t)(sc->n.size() / 3),
                           uvbase = (int32_t)(sc->uv.size() / 2);

@@ -80,6 +80,8 @@ struct AppParams {
 
 // All return "" on success, else an error message; *code receives an LTS_ERR_* value.
 std::string read_app_params(const std::string& path, AppParams* out, int* code);
+// core/FileIO.cuh:73-164: mesh_name.obj -> mesh_name.bin in the reference's binary layout.
+std::string obj_to_bin(const std::string& mesh_name, int* code);
 std::string load_scene(const std::string& root, const std::string& scene, const std::string& subject,
                        int32_t width, int32_t height, HostScene* out, int* code);
 

@@ -9,6 +9,9 @@
  *       AABB of all 2N-1 nodes), world-space triangle vertices in primitive order, the camera
  *       (rendering/Camera.cu:9-43) and the light power distribution
  *       (intergrators/IntegratorHelper.cuh:147-162).
+ *   lts_ref image IN W H FORMAT OUT
+ *       writeToPPM (FORMAT 0) / writeToPFM (FORMAT 1) (core/ImageO.cuh:16-78), the writers of
+ *       Camera::sendRenderToImageFile (rendering/Camera.cu:250-253), on W x H x 3 raw floats.
  *   lts_ref render ROOT SCENE SUBJECT OUT W H SPP MAXB RR SEED X0 Y0 X1 Y1 THREADS FILM
  *       PathTracingIntegrator::evaluate (PathTracingIntegrator.cuh:26-109) over the pixel
  *       crop [X0,X1)x[Y0,Y1) -> per-(pixel, sample) radiance L and a 64-bit FNV-1a hash of the
@@ -243,9 +246,20 @@ static int cmd_render(int argc, char** argv) {
     return 0;
 }
 
+static int cmd_image(int argc, char** argv) {
+    if (argc < 7) return 2;
+    const int w = atoi(argv[3]), h = atoi(argv[4]), format = atoi(argv[5]);
+    std::vector<float> rgb((size_t)w * h * 3);
+    FILE* f = fopen(argv[2], "rb");
+    if (!f || fread(rgb.data(), sizeof(float), rgb.size(), f) != rgb.size()) return 3;
+    fclose(f);
+    const bool ok = format == 0 ? writeToPPM(argv[6], rgb.data(), w, h) : writeToPFM(argv[6], rgb.data(), w, h);
+    return ok ? 0 : 3;
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) {
-        fprintf(stderr, "usage: lts_ref bvh|render ...\n");
+        fprintf(stderr, "usage: lts_ref bvh|render|image ...\n");
         return 2;
     }
     std::cout.setstate(std::ios_base::failbit); /* silence the loader's banners */
@@ -253,6 +267,7 @@ int main(int argc, char** argv) {
     int rc = 2;
     if (c == "bvh") rc = cmd_bvh(argc, argv);
     if (c == "render") rc = cmd_render(argc, argv);
+    if (c == "image") rc = cmd_image(argc, argv);
     if (rc == 2) fprintf(stderr, "bad arguments\n");
     return rc;
 }
