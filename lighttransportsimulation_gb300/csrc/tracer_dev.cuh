@@ -387,6 +387,24 @@ __device__ __forceinline__ WideAxis wide_axis(real p, real o, real inv, uint32_t
 __device__ __forceinline__ real wide_byte(uint32_t lo, uint32_t hi, int s) {
     return __uint2float_rn(((s < 4 ? lo : hi) >> ((s & 3) * 8)) & 0xffu);
 }
+// Three-input min / max (one instruction on sm_100 and later: PTX ISA 8.8).
+__device__ __forceinline__ float fmax3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+// Bit s of an 8-bit child mask to bit s ^ oct (the ray's octant order).
+__device__ __forceinline__ uint32_t octant_order(uint32_t m, uint32_t oct) {
+    if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (oct & 4u) m = ((m & 0x0fu) << 4) | ((m >> 4) & 0x0fu);
+    return m;
+}
 
 // One node; returns true when the traversal has finished.
 __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const SceneView& sv, uint32_t* stack,
@@ -407,21 +425,25 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
         const WideAxis ax = wide_axis(h.x, t.r.o.x, t.r.inv.x, hb & 0xffu, t.r.neg[0], q0.x, q0.y, q1.z, q1.w);
         const WideAxis ay = wide_axis(h.y, t.r.o.y, t.r.inv.y, (hb >> 8) & 0xffu, t.r.neg[1], q0.z, q0.w, q2.x, q2.y);
         const WideAxis az = wide_axis(h.z, t.r.o.z, t.r.inv.z, (hb >> 16) & 0xffu, t.r.neg[2], q1.x, q1.y, q2.z, q2.w);
+        // every slot is tested (a warp runs a slot's test whenever any of its nodes has that
+        // slot) and the empty ones are masked off after; the interval is clipped to [0, tmax]
+        // and tested once, which also enters the boxes touching t = 0 or t = tmax exactly (a
+        // superset of the boxes the reference's test enters: the closest hit is unchanged)
+        uint32_t hit8 = 0;
 #pragma unroll
         for (int s = 0; s < 8; ++s) {
-            if (!((omask >> s) & 1u)) continue;
             const real tnx = xfma(wide_byte(ax.near_lo, ax.near_hi, s), ax.A, ax.Bn);
             const real tny = xfma(wide_byte(ay.near_lo, ay.near_hi, s), ay.A, ay.Bn);
             const real tnz = xfma(wide_byte(az.near_lo, az.near_hi, s), az.A, az.Bn);
             const real tfx = xfma(wide_byte(ax.far_lo, ax.far_hi, s), ax.Af, ax.Bf);
             const real tfy = xfma(wide_byte(ay.far_lo, ay.far_hi, s), ay.Af, ay.Bf);
             const real tfz = xfma(wide_byte(az.far_lo, az.far_hi, s), az.Af, az.Bf);
-            const real tn = xmax(xmax(tnx, tny), tnz), tf = xmin(xmin(tfx, tfy), tfz);
-            if (tn <= tf && tn < t.tmax && tf > 0.0f) {
-                if ((imask >> s) & 1u) hits |= 1u << ((uint32_t)s ^ oct);
-                else leaves |= 1u << s;
-            }
+            const real tn = fmax3f(tnx, tny, fmaxf(tnz, 0.0f)), tf = fmin3f(tfx, tfy, fminf(tfz, t.tmax));
+            hit8 |= (tn <= tf ? 1u : 0u) << s;
         }
+        hit8 &= omask;
+        leaves = hit8 & ~imask;
+        hits = octant_order(hit8 & imask, oct);
     } else {  // an axis-parallel ray: the reference's slab test on the decoded planes
         const real sx = wide_scale(hb & 0xffu), sy = wide_scale((hb >> 8) & 0xffu), sz = wide_scale((hb >> 16) & 0xffu);
 #pragma unroll
