@@ -84,7 +84,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                                si.sn.z, beta.r, beta.g, beta.b, L.r);
             if (bounce == 0 || specular) {
                 if (hit) {
-                    const int li = __ldg(sv.prim_light + si.prim);
+                    const int li = si.light;
                     if (li >= 0) {
                         const DevLight& Lt = sv.lights[li];
                         const Spec le = dot(si.n, -rd) > 0.f ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
@@ -197,7 +197,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                             if (RECORD) fnv_mix(sig, 0x200000000ull + (uint64_t)((found ? lit.prim : -1) + 1));
                             Spec Li = spec(0.0f);
                             if (found) {
-                                if (__ldg(sv.prim_light + lit.prim) == off && Lt.kind == 0)
+                                if (lit.light == off && Lt.kind == 0)
                                     Li = dot(lit.n, -wi) > 0.f ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
                             } else {
                                 Li = Lt.kind == 1 ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);

@@ -54,6 +54,36 @@ __global__ void k_resolve(const double* __restrict__ film, float* __restrict__ r
     }
 }
 
+// Shading record of each scene triangle (layout: SceneView::prim_rec) from the loader's
+// per-triangle corner indices: positions, uvs or the defaults (0,0) (1,0) (1,1)
+// (Triangle.cu:137-143), vertex normals or zeros, and (has normals, mesh, area light, 0).
+__global__ void k_build_prim_rec(const float4* __restrict__ prim_v, const int4* __restrict__ prim_n,
+                                 const int4* __restrict__ prim_uv, const float* __restrict__ normals,
+                                 const float* __restrict__ uvs, const int32_t* __restrict__ prim_light, int nt,
+                                 float4* __restrict__ rec) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int4 ni = prim_n[t], ui = prim_uv[t];
+    float uv[6] = {0.f, 0.f, 1.f, 0.f, 1.f, 1.f};
+    if (ui.x >= 0) {
+        const int u3[3] = {ui.x, ui.y, ui.z};
+        for (int c = 0; c < 3; ++c) {
+            uv[2 * c] = uvs[2 * u3[c]];
+            uv[2 * c + 1] = uvs[2 * u3[c] + 1];
+        }
+    }
+    float4* r = rec + 8 * (size_t)t;
+    const int n3[3] = {ni.x, ni.y, ni.z};
+    for (int c = 0; c < 3; ++c) {
+        const float4 q = prim_v[3 * (size_t)t + c];
+        r[c] = make_float4(q.x, q.y, q.z, uv[c]);
+        r[3 + c] = ni.x >= 0 ? make_float4(normals[3 * n3[c]], normals[3 * n3[c] + 1], normals[3 * n3[c] + 2], uv[3 + c])
+                             : make_float4(0.f, 0.f, 0.f, uv[3 + c]);
+    }
+    reinterpret_cast<int4*>(r)[6] = make_int4(ni.x >= 0 ? 1 : 0, ni.w, prim_light[t], 0);
+    r[7] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 __global__ void k_gather_leaves(const float4* __restrict__ prim_v, const int32_t* __restrict__ leaf_prim, int n,
                                 float4* __restrict__ leaf_v) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
@@ -225,11 +255,19 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
     std::vector<float> filt(sc.filter, sc.filter + 256);
     std::string e;
     if (!(e = upload(bufs_[0], pv, s)).empty()) return e;
-    if (!(e = upload(bufs_[1], pn, s)).empty()) return e;
-    if (!(e = upload(bufs_[2], puv, s)).empty()) return e;
-    if (!(e = upload(bufs_[3], sc.n, s)).empty()) return e;
-    if (!(e = upload(bufs_[4], sc.uv, s)).empty()) return e;
-    if (!(e = upload(bufs_[5], sc.prim_light, s)).empty()) return e;
+    // compact per-triangle indices up, shading records built on the device
+    if (!(e = upload(bufs_[2], pn, s)).empty()) return e;
+    if (!(e = upload(bufs_[3], puv, s)).empty()) return e;
+    if (!(e = upload(bufs_[4], sc.n, s)).empty()) return e;
+    if (!(e = upload(bufs_[5], sc.uv, s)).empty()) return e;
+    if (!(e = upload(bufs_[11], sc.prim_light, s)).empty()) return e;
+    TRY(dev_alloc(&bufs_[1], 128 * (size_t)(nt > 0 ? nt : 1)));
+    if (nt > 0)
+        k_build_prim_rec<<<(nt + 255) / 256, 256, 0, s>>>((const float4*)bufs_[0], (const int4*)bufs_[2],
+                                                          (const int4*)bufs_[3], (const float*)bufs_[4],
+                                                          (const float*)bufs_[5], (const int32_t*)bufs_[11], nt,
+                                                          (float4*)bufs_[1]);
+    TRY(cudaGetLastError());
     if (!(e = upload(bufs_[6], mats, s)).empty()) return e;
     if (!(e = upload(bufs_[7], lights, s)).empty()) return e;
     if (!(e = upload(bufs_[8], sc.light_func, s)).empty()) return e;
@@ -242,11 +280,7 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
     view_.width = sc.width;
     view_.height = sc.height;
     view_.prim_v = (const float4*)bufs_[0];
-    view_.prim_n = (const int4*)bufs_[1];
-    view_.prim_uv = (const int4*)bufs_[2];
-    view_.normals = (const float*)bufs_[3];
-    view_.uvs = (const float*)bufs_[4];
-    view_.prim_light = (const int32_t*)bufs_[5];
+    view_.prim_rec = (const float4*)bufs_[1];
     view_.mats = (const DevMat*)bufs_[6];
     view_.lights = (const DevLight*)bufs_[7];
     view_.light_func = (const float*)bufs_[8];

@@ -35,11 +35,14 @@ struct SceneView {
     int32_t ntri, nlight, width, height, has_normals_any;
     const float4* __restrict__ leaf_v;   // [3 ntri] triangle of leaf l: p0 (w = prim id bits), p1, p2
     const float4* __restrict__ prim_v;   // [3 ntri] scene order
-    const int4* __restrict__ prim_n;     // [ntri] normal indices (-1: none), w = mesh (= material) index
-    const int4* __restrict__ prim_uv;    // [ntri] uv indices (-1: none)
-    const float* __restrict__ normals;   // [3 nn]
-    const float* __restrict__ uvs;       // [2 nuv]
-    const int32_t* __restrict__ prim_light;
+    // [8 ntri] shading record of each scene triangle, one 128-byte line (what a hit reads):
+    //   [0] p0.xyz uv0.x  [1] p1.xyz uv0.y  [2] p2.xyz uv1.x
+    //   [3] n0.xyz uv1.y  [4] n1.xyz uv2.x  [5] n2.xyz uv2.y
+    //   [6] int bits: has vertex normals, mesh (= material) index, area-light index (-1: none), 0
+    //   [7] unused
+    // uvs are the mesh's, or (0,0) (1,0) (1,1) when it has none (Triangle.cu:137-143); normals
+    // are zero when the mesh has none.
+    const float4* __restrict__ prim_rec;
     const DevMat* __restrict__ mats;
     const DevLight* __restrict__ lights;
     const float* __restrict__ light_func;

@@ -139,8 +139,9 @@ __device__ __forceinline__ void prim_tri(const SceneView& sv, int prim, V3& p0, 
     p1 = f4v(__ldg(sv.prim_v + 3 * prim + 1));
     p2 = f4v(__ldg(sv.prim_v + 3 * prim + 2));
 }
-__device__ __forceinline__ V3 normal_at(const SceneView& sv, int idx) {
-    return v3(__ldg(sv.normals + 3 * idx), __ldg(sv.normals + 3 * idx + 1), __ldg(sv.normals + 3 * idx + 2));
+// The shading-record word of a triangle: (has vertex normals, mesh, area-light index, 0).
+__device__ __forceinline__ int4 prim_word(const SceneView& sv, int prim) {
+    return __ldg(reinterpret_cast<const int4*>(sv.prim_rec) + 8 * (size_t)prim + 6);
 }
 
 // ------------------------------------------------------------------ triangle tests
@@ -190,6 +191,7 @@ struct SI {
     V3 sn, sdpdu;       // shading normal and tangent
     V3 dpdx, dpdy;      // computeDifferentials
     int prim;
+    int mesh, light;    // material index, area-light index (-1: none) of the primitive
 };
 
 __device__ __forceinline__ void coordinate_system(V3 v1, V3& v2, V3& v3o) {
@@ -203,17 +205,17 @@ __device__ __forceinline__ void coordinate_system(V3 v1, V3& v2, V3& v3o) {
 
 // Builds the SurfaceInteraction of a hit (Triangle.cu:128-199 and the SurfaceInteraction
 // constructor, geometry/Interaction.cuh:85-116).
-__device__ void make_si(const SceneView& sv, int prim, V3 p0, V3 p1, V3 p2, V3 d, real u, real v, real inv,
-                        SI& si) {
+// Triangle::intersect's SurfaceInteraction (shapes/Triangle.cu:130-203) from the triangle's
+// shading record: positions, uvs (or the defaults) and vertex normals in one 128-byte line.
+__device__ void make_si(const SceneView& sv, int prim, V3 d, real u, real v, real inv, SI& si) {
+    const float4* rec = sv.prim_rec + 8 * (size_t)prim;
+    const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2);
+    const float4 r3 = __ldg(rec + 3), r4 = __ldg(rec + 4), r5 = __ldg(rec + 5);
+    const int4 word = __ldg(reinterpret_cast<const int4*>(rec) + 6);
+    const V3 p0 = v3(r0.x, r0.y, r0.z), p1 = v3(r1.x, r1.y, r1.z), p2 = v3(r2.x, r2.y, r2.z);
     const real w = 1 - u - v;
     const V3 e1 = p1 - p0, e2 = p2 - p0;
-    const int4 uvi = __ldg(sv.prim_uv + prim);
-    real uv0x = 0, uv0y = 0, uv1x = 1, uv1y = 0, uv2x = 1, uv2y = 1;
-    if (uvi.x >= 0) {
-        uv0x = __ldg(sv.uvs + 2 * uvi.x); uv0y = __ldg(sv.uvs + 2 * uvi.x + 1);
-        uv1x = __ldg(sv.uvs + 2 * uvi.y); uv1y = __ldg(sv.uvs + 2 * uvi.y + 1);
-        uv2x = __ldg(sv.uvs + 2 * uvi.z); uv2y = __ldg(sv.uvs + 2 * uvi.z + 1);
-    }
+    const real uv0x = r0.w, uv0y = r1.w, uv1x = r2.w, uv1y = r3.w, uv2x = r4.w, uv2y = r5.w;
     const real d02x = uv0x - uv2x, d02y = uv0y - uv2y, d12x = uv1x - uv2x, d12y = uv1y - uv2y;
     const V3 dp02 = p0 - p2, dp12 = p1 - p2;
     const real determinant = d02x * d12y - d02y * d12x;
@@ -237,9 +239,10 @@ __device__ void make_si(const SceneView& sv, int prim, V3 p0, V3 p1, V3 p2, V3 d
     si.sn = si.n;
     si.sdpdu = dpdu;
     si.prim = prim;
-    const int4 ni = __ldg(sv.prim_n + prim);
-    if (ni.x >= 0) {
-        const V3 n0 = normal_at(sv, ni.x), n1 = normal_at(sv, ni.y), n2 = normal_at(sv, ni.z);
+    si.mesh = word.y;
+    si.light = word.z;
+    if (word.x) {
+        const V3 n0 = v3(r3.x, r3.y, r3.z), n1 = v3(r4.x, r4.y, r4.z), n2 = v3(r5.x, r5.y, r5.z);
         const V3 ns = normalize(n0 * w + n1 * u + n2 * v);
         V3 ss = si.dpdu;
         V3 ts = cross(ns, ss);
@@ -583,9 +586,7 @@ __device__ __forceinline__ bool scene_intersect(const SceneView& sv, int nleaf, 
     real bu = 0, bv = 0, binv = 0;
     const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk);
     if (prim < 0) return false;
-    V3 p0, p1, p2;
-    prim_tri(sv, prim, p0, p1, p2);
-    make_si(sv, prim, p0, p1, p2, d, bu, bv, binv, si);
+    make_si(sv, prim, d, bu, bv, binv, si);
     return true;
 }
 __device__ __forceinline__ bool scene_occluded(const SceneView& sv, int nleaf, V3 o, V3 d, real tmax, uint32_t* stack,
@@ -1007,7 +1008,7 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, real& pdf, uin
 // Material::computeScatteringFunctions (materials/Material.cuh:31-130) into a Bsdf record.
 // Returns false when the primitive has no material (the reference's skipped 'M' entries).
 __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* sig) {
-    const int mesh = __ldg(&sv.prim_n[si.prim].w);
+    const int mesh = si.mesh;
     const DevMat& m = sv.mats[mesh];
     if (m.kind == 0) return false;
     f.ns = si.sn;
@@ -1085,7 +1086,7 @@ __device__ real area_pdf(const SceneView& sv, const DevLight& L, V3 p, V3 perr, 
     real t, u, v, inv;
     if (!tri_test(p0, p1, p2, o, wi, INFINITY, t, u, v, inv)) return 0;
     SI is;
-    make_si(sv, L.prim, p0, p1, p2, wi, u, v, inv, is);
+    make_si(sv, L.prim, wi, u, v, inv, is);
     const V3 dpt = p - is.p;
     return len2(dpt) / (absdot(is.n, -wi) * L.area);
 }
@@ -1103,10 +1104,11 @@ __device__ bool sample_li(const SceneView& sv, const DevLight& L, const SI& si, 
         const real b2 = 1 - b0 - b1;
         const V3 ps = p0 * b0 + p1 * b1 + p2 * b2;
         V3 ns;
-        const int4 ni = __ldg(sv.prim_n + L.prim);
-        if (ni.x >= 0)
-            ns = normalize(normal_at(sv, ni.x) * b0 + normal_at(sv, ni.y) * b1 + normal_at(sv, ni.z) * b2);
-        else
+        if (prim_word(sv, L.prim).x) {
+            const float4* rec = sv.prim_rec + 8 * (size_t)L.prim;
+            const float4 n0 = __ldg(rec + 3), n1 = __ldg(rec + 4), n2 = __ldg(rec + 5);
+            ns = normalize(v3(n0.x, n0.y, n0.z) * b0 + v3(n1.x, n1.y, n1.z) * b1 + v3(n2.x, n2.y, n2.z) * b2);
+        } else
             ns = normalize(cross(p1 - p0, p2 - p0));
         const V3 pabs = vabs(p0 * b0) + vabs(p1 * b1) + vabs(p2 * b2);
         ls.perr1 = pabs * gamma_n(6);

@@ -241,26 +241,24 @@ __device__ __forceinline__ void wf_ray_end(int kind, const Trav& t, const SceneV
     } else if (kind == TR_SHADOW) {
         st.vis[p] = t.best == 1 ? 0u : 1u;
     } else {
-        const float4 d = st.mis_d[p], fv = st.mis_fv[p], x = st.mis_x[p];
-        const V3 wi = v3(d.x, d.y, d.z);
+        // Landing on the sampled area light needs the surface at the hit (its normal faces the
+        // ray?): that evaluation is left to finalize (ld_mis.w = 2, xyz = barycentrics and inv),
+        // which has the registers for it; here only the light index of the hit is read.
+        const float4 x = st.mis_x[p];
         const int off = __float_as_int(x.y);
         const DevLight& Lt = sv.lights[off];
         const bool found = t.best >= 0;
-        Spec Li = spec(0.0f);
         if (found) {
-            SI lit;
-            V3 p0, p1, p2;
-            prim_tri(sv, t.best, p0, p1, p2);
-            make_si(sv, t.best, p0, p1, p2, wi, t.bu, t.bv, t.binv, lit);
-            if (__ldg(sv.prim_light + lit.prim) == off && Lt.kind == 0)
-                Li = dot(lit.n, -wi) > 0.f ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
+            const bool on_light = prim_word(sv, t.best).z == off && Lt.kind == 0;
+            st.ld_mis[p] = on_light ? make_float4(t.bu, t.bv, t.binv, 2.f) : make_float4(0.f, 0.f, 0.f, 0.f);
         } else {
-            Li = Lt.kind == 1 ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
+            const float4 fv = st.mis_fv[p];
+            const Spec Li = Lt.kind == 1 ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
+            Spec c = spec(0.0f);
+            const bool add = !is_black(Li);
+            if (add) c = Spec{fv.x, fv.y, fv.z} * Li * spec(1.0f) * fv.w / x.x;
+            st.ld_mis[p] = make_float4(c.r, c.g, c.b, add ? 1.f : 0.f);
         }
-        Spec c = spec(0.0f);
-        const bool add = !is_black(Li);
-        if (add) c = Spec{fv.x, fv.y, fv.z} * Li * spec(1.0f) * fv.w / x.x;
-        st.ld_mis[p] = make_float4(c.r, c.g, c.b, add ? 1.f : 0.f);
         st.mis_hit[p] = found ? t.best + 1 : 0;
     }
 }
@@ -363,7 +361,7 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_classify(const SceneView sv, Wf
     if (t >= (int)ctl->n_ext) return;
     const int p = q[t];
     const int prim = st.hprim[p];
-    const int c = prim < 0 ? 0 : sv.mats[__ldg(&sv.prim_n[prim].w)].shade_class;
+    const int c = prim < 0 ? 0 : sv.mats[prim_word(sv, prim).y].shade_class;
     const unsigned grp = __match_any_sync(__activemask(), c);
     const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
     uint32_t base = 0;
@@ -415,13 +413,11 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
     SI si;
     if (hit) {
         const float4 h = st.huvi[p];
-        V3 p0, p1, p2;
-        prim_tri(sv, prim, p0, p1, p2);
-        make_si(sv, prim, p0, p1, p2, rd, h.x, h.y, h.z, si);
+        make_si(sv, prim, rd, h.x, h.y, h.z, si);
     }
     if (bounce == 0 || specular) {
         if (hit) {
-            const int li = __ldg(sv.prim_light + prim);
+            const int li = si.light;
             if (li >= 0) {
                 const DevLight& Lt = sv.lights[li];
                 const Spec le = dot(si.n, -rd) > 0.f ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
@@ -627,7 +623,19 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
         if (RECORD && st.ev_mis[p]) fnv_mix(sig, st.ev_mis[p]);
         if (pend & WF_MIS) {
             if (RECORD) fnv_mix(sig, 0x200000000ull + (uint64_t)st.mis_hit[p]);
-            const float4 c = st.ld_mis[p];
+            float4 c = st.ld_mis[p];
+            if (c.w == 2.f) {  // the BSDF ray landed on the sampled area light (IntegratorHelper.cuh:225-243)
+                const float4 d = st.mis_d[p], fv = st.mis_fv[p], x = st.mis_x[p];
+                const V3 wi = v3(d.x, d.y, d.z);
+                const DevLight& Lt = sv.lights[__float_as_int(x.y)];
+                SI lit;
+                make_si(sv, st.mis_hit[p] - 1, wi, c.x, c.y, c.z, lit);
+                const Spec Li = dot(lit.n, -wi) > 0.f ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
+                Spec cs = spec(0.0f);
+                const bool add = !is_black(Li);
+                if (add) cs = Spec{fv.x, fv.y, fv.z} * Li * spec(1.0f) * fv.w / x.x;
+                c = make_float4(cs.r, cs.g, cs.b, add ? 1.f : 0.f);
+            }
             if (c.w != 0.f) Ld = Ld + Spec{c.x, c.y, c.z};
         }
         const float4 nb = st.nee_beta[p];
