@@ -333,6 +333,7 @@ struct Trav {
     int best;  // closest: primitive (-1 none); any: 1 on a hit
     int node, sp;
     uint32_t gbase, gbits;
+    uint32_t lbits, lbase;  // split steps: pending leaf slots (bits 0-7) | leaf-slot mask << 8, first triangle
 };
 
 // Returns true when the ray needs traversal steps; false when it is already resolved (missed
@@ -347,6 +348,8 @@ __device__ __forceinline__ bool trav_begin(const bool any, Trav& t, const SceneV
     t.sp = 0;
     t.gbase = 0;
     t.gbits = 0;
+    t.lbits = 0;
+    t.lbase = 0;
     real te;
     const float* rb = sv.root_bounds;
     if (!slab(t.r, t.tmax, __ldg(rb), __ldg(rb + 1), __ldg(rb + 2), __ldg(rb + 3), __ldg(rb + 4), __ldg(rb + 5), te))
@@ -503,6 +506,117 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
     const uint32_t s = p ^ oct;
     t.node = (int)t.gbase + __popc((t.gbits >> 8) & ((1u << s) - 1u));
     return false;
+}
+
+// The same node visit split in two (the wavefront trace kernel): wide_node_step tests the child
+// boxes and leaves the node's hit leaves pending in t.lbits instead of testing them; then
+// wide_leaf_step tests them one triangle per call before the next node step.  Per ray the order
+// of box and triangle tests is trav_step_wide's, so the hits are the same; a warp can run the
+// triangle tests of all its lanes together instead of inside divergent node steps.  Both
+// return true when the traversal has finished.
+__device__ __forceinline__ bool wide_node_step(const bool any, Trav& t, const SceneView& sv, uint32_t* stack,
+                                               uint32_t* err, Work& wk) {
+    if ((unsigned)t.node >= (unsigned)sv.wcount) {
+        atomicOr(err, DEV_ERR_BAD_INDEX);
+        return true;
+    }
+    const uint32_t oct = (t.r.neg[0] ? 1u : 0u) | (t.r.neg[1] ? 2u : 0u) | (t.r.neg[2] ? 4u : 0u);
+    const WideNode* nd = sv.wnodes + t.node;
+    const float4 h = __ldg(&nd->h);
+    const uint4 m = __ldg(&nd->m), q0 = __ldg(&nd->q0), q1 = __ldg(&nd->q1), q2 = __ldg(&nd->q2);
+    ++wk.nodes;
+    const uint32_t hb = __float_as_uint(h.w);
+    const uint32_t imask = hb >> 24, omask = m.z;
+    uint32_t hits = 0, leaves = 0;
+    if (isfinite(t.r.inv.x) && isfinite(t.r.inv.y) && isfinite(t.r.inv.z)) {
+        const WideAxis ax = wide_axis(h.x, t.r.o.x, t.r.inv.x, hb & 0xffu, t.r.neg[0], q0.x, q0.y, q1.z, q1.w);
+        const WideAxis ay = wide_axis(h.y, t.r.o.y, t.r.inv.y, (hb >> 8) & 0xffu, t.r.neg[1], q0.z, q0.w, q2.x, q2.y);
+        const WideAxis az = wide_axis(h.z, t.r.o.z, t.r.inv.z, (hb >> 16) & 0xffu, t.r.neg[2], q1.x, q1.y, q2.z, q2.w);
+        // every slot is tested (a warp runs a slot's test whenever any of its nodes has that
+        // slot) and the empty ones are masked off after; the interval is clipped to [0, tmax]
+        // and tested once, which also enters the boxes touching t = 0 or t = tmax exactly (a
+        // superset of the boxes the reference's test enters: the closest hit is unchanged)
+        uint32_t hit8 = 0;
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const real tnx = xfma(wide_byte(ax.near_lo, ax.near_hi, s), ax.A, ax.Bn);
+            const real tny = xfma(wide_byte(ay.near_lo, ay.near_hi, s), ay.A, ay.Bn);
+            const real tnz = xfma(wide_byte(az.near_lo, az.near_hi, s), az.A, az.Bn);
+            const real tfx = xfma(wide_byte(ax.far_lo, ax.far_hi, s), ax.Af, ax.Bf);
+            const real tfy = xfma(wide_byte(ay.far_lo, ay.far_hi, s), ay.Af, ay.Bf);
+            const real tfz = xfma(wide_byte(az.far_lo, az.far_hi, s), az.Af, az.Bf);
+            const real tn = fmax3f(tnx, tny, fmaxf(tnz, 0.0f)), tf = fmin3f(tfx, tfy, fminf(tfz, t.tmax));
+            hit8 |= (tn <= tf ? 1u : 0u) << s;
+        }
+        hit8 &= omask;
+        leaves = hit8 & ~imask;
+        hits = octant_order(hit8 & imask, oct);
+    } else {  // an axis-parallel ray: the reference's slab test on the decoded planes
+        const real sx = wide_scale(hb & 0xffu), sy = wide_scale((hb >> 8) & 0xffu), sz = wide_scale((hb >> 16) & 0xffu);
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            if (!((omask >> s) & 1u)) continue;
+            const int sh = (s & 3) * 8;
+            const uint32_t lx = ((s < 4 ? q0.x : q0.y) >> sh) & 0xffu, ly = ((s < 4 ? q0.z : q0.w) >> sh) & 0xffu;
+            const uint32_t lz = ((s < 4 ? q1.x : q1.y) >> sh) & 0xffu, hx = ((s < 4 ? q1.z : q1.w) >> sh) & 0xffu;
+            const uint32_t hy = ((s < 4 ? q2.x : q2.y) >> sh) & 0xffu, hz = ((s < 4 ? q2.z : q2.w) >> sh) & 0xffu;
+            real te;
+            if (slab(t.r, t.tmax, wide_plane(h.x, lx, sx), wide_plane(h.y, ly, sy), wide_plane(h.z, lz, sz),
+                     wide_plane(h.x, hx, sx), wide_plane(h.y, hy, sy), wide_plane(h.z, hz, sz), te)) {
+                if ((imask >> s) & 1u) hits |= 1u << ((uint32_t)s ^ oct);
+                else leaves |= 1u << s;
+            }
+        }
+    }
+    if (leaves) {
+        t.lbits = leaves | ((omask & ~imask) << 8);
+        t.lbase = m.y;
+    }
+    if (hits) {
+        if (t.gbits & 0xffu) {
+            if (2 * t.sp + 1 >= kStack) {
+                atomicOr(err, DEV_ERR_STACK_OVERFLOW);
+                return true;
+            }
+            stack[(2 * t.sp) * kThreads] = t.gbase;
+            stack[(2 * t.sp + 1) * kThreads] = t.gbits;
+            ++t.sp;
+        }
+        t.gbase = m.x;
+        t.gbits = hits | (imask << 8);
+    }
+    if (!(t.gbits & 0xffu)) {
+        if (t.sp == 0) {  // no node left: done unless leaves are pending
+            t.node = -1;
+            return t.lbits == 0u;
+        }
+        --t.sp;
+        t.gbase = stack[(2 * t.sp) * kThreads];
+        t.gbits = stack[(2 * t.sp + 1) * kThreads];
+    }
+    const uint32_t p = (uint32_t)__ffs(t.gbits & 0xffu) - 1u;
+    t.gbits &= ~(1u << p);
+    const uint32_t s = p ^ oct;
+    t.node = (int)t.gbase + __popc((t.gbits >> 8) & ((1u << s) - 1u));
+    return false;
+}
+
+
+__device__ __forceinline__ bool wide_leaf_step(const bool any, Trav& t, const SceneView& sv, uint32_t* err, Work& wk) {
+    const int s = __ffs(t.lbits & 0xffu) - 1;
+    const int tri = (int)t.lbase + __popc((t.lbits >> 8) & ((1u << s) - 1u));
+    t.lbits &= ~(1u << s);
+    if ((unsigned)tri >= (unsigned)sv.ntri) {
+        atomicOr(err, DEV_ERR_BAD_INDEX);
+        return true;
+    }
+    ++wk.tris;
+    if (leaf_test(any, sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+        t.best = 1;
+        return true;
+    }
+    if (!(t.lbits & 0xffu)) t.lbits = 0u;
+    return t.lbits == 0u && t.node < 0;
 }
 
 #endif  // !LTS_FP64

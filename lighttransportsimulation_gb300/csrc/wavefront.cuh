@@ -266,6 +266,10 @@ __device__ __forceinline__ void wf_ray_end(int kind, const Trav& t, const SceneV
 // Lanes left idle before a warp fetches new rays (while the lists last).
 constexpr int kRefillIdle = 8;
 // Resident blocks per SM the trace kernel is compiled for (caps its registers).
+#ifndef LTS_LEAF_BIAS
+#define LTS_LEAF_BIAS 1  // leaf steps when lanes with pending leaves x 4 >= lanes due a node x this
+#endif
+constexpr int kLeafBias = LTS_LEAF_BIAS;
 #ifndef LTS_TRACE_MIN_BLOCKS
 #define LTS_TRACE_MIN_BLOCKS 7
 #endif
@@ -334,14 +338,26 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
             continue;
         }
         for (;;) {
-            if (active) {
-                const bool any = kind == TR_SHADOW;
-                if (WIDE ? trav_step_wide(any, t, sv, stack, rp.err, cur)
-                         : trav_step_binary(any, t, sv, stack, rp.err, cur)) {
-                    wf_ray_end(kind, t, sv, st, p);
-                    credit();
-                    active = false;
+            bool fin = false;
+            if (WIDE) {
+                // lanes with pending leaf triangles and lanes due a node visit: the warp runs
+                // whichever step more of its lanes wait for
+                const bool has_leaf = active && (t.lbits & 0xffu) != 0u;
+                const bool want_node = active && !has_leaf;
+                const unsigned lm = __ballot_sync(~0u, has_leaf), nm = __ballot_sync(~0u, want_node);
+                const bool leaf_mode = lm != 0u && __popc(lm) * 4 >= __popc(nm) * kLeafBias;
+                if (leaf_mode ? has_leaf : want_node) {
+                    const bool any = kind == TR_SHADOW;
+                    fin = leaf_mode ? wide_leaf_step(any, t, sv, rp.err, cur)
+                                    : wide_node_step(any, t, sv, stack, rp.err, cur);
                 }
+            } else if (active) {
+                fin = trav_step_binary(kind == TR_SHADOW, t, sv, stack, rp.err, cur);
+            }
+            if (fin) {
+                wf_ray_end(kind, t, sv, st, p);
+                credit();
+                active = false;
             }
             const unsigned act = __ballot_sync(~0u, active);
             if (act == 0u || (!exhausted && 32 - __popc(act) >= kRefillIdle)) break;
