@@ -405,7 +405,7 @@ __device__ __forceinline__ int shade_entry(const WfState& st, int pool) {
 
 // Resident blocks per SM the shade kernel is compiled for (caps its registers).
 #ifndef LTS_SHADE_MIN_BLOCKS
-#define LTS_SHADE_MIN_BLOCKS 5
+#define LTS_SHADE_MIN_BLOCKS 6
 #endif
 // Launched with ceil(paths / kWfBlock) + kShadeClasses blocks over the class-grouped lists.
 template <bool RECORD>
