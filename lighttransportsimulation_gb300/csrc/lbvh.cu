@@ -213,6 +213,10 @@ __global__ void k_digit_prefix(const uint32_t* __restrict__ hist, uint32_t* __re
 #ifndef LTS_SORT_MIN_BLOCKS
 #define LTS_SORT_MIN_BLOCKS 4  // resident sort tiles per SM the register budget is cut for
 #endif
+#ifndef LTS_SORT_LOOKBACK
+#define LTS_SORT_LOOKBACK 4  // predecessor tiles read per look-back round trip
+#endif
+constexpr int kLookback = LTS_SORT_LOOKBACK;
 #ifndef LTS_SORT_BALLOT_MATCH
 #define LTS_SORT_BALLOT_MATCH 1  // 0: __match_any_sync
 #endif
@@ -301,21 +305,37 @@ __global__ __launch_bounds__(kSortThreads, LTS_SORT_MIN_BLOCKS) void k_onesweep(
     s_tile_start[dig] = start;
     uint32_t excl = 0;
     if (tile > 0) {
+        // look back kLookback predecessors per round trip (each status word carries its flag and
+        // count together), consumed newest first until an inclusive prefix; a predecessor that
+        // has published nothing yet is re-read (bounded wait)
         int k = tile - 1, spins = 0;
         while (k >= 0) {
-            const uint32_t v = ld_relaxed(status + (size_t)k * 256 + dig);
-            const uint32_t f = v & ~kCountMask;
-            if (f == 0) {
+            uint32_t v[kLookback];
+#pragma unroll
+            for (int j = 0; j < kLookback; ++j)
+                v[j] = k - j >= 0 ? ld_relaxed(status + (size_t)(k - j) * 256 + dig) : kFlagPrefix;
+            int used = kLookback;
+            bool done = false;
+#pragma unroll
+            for (int j = 0; j < kLookback; ++j) {
+                if (done || used < kLookback) continue;
+                const uint32_t f = v[j] & ~kCountMask;
+                if (f == 0) {
+                    used = j;
+                } else {
+                    excl += v[j] & kCountMask;
+                    done = f == kFlagPrefix;
+                }
+            }
+            if (done) break;
+            k -= used;
+            if (used < kLookback) {
                 if (++spins > kSpinLimit) {
                     atomicOr(err, DEV_ERR_LOOKBACK_TIMEOUT);
                     break;
                 }
-                __nanosleep(64);
-                continue;
+                __nanosleep(32);
             }
-            excl += v & kCountMask;
-            if (f == kFlagPrefix) break;
-            --k;
         }
         st_relaxed(st + dig, kFlagPrefix | (excl + tot));
     }
