@@ -724,8 +724,11 @@ __device__ __forceinline__ V3 offset_origin(V3 p, V3 perr, V3 n, V3 w) {
 }
 
 // ------------------------------------------------------------------ textures
-__constant__ unsigned char c_perm[512];
-__constant__ float c_marble[10][3];
+// Perlin permutation and marble colour tables in device memory, read through L1: the lanes of a
+// warp index them at different places, which the constant cache would serve one address at a
+// time (a 512-byte table spans four L1 lines).
+__device__ unsigned char c_perm[512];
+__device__ float c_marble[10][3];
 
 __device__ __forceinline__ real noise_weight(real t) {
     const real t3 = t * t * t, t4 = t3 * t;
@@ -733,7 +736,7 @@ __device__ __forceinline__ real noise_weight(real t) {
 }
 __device__ __forceinline__ real lerpf(real t, real a, real b) { return (1 - t) * a + t * b; }
 __device__ __forceinline__ real grad(int x, int y, int z, real dx, real dy, real dz) {
-    int h = c_perm[c_perm[c_perm[x] + y] + z];
+    int h = __ldg(c_perm + __ldg(c_perm + __ldg(c_perm + x) + y) + z);
     h &= 15;
     const real u = h < 8 || h == 12 || h == 13 ? dx : dy;
     const real v = h < 4 || h == 12 || h == 13 ? dy : dz;
@@ -819,7 +822,8 @@ __device__ Spec eval_texture(const DevTex& t, const SI& si, EvSink* sig) {
             tt = (tt * 6.0f - first);
             Spec c[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) c[k] = Spec{c_marble[first + k][0], c_marble[first + k][1], c_marble[first + k][2]};
+            for (int k = 0; k < 4; ++k)
+                c[k] = Spec{__ldg(&c_marble[first + k][0]), __ldg(&c_marble[first + k][1]), __ldg(&c_marble[first + k][2])};
             Spec s0 = c[0] * (1.0f - tt) + c[1] * tt;
             Spec s1 = c[1] * (1.0f - tt) + c[2] * tt;
             const Spec s2 = c[2] * (1.0f - tt) + c[3] * tt;

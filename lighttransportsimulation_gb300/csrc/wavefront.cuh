@@ -264,7 +264,10 @@ __device__ __forceinline__ void wf_ray_end(int kind, const Trav& t, const SceneV
 }
 
 // Lanes left idle before a warp fetches new rays (while the lists last).
-constexpr int kRefillIdle = 8;
+#ifndef LTS_REFILL_IDLE
+#define LTS_REFILL_IDLE 12 // idle lanes of a warp that trigger fetching new rays
+#endif
+constexpr int kRefillIdle = LTS_REFILL_IDLE;
 // Resident blocks per SM the trace kernel is compiled for (caps its registers).
 #ifndef LTS_LEAF_BIAS
 #define LTS_LEAF_BIAS 1  // leaf steps when lanes with pending leaves x 4 >= lanes due a node x this
