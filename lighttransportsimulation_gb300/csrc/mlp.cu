@@ -95,8 +95,21 @@ constexpr uint32_t kSGz = kSH + 5 * 16384;
 constexpr uint32_t kSGa = kSGz + 4096;
 constexpr uint32_t kTrainBar = kSGa + 16384;
 constexpr uint32_t kTrainSmem = kTrainBar + 64;
-constexpr uint32_t kFwdBar = kSH + 2 * 16384;
-constexpr uint32_t kFwdSmem = kFwdBar + 64;
+// Inference keeps kFwdGroups tiles in flight per CTA (one CTA per SM), one warpgroup of 128
+// threads per tile, sharing the weights: each tile has one 24 KB operand buffer at
+// fwd_buf(g) -- its features X (128 x 96), then each hidden layer's activations (128 x 64),
+// written over the buffer once the layer's products have completed -- an mbarrier and 64 TMEM
+// columns.
+#ifndef LTS_MLP_FWD_GROUPS
+#define LTS_MLP_FWD_GROUPS 6
+#endif
+constexpr int kFwdGroups = LTS_MLP_FWD_GROUPS;
+constexpr uint32_t kFwdTileBytes = 24576;
+__host__ __device__ constexpr uint32_t fwd_buf(int g) { return kSX + kFwdTileBytes * (uint32_t)g; }
+constexpr uint32_t kFwdBar = kSX + kFwdTileBytes * kFwdGroups;  // kFwdGroups mbarriers, then the TMEM slot
+constexpr uint32_t kFwdSmem = kFwdBar + 8 * kFwdGroups + 16;
+constexpr uint32_t kFwdCols = 64 * kFwdGroups <= 128 ? 128 : (64 * kFwdGroups <= 256 ? 256 : 512);
+static_assert(64 * kFwdGroups <= 512 && kFwdSmem <= 232448, "inference tiles exceed TMEM or shared memory");
 // TMEM columns: 0..63 the working product; dW_k^T accumulators (training) at kDwCol(k)
 __host__ __device__ constexpr uint32_t kDwCol(int L) { return 64u * (uint32_t)(L + 1); }
 
@@ -202,39 +215,93 @@ __device__ __forceinline__ void load_feature_row(unsigned char* smem, const uint
     }
 }
 
+// Named barrier over the 128 threads of warpgroup `id - 1` (barrier 0 is __syncthreads).
+__device__ __forceinline__ void wg_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ bool wg_sync_and(int id, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 p, %1, 0;\nbar.red.and.pred q, %2, 128, p;\nselp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id)
+        : "memory");
+    return r != 0;
+}
+// The warpgroup's shared-memory operands written so far, visible to the tensor cores.
+__device__ __forceinline__ void wg_publish(int id) {
+    fence_async_smem();
+    tc_fence_before();
+    wg_sync(id);
+    tc_fence_after();
+}
+
 // Inference: out[r * stride + c] = exp(z_c), c < 3, for the feature rows r = rows[i] (rows null:
-// r = i), i < n.  Persistent CTAs of 128 threads, one row per thread.
-__global__ __launch_bounds__(128) void k_mlp_forward(const uint16_t* __restrict__ w16, const uint16_t* __restrict__ feat,
-                                                     const int32_t* __restrict__ rows, int n, const uint32_t* d_n,
-                                                     float* __restrict__ out, int stride, uint32_t* err) {
+// r = i), i < n.  Persistent CTAs of kFwdGroups warpgroups; warpgroup g runs tiles
+// blockIdx.x * kFwdGroups + g, + gridDim.x * kFwdGroups, ..., one row per thread, and
+// synchronises with named barrier 1 + g only, so the tiles of a CTA overlap each other's
+// epilogues and waits.
+__global__ __launch_bounds__(128 * kFwdGroups) void k_mlp_forward(const uint16_t* __restrict__ w16,
+                                                                 const uint16_t* __restrict__ feat,
+                                                                 const int32_t* __restrict__ rows, int n,
+                                                                 const uint32_t* d_n, float* __restrict__ out,
+                                                                 int stride, uint32_t* err) {
     if (d_n) n = min(n, (int)*d_n);  // a count produced on the device (at most n)
     extern __shared__ __align__(1024) unsigned char smem[];
-    uint64_t* mbar = (uint64_t*)(smem + kFwdBar);
-    uint32_t* tslot = (uint32_t*)(smem + kFwdBar + 16);
+    const int g = threadIdx.x >> 7, row = threadIdx.x & 127, bar_id = 1 + g;
+    uint64_t* mbar = (uint64_t*)(smem + kFwdBar) + g;
+    uint32_t* tslot = (uint32_t*)(smem + kFwdBar + 8 * kFwdGroups);
     load_weights(smem, w16);
-    if (threadIdx.x == 0) mbar_init(mbar, 1);
-    if ((threadIdx.x >> 5) == 0) tmem_alloc(tslot, 64);
+    if (row == 0) mbar_init(mbar, 1);
+    if ((threadIdx.x >> 5) == 0) tmem_alloc(tslot, kFwdCols);
     publish_smem();
-    const uint32_t tmem = *tslot;
+    const uint32_t tmem = *tslot + 64u * (uint32_t)g;
+    const uint32_t lane_base = (uint32_t)(32 * ((threadIdx.x >> 5) & 3)) << 16;  // warp w: lanes 32 (w % 4) ..
+    const uint32_t sbase = smem_u32(smem), buf = fwd_buf(g);
     uint32_t phase = 0;
     const int ntiles = (n + 127) / 128;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long i = (long)tile * 128 + threadIdx.x;
+    for (int tile = blockIdx.x * kFwdGroups + g; tile < ntiles; tile += gridDim.x * kFwdGroups) {
+        const long i = (long)tile * 128 + row;
         const bool valid = i < n;
         const long r = valid ? (rows ? (long)__ldg(rows + i) : i) : 0;
-        load_feature_row(smem, feat, r, valid);
-        publish_smem();
-        float z[16];
-        if (!mlp_forward_tile<false>(smem, tmem, mbar, phase, err, z)) break;
-        if (valid)
-            for (int c = 0; c < kMlpOut; ++c) out[r * stride + c] = expf(z[c]);
+        const uint4* src = (const uint4*)(feat + r * kMlpIn);
+        for (int j = 0; j < kMlpIn / 8; ++j) {
+            const uint4 q = valid ? __ldg(src + j) : make_uint4(0, 0, 0, 0);
+            *(uint4*)(smem + buf + rc_offset(row, 8 * j, kMlpIn)) = q;
+        }
+        wg_publish(bar_id);
+        bool ok = true;
+        for (int L = 0; L < kMlpLayers; ++L) {
+            const int K = mlp_in(L), N = mlp_out(L);
+            if (row == 0) {
+                issue_fwd(tmem, sbase, buf, K, kSW(L), N, K);
+                umma_commit(mbar);
+            }
+            ok = wg_sync_and(bar_id, mbar_wait(mbar, phase, err));  // every thread of the warpgroup agrees
+            phase ^= 1u;
+            tc_fence_after();
+            if (!ok) break;
+            if (L < kMlpLayers - 1) {
+                float v[64];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) tmem_ld16(tmem + lane_base + 16 * q, v + 16 * q);
+#pragma unroll
+                for (int k = 0; k < 64; ++k) v[k] = fmaxf(v[k], 0.0f);
+                rc_store_row(smem + buf, row, 64, v);  // the layer's products have read the buffer
+                wg_publish(bar_id);
+            } else {
+                float z[16];
+                tmem_ld16(tmem + lane_base, z);
+                if (valid)
+                    for (int c = 0; c < kMlpOut; ++c) out[r * stride + c] = expf(z[c]);
+            }
+        }
+        if (!ok) break;
         tc_fence_before();
-        __syncthreads();  // every row read the output before the next tile's products
+        wg_sync(bar_id);  // every row read the output before the next tile's products
         tc_fence_after();
     }
     tc_fence_before();
     __syncthreads();
-    if ((threadIdx.x >> 5) == 0) tmem_free(tmem, 64);
+    if ((threadIdx.x >> 5) == 0) tmem_free(*tslot, kFwdCols);
 }
 
 // Training: gradient of mean over samples and channels of (pred - t)^2 / (pred^2 + 0.01)
@@ -430,7 +497,7 @@ std::string Mlp::init(uint32_t seed, cudaStream_t s) {
         TRY(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem));
         TRY(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem));
         blocks_train_ = sms;
-        blocks_fwd_ = 2 * sms;
+        blocks_fwd_ = sms;  // one CTA of kFwdGroups tiles per SM
     }
     // He-uniform weights, xorshift32 stream from the seed; W5 rows 3..15 zero
     std::vector<float> w(kMlpParams, 0.0f);
@@ -488,8 +555,9 @@ std::string Mlp::forward(const uint16_t* d_feat, int n, float* d_out, uint32_t* 
     if (!w32_) return "MLP not initialised";
     if (n <= 0) return "";
     const int tiles = (n + 127) / 128;
-    k_mlp_forward<<<std::min(tiles, blocks_fwd_), 128, kFwdSmem, s>>>(w16_, d_feat, d_rows, n, d_n, d_out, out_stride,
-                                                                     d_err);
+    const int groups = (tiles + kFwdGroups - 1) / kFwdGroups;
+    k_mlp_forward<<<std::min(groups, blocks_fwd_), 128 * kFwdGroups, kFwdSmem, s>>>(w16_, d_feat, d_rows, n, d_n, d_out,
+                                                                                   out_stride, d_err);
     TRY(cudaGetLastError());
     return "";
 }
