@@ -265,14 +265,14 @@ int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char
     ctx->bvh_is_scene = false;
     if (ctx->device == -1) return LTS_OK;
     CK(cudaSetDevice(ctx->device));
-    std::vector<float> soup;
-    ctx->scene.triangle_soup(soup);
-    int rc = ensure_tri_buffer(ctx, soup.size());
-    if (rc) return rc;
-    CK(cudaMemcpyAsync(ctx->d_tri, soup.data(), soup.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     if (!ctx->tracer) ctx->tracer.reset(new Tracer());
     std::string e = ctx->tracer->upload_scene(ctx->scene, ctx->stream);
     if (!e.empty()) return fail(ctx, e.find("memory") != std::string::npos ? LTS_ERR_OOM : LTS_ERR_CUDA, e);
+    // the LBVH input (9 floats per triangle), expanded on the device from the uploaded tables
+    int rc = ensure_tri_buffer(ctx, 9 * (size_t)ctx->scene.triangles());
+    if (rc) return rc;
+    e = ctx->tracer->triangle_soup(ctx->d_tri, ctx->stream);
+    if (!e.empty()) return fail(ctx, LTS_ERR_CUDA, e);
     CK(cudaStreamSynchronize(ctx->stream));
     return LTS_OK;
 }

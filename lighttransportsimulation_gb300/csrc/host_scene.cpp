@@ -523,6 +523,12 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
             const Xform& X = m >= sub_meshes ? ident : subject_xf;
             const int32_t pbase = (int32_t)(sc->p.size() / 3), nbase = (int32_t)(sc->n.size() / 3),
                           uvbase = (int32_t)(sc->uv.size() / 2);
+            sc->p.reserve(sc->p.size() + 3 * (size_t)md.np);
+            sc->n.reserve(sc->n.size() + 3 * (size_t)md.nn);
+            sc->tri_p.reserve(sc->tri_p.size() + 3 * (size_t)md.ntri);
+            sc->tri_uv.reserve(sc->tri_uv.size() + 3 * (size_t)md.ntri);
+            sc->tri_n.reserve(sc->tri_n.size() + 3 * (size_t)md.ntri);
+            sc->tri_mesh.reserve(sc->tri_mesh.size() + (size_t)md.ntri);
             for (int32_t i = 0; i < md.np; ++i) {
                 V3 w = X.point({md.p[3 * i], md.p[3 * i + 1], md.p[3 * i + 2]});
                 sc->p.push_back(w.x); sc->p.push_back(w.y); sc->p.push_back(w.z);

@@ -54,33 +54,54 @@ __global__ void k_resolve(const double* __restrict__ film, float* __restrict__ r
     }
 }
 
-// Shading record of each scene triangle (layout: SceneView::prim_rec) from the loader's
-// per-triangle corner indices: positions, uvs or the defaults (0,0) (1,0) (1,1)
-// (Triangle.cu:137-143), vertex normals or zeros, and (has normals, mesh, area light, 0).
-__global__ void k_build_prim_rec(const float4* __restrict__ prim_v, const int4* __restrict__ prim_n,
-                                 const int4* __restrict__ prim_uv, const float* __restrict__ normals,
-                                 const float* __restrict__ uvs, const int32_t* __restrict__ prim_light, int nt,
-                                 float4* __restrict__ rec) {
+// Scene-order triangles as 3 float4 (w = 0) from the vertex pool and the corner indices.
+__global__ void k_expand_tris(const float* __restrict__ p, const int32_t* __restrict__ tri_p, int nt,
+                              float4* __restrict__ prim_v) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nt) return;
-    const int4 ni = prim_n[t], ui = prim_uv[t];
+    for (int c = 0; c < 3; ++c) {
+        const int vi = tri_p[3 * t + c];
+        prim_v[3 * (size_t)t + c] = make_float4(p[3 * vi], p[3 * vi + 1], p[3 * vi + 2], 0.f);
+    }
+}
+// The same triangles as 9 floats each (the LBVH build's input).
+__global__ void k_soup_from_tris(const float4* __restrict__ prim_v, int nt, float* __restrict__ soup) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    for (int c = 0; c < 3; ++c) {
+        const float4 q = prim_v[3 * (size_t)t + c];
+        soup[9 * (size_t)t + 3 * c] = q.x;
+        soup[9 * (size_t)t + 3 * c + 1] = q.y;
+        soup[9 * (size_t)t + 3 * c + 2] = q.z;
+    }
+}
+
+// Shading record of each scene triangle (layout: SceneView::prim_rec) from the loader's
+// per-corner indices (-1 for none): positions, uvs or the defaults (0,0) (1,0) (1,1)
+// (Triangle.cu:137-143), vertex normals or zeros, and (has normals, mesh, area light, 0).
+__global__ void k_build_prim_rec(const float4* __restrict__ prim_v, const int32_t* __restrict__ tri_n,
+                                 const int32_t* __restrict__ tri_uv, const int32_t* __restrict__ tri_mesh,
+                                 const float* __restrict__ normals, const float* __restrict__ uvs,
+                                 const int32_t* __restrict__ prim_light, int nt, float4* __restrict__ rec) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int n3[3] = {tri_n[3 * t], tri_n[3 * t + 1], tri_n[3 * t + 2]};
+    const int u3[3] = {tri_uv[3 * t], tri_uv[3 * t + 1], tri_uv[3 * t + 2]};
     float uv[6] = {0.f, 0.f, 1.f, 0.f, 1.f, 1.f};
-    if (ui.x >= 0) {
-        const int u3[3] = {ui.x, ui.y, ui.z};
+    if (u3[0] >= 0) {
         for (int c = 0; c < 3; ++c) {
             uv[2 * c] = uvs[2 * u3[c]];
             uv[2 * c + 1] = uvs[2 * u3[c] + 1];
         }
     }
     float4* r = rec + 8 * (size_t)t;
-    const int n3[3] = {ni.x, ni.y, ni.z};
     for (int c = 0; c < 3; ++c) {
         const float4 q = prim_v[3 * (size_t)t + c];
         r[c] = make_float4(q.x, q.y, q.z, uv[c]);
-        r[3 + c] = ni.x >= 0 ? make_float4(normals[3 * n3[c]], normals[3 * n3[c] + 1], normals[3 * n3[c] + 2], uv[3 + c])
-                             : make_float4(0.f, 0.f, 0.f, uv[3 + c]);
+        r[3 + c] = n3[0] >= 0 ? make_float4(normals[3 * n3[c]], normals[3 * n3[c] + 1], normals[3 * n3[c] + 2], uv[3 + c])
+                              : make_float4(0.f, 0.f, 0.f, uv[3 + c]);
     }
-    reinterpret_cast<int4*>(r)[6] = make_int4(ni.x >= 0 ? 1 : 0, ni.w, prim_light[t], 0);
+    reinterpret_cast<int4*>(r)[6] = make_int4(n3[0] >= 0 ? 1 : 0, tri_mesh[t], prim_light[t], 0);
     r[7] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
@@ -112,12 +133,22 @@ static_assert(kWfBlock == kThreads, "wavefront stages share the traversal stack 
         if (e_ != cudaSuccess) return std::string(#call ": ") + cudaGetErrorString(e_); \
     } while (0)
 
-template <class T>
-std::string upload(void*& slot, const std::vector<T>& v, cudaStream_t s) {
+// A device buffer of at least `bytes` in `slot` (capacity `cap`): kept when big enough, so that
+// loading another scene of the same size allocates nothing.
+std::string reserve_buf(void*& slot, size_t& cap, size_t bytes) {
+    bytes = std::max<size_t>(bytes, 16);
+    if (slot && cap >= bytes) return "";
     if (slot) dev_free(slot);
     slot = nullptr;
-    const size_t b = std::max<size_t>(sizeof(T) * v.size(), 16);
-    TRY(dev_alloc(&slot, b));
+    cap = 0;
+    TRY(dev_alloc(&slot, bytes));
+    cap = bytes;
+    return "";
+}
+template <class T>
+std::string upload(void*& slot, size_t& cap, const std::vector<T>& v, cudaStream_t s) {
+    const std::string e = reserve_buf(slot, cap, sizeof(T) * v.size());
+    if (!e.empty()) return e;
     if (!v.empty()) TRY(cudaMemcpyAsync(slot, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
     return "";
 }
@@ -127,9 +158,10 @@ float quake_host(float f) { return quake_rsqrt(f); }
 }  // namespace
 
 void Tracer::free_all() {
-    for (void*& p : bufs_) {
-        if (p) dev_free(p);
-        p = nullptr;
+    for (int k = 0; k < kSceneBufs; ++k) {
+        if (bufs_[k]) dev_free(bufs_[k]);
+        bufs_[k] = nullptr;
+        bufcap_[k] = 0;
     }
     dev_free(leaf_v_);
     leaf_v_ = nullptr;
@@ -193,7 +225,9 @@ Tracer::~Tracer() {
 }
 
 std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
-    free_all();
+    // buffers stay allocated (each is re-sized where it is used); the leaf-ordered triangle copy
+    // belongs to the previous scene's BVH
+    leaf_serial_ = 0;
     static bool consts = false;
     if (!consts) {
         unsigned char p2[512];
@@ -208,16 +242,6 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
         TRY(cudaEventCreate(&ev1_));
     }
     const int nt = sc.triangles();
-    std::vector<float4> pv(3 * (size_t)nt);
-    std::vector<int4> pn((size_t)nt), puv((size_t)nt);
-    for (int t = 0; t < nt; ++t) {
-        for (int c = 0; c < 3; ++c) {
-            const int vi = sc.tri_p[3 * t + c];
-            pv[3 * (size_t)t + c] = make_float4(sc.p[3 * vi], sc.p[3 * vi + 1], sc.p[3 * vi + 2], 0.f);
-        }
-        pn[t] = make_int4(sc.tri_n[3 * t], sc.tri_n[3 * t + 1], sc.tri_n[3 * t + 2], sc.tri_mesh[t]);
-        puv[t] = make_int4(sc.tri_uv[3 * t], sc.tri_uv[3 * t + 1], sc.tri_uv[3 * t + 2], 0);
-    }
     std::vector<DevMat> mats(sc.materials.size());
     std::vector<int> class_keys;  // shade classes: distinct (kind, Oren-Nayar, texture kinds) in order of appearance
     for (size_t m = 0; m < mats.size(); ++m) {
@@ -253,27 +277,33 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
         lights[l].area = h.area;
     }
     std::vector<float> filt(sc.filter, sc.filter + 256);
+    // vertex pools and per-corner indices go up as loaded; the per-triangle positions and the
+    // shading records are expanded on the device
     std::string e;
-    if (!(e = upload(bufs_[0], pv, s)).empty()) return e;
-    // compact per-triangle indices up, shading records built on the device
-    if (!(e = upload(bufs_[2], pn, s)).empty()) return e;
-    if (!(e = upload(bufs_[3], puv, s)).empty()) return e;
-    if (!(e = upload(bufs_[4], sc.n, s)).empty()) return e;
-    if (!(e = upload(bufs_[5], sc.uv, s)).empty()) return e;
-    if (!(e = upload(bufs_[11], sc.prim_light, s)).empty()) return e;
-    TRY(dev_alloc(&bufs_[1], 128 * (size_t)(nt > 0 ? nt : 1)));
-    if (nt > 0)
-        k_build_prim_rec<<<(nt + 255) / 256, 256, 0, s>>>((const float4*)bufs_[0], (const int4*)bufs_[2],
-                                                          (const int4*)bufs_[3], (const float*)bufs_[4],
-                                                          (const float*)bufs_[5], (const int32_t*)bufs_[11], nt,
-                                                          (float4*)bufs_[1]);
+    if (!(e = upload(bufs_[12], bufcap_[12], sc.p, s)).empty()) return e;
+    if (!(e = upload(bufs_[13], bufcap_[13], sc.tri_p, s)).empty()) return e;
+    if (!(e = upload(bufs_[2], bufcap_[2], sc.tri_n, s)).empty()) return e;
+    if (!(e = upload(bufs_[3], bufcap_[3], sc.tri_uv, s)).empty()) return e;
+    if (!(e = upload(bufs_[4], bufcap_[4], sc.n, s)).empty()) return e;
+    if (!(e = upload(bufs_[5], bufcap_[5], sc.uv, s)).empty()) return e;
+    if (!(e = upload(bufs_[11], bufcap_[11], sc.prim_light, s)).empty()) return e;
+    if (!(e = upload(bufs_[14], bufcap_[14], sc.tri_mesh, s)).empty()) return e;
+    if (!(e = upload(bufs_[6], bufcap_[6], mats, s)).empty()) return e;
+    if (!(e = upload(bufs_[7], bufcap_[7], lights, s)).empty()) return e;
+    if (!(e = upload(bufs_[8], bufcap_[8], sc.light_func, s)).empty()) return e;
+    if (!(e = upload(bufs_[9], bufcap_[9], sc.light_cdf, s)).empty()) return e;
+    if (!(e = upload(bufs_[10], bufcap_[10], filt, s)).empty()) return e;
+    if (!(e = reserve_buf(bufs_[0], bufcap_[0], 48 * (size_t)nt)).empty()) return e;
+    if (!(e = reserve_buf(bufs_[1], bufcap_[1], 128 * (size_t)nt)).empty()) return e;
+    if (nt > 0) {
+        k_expand_tris<<<(nt + 255) / 256, 256, 0, s>>>((const float*)bufs_[12], (const int32_t*)bufs_[13], nt,
+                                                       (float4*)bufs_[0]);
+        k_build_prim_rec<<<(nt + 255) / 256, 256, 0, s>>>(
+            (const float4*)bufs_[0], (const int32_t*)bufs_[2], (const int32_t*)bufs_[3], (const int32_t*)bufs_[14],
+            (const float*)bufs_[4], (const float*)bufs_[5], (const int32_t*)bufs_[11], nt, (float4*)bufs_[1]);
+    }
     TRY(cudaGetLastError());
-    if (!(e = upload(bufs_[6], mats, s)).empty()) return e;
-    if (!(e = upload(bufs_[7], lights, s)).empty()) return e;
-    if (!(e = upload(bufs_[8], sc.light_func, s)).empty()) return e;
-    if (!(e = upload(bufs_[9], sc.light_cdf, s)).empty()) return e;
-    if (!(e = upload(bufs_[10], filt, s)).empty()) return e;
-    TRY(dev_alloc((void**)&counters_, 128));
+    if (!counters_) TRY(dev_alloc((void**)&counters_, 128));
     view_ = SceneView{};
     view_.ntri = nt;
     view_.nlight = (int)lights.size();
@@ -288,6 +318,13 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
     view_.light_func_int = sc.light_func_int;
     view_.filter = (const float*)bufs_[10];
     memcpy(view_.cam, sc.cam, sizeof sc.cam);
+    return "";
+}
+
+std::string Tracer::triangle_soup(float* d_soup, cudaStream_t s) const {
+    if (view_.ntri > 0)
+        k_soup_from_tris<<<(view_.ntri + 255) / 256, 256, 0, s>>>(view_.prim_v, view_.ntri, d_soup);
+    TRY(cudaGetLastError());
     return "";
 }
 

@@ -101,6 +101,8 @@ class Tracer {
     Tracer& operator=(const Tracer&) = delete;
 
     std::string upload_scene(const HostScene& sc, cudaStream_t s);
+    // The uploaded scene's triangles as 9 floats each, scene order (the LBVH build's input).
+    std::string triangle_soup(float* d_soup, cudaStream_t s) const;
     std::string render(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, lts_render_out* out,
                        cudaStream_t s, uint32_t* d_err);
     std::string render_async(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
@@ -169,7 +171,9 @@ class Tracer {
     unsigned wf_sms_ = 0;  // resident blocks of k_wf_trace (wide, binary) on this device
     SceneView view_{};
     WideBvh wide_;
-    void* bufs_[16] = {nullptr};
+    static constexpr int kSceneBufs = 16;
+    void* bufs_[kSceneBufs] = {nullptr};   // scene tables, kept across scene loads while big enough
+    size_t bufcap_[kSceneBufs] = {0};
     float4* leaf_v_ = nullptr;
     int leaf_n_ = 0;
     uint64_t leaf_serial_ = 0;  // Lbvh::serial the leaf_v_ copy was gathered for
