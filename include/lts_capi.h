@@ -295,6 +295,9 @@ typedef struct {
     double cache_queries;
     int32_t cache_train_samples;
     double cache_train_loss, cache_bias, cache_train_ms;
+    /* last lts_load_scene: host milliseconds parsing the files, and uploading the tables and
+     * expanding them on the device (until the stream is idle) */
+    double scene_parse_ms, scene_upload_ms;
 } lts_metrics;
 int lts_get_metrics(lts_ctx* ctx, lts_metrics* out);
 

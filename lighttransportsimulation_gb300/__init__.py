@@ -86,7 +86,8 @@ class Metrics(ctypes.Structure):
                 ("kind_node_visits", ctypes.c_double * 3), ("kind_tri_tests", ctypes.c_double * 3),
                 ("cache_queries", ctypes.c_double), ("cache_train_samples", ctypes.c_int32),
                 ("cache_train_loss", ctypes.c_double), ("cache_bias", ctypes.c_double),
-                ("cache_train_ms", ctypes.c_double)]
+                ("cache_train_ms", ctypes.c_double), ("scene_parse_ms", ctypes.c_double),
+                ("scene_upload_ms", ctypes.c_double)]
 
 
 _lib = None

@@ -61,7 +61,7 @@ def build(verbose=False, force=False):
         obj = os.path.join(LIBDIR, "obj", f + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", src, "-o", obj])
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -74,7 +74,7 @@ def build(verbose=False, force=False):
             if r.returncode:
                 raise RuntimeError(f"compile failed: {cmd[-3]}")
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-lcudart"]
+        cmd = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-lcudart", "-Xcompiler", "-pthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

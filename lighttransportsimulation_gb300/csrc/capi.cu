@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -257,8 +258,12 @@ int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char
     if (!ctx || !root || !scene) return fail(ctx, LTS_ERR_ARG, "null argument");
     int code = LTS_OK;
     HostScene sc;
+    const auto t0 = std::chrono::steady_clock::now();
     std::string msg = load_scene(root, scene, subject ? subject : "", width, height, &sc, &code);
     if (code) return fail(ctx, code, msg);
+    const auto t1 = std::chrono::steady_clock::now();
+    ctx->metrics.scene_parse_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    ctx->metrics.scene_upload_ms = 0;
     ctx->scene = std::move(sc);
     ctx->loaded = true;
     ctx->bvh_mode = -1;
@@ -274,6 +279,8 @@ int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char
     e = ctx->tracer->triangle_soup(ctx->d_tri, ctx->stream);
     if (!e.empty()) return fail(ctx, LTS_ERR_CUDA, e);
     CK(cudaStreamSynchronize(ctx->stream));
+    ctx->metrics.scene_upload_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
     return LTS_OK;
 }
 

@@ -10,7 +10,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <algorithm>
+#include <atomic>
 #include <sstream>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -105,6 +108,28 @@ class Tokens {
     size_t pos_ = 0;
 };
 
+// f(begin, end) over [0, n) in contiguous chunks on up to 16 host threads (serially below 32K
+// items).  The loops it runs write disjoint elements, so the result does not depend on the split.
+template <class F>
+void parallel_ranges(size_t n, const F& f) {
+    const size_t kMin = size_t(1) << 15;
+    unsigned nt = std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+    if (n < 2 * kMin || nt <= 1) {
+        f(size_t(0), n);
+        return;
+    }
+    nt = (unsigned)std::min<size_t>(nt, n / kMin);
+    const size_t chunk = (n + nt - 1) / nt;
+    std::vector<std::thread> th;
+    th.reserve(nt - 1);
+    for (unsigned k = 1; k < nt; ++k) {
+        const size_t b = k * chunk, e = std::min(n, b + chunk);
+        if (b < e) th.emplace_back([&f, b, e] { f(b, e); });
+    }
+    f(size_t(0), std::min(n, chunk));
+    for (auto& t : th) t.join();
+}
+
 struct ParseError {
     int code;
     std::string msg;
@@ -170,12 +195,19 @@ MeshData read_bin(const std::string& path) {
 // Every corner's position index, and its uv / normal index when the mesh has any, in range (the
 // reference reads out of bounds otherwise).
 void check_indices(const MeshData& m, const std::string& name) {
-    for (int32_t t = 0; t < m.ntri; ++t)
-        for (int c = 0; c < 3; ++c) {
-            const int32_t ip = m.idx[9 * t + 3 * c], iu = m.idx[9 * t + 3 * c + 1], in = m.idx[9 * t + 3 * c + 2];
-            if (ip < 0 || ip >= m.np || (m.nuv > 0 && (iu < 0 || iu >= m.nuv)) || (m.nn > 0 && (in < 0 || in >= m.nn)))
-                throw ParseError{LTS_ERR_PARSE, "vertex index out of range in mesh " + name};
-        }
+    std::atomic<bool> bad{false};
+    parallel_ranges((size_t)m.ntri, [&](size_t b, size_t e) {
+        for (size_t t = b; t < e; ++t)
+            for (int c = 0; c < 3; ++c) {
+                const int32_t ip = m.idx[9 * t + 3 * c], iu = m.idx[9 * t + 3 * c + 1], in = m.idx[9 * t + 3 * c + 2];
+                if (ip < 0 || ip >= m.np || (m.nuv > 0 && (iu < 0 || iu >= m.nuv)) ||
+                    (m.nn > 0 && (in < 0 || in >= m.nn))) {
+                    bad = true;
+                    return;
+                }
+            }
+    });
+    if (bad) throw ParseError{LTS_ERR_PARSE, "vertex index out of range in mesh " + name};
 }
 
 // core/FileIO.cuh:73-164 (parseMeshFile): the whole file is read as whitespace-separated tokens
@@ -522,32 +554,40 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
             check_indices(md, files[m]);
             const Xform& X = m >= sub_meshes ? ident : subject_xf;
             const int32_t pbase = (int32_t)(sc->p.size() / 3), nbase = (int32_t)(sc->n.size() / 3),
-                          uvbase = (int32_t)(sc->uv.size() / 2);
-            sc->p.reserve(sc->p.size() + 3 * (size_t)md.np);
-            sc->n.reserve(sc->n.size() + 3 * (size_t)md.nn);
-            sc->tri_p.reserve(sc->tri_p.size() + 3 * (size_t)md.ntri);
-            sc->tri_uv.reserve(sc->tri_uv.size() + 3 * (size_t)md.ntri);
-            sc->tri_n.reserve(sc->tri_n.size() + 3 * (size_t)md.ntri);
-            sc->tri_mesh.reserve(sc->tri_mesh.size() + (size_t)md.ntri);
-            for (int32_t i = 0; i < md.np; ++i) {
-                V3 w = X.point({md.p[3 * i], md.p[3 * i + 1], md.p[3 * i + 2]});
-                sc->p.push_back(w.x); sc->p.push_back(w.y); sc->p.push_back(w.z);
-            }
-            for (int32_t i = 0; i < md.nn; ++i) {
-                V3 w = X.normal({md.n[3 * i], md.n[3 * i + 1], md.n[3 * i + 2]});
-                sc->n.push_back(w.x); sc->n.push_back(w.y); sc->n.push_back(w.z);
-            }
-            sc->uv.insert(sc->uv.end(), md.uv.begin(), md.uv.end());
-            sc->mesh_first_tri.push_back((int32_t)sc->tri_mesh.size());
-            sc->mesh_tri_count.push_back(md.ntri);
-            for (int32_t t = 0; t < md.ntri; ++t) {
-                for (int c = 0; c < 3; ++c) {
-                    sc->tri_p.push_back(pbase + md.idx[9 * t + 3 * c]);
-                    sc->tri_uv.push_back(md.nuv > 0 ? uvbase + md.idx[9 * t + 3 * c + 1] : -1);
-                    sc->tri_n.push_back(md.nn > 0 ? nbase + md.idx[9 * t + 3 * c + 2] : -1);
+                          uvbase = (int32_t)(sc->uv.size() / 2), tbase = (int32_t)sc->tri_mesh.size();
+            sc->p.resize(3 * ((size_t)pbase + md.np));
+            parallel_ranges((size_t)md.np, [&](size_t b, size_t e) {
+                for (size_t i = b; i < e; ++i) {
+                    const V3 w = X.point({md.p[3 * i], md.p[3 * i + 1], md.p[3 * i + 2]});
+                    float* o = &sc->p[3 * ((size_t)pbase + i)];
+                    o[0] = w.x; o[1] = w.y; o[2] = w.z;
                 }
-                sc->tri_mesh.push_back(m);
-            }
+            });
+            sc->n.resize(3 * ((size_t)nbase + md.nn));
+            parallel_ranges((size_t)md.nn, [&](size_t b, size_t e) {
+                for (size_t i = b; i < e; ++i) {
+                    const V3 w = X.normal({md.n[3 * i], md.n[3 * i + 1], md.n[3 * i + 2]});
+                    float* o = &sc->n[3 * ((size_t)nbase + i)];
+                    o[0] = w.x; o[1] = w.y; o[2] = w.z;
+                }
+            });
+            sc->uv.insert(sc->uv.end(), md.uv.begin(), md.uv.end());
+            sc->mesh_first_tri.push_back(tbase);
+            sc->mesh_tri_count.push_back(md.ntri);
+            const size_t nc = 3 * ((size_t)tbase + md.ntri);
+            sc->tri_p.resize(nc);
+            sc->tri_uv.resize(nc);
+            sc->tri_n.resize(nc);
+            sc->tri_mesh.resize((size_t)tbase + md.ntri, m);
+            parallel_ranges((size_t)md.ntri, [&](size_t b, size_t e) {
+                for (size_t t = b; t < e; ++t)
+                    for (int c = 0; c < 3; ++c) {
+                        const size_t o = 3 * ((size_t)tbase + t) + c;
+                        sc->tri_p[o] = pbase + md.idx[9 * t + 3 * c];
+                        sc->tri_uv[o] = md.nuv > 0 ? uvbase + md.idx[9 * t + 3 * c + 1] : -1;
+                        sc->tri_n[o] = md.nn > 0 ? nbase + md.idx[9 * t + 3 * c + 2] : -1;
+                    }
+            });
         }
         sc->subject_meshes = sub_meshes;
         sc->area_light_meshes = area_meshes;
