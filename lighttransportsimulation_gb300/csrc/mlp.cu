@@ -84,7 +84,7 @@ __global__ __launch_bounds__(128) void k_umma_probe(const uint16_t* __restrict__
 
 // ------------------------------------------------------------------ the radiance-cache MLP
 // Shared memory (bytes).  Weights in RC layout: W0 64x96, W1..W4 64x64, W5 16x64; the input
-// tile X (128 x 96), hidden activations H1..H5 (128 x 64 each; the forward-only kernel keeps two),
+// tile X (128 x 96), hidden activations H1..H5 (128 x 64 each),
 // the output-gradient tile Gz (128 x 16) and one hidden-gradient tile Ga (128 x 64).  MN-major
 // reads of a 64- or 96-column buffer with M = 128 run past its end into the next buffer; those
 // product rows are never used.
@@ -175,16 +175,15 @@ __device__ __forceinline__ void tmem_row64(uint32_t tmem, int c0, float* v) {
     for (int q = 0; q < 4; ++q) tmem_ld16(tmem + lane_base + c0 + 16 * q, v + 16 * q);
 }
 
-// Forward pass of one 128-row tile whose features are already in X; leaves the hidden
-// activations in the H slots (train: H1..H5; forward-only: ping-pong) and returns z (16 values).
-template <bool TRAIN>
+// Forward pass of one 128-row training tile whose features are already in X; leaves the hidden
+// activations H1..H5 in their slots (the backward pass reads them) and returns z (16 values).
 __device__ bool mlp_forward_tile(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint32_t& phase, uint32_t* err,
                                  float* z) {
     const uint32_t sbase = smem_u32(smem);
     const int row = threadIdx.x;
     float v[64];
     for (int L = 0; L < kMlpLayers; ++L) {
-        const uint32_t a_off = L == 0 ? kSX : kSH + (TRAIN ? (L - 1) : ((L - 1) & 1)) * 16384;
+        const uint32_t a_off = L == 0 ? kSX : kSH + (L - 1) * 16384;
         const int K = mlp_in(L), N = mlp_out(L);
         if (threadIdx.x == 0) {
             issue_fwd(tmem, sbase, a_off, K, kSW(L), N, K);
@@ -197,7 +196,7 @@ __device__ bool mlp_forward_tile(unsigned char* smem, uint32_t tmem, uint64_t* m
             tmem_row64(tmem, 0, v);
 #pragma unroll
             for (int k = 0; k < 64; ++k) v[k] = fmaxf(v[k], 0.0f);
-            rc_store_row(smem + kSH + (TRAIN ? L : (L & 1)) * 16384, row, 64, v);
+            rc_store_row(smem + kSH + L * 16384, row, 64, v);
             publish_smem();
         } else {
             tmem_ld16(tmem + ((uint32_t)(32 * (threadIdx.x >> 5)) << 16), z);
@@ -332,7 +331,7 @@ __global__ __launch_bounds__(128) void k_mlp_train(const uint16_t* __restrict__ 
         load_feature_row(smem, feat, grow, valid);
         publish_smem();
         float z[16];
-        if (!(ok = mlp_forward_tile<true>(smem, tmem, mbar, phase, err, z))) break;
+        if (!(ok = mlp_forward_tile(smem, tmem, mbar, phase, err, z))) break;
         // output gradient
         float g[64];
 #pragma unroll

@@ -32,7 +32,7 @@ struct DevLight {
 
 // Everything a render kernel reads, passed by value.
 struct SceneView {
-    int32_t ntri, nlight, width, height, has_normals_any;
+    int32_t ntri, nlight, width, height;
     const float4* __restrict__ leaf_v;   // [3 ntri] triangle of leaf l: p0 (w = prim id bits), p1, p2
     const float4* __restrict__ prim_v;   // [3 ntri] scene order
     // [8 ntri] shading record of each scene triangle, one 128-byte line (what a hit reads):
