@@ -140,6 +140,8 @@ def cpu_port_sample(wl, seconds_target=15.0, threads=None):
 
 
 def dist_setup(n):
+    """One process per GPU (torchrun's RANK / WORLD_SIZE / LOCAL_RANK / MASTER_*): replicas of the
+    same render, no collective on the data path; NCCL on GPUs, gloo without (host-side tests)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -147,18 +149,29 @@ def dist_setup(n):
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
     return rank, world, local, dist
 
 
 def barrier_max(dist, value):
+    """The largest `value` over the ranks (the timing every replica reports is the slowest's)."""
     if dist is None:
         return value
     import torch
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(world, units_per_rank, seconds_max):
+    """Whole-job throughput of `world` replicas each doing `units_per_rank` (weak scaling), over
+    the slowest replica's time."""
+    return world * units_per_rank / seconds_max
 
 
 def run_reference(args, wl):
@@ -322,7 +335,7 @@ def run_gpu(args, wl):
     launches_step, iters_step = mt.render_launches, mt.render_iterations
     ms = e0.elapsed_time(e1) / args.steps
     ms = barrier_max(dist, ms)
-    value = world * paths / (ms * 1e-3) / 1e6
+    value = replica_throughput(world, paths, ms * 1e-3) / 1e6
 
     # one counted render for the roofline's algorithmic bytes and the per-stage device times (the
     # same kernels, launched one by one instead of as graphs so that each stage can be timed)
@@ -364,7 +377,7 @@ def run_gpu(args, wl):
             wl["spp"], wl["seed"])
         t_e2e.append(time.perf_counter() - t0)
     e2e_s = barrier_max(dist, statistics.median(t_e2e))
-    e2e = world * paths / e2e_s / 1e6
+    e2e = replica_throughput(world, paths, e2e_s) / 1e6
 
     lbvh = None
     if rank == 0 and not args.skip_lbvh:
