@@ -639,6 +639,15 @@ __global__ __launch_bounds__(kBlock) void k_tree_top(const float* __restrict__ t
 }
 
 inline int grid_for(long items, int per_block) { return (int)((items + per_block - 1) / per_block); }
+#ifndef LTS_TREE_TOP_BLOCKS_PER_SM
+#define LTS_TREE_TOP_BLOCKS_PER_SM 32
+#endif
+// k_tree_top's grid: close to one listed child per thread (the list holds at most 2n - 2;
+// each climb is a chain of dependent device-memory round trips, so a thread should start its
+// climbs at once rather than one after another), capped at LTS_TREE_TOP_BLOCKS_PER_SM per SM.
+inline int tree_top_grid(long n, int sms) {
+    return (int)std::max<long>(1, std::min<long>(grid_for(2 * n, kBlock), (long)sms * LTS_TREE_TOP_BLOCKS_PER_SM));
+}
 
 }  // namespace
 
@@ -747,8 +756,8 @@ std::string Lbvh::build(const float* d_tri, int nn, int md, int code_limit, cuda
                                                                 leaf_prim, root_bounds);
     ++launches;
     if (nn > 1) {
-        k_tree_top<<<sms * 4, kBlock, 0, s>>>(d_tri, nn, md, ids, codes, nodes, flags_, epoch_, pending, counters_ + 4,
-                                              root_bounds);
+        k_tree_top<<<tree_top_grid(nn, sms), kBlock, 0, s>>>(d_tri, nn, md, ids, codes, nodes, flags_, epoch_, pending,
+                                                             counters_ + 4, root_bounds);
         ++launches;
     }
     LTS_TRY(cudaEventRecord(ev_[5], s));
@@ -882,8 +891,8 @@ extern "C" int lts_bvh_build_noalloc(const float* d_tri, int32_t n, int32_t mode
     k_tree<<<grid_for((long)N, kTreeBlock), kTreeBlock, 0, s>>>(d_tri, n, mode, d_ids, d_codes, nodes, pending,
                                                                 counters + 4, d_leaf_prim, d_root_bounds);
     if (n > 1)
-        k_tree_top<<<sms * 4, kBlock, 0, s>>>(d_tri, n, mode, d_ids, d_codes, nodes, flags, 1u, pending, counters + 4,
-                                              d_root_bounds);
+        k_tree_top<<<tree_top_grid(n, sms), kBlock, 0, s>>>(d_tri, n, mode, d_ids, d_codes, nodes, flags, 1u, pending,
+                                                            counters + 4, d_root_bounds);
     if (cudaGetLastError() != cudaSuccess) return LTS_ERR_CUDA;
     uint32_t h_err = 0;
     if (cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return LTS_ERR_CUDA;
