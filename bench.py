@@ -307,6 +307,7 @@ def run_gpu(args, wl):
     ctx = lts.Context(local)
     scene = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
     ctx.set_option("bvh_width", args.bvh_width)
+    ctx.set_option("render_bvh", args.render_bvh)
     integ = lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], scene, integrator=args.integrator)
     desc = integ.desc(wl["spp"], wl["seed"])
     stream = torch.cuda.ExternalStream(ctx.stream())
@@ -342,6 +343,7 @@ def run_gpu(args, wl):
     ctx.set_option("wavefront_graph", 0)
     r = integ.render(wl["spp"], wl["seed"], film=False)
     mr = ctx.metrics()
+    render_bvh_ms = round(mr.render_bvh_ms, 3)
     ctx.set_option("wavefront_graph", 1)
     stages = None
     if args.integrator == 0:
@@ -392,7 +394,9 @@ def run_gpu(args, wl):
                        "max_bounce": wl["max_bounce"], "rr_start": wl["rr_start"], "seed": wl["seed"],
                        "triangles": scene.info["triangles"],
                        "integrator": ["megakernel", "wavefront"][args.integrator],
-                       "bvh": "sorted-leaf LBVH" + (", collapsed 8-wide" if args.bvh_width == 8 else ""),
+                       "bvh": ("sorted-leaf LBVH" if args.bvh_width == 2 else
+                               ("PLOC tree over the LBVH's Morton order" if args.render_bvh else "sorted-leaf LBVH")
+                               + ", collapsed 8-wide"),
                        "l2": "inputs (BVH + triangles) exceed L2; no flush", "parallelism": f"replicas x{world}"},
             "mrays_per_s": round(r["rays"] / (r["render_ms"] * 1e-3) / 1e6, 2),
             "e2e": {"value": round(e2e, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -405,6 +409,7 @@ def run_gpu(args, wl):
                          "algorithmic": alg_text, "algorithmic_bytes_per_step": alg_bytes},
             "stage_ms": stages,
             "traversal": {"node_visits": r["node_visits"], "tri_tests": r["tri_tests"], "rays": r["rays"],
+                          "render_bvh_build_ms": render_bvh_ms,
                           "rays_by_kind": {"path": mr.kind_rays[0], "shadow": mr.kind_rays[1], "mis": mr.kind_rays[2]}},
             "lbvh": lbvh,
             "cpu_baseline": cpu,
@@ -591,6 +596,8 @@ def main():
                     help="traversal structure: 8-wide compressed BVH or the binary LBVH")
     ap.add_argument("--lbvh-only", type=int, default=0, metavar="N",
                     help="only time the LBVH build over N random triangles (seed 1)")
+    ap.add_argument("--render-bvh", type=int, default=1, choices=[0, 1],
+                    help="tree the 8-wide BVH is collapsed from: 1 PLOC clustering, 0 the LBVH itself")
     ap.add_argument("--views64", action="store_true", help="64 batched uneven views (autotuned, with the cache)")
     ap.add_argument("--mlp-only", action="store_true",
                     help="radiance-cache network alone: inference over 1920x1080 queries, one 65,536-sample training step")

@@ -236,7 +236,10 @@ int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts
  *                             launched in groups with one host check per group; 0: kernel by
  *                             kernel with host-sized grids and per-stage timing (lts_metrics)
  *   "bvh_width"               traversal structure: 8 (default) the 8-wide compressed BVH collapsed
- *                             from the LBVH, 2 the binary LBVH itself; both give the same hits
+ *                             from a binary tree, 2 the binary LBVH itself; all give the same hits
+ *   "render_bvh"              binary tree the 8-wide BVH is collapsed from: 1 (default) a
+ *                             surface-area tree clustered (PLOC) from the LBVH's Morton order,
+ *                             0 the LBVH itself
  *   "wavefront_pool"          path-state pool capacity in paths (0: automatic, 2^21)
  *   "wavefront_sample_chunk"  finished-sample buffer capacity in samples (0: automatic, 2^27);
  *                             samples per pixel are rendered in chunks that fit it
@@ -298,6 +301,8 @@ typedef struct {
     /* last lts_load_scene: host milliseconds parsing the files, and uploading the tables and
      * expanding them on the device (until the stream is idle) */
     double scene_parse_ms, scene_upload_ms;
+    /* device milliseconds of the last render-BVH rebuild (clustering + 8-wide collapse) */
+    double render_bvh_ms;
 } lts_metrics;
 int lts_get_metrics(lts_ctx* ctx, lts_metrics* out);
 

@@ -87,7 +87,7 @@ class Metrics(ctypes.Structure):
                 ("cache_queries", ctypes.c_double), ("cache_train_samples", ctypes.c_int32),
                 ("cache_train_loss", ctypes.c_double), ("cache_bias", ctypes.c_double),
                 ("cache_train_ms", ctypes.c_double), ("scene_parse_ms", ctypes.c_double),
-                ("scene_upload_ms", ctypes.c_double)]
+                ("scene_upload_ms", ctypes.c_double), ("render_bvh_ms", ctypes.c_double)]
 
 
 _lib = None

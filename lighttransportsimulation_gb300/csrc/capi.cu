@@ -622,6 +622,9 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
     } else if (!strcmp(key, "bvh_width")) {
         if (value != 2 && value != 8) return fail(ctx, LTS_ERR_ARG, "bvh_width must be 2 or 8");
         ctx->tracer->bvh_width = (int)value;
+    } else if (!strcmp(key, "render_bvh")) {
+        if (value != 0 && value != 1) return fail(ctx, LTS_ERR_ARG, "render_bvh must be 0 or 1");
+        ctx->tracer->render_bvh = (int)value;
     } else if (!strcmp(key, "wavefront_sample_chunk")) {
         ctx->tracer->wf_sample_cap = (long)value;
     } else {
@@ -657,6 +660,7 @@ int lts_get_metrics(lts_ctx* ctx, lts_metrics* out) {
     out->cache_train_loss = ctx->tracer ? ctx->tracer->last_train_loss : 0.0;
     out->cache_bias = ctx->tracer ? ctx->tracer->last_cache_bias : 0.0;
     out->cache_train_ms = ctx->tracer ? ctx->tracer->last_train_ms : 0.0;
+    out->render_bvh_ms = ctx->tracer ? ctx->tracer->last_render_bvh_ms : 0.0;
     for (int k = 0; k < 3; ++k) {
         out->kind_rays[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k] : 0.0;
         out->kind_node_visits[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k + 1] : 0.0;

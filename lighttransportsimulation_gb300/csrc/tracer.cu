@@ -356,8 +356,17 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
     // 8-wide compressed BVH collapsed from the binary tree (kept while the tree is unchanged); it
     // is used when the wide tree's depth fits the traversal stack
     bool use_wide = bvh_width == 8 && bvh.n >= 2;
-    if (use_wide && wide_.serial != bvh.serial) {
-        const std::string e = wide_.build(bvh, leaf_v_, s, d_err);
+    const uint64_t wide_key = 2 * bvh.serial + (render_bvh ? 1 : 0);  // the binary tree it is collapsed from
+    if (use_wide && wide_.serial != wide_key) {
+        std::string e;
+        if (render_bvh) {
+            e = ploc_.build(leaf_v_, bvh.n, s, d_err);
+            if (e.empty()) e = wide_.build(ploc_.nodes, bvh.n, wide_key, leaf_v_, s, d_err);
+            last_render_bvh_ms = ploc_.build_ms + wide_.build_ms;
+        } else {
+            e = wide_.build(bvh.nodes, bvh.n, wide_key, leaf_v_, s, d_err);
+            last_render_bvh_ms = wide_.build_ms;
+        }
         if (!e.empty()) return e;
     }
     if (use_wide && wide_.levels - 1 > kStack / 2) use_wide = false;

@@ -11,6 +11,7 @@
 #include "host_scene.hpp"
 #include "lbvh.cuh"
 #include "wide_bvh.cuh"
+#include "ploc.cuh"
 
 namespace lts {
 
@@ -120,6 +121,10 @@ class Tracer {
     long wf_pool = 0;
     // Traversal structure: 8 = the collapsed 8-wide compressed BVH, 2 = the binary LBVH.
     int bvh_width = 8;
+    // Binary tree the 8-wide BVH is collapsed from: 1 = PLOC over the LBVH's Morton order,
+    // 0 = the LBVH itself.
+    int render_bvh = 1;
+    float last_render_bvh_ms = 0;  // PLOC + collapse of the last rebuild
     // Radiance cache (wavefront integrator): on/off, the MLP it queries and trains (owned by the
     // context), the share of paths traced in full (per mille), training records per render, Adam
     // steps per render and learning rate; statistics of the last render.
@@ -171,6 +176,7 @@ class Tracer {
     unsigned wf_sms_ = 0;  // resident blocks of k_wf_trace (wide, binary) on this device
     SceneView view_{};
     WideBvh wide_;
+    PlocBvh ploc_;
     static constexpr int kSceneBufs = 16;
     void* bufs_[kSceneBufs] = {nullptr};   // scene tables, kept across scene loads while big enough
     size_t bufcap_[kSceneBufs] = {0};

@@ -218,7 +218,12 @@ WideBvh::~WideBvh() {
 }
 
 std::string WideBvh::build(const Lbvh& bvh, const float4* leaf_v, cudaStream_t s, uint32_t* d_err) {
-    n = bvh.n;
+    return build(bvh.nodes, bvh.n, bvh.serial, leaf_v, s, d_err);
+}
+
+std::string WideBvh::build(const BvhNode* bnodes, int nleaves, uint64_t key, const float4* leaf_v, cudaStream_t s,
+                           uint32_t* d_err) {
+    n = nleaves;
     count = levels = 0;
     serial = 0;
     if (n < 2) return "wide BVH needs at least two primitives";
@@ -250,7 +255,7 @@ std::string WideBvh::build(const Lbvh& bvh, const float4* leaf_v, cudaStream_t s
     int nin = 1;
     while (nin > 0) {
         TRY(cudaMemsetAsync(counters_ + 2, 0, 4, s));
-        k_collapse<<<(nin + 127) / 128, 128, 0, s>>>(bvh.nodes, leaf_v, in, nin, out, counters_, nodes, tris, n - 1, n,
+        k_collapse<<<(nin + 127) / 128, 128, 0, s>>>(bnodes, leaf_v, in, nin, out, counters_, nodes, tris, n - 1, n,
                                                      d_err);
         TRY(cudaGetLastError());
         TRY(cudaMemcpyAsync(counters_host_, counters_, 16, cudaMemcpyDeviceToHost, s));
@@ -270,7 +275,7 @@ std::string WideBvh::build(const Lbvh& bvh, const float4* leaf_v, cudaStream_t s
     TRY(cudaMemcpy(&flags, d_err, 4, cudaMemcpyDeviceToHost));
     if (flags & DEV_ERR_CAPACITY) return "wide BVH collapse overflowed its node or triangle capacity";
     if ((int)counters_host_[1] != n) return "wide BVH collapse lost triangles";
-    serial = bvh.serial;
+    serial = key;
     return "";
 }
 

@@ -50,11 +50,15 @@ class WideBvh {
     // Collapses `bvh` (n >= 2 leaves) whose leaf l holds triangle leaf_v[3l .. 3l+2] (w of the
     // first vertex = primitive id).  Synchronises on s once per tree level.
     std::string build(const Lbvh& bvh, const float4* leaf_v, cudaStream_t s, uint32_t* d_err);
+    // The same from any binary BVH over the n leaves of leaf_v (BvhNode form, root 0), cached
+    // under `key`.
+    std::string build(const BvhNode* bnodes, int nleaves, uint64_t key, const float4* leaf_v, cudaStream_t s,
+                      uint32_t* d_err);
 
     WideNode* nodes = nullptr;  // [count]; the root is node 0
     float4* tris = nullptr;     // [3 n] triangles in wide-leaf order
     int count = 0, levels = 0, n = 0;
-    uint64_t serial = 0;        // Lbvh::serial this was collapsed from
+    uint64_t serial = 0;        // key of the binary tree this was collapsed from
     float build_ms = 0;
 
    private:

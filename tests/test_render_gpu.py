@@ -215,3 +215,24 @@ def test_graph_and_kernel_by_kernel_iterations_agree(ctx, scene_dirs):
     assert np.array_equal(out[0]["sig"], out[1]["sig"])
     assert np.array_equal(out[0]["L"].view(np.uint32), out[1]["L"].view(np.uint32))
     assert np.array_equal(out[0]["film"].view(np.uint32), out[1]["film"].view(np.uint32))
+
+
+@pytest.mark.parametrize("kind", ["box_sphere", "materials"])
+def test_render_bvh_choice_finds_the_same_hits(ctx, scene_dirs, kind):
+    """The 8-wide BVH collapsed from the PLOC tree (render_bvh 1) and from the LBVH itself
+    (render_bvh 0) traverse the same triangles: the per-sample hit and visibility signatures
+    agree except where a ray meets an edge shared by two triangles at the same distance (the
+    test order then picks one of them), and the radiance agrees to 1e-4."""
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs[kind]
+    s = lts.Scene.parse(ctx, d, sc, sub, 64, 64)
+    integ = lts.PathTracingIntegrator(8, 3, s, integrator=1)
+    out = {}
+    for rb in (0, 1):
+        ctx.set_option("render_bvh", rb)
+        out[rb] = integ.render(8, 5, record=True)
+    ctx.set_option("render_bvh", 1)
+    same = (out[0]["sig"] == out[1]["sig"]).reshape(-1)
+    assert same.mean() >= 0.999
+    a, b = out[0]["L"].reshape(-1, 3)[same], out[1]["L"].reshape(-1, 3)[same]
+    assert np.all(np.abs(a - b) <= 1e-4 * np.maximum(1.0, np.abs(a)))
