@@ -395,8 +395,9 @@ def run_gpu(args, wl):
                        "triangles": scene.info["triangles"],
                        "integrator": ["megakernel", "wavefront"][args.integrator],
                        "bvh": ("sorted-leaf LBVH" if args.bvh_width == 2 else
-                               ("PLOC tree over the LBVH's Morton order" if args.render_bvh else "sorted-leaf LBVH")
-                               + ", collapsed 8-wide"),
+                               {0: "sorted-leaf LBVH, collapsed 8-wide (greedy)",
+                                1: "PLOC tree over the LBVH's Morton order, collapsed 8-wide (SAH-optimal)",
+                                2: "PLOC tree over the LBVH's Morton order, collapsed 8-wide (greedy)"}[args.render_bvh]),
                        "l2": "inputs (BVH + triangles) exceed L2; no flush", "parallelism": f"replicas x{world}"},
             "mrays_per_s": round(r["rays"] / (r["render_ms"] * 1e-3) / 1e6, 2),
             "e2e": {"value": round(e2e, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -596,8 +597,9 @@ def main():
                     help="traversal structure: 8-wide compressed BVH or the binary LBVH")
     ap.add_argument("--lbvh-only", type=int, default=0, metavar="N",
                     help="only time the LBVH build over N random triangles (seed 1)")
-    ap.add_argument("--render-bvh", type=int, default=1, choices=[0, 1],
-                    help="tree the 8-wide BVH is collapsed from: 1 PLOC clustering, 0 the LBVH itself")
+    ap.add_argument("--render-bvh", type=int, default=1, choices=[0, 1, 2],
+                    help="tree the 8-wide BVH is collapsed from: 1 PLOC clustering with the SAH-optimal "
+                         "collapse, 2 PLOC with the greedy collapse, 0 the LBVH itself")
     ap.add_argument("--views64", action="store_true", help="64 batched uneven views (autotuned, with the cache)")
     ap.add_argument("--mlp-only", action="store_true",
                     help="radiance-cache network alone: inference over 1920x1080 queries, one 65,536-sample training step")

@@ -239,7 +239,9 @@ int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts
  *                             from a binary tree, 2 the binary LBVH itself; all give the same hits
  *   "render_bvh"              binary tree the 8-wide BVH is collapsed from: 1 (default) a
  *                             surface-area tree clustered (PLOC) from the LBVH's Morton order,
- *                             0 the LBVH itself
+ *                             collapsed by the SAH-optimal choice of children; 2 the same tree
+ *                             collapsed greedily (largest child opened first); 0 the LBVH itself,
+ *                             collapsed greedily
  *   "wavefront_pool"          path-state pool capacity in paths (0: automatic, 2^21)
  *   "wavefront_sample_chunk"  finished-sample buffer capacity in samples (0: automatic, 2^27);
  *                             samples per pixel are rendered in chunks that fit it

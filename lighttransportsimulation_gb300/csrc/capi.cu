@@ -623,7 +623,7 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
         if (value != 2 && value != 8) return fail(ctx, LTS_ERR_ARG, "bvh_width must be 2 or 8");
         ctx->tracer->bvh_width = (int)value;
     } else if (!strcmp(key, "render_bvh")) {
-        if (value != 0 && value != 1) return fail(ctx, LTS_ERR_ARG, "render_bvh must be 0 or 1");
+        if (value < 0 || value > 2) return fail(ctx, LTS_ERR_ARG, "render_bvh must be 0, 1 or 2");
         ctx->tracer->render_bvh = (int)value;
     } else if (!strcmp(key, "wavefront_sample_chunk")) {
         ctx->tracer->wf_sample_cap = (long)value;

@@ -149,7 +149,8 @@ __global__ __launch_bounds__(kScanBlock) void k_ploc_apply(const float4* __restr
                                                            const int32_t* __restrict__ nn, const int2* __restrict__ excl,
                                                            const int2* __restrict__ block_pref, int nk, int node_base,
                                                            float4* __restrict__ lo_out, float4* __restrict__ hi_out,
-                                                           BvhNode* __restrict__ nodes, int node_cap, uint32_t* err) {
+                                                           BvhNode* __restrict__ nodes, float* __restrict__ sah,
+                                                           int node_cap, uint32_t* err) {
     const int i = blockIdx.x * kScanBlock + threadIdx.x;
     if (i >= nk) return;
     const int j = nn[i];
@@ -174,8 +175,30 @@ __global__ __launch_bounds__(kScanBlock) void k_ploc_apply(const float4* __restr
     P[1] = make_float4(ihi.y, ihi.z, jlo.x, jlo.y);
     P[2] = make_float4(jlo.z, jhi.x, jhi.y, jhi.z);
     reinterpret_cast<int4*>(P)[3] = make_int4(__float_as_int(ilo.w), __float_as_int(jlo.w), 0, 0);
-    lo_out[pos] = make_float4(fminf(ilo.x, jlo.x), fminf(ilo.y, jlo.y), fminf(ilo.z, jlo.z), __int_as_float(node));
-    hi_out[pos] = make_float4(fmaxf(ihi.x, jhi.x), fmaxf(ihi.y, jhi.y), fmaxf(ihi.z, jhi.z), 0.f);
+    const float4 ulo = make_float4(fminf(ilo.x, jlo.x), fminf(ilo.y, jlo.y), fminf(ilo.z, jlo.z), __int_as_float(node));
+    const float4 uhi = make_float4(fmaxf(ihi.x, jhi.x), fmaxf(ihi.y, jhi.y), fmaxf(ihi.z, jhi.z), 0.f);
+    lo_out[pos] = ulo;
+    hi_out[pos] = uhi;
+    // SAH collapse costs of the new node from its children's (formed in earlier iterations)
+    float cl[8], cr[8];
+    const int ci = __float_as_int(ilo.w), cj = __float_as_int(jlo.w);
+    for (int k = 0; k < 8; ++k) {
+        cl[k] = ci < 0 ? kSahTri * union_half_area(ilo, ihi, ilo, ihi) : sah[8 * (size_t)ci + k];
+        cr[k] = cj < 0 ? kSahTri * union_half_area(jlo, jhi, jlo, jhi) : sah[8 * (size_t)cj + k];
+    }
+    float dist[9];  // dist[i]: best split of i slots between the two children
+    for (int i = 2; i <= 8; ++i) {
+        float b = INFINITY;
+        for (int k = 1; k < i; ++k) b = fminf(b, cl[k - 1] + cr[i - k - 1]);
+        dist[i] = b;
+    }
+    float c = kSahNode * union_half_area(ulo, uhi, ulo, uhi) + dist[8];  // C(node, 1): its own wide node
+    float* out_c = sah + 8 * (size_t)node;
+    out_c[0] = c;
+    for (int i = 2; i <= 8; ++i) {
+        c = fminf(c, dist[i]);
+        out_c[i - 1] = c;
+    }
 }
 
 }  // namespace
@@ -187,10 +210,11 @@ __global__ __launch_bounds__(kScanBlock) void k_ploc_apply(const float4* __restr
     } while (0)
 
 void PlocBvh::release() {
-    void* ptrs[] = {nodes, lo_a_, hi_a_, lo_b_, hi_b_, nn_, excl_, block_sums_, counters_};
+    void* ptrs[] = {nodes, sah, lo_a_, hi_a_, lo_b_, hi_b_, nn_, excl_, block_sums_, counters_};
     for (void* p : ptrs)
         if (p) dev_free(p);
     nodes = nullptr;
+    sah = nullptr;
     lo_a_ = hi_a_ = lo_b_ = hi_b_ = nullptr;
     nn_ = nullptr;
     excl_ = block_sums_ = nullptr;
@@ -211,6 +235,7 @@ std::string PlocBvh::build(const float4* leaf_v, int nl, cudaStream_t s, uint32_
         release();
         const size_t N = (size_t)n;
         TRY(dev_alloc((void**)&nodes, sizeof(BvhNode) * (N - 1)));
+        TRY(dev_alloc((void**)&sah, 32 * (N - 1)));
         TRY(dev_alloc((void**)&lo_a_, 16 * N));
         TRY(dev_alloc((void**)&hi_a_, 16 * N));
         TRY(dev_alloc((void**)&lo_b_, 16 * N));
@@ -235,8 +260,8 @@ std::string PlocBvh::build(const float4* leaf_v, int nl, cudaStream_t s, uint32_
         k_ploc_nn<<<grid_of(nk, kPlocBlock), kPlocBlock, 0, s>>>(lo, hi, nk, nn_);
         k_ploc_scan<<<nb, kScanBlock, 0, s>>>(nn_, nk, excl_, block_sums_);
         k_ploc_block_prefix<<<1, kScanBlock, 0, s>>>(block_sums_, nb, counters_);
-        k_ploc_apply<<<nb, kScanBlock, 0, s>>>(lo, hi, nn_, excl_, block_sums_, nk, node_base, lo2, hi2, nodes, n - 1,
-                                               d_err);
+        k_ploc_apply<<<nb, kScanBlock, 0, s>>>(lo, hi, nn_, excl_, block_sums_, nk, node_base, lo2, hi2, nodes, sah,
+                                               n - 1, d_err);
         TRY(cudaGetLastError());
         TRY(cudaMemcpyAsync(counters_host_, counters_, 8, cudaMemcpyDeviceToHost, s));
         TRY(cudaStreamSynchronize(s));

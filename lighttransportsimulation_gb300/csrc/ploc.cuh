@@ -23,6 +23,7 @@ namespace lts {
 #define LTS_PLOC_RADIUS 8  // neighbours searched on either side of a cluster (8, 16, 32, 64 measured)
 #endif
 constexpr int kPlocRadius = LTS_PLOC_RADIUS;
+constexpr float kSahNode = 1.0f, kSahTri = 0.3f;
 
 class PlocBvh {
    public:
@@ -37,6 +38,10 @@ class PlocBvh {
     std::string build(const float4* leaf_v, int n, cudaStream_t s, uint32_t* d_err);
 
     BvhNode* nodes = nullptr;  // [n - 1]
+    // [n - 1][8]: sah[8 k + i - 1] = C(k, i), the smallest SAH cost of covering node k's subtree
+    // with at most i children of an 8-wide node (Ylitie, Karras and Laine, HPG 2017: node cost
+    // kSahNode, triangle cost kSahTri, one triangle per leaf), filled as the nodes are formed
+    float* sah = nullptr;
     int n = 0, iterations = 0;
     float build_ms = 0;
 

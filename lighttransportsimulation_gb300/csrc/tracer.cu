@@ -356,15 +356,17 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
     // 8-wide compressed BVH collapsed from the binary tree (kept while the tree is unchanged); it
     // is used when the wide tree's depth fits the traversal stack
     bool use_wide = bvh_width == 8 && bvh.n >= 2;
-    const uint64_t wide_key = 2 * bvh.serial + (render_bvh ? 1 : 0);  // the binary tree it is collapsed from
+    const uint64_t wide_key = 4 * bvh.serial + (uint64_t)render_bvh;  // the binary tree and collapse it came from
     if (use_wide && wide_.serial != wide_key) {
         std::string e;
         if (render_bvh) {
             e = ploc_.build(leaf_v_, bvh.n, s, d_err);
-            if (e.empty()) e = wide_.build(ploc_.nodes, bvh.n, wide_key, leaf_v_, s, d_err);
+            if (e.empty())
+                e = wide_.build(ploc_.nodes, render_bvh == 1 ? ploc_.sah : nullptr, bvh.n, wide_key, leaf_v_, s,
+                                d_err);
             last_render_bvh_ms = ploc_.build_ms + wide_.build_ms;
         } else {
-            e = wide_.build(bvh.nodes, bvh.n, wide_key, leaf_v_, s, d_err);
+            e = wide_.build(bvh.nodes, nullptr, bvh.n, wide_key, leaf_v_, s, d_err);
             last_render_bvh_ms = wide_.build_ms;
         }
         if (!e.empty()) return e;

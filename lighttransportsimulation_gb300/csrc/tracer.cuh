@@ -121,8 +121,8 @@ class Tracer {
     long wf_pool = 0;
     // Traversal structure: 8 = the collapsed 8-wide compressed BVH, 2 = the binary LBVH.
     int bvh_width = 8;
-    // Binary tree the 8-wide BVH is collapsed from: 1 = PLOC over the LBVH's Morton order,
-    // 0 = the LBVH itself.
+    // Binary tree the 8-wide BVH is collapsed from, and how: 1 = PLOC over the LBVH's Morton
+    // order, SAH-optimal collapse; 2 = the PLOC tree, greedy collapse; 0 = the LBVH itself, greedy.
     int render_bvh = 1;
     float last_render_bvh_ms = 0;  // PLOC + collapse of the last rebuild
     // Radiance cache (wavefront integrator): on/off, the MLP it queries and trains (owned by the

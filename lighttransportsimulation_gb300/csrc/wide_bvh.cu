@@ -6,6 +6,7 @@
 #include <string>
 
 #include "dev_common.cuh"
+#include "ploc.cuh"
 #include "wide_bvh.cuh"
 
 namespace lts {
@@ -40,36 +41,120 @@ __device__ int axis_exponent(float ext) {
     return max(e, -126);
 }
 
-// One item: interior binary node it.x becomes wide node it.y.  Children are gathered by
-// repeatedly opening the interior child of largest surface area until there are eight or only
-// leaves remain; slots are assigned greedily so that slot s (bit 0: +x, bit 1: +y, bit 2: +z)
-// holds the child whose centroid lies furthest towards that octant of the node.
-__global__ __launch_bounds__(128) void k_collapse(const BvhNode* __restrict__ bn, const float4* __restrict__ leaf_v,
-                                                  const int2* __restrict__ in, int nin, int2* __restrict__ out,
-                                                  uint32_t* counters, WideNode* __restrict__ wn,
-                                                  float4* __restrict__ wtri, int cap_nodes, int cap_tris,
-                                                  uint32_t* err) {
+// SAH collapse costs of a child: its row of the cost table (interior), or kSahTri x its half
+// area for every slot count (a leaf: one triangle).
+__device__ __forceinline__ void child_costs(const Child& c, const float* __restrict__ sah, float out[8]) {
+    if (c.ref < 0) {
+        const float v = kSahTri * half_area(c);
+        for (int k = 0; k < 8; ++k) out[k] = v;
+    } else {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(sah + 8 * (size_t)c.ref));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(sah + 8 * (size_t)c.ref) + 1);
+        out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
+        out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
+    }
+}
+
+// Slots given to the left child when i >= 2 slots are split between l and r: the k in 1..i-1
+// with the smallest C(l, k) + C(r, i - k) (the smallest k among equal costs).
+__device__ __forceinline__ int best_split(const Child& l, const Child& r, int i, const float* __restrict__ sah) {
+    float cl[8], cr[8];
+    child_costs(l, sah, cl);
+    child_costs(r, sah, cr);
+    int bk = 1;
+    float bc = INFINITY;
+    for (int k = 1; k < i; ++k) {
+        const float c = cl[k - 1] + cr[i - k - 1];
+        if (c < bc) {
+            bc = c;
+            bk = k;
+        }
+    }
+    return bk;
+}
+
+// One item: interior binary node it.x becomes wide node it.y.
+//   kSah false: children are gathered by repeatedly opening the interior child of largest
+//     surface area until there are eight or only leaves remain.
+//   kSah true: the SAH-optimal choice of the cost table (Ylitie, Karras and Laine, HPG 2017):
+//     the node's two binary children share its eight slots at the best split; a subtree given
+//     i slots takes the fewest slots i' <= i of equal cost C(n, i') = C(n, i), and with i' = 1
+//     becomes one interior child (a wide node of its own), else splits i' between its children
+//     the same way.  Every subtree is given at least one slot and the shares sum to at most
+//     eight, so at most eight children result (and the pending list never holds more than eight).
+// Slots are assigned greedily so that slot s (bit 0: +x, bit 1: +y, bit 2: +z) holds the child
+// whose centroid lies furthest towards that octant of the node.
+template <bool kSah>
+__global__ __launch_bounds__(128) void k_collapse(const BvhNode* __restrict__ bn, const float* __restrict__ sah,
+                                                  const float4* __restrict__ leaf_v, const int2* __restrict__ in,
+                                                  int nin, int2* __restrict__ out, uint32_t* counters,
+                                                  WideNode* __restrict__ wn, float4* __restrict__ wtri, int cap_nodes,
+                                                  int cap_tris, uint32_t* err) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nin) return;
     const int2 it = in[t];
     Child ch[8];
-    int cnt = 2;
-    split_node(bn[it.x], ch[0], ch[1]);
-    while (cnt < 8) {
-        int best = -1;
-        float ba = -1.0f;
-        for (int k = 0; k < cnt; ++k)
-            if (ch[k].ref >= 0) {
-                const float a = half_area(ch[k]);
-                if (a > ba) {
-                    ba = a;
-                    best = k;
-                }
+    int cnt = 0;
+    if constexpr (kSah) {
+        Child pend[8];
+        int budget[8];
+        int np = 0;
+        Child l, r;
+        split_node(bn[it.x], l, r);
+        int k = best_split(l, r, 8, sah);
+        pend[0] = r;
+        budget[0] = 8 - k;
+        pend[1] = l;
+        budget[1] = k;
+        np = 2;
+        while (np > 0) {
+            --np;
+            const Child c = pend[np];
+            int i = budget[np];
+            if (c.ref >= 0 && i > 1) {
+                float cc[8];
+                child_costs(c, sah, cc);
+                while (i > 1 && cc[i - 2] == cc[i - 1]) --i;
             }
-        if (best < 0) break;
-        const BvhNode nd = bn[ch[best].ref];
-        split_node(nd, ch[best], ch[cnt]);
-        ++cnt;
+            if (c.ref < 0 || i == 1) {
+                if (cnt >= 8) {  // unreachable: the shares never exceed eight slots
+                    atomicOr(err, DEV_ERR_CAPACITY);
+                    return;
+                }
+                ch[cnt++] = c;
+                continue;
+            }
+            if (np + 2 > 8) {  // unreachable: every pending share is at least one slot
+                atomicOr(err, DEV_ERR_CAPACITY);
+                return;
+            }
+            split_node(bn[c.ref], l, r);
+            k = best_split(l, r, i, sah);
+            pend[np] = r;
+            budget[np] = i - k;
+            pend[np + 1] = l;
+            budget[np + 1] = k;
+            np += 2;
+        }
+    } else {
+        cnt = 2;
+        split_node(bn[it.x], ch[0], ch[1]);
+        while (cnt < 8) {
+            int best = -1;
+            float ba = -1.0f;
+            for (int k = 0; k < cnt; ++k)
+                if (ch[k].ref >= 0) {
+                    const float a = half_area(ch[k]);
+                    if (a > ba) {
+                        ba = a;
+                        best = k;
+                    }
+                }
+            if (best < 0) break;
+            const BvhNode nd = bn[ch[best].ref];
+            split_node(nd, ch[best], ch[cnt]);
+            ++cnt;
+        }
     }
     float nlo[3], nhi[3];
     for (int a = 0; a < 3; ++a) {
@@ -218,11 +303,11 @@ WideBvh::~WideBvh() {
 }
 
 std::string WideBvh::build(const Lbvh& bvh, const float4* leaf_v, cudaStream_t s, uint32_t* d_err) {
-    return build(bvh.nodes, bvh.n, bvh.serial, leaf_v, s, d_err);
+    return build(bvh.nodes, nullptr, bvh.n, bvh.serial, leaf_v, s, d_err);
 }
 
-std::string WideBvh::build(const BvhNode* bnodes, int nleaves, uint64_t key, const float4* leaf_v, cudaStream_t s,
-                           uint32_t* d_err) {
+std::string WideBvh::build(const BvhNode* bnodes, const float* sah, int nleaves, uint64_t key, const float4* leaf_v,
+                           cudaStream_t s, uint32_t* d_err) {
     n = nleaves;
     count = levels = 0;
     serial = 0;
@@ -255,8 +340,12 @@ std::string WideBvh::build(const BvhNode* bnodes, int nleaves, uint64_t key, con
     int nin = 1;
     while (nin > 0) {
         TRY(cudaMemsetAsync(counters_ + 2, 0, 4, s));
-        k_collapse<<<(nin + 127) / 128, 128, 0, s>>>(bnodes, leaf_v, in, nin, out, counters_, nodes, tris, n - 1, n,
-                                                     d_err);
+        if (sah)
+            k_collapse<true><<<(nin + 127) / 128, 128, 0, s>>>(bnodes, sah, leaf_v, in, nin, out, counters_, nodes,
+                                                               tris, n - 1, n, d_err);
+        else
+            k_collapse<false><<<(nin + 127) / 128, 128, 0, s>>>(bnodes, sah, leaf_v, in, nin, out, counters_, nodes,
+                                                                tris, n - 1, n, d_err);
         TRY(cudaGetLastError());
         TRY(cudaMemcpyAsync(counters_host_, counters_, 16, cudaMemcpyDeviceToHost, s));
         TRY(cudaStreamSynchronize(s));

@@ -51,9 +51,10 @@ class WideBvh {
     // first vertex = primitive id).  Synchronises on s once per tree level.
     std::string build(const Lbvh& bvh, const float4* leaf_v, cudaStream_t s, uint32_t* d_err);
     // The same from any binary BVH over the n leaves of leaf_v (BvhNode form, root 0), cached
-    // under `key`.
-    std::string build(const BvhNode* bnodes, int nleaves, uint64_t key, const float4* leaf_v, cudaStream_t s,
-                      uint32_t* d_err);
+    // under `key`; with `sah` (the tree's collapse cost table, PlocBvh::sah) the children of each
+    // wide node are the SAH-optimal choice, without it the greedy largest-area opening.
+    std::string build(const BvhNode* bnodes, const float* sah, int nleaves, uint64_t key, const float4* leaf_v,
+                      cudaStream_t s, uint32_t* d_err);
 
     WideNode* nodes = nullptr;  // [count]; the root is node 0
     float4* tris = nullptr;     // [3 n] triangles in wide-leaf order

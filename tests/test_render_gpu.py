@@ -219,20 +219,22 @@ def test_graph_and_kernel_by_kernel_iterations_agree(ctx, scene_dirs):
 
 @pytest.mark.parametrize("kind", ["box_sphere", "materials"])
 def test_render_bvh_choice_finds_the_same_hits(ctx, scene_dirs, kind):
-    """The 8-wide BVH collapsed from the PLOC tree (render_bvh 1) and from the LBVH itself
-    (render_bvh 0) traverse the same triangles: the per-sample hit and visibility signatures
-    agree except where a ray meets an edge shared by two triangles at the same distance (the
-    test order then picks one of them), and the radiance agrees to 1e-4."""
+    """The 8-wide BVH collapsed from the PLOC tree (render_bvh 1: SAH-optimal collapse, 2:
+    greedy) and from the LBVH itself (render_bvh 0) traverse the same triangles: the per-sample
+    hit and visibility signatures agree except where a ray meets an edge shared by two triangles
+    at the same distance (the test order then picks one of them), and the radiance agrees to
+    1e-4."""
     import lighttransportsimulation_gb300 as lts
     d, sc, sub = scene_dirs[kind]
     s = lts.Scene.parse(ctx, d, sc, sub, 64, 64)
     integ = lts.PathTracingIntegrator(8, 3, s, integrator=1)
     out = {}
-    for rb in (0, 1):
+    for rb in (0, 1, 2):
         ctx.set_option("render_bvh", rb)
         out[rb] = integ.render(8, 5, record=True)
     ctx.set_option("render_bvh", 1)
-    same = (out[0]["sig"] == out[1]["sig"]).reshape(-1)
-    assert same.mean() >= 0.999
-    a, b = out[0]["L"].reshape(-1, 3)[same], out[1]["L"].reshape(-1, 3)[same]
-    assert np.all(np.abs(a - b) <= 1e-4 * np.maximum(1.0, np.abs(a)))
+    for rb in (1, 2):
+        same = (out[0]["sig"] == out[rb]["sig"]).reshape(-1)
+        assert same.mean() >= 0.999
+        a, b = out[0]["L"].reshape(-1, 3)[same], out[rb]["L"].reshape(-1, 3)[same]
+        assert np.all(np.abs(a - b) <= 1e-4 * np.maximum(1.0, np.abs(a)))
