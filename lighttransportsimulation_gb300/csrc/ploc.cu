@@ -174,14 +174,14 @@ __global__ __launch_bounds__(kScanBlock) void k_ploc_apply(const float4* __restr
     P[0] = make_float4(ilo.x, ilo.y, ilo.z, ihi.x);
     P[1] = make_float4(ihi.y, ihi.z, jlo.x, jlo.y);
     P[2] = make_float4(jlo.z, jhi.x, jhi.y, jhi.z);
-    reinterpret_cast<int4*>(P)[3] = make_int4(__float_as_int(ilo.w), __float_as_int(jlo.w), 0, 0);
+    const int ci = __float_as_int(ilo.w), cj = __float_as_int(jlo.w);
+    const int count = (ci < 0 ? 1 : nodes[ci].d.z) + (cj < 0 ? 1 : nodes[cj].d.z);
     const float4 ulo = make_float4(fminf(ilo.x, jlo.x), fminf(ilo.y, jlo.y), fminf(ilo.z, jlo.z), __int_as_float(node));
     const float4 uhi = make_float4(fmaxf(ihi.x, jhi.x), fmaxf(ihi.y, jhi.y), fmaxf(ihi.z, jhi.z), 0.f);
     lo_out[pos] = ulo;
     hi_out[pos] = uhi;
     // SAH collapse costs of the new node from its children's (formed in earlier iterations)
     float cl[8], cr[8];
-    const int ci = __float_as_int(ilo.w), cj = __float_as_int(jlo.w);
     for (int k = 0; k < 8; ++k) {
         cl[k] = ci < 0 ? kSahTri * union_half_area(ilo, ihi, ilo, ihi) : sah[8 * (size_t)ci + k];
         cr[k] = cj < 0 ? kSahTri * union_half_area(jlo, jhi, jlo, jhi) : sah[8 * (size_t)cj + k];
@@ -192,7 +192,13 @@ __global__ __launch_bounds__(kScanBlock) void k_ploc_apply(const float4* __restr
         for (int k = 1; k < i; ++k) b = fminf(b, cl[k - 1] + cr[i - k - 1]);
         dist[i] = b;
     }
-    float c = kSahNode * union_half_area(ulo, uhi, ulo, uhi) + dist[8];  // C(node, 1): its own wide node
+    // C(node, 1): its own wide node, or one leaf slot of all its triangles
+    const float area = union_half_area(ulo, uhi, ulo, uhi);
+    const float c_node = kSahNode * area + dist[8];
+    const float c_leaf = count <= kWideLeafMax ? kSahTri * area * (float)count : INFINITY;
+    const bool leaf_slot = c_leaf < c_node;
+    float c = leaf_slot ? c_leaf : c_node;
+    reinterpret_cast<int4*>(P)[3] = make_int4(ci, cj, count, leaf_slot ? 1 : 0);
     float* out_c = sah + 8 * (size_t)node;
     out_c[0] = c;
     for (int i = 2; i <= 8; ++i) {

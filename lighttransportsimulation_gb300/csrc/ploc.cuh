@@ -23,7 +23,15 @@ namespace lts {
 #define LTS_PLOC_RADIUS 8  // neighbours searched on either side of a cluster (8, 16, 32, 64 measured)
 #endif
 constexpr int kPlocRadius = LTS_PLOC_RADIUS;
-constexpr float kSahNode = 1.0f, kSahTri = 0.3f;
+#ifndef LTS_SAH_TRI
+#define LTS_SAH_TRI 0.5f  // SAH cost of a triangle test relative to a wide-node visit (0.2 .. 1.0 measured)
+#endif
+constexpr float kSahNode = 1.0f, kSahTri = LTS_SAH_TRI;
+#ifndef LTS_WIDE_LEAF_MAX
+#define LTS_WIDE_LEAF_MAX 3  // triangles one leaf slot of an 8-wide node may hold (1, 2, 3 measured)
+#endif
+constexpr int kWideLeafMax = LTS_WIDE_LEAF_MAX;
+static_assert(kWideLeafMax >= 1 && kWideLeafMax <= 3, "a leaf slot holds one to three triangles");
 
 class PlocBvh {
    public:
@@ -33,14 +41,17 @@ class PlocBvh {
     PlocBvh& operator=(const PlocBvh&) = delete;
 
     // Binary BVH over the n >= 2 leaves of leaf_v (3 float4 per leaf: the triangle of leaf l)
-    // in BvhNode form (nodes[0] the root; child >= 0 an interior node, < 0 leaf ~l; d.z, d.w 0).
+    // in BvhNode form (nodes[0] the root; child >= 0 an interior node, < 0 leaf ~l; d.z the
+    // subtree's triangle count, d.w 1 when the subtree's smallest one-slot cost C(k, 1) is a leaf
+    // slot holding all its triangles, else 0).
     // Synchronises on s once per clustering iteration.
     std::string build(const float4* leaf_v, int n, cudaStream_t s, uint32_t* d_err);
 
     BvhNode* nodes = nullptr;  // [n - 1]
     // [n - 1][8]: sah[8 k + i - 1] = C(k, i), the smallest SAH cost of covering node k's subtree
     // with at most i children of an 8-wide node (Ylitie, Karras and Laine, HPG 2017: node cost
-    // kSahNode, triangle cost kSahTri, one triangle per leaf), filled as the nodes are formed
+    // kSahNode, triangle cost kSahTri, leaf slots of up to kWideLeafMax triangles), filled as the
+    // nodes are formed
     float* sah = nullptr;
     int n = 0, iterations = 0;
     float build_ms = 0;

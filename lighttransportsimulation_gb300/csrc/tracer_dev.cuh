@@ -333,7 +333,7 @@ struct Trav {
     int best;  // closest: primitive (-1 none); any: 1 on a hit
     int node, sp;
     uint32_t gbase, gbits;
-    uint32_t lbits, lbase;  // split steps: pending leaf slots (bits 0-7) | leaf-slot mask << 8, first triangle
+    uint32_t lbits, lbase;  // split steps: the last node's pending triangles (bit k: triangle lbase + k)
 };
 
 // Returns true when the ray needs traversal steps; false when it is already resolved (missed
@@ -412,6 +412,19 @@ __device__ __forceinline__ uint32_t octant_order(uint32_t m, uint32_t oct) {
     return m;
 }
 
+// The triangles of a node's hit leaf slots `leaves`, given its leaf layout u (WideNode m.w):
+// bit k set = triangle m.y + k.  A slot's group of u is 1, 3 or 7, so shifting it to the count
+// of triangles in the slots before it gives the slot's triangles.
+__device__ __forceinline__ uint32_t leaf_tri_bits(uint32_t leaves, uint32_t u) {
+    uint32_t tb = 0;
+    while (leaves) {
+        const int s = __ffs(leaves) - 1;
+        leaves &= leaves - 1u;
+        tb |= ((u >> (3 * s)) & 7u) << __popc(u & ((1u << (3 * s)) - 1u));
+    }
+    return tb;
+}
+
 // One node; returns true when the traversal has finished.
 __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const SceneView& sv, uint32_t* stack,
                                                uint32_t* err, Work& wk) {
@@ -467,11 +480,10 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
             }
         }
     }
-    const uint32_t lmask = omask & ~imask;
-    while (leaves) {
-        const int s = __ffs(leaves) - 1;
-        leaves &= leaves - 1u;
-        const int tri = (int)m.y + __popc(lmask & ((1u << s) - 1u));
+    uint32_t tb = leaves ? leaf_tri_bits(leaves, m.w) : 0u;
+    while (tb) {
+        const int tri = (int)m.y + __ffs(tb) - 1;
+        tb &= tb - 1u;
         if ((unsigned)tri >= (unsigned)sv.ntri) {
             atomicOr(err, DEV_ERR_BAD_INDEX);
             return true;
@@ -569,7 +581,7 @@ __device__ __forceinline__ bool wide_node_step(const bool any, Trav& t, const Sc
         }
     }
     if (leaves) {
-        t.lbits = leaves | ((omask & ~imask) << 8);
+        t.lbits = leaf_tri_bits(leaves, m.w);
         t.lbase = m.y;
     }
     if (hits) {
@@ -603,9 +615,8 @@ __device__ __forceinline__ bool wide_node_step(const bool any, Trav& t, const Sc
 
 
 __device__ __forceinline__ bool wide_leaf_step(const bool any, Trav& t, const SceneView& sv, uint32_t* err, Work& wk) {
-    const int s = __ffs(t.lbits & 0xffu) - 1;
-    const int tri = (int)t.lbase + __popc((t.lbits >> 8) & ((1u << s) - 1u));
-    t.lbits &= ~(1u << s);
+    const int tri = (int)t.lbase + __ffs(t.lbits) - 1;
+    t.lbits &= t.lbits - 1u;
     if ((unsigned)tri >= (unsigned)sv.ntri) {
         atomicOr(err, DEV_ERR_BAD_INDEX);
         return true;
@@ -615,7 +626,6 @@ __device__ __forceinline__ bool wide_leaf_step(const bool any, Trav& t, const Sc
         t.best = 1;
         return true;
     }
-    if (!(t.lbits & 0xffu)) t.lbits = 0u;
     return t.lbits == 0u && t.node < 0;
 }
 

@@ -345,7 +345,7 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
             if (WIDE) {
                 // lanes with pending leaf triangles and lanes due a node visit: the warp runs
                 // whichever step more of its lanes wait for
-                const bool has_leaf = active && (t.lbits & 0xffu) != 0u;
+                const bool has_leaf = active && t.lbits != 0u;
                 const bool want_node = active && !has_leaf;
                 const unsigned lm = __ballot_sync(~0u, has_leaf), nm = __ballot_sync(~0u, want_node);
                 const bool leaf_mode = lm != 0u && __popc(lm) * 4 >= __popc(nm) * kLeafBias;

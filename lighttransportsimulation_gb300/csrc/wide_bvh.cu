@@ -14,16 +14,48 @@ namespace {
 
 struct Child {
     float lo[3], hi[3];
-    int ref;  // >= 0 interior binary node, < 0 leaf ~l
+    int ref;     // >= 0 interior binary node, < 0 leaf ~l
+    int ntri;    // 0: an interior child (a wide node of its own); 1..3: a leaf slot of these leaves
+    int leaf[3];
 };
+
+__device__ __forceinline__ void set_ref(Child& c, int ref) {
+    c.ref = ref;
+    c.ntri = ref < 0 ? 1 : 0;
+    c.leaf[0] = ~ref;
+}
 
 __device__ __forceinline__ void split_node(const BvhNode& nd, Child& l, Child& r) {
     l.lo[0] = nd.a.x; l.lo[1] = nd.a.y; l.lo[2] = nd.a.z;
     l.hi[0] = nd.a.w; l.hi[1] = nd.b.x; l.hi[2] = nd.b.y;
     r.lo[0] = nd.b.z; r.lo[1] = nd.b.w; r.lo[2] = nd.c.x;
     r.hi[0] = nd.c.y; r.hi[1] = nd.c.z; r.hi[2] = nd.c.w;
-    l.ref = nd.d.x;
-    r.ref = nd.d.y;
+    set_ref(l, nd.d.x);
+    set_ref(r, nd.d.y);
+}
+
+// Turns interior child c (a subtree of at most kWideLeafMax triangles) into one leaf slot of all
+// its leaves; false if it has more.
+__device__ __forceinline__ bool gather_leaf_slot(const BvhNode* __restrict__ bn, Child& c) {
+    int st[kWideLeafMax];
+    int ns = 0;
+    st[ns++] = c.ref;
+    c.ntri = 0;
+    while (ns > 0) {
+        const int4 d = __ldg(&bn[st[--ns]].d);
+        const int xs[2] = {d.x, d.y};
+        for (int h = 0; h < 2; ++h) {
+            const int x = xs[h];
+            if (x < 0) {
+                if (c.ntri >= kWideLeafMax) return false;
+                c.leaf[c.ntri++] = ~x;
+            } else {
+                if (ns >= kWideLeafMax) return false;
+                st[ns++] = x;
+            }
+        }
+    }
+    return true;
 }
 
 __device__ __forceinline__ float half_area(const Child& c) {
@@ -82,6 +114,8 @@ __device__ __forceinline__ int best_split(const Child& l, const Child& r, int i,
 //     becomes one interior child (a wide node of its own), else splits i' between its children
 //     the same way.  Every subtree is given at least one slot and the shares sum to at most
 //     eight, so at most eight children result (and the pending list never holds more than eight).
+//     A one-slot subtree whose cheapest form is a leaf slot (BvhNode d.w) becomes one leaf slot
+//     of its up to kWideLeafMax triangles.
 // Slots are assigned greedily so that slot s (bit 0: +x, bit 1: +y, bit 2: +z) holds the child
 // whose centroid lies furthest towards that octant of the node.
 template <bool kSah>
@@ -121,7 +155,12 @@ __global__ __launch_bounds__(128) void k_collapse(const BvhNode* __restrict__ bn
                     atomicOr(err, DEV_ERR_CAPACITY);
                     return;
                 }
-                ch[cnt++] = c;
+                ch[cnt] = c;
+                if (c.ref >= 0 && __ldg(&bn[c.ref].d.w) && !gather_leaf_slot(bn, ch[cnt])) {
+                    atomicOr(err, DEV_ERR_CAPACITY);  // unreachable: d.w is set for small subtrees only
+                    return;
+                }
+                ++cnt;
                 continue;
             }
             if (np + 2 > 8) {  // unreachable: every pending share is at least one slot
@@ -190,17 +229,18 @@ __global__ __launch_bounds__(128) void k_collapse(const BvhNode* __restrict__ bn
         used |= 1u << bs;
         placed |= 1u << bk;
     }
-    uint32_t imask = 0, omask = 0;
+    uint32_t imask = 0, omask = 0, layout = 0;
     int ni = 0, nl = 0;
     for (int s = 0; s < 8; ++s) {
         const int k = slot_child[s];
         if (k < 0) continue;
         omask |= 1u << s;
-        if (ch[k].ref >= 0) {
+        if (ch[k].ntri == 0) {
             imask |= 1u << s;
             ++ni;
         } else {
-            ++nl;
+            layout |= ((1u << ch[k].ntri) - 1u) << (3 * s);
+            nl += ch[k].ntri;
         }
     }
     const uint32_t child_base = ni ? atomicAdd(counters + 0, (uint32_t)ni) : 0u;
@@ -252,7 +292,7 @@ __global__ __launch_bounds__(128) void k_collapse(const BvhNode* __restrict__ bn
     }
     WideNode w;
     w.h = make_float4(nlo[0], nlo[1], nlo[2], __uint_as_float(ebyte[0] | ebyte[1] << 8 | ebyte[2] << 16 | imask << 24));
-    w.m = make_uint4(child_base, tri_base, omask, 0u);
+    w.m = make_uint4(child_base, tri_base, omask, layout);
     w.q0 = make_uint4((uint32_t)qlo[0], (uint32_t)(qlo[0] >> 32), (uint32_t)qlo[1], (uint32_t)(qlo[1] >> 32));
     w.q1 = make_uint4((uint32_t)qlo[2], (uint32_t)(qlo[2] >> 32), (uint32_t)qhi[0], (uint32_t)(qhi[0] >> 32));
     w.q2 = make_uint4((uint32_t)qhi[1], (uint32_t)(qhi[1] >> 32), (uint32_t)qhi[2], (uint32_t)(qhi[2] >> 32));
@@ -261,17 +301,19 @@ __global__ __launch_bounds__(128) void k_collapse(const BvhNode* __restrict__ bn
     for (int s = 0; s < 8; ++s) {
         const int k = slot_child[s];
         if (k < 0) continue;
-        if (ch[k].ref >= 0) {
+        if (ch[k].ntri == 0) {
             const uint32_t pos = atomicAdd(counters + 2, 1u);
             out[pos] = make_int2(ch[k].ref, (int)child_base + ri);
             ++ri;
         } else {
-            const int l = ~ch[k].ref;
-            float4* dst = wtri + 3 * ((size_t)tri_base + rl);
-            dst[0] = __ldg(leaf_v + 3 * (size_t)l);
-            dst[1] = __ldg(leaf_v + 3 * (size_t)l + 1);
-            dst[2] = __ldg(leaf_v + 3 * (size_t)l + 2);
-            ++rl;
+            for (int j = 0; j < ch[k].ntri; ++j) {
+                const int l = ch[k].leaf[j];
+                float4* dst = wtri + 3 * ((size_t)tri_base + rl);
+                dst[0] = __ldg(leaf_v + 3 * (size_t)l);
+                dst[1] = __ldg(leaf_v + 3 * (size_t)l + 1);
+                dst[2] = __ldg(leaf_v + 3 * (size_t)l + 2);
+                ++rl;
+            }
         }
     }
 }

@@ -22,9 +22,10 @@ namespace lts {
 //   h.w    bits: e_x | e_y << 8 | e_z << 16 | imask << 24, e = biased exponent of the axis scale
 //          2^(e-127); imask bit s set: slot s is an interior child
 //   m.x    index of the first interior child (interior children are stored in slot order)
-//   m.y    index of the first leaf triangle (leaf children, one triangle each, in slot order)
+//   m.y    index of the first leaf triangle (the leaf children's triangles, in slot order)
 //   m.z    omask: bit s set: slot s is occupied
-//   m.w    unused
+//   m.w    leaf layout: bits 3s .. 3s+2 hold 1, 3 or 7 for a leaf slot s of 1, 2 or 3 triangles
+//          (0 for interior and empty slots), so triangle m.y + k is the k-th set bit of m.w
 //   q0     qlo_x[8] (x, y words), qlo_y[8] (z, w words); q1 = qlo_z[8], qhi_x[8];
 //   q2     qhi_y[8], qhi_z[8]; byte s of each 8-byte group belongs to slot s
 struct alignas(16) WideNode {
