@@ -308,6 +308,8 @@ def run_gpu(args, wl):
     scene = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
     ctx.set_option("bvh_width", args.bvh_width)
     ctx.set_option("render_bvh", args.render_bvh)
+    if args.pool:
+        ctx.set_option("wavefront_pool", args.pool)
     integ = lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], scene, integrator=args.integrator)
     desc = integ.desc(wl["spp"], wl["seed"])
     stream = torch.cuda.ExternalStream(ctx.stream())
@@ -398,6 +400,7 @@ def run_gpu(args, wl):
                                {0: "sorted-leaf LBVH, collapsed 8-wide (greedy)",
                                 1: "PLOC tree over the LBVH's Morton order, collapsed 8-wide (SAH-optimal)",
                                 2: "PLOC tree over the LBVH's Morton order, collapsed 8-wide (greedy)"}[args.render_bvh]),
+                       "path_pool": args.pool or "automatic (all paths of the render, up to 2^26)",
                        "l2": "inputs (BVH + triangles) exceed L2; no flush", "parallelism": f"replicas x{world}"},
             "mrays_per_s": round(r["rays"] / (r["render_ms"] * 1e-3) / 1e6, 2),
             "e2e": {"value": round(e2e, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -600,6 +603,8 @@ def main():
     ap.add_argument("--render-bvh", type=int, default=1, choices=[0, 1, 2],
                     help="tree the 8-wide BVH is collapsed from: 1 PLOC clustering with the SAH-optimal "
                          "collapse, 2 PLOC with the greedy collapse, 0 the LBVH itself")
+    ap.add_argument("--pool", type=int, default=0, metavar="PATHS",
+                    help="wavefront path-state pool capacity (0: the renderer's automatic size)")
     ap.add_argument("--views64", action="store_true", help="64 batched uneven views (autotuned, with the cache)")
     ap.add_argument("--mlp-only", action="store_true",
                     help="radiance-cache network alone: inference over 1920x1080 queries, one 65,536-sample training step")

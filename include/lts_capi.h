@@ -209,10 +209,11 @@ int lts_render_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts_r
                      float* const* films_rgb, lts_render_out* out);
 
 /* Autotuner (no counterpart in the reference): renders the views at 1/8 of their spp under each
- * candidate shape of the wavefront -- path-pool capacity 2^18 .. 2^22 (queue size), persistent
- * trace blocks per SM 2 / 4 / all resident (block shape), graph or kernel-by-kernel iterations --
- * one knob at a time from the current settings, keeps the fastest and leaves it set on the
- * context (the options wavefront_pool, trace_blocks_per_sm, wavefront_graph). */
+ * candidate shape of the wavefront -- path-pool capacity 2^18 .. 2^26 below the tuning render's
+ * path count, or the automatic pool (queue size), persistent trace blocks per SM 2 / 4 / all
+ * resident (block shape), graph or kernel-by-kernel iterations -- one knob at a time from the
+ * current settings, keeps the fastest and leaves it set on the context (the options
+ * wavefront_pool, trace_blocks_per_sm, wavefront_graph).  pool_log2 0: the automatic pool. */
 typedef struct {
     int32_t pool_log2, trace_blocks_per_sm, graph;
     double ms_default, ms_best; /* device ms of one tuning render before and after */
@@ -242,7 +243,9 @@ int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts
  *                             collapsed by the SAH-optimal choice of children; 2 the same tree
  *                             collapsed greedily (largest child opened first); 0 the LBVH itself,
  *                             collapsed greedily
- *   "wavefront_pool"          path-state pool capacity in paths (0: automatic, 2^21)
+ *   "wavefront_pool"          path-state pool capacity in paths (0: automatic -- every path of
+ *                             a batch at once, up to 2^26 slots and a quarter of the free
+ *                             device memory, ~400 B per slot, ~650 B with the radiance cache)
  *   "wavefront_sample_chunk"  finished-sample buffer capacity in samples (0: automatic, 2^27);
  *                             samples per pixel are rendered in chunks that fit it
  * Unknown keys and negative values return LTS_ERR_ARG. */

@@ -117,7 +117,7 @@ class Tracer {
                              uint32_t* d_err);
 
     double last_ms = 0, last_paths = 0, last_rays = 0, last_node_visits = 0, last_tri_tests = 0;
-    // Path-pool capacity of the wavefront integrator (0: automatic).
+    // Path-pool capacity of the wavefront integrator (0: automatic, see auto_pool).
     long wf_pool = 0;
     // Traversal structure: 8 = the collapsed 8-wide compressed BVH, 2 = the binary LBVH.
     int bvh_width = 8;
@@ -165,6 +165,10 @@ class Tracer {
     std::string run_wavefront(const std::vector<std::vector<WfView>>& batches, const Lbvh& bvh, cudaStream_t s,
                               uint32_t* d_err, const RenderParams& rp, const SceneView& sv);
     void* wf_bufs_[48] = {nullptr};
+    // Device bytes per pool slot: the path state and lists, and the radiance cache's features,
+    // prediction, query list and training-record links.
+    static constexpr size_t kPoolSlotBytes = 392, kCacheSlotBytes = 248;
+    long auto_pool(bool cache) const;
     long wf_cache_cap_ = 0, wf_train_cap_ = 0;
     std::string train_cache(uint32_t* d_counts, uint16_t* tr_feat, float* tr_target, uint32_t tr_cap, cudaStream_t s,
                             uint32_t* d_err);

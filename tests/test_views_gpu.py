@@ -58,7 +58,8 @@ def test_autotuner_picks_a_setting_and_keeps_results(ctx, scene_dirs):
     before, _ = lts.render_views(s, VIEWS, 5, 3)
     res = lts.autotune_views(s, VIEWS, 5, 3)
     print(res)
-    assert 18 <= res["pool_log2"] <= 22 and res["trace_blocks_per_sm"] in (0, 2, 4) and res["graph"] in (0, 1)
+    assert (res["pool_log2"] == 0 or 18 <= res["pool_log2"] <= 26) and res["trace_blocks_per_sm"] in (0, 2, 4) \
+        and res["graph"] in (0, 1)
     assert res["ms_best"] <= res["ms_default"]
     after, _ = lts.render_views(s, VIEWS, 5, 3)
     for a, b in zip(before, after):
