@@ -74,8 +74,9 @@ struct RenderParams {
 
 // One slice of a batched wavefront render: samples s_first .. s_first + nsc - 1 per pixel of a
 // view's crop.  Batch sample index w in [base, base + nsc * npix) maps to sample
-// s_first + (w - base) / npix of crop pixel (w - base) % npix (sample-major).  Plain data shared
-// by the host and the kernels.
+// s_first + (w - base) / npix of crop pixel (w - base) % npix in row-major order (sample-major;
+// the finished samples are stored in this order; generation visits the pixels in tiles).  Plain
+// data shared by the host and the kernels.
 constexpr int kMaxViews = 256;  // view slices per wavefront batch
 struct WfView {
     float cam[12];                 // origin, right, up, lower-left corner (HostScene::cam[0..11])

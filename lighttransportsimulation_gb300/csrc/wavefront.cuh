@@ -34,7 +34,8 @@ constexpr int kWfBlock = 128;
 constexpr uint64_t kSigBasis = 0xcbf29ce484222325ull;
 
 struct WfState {
-    int32_t *pix, *smp, *wid;  // pixel (within its view's film), sample, index within the batch
+    int32_t *pix, *smp, *wid;  // pixel (within its view's film), sample, the sample's batch index
+                               // in row-major pixel order (where finalize stores it)
     int32_t* view;             // slice of the batch the path belongs to
     const WfView* views;       // the batch's slices (count in WfCtl::nviews)
     uint32_t *draw, *flags, *pend, *vis;
@@ -152,6 +153,36 @@ __device__ __forceinline__ void camera_ray(const WfView& vw, float pfx, float pf
     ryd = rd + (dy0 - rd) * spp_scale;
 }
 
+// Order in which a slice's samples of one sample index visit the crop's pixels: 8 x 4 tiles
+// (one warp each) left to right in bands of four rows, so the rays a warp traces start from a
+// compact patch of the image instead of a 32 x 1 strip (partial tiles at the right and bottom
+// edges are row-major).  Position k in 0 .. cw * ch - 1 -> crop pixel (ci, cj).
+#ifndef LTS_PIXEL_TILES
+#define LTS_PIXEL_TILES 1  // 0: row-major pixel order
+#endif
+constexpr int kTileW = 8, kTileH = 4;
+__device__ __forceinline__ void tile_pixel(long k, int cw, int ch, int& ci, int& cj) {
+    if (!LTS_PIXEL_TILES) {
+        ci = (int)(k % cw);
+        cj = (int)(k / cw);
+        return;
+    }
+    const long band_px = (long)kTileH * cw;
+    const int band = (int)(k / band_px);
+    const int rows = min(kTileH, ch - band * kTileH);
+    const int o = (int)(k - band * band_px);
+    const int full = cw / kTileW, tile_px = kTileW * rows;
+    if (o < full * tile_px) {
+        const int tx = o / tile_px, r = o - tx * tile_px;
+        ci = tx * kTileW + r % kTileW;
+        cj = band * kTileH + r / kTileW;
+    } else {  // the narrower last tile of the band
+        const int rem = cw - full * kTileW, r = o - full * tile_px;
+        ci = full * kTileW + r % rem;
+        cj = band * kTileH + r / rem;
+    }
+}
+
 // generate: starts batch samples gen0 .. gen0 + take - 1 in the first `take` free slots,
 // appending them to the path-ray list after its `n_cont` continuing paths.
 __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, const RenderParams rp, WfState st,
@@ -169,7 +200,9 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, co
     const int cw = vw.x1 - vw.x0;
     const int s = vw.s_first + (int)(local / vw.npix);
     const long pc = local % vw.npix;
-    const int i = vw.x0 + (int)(pc % cw), j = vw.y0 + (int)(pc / cw);
+    int ci, cj;
+    tile_pixel(pc, cw, vw.y1 - vw.y0, ci, cj);
+    const int i = vw.x0 + ci, j = vw.y0 + cj;
     const int id = j * vw.W + i;
     Rng rng;
     rng.key = vw.seed + wang_hash((uint32_t)id);
@@ -183,7 +216,7 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, co
     st.view[slot] = v;
     st.pix[slot] = id;
     st.smp[slot] = s;
-    st.wid[slot] = (int32_t)w;
+    st.wid[slot] = (int32_t)(w - pc + (long)cj * cw + ci);  // the sample's place in row-major order
     st.draw[slot] = rng.draw;
     st.flags[slot] = (st.cache && wang_hash((uint32_t)id ^ ((uint32_t)s * 0x9E3779B9u)) % 1000u < st.unb_permille)
                          ? FL_UNBIASED : 0u;
