@@ -83,10 +83,15 @@ struct WfCtl {
 __device__ __forceinline__ float bsdf_roughness(const Bsdf& f) {
     return (f.lobe == LOBE_LAMBERT || f.lobe == LOBE_OREN_NAYAR) ? 1.0f : (f.lobe == LOBE_MICROFACET ? f.alpha : 0.0f);
 }
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
+}
+// The 96 features as bf16, written four at a time (8-byte words) as they are computed, so no
+// 96-entry array has to live in registers or local memory: sin of the 36 position angles at
+// 0..35, their cos at 36..71, then the 14 scalars at 72..85, zeros to 95.
 __device__ void write_features(const WfState& st, const SI& si, const Bsdf& f, uint16_t* out) {
-    float v[96];
-#pragma unroll
-    for (int k = 0; k < 96; ++k) v[k] = 0.0f;
+    uint2* o = reinterpret_cast<uint2*>(out);
     const float pc[3] = {si.p.x, si.p.y, si.p.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -94,35 +99,28 @@ __device__ void write_features(const WfState& st, const SI& si, const Bsdf& f, u
         const float u = ext > 0.0f ? (pc[a] - lo) / ext : 0.5f;
         float fr = 3.14159265358979f;
 #pragma unroll
-        for (int j = 0; j < 12; ++j) {
-            float sn, cs;
-            sincosf(u * fr, &sn, &cs);
-            v[a * 12 + j] = sn;
-            v[36 + a * 12 + j] = cs;
-            fr *= 2.0f;
+        for (int c = 0; c < 3; ++c) {  // frequencies 4c .. 4c + 3 of axis a
+            float sn[4], cs[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                sincosf(u * fr, &sn[q], &cs[q]);
+                fr *= 2.0f;
+            }
+            const int m = a * 12 + 4 * c;
+            o[m / 4] = make_uint2(bf16x2(sn[0], sn[1]), bf16x2(sn[2], sn[3]));
+            o[9 + m / 4] = make_uint2(bf16x2(cs[0], cs[1]), bf16x2(cs[2], cs[3]));
         }
     }
-    v[72] = si.wo.x; v[73] = si.wo.y; v[74] = si.wo.z;
-    v[75] = si.sn.x; v[76] = si.sn.y; v[77] = si.sn.z;
-    v[78] = bsdf_roughness(f);
+    const float rough = bsdf_roughness(f);
     const bool diffuse = f.lobe == LOBE_LAMBERT || f.lobe == LOBE_OREN_NAYAR;
     const Spec ks = f.lobe == LOBE_MICROFACET ? spec(1.0f) : f.R;
-    if (diffuse) {
-        v[79] = f.R.r; v[80] = f.R.g; v[81] = f.R.b;
-    } else {
-        v[82] = ks.r; v[83] = ks.g; v[84] = ks.b;
-    }
-    v[85] = 1.0f;
-    uint4* o = (uint4*)out;
-#pragma unroll
-    for (int j = 0; j < 12; ++j) {
-        uint32_t w[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            w[q] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[8 * j + 2 * q])) |
-                   ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[8 * j + 2 * q + 1])) << 16);
-        o[j] = make_uint4(w[0], w[1], w[2], w[3]);
-    }
+    const Spec kd = diffuse ? f.R : spec(0.0f), kss = diffuse ? spec(0.0f) : ks;
+    o[18] = make_uint2(bf16x2(si.wo.x, si.wo.y), bf16x2(si.wo.z, si.sn.x));
+    o[19] = make_uint2(bf16x2(si.sn.y, si.sn.z), bf16x2(rough, kd.r));
+    o[20] = make_uint2(bf16x2(kd.g, kd.b), bf16x2(kss.r, kss.g));
+    o[21] = make_uint2(bf16x2(kss.b, 1.0f), 0u);
+    o[22] = make_uint2(0u, 0u);
+    o[23] = make_uint2(0u, 0u);
 }
 
 // Resume a (pixel, sample) stream at draw `draw` (regenerates the current Philox block).

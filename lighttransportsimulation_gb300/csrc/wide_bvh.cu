@@ -1,5 +1,5 @@
-// Collapse of the binary LBVH into the 8-wide compressed BVH (see wide_bvh.cuh), one kernel
-// launch per level of the wide tree.
+// Collapse of a binary BVH (the LBVH, or the PLOC tree with its SAH cost table) into the 8-wide
+// compressed BVH (see wide_bvh.cuh), one kernel launch per level of the wide tree.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -1,11 +1,14 @@
-// 8-wide compressed BVH for traversal (sm_103a), collapsed from the Karras LBVH.
+// 8-wide compressed BVH for traversal (sm_103a), collapsed from a binary BVH over the LBVH's
+// leaves.
 //
 // The reference traverses its binary LBVH (acceleration/BVH.cuh:331-398).  The binary tree is
-// still built exactly as the reference builds it (lbvh.cu); for rendering it is collapsed into
-// nodes of up to eight children with child boxes quantised to 8 bits per plane relative to the
-// node's origin and a power-of-two scale per axis (the compressed wide BVH of Ylitie, Karras and
-// Laine, HPG 2017, in a layout of our own).  Decoded boxes always contain the exact child boxes,
-// so traversal enters every box the binary traversal enters and finds the same closest hit.
+// still built exactly as the reference builds it (lbvh.cu); for rendering, it or a PLOC tree
+// clustered from its Morton order (ploc.cu) is collapsed into nodes of up to eight children --
+// interior nodes, or leaf slots of one to three triangles -- with child boxes quantised to 8 bits
+// per plane relative to the node's origin and a power-of-two scale per axis (the compressed wide
+// BVH of Ylitie, Karras and Laine, HPG 2017, in a layout of our own).  Decoded boxes always
+// contain the exact child boxes, and every triangle sits in exactly one leaf slot, so traversal
+// finds the same closest hit as the binary traversal.
 #pragma once
 
 #include <cuda_runtime.h>
