@@ -228,23 +228,8 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, co
     q_ext[n_cont + t] = slot;
 }
 
-// Work counters: [0..2] all rays (rays, node visits, triangle tests), then the same three per
-// traversal kind (0 extend, 1 shadow, 2 MIS) at [3 + 3 * kind].  Called by all 32 lanes.
-__device__ __forceinline__ void count_work(const RenderParams& rp, unsigned rays, const Work& wk, int kind) {
-    const unsigned tr = __reduce_add_sync(~0u, rays);
-    const unsigned tn = __reduce_add_sync(~0u, wk.nodes), tt = __reduce_add_sync(~0u, wk.tris);
-    if ((threadIdx.x & 31u) == 0u && rp.counters && tr) {
-        unsigned long long* c = rp.counters;
-        unsigned long long* k = rp.counters + 3 + 3 * kind;
-        atomicAdd(c, (unsigned long long)tr);
-        atomicAdd(c + 1, (unsigned long long)tn);
-        atomicAdd(c + 2, (unsigned long long)tt);
-        atomicAdd(k, (unsigned long long)tr);
-        atomicAdd(k + 1, (unsigned long long)tn);
-        atomicAdd(k + 2, (unsigned long long)tt);
-    }
-}
-
+// Work counters (RenderParams::counters): [0..2] all rays (rays, node visits, triangle tests),
+// then the same three per traversal kind (0 extend, 1 shadow, 2 MIS) at [3 + 3 * kind].
 enum : int { TR_EXTEND = 0, TR_SHADOW = 1, TR_MIS = 2 };
 
 
@@ -320,7 +305,12 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
                                                        const int32_t* __restrict__ q_ext,
                                                        const WfCtl* __restrict__ ctl, uint32_t* fetch, int nleaf) {
     __shared__ uint32_t s_stack[kStack * kWfBlock];
+    // the block's finished rays, node visits and triangle tests per traversal kind (kept out of
+    // the registers of the traversal loop)
+    __shared__ uint32_t s_work[9];
     uint32_t* stack = s_stack + threadIdx.x;
+    if (threadIdx.x < 9) s_work[threadIdx.x] = 0u;
+    __syncthreads();
     const uint32_t n_ext = ctl->n_ext, n_sh = ctl->n_sh, n_mis = ctl->n_mis;
     const uint32_t e1 = n_ext, e2 = n_ext + n_sh, n = n_ext + n_sh + n_mis;
     const unsigned lane = threadIdx.x & 31u;
@@ -328,22 +318,11 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
     int p = -1, kind = 0;
     bool active = false, exhausted = false;
     Work cur{0u, 0u};  // work of the ray in flight, credited to its kind when it finishes
-    Work w0{0u, 0u}, w1{0u, 0u}, w2{0u, 0u};
-    unsigned r0 = 0, r1 = 0, r2 = 0;
     auto credit = [&]() {
-        if (kind == TR_EXTEND) {
-            w0.nodes += cur.nodes;
-            w0.tris += cur.tris;
-            ++r0;
-        } else if (kind == TR_SHADOW) {
-            w1.nodes += cur.nodes;
-            w1.tris += cur.tris;
-            ++r1;
-        } else {
-            w2.nodes += cur.nodes;
-            w2.tris += cur.tris;
-            ++r2;
-        }
+        uint32_t* w = s_work + 3 * kind;
+        atomicAdd(w, 1u);
+        atomicAdd(w + 1, cur.nodes);
+        atomicAdd(w + 2, cur.tris);
         cur.nodes = cur.tris = 0u;
     };
     for (;;) {
@@ -397,9 +376,14 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
             if (act == 0u || (!exhausted && 32 - __popc(act) >= kRefillIdle)) break;
         }
     }
-    count_work(rp, r0, w0, TR_EXTEND);
-    count_work(rp, r1, w1, TR_SHADOW);
-    count_work(rp, r2, w2, TR_MIS);
+    __syncthreads();
+    if (threadIdx.x < 9 && rp.counters) {
+        const uint32_t v = s_work[threadIdx.x];
+        if (v) {
+            atomicAdd(rp.counters + 3 + threadIdx.x, (unsigned long long)v);  // per kind
+            atomicAdd(rp.counters + threadIdx.x % 3, (unsigned long long)v);  // all rays
+        }
+    }
 }
 
 // shade: one bounce of PathTracingIntegrator::evaluate up to the next ray.
