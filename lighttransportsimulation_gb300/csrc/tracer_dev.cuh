@@ -262,32 +262,31 @@ __device__ void make_si(const SceneView& sv, int prim, V3 d, real u, real v, rea
 // ------------------------------------------------------------------ BVH traversal
 struct TraceRay {
     V3 o, d, inv;
-    int neg[3];
+    // direction sign per axis (from inv: -0 gives -inf), derived where used rather than held in
+    // three more registers through the traversal loop
+    __device__ __forceinline__ bool neg(int a) const { return (a == 0 ? inv.x : (a == 1 ? inv.y : inv.z)) < 0; }
 };
 __device__ __forceinline__ TraceRay make_trace_ray(V3 o, V3 d) {
     TraceRay r;
     r.o = o;
     r.d = d;
     r.inv = v3(xdiv(1.0f, d.x), xdiv(1.0f, d.y), xdiv(1.0f, d.z));
-    r.neg[0] = r.inv.x < 0;
-    r.neg[1] = r.inv.y < 0;
-    r.neg[2] = r.inv.z < 0;
     return r;
 }
 // Bounds3::simpleIntersect (geometry/Bound.cuh:199-227), returning the entry distance.
 __device__ __forceinline__ bool slab(const TraceRay& r, real tmax_ray, real mnx, real mny, real mnz, real mxx,
                                      real mxy, real mxz, real& tentry) {
-    real tMin = ((r.neg[0] ? mxx : mnx) - r.o.x) * r.inv.x;
-    real tMax = ((r.neg[0] ? mnx : mxx) - r.o.x) * r.inv.x;
-    const real tyMin = ((r.neg[1] ? mxy : mny) - r.o.y) * r.inv.y;
-    real tyMax = ((r.neg[1] ? mny : mxy) - r.o.y) * r.inv.y;
+    real tMin = ((r.neg(0) ? mxx : mnx) - r.o.x) * r.inv.x;
+    real tMax = ((r.neg(0) ? mnx : mxx) - r.o.x) * r.inv.x;
+    const real tyMin = ((r.neg(1) ? mxy : mny) - r.o.y) * r.inv.y;
+    real tyMax = ((r.neg(1) ? mny : mxy) - r.o.y) * r.inv.y;
     tMax *= kSlabScale;
     tyMax *= kSlabScale;
     if (tMin > tyMax || tyMin > tMax) return false;
     if (tyMin > tMin) tMin = tyMin;
     if (tyMax < tMax) tMax = tyMax;
-    const real tzMin = ((r.neg[2] ? mxz : mnz) - r.o.z) * r.inv.z;
-    real tzMax = ((r.neg[2] ? mnz : mxz) - r.o.z) * r.inv.z;
+    const real tzMin = ((r.neg(2) ? mxz : mnz) - r.o.z) * r.inv.z;
+    real tzMax = ((r.neg(2) ? mnz : mxz) - r.o.z) * r.inv.z;
     tzMax *= kSlabScale;
     if (tMin > tzMax || tzMin > tMax) return false;
     if (tzMin > tMin) tMin = tzMin;
@@ -432,7 +431,7 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
         atomicOr(err, DEV_ERR_BAD_INDEX);
         return true;
     }
-    const uint32_t oct = (t.r.neg[0] ? 1u : 0u) | (t.r.neg[1] ? 2u : 0u) | (t.r.neg[2] ? 4u : 0u);
+    const uint32_t oct = (t.r.neg(0) ? 1u : 0u) | (t.r.neg(1) ? 2u : 0u) | (t.r.neg(2) ? 4u : 0u);
     const WideNode* nd = sv.wnodes + t.node;
     const float4 h = __ldg(&nd->h);
     const uint4 m = __ldg(&nd->m), q0 = __ldg(&nd->q0), q1 = __ldg(&nd->q1), q2 = __ldg(&nd->q2);
@@ -441,9 +440,9 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
     const uint32_t imask = hb >> 24, omask = m.z;
     uint32_t hits = 0, leaves = 0;
     if (isfinite(t.r.inv.x) && isfinite(t.r.inv.y) && isfinite(t.r.inv.z)) {
-        const WideAxis ax = wide_axis(h.x, t.r.o.x, t.r.inv.x, hb & 0xffu, t.r.neg[0], q0.x, q0.y, q1.z, q1.w);
-        const WideAxis ay = wide_axis(h.y, t.r.o.y, t.r.inv.y, (hb >> 8) & 0xffu, t.r.neg[1], q0.z, q0.w, q2.x, q2.y);
-        const WideAxis az = wide_axis(h.z, t.r.o.z, t.r.inv.z, (hb >> 16) & 0xffu, t.r.neg[2], q1.x, q1.y, q2.z, q2.w);
+        const WideAxis ax = wide_axis(h.x, t.r.o.x, t.r.inv.x, hb & 0xffu, t.r.neg(0), q0.x, q0.y, q1.z, q1.w);
+        const WideAxis ay = wide_axis(h.y, t.r.o.y, t.r.inv.y, (hb >> 8) & 0xffu, t.r.neg(1), q0.z, q0.w, q2.x, q2.y);
+        const WideAxis az = wide_axis(h.z, t.r.o.z, t.r.inv.z, (hb >> 16) & 0xffu, t.r.neg(2), q1.x, q1.y, q2.z, q2.w);
         // every slot is tested (a warp runs a slot's test whenever any of its nodes has that
         // slot) and the empty ones are masked off after; the interval is clipped to [0, tmax]
         // and tested once, which also enters the boxes touching t = 0 or t = tmax exactly (a
@@ -532,7 +531,7 @@ __device__ __forceinline__ bool wide_node_step(const bool any, Trav& t, const Sc
         atomicOr(err, DEV_ERR_BAD_INDEX);
         return true;
     }
-    const uint32_t oct = (t.r.neg[0] ? 1u : 0u) | (t.r.neg[1] ? 2u : 0u) | (t.r.neg[2] ? 4u : 0u);
+    const uint32_t oct = (t.r.neg(0) ? 1u : 0u) | (t.r.neg(1) ? 2u : 0u) | (t.r.neg(2) ? 4u : 0u);
     const WideNode* nd = sv.wnodes + t.node;
     const float4 h = __ldg(&nd->h);
     const uint4 m = __ldg(&nd->m), q0 = __ldg(&nd->q0), q1 = __ldg(&nd->q1), q2 = __ldg(&nd->q2);
@@ -541,9 +540,9 @@ __device__ __forceinline__ bool wide_node_step(const bool any, Trav& t, const Sc
     const uint32_t imask = hb >> 24, omask = m.z;
     uint32_t hits = 0, leaves = 0;
     if (isfinite(t.r.inv.x) && isfinite(t.r.inv.y) && isfinite(t.r.inv.z)) {
-        const WideAxis ax = wide_axis(h.x, t.r.o.x, t.r.inv.x, hb & 0xffu, t.r.neg[0], q0.x, q0.y, q1.z, q1.w);
-        const WideAxis ay = wide_axis(h.y, t.r.o.y, t.r.inv.y, (hb >> 8) & 0xffu, t.r.neg[1], q0.z, q0.w, q2.x, q2.y);
-        const WideAxis az = wide_axis(h.z, t.r.o.z, t.r.inv.z, (hb >> 16) & 0xffu, t.r.neg[2], q1.x, q1.y, q2.z, q2.w);
+        const WideAxis ax = wide_axis(h.x, t.r.o.x, t.r.inv.x, hb & 0xffu, t.r.neg(0), q0.x, q0.y, q1.z, q1.w);
+        const WideAxis ay = wide_axis(h.y, t.r.o.y, t.r.inv.y, (hb >> 8) & 0xffu, t.r.neg(1), q0.z, q0.w, q2.x, q2.y);
+        const WideAxis az = wide_axis(h.z, t.r.o.z, t.r.inv.z, (hb >> 16) & 0xffu, t.r.neg(2), q1.x, q1.y, q2.z, q2.w);
         // every slot is tested (a warp runs a slot's test whenever any of its nodes has that
         // slot) and the empty ones are masked off after; the interval is clipped to [0, tmax]
         // and tested once, which also enters the boxes touching t = 0 or t = tmax exactly (a

@@ -311,8 +311,6 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
     uint32_t* stack = s_stack + threadIdx.x;
     if (threadIdx.x < 9) s_work[threadIdx.x] = 0u;
     __syncthreads();
-    const uint32_t n_ext = ctl->n_ext, n_sh = ctl->n_sh, n_mis = ctl->n_mis;
-    const uint32_t e1 = n_ext, e2 = n_ext + n_sh, n = n_ext + n_sh + n_mis;
     const unsigned lane = threadIdx.x & 31u;
     Trav t;
     int p = -1, kind = 0;
@@ -328,6 +326,8 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
     for (;;) {
         const unsigned idle = __ballot_sync(~0u, !active);
         if (!exhausted && __popc(idle) >= kRefillIdle) {
+            // the list sizes, read at each refill rather than held through the traversal
+            const uint32_t e1 = __ldg(&ctl->n_ext), e2 = e1 + __ldg(&ctl->n_sh), n = e2 + __ldg(&ctl->n_mis);
             const int leader = __ffs(idle) - 1;
             uint32_t base = 0;
             if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(idle));
