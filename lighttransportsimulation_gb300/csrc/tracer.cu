@@ -105,15 +105,20 @@ __global__ void k_build_prim_rec(const float4* __restrict__ prim_v, const int32_
     r[7] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-__global__ void k_gather_leaves(const float4* __restrict__ prim_v, const int32_t* __restrict__ leaf_prim, int n,
+// Leaf-ordered triangles: w of the first vertex = primitive id, w of the second = the shade
+// class of its material (what a closest hit records, see hit_prim / hit_class).
+__global__ void k_gather_leaves(const float4* __restrict__ prim_v, const float4* __restrict__ prim_rec,
+                                const DevMat* __restrict__ mats, const int32_t* __restrict__ leaf_prim, int n,
                                 float4* __restrict__ leaf_v) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= n) return;
     const int p = __ldg(leaf_prim + l);
-    float4 a = __ldg(prim_v + 3 * p);
+    float4 a = __ldg(prim_v + 3 * p), b = __ldg(prim_v + 3 * p + 1);
     a.w = __int_as_float(p);
+    const int mesh = __float_as_int(__ldg(prim_rec + 8 * (size_t)p + 6).y);
+    b.w = __int_as_float(__ldg(&mats[mesh].shade_class));
     leaf_v[3 * l] = a;
-    leaf_v[3 * l + 1] = __ldg(prim_v + 3 * p + 1);
+    leaf_v[3 * l + 1] = b;
     leaf_v[3 * l + 2] = __ldg(prim_v + 3 * p + 2);
 }
 
@@ -349,7 +354,8 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
         dev_free(leaf_v_);
         leaf_v_ = nullptr;
         TRY(dev_alloc((void**)&leaf_v_, sizeof(float4) * 3 * (size_t)bvh.n));
-        k_gather_leaves<<<(bvh.n + 255) / 256, 256, 0, s>>>(view_.prim_v, bvh.leaf_prim, bvh.n, leaf_v_);
+        k_gather_leaves<<<(bvh.n + 255) / 256, 256, 0, s>>>(view_.prim_v, view_.prim_rec, view_.mats, bvh.leaf_prim,
+                                                            bvh.n, leaf_v_);
         leaf_serial_ = bvh.serial;
         leaf_n_ = bvh.n;
     }

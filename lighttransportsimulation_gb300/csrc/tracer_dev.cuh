@@ -295,6 +295,15 @@ __device__ __forceinline__ bool slab(const TraceRay& r, real tmax_ray, real mnx,
     return (tMin < tmax_ray) && (tMax > 0);
 }
 
+// A closest hit as the traversal records it: the primitive id (below 2^24, the LBVH's limit) with
+// the shade class of its material (1 .. 15) in bits 24 .. 27, both read from the leaf triangle
+// (w of its first and second vertex), so the wavefront can group hits by class without reading
+// the shading record; -1: no hit.
+constexpr int kHitPrimBits = 24;
+constexpr int kHitPrimMask = (1 << kHitPrimBits) - 1;
+__device__ __forceinline__ int hit_prim(int best) { return best < 0 ? best : (best & kHitPrimMask); }
+__device__ __forceinline__ int hit_class(int best) { return best < 0 ? 0 : (best >> kHitPrimBits); }
+
 __device__ __forceinline__ bool leaf_test(const bool any, const float4* __restrict__ tv, int leaf, const TraceRay& r,
                                           real& tmax, int& best, real& bu, real& bv, real& binv) {
     const float4 a = __ldg(tv + 3 * leaf), b = __ldg(tv + 3 * leaf + 1), c = __ldg(tv + 3 * leaf + 2);
@@ -302,7 +311,7 @@ __device__ __forceinline__ bool leaf_test(const bool any, const float4* __restri
     real t, u, v, inv;
     if (tri_test(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax, t, u, v, inv)) {
         tmax = t;
-        best = __float_as_int(a.w);
+        best = __float_as_int(a.w) | (__float_as_int(b.w) << kHitPrimBits);
         bu = u;
         bv = v;
         binv = inv;
@@ -695,7 +704,7 @@ __device__ int traverse(const SceneView& sv, int nleaf, const TraceRay& r, real&
     bu = t.bu;
     bv = t.bv;
     binv = t.binv;
-    return ANY ? (t.best == 1 ? 1 : -1) : t.best;
+    return ANY ? (t.best == 1 ? 1 : -1) : hit_prim(t.best);
 }
 
 struct Hit {

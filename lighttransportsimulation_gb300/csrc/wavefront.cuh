@@ -252,7 +252,7 @@ __device__ __forceinline__ bool wf_ray_begin(int kind, Trav& t, const SceneView&
 // (IntegratorHelper.cuh:225-243).
 __device__ __forceinline__ void wf_ray_end(int kind, const Trav& t, const SceneView& sv, WfState& st, int p) {
     if (kind == TR_EXTEND) {
-        st.hprim[p] = t.best;
+        st.hprim[p] = t.best;  // with its shade class (hit_prim / hit_class)
         st.huvi[p] = make_float4(t.bu, t.bv, t.binv, t.tmax);
     } else if (kind == TR_SHADOW) {
         st.vis[p] = t.best == 1 ? 0u : 1u;
@@ -263,9 +263,10 @@ __device__ __forceinline__ void wf_ray_end(int kind, const Trav& t, const SceneV
         const float4 x = st.mis_x[p];
         const int off = __float_as_int(x.y);
         const DevLight& Lt = sv.lights[off];
-        const bool found = t.best >= 0;
+        const int hp = hit_prim(t.best);
+        const bool found = hp >= 0;
         if (found) {
-            const bool on_light = prim_word(sv, t.best).z == off && Lt.kind == 0;
+            const bool on_light = prim_word(sv, hp).z == off && Lt.kind == 0;
             st.ld_mis[p] = on_light ? make_float4(t.bu, t.bv, t.binv, 2.f) : make_float4(0.f, 0.f, 0.f, 0.f);
         } else {
             const float4 fv = st.mis_fv[p];
@@ -275,7 +276,7 @@ __device__ __forceinline__ void wf_ray_end(int kind, const Trav& t, const SceneV
             if (add) c = Spec{fv.x, fv.y, fv.z} * Li * spec(1.0f) * fv.w / x.x;
             st.ld_mis[p] = make_float4(c.r, c.g, c.b, add ? 1.f : 0.f);
         }
-        st.mis_hit[p] = found ? t.best + 1 : 0;
+        st.mis_hit[p] = found ? hp + 1 : 0;
     }
 }
 
@@ -394,8 +395,7 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_classify(const SceneView sv, Wf
     const int t = blockIdx.x * kWfBlock + threadIdx.x;
     if (t >= (int)ctl->n_ext) return;
     const int p = q[t];
-    const int prim = st.hprim[p];
-    const int c = prim < 0 ? 0 : sv.mats[prim_word(sv, prim).y].shade_class;
+    const int c = hit_class(st.hprim[p]);  // 0: left the scene
     const unsigned grp = __match_any_sync(__activemask(), c);
     const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
     uint32_t base = 0;
@@ -440,7 +440,7 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
     Spec beta{b4.x, b4.y, b4.z}, L{l4.x, l4.y, l4.z};
     uint64_t sig = RECORD ? st.sig[p] : 0ull;
     EvSink evs{&sig, 0};
-    const int prim = st.hprim[p];
+    const int prim = hit_prim(st.hprim[p]);
     const bool hit = prim >= 0;
     uint32_t pend = 0;
     if (RECORD) fnv_mix(sig, 0x100000000ull + (uint64_t)(prim + 1));
