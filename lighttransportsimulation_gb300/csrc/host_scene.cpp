@@ -17,6 +17,10 @@
 #include <utility>
 #include <vector>
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include "../../include/lts_capi.h"
 
 namespace lts {
@@ -157,22 +161,52 @@ int toki(Tokens& s, const char* what) {
     }
 }
 
+// One mesh file: the whole .bin image (read_bin) or the vectors parse_obj fills; P(), UV(), N()
+// and I() view either.
 struct MeshData {
     int32_t ntri = 0, np = 0, nuv = 0, nn = 0;
-    std::vector<float> p, uv, n;
-    std::vector<int32_t> idx;
+    HostVec<char> bin;                  // .bin file: 16-byte header, P, UV, N, indices
+    std::vector<float> sp, suv, sn;     // .obj
+    std::vector<int32_t> sidx;
+    const float* P() const { return bin.empty() ? sp.data() : reinterpret_cast<const float*>(bin.data() + 16); }
+    const float* UV() const { return bin.empty() ? suv.data() : P() + 3 * (size_t)np; }
+    const float* N() const { return bin.empty() ? sn.data() : UV() + 2 * (size_t)nuv; }
+    const int32_t* I() const {
+        return bin.empty() ? sidx.data() : reinterpret_cast<const int32_t*>(N() + 3 * (size_t)nn);
+    }
 };
 
-// core/FileIO.cuh:170-206 (binMeshRead), with size checks the reference does not make.
+// core/FileIO.cuh:170-206 (binMeshRead), with size checks the reference does not make.  The file
+// is read whole, in contiguous parts on up to 16 threads (positioned reads), into a buffer that is
+// not zeroed first.
 MeshData read_bin(const std::string& path) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f.good()) throw ParseError{LTS_ERR_IO, "cannot open mesh " + path};
-    f.seekg(0, std::ios::end);
-    const long long size = (long long)f.tellg();
-    f.seekg(0, std::ios::beg);
+    const int fd = ::open(path.c_str(), O_RDONLY);
+    if (fd < 0) throw ParseError{LTS_ERR_IO, "cannot open mesh " + path};
+    struct stat st;
+    if (::fstat(fd, &st) != 0) {
+        ::close(fd);
+        throw ParseError{LTS_ERR_IO, "cannot stat mesh " + path};
+    }
+    const long long size = (long long)st.st_size;
     MeshData m;
+    m.bin.resize((size_t)std::max(0LL, size));
+    std::atomic<bool> failed{false};
+    parallel_ranges((size_t)m.bin.size(), [&](size_t b, size_t e) {
+        while (b < e) {
+            const ssize_t r = ::pread(fd, m.bin.data() + b, e - b, (off_t)b);
+            if (r < 0 && errno == EINTR) continue;
+            if (r <= 0) {
+                failed = true;
+                return;
+            }
+            b += (size_t)r;
+        }
+    });
+    ::close(fd);
+    if (failed) throw ParseError{LTS_ERR_IO, "cannot read mesh " + path};
     int32_t hdr[4];
-    if (size < 16 || !f.read((char*)hdr, 16)) throw ParseError{LTS_ERR_PARSE, "short mesh header in " + path};
+    if (size < 16) throw ParseError{LTS_ERR_PARSE, "short mesh header in " + path};
+    std::memcpy(hdr, m.bin.data(), 16);
     m.ntri = hdr[0];
     m.np = hdr[1];
     m.nuv = hdr[2];
@@ -181,14 +215,6 @@ MeshData read_bin(const std::string& path) {
         throw ParseError{LTS_ERR_PARSE, "negative counts in " + path};
     const long long need = 16 + 12LL * m.np + 8LL * m.nuv + 12LL * m.nn + 36LL * m.ntri;
     if (size < need) throw ParseError{LTS_ERR_PARSE, "truncated mesh " + path};
-    m.p.resize(3 * (size_t)m.np);
-    m.uv.resize(2 * (size_t)m.nuv);
-    m.n.resize(3 * (size_t)m.nn);
-    m.idx.resize(9 * (size_t)m.ntri);
-    f.read((char*)m.p.data(), 12LL * m.np);
-    f.read((char*)m.uv.data(), 8LL * m.nuv);
-    f.read((char*)m.n.data(), 12LL * m.nn);
-    f.read((char*)m.idx.data(), 36LL * m.ntri);
     return m;
 }
 
@@ -196,10 +222,11 @@ MeshData read_bin(const std::string& path) {
 // reference reads out of bounds otherwise).
 void check_indices(const MeshData& m, const std::string& name) {
     std::atomic<bool> bad{false};
+    const int32_t* idx = m.I();
     parallel_ranges((size_t)m.ntri, [&](size_t b, size_t e) {
         for (size_t t = b; t < e; ++t)
             for (int c = 0; c < 3; ++c) {
-                const int32_t ip = m.idx[9 * t + 3 * c], iu = m.idx[9 * t + 3 * c + 1], in = m.idx[9 * t + 3 * c + 2];
+                const int32_t ip = idx[9 * t + 3 * c], iu = idx[9 * t + 3 * c + 1], in = idx[9 * t + 3 * c + 2];
                 if (ip < 0 || ip >= m.np || (m.nuv > 0 && (iu < 0 || iu >= m.nuv)) ||
                     (m.nn > 0 && (in < 0 || in >= m.nn))) {
                     bad = true;
@@ -267,11 +294,11 @@ MeshData parse_obj(const std::string& path) {
     std::string t;
     while (next(t)) {
         if (t == "v") {
-            for (int k = 0; k < 3; ++k) m.p.push_back(num("vertex"));
+            for (int k = 0; k < 3; ++k) m.sp.push_back(num("vertex"));
         } else if (t == "vt") {
-            for (int k = 0; k < 2; ++k) m.uv.push_back(num("texture coordinate"));
+            for (int k = 0; k < 2; ++k) m.suv.push_back(num("texture coordinate"));
         } else if (t == "vn") {
-            for (int k = 0; k < 3; ++k) m.n.push_back(num("normal"));
+            for (int k = 0; k < 3; ++k) m.sn.push_back(num("normal"));
         } else if (t == "f") {
             for (int c = 0; c < 3; ++c) {
                 std::string corner;
@@ -284,29 +311,29 @@ MeshData parse_obj(const std::string& path) {
                     if (e == std::string::npos) break;
                     b = e + 1;
                 }
-                const bool with_uv = !m.uv.empty();
+                const bool with_uv = !m.suv.empty();
                 if (parts.size() < 3)
                     throw ParseError{LTS_ERR_PARSE, "face corner '" + corner + "' is not p/uv/n in " + path};
                 const char* base = corner.data();
                 int i = 0;
                 if (!field(base + parts[0].first, base + parts[0].first + parts[0].second, i))
                     throw ParseError{LTS_ERR_PARSE, "face corner '" + corner + "' has no vertex index in " + path};
-                m.idx.push_back(i - 1);
+                m.sidx.push_back(i - 1);
                 if (with_uv) {
                     field(base + parts[1].first, base + parts[1].first + parts[1].second, i);
-                    m.idx.push_back(i - 1);
+                    m.sidx.push_back(i - 1);
                 } else {
-                    m.idx.push_back(0);
+                    m.sidx.push_back(0);
                 }
                 field(base + parts[2].first, base + parts[2].first + parts[2].second, i);
-                m.idx.push_back(i - 1);
+                m.sidx.push_back(i - 1);
             }
             ++m.ntri;
         }
     }
-    m.np = (int32_t)(m.p.size() / 3);
-    m.nuv = (int32_t)(m.uv.size() / 2);
-    m.nn = (int32_t)(m.n.size() / 3);
+    m.np = (int32_t)(m.sp.size() / 3);
+    m.nuv = (int32_t)(m.suv.size() / 2);
+    m.nn = (int32_t)(m.sn.size() / 3);
     return m;
 }
 
@@ -316,10 +343,10 @@ bool write_bin(const std::string& path, const MeshData& m) {
     if (!f.good()) return false;
     const int32_t hdr[4] = {m.ntri, m.np, m.nuv, m.nn};
     f.write((const char*)hdr, 16);
-    f.write((const char*)m.p.data(), 12LL * m.np);
-    f.write((const char*)m.uv.data(), 8LL * m.nuv);
-    f.write((const char*)m.n.data(), 12LL * m.nn);
-    f.write((const char*)m.idx.data(), 36LL * m.ntri);
+    f.write((const char*)m.P(), 12LL * m.np);
+    f.write((const char*)m.UV(), 8LL * m.nuv);
+    f.write((const char*)m.N(), 12LL * m.nn);
+    f.write((const char*)m.I(), 36LL * m.ntri);
     return f.good();
 }
 
@@ -545,49 +572,70 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
             throw ParseError{LTS_ERR_PARSE, "fewer materials than meshes (material index == mesh index)"};
 
         // Mesh loading + transforms (SceneLoader.cuh:264-282, shapes/Triangle.cu:20-43).
-        sc->p.clear(); sc->n.clear(); sc->uv.clear();
-        sc->tri_p.clear(); sc->tri_n.clear(); sc->tri_uv.clear(); sc->tri_mesh.clear();
-        sc->mesh_first_tri.clear(); sc->mesh_tri_count.clear();
-        const Xform ident;  // Transform(1)
+        // Every mesh is read (and checked) first, so each table is sized once; each mesh then
+        // fills its own ranges of them in parallel.
+        std::vector<MeshData> mds(meshes);
+        size_t np_all = 0, nn_all = 0, nuv_all = 0, nt_all = 0;
         for (int m = 0; m < meshes; ++m) {
-            MeshData md = read_mesh(files[m]);
-            check_indices(md, files[m]);
+            mds[m] = read_mesh(files[m]);
+            check_indices(mds[m], files[m]);
+            np_all += (size_t)mds[m].np;
+            nn_all += (size_t)mds[m].nn;
+            nuv_all += (size_t)mds[m].nuv;
+            nt_all += (size_t)mds[m].ntri;
+        }
+        if (nt_all > (size_t)INT32_MAX / 3 || np_all > (size_t)INT32_MAX / 3)
+            throw ParseError{LTS_ERR_PARSE, "scene too large"};
+        sc->p.resize(3 * np_all);
+        sc->n.resize(3 * nn_all);
+        sc->uv.resize(2 * nuv_all);
+        sc->tri_p.resize(3 * nt_all);
+        sc->tri_n.resize(3 * nt_all);
+        sc->tri_uv.resize(3 * nt_all);
+        sc->tri_mesh.resize(nt_all);
+        sc->mesh_first_tri.clear();
+        sc->mesh_tri_count.clear();
+        const Xform ident;  // Transform(1)
+        size_t pbase = 0, nbase = 0, uvbase = 0, tbase = 0;
+        for (int m = 0; m < meshes; ++m) {
+            const MeshData& md = mds[m];
             const Xform& X = m >= sub_meshes ? ident : subject_xf;
-            const int32_t pbase = (int32_t)(sc->p.size() / 3), nbase = (int32_t)(sc->n.size() / 3),
-                          uvbase = (int32_t)(sc->uv.size() / 2), tbase = (int32_t)sc->tri_mesh.size();
-            sc->p.resize(3 * ((size_t)pbase + md.np));
+            const float *mp = md.P(), *mn = md.N(), *muv = md.UV();
+            const int32_t* mi = md.I();
             parallel_ranges((size_t)md.np, [&](size_t b, size_t e) {
                 for (size_t i = b; i < e; ++i) {
-                    const V3 w = X.point({md.p[3 * i], md.p[3 * i + 1], md.p[3 * i + 2]});
-                    float* o = &sc->p[3 * ((size_t)pbase + i)];
+                    const V3 w = X.point({mp[3 * i], mp[3 * i + 1], mp[3 * i + 2]});
+                    float* o = &sc->p[3 * (pbase + i)];
                     o[0] = w.x; o[1] = w.y; o[2] = w.z;
                 }
             });
-            sc->n.resize(3 * ((size_t)nbase + md.nn));
             parallel_ranges((size_t)md.nn, [&](size_t b, size_t e) {
                 for (size_t i = b; i < e; ++i) {
-                    const V3 w = X.normal({md.n[3 * i], md.n[3 * i + 1], md.n[3 * i + 2]});
-                    float* o = &sc->n[3 * ((size_t)nbase + i)];
+                    const V3 w = X.normal({mn[3 * i], mn[3 * i + 1], mn[3 * i + 2]});
+                    float* o = &sc->n[3 * (nbase + i)];
                     o[0] = w.x; o[1] = w.y; o[2] = w.z;
                 }
             });
-            sc->uv.insert(sc->uv.end(), md.uv.begin(), md.uv.end());
-            sc->mesh_first_tri.push_back(tbase);
+            if (md.nuv > 0) std::memcpy(&sc->uv[2 * uvbase], muv, 8 * (size_t)md.nuv);
+            sc->mesh_first_tri.push_back((int32_t)tbase);
             sc->mesh_tri_count.push_back(md.ntri);
-            const size_t nc = 3 * ((size_t)tbase + md.ntri);
-            sc->tri_p.resize(nc);
-            sc->tri_uv.resize(nc);
-            sc->tri_n.resize(nc);
-            sc->tri_mesh.resize((size_t)tbase + md.ntri, m);
+            const int32_t pb = (int32_t)pbase, nb = (int32_t)nbase, ub = (int32_t)uvbase;
+            const bool has_uv = md.nuv > 0, has_n = md.nn > 0;
             parallel_ranges((size_t)md.ntri, [&](size_t b, size_t e) {
-                for (size_t t = b; t < e; ++t)
+                for (size_t t = b; t < e; ++t) {
                     for (int c = 0; c < 3; ++c) {
-                        const size_t o = 3 * ((size_t)tbase + t) + c;
-                        sc->tri_p[o] = pbase + md.idx[9 * t + 3 * c];
-                        sc->tri_uv[o] = md.nuv > 0 ? uvbase + md.idx[9 * t + 3 * c + 1] : -1;
-                        sc->tri_n[o] = md.nn > 0 ? nbase + md.idx[9 * t + 3 * c + 2] : -1;
+                        const size_t o = 3 * (tbase + t) + c;
+                        sc->tri_p[o] = pb + mi[9 * t + 3 * c];
+                        sc->tri_uv[o] = has_uv ? ub + mi[9 * t + 3 * c + 1] : -1;
+                        sc->tri_n[o] = has_n ? nb + mi[9 * t + 3 * c + 2] : -1;
                     }
+                    sc->tri_mesh[tbase + t] = m;
+                }
             });
+            pbase += (size_t)md.np;
+            nbase += (size_t)md.nn;
+            uvbase += (size_t)md.nuv;
+            tbase += (size_t)md.ntri;
         }
         sc->subject_meshes = sub_meshes;
         sc->area_light_meshes = area_meshes;

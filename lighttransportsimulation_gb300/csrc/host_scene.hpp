@@ -4,10 +4,39 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
+#include <new>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 namespace lts {
+
+// Allocator whose resize leaves new elements uninitialised (default-initialised) instead of
+// zeroing them: the loader sizes each table once and fills every element in parallel, so a
+// zeroing pass would only touch every page once more, on one thread.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+    using value_type = T;
+    template <class U>
+    struct rebind {
+        using other = NoInitAlloc<U>;
+    };
+    NoInitAlloc() = default;
+    template <class U>
+    NoInitAlloc(const NoInitAlloc<U>&) noexcept {}
+    template <class U>
+    void construct(U* q) noexcept(std::is_nothrow_default_constructible<U>::value) {
+        ::new (static_cast<void*>(q)) U;
+    }
+    template <class U, class... A>
+    void construct(U* q, A&&... a) {
+        ::new (static_cast<void*>(q)) U(std::forward<A>(a)...);
+    }
+};
+template <class T>
+using HostVec = std::vector<T, NoInitAlloc<T>>;
 
 enum TexKind : int32_t { TEX_CONSTANT = 0, TEX_FBM = 1, TEX_WRINKLED = 2, TEX_MARBLE = 3, TEX_WINDY = 4 };
 enum MatKind : int32_t {
@@ -48,13 +77,13 @@ struct HostScene {
     float filter[256] = {0};
 
     // Vertex pools (world space) and per-triangle corner indices into them.
-    std::vector<float> p;       // 3 per vertex
-    std::vector<float> n;       // 3 per normal
-    std::vector<float> uv;      // 2 per uv
-    std::vector<int32_t> tri_p;   // 3 per triangle
-    std::vector<int32_t> tri_n;   // 3 per triangle, -1 when the mesh has no normals
-    std::vector<int32_t> tri_uv;  // 3 per triangle, -1 when the mesh has no uvs
-    std::vector<int32_t> tri_mesh;
+    HostVec<float> p;       // 3 per vertex
+    HostVec<float> n;       // 3 per normal
+    HostVec<float> uv;      // 2 per uv
+    HostVec<int32_t> tri_p;   // 3 per triangle
+    HostVec<int32_t> tri_n;   // 3 per triangle, -1 when the mesh has no normals
+    HostVec<int32_t> tri_uv;  // 3 per triangle, -1 when the mesh has no uvs
+    HostVec<int32_t> tri_mesh;
 
     std::vector<int32_t> mesh_first_tri, mesh_tri_count;
     int32_t subject_meshes = 0;
@@ -62,7 +91,7 @@ struct HostScene {
     bool has_infinite = false;
 
     std::vector<HostMaterial> materials;  // one per mesh (material index == mesh index)
-    std::vector<int32_t> prim_light;      // per triangle: light index or -1
+    HostVec<int32_t> prim_light;          // per triangle: light index or -1
     std::vector<HostLight> lights;        // sampling order of the reference's light array
     std::vector<float> light_func, light_cdf;  // Distribution1D over power().y()
     float light_func_int = 0;                  // Distribution1D::funcInt (before normalising)

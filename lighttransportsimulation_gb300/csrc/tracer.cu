@@ -150,8 +150,8 @@ std::string reserve_buf(void*& slot, size_t& cap, size_t bytes) {
     cap = bytes;
     return "";
 }
-template <class T>
-std::string upload(void*& slot, size_t& cap, const std::vector<T>& v, cudaStream_t s) {
+template <class T, class A>
+std::string upload(void*& slot, size_t& cap, const std::vector<T, A>& v, cudaStream_t s) {
     const std::string e = reserve_buf(slot, cap, sizeof(T) * v.size());
     if (!e.empty()) return e;
     if (!v.empty()) TRY(cudaMemcpyAsync(slot, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
