@@ -74,6 +74,10 @@ struct lts_ctx {
     uint32_t* d_error = nullptr;
 
     HostScene scene;
+    // The scene before the current one: the next load parses into it (its tables keep their
+    // capacity, so a reload of a same-sized scene allocates nothing) and then swaps it in, so a
+    // load that fails leaves `scene` as it was.
+    HostScene spare_scene;
     bool loaded = false;
     float* d_tri = nullptr;  // scene triangle soup, 9 floats per triangle (scene order)
     size_t d_tri_cap = 0;
@@ -257,14 +261,13 @@ int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char
                    int32_t height) {
     if (!ctx || !root || !scene) return fail(ctx, LTS_ERR_ARG, "null argument");
     int code = LTS_OK;
-    HostScene sc;
     const auto t0 = std::chrono::steady_clock::now();
-    std::string msg = load_scene(root, scene, subject ? subject : "", width, height, &sc, &code);
+    std::string msg = load_scene(root, scene, subject ? subject : "", width, height, &ctx->spare_scene, &code);
     if (code) return fail(ctx, code, msg);
     const auto t1 = std::chrono::steady_clock::now();
     ctx->metrics.scene_parse_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
     ctx->metrics.scene_upload_ms = 0;
-    ctx->scene = std::move(sc);
+    std::swap(ctx->scene, ctx->spare_scene);
     ctx->loaded = true;
     ctx->bvh_mode = -1;
     ctx->bvh_is_scene = false;
