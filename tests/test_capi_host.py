@@ -89,3 +89,26 @@ def test_host_only_context_has_no_device_path(built_lib, scene_dirs):
     with pytest.raises(lts.LtsError) as e:
         s.create_bvh_tree(lts.BVH_REFERENCE)
     assert e.value.code == 7
+
+
+def test_reloads_and_a_failed_load_keep_the_scene(built_lib, scene_dirs, tmp_path):
+    """A load that fails leaves the loaded scene as it was; loads of scenes of other sizes in
+    turn (the context parses each into the previous scene's tables) give the same triangles as
+    a fresh context."""
+    import lighttransportsimulation_gb300 as lts
+    d1, sc1, sub1 = scene_dirs["box_sphere"]
+    d2, sc2, sub2 = scene_dirs["materials"]
+    ref = {}
+    for key, (d, sc, sub) in (("a", (d1, sc1, sub1)), ("b", (d2, sc2, sub2))):
+        c = lts.Context(-1)
+        ref[key] = lts.Scene.parse(c, d, sc, sub, 32, 32).triangles().copy()
+        c.close()
+    ctx = lts.Context(-1)
+    s = lts.Scene.parse(ctx, d1, sc1, sub1, 32, 32)
+    with pytest.raises(lts.LtsError):
+        lts.Scene.parse(ctx, str(tmp_path), "nope", None, 32, 32)
+    assert np.array_equal(s.triangles().view(np.uint32), ref["a"].view(np.uint32))
+    for key, (d, sc, sub) in (("b", (d2, sc2, sub2)), ("a", (d1, sc1, sub1)), ("b", (d2, sc2, sub2))):
+        s = lts.Scene.parse(ctx, d, sc, sub, 32, 32)
+        assert np.array_equal(s.triangles().view(np.uint32), ref[key].view(np.uint32))
+    ctx.close()
