@@ -38,15 +38,44 @@ def scene_digest(d):
     return out
 
 
+# The reference's own shipped scenes (tests/golden/shipped_inputs.npz holds their input files,
+# tests/golden/make_golden.py made the fixtures from the reference): kind -> (scene, subject).
+SHIPPED = {"closeup_diamond": ("res/platforms/closeupPlane", "res/diamond"),
+           "closeup_moai": ("res/platforms/closeupPlane", "res/moai"),
+           "bigbox_diamond": ("res/platforms/bigBox", "res/diamond")}
+
+
+def write_shipped(d):
+    """Recreates the shipped scenes' input files under d, at their paths in the reference tree."""
+    import hashlib
+    z = np.load(os.path.join(GOLDEN, "shipped_inputs.npz"))
+    digest = []
+    for k in z.files:
+        rel = k[4:].replace("__", "/")
+        os.makedirs(os.path.join(d, os.path.dirname(rel)), exist_ok=True)
+        data = z[k].tobytes()
+        with open(os.path.join(d, rel), "wb") as fh:
+            fh.write(data)
+        digest.append(f"{rel}:{hashlib.sha256(data).hexdigest()}")
+    return digest
+
+
 @pytest.fixture(scope="session")
 def scene_dirs(tmp_path_factory):
-    """Generated parity scenes, checked against the digests recorded in the fixtures."""
+    """Generated parity scenes and the reference's shipped scenes, checked against the digests
+    recorded in the fixtures."""
     out = {}
     for kind in ("box_sphere", "materials", "stress_small"):
         d = str(tmp_path_factory.mktemp(kind))
         sc, sub = write_scene(kind, d)
         fx = np.load(os.path.join(GOLDEN, f"lbvh_{kind}.npz" if kind != "stress_small" else f"render_{kind}.npz"))
         assert list(fx["scene_digest"]) == scene_digest(d), f"scene generator drifted for {kind}"
+        out[kind] = (d, sc, sub)
+    d = str(tmp_path_factory.mktemp("shipped"))
+    digest = write_shipped(d)
+    for kind, (sc, sub) in SHIPPED.items():
+        fx = np.load(os.path.join(GOLDEN, f"lbvh_{kind}.npz"))
+        assert sorted(fx["scene_digest"]) == sorted(digest), f"shipped inputs differ from the fixture's for {kind}"
         out[kind] = (d, sc, sub)
     return out
 

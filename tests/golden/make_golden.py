@@ -16,6 +16,7 @@ lighttransportsimulation_gb300.scenes, and stores what the parity tests compare 
 Each fixture records sha256 digests of the scene files it was made from, so a test can tell a
 changed generator from a changed renderer.  Usage (from the repository root):
     oracle/ref/build_ref.sh && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py shipped /path/to/reference   # the shipped scenes (SHIPPED)
 """
 import hashlib
 import os
@@ -42,6 +43,40 @@ CASES = {
 }
 
 
+# The reference's own shipped scenes (res/ of the reference tree) that need no image texture:
+# the scene of the published 1080p times with two of its subjects (app.params:20-23), and the
+# big box with an area and an infinite light.  Their input files are stored in
+# shipped_inputs.npz, so that the tests can rebuild the scene directory without the reference.
+SHIPPED_FILES = ["res/platforms/closeupPlane.scene", "res/platforms/triPlane.bin", "res/platforms/bigBox.scene",
+                 "res/platforms/bigBox.bin", "res/platforms/bigBox_light.bin", "res/diamond.subject",
+                 "res/diamond.bin", "res/moai.subject", "res/moai.bin"]
+SHIPPED = {
+    "closeup_diamond": dict(scene="res/platforms/closeupPlane", subject="res/diamond", w=480, h=270, spp=4, maxb=5,
+                            rr=2, seed=3, crop=(220, 95, 260, 135), film=dict(w=96, h=54, spp=16)),
+    "closeup_moai": dict(scene="res/platforms/closeupPlane", subject="res/moai", w=480, h=270, spp=4, maxb=5,
+                         rr=2, seed=3, crop=(220, 80, 260, 120), film=dict(w=96, h=54, spp=16)),
+    "bigbox_diamond": dict(scene="res/platforms/bigBox", subject="res/diamond", w=480, h=270, spp=4, maxb=5,
+                           rr=2, seed=3, crop=(220, 115, 260, 155), film=dict(w=96, h=54, spp=16)),
+}
+
+
+def shipped_key(rel):
+    return "in__" + rel.replace("/", "__")
+
+
+def write_shipped_inputs(npz_path, d):
+    """Recreates the shipped scenes' input files under directory d (paths as in the reference
+    tree, relative to its root, which the .scene files name their meshes by)."""
+    z = np.load(npz_path)
+    for k in z.files:
+        if not k.startswith("in__"):
+            continue
+        rel = k[4:].replace("__", "/")
+        os.makedirs(os.path.join(d, os.path.dirname(rel)), exist_ok=True)
+        with open(os.path.join(d, rel), "wb") as fh:
+            fh.write(z[k].tobytes())
+
+
 def scene_digest(d):
     h = {}
     for f in sorted(os.listdir(d)):
@@ -54,9 +89,60 @@ def run(args):
     subprocess.run([REF] + [str(a) for a in args], check=True)
 
 
+def make_case(name, c, root, sc, sub, digest):
+    b = os.path.join(root, "bvh.ltsd")
+    run(["bvh", root, sc, sub, b, c["w"], c["h"]])
+    d = ltsd.read(b)
+    os.remove(b)
+    if d["tri_p"].size > 9 * 20000:  # large meshes: the loader's triangles are pinned by their digest
+        d["tri_p_sha256"] = np.array(hashlib.sha256(np.ascontiguousarray(d.pop("tri_p")).tobytes()).hexdigest())
+    np.savez_compressed(os.path.join(OUT, f"lbvh_{name}.npz"), scene_digest=digest, **d)
+    r = os.path.join(root, "render.ltsd")
+    x0, y0, x1, y1 = c["crop"]
+    run(["render", root, sc, sub, r, c["w"], c["h"], c["spp"], c["maxb"], c["rr"], c["seed"], x0, y0, x1, y1, 8, 0])
+    d = ltsd.read(r)
+    os.remove(r)
+    meta = np.array([c["w"], c["h"], c["spp"], c["maxb"], c["rr"], c["seed"], x0, y0, x1, y1], np.int64)
+    np.savez_compressed(os.path.join(OUT, f"render_{name}.npz"), scene_digest=digest, meta=meta, L=d["L"], sig=d["sig"])
+    f = c["film"]
+    r2 = os.path.join(root, "film.ltsd")
+    run(["render", root, sc, sub, r2, f["w"], f["h"], f["spp"], c["maxb"], c["rr"], c["seed"], 0, 0, f["w"], f["h"], 1, 1])
+    d = ltsd.read(r2)
+    os.remove(r2)
+    meta = np.array([f["w"], f["h"], f["spp"], c["maxb"], c["rr"], c["seed"]], np.int64)
+    np.savez_compressed(os.path.join(OUT, f"film_{name}.npz"), scene_digest=digest, meta=meta, film=d["film"])
+    print(name, "ok")
+
+
+def make_shipped(reference_root):
+    """Fixtures of the reference's shipped scenes; `reference_root` is the reference checkout."""
+    files = {}
+    for rel in SHIPPED_FILES:
+        with open(os.path.join(reference_root, rel), "rb") as fh:
+            files[shipped_key(rel)] = np.frombuffer(fh.read(), np.uint8)
+    inputs = os.path.join(OUT, "shipped_inputs.npz")
+    np.savez_compressed(inputs, **files)
+    with tempfile.TemporaryDirectory() as td:
+        write_shipped_inputs(inputs, td)
+        digest = np.array([f"{k}:{v}" for k, v in shipped_digest(td).items()])
+        for name, c in SHIPPED.items():
+            make_case(name, c, td + "/", c["scene"], c["subject"], digest)
+
+
+def shipped_digest(d):
+    h = {}
+    for rel in SHIPPED_FILES:
+        with open(os.path.join(d, rel), "rb") as fh:
+            h[rel] = hashlib.sha256(fh.read()).hexdigest()
+    return h
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit("oracle/_ref/lts_ref is missing: run oracle/ref/build_ref.sh first")
+    if len(sys.argv) > 1 and sys.argv[1] == "shipped":
+        make_shipped(sys.argv[2] if len(sys.argv) > 2 else "/root/reference")
+        return
     for name, c in CASES.items():
         with tempfile.TemporaryDirectory() as td:
             sc, sub = c["write"](td)

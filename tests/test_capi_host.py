@@ -21,8 +21,13 @@ def test_library_exports_header_symbols(built_lib):
     assert sorted(lts.EXPORTS) == declared
 
 
-@pytest.mark.parametrize("kind", ["box_sphere", "materials"])
+@pytest.mark.parametrize("kind", ["box_sphere", "materials", "closeup_diamond", "closeup_moai", "bigbox_diamond"])
 def test_loader_matches_reference(built_lib, scene_dirs, kind):
+    """The host loader against the reference's parseScene: world triangles (bit patterns, or
+    their sha256 for large meshes), camera and light distribution, on the synthetic parity
+    scenes and the reference's own shipped scenes."""
+    import hashlib
+
     import lighttransportsimulation_gb300 as lts
     d, sc, sub = scene_dirs[kind]
     fx = np.load(os.path.join(GOLDEN, f"lbvh_{kind}.npz"))
@@ -30,7 +35,10 @@ def test_loader_matches_reference(built_lib, scene_dirs, kind):
     ctx = lts.Context(-1)
     s = lts.Scene.parse(ctx, d, sc, sub, int(meta[0]), int(meta[1]))
     tri = s.triangles().reshape(-1)
-    assert np.array_equal(tri.view(np.uint32), fx["tri_p"].view(np.uint32))
+    if "tri_p" in fx.files:
+        assert np.array_equal(tri.view(np.uint32), fx["tri_p"].view(np.uint32))
+    else:
+        assert hashlib.sha256(tri.tobytes()).hexdigest() == str(fx["tri_p_sha256"])
     assert np.array_equal(s.camera().view(np.uint32), fx["camera"].view(np.uint32))
     func, cdf = s.light_distribution()
     assert np.array_equal(func.view(np.uint32), fx["light_func"].view(np.uint32))
@@ -111,4 +119,55 @@ def test_reloads_and_a_failed_load_keep_the_scene(built_lib, scene_dirs, tmp_pat
     for key, (d, sc, sub) in (("b", (d2, sc2, sub2)), ("a", (d1, sc1, sub1)), ("b", (d2, sc2, sub2))):
         s = lts.Scene.parse(ctx, d, sc, sub, 32, 32)
         assert np.array_equal(s.triangles().view(np.uint32), ref[key].view(np.uint32))
+    ctx.close()
+
+
+def _scene_state(s):
+    func, cdf = s.light_distribution()
+    return {"info": s.query_info(), "tri": s.triangles().view(np.uint32).copy(),
+            "cam": s.camera().view(np.uint32).copy(), "func": func.view(np.uint32).copy(),
+            "cdf": cdf.view(np.uint32).copy()}
+
+
+def test_failed_load_part_way_keeps_the_scene(built_lib, scene_dirs, tmp_path):
+    """Loads that fail after the scene header -- a truncated mesh, a vertex index out of range,
+    an unknown material code -- have already written into the spare tables (materials cleared,
+    tables resized); the loaded scene's info, triangles, camera and light distribution still
+    equal a fresh context's."""
+    import shutil
+
+    import lighttransportsimulation_gb300 as lts
+    d1, sc1, sub1 = scene_dirs["materials"]
+    fresh = lts.Context(-1)
+    want = _scene_state(lts.Scene.parse(fresh, d1, sc1, sub1, 40, 24))
+    fresh.close()
+
+    d2 = str(tmp_path / "broken")
+    shutil.copytree(scene_dirs["box_sphere"][0], d2)
+    sc2, sub2 = scene_dirs["box_sphere"][1], scene_dirs["box_sphere"][2]
+    b = os.path.join(d2, "sphere.bin")
+    raw = open(b, "rb").read()
+    ntri, npnt, nuv, nn = struct.unpack("<4i", raw[:16])
+    off = 16 + 12 * npnt + 8 * nuv + 12 * nn
+    bad_index = bytearray(raw)
+    bad_index[off + 36 * (ntri - 1):off + 36 * (ntri - 1) + 4] = struct.pack("<i", npnt + 7)
+    subj = os.path.join(d2, "sphere.subject")
+    txt = open(subj).read()
+    breakers = [
+        lambda: open(b, "wb").write(raw[:off + 36 * (ntri // 2)]),     # mesh ends mid index table
+        lambda: open(b, "wb").write(bytes(bad_index)),                  # last triangle out of range
+        lambda: (open(b, "wb").write(raw),
+                 open(subj, "w").write(txt.replace("L\tc\t0.8 0.8 0.8", "Q\tc\t0.8 0.8 0.8"))),  # unknown material
+    ]
+    ctx = lts.Context(-1)
+    s = lts.Scene.parse(ctx, d1, sc1, sub1, 40, 24)
+    for brk in breakers:
+        brk()
+        with pytest.raises(lts.LtsError) as e:
+            lts.Scene.parse(ctx, d2, sc2, sub2, 64, 64)
+        assert e.value.code == 3
+        got = _scene_state(s)
+        assert got["info"] == want["info"]
+        for k in ("tri", "cam", "func", "cdf"):
+            assert np.array_equal(got[k], want[k]), k
     ctx.close()

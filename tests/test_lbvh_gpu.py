@@ -22,7 +22,7 @@ def _u32(a):
     return np.ascontiguousarray(a).view(np.uint32)
 
 
-@pytest.mark.parametrize("kind", ["box_sphere", "materials"])
+@pytest.mark.parametrize("kind", ["box_sphere", "materials", "closeup_diamond", "closeup_moai", "bigbox_diamond"])
 def test_reference_mode_bit_exact(ctx, scene_dirs, kind):
     """Codes, stable order, children and every node's AABB bit pattern equal the reference's."""
     import lighttransportsimulation_gb300 as lts
@@ -109,20 +109,27 @@ def test_rebuilds_reuse_the_arrival_words(ctx):
         lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"], np.concatenate([mn, mx], 1)[ids])
 
 
-def test_one_million_random_triangles(ctx):
-    """The build benchmark's 1M case (seed 1): codes, order and topology bit-exact; boxes consistent."""
+@pytest.mark.parametrize("n", [1_000_000, 16_000_000])
+def test_benchmark_sizes_both_modes(ctx, n):
+    """The build benchmark's random triangles (seed 1) at 1M and 16M, in the reference's mode
+    (leaf l holds primitive l) and the sorted-leaf mode: codes, stable order and topology
+    bit-exact against the numpy statement; every interior box the union of its children and
+    every leaf box its primitive's, bit for bit."""
     import lighttransportsimulation_gb300 as lts
     from lighttransportsimulation_gb300 import scenes
     from oracle import lbvh_np
-    tris = scenes.random_triangles(1_000_000, seed=1)
-    out = lts.build_bvh_triangles(ctx, tris, lts.BVH_SORTED)
+    tris = scenes.random_triangles(n, seed=1)
     codes, ids = lbvh_np.stable_sort(*lbvh_np.morton_codes(tris))
-    assert np.array_equal(out["sorted_codes"], codes) and np.array_equal(out["sorted_ids"], ids)
     left, right = lbvh_np.karras_topology(codes)
-    assert np.array_equal(out["node_left"][:-1][: len(left)], left)
-    assert np.array_equal(out["node_right"][: len(right)], right)
     mn, mx = lbvh_np.tri_bounds(tris)
-    lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"], np.concatenate([mn, mx], 1)[ids])
+    boxes = np.concatenate([mn, mx], 1)
+    for mode in (lts.BVH_REFERENCE, lts.BVH_SORTED):
+        out = lts.build_bvh_triangles(ctx, tris, mode)
+        assert np.array_equal(out["sorted_codes"], codes) and np.array_equal(out["sorted_ids"], ids)
+        assert np.array_equal(out["node_left"][: n - 1], left) and np.array_equal(out["node_right"][: n - 1], right)
+        lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"],
+                           boxes if mode == lts.BVH_REFERENCE else boxes[ids])
+        del out
 
 
 def test_reference_mode_code_limit(ctx):

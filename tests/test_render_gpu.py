@@ -43,7 +43,10 @@ def ctx(built_lib):
     c.close()
 
 
-@pytest.mark.parametrize("kind", ["box_sphere", "materials", "stress_small"])
+KINDS = ["box_sphere", "materials", "stress_small", "closeup_diamond", "closeup_moai", "bigbox_diamond"]
+
+
+@pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("bvh_mode,integrator,width", [(0, 0, 2), (0, 1, 8), (1, 0, 8), (1, 1, 8), (1, 1, 2), (1, 2, 2)])
 def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator, width):
     import lighttransportsimulation_gb300 as lts
@@ -85,7 +88,7 @@ def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator, width)
         assert drift[same].all()
 
 
-@pytest.mark.parametrize("kind", ["box_sphere", "materials", "stress_small"])
+@pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("integrator", [0, 1, 2])
 def test_film_matches_reference(ctx, scene_dirs, kind, integrator):
     """Full-frame film (Kahan FP32 + FP64 resolve) against the reference's single-thread film."""
