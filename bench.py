@@ -1,26 +1,37 @@
 #!/usr/bin/env python
-"""Benchmark: plain path tracer on the displaced-icosphere workload, 1 GB300.
+"""Benchmark: the path tracer on the material-stress scene, 1 GB300.
 
-Workload (one step = one full render): the open-front box of 5 Lambertian walls and a 0.5x0.5
-ceiling light (Le 10) holding a level-8 icosphere (1,310,720 triangles) radially displaced by
-0.1 * fbm(8 octaves, omega 0.5) with a wrinkled Lambertian texture (8 octaves, omega 0.5);
-1024 x 1024 pixels, 64 spp, 8 bounces, Russian roulette from bounce 3, sampler seed 0.
-67,108,864 paths per step.  Synthetic seeded data written in the reference's own .scene /
-.subject / .bin formats (lighttransportsimulation_gb300.scenes).
+Workload (one step = one full render): inside the open-front box of Lambertian walls with the
+0.5x0.5 ceiling light (Le 10), a displaced glass sphere (UV sphere of 261,120 triangles, IOR 1.5),
+eight rough Trowbridge-Reitz conductor spheres (261,120 triangles each, alpha drawn from
+U[0.05, 0.5], seed 2, pre-transformed copies), a marble-textured Lambertian floor (8 octaves,
+omega 0.5, scale 4) and a constant infinite light of 0.5: 2,350,092 triangles; 1920 x 1080
+pixels, 256 spp, 16 bounces, Russian roulette from bounce 4, sampler seed 0.  530,841,600 paths
+per step.  Synthetic seeded data written in the reference's own .scene / .subject / .bin formats
+(lighttransportsimulation_gb300.scenes).
 
 Reported (one JSON line on rank 0):
-  value      Mpaths/s with the scene and BVH resident in HBM (device time, CUDA events on the
-             renderer's stream, max over ranks);
-  e2e        Mpaths/s through the public API per step: scene upload from host (H2D), LBVH
-             build, render, film read back (D2H);
-  roofline   the render kernel's BVH-node + triangle + film bytes (counted by the kernel) per
-             launch / launch time, against the measured HBM copy bandwidth;
-  lbvh       device time of the bit-exact LBVH build on 1M and 16M random triangles (seed 1)
-             against the 304 B/primitive algorithmic model;
+  value      Mpaths/s of the wavefront integrator with the scene and BVH resident in HBM (device
+             time, CUDA events on the renderer's stream, max over ranks);
+  e2e        Mpaths/s through the public API per step: scene parse and upload from host (H2D),
+             LBVH build, render-BVH build, render, film read back (D2H);
+  roofline   the dominant kernel, k_wf_trace: algorithmic bytes per launch = 32 B per BVH node
+             visit + 36 B per triangle test (the fixed traversal model), over its CUDA-event
+             launch time, against the measured HBM copy bandwidth; beside it the same bytes
+             against an L2 copy bandwidth measured in this run, and 16 FP32 ops per node visit +
+             40 per triangle test against the FP32 issue rate at the sampled SM clock;
+  time_to_rmse  device seconds for the plain megakernel, the plain wavefront and the wavefront
+             with the radiance cache to bring the same scene to RMSE <= 1e-2 against an FP64
+             oracle render of a centred crop (film accumulated over frames);
+  lbvh       device time of the LBVH build on 1M and 16M random triangles (seed 1), in the
+             reference's bit-exact mode and in the sorted-leaf mode, against the 304 B/primitive
+             algorithmic model;
   cpu_baseline  the oracle's CPU port of the reference integrator (OpenMP, all host cores) on
-             a bounded pixel sample of the same workload.
+             a bounded pixel band of the same workload;
+  displaced_icosphere  the same figures (value, e2e) for the displaced-icosphere render
+             (1,310,732 triangles, 1024 x 1024, 64 spp, 8 bounces).
 --impl reference times that CPU port alone, on the same workload and metric.
-Inputs (BVH + triangles, ~150 MB) exceed the 129 MB L2, so no flush runs between steps.
+Inputs (BVH + triangles, ~400 MB) exceed the 129 MB L2, so no flush runs between steps.
 """
 import argparse
 import json
@@ -44,6 +55,13 @@ SMALL = dict(name="displaced_icosphere_box_small", width=256, height=256, spp=16
 # area + infinite light
 STRESS = dict(name="stress_glass_conductors", width=1920, height=1080, spp=256, max_bounce=16, rr_start=4,
               seed=0, level=0)
+
+
+WORKLOADS = {"stress": STRESS, "displaced": WORKLOAD, "small": SMALL}
+
+
+def scene_triangles(wl):
+    return (20 * 4 ** wl["level"] + 12) if wl is not STRESS else 9 * 261120 + 12
 
 
 def scene_dir(wl):
@@ -197,42 +215,47 @@ def run_reference(args, wl):
             "impl": "reference",
             "config": {"workload": wl["name"], "width": wl["width"], "height": wl["height"], "spp": wl["spp"],
                        "max_bounce": wl["max_bounce"], "rr_start": wl["rr_start"], "seed": wl["seed"],
-                       "triangles": (20 * 4 ** wl["level"] + 12) if wl is not STRESS else 9 * 261120 + 12},
+                       "triangles": scene_triangles(wl)},
             "cpu_baseline": {**res, "value": v},
             "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def lbvh_bench(ctx, n, steps, warmup, mode, peaks):
+def lbvh_bench(ctx, n, steps, warmup, modes, peaks):
+    """Device time per LBVH build of n random triangles (seed 1) in each of `modes`
+    (lts.BVH_REFERENCE: the reference's bit-exact tree; lts.BVH_SORTED: sorted-leaf tree), CUDA
+    events on the context's stream, against the 304 B/primitive algorithmic model."""
     import ctypes
 
-    import numpy as np
     import torch
 
+    import lighttransportsimulation_gb300 as lts
     from lighttransportsimulation_gb300 import scenes
     tris = torch.from_numpy(scenes.random_triangles(n, seed=1).reshape(-1)).cuda()
     stream = torch.cuda.ExternalStream(ctx.stream())
     torch.cuda.synchronize()
-    for _ in range(warmup):
-        ctx.check(ctx.lib.lts_bvh_build_device_async(ctx.h, ctypes.c_void_p(tris.data_ptr()), n, mode, -1))
-    ctx.check(ctx.lib.lts_bvh_dump_get(ctx.h, None))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(steps):
-        ctx.check(ctx.lib.lts_bvh_build_device_async(ctx.h, ctypes.c_void_p(tris.data_ptr()), n, mode, -1))
-    e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    m = ctx.metrics()
-    ctx.check(ctx.lib.lts_bvh_dump_get(ctx.h, None))
-    m = ctx.metrics()
-    stages = [round(x, 4) for x in m.bvh_stage_ms]
-    alg = 304.0 * n
-    gbs = alg / (ms * 1e-3) / 1e9
+    out = []
+    for mode in modes:
+        for _ in range(warmup):
+            ctx.check(ctx.lib.lts_bvh_build_device_async(ctx.h, ctypes.c_void_p(tris.data_ptr()), n, mode, -1))
+        ctx.check(ctx.lib.lts_bvh_dump_get(ctx.h, None))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            ctx.check(ctx.lib.lts_bvh_build_device_async(ctx.h, ctypes.c_void_p(tris.data_ptr()), n, mode, -1))
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        ctx.check(ctx.lib.lts_bvh_dump_get(ctx.h, None))
+        stages = [round(x, 4) for x in ctx.metrics().bvh_stage_ms]
+        alg = 304.0 * n
+        gbs = alg / (ms * 1e-3) / 1e9
+        out.append({"n": n, "mode": "reference" if mode == lts.BVH_REFERENCE else "sorted", "ms": round(ms, 4),
+                    "stage_ms_last": stages, "stages": ["bounds", "morton", "sort", "clear", "tree"],
+                    "algorithmic_bytes": alg, "achieved_gbs": round(gbs, 1), "frac_of_hbm": round(gbs / peaks["hbm_gbs"], 4)})
     del tris
     torch.cuda.empty_cache()
-    return {"n": n, "ms": round(ms, 4), "stage_ms_last": stages, "algorithmic_bytes": alg, "achieved_gbs": round(gbs, 1),
-            "frac_of_hbm": round(gbs / peaks["hbm_gbs"], 4)}
+    return out
 
 
 MLP_FWD_FLOP = 2 * (96 * 64 + 4 * 64 * 64 + 64 * 3)  # per query: the six layers' products (3 outputs)
@@ -278,26 +301,118 @@ def mlp_bench(ctx, steps, warmup, peaks, queries=1920 * 1080, train_rows=65536):
     return res
 
 
-def profiled_traffic(kernel, workload, bvh_width):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary (dram__bytes_read.sum +
-    dram__bytes_write.sum over every launch of one render, divided by the launches), or None."""
-    path = os.path.join(ROOT, "profiles", "trace_wavefront_bench.md")
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        m = re.search(r"<!-- traffic: (.*) -->", line)
-        if not m:
-            continue
-        kv = dict(x.split("=", 1) for x in m.group(1).split())
-        if kv.get("kernel") == kernel and kv.get("workload") == workload and kv.get("bvh_width") == str(bvh_width):
-            return int(kv["bytes_per_launch"])
-    return None
+def l2_copy_gbs(reps=100):
+    """Copy bandwidth of a working set that stays in the 129 MB L2: two 24 MiB buffers copied into
+    each other in turn (read + write bytes per copy), CUDA events on torch's stream, best of three
+    rounds.  The L2 figure that the traversal's byte model is held against."""
+    import torch
+    n = 24 << 20
+    a = torch.ones(n, dtype=torch.uint8, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(10):
+        b.copy_(a)
+        a.copy_(b)
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            b.copy_(a)
+            a.copy_(b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * reps * 2 * n / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    del a, b
+    return best
+
+
+def trace_roofline(mr, peaks, peak_kind, l2_gbs, sm_mhz, sms):
+    """Roofline of k_wf_trace over one counted render (metrics `mr` of a kernel-by-kernel render):
+    the traversal's fixed model, 32 B per BVH node visit + 36 B per triangle test of algorithmic
+    bytes and 16 + 40 FP32 ops, per launch and over the launches' CUDA-event time."""
+    nodes, tris = sum(mr.kind_node_visits), sum(mr.kind_tri_tests)
+    launches = max(1, mr.render_iterations)
+    kernel_ms = mr.render_stage_ms[1]
+    alg = 32.0 * nodes + 36.0 * tris
+    achieved = alg / (kernel_ms * 1e-3) / 1e9
+    ops = 16.0 * nodes + 40.0 * tris
+    fp32_peak = sms * 128 * sm_mhz * 1e6  # FP32 lanes per SM x clock
+    fp32_frac = ops / (kernel_ms * 1e-3) / fp32_peak
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None, "kernel": "k_wf_trace",
+            "peak_kind": peak_kind,
+            "algorithmic": "32 B per BVH node visit + 36 B per triangle test (per launch: node visits and "
+                           "triangle tests of the launch, counted by the kernel)",
+            "algorithmic_bytes_per_launch": round(alg / launches), "launches_per_step": launches,
+            "kernel_ms_per_step": round(kernel_ms, 3),
+            "l2": {"achieved": round(achieved, 1), "peak": round(l2_gbs, 1), "unit": "GB/s",
+                   "frac": round(achieved / l2_gbs, 4), "peak_kind": "L2 copy measured in this run"},
+            "fp32_issue": {"ops_per_step": ops, "achieved_tops": round(ops / (kernel_ms * 1e-3) / 1e12, 3),
+                           "peak_tops": round(fp32_peak / 1e12, 2), "frac": round(fp32_frac, 4),
+                           "model": "16 FP32 ops per node visit + 40 per triangle test; peak = SMs x 128 "
+                                    "FP32 lanes x sampled SM clock"}}
+
+
+def render_timed(ctx, desc, steps, stream):
+    """Device milliseconds per render of `steps` back-to-back renders (CUDA events on the
+    renderer's stream)."""
+    import ctypes
+
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.check(ctx.lib.lts_render_async(ctx.h, ctypes.byref(desc)))
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def e2e_render(ctx, wl, integrator, reps):
+    """Seconds per end-to-end render through the public API: parse + upload the scene, LBVH,
+    render-BVH, render, film read back; median of `reps`.  Returns (seconds, h2d, d2h bytes)."""
+    import torch
+
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dir(wl)
+    t, h2d = [], 0
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
+        lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], s2, integrator=integrator).render(
+            wl["spp"], wl["seed"])
+        t.append(time.perf_counter() - t0)
+        h2d = ctx.metrics().scene_upload_bytes
+    return statistics.median(t), int(h2d), wl["width"] * wl["height"] * 12
+
+
+def displaced_extra(args, ctx):
+    """The displaced-icosphere render (1024 x 1024, 64 spp, 8 bounces, 1,310,732 triangles):
+    device Mpaths/s over 3 renders and end to end through the public API."""
+    import torch
+
+    import lighttransportsimulation_gb300 as lts
+    wl = WORKLOAD
+    d, sc, sub = scene_dir(wl)
+    scene = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
+    integ = lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], scene, integrator=1)
+    desc = integ.desc(wl["spp"], wl["seed"])
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    render_timed(ctx, desc, 2, stream)
+    ms = render_timed(ctx, desc, 3, stream)
+    paths = wl["width"] * wl["height"] * wl["spp"]
+    e2e_s, h2d, d2h = e2e_render(ctx, wl, 1, 1)
+    return {"workload": wl["name"], "width": wl["width"], "height": wl["height"], "spp": wl["spp"],
+            "max_bounce": wl["max_bounce"], "rr_start": wl["rr_start"], "triangles": scene.info["triangles"],
+            "value": round(paths / (ms * 1e-3) / 1e6, 3), "unit": "Mpaths/s", "ms_per_step": round(ms, 3),
+            "e2e": {"value": round(paths / e2e_s / 1e6, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h}}
 
 
 def run_gpu(args, wl):
     import ctypes
 
-    import numpy as np
     import torch
 
     import lighttransportsimulation_gb300 as lts
@@ -315,78 +430,53 @@ def run_gpu(args, wl):
     stream = torch.cuda.ExternalStream(ctx.stream())
     paths = wl["width"] * wl["height"] * wl["spp"]
 
-    # warm-up (also builds the LBVH and the leaf-ordered triangles)
+    # warm-up (also builds the LBVH, the render BVH and the leaf-ordered triangles)
     for _ in range(args.warmup):
         ctx.check(ctx.lib.lts_render_async(ctx.h, ctypes.byref(desc)))
     torch.cuda.synchronize()
     ctx.check(ctx.lib.lts_film_get(ctx.h, None, None))
 
     # device-resident timed region
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    kernel_ms = []
     with ClockSampler(local) as clk:
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            ctx.check(ctx.lib.lts_render_async(ctx.h, ctypes.byref(desc)))
-        e1.record(stream)
-        e1.synchronize()
+        ms = render_timed(ctx, desc, args.steps, stream)
     ctx.check(ctx.lib.lts_film_get(ctx.h, None, None))
     mt = ctx.metrics()
     launches_step, iters_step = mt.render_launches, mt.render_iterations
-    ms = e0.elapsed_time(e1) / args.steps
     ms = barrier_max(dist, ms)
     value = replica_throughput(world, paths, ms * 1e-3) / 1e6
+    clocks = clk.summary()
 
-    # one counted render for the roofline's algorithmic bytes and the per-stage device times (the
-    # same kernels, launched one by one instead of as graphs so that each stage can be timed)
+    # one counted render for the roofline's work counts and the per-stage device times (the same
+    # kernels, launched one by one instead of as graphs so that each stage can be timed)
     ctx.set_option("wavefront_graph", 0)
     r = integ.render(wl["spp"], wl["seed"], film=False)
     mr = ctx.metrics()
     render_bvh_ms = round(mr.render_bvh_ms, 3)
     ctx.set_option("wavefront_graph", 1)
-    stages = None
-    if args.integrator == 0:
-        kernel, kernel_ms, kernel_launches = "k_pathtrace", r["render_ms"], 1
-        alg_bytes = 64.0 * r["node_visits"] + 48.0 * r["tri_tests"] + 32.0 * paths
-        alg_text = "64 B per BVH node visit + 48 B per triangle test + 32 B film per path"
-    else:
+    stages, roofline = None, None
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    if args.integrator == 1:
         names = ["generate", "trace", "finalize", "shade", "compact", "gather"]
         stages = {n: round(mr.render_stage_ms[k], 3) for k, n in enumerate(names)}
-        # k_wf_trace (path, shadow and MIS rays in one launch): nodes, triangles, plus the path-state
-        # bytes each ray reads and writes
-        node_b = 80.0 if args.bvh_width == 8 else 64.0
-        state = [56.0, 40.0, 88.0]
-        alg_bytes = sum(node_b * mr.kind_node_visits[k] + 48.0 * mr.kind_tri_tests[k] + state[k] * mr.kind_rays[k]
-                        for k in range(3))
-        alg_text = (f"{int(node_b)} B per BVH node visit + 48 B per triangle test + path state per ray "
-                    f"(56 B path ray, 40 B shadow ray, 88 B MIS ray)")
-        kernel = "k_wf_trace"
-        kernel_ms = mr.render_stage_ms[1]
-        kernel_launches = mr.render_iterations
-    achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
-    traffic = profiled_traffic(kernel, wl["name"], args.bvh_width)
+        roofline = trace_roofline(mr, peaks, peak_kind, l2_copy_gbs(), sm_mhz, sms)
 
-    # end to end through the public API: upload scene (H2D), build, render, read film (D2H)
-    h2d = scene.info["triangles"] * 48 + scene.info["triangles"] * 16 * 2
-    d2h = wl["width"] * wl["height"] * 12
-    t_e2e = []
-    for _ in range(max(1, min(args.steps, 3))):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        s2 = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
-        lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], s2, integrator=args.integrator).render(
-            wl["spp"], wl["seed"])
-        t_e2e.append(time.perf_counter() - t0)
-    e2e_s = barrier_max(dist, statistics.median(t_e2e))
+    # end to end through the public API: parse + upload (H2D), builds, render, film (D2H)
+    e2e_s, h2d, d2h = e2e_render(ctx, wl, args.integrator, max(1, min(args.steps, 3)))
+    e2e_s = barrier_max(dist, e2e_s)
     e2e = replica_throughput(world, paths, e2e_s) / 1e6
 
+    solo = rank == 0 and world == 1
     lbvh = None
     if rank == 0 and not args.skip_lbvh:
-        lbvh = [lbvh_bench(ctx, n, 5, 3, lts.BVH_SORTED, peaks) for n in (1_000_000, 16_000_000)]
-    cpu = cpu_port_sample(wl) if (rank == 0 and world == 1 and not args.skip_cpu) else None
+        lbvh = [x for n in (1_000_000, 16_000_000)
+                for x in lbvh_bench(ctx, n, 5, 3, (lts.BVH_REFERENCE, lts.BVH_SORTED), peaks)]
+    cpu = cpu_port_sample(wl) if (solo and not args.skip_cpu) else None
+    ttr = time_to_rmse(args, ctx) if (solo and wl is STRESS and not args.skip_ttr) else None
+    extra = displaced_extra(args, ctx) if (solo and wl is STRESS and not args.skip_displaced) else None
     if rank == 0:
         line = {
             "metric": "Mpaths/s", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
@@ -405,19 +495,16 @@ def run_gpu(args, wl):
             "mrays_per_s": round(r["rays"] / (r["render_ms"] * 1e-3) / 1e6, 2),
             "e2e": {"value": round(e2e, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "seconds_per_step": round(e2e_s, 4)},
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": round(achieved / peaks["hbm_gbs"], 4),
-                         "traffic": traffic, "traffic_source": "profiles/trace_wavefront_bench.md" if traffic else None,
-                         "kernel": kernel, "launches_per_step": kernel_launches,
-                         "kernel_ms_per_step": round(kernel_ms, 3), "peak_kind": peak_kind,
-                         "algorithmic": alg_text, "algorithmic_bytes_per_step": alg_bytes},
+            "roofline": roofline,
             "stage_ms": stages,
             "traversal": {"node_visits": r["node_visits"], "tri_tests": r["tri_tests"], "rays": r["rays"],
                           "render_bvh_build_ms": render_bvh_ms,
                           "rays_by_kind": {"path": mr.kind_rays[0], "shadow": mr.kind_rays[1], "mis": mr.kind_rays[2]}},
+            "time_to_rmse": ttr,
             "lbvh": lbvh,
             "cpu_baseline": cpu,
-            "clocks": clk.summary(),
+            "displaced_icosphere": extra,
+            "clocks": clocks,
             "gpu_launches": int(args.steps) * launches_step,
             "kernel_launches_per_step": launches_step,
             "wavefront_iterations_per_step": iters_step,
@@ -488,14 +575,18 @@ def views64(args):
 TTR_LEVELS = (0.05, 0.03, 0.02, 0.015, 0.0125, 0.01)
 
 
-def time_to_rmse(args):
-    """Time for the cached wavefront renderer and for the plain megakernel to bring the stress scene
-    (1920x1080, 16 bounces, roulette from 4) to an RMSE <= target against an FP64 oracle render.
-    The oracle is the FP64 megakernel on a centred crop at high spp; RMSE is taken over the crop's
-    interior (2 pixels in from its edge: border pixels of a crop render miss splats from outside).
-    Both renderers accumulate full frames (film_accumulate); time = summed device time of the
-    renders (for the cached renderer this includes the bias check and the Adam steps after each
-    frame, and its warm-up frames)."""
+def time_to_rmse(args, ctx):
+    """Device seconds for the plain megakernel, the plain wavefront and the wavefront with the
+    radiance cache to bring the stress scene (1920x1080, 16 bounces, roulette from 4) to an RMSE
+    <= target against an FP64 oracle render.
+
+    RMSE = sqrt(mean over pixels x RGB of (I - I_oracle)^2) of the resolved linear film, over the
+    interior (2 pixels in) of a centred crop: the oracle is the FP64 renderer on that crop at
+    high spp (border pixels of a crop render miss splats from outside it).  Every renderer
+    renders full frames and accumulates its film across frames (film_accumulate); its time is the
+    summed device time of its renders (for the cached renderer including its warm-up frames and
+    the bias check and Adam steps after every frame).  `image_bias` is the relative difference
+    of the crop interior's mean from the oracle's at the end of the run."""
     import numpy as np
 
     import lighttransportsimulation_gb300 as lts
@@ -504,20 +595,19 @@ def time_to_rmse(args):
     cw, ch = args.ttr_crop
     x0, y0 = (W - cw) // 2, (H - ch) // 2
     x1, y1 = x0 + cw, y0 + ch
-    ctx = lts.Context(0)
     d, sc, sub = scene_dir(wl)
     scene = lts.Scene.parse(ctx, d, sc, sub, W, H)
     maxb, rr = wl["max_bounce"], wl["rr_start"]
+    t_start = time.time()
 
     def interior(film):
         img = film.reshape(H, W, 3)[::-1]  # the resolve flips rows; undo to index by pixel row
         return img[y0 + 2:y1 - 2, x0 + 2:x1 - 2].astype(np.float64)
 
-    # FP64 oracle on the crop, in passes of at most 256 spp
-    t0 = time.time()
+    # FP64 oracle on the crop, in passes of at most 1024 spp
     oracle_ms = 0.0
     o = lts.PathTracingIntegrator(maxb, rr, scene, integrator=lts.INTEGRATOR_FP64)
-    spp_pass = min(args.ttr_oracle_spp, 256)
+    spp_pass = min(args.ttr_oracle_spp, 1024)
     npass = max(1, args.ttr_oracle_spp // spp_pass)
     half = None
     for k in range(npass):
@@ -528,12 +618,15 @@ def time_to_rmse(args):
             half = interior(r["film"])
     oracle = interior(r["film"])
     ctx.set_option("film_accumulate", 0)
-    # the oracle's own error, estimated from its first half against the whole
+    # the oracle's own error, estimated from its first half against the whole (the half's error
+    # against the truth is ~sqrt(2) x the whole's, and their difference ~ the whole's error)
     oracle_err = float(np.sqrt(np.mean((half - oracle) ** 2))) if half is not None else None
+    omean = float(oracle.mean())
 
     def run(kind):
-        integ = lts.PathTracingIntegrator(maxb, rr, scene, integrator=0 if kind == "plain" else 1)
-        spp = args.ttr_spp_plain if kind == "plain" else args.ttr_spp_cached
+        integ = lts.PathTracingIntegrator(maxb, rr, scene, integrator=0 if kind == "megakernel" else 1)
+        spp = {"megakernel": args.ttr_spp_plain, "wavefront": args.ttr_spp_wavefront,
+               "cached": args.ttr_spp_cached}[kind]
         dev_ms, curve, reached = 0.0, [], None
         if kind == "cached":
             lts.RadianceCacheMLP(ctx, seed=7)
@@ -541,14 +634,15 @@ def time_to_rmse(args):
             for k in range(args.ttr_warmup):
                 ctx.set_option("film_accumulate", 0)
                 dev_ms += integ.render(1, 90_000 + k, film=False)["render_ms"]
-        frame = 0
+        frame, img = 0, None
         while dev_ms < 1000 * args.ttr_max_seconds:
             ctx.set_option("film_accumulate", 0 if frame == 0 else 1)
             r = integ.render(spp, 1_000 + frame)
             dev_ms += r["render_ms"]
             frame += 1
-            e = float(np.sqrt(np.mean((interior(r["film"]) - oracle) ** 2)))
-            curve.append((frame * spp, round(dev_ms / 1000, 3), round(e, 5)))
+            img = interior(r["film"])
+            e = float(np.sqrt(np.mean((img - oracle) ** 2)))
+            curve.append((frame * spp, round(dev_ms / 1000, 4), round(e, 5)))
             if e <= args.ttr_target:
                 reached = dev_ms / 1000
                 break
@@ -559,29 +653,35 @@ def time_to_rmse(args):
         for lv in TTR_LEVELS:
             hit = next((c for c in curve if c[2] <= lv), None)
             levels[str(lv)] = hit[1] if hit else None
-        out = {"seconds_to_target": reached, "seconds_run": round(dev_ms / 1000, 3), "spp": frame * spp,
-               "final_rmse": curve[-1][2], "seconds_to_rmse": levels,
+        out = {"seconds_to_target": round(reached, 4) if reached else None, "seconds_run": round(dev_ms / 1000, 3),
+               "spp": frame * spp, "frame_spp": spp, "final_rmse": curve[-1][2],
+               "image_bias": round((float(img.mean()) - omean) / omean, 5), "seconds_to_rmse": levels,
                "curve": curve[:: max(1, len(curve) // 12)] + curve[-1:]}
         if kind == "cached":
-            out.update(cache_bias=round(m.cache_bias, 4), train_loss=round(m.cache_train_loss, 4),
-                       warmup_frames=args.ttr_warmup)
+            out.update(cache_record_bias=round(m.cache_bias, 4), train_loss=round(m.cache_train_loss, 4),
+                       warmup_frames=args.ttr_warmup, unbiased_share=0.03, lr=1e-3,
+                       train_records_per_frame=m.cache_train_samples)
         return out
 
-    plain = run("plain")
+    mk = run("megakernel")
+    wf = run("wavefront")
     cached = run("cached")
-    line = {"metric": "time-to-RMSE", "target_rmse": args.ttr_target, "unit": "s", "higher_is_better": False,
-            "config": {"workload": wl["name"], "width": W, "height": H, "max_bounce": maxb, "rr_start": rr,
-                       "crop": [x0, y0, x1, y1], "oracle_spp": npass * spp_pass,
-                       "oracle_seconds": round(oracle_ms / 1000, 2), "oracle_rmse_estimate": oracle_err,
-                       "frame_spp": {"plain": args.ttr_spp_plain, "cached": args.ttr_spp_cached}},
-            "plain_megakernel": plain, "cached_wavefront": cached,
-            "speedup": (plain["seconds_to_target"] / cached["seconds_to_target"])
-            if plain["seconds_to_target"] and cached["seconds_to_target"] else None,
-            "speedup_by_rmse": {k: (round(plain["seconds_to_rmse"][k] / v, 2) if v and plain["seconds_to_rmse"][k] else None)
-                                for k, v in cached["seconds_to_rmse"].items()},
-            "wall_s": round(time.time() - t0, 1)}
-    print(json.dumps(line))
-    ctx.close()
+
+    def ratio(a, b):
+        return round(a / b, 2) if a and b else None
+
+    return {"target_rmse": args.ttr_target, "unit": "s", "higher_is_better": False,
+            "rmse": "sqrt(mean over crop-interior pixels x RGB of (I - I_oracle)^2), resolved linear film",
+            "crop": [x0, y0, x1, y1], "oracle": {"renderer": "FP64 megakernel", "spp": npass * spp_pass,
+                                                 "seconds": round(oracle_ms / 1000, 2),
+                                                 "rmse_estimate": oracle_err, "mean": omean},
+            "plain_megakernel": mk, "plain_wavefront": wf, "cached_wavefront": cached,
+            "speedup": ratio(mk["seconds_to_target"], cached["seconds_to_target"]),
+            "speedup_vs_plain_wavefront": ratio(wf["seconds_to_target"], cached["seconds_to_target"]),
+            "speedup_by_rmse": {k: ratio(mk["seconds_to_rmse"][k], v) for k, v in cached["seconds_to_rmse"].items()},
+            "speedup_vs_plain_wavefront_by_rmse": {k: ratio(wf["seconds_to_rmse"][k], v)
+                                                   for k, v in cached["seconds_to_rmse"].items()},
+            "wall_s": round(time.time() - t_start, 1)}
 
 
 def main():
@@ -590,16 +690,20 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--small", action="store_true", help="256x256x16 spp level-6 sphere (quick check)")
-    ap.add_argument("--stress", action="store_true",
-                    help="the glass + rough-conductor stress scene (1920x1080, 256 spp, 16 bounces)")
+    ap.add_argument("--workload", default="stress", choices=sorted(WORKLOADS),
+                    help="stress: glass + rough conductors, 1920x1080, 256 spp, 16 bounces (default); "
+                         "displaced: displaced icosphere, 1024x1024, 64 spp, 8 bounces; small: its "
+                         "256x256x16 spp level-6 version (quick check)")
+    ap.add_argument("--small", action="store_true", help="same as --workload small")
     ap.add_argument("--skip-lbvh", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-ttr", action="store_true", help="leave out the time-to-RMSE block")
+    ap.add_argument("--skip-displaced", action="store_true", help="leave out the displaced-icosphere figures")
     ap.add_argument("--integrator", type=int, default=1, choices=[0, 1], help="0 megakernel, 1 wavefront")
     ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8],
                     help="traversal structure: 8-wide compressed BVH or the binary LBVH")
     ap.add_argument("--lbvh-only", type=int, default=0, metavar="N",
-                    help="only time the LBVH build over N random triangles (seed 1)")
+                    help="only time the LBVH build over N random triangles (seed 1), both modes")
     ap.add_argument("--render-bvh", type=int, default=1, choices=[0, 1, 2],
                     help="tree the 8-wide BVH is collapsed from: 1 PLOC clustering with the SAH-optimal "
                          "collapse, 2 PLOC with the greedy collapse, 0 the LBVH itself")
@@ -609,18 +713,22 @@ def main():
     ap.add_argument("--mlp-only", action="store_true",
                     help="radiance-cache network alone: inference over 1920x1080 queries, one 65,536-sample training step")
     ap.add_argument("--time-to-rmse", action="store_true",
-                    help="time for the cached wavefront and the plain megakernel to reach --ttr-target RMSE")
+                    help="only the time-to-RMSE block (megakernel, wavefront, cached wavefront)")
     ap.add_argument("--ttr-target", type=float, default=1e-2)
     ap.add_argument("--ttr-crop", type=int, nargs=2, default=[192, 108])
-    ap.add_argument("--ttr-oracle-spp", type=int, default=16384)
-    ap.add_argument("--ttr-spp-plain", type=int, default=8)
-    ap.add_argument("--ttr-spp-cached", type=int, default=4)
+    ap.add_argument("--ttr-oracle-spp", type=int, default=65536)
+    ap.add_argument("--ttr-spp-plain", type=int, default=8, help="spp per frame of the plain megakernel")
+    ap.add_argument("--ttr-spp-wavefront", type=int, default=8, help="spp per frame of the plain wavefront")
+    ap.add_argument("--ttr-spp-cached", type=int, default=4, help="spp per frame of the cached wavefront")
     ap.add_argument("--ttr-warmup", type=int, default=8)
     ap.add_argument("--ttr-max-seconds", type=float, default=60.0)
     args = ap.parse_args()
-    wl = SMALL if args.small else (STRESS if args.stress else WORKLOAD)
+    wl = WORKLOADS["small" if args.small else args.workload]
     if args.time_to_rmse:
-        time_to_rmse(args)
+        import lighttransportsimulation_gb300 as lts
+        ctx = lts.Context(0)
+        print(json.dumps({"time_to_rmse": time_to_rmse(args, ctx)}))
+        ctx.close()
         return
     if args.views64:
         views64(args)
@@ -628,7 +736,8 @@ def main():
     if args.lbvh_only:
         import lighttransportsimulation_gb300 as lts
         ctx = lts.Context(0)
-        print(json.dumps(lbvh_bench(ctx, args.lbvh_only, args.steps, args.warmup, lts.BVH_SORTED, measured_peaks()[0])))
+        print(json.dumps(lbvh_bench(ctx, args.lbvh_only, args.steps, args.warmup, (lts.BVH_REFERENCE, lts.BVH_SORTED),
+                                    measured_peaks()[0])))
         ctx.close()
         return
     if args.mlp_only:

@@ -24,7 +24,7 @@ extern "C" {
 #define LTS_ERR_IO 2          /* file missing or unreadable                            */
 #define LTS_ERR_PARSE 3       /* malformed app.params / .scene / .subject / .bin       */
 #define LTS_ERR_CUDA 4        /* CUDA runtime error (message in lts_last_error)        */
-#define LTS_ERR_OOM 5         /* device allocation failed or exceeded LTS_MAX_DEVICE_MB */
+#define LTS_ERR_OOM 5         /* an allocation failed or exceeded LTS_MAX_DEVICE_MB    */
 #define LTS_ERR_UNSUPPORTED 6 /* input uses a feature outside this renderer's scope    */
 #define LTS_ERR_STATE 7       /* call order (e.g. render before load)                  */
 #define LTS_ERR_DEVICE 8      /* a kernel reported an error flag (queue overflow, wait limit) */
@@ -133,9 +133,11 @@ int lts_bvh_dump_get(lts_ctx* ctx, lts_bvh_dump* dump);
  * [(n-1) x 64 bytes: left box, right box, children (>= 0 interior, < 0 leaf ~l), first and last
  * leaf of the node's range], d_leaf_prim
  * [n], d_root_bounds [6].  Runs on `stream` (a cudaStream_t, NULL for the default stream) and
- * waits for it before returning.  The first call on a device looks up the array's address
- * (may load the module): make it before any stream capture.  Calls share the array, so calls
- * that overlap on the GPU race. */
+ * blocks until that work has finished: it copies the kernels' error word to the host and
+ * synchronises the stream before returning.  The first call on a device looks up the array's
+ * address (may load the module): make it before any stream capture.  The address is kept for
+ * the process's life, so after cudaDeviceReset of a device this entry point is not called on it
+ * again.  Calls share the array, so calls that overlap on the GPU race. */
 #define LTS_NOALLOC_MAX_PRIMITIVES 262144
 int lts_bvh_build_noalloc(const float* d_tri_p9, int32_t n, int32_t mode, int32_t code_limit,
                           uint32_t* d_sorted_codes, int32_t* d_sorted_ids, void* d_nodes, int32_t* d_leaf_prim,
@@ -248,8 +250,19 @@ int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts
  *                             device memory, ~400 B per slot, ~650 B with the radiance cache)
  *   "wavefront_sample_chunk"  finished-sample buffer capacity in samples (0: automatic, 2^27);
  *                             samples per pixel are rendered in chunks that fit it
+ *   "debug_spin_limit"        poll limit of every bounded wait of the kernels (the sort's
+ *                             look-back on a predecessor tile, the tensor-core mbarrier waits);
+ *                             0 restores the default (2^22 polls, over a second).  A test lowers
+ *                             it to see a wait run out; accepted before any scene is loaded
  * Unknown keys and negative values return LTS_ERR_ARG. */
 int lts_set_option(lts_ctx* ctx, const char* key, int64_t value);
+
+/* Check of the bounded waits (no counterpart in the reference; the reference has no bounded
+ * wait).  Runs one wait that nothing ends: which 0 polls a flag word as the sort's look-back
+ * does, which 1 waits on an mbarrier phase as the tensor-core kernels do.  The wait gives up
+ * after the poll limit, the kernel sets its error flag and returns, and the call returns
+ * LTS_ERR_DEVICE with the flag in lts_last_error; the context stays usable. */
+int lts_debug_wait_timeout(lts_ctx* ctx, int32_t which);
 
 /* Tensor-core layout check (no counterpart in the reference): one 5th-generation tensor-core
  * product of bf16 operands with FP32 accumulation, in one of the three operand arrangements the
@@ -308,6 +321,8 @@ typedef struct {
     double scene_parse_ms, scene_upload_ms;
     /* device milliseconds of the last render-BVH rebuild (clustering + 8-wide collapse) */
     double render_bvh_ms;
+    /* host-to-device bytes copied by the last lts_load_scene (the scene's tables) */
+    int64_t scene_upload_bytes;
 } lts_metrics;
 int lts_get_metrics(lts_ctx* ctx, lts_metrics* out);
 

@@ -38,7 +38,8 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_write_image", "lts_get_metrics", "lts_bvh_build_noalloc", "lts_debug_trace_sample",
            "lts_debug_trace_get", "lts_set_option", "lts_debug_umma_probe", "lts_mlp_init", "lts_mlp_set_params",
            "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step", "lts_mlp_forward_device_async",
-           "lts_mlp_train_step_device_async", "lts_render_views", "lts_autotune_views", "lts_obj_to_bin"]
+           "lts_mlp_train_step_device_async", "lts_render_views", "lts_autotune_views", "lts_obj_to_bin",
+           "lts_debug_wait_timeout"]
 
 
 class LtsError(RuntimeError):
@@ -87,7 +88,8 @@ class Metrics(ctypes.Structure):
                 ("cache_queries", ctypes.c_double), ("cache_train_samples", ctypes.c_int32),
                 ("cache_train_loss", ctypes.c_double), ("cache_bias", ctypes.c_double),
                 ("cache_train_ms", ctypes.c_double), ("scene_parse_ms", ctypes.c_double),
-                ("scene_upload_ms", ctypes.c_double), ("render_bvh_ms", ctypes.c_double)]
+                ("scene_upload_ms", ctypes.c_double), ("render_bvh_ms", ctypes.c_double),
+                ("scene_upload_bytes", ctypes.c_int64)]
 
 
 _lib = None
@@ -133,6 +135,7 @@ def library():
             "lts_mlp_train_step_device_async": (I, [P, P, P, I, ctypes.c_float, P]),
             "lts_render_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P, ctypes.POINTER(RenderOut)]),
             "lts_autotune_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P]),
+            "lts_debug_wait_timeout": (I, [P, I]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)

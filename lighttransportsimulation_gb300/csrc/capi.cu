@@ -111,7 +111,9 @@ int check_device_error(lts_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     if (h) {
         CK(cudaMemsetAsync(ctx->d_error, 0, 4, ctx->stream));
-        return fail(ctx, LTS_ERR_DEVICE, "a kernel reported device error flags 0x" + std::to_string(h));
+        char hex[16];
+        snprintf(hex, sizeof hex, "0x%x", h);
+        return fail(ctx, LTS_ERR_DEVICE, std::string("a kernel reported device error flags ") + hex);
     }
     return LTS_OK;
 }
@@ -267,6 +269,7 @@ int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char
     const auto t1 = std::chrono::steady_clock::now();
     ctx->metrics.scene_parse_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
     ctx->metrics.scene_upload_ms = 0;
+    ctx->metrics.scene_upload_bytes = 0;
     std::swap(ctx->scene, ctx->spare_scene);
     ctx->loaded = true;
     ctx->bvh_mode = -1;
@@ -274,14 +277,24 @@ int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char
     if (ctx->device == -1) return LTS_OK;
     CK(cudaSetDevice(ctx->device));
     if (!ctx->tracer) ctx->tracer.reset(new Tracer());
+    // From here on the host scene is the new one: if its upload fails part way, the device copy
+    // is incomplete (and buffers of the previous scene may already be freed), so the context
+    // holds no usable scene until the next load succeeds.
+    auto upload_failed = [ctx](int code, const std::string& msg) {
+        ctx->loaded = false;
+        ctx->tracer->drop_scene();
+        return fail(ctx, code, msg);
+    };
     std::string e = ctx->tracer->upload_scene(ctx->scene, ctx->stream);
-    if (!e.empty()) return fail(ctx, e.find("memory") != std::string::npos ? LTS_ERR_OOM : LTS_ERR_CUDA, e);
+    if (!e.empty()) return upload_failed(e.find("memory") != std::string::npos ? LTS_ERR_OOM : LTS_ERR_CUDA, e);
     // the LBVH input (9 floats per triangle), expanded on the device from the uploaded tables
     int rc = ensure_tri_buffer(ctx, 9 * (size_t)ctx->scene.triangles());
-    if (rc) return rc;
+    if (rc) return upload_failed(rc, ctx->err);
     e = ctx->tracer->triangle_soup(ctx->d_tri, ctx->stream);
-    if (!e.empty()) return fail(ctx, LTS_ERR_CUDA, e);
-    CK(cudaStreamSynchronize(ctx->stream));
+    if (!e.empty()) return upload_failed(LTS_ERR_CUDA, e);
+    const cudaError_t se = cudaStreamSynchronize(ctx->stream);
+    if (se != cudaSuccess) return upload_failed(LTS_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(se));
+    ctx->metrics.scene_upload_bytes = (int64_t)ctx->tracer->last_upload_bytes;
     ctx->metrics.scene_upload_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
     return LTS_OK;
@@ -595,6 +608,14 @@ int lts_mlp_train_step_device_async(lts_ctx* ctx, const uint16_t* d_features, co
 int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
     if (!ctx || !key) return LTS_ERR_ARG;
     if (value < 0) return fail(ctx, LTS_ERR_ARG, "option value must be >= 0");
+    if (!strcmp(key, "debug_spin_limit")) {
+        if (ctx->device < 0) return fail(ctx, LTS_ERR_STATE, "host-only context");
+        if (value > (1 << 30)) return fail(ctx, LTS_ERR_ARG, "debug_spin_limit too large");
+        CK(cudaSetDevice(ctx->device));
+        std::string e = lbvh_set_spin_limit((int)value);
+        if (e.empty()) e = mlp_set_spin_limit((int)value);
+        return e.empty() ? LTS_OK : fail(ctx, LTS_ERR_CUDA, e);
+    }
     if (!ctx->tracer) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
     if (!strcmp(key, "wavefront_pool")) {
         if (value >= (1ll << 30)) return fail(ctx, LTS_ERR_ARG, "wavefront_pool too large");
@@ -636,6 +657,17 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
     return LTS_OK;
 }
 
+int lts_debug_wait_timeout(lts_ctx* ctx, int32_t which) {
+    if (!ctx) return LTS_ERR_ARG;
+    if (which < 0 || which > 1) return fail(ctx, LTS_ERR_ARG, "which must be 0 or 1");
+    if (ctx->device < 0) return fail(ctx, LTS_ERR_STATE, "host-only context");
+    CK(cudaSetDevice(ctx->device));
+    const std::string e = which == 0 ? lbvh_debug_wait_flag(ctx->d_error, ctx->stream)
+                                     : mlp_debug_mbar_timeout(ctx->d_error, ctx->stream);
+    if (!e.empty()) return fail(ctx, LTS_ERR_CUDA, e);
+    return check_device_error(ctx);
+}
+
 int lts_debug_trace_sample(lts_ctx* ctx, int64_t k) {
     if (!ctx) return LTS_ERR_ARG;
     if (!ctx->tracer) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
@@ -664,6 +696,7 @@ int lts_get_metrics(lts_ctx* ctx, lts_metrics* out) {
     out->cache_bias = ctx->tracer ? ctx->tracer->last_cache_bias : 0.0;
     out->cache_train_ms = ctx->tracer ? ctx->tracer->last_train_ms : 0.0;
     out->render_bvh_ms = ctx->tracer ? ctx->tracer->last_render_bvh_ms : 0.0;
+    out->scene_upload_bytes = ctx->metrics.scene_upload_bytes;
     for (int k = 0; k < 3; ++k) {
         out->kind_rays[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k] : 0.0;
         out->kind_node_visits[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k + 1] : 0.0;

@@ -10,6 +10,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <new>
+#include <stdexcept>
 #include <algorithm>
 #include <atomic>
 #include <sstream>
@@ -450,6 +452,12 @@ std::string obj_to_bin(const std::string& mesh_name, int* code) {
     } catch (const ParseError& e) {
         *code = e.code;
         return e.msg;
+    } catch (const std::bad_alloc&) {
+        *code = LTS_ERR_OOM;
+        return "out of host memory";
+    } catch (const std::exception& e) {  // e.g. std::system_error when a loader thread cannot start
+        *code = LTS_ERR_IO;
+        return std::string("load failed: ") + e.what();
     }
     *code = LTS_OK;
     return "";
@@ -475,6 +483,12 @@ std::string read_app_params(const std::string& path, AppParams* out, int* code) 
     } catch (const ParseError& e) {
         *code = e.code;
         return e.msg;
+    } catch (const std::bad_alloc&) {
+        *code = LTS_ERR_OOM;
+        return "out of host memory";
+    } catch (const std::exception& e) {  // e.g. std::system_error when a loader thread cannot start
+        *code = LTS_ERR_IO;
+        return std::string("load failed: ") + e.what();
     }
     *code = LTS_OK;
     return "";
@@ -729,6 +743,12 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
     } catch (const ParseError& e) {
         *code = e.code;
         return e.msg;
+    } catch (const std::bad_alloc&) {
+        *code = LTS_ERR_OOM;
+        return "out of host memory";
+    } catch (const std::exception& e) {  // e.g. std::system_error when a loader thread cannot start
+        *code = LTS_ERR_IO;
+        return std::string("load failed: ") + e.what();
     }
     return "";
 }

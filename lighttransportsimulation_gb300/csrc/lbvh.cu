@@ -38,6 +38,28 @@ __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
 
 // Stage a block's run of `count` triangles (9 floats each) into shared memory with 16-byte
 // loads when the run start is 16-byte aligned, scalar loads otherwise.
+// Poll limit of the waits on another block's flag: kSpinLimit, unless a test shrinks it
+// (lts_set_option "debug_spin_limit") to see a wait run out.
+__device__ int g_spin_limit = kSpinLimit;
+
+// One poll of a bounded wait: counts it and backs off, or, past the limit, sets
+// DEV_ERR_LOOKBACK_TIMEOUT and returns false so that the caller gives up.
+__device__ __forceinline__ bool spin_or_give_up(int& spins, uint32_t* err) {
+    if (++spins > g_spin_limit) {
+        atomicOr(err, DEV_ERR_LOOKBACK_TIMEOUT);
+        return false;
+    }
+    __nanosleep(32);
+    return true;
+}
+
+// Check of the bounded wait itself: one thread waits on a flag word that nothing sets.
+__global__ void k_debug_wait_flag(const uint32_t* flag, uint32_t* err) {
+    int spins = 0;
+    while (ld_relaxed(flag) == 0u)
+        if (!spin_or_give_up(spins, err)) return;
+}
+
 __device__ __forceinline__ void stage_tris(const float* __restrict__ tri, long first, int count, float* s) {
     const long f0 = first * 9;
     const int nf = count * 9;
@@ -329,13 +351,7 @@ __global__ __launch_bounds__(kSortThreads, LTS_SORT_MIN_BLOCKS) void k_onesweep(
             }
             if (done) break;
             k -= used;
-            if (used < kLookback) {
-                if (++spins > kSpinLimit) {
-                    atomicOr(err, DEV_ERR_LOOKBACK_TIMEOUT);
-                    break;
-                }
-                __nanosleep(32);
-            }
+            if (used < kLookback && !spin_or_give_up(spins, err)) break;
         }
         st_relaxed(st + dig, kFlagPrefix | (excl + tot));
     }
@@ -765,6 +781,25 @@ std::string Lbvh::build(const float* d_tri, int nn, int md, int code_limit, cuda
     return "";
 }
 
+std::string lbvh_set_spin_limit(int limit) {
+    const int v = limit > 0 ? limit : kSpinLimit;
+    LTS_TRY(cudaMemcpyToSymbol(g_spin_limit, &v, sizeof v));
+    return "";
+}
+
+std::string lbvh_debug_wait_flag(uint32_t* d_err, cudaStream_t s) {
+    uint32_t* flag = nullptr;
+    LTS_TRY(dev_alloc((void**)&flag, 4));
+    cudaError_t e = cudaMemsetAsync(flag, 0, 4, s);
+    if (e == cudaSuccess) {
+        k_debug_wait_flag<<<1, 1, 0, s>>>(flag, d_err);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    dev_free(flag);
+    return e == cudaSuccess ? std::string() : std::string("debug wait: ") + cudaGetErrorString(e);
+}
+
 void Lbvh::stage_ms(float out[5]) const {
     for (int i = 0; i < 5; ++i) {
         out[i] = 0.f;
@@ -794,7 +829,10 @@ void Lbvh::stage_ms(float out[5]) const {
 // start of each call, and two calls that overlap on the GPU (different streams, or different host
 // threads) race on it.  The first call on a device looks up the array's device address with
 // cudaGetSymbolAddress (which may load the module), so that first call should be made before any
-// stream capture begins.
+// stream capture begins.  The address is kept for the life of the process: after
+// cudaDeviceReset on a device, its next call would use a stale address, so a program that resets
+// a device does not call this entry point on it again.  Every call blocks until its work on the
+// given stream has finished (it reads the kernels' error word back before returning).
 // ---------------------------------------------------------------------------------------------
 namespace lts {
 namespace {
@@ -865,12 +903,12 @@ extern "C" int lts_bvh_build_noalloc(const float* d_tri, int32_t n, int32_t mode
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return LTS_ERR_CUDA;
     const int stream_grid = std::min(grid_for((long)N, kBlock), sms * 8);
     // clear everything the kernels expect to start zeroed (or all-ones)
-    cudaMemsetAsync(err, 0, 4, s);
-    cudaMemsetAsync(gbounds, 0xff, 12, s);
-    cudaMemsetAsync(gbounds + 3, 0x00, 12, s);
-    cudaMemsetAsync(hist, 0, 4 * 4 * 256, s);
-    cudaMemsetAsync(status, 0, 4 * 4 * 256 * tiles, s);
-    cudaMemsetAsync(counters, 0, 4 * 8, s);
+    if (cudaMemsetAsync(err, 0, 4, s) != cudaSuccess || cudaMemsetAsync(gbounds, 0xff, 12, s) != cudaSuccess ||
+        cudaMemsetAsync(gbounds + 3, 0x00, 12, s) != cudaSuccess ||
+        cudaMemsetAsync(hist, 0, 4 * 4 * 256, s) != cudaSuccess ||
+        cudaMemsetAsync(status, 0, 4 * 4 * 256 * tiles, s) != cudaSuccess ||
+        cudaMemsetAsync(counters, 0, 4 * 8, s) != cudaSuccess)
+        return LTS_ERR_CUDA;
     k_scene_bounds<<<stream_grid, kBlock, 0, s>>>(d_tri, n, gbounds);
     const bool identity = code_limit < 0 || code_limit >= n;  // every id is its position
     k_morton<<<stream_grid, kBlock, 0, s>>>(d_tri, n, gbounds, code_limit, d_codes, identity ? nullptr : d_ids, hist);
@@ -886,7 +924,7 @@ extern "C" int lts_bvh_build_noalloc(const float* d_tri, int32_t n, int32_t mode
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
-    if (n > 1) cudaMemsetAsync(flags, 0, 4 * (N - 1), s);  // arrival words, epoch 1
+    if (n > 1 && cudaMemsetAsync(flags, 0, 4 * (N - 1), s) != cudaSuccess) return LTS_ERR_CUDA;  // arrival words, epoch 1
     int32_t* pending = reinterpret_cast<int32_t*>(codes_alt);  // codes_alt and ids_alt: 2n ints
     k_tree<<<grid_for((long)N, kTreeBlock), kTreeBlock, 0, s>>>(d_tri, n, mode, d_ids, d_codes, nodes, pending,
                                                                 counters + 4, d_leaf_prim, d_root_bounds);

@@ -69,4 +69,10 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = LTS_SORT_ITEMS;
 constexpr int kSortTile = kSortThreads * kSortItems;
 
+// Bounded waits on another block's flag (the sort's look-back): set the poll limit (<= 0: the
+// default kSpinLimit); run one such wait on a flag that nothing sets, so that it runs out and
+// sets DEV_ERR_LOOKBACK_TIMEOUT in *d_err (synchronises the stream).
+std::string lbvh_set_spin_limit(int limit);
+std::string lbvh_debug_wait_flag(uint32_t* d_err, cudaStream_t s);
+
 }  // namespace lts

@@ -27,9 +27,12 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
     __shared__ uint32_t s_stack[kStack * kThreads];
     const int tid = threadIdx.y * kBX + threadIdx.x;
     uint32_t* stack = s_stack + tid;
-#if !LTS_FP64  // the FP64 build adds every splat to the FP64 film directly
+#if !LTS_FP64
     __shared__ float s_film[32 * kThreads];
     float* acc = s_film + tid;
+#else  // the FP64 build sums its 2x2 core pixels in double (no compensation needed)
+    __shared__ double s_film64[16 * kThreads];
+    double* acc64 = s_film64 + tid;
 #endif
     const int i = rp.x0 + blockIdx.x * kBX + threadIdx.x;
     const int j = rp.y0 + blockIdx.y * kBY + threadIdx.y;
@@ -41,6 +44,9 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
 #if !LTS_FP64
 #pragma unroll
     for (int k = 0; k < 32; ++k) acc[k * kThreads] = 0.0f;
+#else
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc64[k * kThreads] = 0.0;
 #endif
 
     const float* cam = sv.cam;
@@ -51,7 +57,10 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
     Rng rng;
     rng.key = rp.seed + wang_hash((uint32_t)id);
 
-    for (int s = 0; s < rp.spp; ++s) {
+    // samples of the pixel: all of them when gridDim.z is 1 (the float renderer); the FP64 oracle
+    // launch splits them over z so that a small crop still fills the GPU (every sample has its own
+    // counter-based stream, so the split changes no value)
+    for (int s = (int)blockIdx.z; s < rp.spp; s += (int)gridDim.z) {
         rng.sample = (uint32_t)s;
         rng.draw = 0;
         uint64_t sig = 0xcbf29ce484222325ull;
@@ -242,13 +251,18 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
                     const real wgt = __ldg(sv.filter + iy * 16 + ix);
                     const Spec c = L * wgt;
                     const int ox = x - i, oy = y - j;
-                    if (!LTS_FP64 && ox >= 0 && ox <= 1 && oy >= 0 && oy <= 1) {
-#if !LTS_FP64
+                    if (ox >= 0 && ox <= 1 && oy >= 0 && oy <= 1) {
                         const int base = (oy * 2 + ox) * 4;
+#if !LTS_FP64
                         kahan_add(acc + (base + 0) * kThreads, acc + (16 + base + 0) * kThreads, c.r);
                         kahan_add(acc + (base + 1) * kThreads, acc + (16 + base + 1) * kThreads, c.g);
                         kahan_add(acc + (base + 2) * kThreads, acc + (16 + base + 2) * kThreads, c.b);
                         kahan_add(acc + (base + 3) * kThreads, acc + (16 + base + 3) * kThreads, wgt);
+#else
+                        acc64[(base + 0) * kThreads] += (double)c.r;
+                        acc64[(base + 1) * kThreads] += (double)c.g;
+                        acc64[(base + 2) * kThreads] += (double)c.b;
+                        acc64[(base + 3) * kThreads] += (double)wgt;
 #endif
                     } else {
                         double* fp = rp.film + 4 * ((size_t)y * W + x);
@@ -269,8 +283,7 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
             rp.sample_sig[k] = sig;
         }
     }
-#if !LTS_FP64
-    // flush the 2x2 core accumulators (sum minus compensation) to the FP64 film
+    // flush the 2x2 core accumulators (float: sum minus compensation) to the FP64 film
     for (int oy = 0; oy < 2; ++oy)
         for (int ox = 0; ox < 2; ++ox) {
             const int x = i + ox, y = j + oy;
@@ -278,11 +291,15 @@ __global__ __launch_bounds__(kThreads) void k_pathtrace(const SceneView sv, cons
             double* fp = rp.film + 4 * ((size_t)y * W + x);
             const int base = (oy * 2 + ox) * 4;
             for (int c = 0; c < 4; ++c) {
+#if !LTS_FP64
                 const float sum = acc[(base + c) * kThreads], cmp = acc[(16 + base + c) * kThreads];
                 if (sum != 0.0f || cmp != 0.0f) atomicAdd(fp + c, (double)sum - (double)cmp);
+#else
+                const double sum = acc64[(base + c) * kThreads];
+                if (sum != 0.0) atomicAdd(fp + c, sum);
+#endif
             }
         }
-#endif
     // ray counter: one atomic per warp (lanes outside the crop have already returned)
     const unsigned mask = __activemask();
     const unsigned tot = __reduce_add_sync(mask, (unsigned)rays);

@@ -436,6 +436,14 @@ __global__ void k_to_bf16(const float* __restrict__ w, uint16_t* __restrict__ w1
     if (i < n) w16[i] = __bfloat16_as_ushort(__float2bfloat16_rn(w[i]));
 }
 
+// Check of the bounded mbarrier wait itself: an mbarrier expecting one arrival that never comes.
+__global__ void k_debug_mbar_timeout(uint32_t* err) {
+    __shared__ __align__(8) uint64_t mbar;
+    if (threadIdx.x == 0) mbar_init(&mbar, 1);
+    __syncthreads();
+    (void)mbar_wait(&mbar, 0, err);
+}
+
 }  // namespace
 
 #define TRY(call)                                                                       \
@@ -580,6 +588,19 @@ std::string Mlp::adam(float lr, cudaStream_t s) {
     const float c1 = 1.0f - std::pow(b1, (float)steps), c2 = 1.0f - std::pow(b2, (float)steps);
     k_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(w32_, grad_, m_, v_, w16_, kMlpParams, lr, b1, b2, c1, c2, 1e-8f);
     TRY(cudaGetLastError());
+    return "";
+}
+
+std::string mlp_set_spin_limit(int limit) {
+    const int v = limit > 0 ? limit : kSpinLimit;
+    TRY(cudaMemcpyToSymbol(g_mbar_spin_limit, &v, sizeof v));
+    return "";
+}
+
+std::string mlp_debug_mbar_timeout(uint32_t* d_err, cudaStream_t s) {
+    k_debug_mbar_timeout<<<1, 32, 0, s>>>(d_err);
+    TRY(cudaGetLastError());
+    TRY(cudaStreamSynchronize(s));
     return "";
 }
 

@@ -66,4 +66,10 @@ class Mlp {
     std::string sync_bf16(cudaStream_t s);
 };
 
+// Bounded mbarrier waits of the tensor-core kernels: set the poll limit (<= 0: the default
+// kSpinLimit); run one wait on an mbarrier phase that nothing completes, so that it runs out and
+// sets DEV_ERR_MMA_TIMEOUT in *d_err (synchronises the stream).
+std::string mlp_set_spin_limit(int limit);
+std::string mlp_debug_mbar_timeout(uint32_t* d_err, cudaStream_t s);
+
 }  // namespace lts

@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 
 #include "dev_common.cuh"
@@ -32,7 +33,13 @@ std::string render64_launch(const SceneView& sv, const RenderParams& rp, int nle
     v.wnodes = nullptr;  // binary traversal in double
     v.wtris = nullptr;
     const dim3 block(kBX, kBY);
-    const dim3 grid((rp.x1 - rp.x0 + kBX - 1) / kBX, (rp.y1 - rp.y0 + kBY - 1) / kBY);
+    dim3 grid((rp.x1 - rp.x0 + kBX - 1) / kBX, (rp.y1 - rp.y0 + kBY - 1) / kBY);
+    // one block per pixel tile leaves most SMs idle on the small high-spp crops this renderer
+    // draws: split the samples over z until there are ~16 blocks per SM
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long tiles = (long)grid.x * grid.y;
+    grid.z = (unsigned)std::max(1L, std::min<long>({(long)rp.spp, (16L * sms + tiles - 1) / tiles, 65535L}));
     if (record)
         k_pathtrace<true><<<grid, block, 0, s>>>(v, rp, nleaf);
     else

@@ -151,10 +151,11 @@ std::string reserve_buf(void*& slot, size_t& cap, size_t bytes) {
     return "";
 }
 template <class T, class A>
-std::string upload(void*& slot, size_t& cap, const std::vector<T, A>& v, cudaStream_t s) {
+std::string upload(void*& slot, size_t& cap, const std::vector<T, A>& v, cudaStream_t s, size_t* bytes) {
     const std::string e = reserve_buf(slot, cap, sizeof(T) * v.size());
     if (!e.empty()) return e;
     if (!v.empty()) TRY(cudaMemcpyAsync(slot, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+    *bytes += sizeof(T) * v.size();
     return "";
 }
 
@@ -229,10 +230,26 @@ Tracer::~Tracer() {
         if (e) cudaEventDestroy(e);
 }
 
+void Tracer::drop_scene() {
+    for (int k = 0; k < kSceneBufs; ++k) {
+        if (bufs_[k]) dev_free(bufs_[k]);
+        bufs_[k] = nullptr;
+        bufcap_[k] = 0;
+    }
+    dev_free(leaf_v_);
+    leaf_v_ = nullptr;
+    leaf_n_ = 0;
+    leaf_serial_ = 0;
+    view_ = SceneView{};
+}
+
 std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
     // buffers stay allocated (each is re-sized where it is used); the leaf-ordered triangle copy
-    // belongs to the previous scene's BVH
+    // belongs to the previous scene's BVH.  The view is rebuilt below: until then it names no
+    // table, since a failed upload can leave any of them freed or half written.
     leaf_serial_ = 0;
+    last_upload_bytes = 0;
+    view_ = SceneView{};
     static bool consts = false;
     if (!consts) {
         unsigned char p2[512];
@@ -285,19 +302,19 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
     // vertex pools and per-corner indices go up as loaded; the per-triangle positions and the
     // shading records are expanded on the device
     std::string e;
-    if (!(e = upload(bufs_[12], bufcap_[12], sc.p, s)).empty()) return e;
-    if (!(e = upload(bufs_[13], bufcap_[13], sc.tri_p, s)).empty()) return e;
-    if (!(e = upload(bufs_[2], bufcap_[2], sc.tri_n, s)).empty()) return e;
-    if (!(e = upload(bufs_[3], bufcap_[3], sc.tri_uv, s)).empty()) return e;
-    if (!(e = upload(bufs_[4], bufcap_[4], sc.n, s)).empty()) return e;
-    if (!(e = upload(bufs_[5], bufcap_[5], sc.uv, s)).empty()) return e;
-    if (!(e = upload(bufs_[11], bufcap_[11], sc.prim_light, s)).empty()) return e;
-    if (!(e = upload(bufs_[14], bufcap_[14], sc.tri_mesh, s)).empty()) return e;
-    if (!(e = upload(bufs_[6], bufcap_[6], mats, s)).empty()) return e;
-    if (!(e = upload(bufs_[7], bufcap_[7], lights, s)).empty()) return e;
-    if (!(e = upload(bufs_[8], bufcap_[8], sc.light_func, s)).empty()) return e;
-    if (!(e = upload(bufs_[9], bufcap_[9], sc.light_cdf, s)).empty()) return e;
-    if (!(e = upload(bufs_[10], bufcap_[10], filt, s)).empty()) return e;
+    if (!(e = upload(bufs_[12], bufcap_[12], sc.p, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[13], bufcap_[13], sc.tri_p, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[2], bufcap_[2], sc.tri_n, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[3], bufcap_[3], sc.tri_uv, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[4], bufcap_[4], sc.n, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[5], bufcap_[5], sc.uv, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[11], bufcap_[11], sc.prim_light, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[14], bufcap_[14], sc.tri_mesh, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[6], bufcap_[6], mats, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[7], bufcap_[7], lights, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[8], bufcap_[8], sc.light_func, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[9], bufcap_[9], sc.light_cdf, s, &last_upload_bytes)).empty()) return e;
+    if (!(e = upload(bufs_[10], bufcap_[10], filt, s, &last_upload_bytes)).empty()) return e;
     if (!(e = reserve_buf(bufs_[0], bufcap_[0], 48 * (size_t)nt)).empty()) return e;
     if (!(e = reserve_buf(bufs_[1], bufcap_[1], 128 * (size_t)nt)).empty()) return e;
     if (nt > 0) {
@@ -581,6 +598,17 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
     st.cache = cache ? 1 : 0;
     st.unb_permille = (uint32_t)std::max(0, std::min(1000, cache_unbiased_permille));
     st.tr_cap = (uint32_t)std::max(0, cache_train_cap);
+    {
+        // acceptance rate of the training-record coin: the previous render's eligible vertices
+        // per path (before any render: every unbiased path), scaled so that ~90 % of tr_cap fills
+        long paths = 0;
+        for (const auto& bt : batches)
+            for (const WfView& v : bt) paths += v.npix * v.nsc;
+        cache_render_paths_ = (double)paths;
+        const double rate = cache_eligible_rate_ >= 0 ? cache_eligible_rate_ : st.unb_permille / 1000.0;
+        const double expect = rate * (double)paths, keep = 0.9 * (double)st.tr_cap;
+        st.tr_accept = expect <= keep ? 0xFFFFFFFFu : (uint32_t)std::min(4294967295.0, 4294967296.0 * keep / expect);
+    }
     st.bounds = sv.root_bounds;
     if (cache) {
         if (wf_cache_cap_ < P || wf_train_cap_ < (long)st.tr_cap) {
@@ -611,7 +639,7 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
     TRY(cudaEventRecord(ev0_, s));
     TRY(cudaMemsetAsync(st.counts, 0, 128, s));
     k_wf_init_free<<<blocks(P), kWfBlock, 0, s>>>(st.q_free, st.pix, st.counts, (int)P);  // every slot free
-    TRY(cudaMemsetAsync(st.counts + 32, 0, 4, s));  // training records of this render
+    TRY(cudaMemsetAsync(st.counts + 32, 0, 8, s));  // training records and eligible vertices of this render
     const bool rec = rp.sample_sig != nullptr;
     const bool wide = sv.wnodes != nullptr;
     int iters = 0, launches = 1;
@@ -800,10 +828,12 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
 // the records in equal mini-batches.
 std::string Tracer::train_cache(uint32_t* d_counts, uint16_t* tr_feat, float* tr_target, uint32_t tr_cap,
                                 cudaStream_t s, uint32_t* d_err) {
-    uint32_t nrec = 0;
-    TRY(cudaMemcpyAsync(&nrec, d_counts + 32, 4, cudaMemcpyDeviceToHost, s));
+    uint32_t cnt[2] = {0, 0};  // records taken, eligible vertices
+    TRY(cudaMemcpyAsync(cnt, d_counts + 32, 8, cudaMemcpyDeviceToHost, s));
     TRY(cudaStreamSynchronize(s));
-    const int n = (int)std::min<uint32_t>(nrec, tr_cap);
+    if (cache_render_paths_ > 0) cache_eligible_rate_ = cnt[1] / cache_render_paths_;
+    last_train_eligible = (int)cnt[1];
+    const int n = (int)std::min<uint32_t>(cnt[0], tr_cap);
     last_train_samples = n;
     if (n <= 0) return "";
     cudaEvent_t a, b;

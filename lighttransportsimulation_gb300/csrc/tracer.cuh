@@ -103,6 +103,10 @@ class Tracer {
     Tracer& operator=(const Tracer&) = delete;
 
     std::string upload_scene(const HostScene& sc, cudaStream_t s);
+    // Forgets the uploaded scene after a failed upload: the scene tables are freed and the view
+    // is emptied, so nothing can read a half-written or freed table.
+    void drop_scene();
+    size_t last_upload_bytes = 0;  // host-to-device bytes of the last upload_scene
     // The uploaded scene's triangles as 9 floats each, scene order (the LBVH build's input).
     std::string triangle_soup(float* d_soup, cudaStream_t s) const;
     std::string render(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, lts_render_out* out,
@@ -134,7 +138,7 @@ class Tracer {
     int cache_unbiased_permille = 30, cache_train_cap = 65536, cache_train_steps = 4;
     float cache_lr = 1e-3f;
     double last_cache_queries = 0, last_cache_bias = 0;
-    int last_train_samples = 0;
+    int last_train_samples = 0, last_train_eligible = 0;
     float last_train_loss = 0, last_train_ms = 0;
     // Keep the film's sums across renders (progressive rendering) instead of clearing them.
     bool film_accumulate = false;
@@ -171,6 +175,9 @@ class Tracer {
     static constexpr size_t kPoolSlotBytes = 392, kCacheSlotBytes = 248;
     long auto_pool(bool cache) const;
     long wf_cache_cap_ = 0, wf_train_cap_ = 0;
+    // eligible training vertices per path of the last cached render (-1: none yet) and the
+    // path count of the current one (the training-record coin's rate)
+    double cache_eligible_rate_ = -1, cache_render_paths_ = 0;
     std::string train_cache(uint32_t* d_counts, uint16_t* tr_feat, float* tr_target, uint32_t tr_cap, cudaStream_t s,
                             uint32_t* d_err);
     long wf_cap_ = 0, wf_fs_cap_ = 0;

@@ -62,11 +62,16 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
 }
 
-// Waits for phase `parity` of the mbarrier to complete, at most kSpinLimit polls; on timeout
-// sets DEV_ERR_MMA_TIMEOUT and returns false.
+// Poll limit of mbar_wait: kSpinLimit, unless a test shrinks it (lts_set_option
+// "debug_spin_limit") to see a wait run out.
+__device__ int g_mbar_spin_limit = kSpinLimit;
+
+// Waits for phase `parity` of the mbarrier to complete, at most g_mbar_spin_limit polls; on
+// timeout sets DEV_ERR_MMA_TIMEOUT and returns false.
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t* err) {
     const uint32_t a = smem_u32(mbar);
-    for (int i = 0; i < kSpinLimit; ++i) {
+    const int limit = g_mbar_spin_limit;
+    for (int i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"

@@ -29,7 +29,9 @@ namespace {
 
 enum : uint32_t { WF_VIS = 1u, WF_MIS = 2u, WF_NEE = 4u, WF_DONE = 8u, WF_CACHE = 16u };
 // path flags (low byte; the bounce count sits above bit 8)
-enum : uint32_t { FL_SPECULAR = 1u, FL_ROUGH = 2u, FL_UNBIASED = 4u, FL_RECORDED = 8u };
+// FL_RECORDED: the path holds a training record; FL_OFFERED: its one chance of a record (at its
+// first vertex after a rough one) has been taken, whether or not the coin accepted it.
+enum : uint32_t { FL_SPECULAR = 1u, FL_ROUGH = 2u, FL_UNBIASED = 4u, FL_RECORDED = 8u, FL_OFFERED = 16u };
 constexpr int kWfBlock = 128;
 constexpr uint64_t kSigBasis = 0xcbf29ce484222325ull;
 
@@ -59,6 +61,12 @@ struct WfState {
     int cache;
     uint32_t unb_permille;  // share of paths traced in full (unbiased), per mille
     uint32_t tr_cap;        // training records per render
+    // Records are a uniform random subset of the render's eligible vertices (every unbiased
+    // path's first vertex after a rough one, count in counts[33]): a vertex is kept when a hash
+    // of its path is <= tr_accept, a rate set from the previous render's eligible count so that
+    // the records rarely reach tr_cap (first come, first served would keep only the vertices of
+    // the earliest bounces and of the first shade classes).
+    uint32_t tr_accept;
     const float* bounds;    // scene bounds: position features are normalised to the unit cube
     uint16_t* feat;         // [pool][96] features of the vertex a path queries
     float4* cache_L;        // [pool] the cache's radiance for that vertex
@@ -216,8 +224,9 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_generate(const SceneView sv, co
     st.smp[slot] = s;
     st.wid[slot] = (int32_t)(w - pc + (long)cj * cw + ci);  // the sample's place in row-major order
     st.draw[slot] = rng.draw;
-    st.flags[slot] = (st.cache && wang_hash((uint32_t)id ^ ((uint32_t)s * 0x9E3779B9u)) % 1000u < st.unb_permille)
-                         ? FL_UNBIASED : 0u;
+    st.flags[slot] =
+        (st.cache && wang_hash((uint32_t)id ^ ((uint32_t)s * 0x9E3779B9u) ^ (vw.seed * 0x85EBCA6Bu)) % 1000u < st.unb_permille)
+            ? FL_UNBIASED : 0u;
     st.pend[slot] = 0u;
     st.pf[slot] = make_float2(pfx, pfy);
     st.ro[slot] = make_float4(vw.cam[0], vw.cam[1], vw.cam[2], 0.f);
@@ -492,16 +501,21 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
         if (!make_bsdf(sv, si, f, RECORD ? &evs : nullptr)) done = true;
     }
     bool recorded = (flags & FL_RECORDED) != 0, rough_seen = (flags & FL_ROUGH) != 0;
+    bool offered = (flags & FL_OFFERED) != 0;
     if (st.cache && !done && rough_seen) {
         // the vertex after the first rough one: cached paths end here with the cache's radiance,
-        // unbiased paths record a training sample once and go on
+        // unbiased paths are offered one training record here and go on
         if (!(flags & FL_UNBIASED)) {
             write_features(st, si, f, st.feat + (size_t)p * 96);
             st.q_cache[atomicAdd(&st.counts[12], 1u)] = p;
             pend |= WF_CACHE;
             done = true;
-        } else if (!recorded) {
-            const uint32_t r = atomicAdd(&st.counts[32], 1u);
+        } else if (!offered) {
+            offered = true;
+            atomicAdd(&st.counts[33], 1u);
+            const uint32_t coin = wang_hash((uint32_t)st.pix[p] * 0x9E3779B9u ^ (uint32_t)st.smp[p] * 0x85EBCA6Bu ^
+                                            vw.seed * 0xC2B2AE35u ^ 0x27D4EB2Fu);
+            const uint32_t r = coin <= st.tr_accept ? atomicAdd(&st.counts[32], 1u) : 0xFFFFFFFFu;
             if (r < st.tr_cap) {
                 write_features(st, si, f, st.tr_feat + (size_t)r * 96);
                 st.tr_idx[p] = (int32_t)r;
@@ -624,7 +638,7 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
     st.pend[p] = pend | (done ? WF_DONE : 0u);
     st.draw[p] = rng.draw;
     st.flags[p] = ((uint32_t)(bounce + 1) << 8) | (specular ? FL_SPECULAR : 0u) | (rough_seen ? FL_ROUGH : 0u) |
-                  (flags & FL_UNBIASED) | (recorded ? FL_RECORDED : 0u);
+                  (flags & FL_UNBIASED) | (recorded ? FL_RECORDED : 0u) | (offered ? FL_OFFERED : 0u);
     st.beta[p] = make_float4(beta.r, beta.g, beta.b, 0.f);
     st.L[p] = make_float4(L.r, L.g, L.b, 0.f);
     if (RECORD) {
