@@ -543,17 +543,39 @@ def views64(args):
     maxb, rr = wl["max_bounce"], wl["rr_start"]
     lts.render_views(scene, views[:2], maxb, rr)  # warm-up: BVH, buffers
     t_alone = sum(lts.render_views(scene, [v], maxb, rr)[1] for v in views)
-    _, t_batch = lts.render_views(scene, views, maxb, rr)
+    films_plain, t_batch = lts.render_views(scene, views, maxb, rr)
     tuned = lts.autotune_views(scene, views, maxb, rr)
     _, t_tuned = lts.render_views(scene, views, maxb, rr)
     lts.RadianceCacheMLP(ctx, seed=7)
     ctx.set_option("radiance_cache", 1)
     biases = []
     for _ in range(12):  # the cache trains on each render; the last render is the timed one
-        _, t_cached = lts.render_views(scene, views, maxb, rr)
+        films_cached, t_cached = lts.render_views(scene, views, maxb, rr)
         biases.append(round(ctx.metrics().cache_bias, 4))
     m = ctx.metrics()
     ctx.set_option("radiance_cache", 0)
+    # per-view RMSE against the FP64 renderer: each view's camera in a scene file of its own, the
+    # FP64 renderer on a centred 32 x 32 crop at args.views_oracle_spp; RMSE over the crop's
+    # interior (2 pixels in), for the plain and the cached batched films
+    from lighttransportsimulation_gb300 import scenes
+    rmse_plain, rmse_cached, oracle_ms = [], [], 0.0
+    for k, v in enumerate(views):
+        W, H = v["width"], v["height"]
+        x0, y0 = (W - 32) // 2, (H - 32) // 2
+        name = scenes.with_camera(d, sc, v, f"view64_{k}")
+        sv = lts.Scene.parse(ctx, d, name, sub, W, H)
+        o = lts.PathTracingIntegrator(maxb, rr, sv, integrator=lts.INTEGRATOR_FP64)
+        npass = max(1, args.views_oracle_spp // 256)
+        for p in range(npass):
+            ctx.set_option("film_accumulate", 0 if p == 0 else 1)
+            r = o.render(min(256, args.views_oracle_spp), 70_000 + 97 * k + p, crop=(x0, y0, x0 + 32, y0 + 32))
+            oracle_ms += r["render_ms"]
+        ctx.set_option("film_accumulate", 0)
+        ref = r["film"].reshape(H, W, 3)[::-1][y0 + 2:y0 + 30, x0 + 2:x0 + 30].astype(np.float64)
+        for films, out in ((films_plain, rmse_plain), (films_cached, rmse_cached)):
+            img = films[k][::-1][y0 + 2:y0 + 30, x0 + 2:x0 + 30].astype(np.float64)
+            out.append(round(float(np.sqrt(np.mean((img - ref) ** 2))), 5))
+    scene = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
     line = {"metric": "Mpaths/s", "unit": "Mpaths/s", "higher_is_better": True, "data": "synthetic",
             "config": {"workload": "64_uneven_views_displaced_icosphere_box", "views": 64, "paths": paths,
                        "max_bounce": maxb, "rr_start": rr,
@@ -566,6 +588,17 @@ def views64(args):
             "batched_autotuned_cached": round(paths / (t_cached * 1e-3) / 1e6, 2),
             "cache": {"bias": round(m.cache_bias, 4), "bias_by_render": biases, "train_samples": m.cache_train_samples,
                       "train_ms": round(m.cache_train_ms, 3)},
+            "rmse_vs_fp64": {"oracle": f"FP64 renderer, centred 32x32 crop of each view, {args.views_oracle_spp} spp; "
+                                       "RMSE over the crop interior (28x28)",
+                             "oracle_seconds": round(oracle_ms / 1000, 2),
+                             "plain": rmse_plain, "cached": rmse_cached,
+                             "plain_mean": round(float(np.mean(rmse_plain)), 5),
+                             "cached_mean": round(float(np.mean(rmse_cached)), 5),
+                             "by_spp": {str(q): {"plain": round(float(np.mean([e for e, v in zip(rmse_plain, views)
+                                                                                if v["spp"] == q])), 5),
+                                                 "cached": round(float(np.mean([e for e, v in zip(rmse_cached, views)
+                                                                                 if v["spp"] == q])), 5)}
+                                        for q in (4, 16, 64)}},
             "ms": {"one_by_one": round(t_alone, 2), "batched": round(t_batch, 2), "autotuned": round(t_tuned, 2),
                    "cached": round(t_cached, 2)}}
     print(json.dumps(line))
@@ -710,6 +743,8 @@ def main():
     ap.add_argument("--pool", type=int, default=0, metavar="PATHS",
                     help="wavefront path-state pool capacity (0: the renderer's automatic size)")
     ap.add_argument("--views64", action="store_true", help="64 batched uneven views (autotuned, with the cache)")
+    ap.add_argument("--views-oracle-spp", type=int, default=1024,
+                    help="spp of the FP64 oracle crops the 64 views' RMSE is taken against")
     ap.add_argument("--mlp-only", action="store_true",
                     help="radiance-cache network alone: inference over 1920x1080 queries, one 65,536-sample training step")
     ap.add_argument("--time-to-rmse", action="store_true",

@@ -233,6 +233,8 @@ int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts
  *   "radiance_cache_train_samples"     training records per render (default 65536)
  *   "radiance_cache_train_steps"       Adam steps per render (default 4)
  *   "radiance_cache_lr_micro"          learning rate in 1e-6 (default 1000 = 1e-3)
+ *   "radiance_cache_ema_permille"      the cache's queries use an exponential moving average of the
+ *                             weights with this decay per Adam step (per mille; 0: the weights)
  *   "film_accumulate"         1: renders add to the film's sums instead of clearing them
  *   "trace_blocks_per_sm"     persistent trace blocks per SM (0, default: all that stay resident)
  *   "wavefront_graph"         1 (default): each wavefront iteration runs as a captured CUDA graph,
@@ -250,12 +252,74 @@ int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts
  *                             device memory, ~400 B per slot, ~650 B with the radiance cache)
  *   "wavefront_sample_chunk"  finished-sample buffer capacity in samples (0: automatic, 2^27);
  *                             samples per pixel are rendered in chunks that fit it
+ *   "watertight"              0 (default): the reference's triangle tests (Moller-Trumbore with
+ *                             barycentrics shrunk by 1e-4, Triangle.cu:50-128), 1: the watertight
+ *                             test of Woop, Benthin and Wald (2013), which lets no ray through a
+ *                             shared edge or vertex of a closed mesh (the fixed mode; renders differ
+ *                             from the reference's near edges)
+ *   "libm_double"             1: the float integrator's cos, sin, acos and log2 are evaluated in
+ *                             double and rounded once to float (the correctly rounded values, as
+ *                             the reference's host build gets them from glibc); 0 (default): CUDA's
+ *                             float functions.  Process-wide; accepted before any scene is loaded
  *   "debug_spin_limit"        poll limit of every bounded wait of the kernels (the sort's
  *                             look-back on a predecessor tile, the tensor-core mbarrier waits);
  *                             0 restores the default (2^22 polls, over a second).  A test lowers
  *                             it to see a wait run out; accepted before any scene is loaded
  * Unknown keys and negative values return LTS_ERR_ARG. */
 int lts_set_option(lts_ctx* ctx, const char* key, int64_t value);
+
+/* Batch ray queries against the loaded scene, through the renderer's traversal and triangle
+ * tests (the "watertight" option selects the test).  Each ray is one Scene::intersect (any = 0:
+ * closest hit, acceleration/Scene.cuh:26-29) or Scene::simpleIntersect (any = 1: a hit before
+ * tMax, Scene.cuh:30-32).  rays: n x 8 floats {ox, oy, oz, tMax, dx, dy, dz, 0} (host).  Out
+ * (host): prim[n] the hit primitive in scene order (-1: none) or, for any = 1, 1 / 0; t[n] the hit
+ * distance (INFINITY for none; t may be NULL).  Uses the render BVH of the last render, else
+ * builds a sorted-leaf LBVH of the scene. */
+int lts_intersect(lts_ctx* ctx, const float* rays, int32_t n, int32_t any, int32_t* prim, float* t);
+
+/* Known-answer check of single device functions (no counterpart in the reference: it runs the
+ * renderer's float device code on the GPU for values a test compares with the reference's own
+ * functions).  n records of 16 floats in `in` (host), 16 floats out per record in `out` (host);
+ * unused slots are zero.  Function fn and its record layout (inputs -> outputs):
+ *   LTS_KAT_QUAKE_RSQRT        x -> quakeIIIFastInvSqrt(x)                   (Geometry.cuh:15-29)
+ *   LTS_KAT_FRESNEL_DIELECTRIC cos, etaI, etaT -> F                          (BxDF.cuh:16-37)
+ *   LTS_KAT_FRESNEL_CONDUCTOR  cos, etaT rgb, k rgb -> F rgb (etaI = 1)      (BxDF.cuh:44-67)
+ *   LTS_KAT_TR_D               wh xyz, alphaX, alphaY -> D(wh)               (Microfacet.cuh:157-165)
+ *   LTS_KAT_TR_LAMBDA          w xyz, alphaX, alphaY -> Lambda(w)            (Microfacet.cuh:130-137)
+ *   LTS_KAT_TR_G1              w xyz, alphaX, alphaY -> G1(w)                (Microfacet.cuh:167-169)
+ *   LTS_KAT_TR_G               wo xyz, wi xyz, alphaX, alphaY -> G(wo, wi)   (Microfacet.cuh:171-173)
+ *   LTS_KAT_TR_SAMPLE11        cosTheta, u1, u2 -> slopeX, slopeY            (Microfacet.cuh:53-96)
+ *   LTS_KAT_TR_SAMPLE_WH       wo xyz, alphaX, alphaY, u1, u2 -> wh xyz      (Microfacet.cuh:175-185)
+ *   LTS_KAT_TR_PDF             wo xyz, wh xyz, alphaX, alphaY -> Pdf(wo, wh) (Microfacet.cuh:187-189)
+ *   LTS_KAT_MF_F               wo xyz, wi xyz, alpha, R rgb, eta rgb, k rgb -> f rgb
+ *                              (MicrofacetReflection::f with FresnelConductor(1, eta, k), Microfacet.cuh:200-209)
+ *   LTS_KAT_MF_PDF             wo xyz, wi xyz, alpha -> Pdf(wo, wi)          (Microfacet.cuh:224-228)
+ *   LTS_KAT_MF_SAMPLE          wo xyz, alpha, u1, u2, R rgb, eta rgb, k rgb -> wi xyz, f rgb, pdf
+ *                              (MicrofacetReflection::sampleF, Microfacet.cuh:211-222)
+ *   LTS_KAT_PERLIN             x, y, z -> perlinNoise                        (Procedural.cuh:130-155)
+ *   LTS_KAT_FBM                p xyz, dpdx xyz, dpdy xyz, omega, maxOctaves -> fbm (Procedural.cuh:161-179)
+ *   LTS_KAT_TURBULENCE         same inputs -> turbulence                     (Procedural.cuh:181-205)
+ *   LTS_KAT_OFFSET_ORIGIN      p xyz, pError xyz, n xyz, w xyz -> origin xyz (Geometry.cuh:782-797)
+ * The BSDF-level functions are evaluated in the shading frame (identity transform). */
+#define LTS_KAT_QUAKE_RSQRT 0
+#define LTS_KAT_FRESNEL_DIELECTRIC 1
+#define LTS_KAT_FRESNEL_CONDUCTOR 2
+#define LTS_KAT_TR_D 3
+#define LTS_KAT_TR_LAMBDA 4
+#define LTS_KAT_TR_G1 5
+#define LTS_KAT_TR_G 6
+#define LTS_KAT_TR_SAMPLE11 7
+#define LTS_KAT_TR_SAMPLE_WH 8
+#define LTS_KAT_TR_PDF 9
+#define LTS_KAT_MF_F 10
+#define LTS_KAT_MF_PDF 11
+#define LTS_KAT_MF_SAMPLE 12
+#define LTS_KAT_PERLIN 13
+#define LTS_KAT_FBM 14
+#define LTS_KAT_TURBULENCE 15
+#define LTS_KAT_OFFSET_ORIGIN 16
+#define LTS_KAT_COUNT 17
+int lts_debug_kat(lts_ctx* ctx, int32_t fn, const float* in, int32_t n, float* out);
 
 /* Check of the bounded waits (no counterpart in the reference; the reference has no bounded
  * wait).  Runs one wait that nothing ends: which 0 polls a flag word as the sort's look-back

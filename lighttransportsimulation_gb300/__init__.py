@@ -39,7 +39,7 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_debug_trace_get", "lts_set_option", "lts_debug_umma_probe", "lts_mlp_init", "lts_mlp_set_params",
            "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step", "lts_mlp_forward_device_async",
            "lts_mlp_train_step_device_async", "lts_render_views", "lts_autotune_views", "lts_obj_to_bin",
-           "lts_debug_wait_timeout"]
+           "lts_debug_wait_timeout", "lts_debug_kat", "lts_intersect"]
 
 
 class LtsError(RuntimeError):
@@ -136,6 +136,8 @@ def library():
             "lts_render_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P, ctypes.POINTER(RenderOut)]),
             "lts_autotune_views": (I, [P, P, I, ctypes.POINTER(RenderDesc), P]),
             "lts_debug_wait_timeout": (I, [P, I]),
+            "lts_debug_kat": (I, [P, I, P, I, P]),
+            "lts_intersect": (I, [P, P, I, I, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -242,6 +244,27 @@ class Scene:
         cdf = np.empty(n + 1, np.float32)
         self.ctx.check(self.ctx.lib.lts_scene_get_light_distribution(self.ctx.h, _ptr(func), _ptr(cdf)))
         return func[:n], cdf
+
+    def _query(self, o, d, tmax, any_hit):
+        o = np.asarray(o, np.float32).reshape(-1, 3)
+        d = np.asarray(d, np.float32).reshape(-1, 3)
+        n = len(o)
+        rays = np.zeros((n, 8), np.float32)
+        rays[:, 0:3], rays[:, 4:7] = o, d
+        rays[:, 3] = np.broadcast_to(np.asarray(tmax, np.float32), (n,))
+        prim = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        self.ctx.check(self.ctx.lib.lts_intersect(self.ctx.h, _ptr(rays), n, 1 if any_hit else 0, _ptr(prim), _ptr(t)))
+        return prim, t
+
+    def intersect(self, o, d, tmax=np.inf):
+        """Scene::intersect (acceleration/Scene.cuh:26-29) over a batch of rays: the closest hit's
+        primitive in scene order (-1: none) and distance."""
+        return self._query(o, d, tmax, False)
+
+    def simple_intersect(self, o, d, tmax):
+        """Scene::simpleIntersect (acceleration/Scene.cuh:30-32): True where a hit lies before tmax."""
+        return self._query(o, d, tmax, True)[0] == 1
 
     def create_bvh_tree(self, mode=BVH_SORTED, dump=True):
         """LBVH of the scene; returns the dump dict (codes, ids, node arrays) when dump."""

@@ -608,6 +608,13 @@ int lts_mlp_train_step_device_async(lts_ctx* ctx, const uint16_t* d_features, co
 int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
     if (!ctx || !key) return LTS_ERR_ARG;
     if (value < 0) return fail(ctx, LTS_ERR_ARG, "option value must be >= 0");
+    if (!strcmp(key, "libm_double")) {
+        if (ctx->device < 0) return fail(ctx, LTS_ERR_STATE, "host-only context");
+        if (value > 1) return fail(ctx, LTS_ERR_ARG, "libm_double must be 0 or 1");
+        CK(cudaSetDevice(ctx->device));
+        const std::string e = set_libm_double((int)value);
+        return e.empty() ? LTS_OK : fail(ctx, LTS_ERR_CUDA, e);
+    }
     if (!strcmp(key, "debug_spin_limit")) {
         if (ctx->device < 0) return fail(ctx, LTS_ERR_STATE, "host-only context");
         if (value > (1 << 30)) return fail(ctx, LTS_ERR_ARG, "debug_spin_limit too large");
@@ -649,11 +656,69 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
     } else if (!strcmp(key, "render_bvh")) {
         if (value < 0 || value > 2) return fail(ctx, LTS_ERR_ARG, "render_bvh must be 0, 1 or 2");
         ctx->tracer->render_bvh = (int)value;
+    } else if (!strcmp(key, "radiance_cache_ema_permille")) {
+        if (value > 999) return fail(ctx, LTS_ERR_ARG, "radiance_cache_ema_permille must be 0..999");
+        if (!ctx->mlp) return fail(ctx, LTS_ERR_STATE, "no radiance-cache network (lts_mlp_init)");
+        ctx->mlp->ema = (float)value / 1000.0f;
+    } else if (!strcmp(key, "watertight")) {
+        if (value > 1) return fail(ctx, LTS_ERR_ARG, "watertight must be 0 or 1");
+        ctx->tracer->watertight = (int)value;
     } else if (!strcmp(key, "wavefront_sample_chunk")) {
         ctx->tracer->wf_sample_cap = (long)value;
     } else {
         return fail(ctx, LTS_ERR_ARG, std::string("unknown option ") + key);
     }
+    return LTS_OK;
+}
+
+int lts_intersect(lts_ctx* ctx, const float* rays, int32_t n, int32_t any, int32_t* prim, float* t) {
+    if (!ctx || n < 0 || (n > 0 && (!rays || !prim)) || (any != 0 && any != 1) || n > (1 << 28))
+        return fail(ctx, LTS_ERR_ARG, "bad ray query");
+    if (ctx->device == -1) return fail(ctx, LTS_ERR_STATE, "host-only context (device -1) cannot run kernels");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    CK(cudaSetDevice(ctx->device));
+    if (!(ctx->bvh_is_scene && ctx->bvh_mode >= 0)) {  // the last render's BVH, else a sorted-leaf one
+        const int rc = lts_bvh_build(ctx, LTS_BVH_SORTED, nullptr);
+        if (rc) return rc;
+    }
+    if (n == 0) return LTS_OK;
+    unsigned char* d = nullptr;
+    CK(dev_alloc((void**)&d, 32 * (size_t)n + 8 * (size_t)n));
+    float4* d_rays = reinterpret_cast<float4*>(d);
+    int32_t* d_prim = reinterpret_cast<int32_t*>(d + 32 * (size_t)n);
+    float* d_t = reinterpret_cast<float*>(d + 36 * (size_t)n);
+    cudaError_t e = cudaMemcpyAsync(d_rays, rays, 32 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+    std::string msg = e == cudaSuccess ? ctx->tracer->intersect(*ctx->bvh, d_rays, n, any, d_prim, d_t, ctx->stream,
+                                                                 ctx->d_error)
+                                       : "";
+    if (e == cudaSuccess && msg.empty())
+        e = cudaMemcpyAsync(prim, d_prim, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && msg.empty() && t)
+        e = cudaMemcpyAsync(t, d_t, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && msg.empty()) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(d);
+    if (!msg.empty()) return fail(ctx, LTS_ERR_CUDA, msg);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "ray query");
+    return check_device_error(ctx);
+}
+
+int lts_debug_kat(lts_ctx* ctx, int32_t fn, const float* in, int32_t n, float* out) {
+    if (!ctx) return LTS_ERR_ARG;
+    if (fn < 0 || fn >= LTS_KAT_COUNT || n < 0 || (n > 0 && (!in || !out)) || n > (1 << 24))
+        return fail(ctx, LTS_ERR_ARG, "bad known-answer request");
+    if (ctx->device < 0) return fail(ctx, LTS_ERR_STATE, "host-only context");
+    if (n == 0) return LTS_OK;
+    CK(cudaSetDevice(ctx->device));
+    float* d = nullptr;
+    CK(dev_alloc((void**)&d, 2 * 64 * (size_t)n));
+    cudaError_t e = cudaMemcpyAsync(d, in, 64 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+    std::string msg = e == cudaSuccess ? kat_launch(fn, d, n, d + 16 * (size_t)n, ctx->stream) : "";
+    if (e == cudaSuccess && msg.empty())
+        e = cudaMemcpyAsync(out, d + 16 * (size_t)n, 64 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && msg.empty()) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(d);
+    if (!msg.empty()) return fail(ctx, LTS_ERR_CUDA, msg);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "known-answer check");
     return LTS_OK;
 }
 

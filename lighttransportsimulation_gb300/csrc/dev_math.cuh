@@ -46,10 +46,16 @@ __device__ __forceinline__ real xmin(real a, real b) { return fminf(a, b); }
 __device__ __forceinline__ real xmax(real a, real b) { return fmaxf(a, b); }
 __device__ __forceinline__ real xfloor(real a) { return floorf(a); }
 __device__ __forceinline__ real xceil(real a) { return ceilf(a); }
-__device__ __forceinline__ real xcos(real a) { return cosf(a); }
-__device__ __forceinline__ real xsin(real a) { return sinf(a); }
-__device__ __forceinline__ real xacos(real a) { return acosf(a); }
-__device__ __forceinline__ real xlog2(real a) { return log2f(a); }
+// The four transcendentals of the float path.  c_libm_double = 1 (option "libm_double")
+// evaluates them in double and rounds once to float -- the correctly rounded result except when
+// the double result lies within its own last bit of a float rounding boundary -- which is what
+// the reference's host build gets from glibc (or from the double functions it calls on float
+// arguments); 0 (default) uses CUDA's float functions.  The flag is uniform over a launch.
+__constant__ int c_libm_double;
+__device__ __forceinline__ real xcos(real a) { return c_libm_double ? (float)cos((double)a) : cosf(a); }
+__device__ __forceinline__ real xsin(real a) { return c_libm_double ? (float)sin((double)a) : sinf(a); }
+__device__ __forceinline__ real xacos(real a) { return c_libm_double ? (float)acos((double)a) : acosf(a); }
+__device__ __forceinline__ real xlog2(real a) { return c_libm_double ? (float)log2((double)a) : log2f(a); }
 __device__ __forceinline__ real xfma(real a, real b, real c) { return fmaf(a, b, c); }
 __device__ __forceinline__ real xrcp(real a) { return __frcp_rn(a); }     // == (float)(1.0 / (double)a)
 __device__ __forceinline__ real xdiv(real a, real b) { return __fdiv_rn(a, b); }

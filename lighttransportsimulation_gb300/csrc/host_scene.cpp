@@ -580,6 +580,21 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
         float inf_le[3] = {0, 0, 0};
         if (has_inf)
             for (int i = 0; i < 3; ++i) inf_le[i] = tokf(ss, "infinite light Le");
+        // Grammar extension (no counterpart in the reference, whose PointLight, Light.cuh:53-86,
+        // no file can create): after the infinite-light record, the keyword `pointLights`, a
+        // count, and per light `px py pz  Ir Ig Ib` (world-space position, intensity).  The
+        // reference stops reading after the infinite-light record, so it loads such a file
+        // without its point lights; anything else there (platforms/plane.scene keeps a comment
+        // and a material record) is ignored here too.
+        std::vector<float> points;
+        {
+            std::string t;
+            if (ss.next(&t) && t == "pointLights") {
+                const int np = toki(ss, "point light count");
+                if (np < 0) throw ParseError{LTS_ERR_PARSE, "negative point light count"};
+                for (int i = 0; i < 6 * np; ++i) points.push_back(tokf(ss, "point light position / intensity"));
+            }
+        }
         if (area_meshes < 0 || area_meshes > meshes)
             throw ParseError{LTS_ERR_PARSE, "area light mesh count exceeds mesh count"};
         if (mats < meshes)
@@ -679,6 +694,17 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
                 sc->prim_light[L.prim] = (int32_t)sc->lights.size();
                 sc->lights.push_back(L);
             }
+        }
+        // point lights (the extension above) come after the area lights and before the
+        // infinite light: PointLight(LTW, I) at LTW(0, 0, 0) (Light.cuh:60-61)
+        for (size_t k = 0; k + 6 <= points.size(); k += 6) {
+            HostLight L;
+            L.kind = LIGHT_POINT;
+            for (int c = 0; c < 3; ++c) {
+                L.p[c] = points[k + c];
+                L.L[c] = points[k + 3 + c];
+            }
+            sc->lights.push_back(L);
         }
         if (has_inf) {
             HostLight L;

@@ -417,8 +417,11 @@ __global__ __launch_bounds__(128) void k_mlp_train(const uint16_t* __restrict__ 
     if ((threadIdx.x >> 5) == 0) tmem_free(tmem, 512);
 }
 
+// One Adam step, then the inference copy: an exponential moving average of the weights with
+// decay `ema` (0: the weights themselves), kept in FP32 and BF16.
 __global__ void k_adam(float* __restrict__ w, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
-                       uint16_t* __restrict__ w16, int n, float lr, float b1, float b2, float c1, float c2, float eps) {
+                       uint16_t* __restrict__ w16, float* __restrict__ e32, uint16_t* __restrict__ e16, int n, float lr,
+                       float b1, float b2, float c1, float c2, float eps, float ema) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float gi = g[i];
@@ -428,12 +431,20 @@ __global__ void k_adam(float* __restrict__ w, float* __restrict__ g, float* __re
     const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
     w[i] = wi;
     w16[i] = __bfloat16_as_ushort(__float2bfloat16_rn(wi));
+    const float ei = ema > 0.0f ? ema * e32[i] + (1.0f - ema) * wi : wi;
+    e32[i] = ei;
+    e16[i] = __bfloat16_as_ushort(__float2bfloat16_rn(ei));
     g[i] = 0.0f;
 }
 
-__global__ void k_to_bf16(const float* __restrict__ w, uint16_t* __restrict__ w16, int n) {
+__global__ void k_to_bf16(const float* __restrict__ w, uint16_t* __restrict__ w16, float* __restrict__ e32,
+                          uint16_t* __restrict__ e16, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) w16[i] = __bfloat16_as_ushort(__float2bfloat16_rn(w[i]));
+    if (i >= n) return;
+    const uint16_t b = __bfloat16_as_ushort(__float2bfloat16_rn(w[i]));
+    w16[i] = b;
+    e32[i] = w[i];
+    e16[i] = b;
 }
 
 // Check of the bounded mbarrier wait itself: an mbarrier expecting one arrival that never comes.
@@ -487,6 +498,8 @@ Mlp::~Mlp() {
     dev_free(m_);
     dev_free(v_);
     dev_free(w16_);
+    dev_free(e32_);
+    dev_free(e16_);
     dev_free(loss_);
 }
 
@@ -497,6 +510,8 @@ std::string Mlp::init(uint32_t seed, cudaStream_t s) {
         TRY(dev_alloc((void**)&m_, 4 * kMlpParams));
         TRY(dev_alloc((void**)&v_, 4 * kMlpParams));
         TRY(dev_alloc((void**)&w16_, 2 * kMlpParams));
+        TRY(dev_alloc((void**)&e32_, 4 * kMlpParams));
+        TRY(dev_alloc((void**)&e16_, 2 * kMlpParams));
         TRY(dev_alloc((void**)&loss_, 4));
         int dev = 0, sms = 0;
         TRY(cudaGetDevice(&dev));
@@ -525,7 +540,7 @@ std::string Mlp::init(uint32_t seed, cudaStream_t s) {
 }
 
 std::string Mlp::sync_bf16(cudaStream_t s) {
-    k_to_bf16<<<(kMlpParams + 255) / 256, 256, 0, s>>>(w32_, w16_, kMlpParams);
+    k_to_bf16<<<(kMlpParams + 255) / 256, 256, 0, s>>>(w32_, w16_, e32_, e16_, kMlpParams);
     TRY(cudaGetLastError());
     return "";
 }
@@ -563,7 +578,7 @@ std::string Mlp::forward(const uint16_t* d_feat, int n, float* d_out, uint32_t* 
     if (n <= 0) return "";
     const int tiles = (n + 127) / 128;
     const int groups = (tiles + kFwdGroups - 1) / kFwdGroups;
-    k_mlp_forward<<<std::min(groups, blocks_fwd_), 128 * kFwdGroups, kFwdSmem, s>>>(w16_, d_feat, d_rows, n, d_n, d_out,
+    k_mlp_forward<<<std::min(groups, blocks_fwd_), 128 * kFwdGroups, kFwdSmem, s>>>(e16_, d_feat, d_rows, n, d_n, d_out,
                                                                                    out_stride, d_err);
     TRY(cudaGetLastError());
     return "";
@@ -586,7 +601,8 @@ std::string Mlp::adam(float lr, cudaStream_t s) {
     ++steps;
     const float b1 = 0.9f, b2 = 0.99f;
     const float c1 = 1.0f - std::pow(b1, (float)steps), c2 = 1.0f - std::pow(b2, (float)steps);
-    k_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(w32_, grad_, m_, v_, w16_, kMlpParams, lr, b1, b2, c1, c2, 1e-8f);
+    k_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(w32_, grad_, m_, v_, w16_, e32_, e16_, kMlpParams, lr, b1, b2, c1,
+                                                     c2, 1e-8f, ema);
     TRY(cudaGetLastError());
     return "";
 }

@@ -41,6 +41,10 @@ class Mlp {
     std::string set_params(const float* host, cudaStream_t s);  // kMlpParams FP32 values
     std::string get_params(float* host, cudaStream_t s);
 
+    // Inference (forward) uses an exponential moving average of the weights with this decay per
+    // Adam step, training the weights themselves; 0: inference uses the weights.  The average
+    // restarts from the weights at init / set_params.
+    float ema = 0.0f;
     // out[r * out_stride + c] = network(features[r][96])_c for r = rows[i] (rows null: r = i),
     // i < n (device pointers; features are bf16 bits).
     // d_n (device, may be null): the row count to use, at most n (the grid is sized for n).
@@ -62,6 +66,8 @@ class Mlp {
    private:
     float *w32_ = nullptr, *grad_ = nullptr, *m_ = nullptr, *v_ = nullptr, *loss_ = nullptr;
     uint16_t* w16_ = nullptr;
+    float* e32_ = nullptr;  // weight average (inference), FP32 and BF16
+    uint16_t* e16_ = nullptr;
     int blocks_train_ = 0, blocks_fwd_ = 0;
     std::string sync_bf16(cudaStream_t s);
 };

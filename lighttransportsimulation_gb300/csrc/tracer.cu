@@ -122,6 +122,110 @@ __global__ void k_gather_leaves(const float4* __restrict__ prim_v, const float4*
     leaf_v[3 * l + 2] = __ldg(prim_v + 3 * p + 2);
 }
 
+// Known-answer check: one float device function per record (LTS_KAT_* layouts of lts_capi.h).
+__global__ void k_debug_kat(int fn, const float* __restrict__ in, int n, float* __restrict__ out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    float a[16], o[16];
+    for (int k = 0; k < 16; ++k) {
+        a[k] = in[16 * (size_t)r + k];
+        o[k] = 0.0f;
+    }
+    const V3 v0 = v3(a[0], a[1], a[2]), v3_ = v3(a[3], a[4], a[5]);
+    switch (fn) {
+        case LTS_KAT_QUAKE_RSQRT: o[0] = rsqrt_q3(a[0]); break;
+        case LTS_KAT_FRESNEL_DIELECTRIC: o[0] = fresnel_dielectric(a[0], a[1], a[2]); break;
+        case LTS_KAT_FRESNEL_CONDUCTOR: {
+            const Spec F = fresnel_conductor(a[0], Spec{a[1], a[2], a[3]}, Spec{a[4], a[5], a[6]});
+            o[0] = F.r, o[1] = F.g, o[2] = F.b;
+            break;
+        }
+        case LTS_KAT_TR_D: o[0] = tr_d(v0, a[3], a[4]); break;
+        case LTS_KAT_TR_LAMBDA: o[0] = tr_lambda(v0, a[3], a[4]); break;
+        case LTS_KAT_TR_G1: o[0] = tr_g1(v0, a[3], a[4]); break;
+        case LTS_KAT_TR_G: o[0] = tr_g(v0, v3_, a[6], a[7]); break;
+        case LTS_KAT_TR_SAMPLE11: {
+            real sx, sy;
+            tr_sample11(a[0], a[1], a[2], sx, sy);
+            o[0] = sx, o[1] = sy;
+            break;
+        }
+        case LTS_KAT_TR_SAMPLE_WH: {
+            const V3 wh = tr_sample_wh(v0, a[3], a[4], a[5], a[6]);
+            o[0] = wh.x, o[1] = wh.y, o[2] = wh.z;
+            break;
+        }
+        case LTS_KAT_TR_PDF: o[0] = tr_pdf(v0, v3_, a[6], a[7]); break;
+        case LTS_KAT_MF_F:
+        case LTS_KAT_MF_PDF:
+        case LTS_KAT_MF_SAMPLE: {
+            // the conductor lobe of MetalMaterial in its shading frame (identity transform)
+            Bsdf f;
+            f.lobe = LOBE_MICROFACET;
+            f.type = BSDF_REFLECTION | BSDF_GLOSSY;
+            f.ns = f.ng = v3(0, 0, 1);
+            f.ss = v3(1, 0, 0);
+            f.ts = v3(0, 1, 0);
+            f.eta = 1;
+            if (fn == LTS_KAT_MF_SAMPLE) {
+                f.alpha = a[3];
+                f.R = Spec{a[6], a[7], a[8]};
+                f.eta3 = Spec{a[9], a[10], a[11]};
+                f.k = Spec{a[12], a[13], a[14]};
+                V3 wi = v3(0, 0, 0);
+                real pdf = 0;
+                uint32_t st = 0;
+                const Spec v = bsdf_sample(f, v0, wi, F2{a[4], a[5]}, pdf, BSDF_ALL, st, nullptr);
+                o[0] = wi.x, o[1] = wi.y, o[2] = wi.z, o[3] = v.r, o[4] = v.g, o[5] = v.b, o[6] = pdf;
+            } else if (fn == LTS_KAT_MF_F) {
+                f.alpha = a[6];
+                f.R = Spec{a[7], a[8], a[9]};
+                f.eta3 = Spec{a[10], a[11], a[12]};
+                f.k = Spec{a[13], a[14], a[15]};
+                const Spec v = lobe_f(f, v0, v3_);
+                o[0] = v.r, o[1] = v.g, o[2] = v.b;
+            } else {
+                f.alpha = a[6];
+                o[0] = lobe_pdf(f, v0, v3_, nullptr);
+            }
+            break;
+        }
+        case LTS_KAT_PERLIN: o[0] = perlin(a[0], a[1], a[2]); break;
+        case LTS_KAT_FBM:
+        case LTS_KAT_TURBULENCE: {
+            const V3 dx = v3_, dy = v3(a[6], a[7], a[8]);
+            o[0] = fn == LTS_KAT_FBM ? fbm(v0, dx, dy, a[9], (int)a[10], nullptr)
+                                     : turbulence(v0, dx, dy, a[9], (int)a[10], nullptr);
+            break;
+        }
+        case LTS_KAT_OFFSET_ORIGIN: {
+            const V3 po = offset_origin(v0, v3_, v3(a[6], a[7], a[8]), v3(a[9], a[10], a[11]));
+            o[0] = po.x, o[1] = po.y, o[2] = po.z;
+            break;
+        }
+        default: break;
+    }
+    for (int k = 0; k < 16; ++k) out[16 * (size_t)r + k] = o[k];
+}
+
+// Batch ray queries: Scene::intersect (closest hit) or Scene::simpleIntersect (any hit within
+// tMax), one ray per thread, through the renderer's own traversal and triangle tests.
+template <bool ANY>
+__global__ __launch_bounds__(kThreads) void k_intersect(const SceneView sv, int nleaf, const float4* __restrict__ rays,
+                                                        int n, int32_t* __restrict__ prim, float* __restrict__ tout,
+                                                        uint32_t* err) {
+    __shared__ uint32_t s_stack[kStack * kThreads];
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = rays[2 * (size_t)i], b = rays[2 * (size_t)i + 1];
+    const TraceRay r = make_trace_ray(v3(a.x, a.y, a.z), v3(b.x, b.y, b.z));
+    real tmax = a.w, bu = 0, bv = 0, binv = 0;
+    Work wk{0u, 0u};
+    const int h = traverse<ANY>(sv, nleaf, r, tmax, bu, bv, binv, s_stack + threadIdx.x, err, wk);
+    prim[i] = ANY ? (h > 0 ? 1 : 0) : h;
+    if (tout) tout[i] = (!ANY && h >= 0) ? (float)tmax : INFINITY;
+}
+
 }  // namespace
 }  // namespace lts
 
@@ -161,7 +265,35 @@ std::string upload(void*& slot, size_t& cap, const std::vector<T, A>& v, cudaStr
 
 float quake_host(float f) { return quake_rsqrt(f); }
 
+// The procedural textures' tables in this translation unit's device copies (once per process).
+std::string ensure_texture_tables() {
+    static bool consts = false;
+    if (!consts) {
+        unsigned char p2[512];
+        const float* mc = nullptr;
+        texture_tables(p2, &mc);
+        TRY(cudaMemcpyToSymbol(c_perm, p2, 512));
+        TRY(cudaMemcpyToSymbol(c_marble, mc, 30 * sizeof(float)));
+        consts = true;
+    }
+    return "";
+}
+
 }  // namespace
+
+std::string set_libm_double(int on) {
+    const int v = on ? 1 : 0;
+    TRY(cudaMemcpyToSymbol(c_libm_double, &v, sizeof v));
+    return "";
+}
+
+std::string kat_launch(int fn, const float* d_in, int n, float* d_out, cudaStream_t s) {
+    const std::string e = ensure_texture_tables();
+    if (!e.empty()) return e;
+    if (n > 0) k_debug_kat<<<(n + 127) / 128, 128, 0, s>>>(fn, d_in, n, d_out);
+    TRY(cudaGetLastError());
+    return "";
+}
 
 void Tracer::free_all() {
     for (int k = 0; k < kSceneBufs; ++k) {
@@ -250,14 +382,9 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
     leaf_serial_ = 0;
     last_upload_bytes = 0;
     view_ = SceneView{};
-    static bool consts = false;
-    if (!consts) {
-        unsigned char p2[512];
-        const float* mc = nullptr;
-        texture_tables(p2, &mc);
-        TRY(cudaMemcpyToSymbol(c_perm, p2, 512));
-        TRY(cudaMemcpyToSymbol(c_marble, mc, 30 * sizeof(float)));
-        consts = true;
+    {
+        const std::string te = ensure_texture_tables();
+        if (!te.empty()) return te;
     }
     if (!ev0_) {
         TRY(cudaEventCreate(&ev0_));
@@ -350,22 +477,10 @@ std::string Tracer::triangle_soup(float* d_soup, cudaStream_t s) const {
     return "";
 }
 
-std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
-                            uint32_t* d_err, RenderParams* rp, SceneView* sv, long* crop_samples) {
-    if (d.spp < 1 || d.max_bounce < 0) return "bad argument: spp must be >= 1 and max_bounce >= 0";
-    if (d.integrator != LTS_INTEGRATOR_MEGAKERNEL && d.integrator != LTS_INTEGRATOR_WAVEFRONT &&
-        d.integrator != LTS_INTEGRATOR_FP64)
-        return "bad argument: unknown integrator";
-    if (d.integrator == LTS_INTEGRATOR_WAVEFRONT && d.max_bounce < 1)
-        return "bad argument: the wavefront integrator needs max_bounce >= 1";
-    int x0 = d.x0, y0 = d.y0, x1 = d.x1, y1 = d.y1;
-    if (x1 == 0 && y1 == 0) {
-        x0 = y0 = 0;
-        x1 = sc.width;
-        y1 = sc.height;
-    }
-    if (x0 < 0 || y0 < 0 || x1 > sc.width || y1 > sc.height || x0 >= x1 || y0 >= y1) return "bad argument: crop";
-    if (bvh.n != sc.triangles()) return "bad argument: BVH does not match the scene";
+// The scene view with the traversal structures of `bvh`: the leaf-ordered triangles and, with
+// bvh_width 8, the 8-wide compressed BVH collapsed from the binary tree (both kept while the
+// tree is unchanged); the wide tree is used when its depth fits the traversal stack.
+std::string Tracer::traversal_view(const Lbvh& bvh, cudaStream_t s, uint32_t* d_err, SceneView* sv) {
     // leaf-ordered triangles for traversal
     if (leaf_serial_ != bvh.serial || leaf_n_ != bvh.n) {
         dev_free(leaf_v_);
@@ -395,6 +510,52 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
         if (!e.empty()) return e;
     }
     if (use_wide && wide_.levels - 1 > kStack / 2) use_wide = false;
+    *sv = view_;
+    sv->leaf_v = leaf_v_;
+    sv->nodes = bvh.nodes;
+    sv->root_bounds = bvh.root_bounds;
+    sv->wnodes = use_wide ? wide_.nodes : nullptr;
+    sv->wtris = use_wide ? wide_.tris : nullptr;
+    sv->wcount = use_wide ? wide_.count : 0;
+    sv->watertight = watertight;
+    last_wide = use_wide;
+    return "";
+}
+
+std::string Tracer::intersect(const Lbvh& bvh, const float4* d_rays, int n, int any, int32_t* d_prim, float* d_t,
+                              cudaStream_t s, uint32_t* d_err) {
+    if (bvh.n != view_.ntri) return "bad argument: BVH does not match the scene";
+    SceneView sv;
+    const std::string e = traversal_view(bvh, s, d_err, &sv);
+    if (!e.empty()) return e;
+    if (n <= 0) return "";
+    const unsigned grid = (unsigned)((n + kThreads - 1) / kThreads);
+    if (any)
+        k_intersect<true><<<grid, kThreads, 0, s>>>(sv, bvh.n, d_rays, n, d_prim, d_t, d_err);
+    else
+        k_intersect<false><<<grid, kThreads, 0, s>>>(sv, bvh.n, d_rays, n, d_prim, d_t, d_err);
+    TRY(cudaGetLastError());
+    return "";
+}
+
+std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
+                            uint32_t* d_err, RenderParams* rp, SceneView* sv, long* crop_samples) {
+    if (d.spp < 1 || d.max_bounce < 0) return "bad argument: spp must be >= 1 and max_bounce >= 0";
+    if (d.integrator != LTS_INTEGRATOR_MEGAKERNEL && d.integrator != LTS_INTEGRATOR_WAVEFRONT &&
+        d.integrator != LTS_INTEGRATOR_FP64)
+        return "bad argument: unknown integrator";
+    if (d.integrator == LTS_INTEGRATOR_WAVEFRONT && d.max_bounce < 1)
+        return "bad argument: the wavefront integrator needs max_bounce >= 1";
+    int x0 = d.x0, y0 = d.y0, x1 = d.x1, y1 = d.y1;
+    if (x1 == 0 && y1 == 0) {
+        x0 = y0 = 0;
+        x1 = sc.width;
+        y1 = sc.height;
+    }
+    if (x0 < 0 || y0 < 0 || x1 > sc.width || y1 > sc.height || x0 >= x1 || y0 >= y1) return "bad argument: crop";
+    if (bvh.n != sc.triangles()) return "bad argument: BVH does not match the scene";
+    std::string te = traversal_view(bvh, s, d_err, sv);
+    if (!te.empty()) return te;
     const size_t film_bytes = 32 * (size_t)sc.width * sc.height;
     if (film_cap_ < film_bytes) {
         dev_free(film_);
@@ -420,14 +581,6 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
             rec_cap_ = (size_t)ns;
         }
     }
-    *sv = view_;
-    sv->leaf_v = leaf_v_;
-    sv->nodes = bvh.nodes;
-    sv->root_bounds = bvh.root_bounds;
-    sv->wnodes = use_wide ? wide_.nodes : nullptr;
-    sv->wtris = use_wide ? wide_.tris : nullptr;
-    sv->wcount = use_wide ? wide_.count : 0;
-    last_wide = use_wide;
     *rp = RenderParams{};
     rp->spp = d.spp;
     rp->max_bounce = d.max_bounce;

@@ -54,6 +54,7 @@ struct SceneView {
     const WideNode* __restrict__ wnodes;  // 8-wide compressed BVH (null: traverse the binary tree)
     const float4* __restrict__ wtris;     // [3 ntri] triangles in wide-leaf order
     int32_t wcount;                       // wide nodes
+    int32_t watertight;                   // 1: watertight triangle tests (fixed mode), 0: the reference's
     const float* __restrict__ filter;    // 16 x 16 Gaussian table
     float cam[23];
 };
@@ -92,6 +93,13 @@ struct WfView {
 // 10 x 3 marble colours; each translation unit with device textures uploads its own.
 void texture_tables(unsigned char perm512[512], const float** marble30);
 
+// The float renderer's transcendentals (cos, sin, acos, log2): 1 = evaluated in double and
+// rounded once (option "libm_double"), 0 = CUDA's float functions.
+std::string set_libm_double(int on);
+
+// Known-answer check of single float device functions (lts_debug_kat): n records of 16 floats.
+std::string kat_launch(int fn, const float* d_in, int n, float* d_out, cudaStream_t s);
+
 // FP64 oracle renderer (render64.cu): the megakernel integrator in double on the binary LBVH.
 std::string render64_launch(const SceneView& sv, const RenderParams& rp, int nleaf, bool record, cudaStream_t s);
 
@@ -126,6 +134,8 @@ class Tracer {
     long wf_pool = 0;
     // Traversal structure: 8 = the collapsed 8-wide compressed BVH, 2 = the binary LBVH.
     int bvh_width = 8;
+    // Triangle test: 0 = the reference's epsilon-shrunk Moller-Trumbore (parity), 1 = watertight.
+    int watertight = 0;
     // Binary tree the 8-wide BVH is collapsed from, and how: 1 = PLOC over the LBVH's Morton
     // order, SAH-optimal collapse; 2 = the PLOC tree, greedy collapse; 0 = the LBVH itself, greedy.
     int render_bvh = 1;
@@ -161,7 +171,13 @@ class Tracer {
     double last_stage_ms[6] = {0, 0, 0, 0, 0, 0};
     double last_kind_work[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 
+    // Batch ray queries (lts_intersect): rays as n x {o.xyz, tmax, d.xyz, 0} on the device; any = 0
+    // closest hit -> prim (-1: none) and t; any = 1 -> prim 1 (occluded) or 0.
+    std::string intersect(const Lbvh& bvh, const float4* d_rays, int n, int any, int32_t* d_prim, float* d_t,
+                          cudaStream_t s, uint32_t* d_err);
+
    private:
+    std::string traversal_view(const Lbvh& bvh, cudaStream_t s, uint32_t* d_err, SceneView* sv);
     std::string prepare(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                         uint32_t* d_err, RenderParams* rp, SceneView* sv, long* crop_samples);
     void free_all();

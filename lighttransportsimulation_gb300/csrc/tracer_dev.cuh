@@ -184,6 +184,15 @@ __device__ __forceinline__ bool tri_test_shadow(V3 p0, V3 p1, V3 p2, V3 o, V3 d,
     return t > 0 && t < tmax;
 }
 
+// Unfused products and differences (no FMA contraction): the watertight test below needs each
+// 2D edge function to come out exactly negated when the two triangles sharing the edge evaluate
+// it with their vertices in the other order.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ real vcomp(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
 // ------------------------------------------------------------------ surface interaction
 struct SI {
     V3 p, perr, wo, n;  // Interaction
@@ -304,11 +313,69 @@ constexpr int kHitPrimMask = (1 << kHitPrimBits) - 1;
 __device__ __forceinline__ int hit_prim(int best) { return best < 0 ? best : (best & kHitPrimMask); }
 __device__ __forceinline__ int hit_class(int best) { return best < 0 ? 0 : (best >> kHitPrimBits); }
 
+// Watertight ray/triangle test (the fixed mode of the reference's epsilon-shrunk Moller-Trumbore
+// test, whose barycentric margin of 1e-4 lets rays through shared edges): Woop, Benthin and Wald,
+// "Watertight Ray/Triangle Intersection", JCGT 2(1), 2013.  The ray's dominant axis becomes z
+// (x and y swapped when it points down that axis, to keep the winding), the vertices are sheared
+// into ray space, and the signs of the three 2D edge functions decide inside or outside, with an
+// edge function that rounds to zero recomputed in double (exact products).  A ray through a
+// shared edge or vertex of a closed mesh hits one of its triangles.  t in (0, tmax) is tested
+// before the division, on T and det.  u, v: the weights of p1 and p2, as tri_test returns them.
+__device__ __forceinline__ bool tri_test_wt(V3 p0, V3 p1, V3 p2, const TraceRay& r, real tmax, real& t_out,
+                                            real& u_out, real& v_out) {
+    const real ax = xabs(r.d.x), ay = xabs(r.d.y), az = xabs(r.d.z);
+    const int kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1, ky = kx == 2 ? 0 : kx + 1;
+    if (vcomp(r.d, kz) < 0) {
+        const int tmp = kx;
+        kx = ky;
+        ky = tmp;
+    }
+    const real rz = vcomp(r.inv, kz);
+    const real sx = vcomp(r.d, kx) * rz, sy = vcomp(r.d, ky) * rz;
+    const V3 A = p0 - r.o, B = p1 - r.o, C = p2 - r.o;
+    const real Az0 = vcomp(A, kz), Bz0 = vcomp(B, kz), Cz0 = vcomp(C, kz);
+    const real Ax = vcomp(A, kx) - sx * Az0, Ay = vcomp(A, ky) - sy * Az0;
+    const real Bx = vcomp(B, kx) - sx * Bz0, By = vcomp(B, ky) - sy * Bz0;
+    const real Cx = vcomp(C, kx) - sx * Cz0, Cy = vcomp(C, ky) - sy * Cz0;
+    real U = sub_rn(mul_rn(Cx, By), mul_rn(Cy, Bx));
+    real V = sub_rn(mul_rn(Ax, Cy), mul_rn(Ay, Cx));
+    real W = sub_rn(mul_rn(Bx, Ay), mul_rn(By, Ax));
+    if (U == 0 || V == 0 || W == 0) {
+        U = (real)sub_rn(mul_rn((double)Cx, (double)By), mul_rn((double)Cy, (double)Bx));
+        V = (real)sub_rn(mul_rn((double)Ax, (double)Cy), mul_rn((double)Ay, (double)Cx));
+        W = (real)sub_rn(mul_rn((double)Bx, (double)Ay), mul_rn((double)By, (double)Ax));
+    }
+    if ((U < 0 || V < 0 || W < 0) && (U > 0 || V > 0 || W > 0)) return false;
+    const real det = U + V + W;
+    if (det == 0) return false;
+    const real T = U * (rz * Az0) + V * (rz * Bz0) + W * (rz * Cz0);
+    if (det > 0 ? (T <= 0 || T >= tmax * det) : (T >= 0 || T <= tmax * det)) return false;
+    const real rcp = 1 / det;
+    t_out = T * rcp;
+    u_out = V * rcp;
+    v_out = W * rcp;
+    return true;
+}
+// The Moller-Trumbore 1 / det that make_si scales dpdu and dpdv by (the reference's quirk, kept
+// in the watertight mode so that only the hit test differs).
+__device__ __forceinline__ real mt_inv_det(V3 p0, V3 p1, V3 p2, V3 d) { return xrcp(dot(p1 - p0, cross(d, p2 - p0))); }
+
 __device__ __forceinline__ bool leaf_test(const bool any, const float4* __restrict__ tv, int leaf, const TraceRay& r,
-                                          real& tmax, int& best, real& bu, real& bv, real& binv) {
+                                          real& tmax, int& best, real& bu, real& bv, real& binv, const bool wt) {
     const float4 a = __ldg(tv + 3 * leaf), b = __ldg(tv + 3 * leaf + 1), c = __ldg(tv + 3 * leaf + 2);
-    if (any) return tri_test_shadow(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax);
     real t, u, v, inv;
+    if (wt) {
+        if (!tri_test_wt(f4v(a), f4v(b), f4v(c), r, tmax, t, u, v)) return false;
+        if (any) return true;
+        tmax = t;
+        best = __float_as_int(a.w) | (__float_as_int(b.w) << kHitPrimBits);
+        bu = u;
+        bv = v;
+        binv = mt_inv_det(f4v(a), f4v(b), f4v(c), r.d);
+        return false;
+    }
+    if (any) return tri_test_shadow(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax);
     if (tri_test(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax, t, u, v, inv)) {
         tmax = t;
         best = __float_as_int(a.w) | (__float_as_int(b.w) << kHitPrimBits);
@@ -364,7 +431,7 @@ __device__ __forceinline__ bool trav_begin(const bool any, Trav& t, const SceneV
         return false;
     if (nleaf == 1) {
         ++wk.tris;
-        if (leaf_test(any, sv.leaf_v, 0, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) t.best = 1;
+        if (leaf_test(any, sv.leaf_v, 0, t.r, t.tmax, t.best, t.bu, t.bv, t.binv, sv.watertight != 0)) t.best = 1;
         return false;
     }
     return true;
@@ -497,7 +564,7 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
             return true;
         }
         ++wk.tris;
-        if (leaf_test(any, sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+        if (leaf_test(any, sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv, sv.watertight != 0)) {
             t.best = 1;
             return true;
         }
@@ -630,7 +697,7 @@ __device__ __forceinline__ bool wide_leaf_step(const bool any, Trav& t, const Sc
         return true;
     }
     ++wk.tris;
-    if (leaf_test(any, sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+    if (leaf_test(any, sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv, sv.watertight != 0)) {
         t.best = 1;
         return true;
     }
@@ -650,7 +717,7 @@ __device__ __forceinline__ bool trav_step_binary(const bool any, Trav& t, const 
     bool hr = slab(t.r, t.tmax, b.z, b.w, c.x, c.y, c.z, c.w, tr);
     if (hl && lr.x < 0) {
         ++wk.tris;
-        if (leaf_test(any, sv.leaf_v, ~lr.x, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+        if (leaf_test(any, sv.leaf_v, ~lr.x, t.r, t.tmax, t.best, t.bu, t.bv, t.binv, sv.watertight != 0)) {
             t.best = 1;
             return true;
         }
@@ -658,7 +725,7 @@ __device__ __forceinline__ bool trav_step_binary(const bool any, Trav& t, const 
     }
     if (hr && lr.y < 0) {
         ++wk.tris;
-        if (leaf_test(any, sv.leaf_v, ~lr.y, t.r, t.tmax, t.best, t.bu, t.bv, t.binv)) {
+        if (leaf_test(any, sv.leaf_v, ~lr.y, t.r, t.tmax, t.best, t.bu, t.bv, t.binv, sv.watertight != 0)) {
             t.best = 1;
             return true;
         }
@@ -946,6 +1013,13 @@ __device__ void tr_sample11(real cosT, real U1, real U2, real& sx, real& sy) {
     if (cosT >= kOneMinusEpsUp) {
         const real r = xsqrt(U1 / (1 - U1));
         const real phi = mul_dc(U2, LTS_2PI);
+#if !LTS_FP64
+        if (c_libm_double) {  // the reference calls cos / sin in double here and multiplies in double
+            sx = (float)((double)r * cos((double)phi));
+            sy = (float)((double)r * sin((double)phi));
+            return;
+        }
+#endif
         sx = r * xcos(phi);
         sy = r * xsin(phi);
         return;
@@ -983,6 +1057,17 @@ __device__ V3 tr_sample(V3 wi, real ax, real ay, real U1, real U2) {
     sx = ax * sx;
     sy = ay * sy;
     return normalize(v3(-sx, -sy, 1.f));
+}
+
+// TrowbridgeReitzMicrofacetDistribution::sampleWH and ::Pdf (Microfacet.cuh:175-189)
+__device__ __forceinline__ V3 tr_sample_wh(V3 wo, real ax, real ay, real U1, real U2) {
+    const bool flip = wo.z < 0;
+    V3 wh = tr_sample(flip ? -wo : wo, ax, ay, U1, U2);
+    if (flip) wh = -wh;
+    return wh;
+}
+__device__ __forceinline__ real tr_pdf(V3 wo, V3 wh, real ax, real ay) {
+    return tr_d(wh, ax, ay) * tr_g1(wo, ax, ay) * absdot(wo, wh) / xabs(wo.z);
 }
 
 struct Bsdf {
@@ -1043,8 +1128,7 @@ __device__ real lobe_pdf(const Bsdf& f, V3 wo, V3 wi, EvSink* sig) {
         case LOBE_MICROFACET: {
             if (!same_hemi(wo, wi, sig)) return 0;
             const V3 wh = normalize(wo + wi);
-            const real pd = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha, f.alpha) * absdot(wo, wh) / xabs(wo.z);
-            return pd / (4 * dot(wo, wh));
+            return tr_pdf(wo, wh, f.alpha, f.alpha) / (4 * dot(wo, wh));
         }
         default: return 0.0f;
     }
@@ -1124,14 +1208,11 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, real& pdf, uin
         }
         case LOBE_MICROFACET: {  // Microfacet.cuh:211-222
             if (wo.z == 0) return spec(0.0f);
-            const bool flip = wo.z < 0;
-            V3 wh = tr_sample(flip ? -wo : wo, f.alpha, f.alpha, u.x, u.y);
-            if (flip) wh = -wh;
+            const V3 wh = tr_sample_wh(wo, f.alpha, f.alpha, u.x, u.y);
             if (dot(wo, wh) < 0) return spec(0.0f);
             wi = -wo + wh * (2 * dot(wo, wh));
             if (!same_hemi(wo, wi, sig)) return spec(0.0f);
-            const real pd = tr_d(wh, f.alpha, f.alpha) * tr_g1(wo, f.alpha, f.alpha) * absdot(wo, wh) / xabs(wo.z);
-            pdf = pd / (4 * dot(wo, wh));
+            pdf = tr_pdf(wo, wh, f.alpha, f.alpha) / (4 * dot(wo, wh));
             val = lobe_f(f, wo, wi);
             break;
         }
@@ -1220,7 +1301,12 @@ __device__ real area_pdf(const SceneView& sv, const DevLight& L, V3 p, V3 perr, 
     V3 p0, p1, p2;
     prim_tri(sv, L.prim, p0, p1, p2);
     real t, u, v, inv;
-    if (!tri_test(p0, p1, p2, o, wi, INFINITY, t, u, v, inv)) return 0;
+    if (sv.watertight) {
+        if (!tri_test_wt(p0, p1, p2, make_trace_ray(o, wi), INFINITY, t, u, v)) return 0;
+        inv = mt_inv_det(p0, p1, p2, wi);
+    } else if (!tri_test(p0, p1, p2, o, wi, INFINITY, t, u, v, inv)) {
+        return 0;
+    }
     SI is;
     make_si(sv, L.prim, wi, u, v, inv, is);
     const V3 dpt = p - is.p;

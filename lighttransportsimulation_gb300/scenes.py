@@ -236,6 +236,45 @@ def write_box_sphere(d, level=4):
     return "box", "sphere"
 
 
+# Point lights of the point-light scene: world position, intensity (the `pointLights` grammar
+# extension of the loader; the reference has a PointLight but no file syntax for it).
+POINT_LIGHTS = [((-0.6, 0.55, 0.35), (1.6, 1.2, 0.8)), ((0.55, -0.45, 0.5), (0.4, 0.8, 1.6))]
+
+
+def write_point_lights(d, level=3):
+    """The box + icosphere scene lit by the ceiling light, two point lights (POINT_LIGHTS) and a
+    constant infinite light of 0.1 through the open front.  Lights in table order: the two
+    ceiling triangles, the point lights, the infinite light (the reference's NEE never picks the
+    last light, so every point light is sampled)."""
+    os.makedirs(d, exist_ok=True)
+    _box_meshes(d)
+    v, f = icosphere(level)
+    write_bin(os.path.join(d, "sphere.bin"), v * 0.5, v, f, f)
+    text = _box_scene_text()
+    assert text.endswith("0\n")
+    text = text[:-2] + "1\t0.1 0.1 0.1\n" + "pointLights\t%d\n" % len(POINT_LIGHTS) + "".join(
+        "%g %g %g\t%g %g %g\n" % (*p, *i) for p, i in POINT_LIGHTS)
+    with open(os.path.join(d, "points.scene"), "w") as fh:
+        fh.write(text)
+    with open(os.path.join(d, "sphere.subject"), "w") as fh:
+        fh.write("0\n1\tsphere\n1\nL\tc\t0.8 0.8 0.8\t0\n")
+    return "points", "sphere"
+
+
+def with_camera(d, scene, view, name):
+    """Writes d/name.scene: `scene`'s file with its camera line replaced by a view's camera (a dict
+    with frm, at, up, vfov, focus, as lts_render_views takes them), so that lts_render and the FP64
+    renderer draw what that view draws.  Returns name."""
+    with open(os.path.join(d, scene + ".scene")) as fh:
+        lines = fh.read().split("\n")
+    up = view.get("up", (0, 1, 0))
+    lines[0] = "%r %r %r\t%r %r %r\t%r %r %r\t%r\t%r" % (*map(float, view["frm"]), *map(float, view["at"]),
+                                                      *map(float, up), float(view["vfov"]), float(view.get("focus", 1.0)))
+    with open(os.path.join(d, name + ".scene"), "w") as fh:
+        fh.write("\n".join(lines))
+    return name
+
+
 def write_displaced(d, level=8, amplitude=0.1, radius=0.5):
     """Box + level-`level` icosphere displaced by amplitude*fbm(8, 0.5), wrinkled Lambertian."""
     os.makedirs(d, exist_ok=True)

@@ -17,7 +17,7 @@ def build():
     exe = os.path.join(OUT, "lts_port")
     srcs = [os.path.join(HERE, "lts_port.cpp"),
             os.path.join(ROOT, "lighttransportsimulation_gb300", "csrc", "host_scene.cpp")]
-    deps = srcs + [os.path.join(HERE, "lts_rng.h"),
+    deps = srcs + [os.path.join(HERE, "lts_rng.h"), os.path.join(ROOT, "include", "lts_capi.h"),
                    os.path.join(ROOT, "lighttransportsimulation_gb300", "csrc", "host_scene.hpp")]
     if os.path.exists(exe) and all(os.path.getmtime(d) <= os.path.getmtime(exe) for d in deps):
         return exe

@@ -12,6 +12,7 @@
  * CLI (same dump format as oracle/ref/ref_unity.cpp):
  *   lts_port bvh    ROOT SCENE SUBJECT OUT W H [MODE]
  *   lts_port render ROOT SCENE SUBJECT OUT W H SPP MAXB RR SEED X0 Y0 X1 Y1 THREADS FILM [MODE]
+ *   lts_port kat    FN IN OUT   (single functions on raw records, layouts of include/lts_capi.h)
  * MODE 0 (default) is the reference's LBVH (leaf l holds primitive l, Morton codes only below the
  * reference's launch extent), MODE 1 the textbook LBVH (leaf l holds sorted primitive ids[l]).
  */
@@ -28,6 +29,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/lts_capi.h"
 #include "../../lighttransportsimulation_gb300/csrc/host_scene.hpp"
 #include "lts_rng.h"
 
@@ -1217,6 +1219,93 @@ static void dump_bvh(Writer& wr, const Bvh& B) {
     wr.put("node_bounds", 'f', b.data(), b.size(), 4);
 }
 
+/* ---------------------------------------------------------------- known-answer vectors
+ * kat FN IN OUT: the port's own function FN (LTS_KAT_* record layouts of include/lts_capi.h) on
+ * n records of 16 raw float32 inputs, 16 floats out per record.  The distribution's G1, G and
+ * Pdf are the port's isotropic forms: their records carry alphaX == alphaY. */
+static int kat(int fn, const char* in_path, const char* out_path) {
+    FILE* f = fopen(in_path, "rb");
+    if (!f) return 3;
+    std::vector<float> in;
+    float buf[16];
+    while (fread(buf, 4, 16, f) == 16) in.insert(in.end(), buf, buf + 16);
+    fclose(f);
+    const size_t n = in.size() / 16;
+    std::vector<float> out(16 * n, 0.0f);
+    for (size_t r = 0; r < n; ++r) {
+        const float* a = &in[16 * r];
+        float* o = &out[16 * r];
+        const V v0 = mk(a[0], a[1], a[2]), v3 = mk(a[3], a[4], a[5]);
+        Bsdf b;
+        b.lobe = MICRO;
+        b.type = REFL | GLOSSY;
+        b.ns = b.ng = mk(0, 0, 1);
+        b.ss = mk(1, 0, 0);
+        b.ts = mk(0, 1, 0);
+        switch (fn) {
+            case LTS_KAT_QUAKE_RSQRT: o[0] = rsq(a[0]); break;
+            case LTS_KAT_FRESNEL_DIELECTRIC: o[0] = fr_dielectric(a[0], a[1], a[2]); break;
+            case LTS_KAT_FRESNEL_CONDUCTOR: {
+                const S F = fr_conductor(a[0], sp(1.0f), S{a[1], a[2], a[3]}, S{a[4], a[5], a[6]});
+                o[0] = F.r, o[1] = F.g, o[2] = F.b;
+                break;
+            }
+            case LTS_KAT_TR_D: o[0] = tr_d(v0, a[3], a[4]); break;
+            case LTS_KAT_TR_LAMBDA: o[0] = tr_lambda(v0, a[3], a[4]); break;
+            case LTS_KAT_TR_G1: o[0] = tr_g1(v0, a[3]); break;
+            case LTS_KAT_TR_G: o[0] = tr_g(v0, v3, a[6]); break;
+            case LTS_KAT_TR_SAMPLE11: tr_sample11(a[0], a[1], a[2], &o[0], &o[1]); break;
+            case LTS_KAT_TR_SAMPLE_WH: {
+                const bool flip = v0.z < 0;
+                V wh = tr_sample(flip ? -v0 : v0, a[3], a[4], a[5], a[6]);
+                if (flip) wh = -wh;
+                o[0] = wh.x, o[1] = wh.y, o[2] = wh.z;
+                break;
+            }
+            case LTS_KAT_TR_PDF: o[0] = tr_d(v3, a[6], a[6]) * tr_g1(v0, a[6]) * absdot(v0, v3) / fabsf(v0.z); break;
+            case LTS_KAT_MF_F: {
+                b.alpha = a[6];
+                b.R = S{a[7], a[8], a[9]};
+                b.eta3 = S{a[10], a[11], a[12]};
+                b.k = S{a[13], a[14], a[15]};
+                const S v = lobe_f(b, v0, v3);
+                o[0] = v.r, o[1] = v.g, o[2] = v.b;
+                break;
+            }
+            case LTS_KAT_MF_PDF:
+                b.alpha = a[6];
+                o[0] = lobe_pdf(b, v0, v3, nullptr);
+                break;
+            case LTS_KAT_MF_SAMPLE: {
+                b.alpha = a[3];
+                b.R = S{a[6], a[7], a[8]};
+                b.eta3 = S{a[9], a[10], a[11]};
+                b.k = S{a[12], a[13], a[14]};
+                V wi = mk(0, 0, 0);
+                float pdf = 0;
+                uint32_t st = 0;
+                const S v = bsdf_sample(b, v0, &wi, P2{a[4], a[5]}, &pdf, ALL, &st, nullptr);
+                o[0] = wi.x, o[1] = wi.y, o[2] = wi.z, o[3] = v.r, o[4] = v.g, o[5] = v.b, o[6] = pdf;
+                break;
+            }
+            case LTS_KAT_PERLIN: o[0] = perlin(a[0], a[1], a[2]); break;
+            case LTS_KAT_FBM: o[0] = fbm(v0, v3, mk(a[6], a[7], a[8]), a[9], (int)a[10], nullptr); break;
+            case LTS_KAT_TURBULENCE: o[0] = turbulence(v0, v3, mk(a[6], a[7], a[8]), a[9], (int)a[10], nullptr); break;
+            case LTS_KAT_OFFSET_ORIGIN: {
+                const V po = offset_origin(v0, v3, mk(a[6], a[7], a[8]), mk(a[9], a[10], a[11]));
+                o[0] = po.x, o[1] = po.y, o[2] = po.z;
+                break;
+            }
+            default: return 2;
+        }
+    }
+    FILE* g = fopen(out_path, "wb");
+    if (!g) return 3;
+    const bool ok = fwrite(out.data(), 4, out.size(), g) == out.size();
+    fclose(g);
+    return ok ? 0 : 3;
+}
+
 }  // namespace port
 
 int main(int argc, char** argv) {
@@ -1232,6 +1321,7 @@ int main(int argc, char** argv) {
         dump_bvh(wr, sc.bvh);
         return 0;
     }
+    if (cmd == "kat" && argc >= 5) return kat(atoi(argv[2]), argv[3], argv[4]);
     if (cmd == "bvhsoup" && argc >= 5) {  // bvhsoup IN(float32 x 9N raw) OUT MODE [CODE_LIMIT]
         FILE* f = fopen(argv[2], "rb");
         if (!f) return 3;

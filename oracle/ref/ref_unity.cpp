@@ -18,6 +18,11 @@
  *       sample's events (extension hit primitive per bounce, shadow-ray visibility, MIS-ray
  *       hit primitive, texture branch decisions, BSDF grazing tests), the render wall time, and (FILM=1) the resolved film of
  *       Camera::getRender (Camera.cu:256-289).
+ *   lts_ref kat FN IN OUT
+ *       the reference's own single functions (Trowbridge-Reitz distribution and sampling,
+ *       MicrofacetReflection, Fresnel terms, Perlin noise, fbm, turbulence, offsetRayOrigin,
+ *       quakeIIIFastInvSqrt) on raw input records: the known-answer vectors of
+ *       tests/golden/kat_reference.npz (record layouts: LTS_KAT_* in include/lts_capi.h).
  *
  * Build: oracle/ref/build_ref.sh (g++ -E | instrument.pl | g++).  Output: oracle/_ref/lts_ref.
  */
@@ -257,9 +262,102 @@ static int cmd_image(int argc, char** argv) {
     return ok ? 0 : 3;
 }
 
+/* ------------------------------------------------------------------ known-answer vectors
+ * lts_ref kat FN IN OUT: IN holds n records of 16 raw float32 inputs; OUT receives 16 floats per
+ * record, the reference's own function FN (LTS_KAT_* and record layouts of include/lts_capi.h)
+ * evaluated on each. */
+#include "../../include/lts_capi.h"
+
+static int cmd_kat(int argc, char** argv) {
+    if (argc < 5) return 2;
+    const int fn = atoi(argv[2]);
+    FILE* f = fopen(argv[3], "rb");
+    if (!f) return 3;
+    std::vector<float> in;
+    float buf[16];
+    while (fread(buf, 4, 16, f) == 16) in.insert(in.end(), buf, buf + 16);
+    fclose(f);
+    const size_t n = in.size() / 16;
+    std::vector<float> out(16 * n, 0.0f);
+    for (size_t r = 0; r < n; ++r) {
+        const float* a = &in[16 * r];
+        float* o = &out[16 * r];
+        const Vector3f v0(a[0], a[1], a[2]), v3(a[3], a[4], a[5]);
+        switch (fn) {
+            case LTS_KAT_QUAKE_RSQRT: o[0] = quakeIIIFastInvSqrt(a[0]); break;
+            case LTS_KAT_FRESNEL_DIELECTRIC: o[0] = fresnelReflectionDielectric(a[0], a[1], a[2]); break;
+            case LTS_KAT_FRESNEL_CONDUCTOR: {
+                const Spectrum s = fresnelReflectionConductor(a[0], Spectrum(1.0f), Spectrum(a[1], a[2], a[3]),
+                                                              Spectrum(a[4], a[5], a[6]));
+                o[0] = s.r, o[1] = s.g, o[2] = s.b;
+                break;
+            }
+            case LTS_KAT_TR_D: o[0] = TrowbridgeReitzMicrofacetDistribution(a[3], a[4]).d(v0); break;
+            case LTS_KAT_TR_LAMBDA: o[0] = TrowbridgeReitzMicrofacetDistribution(a[3], a[4]).lambda(v0); break;
+            case LTS_KAT_TR_G1: o[0] = TrowbridgeReitzMicrofacetDistribution(a[3], a[4]).g1(v0); break;
+            case LTS_KAT_TR_G: o[0] = TrowbridgeReitzMicrofacetDistribution(a[6], a[7]).g(v0, v3); break;
+            case LTS_KAT_TR_SAMPLE11: TrowbridgeReitzSample11(a[0], a[1], a[2], &o[0], &o[1]); break;
+            case LTS_KAT_TR_SAMPLE_WH: {
+                const Vector3f wh = TrowbridgeReitzMicrofacetDistribution(a[3], a[4]).sampleWH(v0, Point2f(a[5], a[6]));
+                o[0] = wh.x, o[1] = wh.y, o[2] = wh.z;
+                break;
+            }
+            case LTS_KAT_TR_PDF: o[0] = TrowbridgeReitzMicrofacetDistribution(a[6], a[7]).Pdf(v0, v3); break;
+            case LTS_KAT_MF_F:
+            case LTS_KAT_MF_PDF: {
+                Fresnel* fr = fn == LTS_KAT_MF_F ? new FresnelConductor(Spectrum(1.0f), Spectrum(a[10], a[11], a[12]),
+                                                                        Spectrum(a[13], a[14], a[15]))
+                                                 : new FresnelConductor(Spectrum(1.0f), Spectrum(1.0f), Spectrum(1.0f));
+                const Spectrum R = fn == LTS_KAT_MF_F ? Spectrum(a[7], a[8], a[9]) : Spectrum(1.0f);
+                const MicrofacetReflection mr(R, a[6], a[6], fr);
+                if (fn == LTS_KAT_MF_F) {
+                    const Spectrum s = mr.f(v0, v3);
+                    o[0] = s.r, o[1] = s.g, o[2] = s.b;
+                } else {
+                    o[0] = mr.Pdf(v0, v3);
+                }
+                delete fr;
+                break;
+            }
+            case LTS_KAT_MF_SAMPLE: {
+                Fresnel* fr = new FresnelConductor(Spectrum(1.0f), Spectrum(a[9], a[10], a[11]),
+                                                   Spectrum(a[12], a[13], a[14]));
+                const MicrofacetReflection mr(Spectrum(a[6], a[7], a[8]), a[3], a[3], fr);
+                Vector3f wi(0.0f, 0.0f, 0.0f);
+                float pdf = 0.0f;
+                Point2f u(a[4], a[5]);
+                const Spectrum s = mr.sampleF(v0, &wi, u, &pdf);
+                o[0] = wi.x, o[1] = wi.y, o[2] = wi.z, o[3] = s.r, o[4] = s.g, o[5] = s.b, o[6] = pdf;
+                delete fr;
+                break;
+            }
+            case LTS_KAT_PERLIN: o[0] = perlinNoise(a[0], a[1], a[2]); break;
+            case LTS_KAT_FBM:
+            case LTS_KAT_TURBULENCE: {
+                const Point3f p(a[0], a[1], a[2]);
+                const Vector3f dx(a[3], a[4], a[5]), dy(a[6], a[7], a[8]);
+                o[0] = fn == LTS_KAT_FBM ? fbm(p, dx, dy, a[9], (int)a[10]) : turbulence(p, dx, dy, a[9], (int)a[10]);
+                break;
+            }
+            case LTS_KAT_OFFSET_ORIGIN: {
+                const Point3f po = offsetRayOrigin(Point3f(a[0], a[1], a[2]), v3, Normal3f(a[6], a[7], a[8]),
+                                                   Vector3f(a[9], a[10], a[11]));
+                o[0] = po.x, o[1] = po.y, o[2] = po.z;
+                break;
+            }
+            default: return 2;
+        }
+    }
+    FILE* g = fopen(argv[4], "wb");
+    if (!g) return 3;
+    const bool ok = fwrite(out.data(), 4, out.size(), g) == out.size();
+    fclose(g);
+    return ok ? 0 : 3;
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) {
-        fprintf(stderr, "usage: lts_ref bvh|render|image ...\n");
+        fprintf(stderr, "usage: lts_ref bvh|render|image|kat ...\n");
         return 2;
     }
     std::cout.setstate(std::ios_base::failbit); /* silence the loader's banners */
@@ -268,6 +366,7 @@ int main(int argc, char** argv) {
     if (c == "bvh") rc = cmd_bvh(argc, argv);
     if (c == "render") rc = cmd_render(argc, argv);
     if (c == "image") rc = cmd_image(argc, argv);
+    if (c == "kat") rc = cmd_kat(argc, argv);
     if (rc == 2) fprintf(stderr, "bad arguments\n");
     return rc;
 }

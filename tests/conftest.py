@@ -22,6 +22,14 @@ def built_lib():
     return build.build()
 
 
+@pytest.fixture(scope="session")
+def port_exe():
+    """The oracle's CPU port (oracle/_build/lts_port), built on first use."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
+    import build_port
+    return build_port.build()
+
+
 def write_scene(kind, d):
     from lighttransportsimulation_gb300 import scenes
     if kind == "stress_small":  # the stress scene with 16 x 32 spheres (tests/golden/make_golden_port.py)

@@ -171,3 +171,41 @@ def test_failed_load_part_way_keeps_the_scene(built_lib, scene_dirs, tmp_path):
         for k in ("tri", "cam", "func", "cdf"):
             assert np.array_equal(got[k], want[k]), k
     ctx.close()
+
+
+def test_point_light_grammar_extension(built_lib, tmp_path):
+    """`pointLights N  px py pz Ir Ig Ib ...` after the infinite-light record (no counterpart in
+    the reference): the lights table holds the ceiling triangles, then the point lights, then
+    the infinite light; a point light's power is 4 pi I (Light.cuh:83-85), so its entry of the
+    light distribution is the luminance of 4 pi I.  Where the reference build exists, it loads
+    the same file without the point lights, and every other entry matches it bit for bit."""
+    import subprocess
+
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    from oracle import ltsd
+    d = str(tmp_path)
+    sc, sub = scenes.write_point_lights(d)
+    ctx = lts.Context(-1)
+    s = lts.Scene.parse(ctx, d, sc, sub, 64, 64)
+    func, cdf = s.light_distribution()
+    assert s.info["lights"] == 2 + len(scenes.POINT_LIGHTS) + 1 and s.info["has_infinite"] == 1
+    for k, (_, inten) in enumerate(scenes.POINT_LIGHTS):
+        v = np.float32(4 * np.pi)
+        pw = [np.float32(c) * v for c in inten]
+        want = np.float32(0.212671) * pw[0] + np.float32(0.715160) * pw[1] + np.float32(0.072169) * pw[2]
+        assert func[2 + k] == pytest.approx(float(want), rel=1e-6)
+    # a file whose trailing text is not the keyword keeps the reference's reading
+    txt = open(os.path.join(d, sc + ".scene")).read()
+    open(os.path.join(d, "plain.scene"), "w").write(txt[: txt.index("pointLights")] + "// trailing note\n")
+    s2 = lts.Scene.parse(ctx, d, "plain", sub, 64, 64)
+    assert s2.info["lights"] == 3
+    ref = os.path.join(ROOT, "oracle", "_ref", "lts_ref")
+    if os.path.exists(ref):
+        out = str(tmp_path / "b.ltsd")
+        subprocess.run([ref, "bvh", d + "/", sc, sub, out, "64", "64"], check=True)
+        r = ltsd.read(out)
+        keep = np.r_[0:2, 2 + len(scenes.POINT_LIGHTS):len(func)]
+        np.testing.assert_array_equal(r["light_func"], func[keep])
+        np.testing.assert_array_equal(r["light_func"], s2.light_distribution()[0])
+    ctx.close()

@@ -66,12 +66,16 @@ def test_fixtures_reproduce_from_reference(tmp_path):
     for f in os.listdir(GOLDEN):
         if f.endswith(".npz"):
             shutil.copy(os.path.join(GOLDEN, f), tmp_path / f)
-    old = make_golden.OUT
+    import make_golden_kat
+    old, old_kat = make_golden.OUT, make_golden_kat.OUT
     try:
         make_golden.OUT = str(tmp_path)
+        make_golden_kat.OUT = str(tmp_path / "kat_reference.npz")
         make_golden.main()
+        make_golden.make_shipped("/root/reference")
+        make_golden_kat.main()
     finally:
-        make_golden.OUT = old
+        make_golden.OUT, make_golden_kat.OUT = old, old_kat
     for f in os.listdir(GOLDEN):
         if not f.endswith(".npz"):
             continue
@@ -99,3 +103,38 @@ def test_numpy_lbvh_matches_reference_fixture():
         assert np.array_equal(left, fx["node_left"][: n - 1]) and np.array_equal(right, fx["node_right"][: n - 1])
         mn, mx = lbvh_np.tri_bounds(tris)
         lbvh_np.check_tree(fx["node_left"], fx["node_right"], fx["node_bounds"], np.concatenate([mn, mx], 1))
+
+
+def _kat_run(exe, fn, a):
+    import subprocess
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        i, o = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        a.astype(np.float32).tofile(i)
+        subprocess.run([exe, "kat", str(fn), i, o], check=True)
+        return np.fromfile(o, np.float32).reshape(-1, 16)
+
+
+KAT_FUNCS = {"quake_rsqrt": 0, "fresnel_dielectric": 1, "fresnel_conductor": 2, "tr_d": 3, "tr_lambda": 4,
+             "tr_g1": 5, "tr_g": 6, "tr_sample11": 7, "tr_sample_wh": 8, "tr_pdf": 9, "mf_f": 10, "mf_pdf": 11,
+             "mf_sample": 12, "perlin": 13, "fbm": 14, "turbulence": 15, "offset_origin": 16}
+
+
+def kat_compare_mask(name, ref):
+    """Output slots a comparison covers: all 16, except that a rejected microfacet sample
+    (pdf 0) leaves wi unspecified (the reference writes it before rejecting, the others not)."""
+    m = np.ones(ref.shape, bool)
+    if name == "mf_sample":
+        m[ref[:, 6] == 0, 0:3] = False
+    return m
+
+
+@pytest.mark.parametrize("name", list(KAT_FUNCS))
+def test_port_matches_reference_known_answers(port_exe, name):
+    """The port's restatement of each single function against the reference's own function
+    (tests/golden/kat_reference.npz, made by oracle/_ref/lts_ref kat): bit for bit."""
+    z = np.load(os.path.join(GOLDEN, "kat_reference.npz"))
+    ref = z[f"out_{name}"]
+    got = _kat_run(port_exe, KAT_FUNCS[name], z[f"in_{name}"])
+    m = kat_compare_mask(name, ref)
+    assert np.array_equal(got.view(np.uint32)[m], ref.view(np.uint32)[m])

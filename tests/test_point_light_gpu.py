@@ -1,0 +1,47 @@
+"""Point lights (the loader's `pointLights` grammar extension; the reference has PointLight,
+lights/Light.cuh:53-86 and Light.cu:8-26, but no file syntax for it): per-sample parity of the GPU
+renderers against the oracle's CPU port, which restates PointLight::sampleLi and the delta-light
+branch of estimateDirect and is bit-exact to the reference on every scene the reference loads.
+The port runs here, on the same host, on the same scene files.  Tolerances as in
+tests/test_render_gpu.py."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from test_render_gpu import ATOL, MAX_DIVERGENT, RTOL
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("integrator", [0, 1])
+def test_point_lights_match_the_port(built_lib, port_exe, tmp_path, integrator):
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    from oracle import ltsd
+    d = str(tmp_path)
+    sc, sub = scenes.write_point_lights(d)
+    w, h, spp, maxb, rr, seed = 128, 128, 4, 5, 3, 21
+    x0, y0, x1, y1 = 40, 40, 88, 88
+    out = str(tmp_path / "port.ltsd")
+    args = (port_exe, "render", d + "/", sc, sub, out, w, h, spp, maxb, rr, seed, x0, y0, x1, y1, os.cpu_count(), 0, 0)
+    subprocess.run([str(a) for a in args], check=True)
+    ref = ltsd.read(out)
+    ctx = lts.Context(0)
+    try:
+        s = lts.Scene.parse(ctx, d, sc, sub, w, h)
+        assert s.info["lights"] == 2 + len(scenes.POINT_LIGHTS) + 1
+        r = lts.PathTracingIntegrator(maxb, rr, s, integrator=integrator, bvh_mode=lts.BVH_REFERENCE).render(
+            spp, seed, crop=(x0, y0, x1, y1), record=True, film=False)
+    finally:
+        ctx.close()
+    L, Lr = r["L"].reshape(-1, 3), ref["L"].reshape(-1, 3)
+    same = r["sig"].reshape(-1) == ref["sig"].reshape(-1)
+    ok = np.all(np.abs(L - Lr) <= RTOL * np.abs(Lr) + ATOL, axis=1)
+    print(f"integrator {integrator}: divergent {1 - same.mean():.5f}, outside 1e-4 {1 - ok[same].mean():.5f}, "
+          f"mean L {L.mean():.4f} (port {Lr.mean():.4f})")
+    assert np.isfinite(L).all() and Lr.mean() > 0
+    assert 1 - same.mean() <= MAX_DIVERGENT
+    assert 1 - ok[same].mean() <= 0.005
+    assert np.all(np.abs(L - Lr)[same] <= 5e-2 * np.abs(Lr[same]) + 1e-5)

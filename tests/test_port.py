@@ -9,14 +9,6 @@ import pytest
 from conftest import GOLDEN, ROOT
 
 
-@pytest.fixture(scope="session")
-def port_exe():
-    import sys
-    sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
-    import build_port
-    return build_port.build()
-
-
 def _run(exe, *args):
     subprocess.run([exe] + [str(a) for a in args], check=True)
 

@@ -66,3 +66,23 @@ def test_autotuner_picks_a_setting_and_keeps_results(ctx, scene_dirs):
         assert np.allclose(a, b, rtol=1e-5, atol=1e-7)
     for k, v in (("wavefront_pool", 0), ("trace_blocks_per_sm", 0), ("wavefront_graph", 1)):
         ctx.set_option(k, v)
+
+
+def test_batched_view_matches_the_fp64_renderer(ctx, scene_dirs):
+    """A view rendered in a batch (wavefront, FP32) against the FP64 renderer drawing the same
+    samples (a scene file with that view's camera, the view's spp and seed): the films agree to a
+    relative RMSE below 5e-3, the film tolerance of the reference parity tests."""
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    d, sc, sub = scene_dirs["materials"]
+    s = lts.Scene.parse(ctx, d, sc, sub, 64, 64)
+    films, _ = lts.render_views(s, VIEWS, 6, 3)
+    for k in (1, 2):
+        v = VIEWS[k]
+        name = scenes.with_camera(d, sc, v, f"view{k}")
+        sv = lts.Scene.parse(ctx, d, name, sub, v["width"], v["height"])
+        ref = lts.PathTracingIntegrator(6, 3, sv, integrator=lts.INTEGRATOR_FP64).render(v["spp"], v["seed"])["film"]
+        ref = ref.reshape(v["height"], v["width"], 3)
+        err = np.sqrt(np.mean((films[k] - ref) ** 2)) / np.sqrt(np.mean(ref ** 2))
+        print(f"view {k}: {v['width']}x{v['height']} {v['spp']} spp, rel-RMSE against FP64 {err:.3g}")
+        assert err < 5e-3
