@@ -29,7 +29,8 @@ Reported (one JSON line on rank 0):
   cpu_baseline  the oracle's CPU port of the reference integrator (OpenMP, all host cores) on
              a bounded pixel band of the same workload;
   displaced_icosphere  the same figures (value, e2e) for the displaced-icosphere render
-             (1,310,732 triangles, 1024 x 1024, 64 spp, 8 bounces).
+             (1,310,732 triangles, 1024 x 1024, 64 spp, 8 bounces);
+  watertight the same render with the watertight triangle test (option "watertight").
 --impl reference times that CPU port alone, on the same workload and metric.
 Inputs (BVH + triangles, ~400 MB) exceed the 129 MB L2, so no flush runs between steps.
 """
@@ -57,25 +58,31 @@ STRESS = dict(name="stress_glass_conductors", width=1920, height=1080, spp=256, 
               seed=0, level=0)
 
 
-WORKLOADS = {"stress": STRESS, "displaced": WORKLOAD, "small": SMALL}
+# the same scene on a 480x270 film at 64 spp: small cases for profiler captures
+STRESS_SMALL = dict(STRESS, name="stress_glass_conductors_480x270", width=480, height=270, spp=64)
+WORKLOADS = {"stress": STRESS, "displaced": WORKLOAD, "small": SMALL, "stress_small": STRESS_SMALL}
+
+
+def is_stress(wl):
+    return wl["level"] == 0
 
 
 def scene_triangles(wl):
-    return (20 * 4 ** wl["level"] + 12) if wl is not STRESS else 9 * 261120 + 12
+    return (20 * 4 ** wl["level"] + 12) if not is_stress(wl) else 9 * 261120 + 12
 
 
 def scene_dir(wl):
     from lighttransportsimulation_gb300 import scenes
-    d = os.path.join(tempfile.gettempdir(), f"lts_bench_{wl['name']}_{wl['level']}")
+    d = os.path.join(tempfile.gettempdir(), f"lts_bench_{'stress' if is_stress(wl) else wl['name']}_{wl['level']}")
     marker = os.path.join(d, "done")
     if not os.path.exists(marker):
         os.makedirs(d, exist_ok=True)
-        if wl is STRESS:
+        if is_stress(wl):
             scenes.write_stress_scene(d)
         else:
             scenes.write_displaced(d, level=wl["level"])
         open(marker, "w").write("ok")
-    if wl is STRESS:
+    if is_stress(wl):
         return d, "stress", "stress"
     return d, "box", "displaced"
 
@@ -420,6 +427,8 @@ def run_gpu(args, wl):
     peaks, peak_kind = measured_peaks()
     d, sc, sub = scene_dir(wl)
     ctx = lts.Context(local)
+    if args.libm_double is not None:
+        ctx.set_option("libm_double", args.libm_double)
     scene = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
     ctx.set_option("bvh_width", args.bvh_width)
     ctx.set_option("render_bvh", args.render_bvh)
@@ -464,6 +473,22 @@ def run_gpu(args, wl):
         stages = {n: round(mr.render_stage_ms[k], 3) for k, n in enumerate(names)}
         roofline = trace_roofline(mr, peaks, peak_kind, l2_copy_gbs(), sm_mhz, sms)
 
+    # the watertight triangle test (the fixed mode of the reference's test) on the same render:
+    # device Mpaths/s and the trace stage's time
+    watertight = None
+    if args.integrator == 1 and not args.skip_watertight:
+        ctx.set_option("watertight", 1)
+        render_timed(ctx, desc, 1, stream)
+        wt_ms = render_timed(ctx, desc, max(1, min(args.steps, 3)), stream)
+        ctx.set_option("wavefront_graph", 0)
+        integ.render(wl["spp"], wl["seed"], film=False)
+        wt_trace = ctx.metrics().render_stage_ms[1]
+        ctx.set_option("wavefront_graph", 1)
+        ctx.set_option("watertight", 0)
+        watertight = {"value": round(paths / (wt_ms * 1e-3) / 1e6, 3), "unit": "Mpaths/s",
+                      "ms_per_step": round(wt_ms, 3), "trace_ms_per_step": round(wt_trace, 3),
+                      "trace_ms_reference_test": round(mr.render_stage_ms[1], 3)}
+
     # end to end through the public API: parse + upload (H2D), builds, render, film (D2H)
     e2e_s, h2d, d2h = e2e_render(ctx, wl, args.integrator, max(1, min(args.steps, 3)))
     e2e_s = barrier_max(dist, e2e_s)
@@ -500,6 +525,7 @@ def run_gpu(args, wl):
             "traversal": {"node_visits": r["node_visits"], "tri_tests": r["tri_tests"], "rays": r["rays"],
                           "render_bvh_build_ms": render_bvh_ms,
                           "rays_by_kind": {"path": mr.kind_rays[0], "shadow": mr.kind_rays[1], "mis": mr.kind_rays[2]}},
+            "watertight": watertight,
             "time_to_rmse": ttr,
             "lbvh": lbvh,
             "cpu_baseline": cpu,
@@ -732,6 +758,9 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-ttr", action="store_true", help="leave out the time-to-RMSE block")
     ap.add_argument("--skip-displaced", action="store_true", help="leave out the displaced-icosphere figures")
+    ap.add_argument("--skip-watertight", action="store_true", help="leave out the watertight-test render")
+    ap.add_argument("--libm-double", type=int, default=None, choices=[0, 1],
+                    help="set the renderer's libm_double option (float cos/sin/acos/log2 evaluated in double)")
     ap.add_argument("--integrator", type=int, default=1, choices=[0, 1], help="0 megakernel, 1 wavefront")
     ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8],
                     help="traversal structure: 8-wide compressed BVH or the binary LBVH")

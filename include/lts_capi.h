@@ -231,7 +231,7 @@ int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts
  *                             steps on the records.  Needs lts_mlp_init.
  *   "radiance_cache_unbiased_permille" share of full paths (default 30 = 3 %)
  *   "radiance_cache_train_samples"     training records per render (default 65536)
- *   "radiance_cache_train_steps"       Adam steps per render (default 4)
+ *   "radiance_cache_train_steps"       Adam steps per render (default 8)
  *   "radiance_cache_lr_micro"          learning rate in 1e-6 (default 1000 = 1e-3)
  *   "radiance_cache_ema_permille"      the cache's queries use an exponential moving average of the
  *                             weights with this decay per Adam step (per mille; 0: the weights)

@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "liblts_gb300.so")
+APP = os.path.join(LIBDIR, "lts_render_app")  # the C host program (host/render_app.c)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Extra nvcc arguments for tuning builds (e.g. LTS_NVCC_EXTRA="-DLTS_TRACE_MIN_BLOCKS=5"); pass
 # force=True (or delete _lib/obj) when changing them.
@@ -82,6 +83,16 @@ def build(verbose=False, force=False):
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             raise RuntimeError("link failed")
         os.replace(LIB + ".tmp", LIB)
+    app_src = os.path.join(HERE, "host", "render_app.c")
+    if os.path.exists(app_src) and (force or _stale(APP, [app_src, LIB, os.path.join(HERE, "..", "include", "lts_capi.h")])):
+        # the thin C host program over the C-ABI, linked against the library in place
+        cmd = ["gcc", "-O2", "-std=c99", "-Wall", "-o", APP + ".tmp", app_src, "-L" + LIBDIR, "-llts_gb300",
+               "-Wl,-rpath," + LIBDIR]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+            raise RuntimeError("host program link failed")
+        os.replace(APP + ".tmp", APP)
     return LIB
 
 

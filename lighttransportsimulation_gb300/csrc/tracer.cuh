@@ -145,7 +145,7 @@ class Tracer {
     // steps per render and learning rate; statistics of the last render.
     int cache_mode = 0;
     class Mlp* mlp = nullptr;
-    int cache_unbiased_permille = 30, cache_train_cap = 65536, cache_train_steps = 4;
+    int cache_unbiased_permille = 30, cache_train_cap = 65536, cache_train_steps = 8;
     float cache_lr = 1e-3f;
     double last_cache_queries = 0, last_cache_bias = 0;
     int last_train_samples = 0, last_train_eligible = 0;

@@ -209,3 +209,26 @@ def test_point_light_grammar_extension(built_lib, tmp_path):
         np.testing.assert_array_equal(r["light_func"], func[keep])
         np.testing.assert_array_equal(r["light_func"], s2.light_distribution()[0])
     ctx.close()
+
+
+def _app_setup(tmp_path):
+    from lighttransportsimulation_gb300 import build, scenes
+    d = str(tmp_path)
+    sc, sub = scenes.write_box_sphere(d)
+    scenes.write_app_params(os.path.join(d, "app.params"), 64, 48, 4, 5, 3, 1, "out", sc, sub)
+    return d, build.APP
+
+
+def test_host_program_runs_on_a_host_only_context(built_lib, tmp_path):
+    """The thin C host program (host/render_app.c, the reference's main over the C-ABI) compiles,
+    links, reads app.params and parses the scene; with --device -1 its render step reports that it
+    needs a GPU (LTS_ERR_STATE) instead of exiting inside the library."""
+    import subprocess
+    d, app = _app_setup(tmp_path)
+    assert os.path.exists(app)
+    r = subprocess.run([app, d, "--device", "-1"], capture_output=True, text=True)
+    assert r.returncode == 7, r.stderr
+    assert "5132 triangles" in r.stdout and "64x48, 4 spp, 5 bounces" in r.stdout
+    assert "status 7" in r.stderr
+    r = subprocess.run([app, str(tmp_path / "missing")], capture_output=True, text=True)
+    assert r.returncode == 2   # LTS_ERR_IO: no app.params

@@ -2,8 +2,8 @@
 lights/Light.cuh:53-86 and Light.cu:8-26, but no file syntax for it): per-sample parity of the GPU
 renderers against the oracle's CPU port, which restates PointLight::sampleLi and the delta-light
 branch of estimateDirect and is bit-exact to the reference on every scene the reference loads.
-The port runs here, on the same host, on the same scene files.  Tolerances as in
-tests/test_render_gpu.py."""
+The port runs here, on the same host, on the same scene files.  Divergent samples (event hash
+differs) at most 1 % as in tests/test_render_gpu.py; every other sample within 1e-4."""
 import os
 import subprocess
 
@@ -43,5 +43,6 @@ def test_point_lights_match_the_port(built_lib, port_exe, tmp_path, integrator):
           f"mean L {L.mean():.4f} (port {Lr.mean():.4f})")
     assert np.isfinite(L).all() and Lr.mean() > 0
     assert 1 - same.mean() <= MAX_DIVERGENT
-    assert 1 - ok[same].mean() <= 0.005
-    assert np.all(np.abs(L - Lr)[same] <= 5e-2 * np.abs(Lr[same]) + 1e-5)
+    # the port rounds as the reference's host build: on this short-path scene every
+    # non-divergent sample is within the benchmark spec tolerance
+    assert ok[same].all()

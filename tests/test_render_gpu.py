@@ -3,22 +3,23 @@ per-(pixel, sample) radiance, with the shared project sampler.  The stress scene
 conductors cannot be loaded by the reference, so its fixtures come from the oracle port, which
 is bit-exact to the reference on every scene the reference can load.
 
-Tolerance (FP32): a sample whose event hash (hit primitive per bounce, shadow visibility,
-MIS-ray hit, texture branch decisions, the BSDF's reflect/same-hemisphere tests) equals the
-reference's is "non-divergent".  At least 99.5 % of non-divergent samples match to 1e-4 relative
-(plus 1e-6 absolute for near-zero values) and every one of them to 5e-2.  Hash mismatches are
-paths that diverged at a grazing hit or an epsilon-boundary decision; at most 1 % may.
+Rule (float renderers; the library is built without FMA contraction, as the reference's host
+build rounds):
+  * divergent: the sample's event hash (hit primitive per bounce, shadow visibility, MIS-ray hit,
+    texture branch decisions, the BSDF's reflect / same-hemisphere tests) differs from the
+    reference's, or the FP64 renderer's hash for the same sample does: a decision taken at a
+    grazing hit or an epsilon boundary, where exact arithmetic goes the other way.  At most 1 %
+    of the samples may be divergent.
+  * every other sample: |L - L_ref| <= 1e-4 |L_ref| + 1e-6 + 4 |L_fp64 - L_ref| per channel, and no
+    sample may fail (MAX_MISMATCH = 0).  |L_fp64 - L_ref| is the reference's own rounding error on
+    that path, measured against the same path evaluated in double: where the reference's float
+    value is itself that far from the exact value (long mirror, glass and glossy chains amplify the
+    last-bit differences of single operations, including the transcendentals of two libms), a
+    second correct float evaluation differs from it by that much as well.  On paths the reference
+    evaluates accurately the bound is the benchmark spec tolerance, 1e-4.
 
-On the 16-bounce stress scene (glass + rough conductors) the share within 1e-4 is 99.4 %, so
-that scene allows 1 % outside 1e-4 (the same 5e-2 bound on every sample).  The FP64 oracle
-renderer is held to 1e-2 (it does not round like the reference's float code); on the stress scene
-at most 0.1 % of its samples may leave the 5e-2 bound.
-
-Why not 1e-4 for every sample: the GPU rounds with FMA and CUDA's sinf/cosf/log2f, the
-reference's host build without FMA and with glibc's; per-sample traces of the outliers show the
-same event sequence with a relative error that starts near 1e-7 at the first hit and grows along
-mirror, glass and glossy chains (up to ~1e-3 after 8 bounces).  An FMA-free build halves the
-outliers; the rest comes from the libm differences.
+The FP64 renderer itself is held to 1e-2 per sample (it does not round like the reference's
+float code); on the stress scene at most 0.1 % of its samples may leave the 5e-2 bound.
 """
 import os
 
@@ -30,9 +31,10 @@ from conftest import GOLDEN
 pytestmark = pytest.mark.gpu
 
 RTOL, ATOL = 1e-4, 1e-6
-MAX_DIVERGENT = 0.01   # fraction of samples whose event hash differs
-MAX_MISMATCH = 0.005   # fraction of non-divergent samples outside 1e-4
-DRIFT_RTOL = 5e-2      # bound on every non-divergent sample
+MAX_DIVERGENT = 0.01   # fraction of samples flagged divergent
+MAX_MISMATCH = 0       # non-divergent samples outside the bound
+ERR_SCALE = 4.0        # multiple of the reference's own rounding error added to the bound
+DRIFT_RTOL = 5e-2      # bound on every non-divergent sample of the FP64 renderer
 
 
 @pytest.fixture(scope="module")
@@ -43,16 +45,53 @@ def ctx(built_lib):
     c.close()
 
 
+@pytest.fixture(scope="module")
+def fp64_samples(ctx, scene_dirs):
+    """Per-sample radiance and event hashes of the FP64 renderer on each fixture's crop."""
+    import lighttransportsimulation_gb300 as lts
+    cache = {}
+
+    def get(kind):
+        if kind not in cache:
+            d, sc, sub = scene_dirs[kind]
+            fx = np.load(os.path.join(GOLDEN, f"render_{kind}.npz"))
+            w, h, spp, maxb, rr, seed, x0, y0, x1, y1 = (int(v) for v in fx["meta"])
+            s = lts.Scene.parse(ctx, d, sc, sub, w, h)
+            r = lts.PathTracingIntegrator(maxb, rr, s, integrator=lts.INTEGRATOR_FP64).render(
+                spp, seed, crop=(x0, y0, x1, y1), record=True, film=False)
+            cache[kind] = (r["L"].reshape(-1, 3).copy(), r["sig"].reshape(-1).copy())
+        return cache[kind]
+    return get
+
+
+def check_samples(L, sig, Lr, sr, L64, s64, label):
+    """The parity rule of this module over one crop; returns (divergent share, worst excess)."""
+    same = (sig == sr) & (s64 == sr)
+    bound = RTOL * np.abs(Lr) + ATOL + ERR_SCALE * np.abs(L64 - Lr)
+    ok = np.all(np.abs(L - Lr) <= bound, axis=1)
+    bad = np.where(same & ~ok)[0]
+    within = np.all(np.abs(L - Lr) <= RTOL * np.abs(Lr) + ATOL, axis=1)
+    print(f"{label}: samples={len(sig)} divergent={1 - same.mean():.5f} (renderer {np.mean(sig != sr):.5f}, "
+          f"fp64 {np.mean(s64 != sr):.5f}); within 1e-4 {within[same].mean():.6f}; outside the bound {len(bad)}; "
+          f"bit-exact {np.mean(np.all(L.view(np.uint32) == Lr.view(np.uint32), axis=1)):.4f}")
+    for k in bad[:5]:
+        print(f"  sample {k}: L={L[k]} ref={Lr[k]} fp64={L64[k]}")
+    assert np.isfinite(L).all()
+    assert 1.0 - same.mean() <= MAX_DIVERGENT
+    assert len(bad) <= MAX_MISMATCH
+
+
 KINDS = ["box_sphere", "materials", "stress_small", "closeup_diamond", "closeup_moai", "bigbox_diamond"]
 
 
 @pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("bvh_mode,integrator,width", [(0, 0, 2), (0, 1, 8), (1, 0, 8), (1, 1, 8), (1, 1, 2), (1, 2, 2)])
-def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator, width):
+def test_per_sample_radiance(ctx, scene_dirs, fp64_samples, kind, bvh_mode, integrator, width):
     import lighttransportsimulation_gb300 as lts
     d, sc, sub = scene_dirs[kind]
     fx = np.load(os.path.join(GOLDEN, f"render_{kind}.npz"))
     w, h, spp, maxb, rr, seed, x0, y0, x1, y1 = (int(v) for v in fx["meta"])
+    L64, s64 = fp64_samples(kind) if integrator != 2 else (None, None)
     s = lts.Scene.parse(ctx, d, sc, sub, w, h)
     integ = lts.PathTracingIntegrator(maxb, rr, s, integrator=integrator, bvh_mode=bvh_mode)
     ctx.set_option("bvh_width", width)
@@ -64,25 +103,20 @@ def test_per_sample_radiance(ctx, scene_dirs, kind, bvh_mode, integrator, width)
     sig = r["sig"].reshape(-1)
     Lr = fx["L"].reshape(-1, 3)
     sr = fx["sig"].reshape(-1)
+    label = f"{kind} bvh={bvh_mode} integrator={integrator} width={width}"
+    if integrator != 2:
+        check_samples(L, sig, Lr, sr, L64, s64, label)
+        return
+    # the FP64 renderer: same decisions as the reference (<= 1 % divergent), values to 1e-2
     same = sig == sr
-    div = 1.0 - same.mean()
-    # the FP64 oracle renderer evaluates the same samples without the reference's float rounding:
-    # its per-sample values are checked at 1e-2, the float renderers' at 1e-4
-    rtol = RTOL if integrator != 2 else 1e-2
-    ok = np.all(np.abs(L - Lr) <= rtol * np.abs(Lr) + ATOL, axis=1)
-    mism = 1.0 - ok[same].mean()
-    ok4 = np.all(np.abs(L - Lr) <= RTOL * np.abs(Lr) + ATOL, axis=1)
-    print(f"  within 1e-4: {ok4[same].mean():.6f}")
-    print(f"{kind} bvh={bvh_mode} integrator={integrator} width={width}: samples={len(sig)} divergent={div:.5f} mismatched={mism:.6f} "
-          f"maxrel={np.max(np.abs(L - Lr)[same] / (np.abs(Lr[same]) + 1e-6)):.3g}")
+    ok = np.all(np.abs(L - Lr) <= 1e-2 * np.abs(Lr) + ATOL, axis=1)
+    print(f"{label}: samples={len(sig)} divergent={1 - same.mean():.5f} outside 1e-2 {1 - ok[same].mean():.6f}")
     assert np.isfinite(L).all()
-    assert div <= MAX_DIVERGENT
-    assert mism <= (MAX_MISMATCH if kind != "stress_small" else 0.01)
+    assert 1.0 - same.mean() <= MAX_DIVERGENT
+    assert 1.0 - ok[same].mean() <= (0.005 if kind != "stress_small" else 0.01)
     drift = np.all(np.abs(L - Lr) <= DRIFT_RTOL * np.abs(Lr) + 1e-5, axis=1)
     bad = np.where(same & ~drift)[0]
-    for k in bad[:5]:
-        print(f"  drift sample {k}: L={L[k]} ref={Lr[k]}")
-    if integrator == 2 and kind == "stress_small":
+    if kind == "stress_small":
         assert len(bad) <= 0.001 * same.sum()
     else:
         assert drift[same].all()
@@ -111,7 +145,7 @@ def test_film_matches_reference(ctx, scene_dirs, kind, integrator):
 
 def test_wavefront_equals_megakernel_bit_for_bit(ctx, scene_dirs):
     """Same device functions, different schedule: every sample takes the same decisions (identical
-    event hashes); radiance differs only by FMA contraction across kernel boundaries."""
+    event hashes) and, with no multiply-add contracted, the same radiance bit for bit."""
     import lighttransportsimulation_gb300 as lts
     d, sc, sub = scene_dirs["materials"]
     s = lts.Scene.parse(ctx, d, sc, sub, 96, 96)
@@ -121,8 +155,7 @@ def test_wavefront_equals_megakernel_bit_for_bit(ctx, scene_dirs):
     La, Lb = a["L"].reshape(-1, 3), b["L"].reshape(-1, 3)
     ok = np.all(np.abs(La - Lb) <= RTOL * np.abs(La) + ATOL, axis=1)
     print(f"wavefront vs megakernel: bit-equal {np.mean(np.all(La == Lb, axis=1)):.4f}, within 1e-4 {ok.mean():.5f}")
-    assert 1.0 - ok.mean() <= MAX_MISMATCH
-    assert np.all(np.abs(La - Lb) <= DRIFT_RTOL * np.abs(La) + 1e-5)
+    assert np.array_equal(La.view(np.uint32), Lb.view(np.uint32))
 
 
 def test_wavefront_chunked_small_pool(ctx, scene_dirs):
@@ -243,3 +276,24 @@ def test_render_bvh_choice_finds_the_same_hits(ctx, scene_dirs, kind):
         assert same.mean() >= 0.999
         a, b = out[0]["L"].reshape(-1, 3)[same], out[rb]["L"].reshape(-1, 3)[same]
         assert np.all(np.abs(a - b) <= 1e-4 * np.maximum(1.0, np.abs(a)))
+
+
+@pytest.mark.parametrize("integrator", ["megakernel", "wavefront"])
+def test_host_program_writes_the_render(ctx, tmp_path, integrator):
+    """The C host program (host/render_app.c) renders app.params' scene and writes the image the
+    Python API writes for the same render (same film bytes)."""
+    import subprocess
+
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import build, scenes
+    d = str(tmp_path)
+    sc, sub = scenes.write_box_sphere(d)
+    scenes.write_app_params(os.path.join(d, "app.params"), 64, 48, 4, 5, 3, 1, "out", sc, sub)
+    r = subprocess.run([build.APP, d, "--seed", "9", "--integrator", integrator], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    s = lts.Scene.parse(ctx, d, sc, sub, 64, 48)
+    res = lts.PathTracingIntegrator(5, 3, s, integrator={"megakernel": 0, "wavefront": 1}[integrator]).render(4, 9)
+    lts.write_image(os.path.join(d, "py.pfm"), res["film"].reshape(48, 64, 3), 1)
+    a = open(os.path.join(d, "out.pfm"), "rb").read()
+    b = open(os.path.join(d, "py.pfm"), "rb").read()
+    assert a == b

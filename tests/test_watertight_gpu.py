@@ -1,11 +1,11 @@
 """The watertight triangle test (option "watertight", the fixed mode of the reference's
 epsilon-shrunk Moller-Trumbore test) through the ray-query entry point lts_intersect.
 
-Edge leaks: rays from the centre of the closed icosphere (inside the box) aimed exactly at its
-vertices and at the midpoints of its edges.  The reference's test rejects barycentrics within
-1e-4 of a triangle's border, so such rays slip between the triangles and reach the box; the
-watertight test lets none through.  Away from edges both tests hit the same triangle at the same
-distance."""
+Edge leaks: rays from a point near the centre of the closed icosphere (inside the box) aimed
+exactly at its vertices and at the midpoints of its edges.  The reference's test rejects
+barycentrics within 1e-4 of a triangle's border, so such rays slip between the triangles and
+reach the box; the watertight test lets none through.  Away from edges both tests hit the same
+triangle at the same distance."""
 import numpy as np
 import pytest
 
@@ -39,8 +39,13 @@ def _edge_and_vertex_dirs(v, f):
 def test_no_ray_leaks_through_edges_or_vertices(box_scene, width):
     ctx, s, v, f = box_scene
     nsphere = len(f)  # subject meshes come first in scene order
-    dirs = _edge_and_vertex_dirs(v, f)
-    org = np.zeros_like(dirs)
+    # from a point near the centre (not on it: from the centre, rays with a zero direction
+    # component start on the planes of boxes that touch the coordinate planes, where the slab
+    # test's (plane - origin) / d is 0 / 0; that is the box test's degenerate case, not the
+    # triangle test's), through the mesh's vertices and edge midpoints
+    org = np.broadcast_to(np.array([1e-3, 2e-3, -1.5e-3], np.float32), (1, 3))
+    dirs = (_edge_and_vertex_dirs(v, f) - org).astype(np.float32)
+    org = np.repeat(org, len(dirs), axis=0)
     ctx.set_option("bvh_width", width)
     try:
         ctx.set_option("watertight", 0)
@@ -56,7 +61,7 @@ def test_no_ray_leaks_through_edges_or_vertices(box_scene, width):
           f"reference's test, {leak1:.3f} watertight")
     assert leak0 > 0.5      # the reference's test misses most of them
     assert leak1 == 0.0     # the watertight test none
-    assert np.allclose(t1, 0.5, rtol=2e-2)
+    assert np.allclose(t1, 1.0, rtol=1e-4)  # d runs from the origin to the vertex / midpoint: t = 1
 
 
 def test_watertight_equals_reference_away_from_edges(box_scene):
