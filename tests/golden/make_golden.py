@@ -17,6 +17,7 @@ Each fixture records sha256 digests of the scene files it was made from, so a te
 changed generator from a changed renderer.  Usage (from the repository root):
     oracle/ref/build_ref.sh && python tests/golden/make_golden.py
     python tests/golden/make_golden.py shipped /path/to/reference   # the shipped scenes (SHIPPED)
+    python tests/golden/make_golden.py digests                      # the bench scene's digests
 """
 import hashlib
 import os
@@ -137,9 +138,29 @@ def shipped_digest(d):
     return h
 
 
+def make_digests():
+    """digest_displaced.npz: sha256 of every array the reference's loader and LBVH build produce
+    for the displaced-icosphere bench scene (1,310,732 triangles, 1024 x 1024), far too large to
+    store: the world triangles, camera, light distribution, sorted codes / ids, children and node
+    boxes of the reference's own build."""
+    with tempfile.TemporaryDirectory() as td:
+        scenes.write_displaced(td, level=8)
+        digest = np.array([f"{k}:{v}" for k, v in scene_digest(td).items()])
+        b = os.path.join(td, "bvh.ltsd")
+        run(["bvh", td + "/", "box", "displaced", b, 1024, 1024])
+        d = ltsd.read(b)
+        sums = {k: np.array(hashlib.sha256(np.ascontiguousarray(v).tobytes()).hexdigest()) for k, v in d.items()}
+        np.savez_compressed(os.path.join(OUT, "digest_displaced.npz"), scene_digest=digest,
+                            n=np.array(len(d["sorted_codes"])), **sums)
+    print("digest_displaced ok")
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit("oracle/_ref/lts_ref is missing: run oracle/ref/build_ref.sh first")
+    if len(sys.argv) > 1 and sys.argv[1] == "digests":
+        make_digests()
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "shipped":
         make_shipped(sys.argv[2] if len(sys.argv) > 2 else "/root/reference")
         return

@@ -63,3 +63,57 @@ def test_cache_trains_online_and_beats_plain_at_equal_spp(ctx, scene_dirs):
     assert np.mean(losses[-10:]) < np.mean(losses[:5])
     assert abs(np.mean(biases[-10:])) < 0.1
     assert e_cached < e_plain
+
+
+def test_cache_at_config3_settings_beats_plain_wavefront_at_equal_time(ctx, scene_dirs):
+    """The stress scene (glass, rough conductors, marble floor, area + infinite light) at the
+    cached workload's settings: 3 % of paths traced in full, Adam at lr 1e-3, 65,536 training
+    records per frame, 16 bounces, roulette from 4.  Against a 4096-spp plain render: the cached
+    renderer's image bias stays within 5 % and its RMSE is lower than the plain wavefront's after
+    the same device time (both accumulate frames; the cached time includes its warm-up frames,
+    the bias check and the Adam steps)."""
+    import lighttransportsimulation_gb300 as lts
+    d, sc, sub = scene_dirs["stress_small"]
+    W, H = 320, 180
+    s = lts.Scene.parse(ctx, d, sc, sub, W, H)
+    integ = lts.PathTracingIntegrator(16, 4, s, integrator=1)
+    ref = None
+    for k in range(4):
+        ctx.set_option("film_accumulate", 0 if k == 0 else 1)
+        ref = integ.render(1024, 500 + k)["film"].astype(np.float64)
+
+    def accumulate(budget_ms, spp, cached):
+        t, frame, img = 0.0, 0, None
+        if cached:
+            for k in range(8):  # warm-up frames: training only
+                ctx.set_option("film_accumulate", 0)
+                t += integ.render(1, 9000 + k, film=False)["render_ms"]
+        while t < budget_ms:
+            ctx.set_option("film_accumulate", 0 if frame == 0 else 1)
+            r = integ.render(spp, 100 + frame)
+            t += r["render_ms"]
+            frame += 1
+            img = r["film"].astype(np.float64)
+        return img, t, frame
+
+    try:
+        lts.RadianceCacheMLP(ctx, seed=7)
+        ctx.set_option("radiance_cache", 1)
+        for k, v in (("radiance_cache_unbiased_permille", 30), ("radiance_cache_lr_micro", 1000),
+                     ("radiance_cache_train_samples", 65536)):
+            ctx.set_option(k, v)
+        cached, t_cached, n_cached = accumulate(600.0, 4, True)
+        m = ctx.metrics()
+        ctx.set_option("radiance_cache", 0)
+        plain, t_plain, n_plain = accumulate(t_cached, 4, False)
+    finally:
+        ctx.set_option("radiance_cache", 0)
+        ctx.set_option("film_accumulate", 0)
+    bias = (cached.mean() - ref.mean()) / ref.mean()
+    e_plain, e_cached = _rmse(plain, ref), _rmse(cached, ref)
+    print(f"{n_cached} cached frames in {t_cached:.0f} ms, {n_plain} plain frames in {t_plain:.0f} ms; "
+          f"RMSE plain {e_plain:.4f}, cached {e_cached:.4f}; image bias {bias:+.4f}; "
+          f"record bias {m.cache_bias:+.3f}, records {m.cache_train_samples}")
+    assert np.isfinite(cached).all() and m.cache_train_samples > 0
+    assert abs(bias) < 0.05
+    assert e_cached < e_plain

@@ -232,3 +232,29 @@ def test_host_program_runs_on_a_host_only_context(built_lib, tmp_path):
     assert "status 7" in r.stderr
     r = subprocess.run([app, str(tmp_path / "missing")], capture_output=True, text=True)
     assert r.returncode == 2   # LTS_ERR_IO: no app.params
+
+
+def _sha(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_loader_matches_reference_on_the_bench_scene(built_lib, tmp_path):
+    """The displaced-icosphere bench scene (1,310,732 triangles): the loader's world triangles,
+    camera and light distribution have the sha256 digests of the reference's parseScene outputs
+    (tests/golden/digest_displaced.npz, made by oracle/_ref/lts_ref)."""
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    from conftest import scene_digest
+    z = np.load(os.path.join(GOLDEN, "digest_displaced.npz"))
+    d = str(tmp_path)
+    scenes.write_displaced(d, level=8)
+    assert sorted(z["scene_digest"]) == sorted(scene_digest(d)), "scene generator drifted"
+    ctx = lts.Context(-1)
+    s = lts.Scene.parse(ctx, d, "box", "displaced", 1024, 1024)
+    assert s.info["triangles"] == int(z["n"])
+    assert _sha(s.triangles().reshape(-1)) == str(z["tri_p"])
+    assert _sha(s.camera()) == str(z["camera"])
+    func, cdf = s.light_distribution()
+    assert _sha(func) == str(z["light_func"]) and _sha(cdf) == str(z["light_cdf"])
+    ctx.close()

@@ -143,3 +143,20 @@ def test_reference_mode_code_limit(ctx):
     assert np.array_equal(out["sorted_codes"], codes) and np.array_equal(out["sorted_ids"], ids)
     mn, mx = lbvh_np.tri_bounds(tris)
     lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"], np.concatenate([mn, mx], 1))
+
+
+def test_reference_mode_on_the_bench_scene(ctx, tmp_path):
+    """The displaced-icosphere bench scene (1,310,732 triangles) in the reference's mode: codes,
+    order, children and every node box have the sha256 digests of the reference's own build
+    (tests/golden/digest_displaced.npz)."""
+    import hashlib
+
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    z = np.load(os.path.join(GOLDEN, "digest_displaced.npz"))
+    d = str(tmp_path)
+    scenes.write_displaced(d, level=8)
+    s = lts.Scene.parse(ctx, d, "box", "displaced", 1024, 1024)
+    out = s.create_bvh_tree(lts.BVH_REFERENCE)
+    for k in ("sorted_codes", "sorted_ids", "node_key", "node_left", "node_right", "node_bounds"):
+        assert hashlib.sha256(np.ascontiguousarray(out[k]).tobytes()).hexdigest() == str(z[k]), k
