@@ -30,7 +30,10 @@ Reported (one JSON line on rank 0):
              a bounded pixel band of the same workload;
   displaced_icosphere  the same figures (value, e2e) for the displaced-icosphere render
              (1,310,732 triangles, 1024 x 1024, 64 spp, 8 bounces);
-  watertight the same render with the watertight triangle test (option "watertight").
+  watertight the same render with the watertight triangle test (option "watertight");
+  instanced  the stress scene with its conductor spheres as instances of one mesh file, 64 spp:
+             Mpaths/s, render-BVH bytes and build time through the two-level BVH and through one
+             flat tree.
 --impl reference times that CPU port alone, on the same workload and metric.
 Inputs (BVH + triangles, ~400 MB) exceed the 129 MB L2, so no flush runs between steps.
 """
@@ -417,6 +420,46 @@ def displaced_extra(args, ctx):
                     "d2h_bytes_per_step": d2h}}
 
 
+def instanced_extra(args, ctx):
+    """The stress scene with its eight conductor spheres as instances of one 261,120-triangle
+    unit-sphere file (the loader's `instances` record), 1920 x 1080, 64 spp, 16 bounces: device
+    Mpaths/s, render-BVH bytes and build time through the two-level BVH (one tree per prototype
+    under a top level) and through one flat tree over all 2,350,092 triangles."""
+    import torch
+
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    wl = dict(STRESS, spp=64)
+    d = os.path.join(tempfile.gettempdir(), "lts_bench_stress_instanced")
+    marker = os.path.join(d, "done")
+    if not os.path.exists(marker):
+        os.makedirs(d, exist_ok=True)
+        scenes.write_stress_scene(d, instanced=True)
+        open(marker, "w").write("ok")
+    scene = lts.Scene.parse(ctx, d, "stress_inst", "stress_inst", wl["width"], wl["height"])
+    integ = lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], scene, integrator=1)
+    desc = integ.desc(wl["spp"], wl["seed"])
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    paths = wl["width"] * wl["height"] * wl["spp"]
+    out = {"workload": "stress_glass_conductors_instanced", "width": wl["width"], "height": wl["height"],
+           "spp": wl["spp"], "max_bounce": wl["max_bounce"], "rr_start": wl["rr_start"],
+           "triangles": scene.info["triangles"], "instances": scene.info["instances"],
+           "prototypes": scene.info["prototypes"]}
+    try:
+        for tl, key in ((1, "two_level"), (0, "flat")):
+            ctx.set_option("two_level_bvh", tl)
+            render_timed(ctx, desc, 1, stream)  # builds this mode's render BVH
+            m = ctx.metrics()
+            assert m.render_two_level == tl
+            bvh_ms, bvh_bytes = m.render_bvh_ms, m.render_bvh_bytes
+            ms = render_timed(ctx, desc, 2, stream)
+            out[key] = {"value": round(paths / (ms * 1e-3) / 1e6, 3), "unit": "Mpaths/s", "ms_per_step": round(ms, 3),
+                        "render_bvh_bytes": int(bvh_bytes), "render_bvh_build_ms": round(bvh_ms, 3)}
+    finally:
+        ctx.set_option("two_level_bvh", 1)
+    return out
+
+
 def run_gpu(args, wl):
     import ctypes
 
@@ -502,6 +545,7 @@ def run_gpu(args, wl):
     cpu = cpu_port_sample(wl) if (solo and not args.skip_cpu) else None
     ttr = time_to_rmse(args, ctx) if (solo and wl is STRESS and not args.skip_ttr) else None
     extra = displaced_extra(args, ctx) if (solo and wl is STRESS and not args.skip_displaced) else None
+    inst = instanced_extra(args, ctx) if (solo and wl is STRESS and not args.skip_instanced) else None
     if rank == 0:
         line = {
             "metric": "Mpaths/s", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
@@ -530,6 +574,7 @@ def run_gpu(args, wl):
             "lbvh": lbvh,
             "cpu_baseline": cpu,
             "displaced_icosphere": extra,
+            "instanced": inst,
             "clocks": clocks,
             "gpu_launches": int(args.steps) * launches_step,
             "kernel_launches_per_step": launches_step,
@@ -759,6 +804,7 @@ def main():
     ap.add_argument("--skip-ttr", action="store_true", help="leave out the time-to-RMSE block")
     ap.add_argument("--skip-displaced", action="store_true", help="leave out the displaced-icosphere figures")
     ap.add_argument("--skip-watertight", action="store_true", help="leave out the watertight-test render")
+    ap.add_argument("--skip-instanced", action="store_true", help="leave out the instanced stress-scene figures")
     ap.add_argument("--libm-double", type=int, default=None, choices=[0, 1],
                     help="set the renderer's libm_double option (float cos/sin/acos/log2 evaluated in double)")
     ap.add_argument("--integrator", type=int, default=1, choices=[0, 1], help="0 megakernel, 1 wavefront")

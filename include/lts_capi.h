@@ -75,6 +75,7 @@ typedef struct {
     int32_t triangles, meshes, subject_meshes, materials, lights, area_light_meshes, has_infinite;
     int32_t width, height;
     int32_t max_mesh_triangles; /* largest mesh: bounds the reference's Morton launch */
+    int32_t instances, prototypes; /* the `instances` record: instanced mesh entries, their files */
 } lts_scene_info;
 int lts_scene_info_get(lts_ctx* ctx, lts_scene_info* out);
 
@@ -224,8 +225,9 @@ int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts
                        lts_autotune_result* result);
 
 /* Tuning knobs of the renderer (no counterpart in the reference).  Keys:
- *   "radiance_cache"          1: wavefront paths end at the vertex after their first rough vertex
- *                             (roughness > 0.3) with the MLP's radiance there; a share of paths is
+ *   "radiance_cache"          1: wavefront paths end at the first rough vertex (roughness > 0.3)
+ *                             after their first rough vertex, with the MLP's radiance there
+ *                             (specular vertices in between are traced); a share of paths is
  *                             traced in full, supervises the MLP (one record per path at that
  *                             vertex) and measures its bias; after each render the MLP takes Adam
  *                             steps on the records.  Needs lts_mlp_init.
@@ -247,6 +249,11 @@ int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts
  *                             collapsed by the SAH-optimal choice of children; 2 the same tree
  *                             collapsed greedily (largest child opened first); 0 the LBVH itself,
  *                             collapsed greedily
+ *   "two_level_bvh"           scenes with an `instances` record: 1 (default) one 8-wide tree per
+ *                             instanced mesh file (prototype) under a top-level tree over the
+ *                             other triangles, each instance entered with its ray moved to object
+ *                             space; 0 one flat tree over every triangle.  Needs bvh_width 8 and
+ *                             render_bvh 1 or 2; the closest hits are the same up to rounding
  *   "wavefront_pool"          path-state pool capacity in paths (0: automatic -- every path of
  *                             a batch at once, up to 2^26 slots and a quarter of the free
  *                             device memory, ~400 B per slot, ~650 B with the radiance cache)
@@ -387,6 +394,10 @@ typedef struct {
     double render_bvh_ms;
     /* host-to-device bytes copied by the last lts_load_scene (the scene's tables) */
     int64_t scene_upload_bytes;
+    /* device bytes of the nodes, triangles and instance table the last render or ray query
+     * traversed, and 1 when that was the two-level BVH of a scene with instanced meshes */
+    int64_t render_bvh_bytes;
+    int32_t render_two_level;
 } lts_metrics;
 int lts_get_metrics(lts_ctx* ctx, lts_metrics* out);
 

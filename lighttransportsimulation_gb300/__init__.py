@@ -57,7 +57,7 @@ class AppParams(ctypes.Structure):
 class SceneInfo(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in ("triangles", "meshes", "subject_meshes", "materials", "lights",
                                                "area_light_meshes", "has_infinite", "width", "height",
-                                               "max_mesh_triangles")]
+                                               "max_mesh_triangles", "instances", "prototypes")]
 
 
 class BvhDump(ctypes.Structure):
@@ -89,7 +89,8 @@ class Metrics(ctypes.Structure):
                 ("cache_train_loss", ctypes.c_double), ("cache_bias", ctypes.c_double),
                 ("cache_train_ms", ctypes.c_double), ("scene_parse_ms", ctypes.c_double),
                 ("scene_upload_ms", ctypes.c_double), ("render_bvh_ms", ctypes.c_double),
-                ("scene_upload_bytes", ctypes.c_int64)]
+                ("scene_upload_bytes", ctypes.c_int64), ("render_bvh_bytes", ctypes.c_int64),
+                ("render_two_level", ctypes.c_int32)]
 
 
 _lib = None

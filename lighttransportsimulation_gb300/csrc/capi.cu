@@ -314,6 +314,8 @@ int lts_scene_info_get(lts_ctx* ctx, lts_scene_info* out) {
     out->width = s.width;
     out->height = s.height;
     out->max_mesh_triangles = s.max_mesh_triangles();
+    out->instances = (int32_t)s.instances.size();
+    out->prototypes = (int32_t)s.proto_soup.size();
     return LTS_OK;
 }
 
@@ -656,6 +658,9 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
     } else if (!strcmp(key, "render_bvh")) {
         if (value < 0 || value > 2) return fail(ctx, LTS_ERR_ARG, "render_bvh must be 0, 1 or 2");
         ctx->tracer->render_bvh = (int)value;
+    } else if (!strcmp(key, "two_level_bvh")) {
+        if (value > 1) return fail(ctx, LTS_ERR_ARG, "two_level_bvh must be 0 or 1");
+        ctx->tracer->two_level = (int)value;
     } else if (!strcmp(key, "radiance_cache_ema_permille")) {
         if (value > 999) return fail(ctx, LTS_ERR_ARG, "radiance_cache_ema_permille must be 0..999");
         if (!ctx->mlp) return fail(ctx, LTS_ERR_STATE, "no radiance-cache network (lts_mlp_init)");
@@ -762,6 +767,8 @@ int lts_get_metrics(lts_ctx* ctx, lts_metrics* out) {
     out->cache_train_ms = ctx->tracer ? ctx->tracer->last_train_ms : 0.0;
     out->render_bvh_ms = ctx->tracer ? ctx->tracer->last_render_bvh_ms : 0.0;
     out->scene_upload_bytes = ctx->metrics.scene_upload_bytes;
+    out->render_bvh_bytes = ctx->tracer ? (int64_t)ctx->tracer->render_bvh_bytes : 0;
+    out->render_two_level = ctx->tracer && ctx->tracer->last_two_level ? 1 : 0;
     for (int k = 0; k < 3; ++k) {
         out->kind_rays[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k] : 0.0;
         out->kind_node_visits[k] = ctx->tracer ? ctx->tracer->last_kind_work[3 * k + 1] : 0.0;

@@ -384,8 +384,7 @@ HostTexture read_texture(Tokens& s, bool scene_stream, int subject_images) {
         case 'w': t.kind = TEX_WRINKLED; break;
         case 'm': t.kind = TEX_MARBLE; break;
         case 'v': t.kind = TEX_WINDY; break;
-        case 'i':
-            throw ParseError{LTS_ERR_UNSUPPORTED, "image textures ('i') are outside this renderer's scope"};
+        case 'i': t.kind = TEX_IMAGE; break;  // ImageTexture over mipmap v[0], UV mapping (1, 1, 0, 0)
         default:
             throw ParseError{LTS_ERR_UNSUPPORTED, std::string("texture type '") + c + "' is not supported"};
     }
@@ -520,14 +519,23 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
         for (int i = 0; i < 8; ++i) xf[i] = tokf(ss, "subject transform");
         const Xform subject_xf = make_xform({xf[0], xf[1], xf[2]}, {xf[3], xf[4], xf[5]}, xf[6], xf[7]);
 
-        // Images (SceneLoader.cuh:79-97): counted and skipped, never decoded here.
+        // Images (SceneLoader.cuh:79-97): wrap mode clamped to 0..2, file under the root; each
+        // decoded and given its pyramid (image_io.cpp).
         int sub_images = 0, images = 0;
         if (has_subject) images = sub_images = toki(sb, "subject image count");
         images += toki(ss, "scene image count");
+        if (images < 0) throw ParseError{LTS_ERR_PARSE, "negative image count"};
+        sc->images.clear();
+        sc->images.resize((size_t)images);
         for (int i = 0; i < images; ++i) {
             Tokens& s = i >= sub_images ? ss : sb;
-            tok(s, "image wrap");
-            tok(s, "image path");
+            const int wrap = std::min(2, std::max(0, toki(s, "image wrap")));
+            const std::string path = root + tok(s, "image path");
+            int w = 0, h = 0, icode = 0;
+            std::vector<uint8_t> rgb8;
+            const std::string ie = decode_png_file(path, &w, &h, &rgb8, &icode);
+            if (!ie.empty()) throw ParseError{icode, ie};
+            build_pyramid(w, h, rgb8, wrap, &sc->images[(size_t)i]);
         }
         // Meshes (SceneLoader.cuh:99-113).
         int sub_meshes = 0, meshes = 0;
@@ -564,6 +572,9 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
                 default: throw ParseError{LTS_ERR_PARSE, std::string("unknown material type '") + ty + "'"};
             }
             hm.extra = tokf(s, "material extra parameter");
+            for (const HostTexture& t : hm.tex)  // setMatTexture indexes the mipmaps unchecked
+                if (t.kind == TEX_IMAGE && !(t.v[0] >= 0.0f && (int)t.v[0] < images))
+                    throw ParseError{LTS_ERR_PARSE, "image texture index out of range"};
             if (hm.kind == MAT_MATTE && hm.extra != 0) {  // OrenNayar ctor, Microfacet.cuh:18-25
                 const float sigma = (float)((double)hm.extra * (kPi / 180));  // toRadians, GeneralHelper.cuh
                 const float sigma2 = sigma * sigma;
@@ -586,19 +597,73 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
         // reference stops reading after the infinite-light record, so it loads such a file
         // without its point lights; anything else there (platforms/plane.scene keeps a comment
         // and a material record) is ignored here too.
+        // A second extension record, `instances K` and per instance `meshIndex tx ty tz s`: mesh
+        // entry meshIndex (in the global mesh order, subject meshes first) is an instance of its
+        // mesh file, placed at p * s + t (s > 0).  Entries that name the same file share one
+        // prototype; the renderer's 8-wide BVH then holds one bottom-level tree per prototype and
+        // a top level over the instances, instead of every copy's triangles.  Emissive meshes
+        // cannot be instanced.
         std::vector<float> points;
+        std::vector<HostInstance> inst;
         {
             std::string t;
-            if (ss.next(&t) && t == "pointLights") {
-                const int np = toki(ss, "point light count");
-                if (np < 0) throw ParseError{LTS_ERR_PARSE, "negative point light count"};
-                for (int i = 0; i < 6 * np; ++i) points.push_back(tokf(ss, "point light position / intensity"));
+            bool more = ss.next(&t);
+            while (more && (t == "pointLights" || t == "instances")) {
+                if (t == "pointLights") {
+                    const int np = toki(ss, "point light count");
+                    if (np < 0) throw ParseError{LTS_ERR_PARSE, "negative point light count"};
+                    for (int i = 0; i < 6 * np; ++i) points.push_back(tokf(ss, "point light position / intensity"));
+                } else {
+                    const int ni = toki(ss, "instance count");
+                    if (ni < 0) throw ParseError{LTS_ERR_PARSE, "negative instance count"};
+                    for (int i = 0; i < ni; ++i) {
+                        HostInstance h;
+                        h.mesh = toki(ss, "instance mesh index");
+                        for (int c = 0; c < 3; ++c) h.t[c] = tokf(ss, "instance translation");
+                        h.s = tokf(ss, "instance scale");
+                        if (!(h.s > 0.0f)) throw ParseError{LTS_ERR_PARSE, "instance scale must be > 0"};
+                        inst.push_back(h);
+                    }
+                }
+                more = ss.next(&t);
             }
         }
         if (area_meshes < 0 || area_meshes > meshes)
             throw ParseError{LTS_ERR_PARSE, "area light mesh count exceeds mesh count"};
         if (mats < meshes)
             throw ParseError{LTS_ERR_PARSE, "fewer materials than meshes (material index == mesh index)"};
+        // instance of mesh entry m (-1: none); prototypes by mesh file
+        std::vector<int32_t> inst_of(meshes, -1);
+        sc->instances.clear();
+        sc->proto_soup.clear();
+        {
+            std::vector<std::string> proto_files;
+            if (inst.size() > (size_t)kMaxSceneInstances)
+                throw ParseError{LTS_ERR_PARSE, "more than " + std::to_string(kMaxSceneInstances) + " instances"};
+            // the renderer's two-level BVH applies p * s + t alone, so a subject mesh is instanced
+            // only under the identity subject transform (rotation by 0, scale 1, no translation)
+            const bool xf_identity = subject_xf.t.x == 0.0f && subject_xf.t.y == 0.0f && subject_xf.t.z == 0.0f &&
+                                     subject_xf.r.w == 1.0f && subject_xf.r.x == 0.0f && subject_xf.r.y == 0.0f &&
+                                     subject_xf.r.z == 0.0f && subject_xf.s == 1.0f;
+            for (size_t k = 0; k < inst.size(); ++k) {
+                HostInstance h = inst[k];
+                if (h.mesh < 0 || h.mesh >= meshes) throw ParseError{LTS_ERR_PARSE, "instance mesh index out of range"};
+                if (inst_of[h.mesh] >= 0) throw ParseError{LTS_ERR_PARSE, "mesh entry instanced twice"};
+                if (h.mesh >= meshes - area_meshes) throw ParseError{LTS_ERR_PARSE, "an emissive mesh cannot be instanced"};
+                if (h.mesh < sub_meshes && !xf_identity)
+                    throw ParseError{LTS_ERR_PARSE, "an instanced subject mesh needs the identity subject transform"};
+                h.proto = -1;
+                for (size_t q = 0; q < proto_files.size(); ++q)
+                    if (proto_files[q] == files[h.mesh]) h.proto = (int32_t)q;
+                if (h.proto < 0) {
+                    h.proto = (int32_t)proto_files.size();
+                    proto_files.push_back(files[h.mesh]);
+                }
+                inst_of[h.mesh] = (int32_t)sc->instances.size();
+                sc->instances.push_back(h);
+            }
+            sc->proto_soup.resize(proto_files.size());
+        }
 
         // Mesh loading + transforms (SceneLoader.cuh:264-282, shapes/Triangle.cu:20-43).
         // Every mesh is read (and checked) first, so each table is sized once; each mesh then
@@ -631,13 +696,23 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
             const Xform& X = m >= sub_meshes ? ident : subject_xf;
             const float *mp = md.P(), *mn = md.N(), *muv = md.UV();
             const int32_t* mi = md.I();
+            const HostInstance* hi = inst_of[m] >= 0 ? &sc->instances[inst_of[m]] : nullptr;
             parallel_ranges((size_t)md.np, [&](size_t b, size_t e) {
                 for (size_t i = b; i < e; ++i) {
-                    const V3 w = X.point({mp[3 * i], mp[3 * i + 1], mp[3 * i + 2]});
+                    V3 q{mp[3 * i], mp[3 * i + 1], mp[3 * i + 2]};
+                    if (hi) q = V3{q.x * hi->s + hi->t[0], q.y * hi->s + hi->t[1], q.z * hi->s + hi->t[2]};
+                    const V3 w = X.point(q);
                     float* o = &sc->p[3 * (pbase + i)];
                     o[0] = w.x; o[1] = w.y; o[2] = w.z;
                 }
             });
+            if (hi && sc->proto_soup[hi->proto].empty()) {  // the prototype's object-space triangles
+                std::vector<float>& soup = sc->proto_soup[hi->proto];
+                soup.resize(9 * (size_t)md.ntri);
+                for (int32_t t = 0; t < md.ntri; ++t)
+                    for (int c = 0; c < 3; ++c)
+                        for (int k = 0; k < 3; ++k) soup[9 * (size_t)t + 3 * c + k] = mp[3 * (size_t)mi[9 * t + 3 * c] + k];
+            }
             parallel_ranges((size_t)md.nn, [&](size_t b, size_t e) {
                 for (size_t i = b; i < e; ++i) {
                     const V3 w = X.normal({mn[3 * i], mn[3 * i + 1], mn[3 * i + 2]});

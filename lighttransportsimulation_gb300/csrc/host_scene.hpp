@@ -11,6 +11,8 @@
 #include <utility>
 #include <vector>
 
+#include "image_io.hpp"
+
 namespace lts {
 
 // Allocator whose resize leaves new elements uninitialised (default-initialised) instead of
@@ -38,7 +40,7 @@ struct NoInitAlloc : std::allocator<T> {
 template <class T>
 using HostVec = std::vector<T, NoInitAlloc<T>>;
 
-enum TexKind : int32_t { TEX_CONSTANT = 0, TEX_FBM = 1, TEX_WRINKLED = 2, TEX_MARBLE = 3, TEX_WINDY = 4 };
+enum TexKind : int32_t { TEX_CONSTANT = 0, TEX_FBM = 1, TEX_WRINKLED = 2, TEX_MARBLE = 3, TEX_WINDY = 4, TEX_IMAGE = 5 };
 enum MatKind : int32_t {
     MAT_NONE = 0,   // 'M' in the reference: parsed, no material constructed -> no BSDF
     MAT_MATTE = 1,  // 'L' MatteMaterial (Material.cuh:31-55)
@@ -50,7 +52,7 @@ enum LightKind : int32_t { LIGHT_AREA = 0, LIGHT_INFINITE = 1, LIGHT_POINT = 2 }
 
 struct HostTexture {
     int32_t kind = TEX_CONSTANT;
-    float v[4] = {0, 0, 0, 0};  // constant rgb | octaves, omega | octaves, omega, scale, variation
+    float v[4] = {0, 0, 0, 0};  // constant rgb | octaves, omega | octaves, omega, scale, variation | image
 };
 
 struct HostMaterial {
@@ -67,6 +69,17 @@ struct HostLight {
     float p[3] = {0, 0, 0};     // point light position; infinite light world center
     float radius = 0;           // infinite light world radius
     float area = 0;             // area light triangle area
+};
+
+// An instanced mesh entry (the loader's `instances` grammar extension): mesh entry `mesh`
+// places its file's triangles at p * s + t (before the subject transform, for subject meshes).
+// Entries with the same mesh file share prototype `proto`, whose object-space triangles are
+// HostScene::proto_soup[proto].
+constexpr int kMaxSceneInstances = 32;  // instances one scene may hold (bits of a traversal mask)
+struct HostInstance {
+    int32_t mesh = 0, proto = 0;
+    float t[3] = {0, 0, 0};
+    float s = 1;
 };
 
 struct HostScene {
@@ -95,6 +108,15 @@ struct HostScene {
     std::vector<HostLight> lights;        // sampling order of the reference's light array
     std::vector<float> light_func, light_cdf;  // Distribution1D over power().y()
     float light_func_int = 0;                  // Distribution1D::funcInt (before normalising)
+
+    // Instanced mesh entries and their prototypes' object-space triangles (9 floats each, in
+    // the mesh file's order); empty when the scene has no `instances` record.
+    std::vector<HostInstance> instances;
+    std::vector<std::vector<float>> proto_soup;
+
+    // Image textures in the reference's image order (subject images first), each with its mip
+    // pyramid (the fixed mode of ImageTexture / Mipmap).
+    std::vector<HostImage> images;
 
     int32_t triangles() const { return (int32_t)tri_mesh.size(); }
     int32_t max_mesh_triangles() const;

@@ -32,6 +32,8 @@ std::string render64_launch(const SceneView& sv, const RenderParams& rp, int nle
     SceneView v = sv;
     v.wnodes = nullptr;  // binary traversal in double
     v.wtris = nullptr;
+    v.inst = nullptr;  // the flat binary tree holds every instance's triangles
+    v.ninst = 0;
     const dim3 block(kBX, kBY);
     dim3 grid((rp.x1 - rp.x0 + kBX - 1) / kBX, (rp.y1 - rp.y0 + kBY - 1) / kBY);
     // one block per pixel tile leaves most SMs idle on the small high-spp crops this renderer

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -106,13 +107,14 @@ __global__ void k_build_prim_rec(const float4* __restrict__ prim_v, const int32_
 }
 
 // Leaf-ordered triangles: w of the first vertex = primitive id, w of the second = the shade
-// class of its material (what a closest hit records, see hit_prim / hit_class).
+// class of its material (what a closest hit records, see hit_prim / hit_class).  With `ids` the
+// tree was built over the scene triangles ids[0 .. n-1] and leaf_prim indexes that list.
 __global__ void k_gather_leaves(const float4* __restrict__ prim_v, const float4* __restrict__ prim_rec,
                                 const DevMat* __restrict__ mats, const int32_t* __restrict__ leaf_prim, int n,
-                                float4* __restrict__ leaf_v) {
+                                float4* __restrict__ leaf_v, const int32_t* __restrict__ ids = nullptr) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= n) return;
-    const int p = __ldg(leaf_prim + l);
+    const int p = ids ? __ldg(ids + __ldg(leaf_prim + l)) : __ldg(leaf_prim + l);
     float4 a = __ldg(prim_v + 3 * p), b = __ldg(prim_v + 3 * p + 1);
     a.w = __int_as_float(p);
     const int mesh = __float_as_int(__ldg(prim_rec + 8 * (size_t)p + 6).y);
@@ -120,6 +122,42 @@ __global__ void k_gather_leaves(const float4* __restrict__ prim_v, const float4*
     leaf_v[3 * l] = a;
     leaf_v[3 * l + 1] = b;
     leaf_v[3 * l + 2] = __ldg(prim_v + 3 * p + 2);
+}
+
+// The scene triangles ids[0 .. n-1] as 9 floats each (the top-level tree's LBVH input).
+__global__ void k_soup_subset(const float4* __restrict__ prim_v, const int32_t* __restrict__ ids, int n,
+                              float* __restrict__ soup) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int p = __ldg(ids + t);
+    for (int c = 0; c < 3; ++c) {
+        const float4 q = __ldg(prim_v + 3 * (size_t)p + c);
+        soup[9 * (size_t)t + 3 * c] = q.x;
+        soup[9 * (size_t)t + 3 * c + 1] = q.y;
+        soup[9 * (size_t)t + 3 * c + 2] = q.z;
+    }
+}
+// Leaf-ordered triangles of a prototype's tree from its object-space soup: w of the first vertex
+// = the triangle's index in the prototype (the instance adds its first primitive and its class).
+__global__ void k_gather_soup_leaves(const float* __restrict__ soup, const int32_t* __restrict__ leaf_prim, int n,
+                                     float4* __restrict__ leaf_v) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= n) return;
+    const int p = __ldg(leaf_prim + l);
+    const float* q = soup + 9 * (size_t)p;
+    leaf_v[3 * (size_t)l] = make_float4(q[0], q[1], q[2], __int_as_float(p));
+    leaf_v[3 * (size_t)l + 1] = make_float4(q[3], q[4], q[5], 0.f);
+    leaf_v[3 * (size_t)l + 2] = make_float4(q[6], q[7], q[8], 0.f);
+}
+// One tree's wide nodes into the concatenated array: child and triangle indices rebased.
+__global__ void k_rebase_wide(const WideNode* __restrict__ src, int count, uint32_t node_base, uint32_t tri_base,
+                              WideNode* __restrict__ dst) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    WideNode w = src[k];
+    w.m.x += node_base;
+    w.m.y += tri_base;
+    dst[k] = w;
 }
 
 // Known-answer check: one float device function per record (LTS_KAT_* layouts of lts_capi.h).
@@ -221,7 +259,8 @@ __global__ __launch_bounds__(kThreads) void k_intersect(const SceneView sv, int 
     const TraceRay r = make_trace_ray(v3(a.x, a.y, a.z), v3(b.x, b.y, b.z));
     real tmax = a.w, bu = 0, bv = 0, binv = 0;
     Work wk{0u, 0u};
-    const int h = traverse<ANY>(sv, nleaf, r, tmax, bu, bv, binv, s_stack + threadIdx.x, err, wk);
+    const int h = sv.ninst ? traverse<ANY, true>(sv, nleaf, r, tmax, bu, bv, binv, s_stack + threadIdx.x, err, wk)
+                           : traverse<ANY>(sv, nleaf, r, tmax, bu, bv, binv, s_stack + threadIdx.x, err, wk);
     prim[i] = ANY ? (h > 0 ? 1 : 0) : h;
     if (tout) tout[i] = (!ANY && h >= 0) ? (float)tmax : INFINITY;
 }
@@ -295,7 +334,31 @@ std::string kat_launch(int fn, const float* d_in, int n, float* d_out, cudaStrea
     return "";
 }
 
+void Tracer::release_instanced() {
+    for (void* p : {(void*)proto_soup_d_, (void*)world_ids_d_, (void*)isoup_, (void*)ileaf_, (void*)inodes_,
+                    (void*)itris_, (void*)dinst_, (void*)iroot_})
+        dev_free(p);
+    proto_soup_d_ = nullptr;
+    world_ids_d_ = nullptr;
+    isoup_ = nullptr;
+    ileaf_ = nullptr;
+    inodes_ = nullptr;
+    itris_ = nullptr;
+    dinst_ = nullptr;
+    iroot_ = nullptr;
+    isoup_cap_ = ileaf_cap_ = inodes_cap_ = itris_cap_ = 0;
+    inst_host_.clear();
+    proto_off_.clear();
+    proto_n_.clear();
+    proto_box_.clear();
+    world_n_ = 0;
+    icount_ = itri_n_ = ilevels_ = 0;
+    ikey_ = 0;
+    two_level_ok_ = 0;
+}
+
 void Tracer::free_all() {
+    release_instanced();
     for (int k = 0; k < kSceneBufs; ++k) {
         if (bufs_[k]) dev_free(bufs_[k]);
         bufs_[k] = nullptr;
@@ -363,6 +426,7 @@ Tracer::~Tracer() {
 }
 
 void Tracer::drop_scene() {
+    release_instanced();
     for (int k = 0; k < kSceneBufs; ++k) {
         if (bufs_[k]) dev_free(bufs_[k]);
         bufs_[k] = nullptr;
@@ -442,6 +506,42 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
     if (!(e = upload(bufs_[8], bufcap_[8], sc.light_func, s, &last_upload_bytes)).empty()) return e;
     if (!(e = upload(bufs_[9], bufcap_[9], sc.light_cdf, s, &last_upload_bytes)).empty()) return e;
     if (!(e = upload(bufs_[10], bufcap_[10], filt, s, &last_upload_bytes)).empty()) return e;
+    {  // image-texture pyramids in 4 x 4 texel blocks
+        std::vector<DevImage> di(sc.images.size());
+        size_t total = 0;
+        for (size_t i = 0; i < sc.images.size(); ++i) {
+            const HostImage& h = sc.images[i];
+            if (h.levels > kImageLevels) return "bad argument: image too large";
+            DevImage& d = di[i];
+            memset(&d, 0, sizeof d);
+            d.levels = h.levels;
+            d.wrap = h.wrap;
+            d.lod = h.lod;
+            for (int l = 0; l < h.levels; ++l) {
+                d.off[l] = (int32_t)total;
+                d.w[l] = h.w[l];
+                d.h[l] = h.h[l];
+                total += 16 * (size_t)((h.w[l] + 3) / 4) * (size_t)((h.h[l] + 3) / 4);
+            }
+            if (total > (size_t)INT32_MAX) return "bad argument: images too large";
+        }
+        std::vector<float4> tex(total, make_float4(0.f, 0.f, 0.f, 0.f));
+        for (size_t i = 0; i < sc.images.size(); ++i) {
+            const HostImage& h = sc.images[i];
+            for (int l = 0; l < h.levels; ++l) {
+                const int w = h.w[l], bw = (w + 3) / 4;
+                const float* src = h.rgb[l].data();
+                for (int v = 0; v < h.h[l]; ++v)
+                    for (int u = 0; u < w; ++u) {
+                        const float* q = src + 3 * ((size_t)v * w + u);
+                        tex[(size_t)di[i].off[l] + 16 * ((size_t)(v >> 2) * bw + (u >> 2)) + 4 * (v & 3) + (u & 3)] =
+                                make_float4(q[0], q[1], q[2], 0.f);
+                    }
+            }
+        }
+        if (!(e = upload(bufs_[15], bufcap_[15], tex, s, &last_upload_bytes)).empty()) return e;
+        if (!(e = upload(bufs_[16], bufcap_[16], di, s, &last_upload_bytes)).empty()) return e;
+    }
     if (!(e = reserve_buf(bufs_[0], bufcap_[0], 48 * (size_t)nt)).empty()) return e;
     if (!(e = reserve_buf(bufs_[1], bufcap_[1], 128 * (size_t)nt)).empty()) return e;
     if (nt > 0) {
@@ -466,7 +566,169 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
     view_.light_cdf = (const float*)bufs_[9];
     view_.light_func_int = sc.light_func_int;
     view_.filter = (const float*)bufs_[10];
+    view_.img_texels = (const float4*)bufs_[15];
+    view_.images = (const DevImage*)bufs_[16];
     memcpy(view_.cam, sc.cam, sizeof sc.cam);
+    return capture_instances(sc, mats, s);
+}
+
+// The two-level BVH's inputs: each instance's placement, first primitive and shade class, the
+// prototypes' object-space triangles and boxes, and the ids and bounds of the triangles of the
+// other meshes.  The trees are built on first use (build_instanced).
+std::string Tracer::capture_instances(const HostScene& sc, const std::vector<DevMat>& mats, cudaStream_t s) {
+    release_instanced();
+    ++upload_serial_;
+    if (sc.instances.empty()) return "";
+    static_assert(kMaxInstances == kMaxSceneInstances, "instance limits of the loader and the traversal agree");
+    if (sc.instances.size() > (size_t)kMaxInstances) return "bad argument: too many instances";
+    const int nt = sc.triangles();
+    std::vector<char> instanced(sc.mesh_first_tri.size(), 0);
+    for (const HostInstance& h : sc.instances) {
+        InstHost ih;
+        ih.mesh = h.mesh;
+        ih.proto = h.proto;
+        ih.prim_first = sc.mesh_first_tri[h.mesh];
+        ih.ntri = sc.mesh_tri_count[h.mesh];
+        ih.cls = mats[h.mesh].shade_class;
+        for (int c = 0; c < 3; ++c) ih.t[c] = h.t[c];
+        ih.s = h.s;
+        if (ih.ntri * 9 != (int)sc.proto_soup[h.proto].size()) return "bad argument: instance and prototype differ";
+        inst_host_.push_back(ih);
+        instanced[h.mesh] = 1;
+    }
+    std::vector<float> all;
+    for (const std::vector<float>& soup : sc.proto_soup) {
+        proto_off_.push_back(all.size() / 9);
+        proto_n_.push_back((int)(soup.size() / 9));
+        float b[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        for (size_t k = 0; k < soup.size(); ++k) {
+            b[k % 3] = std::min(b[k % 3], soup[k]);
+            b[3 + k % 3] = std::max(b[3 + k % 3], soup[k]);
+        }
+        proto_box_.insert(proto_box_.end(), b, b + 6);
+        all.insert(all.end(), soup.begin(), soup.end());
+    }
+    std::vector<int32_t> ids;
+    for (float& v : world_box_) v = 0;
+    float* wb = world_box_;
+    wb[0] = wb[1] = wb[2] = INFINITY;
+    wb[3] = wb[4] = wb[5] = -INFINITY;
+    for (int t = 0; t < nt; ++t) {
+        if (instanced[sc.tri_mesh[t]]) continue;
+        ids.push_back(t);
+        for (int c = 0; c < 3; ++c)
+            for (int a = 0; a < 3; ++a) {
+                const float v = sc.p[3 * (size_t)sc.tri_p[3 * (size_t)t + c] + a];
+                wb[a] = std::min(wb[a], v);
+                wb[3 + a] = std::max(wb[3 + a], v);
+            }
+    }
+    world_n_ = (int)ids.size();
+    two_level_ok_ = world_n_ >= 2;
+    for (int n : proto_n_) two_level_ok_ = two_level_ok_ && n >= 2;
+    if (!two_level_ok_) return "";  // rendered through the flat tree
+    void* p = nullptr;
+    size_t cap = 0;
+    std::string e = upload(p, cap, all, s, &last_upload_bytes);
+    proto_soup_d_ = (float*)p;
+    if (!e.empty()) return e;
+    p = nullptr;
+    cap = 0;
+    e = upload(p, cap, ids, s, &last_upload_bytes);
+    world_ids_d_ = (int32_t*)p;
+    return e;
+}
+
+std::string Tracer::build_instanced(uint64_t key, cudaStream_t s, uint32_t* d_err) {
+    ikey_ = 0;
+    const int np = (int)proto_n_.size(), ni = (int)inst_host_.size();
+    size_t tot_tris = (size_t)world_n_, tot_nodes = (size_t)world_n_ - 1, max_n = (size_t)world_n_;
+    for (int n : proto_n_) {
+        tot_tris += (size_t)n;
+        tot_nodes += (size_t)n - 1;
+        max_n = std::max(max_n, (size_t)n);
+    }
+    std::string e;
+    void* p;
+    p = isoup_;
+    if (!(e = reserve_buf(p, isoup_cap_, 36 * max_n)).empty()) return e;
+    isoup_ = (float*)p;
+    p = ileaf_;
+    if (!(e = reserve_buf(p, ileaf_cap_, 48 * max_n)).empty()) return e;
+    ileaf_ = (float4*)p;
+    p = inodes_;
+    if (!(e = reserve_buf(p, inodes_cap_, sizeof(WideNode) * tot_nodes)).empty()) return e;
+    inodes_ = (WideNode*)p;
+    p = itris_;
+    if (!(e = reserve_buf(p, itris_cap_, 48 * tot_tris)).empty()) return e;
+    itris_ = (float4*)p;
+    if (!dinst_) TRY(dev_alloc((void**)&dinst_, sizeof(DevInstance) * kMaxInstances));
+    if (!iroot_) TRY(dev_alloc((void**)&iroot_, 6 * sizeof(float)));
+    const auto t0 = std::chrono::steady_clock::now();
+    uint32_t node_base = 0, tri_base = 0;
+    int levels = 0;
+    std::vector<int> roots((size_t)np, 0);
+    for (int tree = -1; tree < np; ++tree) {  // the top level, then one tree per prototype
+        const int n = tree < 0 ? world_n_ : proto_n_[tree];
+        const float* soup = tree < 0 ? isoup_ : proto_soup_d_ + 9 * proto_off_[tree];
+        if (tree < 0) k_soup_subset<<<(n + 255) / 256, 256, 0, s>>>(view_.prim_v, world_ids_d_, n, isoup_);
+        if (!(e = ilbvh_.build(soup, n, BVH_MODE_SORTED, -1, s, d_err)).empty()) return e;
+        if (tree < 0)
+            k_gather_leaves<<<(n + 255) / 256, 256, 0, s>>>(view_.prim_v, view_.prim_rec, view_.mats,
+                                                            ilbvh_.leaf_prim, n, ileaf_, world_ids_d_);
+        else
+            k_gather_soup_leaves<<<(n + 255) / 256, 256, 0, s>>>(soup, ilbvh_.leaf_prim, n, ileaf_);
+        TRY(cudaGetLastError());
+        if (!(e = iploc_.build(ileaf_, n, s, d_err)).empty()) return e;
+        if (!(e = iwide_.build(iploc_.nodes, render_bvh == 1 ? iploc_.sah : nullptr, n, key, ileaf_, s, d_err)).empty())
+            return e;
+        if ((size_t)node_base + iwide_.count > tot_nodes) return "two-level BVH: node count out of range";
+        k_rebase_wide<<<(iwide_.count + 127) / 128, 128, 0, s>>>(iwide_.nodes, iwide_.count, node_base, tri_base,
+                                                                inodes_ + node_base);
+        TRY(cudaGetLastError());
+        TRY(cudaMemcpyAsync(itris_ + 3 * (size_t)tri_base, iwide_.tris, 48 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+        if (tree >= 0) roots[tree] = (int)node_base;
+        node_base += (uint32_t)iwide_.count;
+        tri_base += (uint32_t)n;
+        levels = std::max(levels, iwide_.levels);
+    }
+    // the instance table; world boxes padded by 1e-5 of their largest coordinate, so that they
+    // hold every point the object-space tests can hit after the ray's transform has rounded
+    std::vector<DevInstance> di((size_t)ni);
+    float root[6];
+    for (int a = 0; a < 6; ++a) root[a] = world_box_[a];
+    for (int i = 0; i < ni; ++i) {
+        const InstHost& h = inst_host_[i];
+        const float* b = &proto_box_[6 * (size_t)h.proto];
+        float lo[3], hi[3], m = 0;
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = b[a] * h.s + h.t[a];
+            hi[a] = b[3 + a] * h.s + h.t[a];
+            m = std::max(m, std::max(std::fabs(lo[a]), std::fabs(hi[a])));
+        }
+        const float pad = 1e-5f * m + 1e-30f;
+        for (int a = 0; a < 3; ++a) {
+            lo[a] -= pad;
+            hi[a] += pad;
+            root[a] = std::min(root[a], lo[a]);
+            root[3 + a] = std::max(root[3 + a], hi[a]);
+        }
+        DevInstance& d = di[i];
+        d.xf = make_float4(h.t[0], h.t[1], h.t[2], 1.0f / h.s);
+        d.wlo = make_float4(lo[0], lo[1], lo[2], 0.f);
+        d.whi = make_float4(hi[0], hi[1], hi[2], 0.f);
+        d.olo = make_float4(b[0], b[1], b[2], 0.f);
+        d.ohi = make_float4(b[3], b[4], b[5], 0.f);
+        d.ref = make_int4(roots[h.proto], h.prim_first, h.cls, 0);
+    }
+    TRY(cudaMemcpyAsync(dinst_, di.data(), sizeof(DevInstance) * (size_t)ni, cudaMemcpyHostToDevice, s));
+    TRY(cudaMemcpyAsync(iroot_, root, sizeof root, cudaMemcpyHostToDevice, s));
+    TRY(cudaStreamSynchronize(s));
+    last_render_bvh_ms = (float)std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    icount_ = (int)node_base;
+    itri_n_ = (int)tri_base;
+    ilevels_ = levels;
+    ikey_ = key;
     return "";
 }
 
@@ -492,10 +754,20 @@ std::string Tracer::traversal_view(const Lbvh& bvh, cudaStream_t s, uint32_t* d_
         leaf_n_ = bvh.n;
     }
     // 8-wide compressed BVH collapsed from the binary tree (kept while the tree is unchanged); it
-    // is used when the wide tree's depth fits the traversal stack
+    // is used when the wide tree's depth fits the traversal stack.  Scenes with instanced meshes
+    // use the two-level tree instead (built once per scene upload and render-tree choice).
     bool use_wide = bvh_width == 8 && bvh.n >= 2;
+    bool use_inst = false;
+    if (use_wide && render_bvh != 0 && two_level && two_level_ok_) {
+        const uint64_t ikey = 4 * upload_serial_ + (uint64_t)render_bvh;
+        if (ikey_ != ikey) {
+            const std::string e = build_instanced(ikey, s, d_err);
+            if (!e.empty()) return e;
+        }
+        use_inst = ilevels_ - 1 <= kStack / 2;
+    }
     const uint64_t wide_key = 4 * bvh.serial + (uint64_t)render_bvh;  // the binary tree and collapse it came from
-    if (use_wide && wide_.serial != wide_key) {
+    if (use_wide && !use_inst && wide_.serial != wide_key) {
         std::string e;
         if (render_bvh) {
             e = ploc_.build(leaf_v_, bvh.n, s, d_err);
@@ -509,16 +781,24 @@ std::string Tracer::traversal_view(const Lbvh& bvh, cudaStream_t s, uint32_t* d_
         }
         if (!e.empty()) return e;
     }
-    if (use_wide && wide_.levels - 1 > kStack / 2) use_wide = false;
+    if (use_wide && !use_inst && wide_.levels - 1 > kStack / 2) use_wide = false;
     *sv = view_;
     sv->leaf_v = leaf_v_;
     sv->nodes = bvh.nodes;
-    sv->root_bounds = bvh.root_bounds;
-    sv->wnodes = use_wide ? wide_.nodes : nullptr;
-    sv->wtris = use_wide ? wide_.tris : nullptr;
-    sv->wcount = use_wide ? wide_.count : 0;
+    sv->root_bounds = use_inst ? iroot_ : bvh.root_bounds;
+    sv->wnodes = use_inst ? inodes_ : (use_wide ? wide_.nodes : nullptr);
+    sv->wtris = use_inst ? itris_ : (use_wide ? wide_.tris : nullptr);
+    sv->wcount = use_inst ? icount_ : (use_wide ? wide_.count : 0);
+    sv->wtri_count = use_inst ? itri_n_ : (use_wide ? bvh.n : 0);
+    sv->inst = use_inst ? dinst_ : nullptr;
+    sv->ninst = use_inst ? (int32_t)inst_host_.size() : 0;
     sv->watertight = watertight;
     last_wide = use_wide;
+    last_two_level = use_inst;
+    render_bvh_bytes = use_inst ? sizeof(WideNode) * (size_t)icount_ + 48 * (size_t)itri_n_ +
+                                          sizeof(DevInstance) * inst_host_.size()
+                                : use_wide ? sizeof(WideNode) * (size_t)wide_.count + 48 * (size_t)bvh.n
+                                           : sizeof(BvhNode) * (size_t)(bvh.n - 1) + 48 * (size_t)bvh.n;
     return "";
 }
 
@@ -762,7 +1042,7 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
         const double expect = rate * (double)paths, keep = 0.9 * (double)st.tr_cap;
         st.tr_accept = expect <= keep ? 0xFFFFFFFFu : (uint32_t)std::min(4294967295.0, 4294967296.0 * keep / expect);
     }
-    st.bounds = sv.root_bounds;
+    st.bounds = bvh.root_bounds;  // the cache's position features: the scene's bounds in every BVH mode
     if (cache) {
         if (wf_cache_cap_ < P || wf_train_cap_ < (long)st.tr_cap) {
             for (int k = 36; k < 45; ++k) {
@@ -801,16 +1081,19 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
     for (double& x : last_stage_ms) x = 0;
     // persistent trace grid: every SM filled with as many blocks as stay resident
     if (wf_trace_blocks_[0] == 0) {
-        int dev = 0, sms = 0, per_w = 0, per_b = 0;
+        int dev = 0, sms = 0, per_w = 0, per_b = 0, per_i = 0;
         TRY(cudaGetDevice(&dev));
         TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_w, k_wf_trace<true>, kWfBlock, 0));
         TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, k_wf_trace<false>, kWfBlock, 0));
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_i, k_wf_trace<true, true>, kWfBlock, 0));
         wf_trace_blocks_[0] = (unsigned)std::max(1, per_w * sms);
         wf_trace_blocks_[1] = (unsigned)std::max(1, per_b * sms);
+        wf_trace_blocks_[2] = (unsigned)std::max(1, per_i * sms);
         wf_sms_ = (unsigned)sms;
     }
-    unsigned tb = wf_trace_blocks_[wide ? 0 : 1];
+    const bool two_level = wide && sv.ninst > 0;
+    unsigned tb = wf_trace_blocks_[two_level ? 2 : (wide ? 0 : 1)];
     if (trace_blocks_per_sm > 0) tb = std::min(tb, (unsigned)trace_blocks_per_sm * wf_sms_);
     const unsigned cgrid = (unsigned)((P + kCompactTile - 1) / kCompactTile);
     const dim3 gblock(32, 4);
@@ -834,7 +1117,8 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
         if (!full) TRY(cudaEventRecord(wf_ev_[1], s));
         if (full || nray) {
             const unsigned g = full ? tb : std::min(blocks(nray), tb);
-            if (wide) k_wf_trace<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, d_ctl, st.counts + 8, bvh.n);
+            if (two_level) k_wf_trace<true, true><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, d_ctl, st.counts + 8, bvh.n);
+            else if (wide) k_wf_trace<true><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, d_ctl, st.counts + 8, bvh.n);
             else k_wf_trace<false><<<g, kWfBlock, 0, s>>>(sv, rp, st, q_ext, d_ctl, st.counts + 8, bvh.n);
         }
         if (st.cache && (full || n_query)) {  // the previous shade's cache queries, before finalize adds them

@@ -31,7 +31,30 @@ struct DevLight {
     float L[3], p[3], radius, area;
 };
 
+// One image texture's pyramid (the fixed mode of Mipmap, materials/textures/Mipmap.cuh:34-73):
+// level l holds w[l] x h[l] linear-RGB texels from img_texels + off[l] on, in 4 x 4 blocks
+// (BlockedArray, core/MemoryHelper.cuh:36-100, with the in-block row v & 3): texel (u, v) is
+// 16 (bw (v >> 2) + (u >> 2)) + 4 (v & 3) + (u & 3) with bw = ceil(w / 4).
+constexpr int kImageLevels = 16;
+struct DevImage {
+    int32_t levels, wrap;  // wrap: 0 repeat, 1 black, 2 clamp
+    float lod;             // levels - 1 + log2(0.01), the lookup's level coordinate
+    int32_t pad;
+    int32_t off[kImageLevels], w[kImageLevels], h[kImageLevels];
+};
+
 // Everything a render kernel reads, passed by value.
+// One instance of the two-level render BVH (a mesh entry of the loader's `instances` record):
+// world position = object position * scale + t.  96 bytes, six 16-byte loads.
+struct alignas(16) DevInstance {
+    float4 xf;        // t.xyz, 1 / scale
+    float4 wlo, whi;  // world-space box of the instance's triangles (w unused)
+    float4 olo, ohi;  // object-space box of the prototype's triangles (w unused)
+    int4 ref;         // root node of the prototype's tree, the entry's first primitive (scene
+                      // order), the shade class of its material, 0
+};
+constexpr int kMaxInstances = 32;
+
 struct SceneView {
     int32_t ntri, nlight, width, height;
     const float4* __restrict__ leaf_v;   // [3 ntri] triangle of leaf l: p0 (w = prim id bits), p1, p2
@@ -54,7 +77,12 @@ struct SceneView {
     const WideNode* __restrict__ wnodes;  // 8-wide compressed BVH (null: traverse the binary tree)
     const float4* __restrict__ wtris;     // [3 ntri] triangles in wide-leaf order
     int32_t wcount;                       // wide nodes
+    int32_t wtri_count;                   // triangles in wtris
     int32_t watertight;                   // 1: watertight triangle tests (fixed mode), 0: the reference's
+    const DevInstance* __restrict__ inst;  // two-level render BVH: the instances (null, 0: none)
+    int32_t ninst;
+    const float4* __restrict__ img_texels;  // image-texture pyramids (DevImage)
+    const DevImage* __restrict__ images;
     const float* __restrict__ filter;    // 16 x 16 Gaussian table
     float cam[23];
 };
@@ -140,6 +168,10 @@ class Tracer {
     // order, SAH-optimal collapse; 2 = the PLOC tree, greedy collapse; 0 = the LBVH itself, greedy.
     int render_bvh = 1;
     float last_render_bvh_ms = 0;  // PLOC + collapse of the last rebuild
+    // Scenes with instanced meshes: 1 = the two-level 8-wide BVH (one tree per prototype under
+    // a top level), 0 = one flat tree over every triangle.  Needs bvh_width 8 and render_bvh != 0.
+    int two_level = 1;
+    bool last_two_level = false;  // the last render traversed the two-level BVH
     // Radiance cache (wavefront integrator): on/off, the MLP it queries and trains (owned by the
     // context), the share of paths traced in full (per mille), training records per render, Adam
     // steps per render and learning rate; statistics of the last render.
@@ -176,8 +208,46 @@ class Tracer {
     std::string intersect(const Lbvh& bvh, const float4* d_rays, int n, int any, int32_t* d_prim, float* d_t,
                           cudaStream_t s, uint32_t* d_err);
 
+    // Device bytes of the render BVH's nodes and triangles last used (two-level or flat).
+    size_t render_bvh_bytes = 0;
+
    private:
     std::string traversal_view(const Lbvh& bvh, cudaStream_t s, uint32_t* d_err, SceneView* sv);
+    // Two-level render BVH of a scene with instanced meshes: upload_scene keeps the instances,
+    // the prototypes' object-space triangles and the ids of the other triangles; build_instanced
+    // builds an LBVH + PLOC + 8-wide tree over those other triangles (the top-level tree, root 0,
+    // leaf triangles carrying their scene-order ids) and one over each prototype (leaf triangles
+    // carrying their index in the prototype), and concatenates them with rebased indices.
+    struct InstHost {
+        int32_t mesh, proto, prim_first, ntri, cls;
+        float t[3], s;
+    };
+    std::string capture_instances(const HostScene& sc, const std::vector<DevMat>& mats, cudaStream_t s);
+    std::string build_instanced(uint64_t key, cudaStream_t s, uint32_t* d_err);
+    void release_instanced();
+    std::vector<InstHost> inst_host_;
+    std::vector<size_t> proto_off_;  // first triangle of each prototype in proto_soup_d_
+    std::vector<int> proto_n_;
+    std::vector<float> proto_box_;   // per prototype: object-space lo.xyz, hi.xyz
+    float world_box_[6] = {0, 0, 0, 0, 0, 0};  // the non-instanced triangles' bounds
+    float* proto_soup_d_ = nullptr;  // the prototypes' object-space triangles, 9 floats each
+    int32_t* world_ids_d_ = nullptr; // scene-order ids of the non-instanced triangles
+    int world_n_ = 0;
+    float* isoup_ = nullptr;         // one tree's input triangles (9 floats each)
+    float4* ileaf_ = nullptr;        // one tree's leaf-ordered triangles
+    size_t isoup_cap_ = 0, ileaf_cap_ = 0;
+    Lbvh ilbvh_;
+    PlocBvh iploc_;
+    WideBvh iwide_;
+    WideNode* inodes_ = nullptr;     // the concatenated trees: top level first (root 0)
+    float4* itris_ = nullptr;
+    DevInstance* dinst_ = nullptr;
+    float* iroot_ = nullptr;         // bounds of the whole two-level scene
+    size_t inodes_cap_ = 0, itris_cap_ = 0;
+    int icount_ = 0, itri_n_ = 0, ilevels_ = 0;
+    uint64_t ikey_ = 0;              // key of the scene upload and render-tree choice built from
+    uint64_t upload_serial_ = 0;
+    int two_level_ok_ = 0;
     std::string prepare(const HostScene& sc, const Lbvh& bvh, const lts_render_desc& d, cudaStream_t s,
                         uint32_t* d_err, RenderParams* rp, SceneView* sv, long* crop_samples);
     void free_all();
@@ -200,12 +270,12 @@ class Tracer {
     uint32_t* wf_counts_host_ = nullptr;
     void* wf_ctl_host_ = nullptr;  // pinned mirror of the wavefront control block
     cudaEvent_t wf_ev_[7] = {nullptr};
-    unsigned wf_trace_blocks_[2] = {0, 0};
+    unsigned wf_trace_blocks_[3] = {0, 0, 0};  // resident blocks of k_wf_trace: wide, binary, two-level
     unsigned wf_sms_ = 0;  // resident blocks of k_wf_trace (wide, binary) on this device
     SceneView view_{};
     WideBvh wide_;
     PlocBvh ploc_;
-    static constexpr int kSceneBufs = 16;
+    static constexpr int kSceneBufs = 17;
     void* bufs_[kSceneBufs] = {nullptr};   // scene tables, kept across scene loads while big enough
     size_t bufcap_[kSceneBufs] = {0};
     float4* leaf_v_ = nullptr;

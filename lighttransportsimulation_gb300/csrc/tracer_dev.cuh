@@ -199,6 +199,7 @@ struct SI {
     V3 dpdu, dpdv;      // geometric partials
     V3 sn, sdpdu;       // shading normal and tangent
     V3 dpdx, dpdy;      // computeDifferentials
+    real tu, tv;        // surface uv at the hit (uvHit, Triangle.cu:160)
     int prim;
     int mesh, light;    // material index, area-light index (-1: none) of the primitive
 };
@@ -241,6 +242,8 @@ __device__ void make_si(const SceneView& sv, int prim, V3 d, real u, real v, rea
     const real zs = xabs(w * p0.z) + xabs(u * p1.z) + xabs(v * p2.z);
     si.perr = v3(xs, ys, zs) * gamma_n(7);
     si.p = p0 * w + p1 * u + p2 * v;
+    si.tu = uv0x * w + uv1x * u + uv2x * v;
+    si.tv = uv0y * w + uv1y * u + uv2y * v;
     si.wo = -d;
     si.dpdu = dpdu;
     si.dpdv = dpdv;
@@ -361,27 +364,43 @@ __device__ __forceinline__ bool tri_test_wt(V3 p0, V3 p1, V3 p2, const TraceRay&
 // in the watertight mode so that only the hit test differs).
 __device__ __forceinline__ real mt_inv_det(V3 p0, V3 p1, V3 p2, V3 d) { return xrcp(dot(p1 - p0, cross(d, p2 - p0))); }
 
+// The hit word of a leaf triangle: its primitive id and shade class from the triangle (top-level
+// tree), or, inside instance `ii` of a two-level BVH, the instance's first primitive plus the
+// triangle's index in its prototype and the instance's class; then 1 / det (make_si's dpdu scale)
+// goes from object to world space (det scales with scale^3).
+__device__ __forceinline__ int hit_word(float4 a, float4 b, const bool inst, int ii, const DevInstance* insts,
+                                        real& binv) {
+    if (inst && ii >= 0) {
+        const int4 ref = __ldg(&insts[ii].ref);
+        const real is = __ldg(&insts[ii].xf.w);
+        binv = binv * (is * is * is);
+        return (ref.y + __float_as_int(a.w)) | (ref.z << kHitPrimBits);
+    }
+    return __float_as_int(a.w) | (__float_as_int(b.w) << kHitPrimBits);
+}
+
 __device__ __forceinline__ bool leaf_test(const bool any, const float4* __restrict__ tv, int leaf, const TraceRay& r,
-                                          real& tmax, int& best, real& bu, real& bv, real& binv, const bool wt) {
+                                          real& tmax, int& best, real& bu, real& bv, real& binv, const bool wt,
+                                          const bool inst = false, int ii = -1, const DevInstance* insts = nullptr) {
     const float4 a = __ldg(tv + 3 * leaf), b = __ldg(tv + 3 * leaf + 1), c = __ldg(tv + 3 * leaf + 2);
     real t, u, v, inv;
     if (wt) {
         if (!tri_test_wt(f4v(a), f4v(b), f4v(c), r, tmax, t, u, v)) return false;
         if (any) return true;
         tmax = t;
-        best = __float_as_int(a.w) | (__float_as_int(b.w) << kHitPrimBits);
         bu = u;
         bv = v;
         binv = mt_inv_det(f4v(a), f4v(b), f4v(c), r.d);
+        best = hit_word(a, b, inst, ii, insts, binv);
         return false;
     }
     if (any) return tri_test_shadow(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax);
     if (tri_test(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax, t, u, v, inv)) {
         tmax = t;
-        best = __float_as_int(a.w) | (__float_as_int(b.w) << kHitPrimBits);
         bu = u;
         bv = v;
         binv = inv;
+        best = hit_word(a, b, inst, ii, insts, binv);
     }
     return false;
 }
@@ -409,12 +428,16 @@ struct Trav {
     int node, sp;
     uint32_t gbase, gbits;
     uint32_t lbits, lbase;  // split steps: the last node's pending triangles (bit k: triangle lbase + k)
+    // two-level BVH: the instance being traversed (-1: the top-level tree, whose ray is the world
+    // ray) and the instances whose world boxes the ray enters, still to visit
+    int inst;
+    uint32_t imask;
 };
 
 // Returns true when the ray needs traversal steps; false when it is already resolved (missed
 // the scene bounds, or a one-triangle scene).  any: any hit (shadow rays), else closest hit.
 __device__ __forceinline__ bool trav_begin(const bool any, Trav& t, const SceneView& sv, int nleaf, V3 o, V3 d,
-                                           real tmax, Work& wk) {
+                                           real tmax, Work& wk, const bool inst = false) {
     t.r = make_trace_ray(o, d);
     t.tmax = tmax;
     t.bu = t.bv = t.binv = 0.f;
@@ -425,10 +448,18 @@ __device__ __forceinline__ bool trav_begin(const bool any, Trav& t, const SceneV
     t.gbits = 0;
     t.lbits = 0;
     t.lbase = 0;
+    t.inst = -1;
+    t.imask = 0;
     real te;
     const float* rb = sv.root_bounds;
     if (!slab(t.r, t.tmax, __ldg(rb), __ldg(rb + 1), __ldg(rb + 2), __ldg(rb + 3), __ldg(rb + 4), __ldg(rb + 5), te))
         return false;
+    if (inst) {  // the instances whose world boxes the ray enters
+        for (int i = 0; i < sv.ninst; ++i) {
+            const float4 lo = __ldg(&sv.inst[i].wlo), hi = __ldg(&sv.inst[i].whi);
+            if (slab(t.r, t.tmax, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, te)) t.imask |= 1u << i;
+        }
+    }
     if (nleaf == 1) {
         ++wk.tris;
         if (leaf_test(any, sv.leaf_v, 0, t.r, t.tmax, t.best, t.bu, t.bv, t.binv, sv.watertight != 0)) t.best = 1;
@@ -502,7 +533,7 @@ __device__ __forceinline__ uint32_t leaf_tri_bits(uint32_t leaves, uint32_t u) {
 
 // One node; returns true when the traversal has finished.
 __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const SceneView& sv, uint32_t* stack,
-                                               uint32_t* err, Work& wk) {
+                                               uint32_t* err, Work& wk, const bool inst = false) {
     if ((unsigned)t.node >= (unsigned)sv.wcount) {
         atomicOr(err, DEV_ERR_BAD_INDEX);
         return true;
@@ -559,12 +590,13 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
     while (tb) {
         const int tri = (int)m.y + __ffs(tb) - 1;
         tb &= tb - 1u;
-        if ((unsigned)tri >= (unsigned)sv.ntri) {
+        if ((unsigned)tri >= (unsigned)sv.wtri_count) {
             atomicOr(err, DEV_ERR_BAD_INDEX);
             return true;
         }
         ++wk.tris;
-        if (leaf_test(any, sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv, sv.watertight != 0)) {
+        if (leaf_test(any, sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv, sv.watertight != 0, inst, t.inst,
+                      sv.inst)) {
             t.best = 1;
             return true;
         }
@@ -602,7 +634,7 @@ __device__ __forceinline__ bool trav_step_wide(const bool any, Trav& t, const Sc
 // triangle tests of all its lanes together instead of inside divergent node steps.  Both
 // return true when the traversal has finished.
 __device__ __forceinline__ bool wide_node_step(const bool any, Trav& t, const SceneView& sv, uint32_t* stack,
-                                               uint32_t* err, Work& wk) {
+                                               uint32_t* err, Work& wk, const bool inst = false) {
     if ((unsigned)t.node >= (unsigned)sv.wcount) {
         atomicOr(err, DEV_ERR_BAD_INDEX);
         return true;
@@ -689,15 +721,17 @@ __device__ __forceinline__ bool wide_node_step(const bool any, Trav& t, const Sc
 }
 
 
-__device__ __forceinline__ bool wide_leaf_step(const bool any, Trav& t, const SceneView& sv, uint32_t* err, Work& wk) {
+__device__ __forceinline__ bool wide_leaf_step(const bool any, Trav& t, const SceneView& sv, uint32_t* err, Work& wk,
+                                               const bool inst = false) {
     const int tri = (int)t.lbase + __ffs(t.lbits) - 1;
     t.lbits &= t.lbits - 1u;
-    if ((unsigned)tri >= (unsigned)sv.ntri) {
+    if ((unsigned)tri >= (unsigned)sv.wtri_count) {
         atomicOr(err, DEV_ERR_BAD_INDEX);
         return true;
     }
     ++wk.tris;
-    if (leaf_test(any, sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv, sv.watertight != 0)) {
+    if (leaf_test(any, sv.wtris, tri, t.r, t.tmax, t.best, t.bu, t.bv, t.binv, sv.watertight != 0, inst, t.inst,
+                  sv.inst)) {
         t.best = 1;
         return true;
     }
@@ -751,22 +785,59 @@ __device__ __forceinline__ bool trav_step_binary(const bool any, Trav& t, const 
 }
 
 __device__ __forceinline__ bool trav_step(const bool any, Trav& t, const SceneView& sv, uint32_t* stack, uint32_t* err,
-                                          Work& wk) {
+                                          Work& wk, const bool inst = false) {
 #if LTS_FP64
     return trav_step_binary(any, t, sv, stack, err, wk);
 #else
-    return sv.wnodes ? trav_step_wide(any, t, sv, stack, err, wk) : trav_step_binary(any, t, sv, stack, err, wk);
+    return sv.wnodes ? trav_step_wide(any, t, sv, stack, err, wk, inst) : trav_step_binary(any, t, sv, stack, err, wk);
 #endif
 }
 
+#if !LTS_FP64
+// Two-level BVH: when the traversal of the top-level tree or of an instance has finished, starts
+// the next instance whose world box the ray entered (its object-space ray o' = (o - t) / scale,
+// d' = d / scale keeps the ray parameter, so tmax carries over), skipping instances whose
+// prototype box lies beyond the closest hit so far.  Returns false when none is left (or an
+// any-hit query has its hit).
+__device__ __forceinline__ bool inst_next(const bool any, Trav& t, const SceneView& sv, V3 wo, V3 wd) {
+    if (any && t.best == 1) return false;
+    while (t.imask) {
+        const int i = __ffs(t.imask) - 1;
+        t.imask &= t.imask - 1u;
+        const DevInstance* I = sv.inst + i;
+        const float4 xf = __ldg(&I->xf), lo = __ldg(&I->olo), hi = __ldg(&I->ohi);
+        const int4 ref = __ldg(&I->ref);
+        t.r = make_trace_ray(v3((wo.x - xf.x) * xf.w, (wo.y - xf.y) * xf.w, (wo.z - xf.z) * xf.w),
+                             v3(wd.x * xf.w, wd.y * xf.w, wd.z * xf.w));
+        real te;
+        if (!slab(t.r, t.tmax, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, te)) continue;
+        t.inst = i;
+        t.node = ref.x;
+        t.sp = 0;
+        t.gbase = 0;
+        t.gbits = 0;
+        t.lbits = 0;
+        return true;
+    }
+    return false;
+}
+#endif
+
 // Whole traversal: the hit primitive (closest) or 1 / -1 (any), -1 for a miss.
-template <bool ANY>
+template <bool ANY, bool INST = false>
 __device__ int traverse(const SceneView& sv, int nleaf, const TraceRay& r, real& tmax, real& bu, real& bv,
                         real& binv, uint32_t* stack, uint32_t* err, Work& wk) {
     Trav t;
-    if (trav_begin(ANY, t, sv, nleaf, r.o, r.d, tmax, wk))
-        while (!trav_step(ANY, t, sv, stack, err, wk)) {
+    if (trav_begin(ANY, t, sv, nleaf, r.o, r.d, tmax, wk, INST)) {
+        for (;;) {
+            while (!trav_step(ANY, t, sv, stack, err, wk, INST)) {
+            }
+#if !LTS_FP64
+            if (INST && inst_next(ANY, t, sv, r.o, r.d)) continue;
+#endif
+            break;
         }
+    }
     tmax = t.tmax;
     bu = t.bu;
     bv = t.bv;
@@ -783,7 +854,12 @@ __device__ __forceinline__ bool scene_intersect(const SceneView& sv, int nleaf, 
                                                 uint32_t* stack, uint32_t* err, Work& wk) {
     const TraceRay r = make_trace_ray(o, d);
     real bu = 0, bv = 0, binv = 0;
+#if !LTS_FP64
+    const int prim = sv.ninst ? traverse<false, true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk)
+                              : traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk);
+#else
     const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk);
+#endif
     if (prim < 0) return false;
     make_si(sv, prim, d, bu, bv, binv, si);
     return true;
@@ -792,6 +868,9 @@ __device__ __forceinline__ bool scene_occluded(const SceneView& sv, int nleaf, V
                                                uint32_t* err, Work& wk) {
     const TraceRay r = make_trace_ray(o, d);
     real bu, bv, binv;
+#if !LTS_FP64
+    if (sv.ninst) return traverse<true, true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk) > 0;
+#endif
     return traverse<true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk) > 0;
 }
 
@@ -891,8 +970,55 @@ __device__ real turbulence(V3 p, V3 dpdx, V3 dpdy, real omega, int max_oct, EvSi
     return sum;
 }
 
-__device__ Spec eval_texture(const DevTex& t, const SI& si, EvSink* sig) {
+// Image textures, the fixed mode of ImageTexture::evaluate (ImageTexture.cuh:24-28) over its
+// Mipmap (Mipmap.cuh:14-73) in the reference's operation order.  Fixed: the repeat mode wraps
+// negative coordinates into the level (the reference's fmodf leaves them negative and reads
+// before the level's storage), and a level coordinate past the coarsest level reads texel (0, 0)
+// of that level (the reference reads texel (levels - 1, 0) of level 0).
+__device__ __forceinline__ Spec img_texel(const SceneView& sv, const DevImage* im, int l, int s, int t) {
+    const int w = __ldg(&im->w[l]), h = __ldg(&im->h[l]), wrap = __ldg(&im->wrap);
+    if (wrap == 0) {
+        s %= w;
+        if (s < 0) s += w;
+        t %= h;
+        if (t < 0) t += h;
+    } else if (wrap == 2) {
+        s = s < 0 ? 0 : (s > w - 1 ? w - 1 : s);
+        t = t < 0 ? 0 : (t > h - 1 ? h - 1 : t);
+    } else if (s < 0 || s >= w || t < 0 || t >= h) {
+        return spec(0.0f);
+    }
+    const float4 q = __ldg(sv.img_texels + __ldg(&im->off[l]) + 16 * ((t >> 2) * ((w + 3) >> 2) + (s >> 2)) +
+                           4 * (t & 3) + (s & 3));
+    return Spec{q.x, q.y, q.z};
+}
+// Mipmap::triangle: bilinear over level l (clamped to the pyramid).
+__device__ __forceinline__ Spec img_bilerp(const SceneView& sv, const DevImage* im, int l, real st0, real st1) {
+    const int levels = __ldg(&im->levels);
+    l = l < 0 ? 0 : (l > levels - 1 ? levels - 1 : l);
+    const real s = st0 * (real)__ldg(&im->w[l]) - 0.5f, t = st1 * (real)__ldg(&im->h[l]) - 0.5f;
+    const int s0 = (int)xfloor(s), t0 = (int)xfloor(t);
+    const real ds = s - (real)s0, dt = t - (real)t0;
+    return img_texel(sv, im, l, s0, t0) * ((1 - ds) * (1 - dt)) + img_texel(sv, im, l, s0, t0 + 1) * ((1 - ds) * dt) +
+           img_texel(sv, im, l, s0 + 1, t0) * (ds * (1 - dt)) + img_texel(sv, im, l, s0 + 1, t0 + 1) * (ds * dt);
+}
+// Mipmap::lookUp at the fixed width 0.01 (EVALUATION_WIDTH), whose level coordinate the loader
+// computes once per image.
+__device__ Spec img_lookup(const SceneView& sv, int idx, real st0, real st1) {
+    const DevImage* im = sv.images + idx;
+    const real lod = __ldg(&im->lod);
+    const int levels = __ldg(&im->levels);
+    if (lod < 0) return img_bilerp(sv, im, 0, st0, st1);
+    if (lod >= (real)(levels - 1)) return img_texel(sv, im, levels - 1, 0, 0);
+    const int il = (int)xfloor(lod);
+    const real delta = lod - (real)il;
+    return img_bilerp(sv, im, il, st0, st1) * (1 - delta) + img_bilerp(sv, im, il + 1, st0, st1) * delta;
+}
+
+__device__ Spec eval_texture(const SceneView& sv, const DevTex& t, const SI& si, EvSink* sig) {
     switch (t.kind) {
+        case 5:  // ImageTexture with UVMapping2D(1, 1, 0, 0) (SceneLoader.cuh:375): st = uv
+            return img_lookup(sv, (int)t.v[0], si.tu, si.tv);
         case 1:  // FBmTexture (Procedural.cuh:207-225)
             return spec(fbm(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0], sig));
         case 2:  // WrinkledTexture (Procedural.cuh:227-245)
@@ -1237,7 +1363,7 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* si
     f.eta = 1;
     switch (m.kind) {
         case 1: {  // Matte
-            const Spec kd = eval_texture(m.tex[0], si, sig);
+            const Spec kd = eval_texture(sv, m.tex[0], si, sig);
             if (!is_black(kd)) {
                 f.R = kd;
                 if (m.extra == 0) {
@@ -1253,7 +1379,7 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* si
         }
         case 2: {  // Glass
             f.eta = m.extra;
-            const Spec r = eval_texture(m.tex[0], si, sig), t = eval_texture(m.tex[1], si, sig);
+            const Spec r = eval_texture(sv, m.tex[0], si, sig), t = eval_texture(sv, m.tex[1], si, sig);
             if (is_black(r) && is_black(t)) break;
             f.R = r;
             f.T = t;
@@ -1262,7 +1388,7 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* si
             break;
         }
         case 3: {  // Mirror
-            const Spec r = eval_texture(m.tex[0], si, sig);
+            const Spec r = eval_texture(sv, m.tex[0], si, sig);
             if (is_black(r)) break;
             f.R = r;
             f.lobe = LOBE_SPECULAR_REFL;
@@ -1270,7 +1396,7 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* si
             break;
         }
         case 4: {  // Metal (alpha given directly)
-            f.k = eval_texture(m.tex[0], si, sig);
+            f.k = eval_texture(sv, m.tex[0], si, sig);
             f.eta3 = Spec{m.tex[1].v[0], m.tex[1].v[1], m.tex[1].v[2]};
             f.R = spec(1.0f);
             f.alpha = m.extra;

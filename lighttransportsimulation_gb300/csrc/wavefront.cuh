@@ -91,6 +91,9 @@ struct WfCtl {
 __device__ __forceinline__ float bsdf_roughness(const Bsdf& f) {
     return (f.lobe == LOBE_LAMBERT || f.lobe == LOBE_OREN_NAYAR) ? 1.0f : (f.lobe == LOBE_MICROFACET ? f.alpha : 0.0f);
 }
+// A vertex is rough for the radiance cache above this roughness: the cache is trained and queried
+// at rough vertices only, whose outgoing radiance varies slowly with direction.
+constexpr float kCacheRough = 0.3f;
 __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
     return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
            ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
@@ -244,17 +247,25 @@ enum : int { TR_EXTEND = 0, TR_SHADOW = 1, TR_MIS = 2 };
 
 // The ray of path slot p for each traversal kind.
 __device__ __forceinline__ bool wf_ray_begin(int kind, Trav& t, const SceneView& sv, const WfState& st, int p,
-                                             int nleaf, Work& wk) {
+                                             int nleaf, Work& wk, const bool inst = false) {
     if (kind == TR_EXTEND) {  // path ray, closest hit (BVH::intersect, BVH.cuh:365-398)
         const float4 o = st.ro[p], d = st.rd[p];
-        return trav_begin(false, t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), INFINITY, wk);
+        return trav_begin(false, t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), INFINITY, wk, inst);
     } else if (kind == TR_SHADOW) {  // VisibilityTester::unoccluded (VisibilityTester.cu:9-12), any hit
         const float4 o = st.sh_o[p], d = st.sh_d[p];
-        return trav_begin(true, t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), d.w, wk);
+        return trav_begin(true, t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), d.w, wk, inst);
     } else {  // MIS BSDF ray, closest hit
         const float4 o = st.mis_o[p], d = st.mis_d[p];
-        return trav_begin(false, t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), INFINITY, wk);
+        return trav_begin(false, t, sv, nleaf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), INFINITY, wk, inst);
     }
+}
+// Two-level BVH: the world ray of a ray in flight, re-read from the path state (the traversal
+// holds the current instance's object-space ray) to enter the next instance.
+__device__ __forceinline__ bool wf_ray_next_instance(int kind, Trav& t, const SceneView& sv, const WfState& st,
+                                                     int p) {
+    const float4 o = kind == TR_EXTEND ? st.ro[p] : (kind == TR_SHADOW ? st.sh_o[p] : st.mis_o[p]);
+    const float4 d = kind == TR_EXTEND ? st.rd[p] : (kind == TR_SHADOW ? st.sh_d[p] : st.mis_d[p]);
+    return inst_next(kind == TR_SHADOW, t, sv, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z));
 }
 
 // Results of a finished traversal.  MIS: radiance of the sampled light where the BSDF ray lands
@@ -310,7 +321,7 @@ constexpr int kTraceMinBlocks = LTS_TRACE_MIN_BLOCKS;
 // the warp's longest ray finishes (dynamic ray fetch, Aila and Laine, HPG 2009), and the short
 // shadow and MIS lists share the launch's tail with the path rays.  Launched with whole warps;
 // `fetch` is zeroed before the launch.  WIDE: the 8-wide compressed BVH, else the binary LBVH.
-template <bool WIDE>
+template <bool WIDE, bool INST = false>
 __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const SceneView sv, const RenderParams rp, WfState st,
                                                        const int32_t* __restrict__ q_ext,
                                                        const WfCtl* __restrict__ ctl, uint32_t* fetch, int nleaf) {
@@ -348,7 +359,8 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
                 if (idx < n) {
                     kind = idx < e1 ? TR_EXTEND : (idx < e2 ? TR_SHADOW : TR_MIS);
                     p = kind == TR_EXTEND ? q_ext[idx] : (kind == TR_SHADOW ? st.q_shadow[idx - e1] : st.q_mis[idx - e2]);
-                    active = wf_ray_begin(kind, t, sv, st, p, nleaf, cur);
+                    active = wf_ray_begin(kind, t, sv, st, p, nleaf, cur, INST);
+                    if (INST && !active && t.imask) active = wf_ray_next_instance(kind, t, sv, st, p);
                     if (!active) {
                         wf_ray_end(kind, t, sv, st, p);
                         credit();
@@ -371,8 +383,9 @@ __global__ __launch_bounds__(kWfBlock, kTraceMinBlocks) void k_wf_trace(const Sc
                 const bool leaf_mode = lm != 0u && __popc(lm) * 4 >= __popc(nm) * kLeafBias;
                 if (leaf_mode ? has_leaf : want_node) {
                     const bool any = kind == TR_SHADOW;
-                    fin = leaf_mode ? wide_leaf_step(any, t, sv, rp.err, cur)
-                                    : wide_node_step(any, t, sv, stack, rp.err, cur);
+                    fin = leaf_mode ? wide_leaf_step(any, t, sv, rp.err, cur, INST)
+                                    : wide_node_step(any, t, sv, stack, rp.err, cur, INST);
+                    if (INST && fin && wf_ray_next_instance(kind, t, sv, st, p)) fin = false;
                 }
             } else if (active) {
                 fin = trav_step_binary(kind == TR_SHADOW, t, sv, stack, rp.err, cur);
@@ -502,9 +515,12 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
     }
     bool recorded = (flags & FL_RECORDED) != 0, rough_seen = (flags & FL_ROUGH) != 0;
     bool offered = (flags & FL_OFFERED) != 0;
-    if (st.cache && !done && rough_seen) {
-        // the vertex after the first rough one: cached paths end here with the cache's radiance,
-        // unbiased paths are offered one training record here and go on
+    if (st.cache && !done && rough_seen && bsdf_roughness(f) > kCacheRough) {
+        // the first rough vertex after a rough one: cached paths end here with the cache's
+        // radiance, unbiased paths are offered one training record here and go on.  Specular and
+        // near-specular vertices in between are traced through (their outgoing radiance is
+        // too directional for the network: a caustic seen on a diffuse floor through a glass
+        // sphere would be lost)
         if (!(flags & FL_UNBIASED)) {
             write_features(st, si, f, st.feat + (size_t)p * 96);
             st.q_cache[atomicAdd(&st.counts[12], 1u)] = p;
@@ -525,7 +541,7 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
             }
         }
     }
-    if (!done && bsdf_roughness(f) > 0.3f) rough_seen = true;
+    if (!done && bsdf_roughness(f) > kCacheRough) rough_seen = true;
     uint64_t ev_mis = 0, ev_main = 0;
     if (!done) {
         if (sv.nlight > 0) {

@@ -314,9 +314,14 @@ def uv_sphere(rings, segs):
 STRESS_SPHERE = (256, 512)   # rings, segments: 261,120 triangles per sphere
 
 
-def write_stress_scene(d, rings=STRESS_SPHERE[0], segs=STRESS_SPHERE[1], copies=8, seed=2, amplitude=0.1):
+def write_stress_scene(d, rings=STRESS_SPHERE[0], segs=STRESS_SPHERE[1], copies=8, seed=2, amplitude=0.1,
+                       instanced=False):
     """The material and divergence stress scene (see the module docstring); smaller `rings` and
-    `segs` give the same layout with coarser spheres (parity cases)."""
+    `segs` give the same layout with coarser spheres (parity cases).  instanced: the conductor
+    spheres are `copies` instances of one unit-sphere file (the loader's `instances` record:
+    mesh entry, translation, scale), written as stress_inst.scene / stress_inst.subject; their
+    world triangles are the file's scaled and moved in float32, so they differ from the plain
+    scene's by rounding."""
     os.makedirs(d, exist_ok=True)
     write_quads(os.path.join(d, "s_back.bin"), [((-1, -1, -1), (2, 0, 0), (0, 2, 0)),
                                                   ((-1, 1, -1), (2, 0, 0), (0, 0, 2))])
@@ -340,10 +345,19 @@ def write_stress_scene(d, rings=STRESS_SPHERE[0], segs=STRESS_SPHERE[1], copies=
         centres.append(c)
         alphas.append(float(rng.uniform(0.05, 0.5)))
     names = []
-    for k, c in enumerate(centres):
-        names.append(f"metal{k}")
-        write_bin(os.path.join(d, f"metal{k}.bin"), c + v * r, v, f, f)
-    with open(os.path.join(d, "stress.scene"), "w") as fh:
+    if instanced:
+        write_bin(os.path.join(d, "unit_sphere.bin"), v, v, f, f)
+        names = ["unit_sphere"] * copies
+    else:
+        for k, c in enumerate(centres):
+            names.append(f"metal{k}")
+            write_bin(os.path.join(d, f"metal{k}.bin"), c + v * r, v, f, f)
+    name = "stress_inst" if instanced else "stress"
+    inst = ""
+    if instanced:  # subject meshes come first in the mesh order: glass is 0, the spheres 1 ..
+        inst = "instances\t%d\n" % copies + "".join(
+            "%d\t%r %r %r\t%r\n" % (1 + k, *map(float, c), float(r)) for k, c in enumerate(centres))
+    with open(os.path.join(d, name + ".scene"), "w") as fh:
         fh.write(CAMERA_BOX + IDENTITY_SUBJECT + "0\n"
                  "5\ts_back\ts_floor\tbox_red\tbox_green\tbox_light\n"
                  "5\n"
@@ -353,13 +367,13 @@ def write_stress_scene(d, rings=STRESS_SPHERE[0], segs=STRESS_SPHERE[1], copies=
                  "L\tc\t0.1 0.7 0.1\t0\n"
                  "L\tc\t0 0 0\t0\n"
                  "1\t10 10 10\n"
-                 "1\t0.5 0.5 0.5\n")
-    with open(os.path.join(d, "stress.subject"), "w") as fh:
+                 "1\t0.5 0.5 0.5\n" + inst)
+    with open(os.path.join(d, name + ".subject"), "w") as fh:
         fh.write("0\n%d\tglass\t%s\n%d\n" % (1 + copies, "\t".join(names), 1 + copies))
         fh.write("G\tc\t1 1 1\tc\t1 1 1\t1.5\n")
         for a in alphas:
             fh.write("C\tc\t3.9 2.4 1.8\tc\t0.2 0.4 1.4\t%.6f\n" % a)
-    return "stress", "stress"
+    return name, name
 
 
 def random_triangles(n, seed=1):

@@ -84,7 +84,12 @@ def test_loader_errors(tmp_path, built_lib):
     open(b, "wb").write(raw)
     txt = open(os.path.join(d, "sphere.subject")).read()
     open(os.path.join(d, "sphere.subject"), "w").write(txt.replace("L\tc\t0.8 0.8 0.8", "L\ti\t0"))
-    assert _load_err(d, sc, sub) == 6                            # image texture -> UNSUPPORTED
+    assert _load_err(d, sc, sub) == 3                            # image texture without an image
+    img = txt.replace("L\tc\t0.8 0.8 0.8", "L\ti\t0").replace("0\n", "1\t0\ttex.jpg\n", 1)
+    open(os.path.join(d, "sphere.subject"), "w").write(img)
+    assert _load_err(d, sc, sub) == 2                            # missing image file -> IO
+    open(os.path.join(d, "tex.jpg"), "wb").write(b"\xff\xd8\xff\xe0" + bytes(60))
+    assert _load_err(d, sc, sub) == 6                            # not a PNG -> UNSUPPORTED
     open(os.path.join(d, "sphere.subject"), "w").write("0\n1\tsphere\n")
     assert _load_err(d, sc, sub) == 3                            # premature end of file
 
@@ -257,4 +262,53 @@ def test_loader_matches_reference_on_the_bench_scene(built_lib, tmp_path):
     assert _sha(s.camera()) == str(z["camera"])
     func, cdf = s.light_distribution()
     assert _sha(func) == str(z["light_func"]) and _sha(cdf) == str(z["light_cdf"])
+    ctx.close()
+
+
+def test_instances_grammar_extension(built_lib, tmp_path):
+    """`instances K` and per instance `meshIndex tx ty tz s` after the infinite-light record (no
+    counterpart in the reference): mesh entry meshIndex holds its file's triangles at p * s + t,
+    rounded in float32 as written; entries naming the same file share one prototype.  The scene's
+    triangle table is the flattened one (what the oracle and the flat BVH see), equal to the plain
+    stress scene's up to the rounding of where the placement happens.  Malformed records fail
+    with LTS_ERR_PARSE."""
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    d = str(tmp_path)
+    sc, sub = scenes.write_stress_scene(d, rings=16, segs=32)
+    si, ss = scenes.write_stress_scene(d, rings=16, segs=32, instanced=True)
+    ctx = lts.Context(-1)
+    plain = lts.Scene.parse(ctx, d, sc, sub, 64, 64)
+    tp, ip = plain.triangles(), plain.info
+    inst = lts.Scene.parse(ctx, d, si, ss, 64, 64)
+    ti, ii = inst.triangles(), inst.info
+    assert ii["instances"] == 8 and ii["prototypes"] == 1 and ip["instances"] == 0
+    assert ii["triangles"] == ip["triangles"] and ii["lights"] == ip["lights"]
+    np.testing.assert_allclose(ti, tp, atol=2e-7, rtol=0)
+    # every instanced triangle is the file's, scaled then moved, in float32
+    v, f = scenes.uv_sphere(16, 32)
+    v32 = v.astype(np.float32)
+    per = len(f)
+    glass = per  # mesh entry 0 (the glass sphere) comes first
+    lines = open(os.path.join(d, si + ".scene")).read().split("instances")[1].split("\n")[1:9]
+    for k, line in enumerate(lines):
+        m, t, s = line.split("\t")
+        t = np.array([np.float32(x) for x in t.split()], np.float32)
+        want = v32[f] * np.float32(s) + t
+        got = ti[glass + k * per: glass + (k + 1) * per]
+        assert int(m) == 1 + k and np.array_equal(got, want)
+    txt = open(os.path.join(d, si + ".scene")).read()
+    head, tail = txt.split("instances")
+    for bad in ("instances\t1\n14\t0 0 0\t1\n",     # mesh index out of range (14 entries)
+                "instances\t1\n13\t0 0 0\t1\n",     # the area light's mesh (emissive)
+                "instances\t2\n1\t0 0 0\t1\n1\t0 0 0\t1\n",  # the same entry twice
+                "instances\t1\n1\t0 0 0\t0\n",      # scale not > 0
+                "instances\t1\n1\t0 0\n"):          # premature end
+        open(os.path.join(d, "bad.scene"), "w").write(head + bad)
+        assert _load_err(d, "bad", ss) == 3, bad
+    # a subject mesh is instanced only under the identity subject transform
+    lines = txt.split("\n")
+    lines[1] = "0 0 0\t0 1 0\t0.5\t1"
+    open(os.path.join(d, "rot.scene"), "w").write("\n".join(lines))
+    assert _load_err(d, "rot", ss) == 3
     ctx.close()
