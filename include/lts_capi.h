@@ -66,8 +66,8 @@ int lts_obj_to_bin(const char* mesh_name);
  * reference's parseMesh does, core/FileIO.cuh:213-232), transforms subject meshes, builds the camera for a width x height film and
  * the light table, and uploads SoA tables to the device.  subject may be NULL or "".
  * Replaces parseScene (core/SceneLoader.cuh:195-360) and the init kernels of
- * core/SceneLoader_kernels.cu:8-111.  Image textures ('i') are rejected with
- * LTS_ERR_UNSUPPORTED. */
+ * core/SceneLoader_kernels.cu:8-111.  Image textures ('i') load PNG files in the fixed mode of
+ * lts_scene_get_image; other image formats and interlaced PNGs give LTS_ERR_UNSUPPORTED. */
 int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char* subject,
                    int32_t width, int32_t height);
 
@@ -76,6 +76,7 @@ typedef struct {
     int32_t width, height;
     int32_t max_mesh_triangles; /* largest mesh: bounds the reference's Morton launch */
     int32_t instances, prototypes; /* the `instances` record: instanced mesh entries, their files */
+    int32_t images;                /* image textures */
 } lts_scene_info;
 int lts_scene_info_get(lts_ctx* ctx, lts_scene_info* out);
 
@@ -86,6 +87,20 @@ int lts_scene_info_get(lts_ctx* ctx, lts_scene_info* out);
 int lts_scene_get_triangles(lts_ctx* ctx, float* out_p9);
 int lts_scene_get_camera(lts_ctx* ctx, float* out23);
 int lts_scene_get_light_distribution(lts_ctx* ctx, float* func, float* cdf);
+
+/* Image textures of the loaded scene, in the reference's image order (subject images first):
+ * the fixed mode of ImageTexture / Mipmap (materials/textures/ImageTexture.cuh:13-28,
+ * Mipmap.cuh:34-73, Mipmap_kernel.cu:39-73), whose reference storage is undefined (its
+ * BlockedArray shares rows and writes past its allocation, core/MemoryHelper.cuh:86-100).  PNG
+ * files only (the reference decodes through stb_image); texel = (c / 255)^2.2 in float, rows
+ * flipped so v = 0 is the bottom row; floor(log2(max(w, h))) levels (at least one), level l the
+ * 2 x 2 box mean of level l - 1 with black outside.  wh_levels[3] receives the level's width,
+ * height and the image's level count; rgb (NULL or 3 w h floats) its texels, row-major. */
+int lts_scene_get_image(lts_ctx* ctx, int32_t image, int32_t level, int32_t* wh_levels, float* rgb);
+/* n lookups of one image texture on the device (Mipmap::lookUp at the reference's fixed width
+ * 0.01, Mipmap.cuh:61-72, trilinear between the two levels around log2 of the width):
+ * st[2n] texture coordinates in, rgb[3n] out; host buffers. */
+int lts_debug_image_lookup(lts_ctx* ctx, int32_t image, const float* st, int32_t n, float* rgb);
 
 /* ---------------------------------------------------------------- LBVH */
 /* LTS_BVH_REFERENCE: the reference's build exactly (acceleration/BVH.cuh:77-452): Morton

@@ -39,7 +39,8 @@ EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_rea
            "lts_debug_trace_get", "lts_set_option", "lts_debug_umma_probe", "lts_mlp_init", "lts_mlp_set_params",
            "lts_mlp_get_params", "lts_mlp_forward", "lts_mlp_train_step", "lts_mlp_forward_device_async",
            "lts_mlp_train_step_device_async", "lts_render_views", "lts_autotune_views", "lts_obj_to_bin",
-           "lts_debug_wait_timeout", "lts_debug_kat", "lts_intersect"]
+           "lts_debug_wait_timeout", "lts_debug_kat", "lts_intersect", "lts_scene_get_image",
+           "lts_debug_image_lookup"]
 
 
 class LtsError(RuntimeError):
@@ -57,7 +58,7 @@ class AppParams(ctypes.Structure):
 class SceneInfo(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in ("triangles", "meshes", "subject_meshes", "materials", "lights",
                                                "area_light_meshes", "has_infinite", "width", "height",
-                                               "max_mesh_triangles", "instances", "prototypes")]
+                                               "max_mesh_triangles", "instances", "prototypes", "images")]
 
 
 class BvhDump(ctypes.Structure):
@@ -139,6 +140,8 @@ def library():
             "lts_debug_wait_timeout": (I, [P, I]),
             "lts_debug_kat": (I, [P, I, P, I, P]),
             "lts_intersect": (I, [P, P, I, I, P, P]),
+            "lts_scene_get_image": (I, [P, I, I, P, P]),
+            "lts_debug_image_lookup": (I, [P, I, P, I, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -266,6 +269,22 @@ class Scene:
     def simple_intersect(self, o, d, tmax):
         """Scene::simpleIntersect (acceleration/Scene.cuh:30-32): True where a hit lies before tmax."""
         return self._query(o, d, tmax, True)[0] == 1
+
+    def image(self, index, level=0):
+        """Level `level` of image texture `index` (the fixed mode's pyramid): (h, w, 3) float32,
+        row 0 the bottom row, and the image's level count."""
+        wh = np.zeros(3, np.int32)
+        self.ctx.check(self.ctx.lib.lts_scene_get_image(self.ctx.h, index, level, _ptr(wh), None))
+        out = np.empty(int(wh[0]) * int(wh[1]) * 3, np.float32)
+        self.ctx.check(self.ctx.lib.lts_scene_get_image(self.ctx.h, index, level, _ptr(wh), _ptr(out)))
+        return out.reshape(int(wh[1]), int(wh[0]), 3), int(wh[2])
+
+    def image_lookup(self, index, st):
+        """Mipmap::lookUp of image texture `index` on the device at (n, 2) texture coordinates."""
+        st = np.ascontiguousarray(st, np.float32).reshape(-1, 2)
+        out = np.empty((len(st), 3), np.float32)
+        self.ctx.check(self.ctx.lib.lts_debug_image_lookup(self.ctx.h, index, _ptr(st), len(st), _ptr(out)))
+        return out
 
     def create_bvh_tree(self, mode=BVH_SORTED, dump=True):
         """LBVH of the scene; returns the dump dict (codes, ids, node arrays) when dump."""

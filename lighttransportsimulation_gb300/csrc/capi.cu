@@ -316,6 +316,7 @@ int lts_scene_info_get(lts_ctx* ctx, lts_scene_info* out) {
     out->max_mesh_triangles = s.max_mesh_triangles();
     out->instances = (int32_t)s.instances.size();
     out->prototypes = (int32_t)s.proto_soup.size();
+    out->images = (int32_t)s.images.size();
     return LTS_OK;
 }
 
@@ -724,6 +725,41 @@ int lts_debug_kat(lts_ctx* ctx, int32_t fn, const float* in, int32_t n, float* o
     dev_free(d);
     if (!msg.empty()) return fail(ctx, LTS_ERR_CUDA, msg);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "known-answer check");
+    return LTS_OK;
+}
+
+int lts_scene_get_image(lts_ctx* ctx, int32_t image, int32_t level, int32_t* wh_levels, float* rgb) {
+    if (!ctx || !wh_levels) return fail(ctx, LTS_ERR_ARG, "null argument");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    const std::vector<HostImage>& ims = ctx->scene.images;
+    if (image < 0 || image >= (int32_t)ims.size()) return fail(ctx, LTS_ERR_ARG, "image index out of range");
+    const HostImage& im = ims[(size_t)image];
+    if (level < 0 || level >= im.levels) return fail(ctx, LTS_ERR_ARG, "level out of range");
+    wh_levels[0] = im.w[(size_t)level];
+    wh_levels[1] = im.h[(size_t)level];
+    wh_levels[2] = im.levels;
+    if (rgb) memcpy(rgb, im.rgb[(size_t)level].data(), im.rgb[(size_t)level].size() * sizeof(float));
+    return LTS_OK;
+}
+
+int lts_debug_image_lookup(lts_ctx* ctx, int32_t image, const float* st, int32_t n, float* rgb) {
+    if (!ctx) return LTS_ERR_ARG;
+    if (n < 0 || (n > 0 && (!st || !rgb)) || n > (1 << 24)) return fail(ctx, LTS_ERR_ARG, "bad lookup request");
+    if (ctx->device < 0) return fail(ctx, LTS_ERR_STATE, "host-only context");
+    if (!ctx->loaded) return fail(ctx, LTS_ERR_STATE, "no scene loaded");
+    if (image < 0 || image >= (int32_t)ctx->scene.images.size()) return fail(ctx, LTS_ERR_ARG, "image index out of range");
+    if (n == 0) return LTS_OK;
+    CK(cudaSetDevice(ctx->device));
+    float* d = nullptr;
+    CK(dev_alloc((void**)&d, 20 * (size_t)n));
+    cudaError_t e = cudaMemcpyAsync(d, st, 8 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+    std::string msg = e == cudaSuccess ? ctx->tracer->image_lookup(image, d, n, d + 2 * (size_t)n, ctx->stream) : "";
+    if (e == cudaSuccess && msg.empty())
+        e = cudaMemcpyAsync(rgb, d + 2 * (size_t)n, 12 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && msg.empty()) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(d);
+    if (!msg.empty()) return fail(ctx, LTS_ERR_CUDA, msg);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "image lookup");
     return LTS_OK;
 }
 

@@ -77,14 +77,37 @@ __device__ __forceinline__ V3 vabs(V3 a) { return v3(xabs(a.x), xabs(a.y), xabs(
 __device__ __forceinline__ real comp(V3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
 __device__ __forceinline__ V3 face_towards(V3 n, V3 v) { return dot(n, v) < 0 ? -n : n; }
 
-// a*b - c*d with Kahan's FMA algorithm: within 1.5 ulp, and in nearly every case the correctly
-// rounded result -- which is what the reference's double-precision cross product rounds to
-// (Geometry.cuh:76-83: exact double products, one double subtraction, one float rounding).
+// a*b - c*d as the reference's cross product rounds it (Geometry.cuh:76-83: exact products in
+// double, one double subtraction, one rounding to float), which is the correctly rounded value
+// except when the double subtraction lands within 2^-53 of a float midpoint.  In float: both
+// products split exactly into value + error (FMA), the difference of the values exactly into
+// s + t (TwoSum, Knuth), and s + (t + (e1 - e2)) rounded once more; the inner sum is below half
+// an ulp of s, so the result is the correctly rounded one unless the exact value lies within
+// ~2^-24 ulp of a midpoint (none in 60,000 random and cancelling cases against exact rational
+// arithmetic).  13 operations.
 __device__ __forceinline__ real diff_prod(real a, real b, real c, real d) {
+#if LTS_FP64
+    return a * b - c * d;
+#else
+    const real p1 = a * b, e1 = xfma(a, b, -p1);
+    const real p2 = c * d, e2 = xfma(c, d, -p2);
+    const real s = p1 - p2;
+    const real bb = s - p1;
+    const real t = (p1 - (s - bb)) + (-p2 - bb);
+    return s + (t + (e1 - e2));
+#endif
+}
+// The same within 1.5 ulp in 4 operations (Kahan: w = cd; (ab - w) + (w - cd)), misrounding about
+// 15 % of random cases: the traversal's triangle tests use it, and the winning triangle's values
+// are recomputed with diff_prod (hit_exact).
+__device__ __forceinline__ real diff_prod_fast(real a, real b, real c, real d) {
     const real w = c * d;
     const real e = xfma(-c, d, w);
     const real f = xfma(a, b, -w);
     return f + e;
+}
+__device__ __forceinline__ V3 cross_fast(V3 a, V3 b) {
+    return v3(diff_prod_fast(a.y, b.z, a.z, b.y), diff_prod_fast(a.z, b.x, a.x, b.z), diff_prod_fast(a.x, b.y, a.y, b.x));
 }
 __device__ __forceinline__ V3 cross(V3 a, V3 b) {
     return v3(diff_prod(a.y, b.z, a.z, b.y), diff_prod(a.z, b.x, a.x, b.z), diff_prod(a.x, b.y, a.y, b.x));

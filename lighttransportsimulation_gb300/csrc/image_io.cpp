@@ -398,7 +398,9 @@ std::string decode_png_file(const std::string& path, int* w, int* h, std::vector
 
 void build_pyramid(int w, int h, const std::vector<uint8_t>& rgb8, int wrap, HostImage* img) {
     float lut[256];
-    for (int c = 0; c < 256; ++c) lut[c] = powf((float)c / 255.0f, 2.2f);
+    // (c / 255)^2.2 correctly rounded to float (pow in double, then rounded once): what glibc's
+    // powf gives stb_image for all 256 values, and the same on every host
+    for (int c = 0; c < 256; ++c) lut[c] = (float)std::pow((double)((float)c / 255.0f), (double)2.2f);
     int levels = (int)log2f(fmaxf((float)w, (float)h));  // CreateMipMap, Mipmap_kernel.cu:45
     if (levels < 1) levels = 1;
     img->wrap = wrap;

@@ -32,8 +32,8 @@ struct HostImage {
     std::vector<std::vector<float>> rgb;  // [levels][3 w h]
 };
 
-// The fixed mode's pyramid from decoded 8-bit RGB (top row first): texel = (c / 255)^2.2 in
-// float (stbi_loadf's default LDR-to-linear conversion), rows flipped; floor(log2(max(w, h)))
+// The fixed mode's pyramid from decoded 8-bit RGB (top row first): texel = (c / 255)^2.2 rounded
+// to float (stbi_loadf's default LDR-to-linear conversion), rows flipped; floor(log2(max(w, h)))
 // levels (at least one), level l of max(1, w >> l) x max(1, h >> l) texels, each the mean of the
 // 2 x 2 texels below it with black outside (pyramidInitKernel's box filter over the whole level;
 // the reference's kernel only fills 16 >> l texels per axis).

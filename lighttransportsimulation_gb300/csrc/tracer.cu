@@ -160,6 +160,17 @@ __global__ void k_rebase_wide(const WideNode* __restrict__ src, int count, uint3
     dst[k] = w;
 }
 
+// Image-texture lookups at given texture coordinates (lts_debug_image_lookup).
+__global__ void k_image_lookup(const SceneView sv, int idx, const float* __restrict__ st, int n,
+                               float* __restrict__ rgb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Spec c = img_lookup(sv, idx, st[2 * i], st[2 * i + 1]);
+    rgb[3 * i] = c.r;
+    rgb[3 * i + 1] = c.g;
+    rgb[3 * i + 2] = c.b;
+}
+
 // Known-answer check: one float device function per record (LTS_KAT_* layouts of lts_capi.h).
 __global__ void k_debug_kat(int fn, const float* __restrict__ in, int n, float* __restrict__ out) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -261,6 +272,7 @@ __global__ __launch_bounds__(kThreads) void k_intersect(const SceneView sv, int 
     Work wk{0u, 0u};
     const int h = sv.ninst ? traverse<ANY, true>(sv, nleaf, r, tmax, bu, bv, binv, s_stack + threadIdx.x, err, wk)
                            : traverse<ANY>(sv, nleaf, r, tmax, bu, bv, binv, s_stack + threadIdx.x, err, wk);
+    if (!ANY && h >= 0) hit_exact(sv, h, r.o, r.d, tmax, bu, bv, binv);
     prim[i] = ANY ? (h > 0 ? 1 : 0) : h;
     if (tout) tout[i] = (!ANY && h >= 0) ? (float)tmax : INFINITY;
 }
@@ -729,6 +741,13 @@ std::string Tracer::build_instanced(uint64_t key, cudaStream_t s, uint32_t* d_er
     itri_n_ = (int)tri_base;
     ilevels_ = levels;
     ikey_ = key;
+    return "";
+}
+
+std::string Tracer::image_lookup(int idx, const float* d_st, int n, float* d_rgb, cudaStream_t s) {
+    if (!view_.images) return "no scene on the device";
+    if (n > 0) k_image_lookup<<<(n + 127) / 128, 128, 0, s>>>(view_, idx, d_st, n, d_rgb);
+    TRY(cudaGetLastError());
     return "";
 }
 

@@ -208,6 +208,9 @@ class Tracer {
     std::string intersect(const Lbvh& bvh, const float4* d_rays, int n, int any, int32_t* d_prim, float* d_t,
                           cudaStream_t s, uint32_t* d_err);
 
+    // n image-texture lookups (Mipmap::lookUp) of image `idx` at d_st[2n] into d_rgb[3n].
+    std::string image_lookup(int idx, const float* d_st, int n, float* d_rgb, cudaStream_t s);
+
     // Device bytes of the render BVH's nodes and triangles last used (two-level or flat).
     size_t render_bvh_bytes = 0;
 

@@ -146,17 +146,19 @@ __device__ __forceinline__ int4 prim_word(const SceneView& sv, int prim) {
 
 // ------------------------------------------------------------------ triangle tests
 // Triangle::intersect test part (shapes/Triangle.cu:94-128).
+// EXACT: the reference's cross products (diff_prod); else the faster ones the traversal uses.
+template <bool EXACT = true>
 __device__ __forceinline__ bool tri_test(V3 p0, V3 p1, V3 p2, V3 o, V3 d, real tmax, real& t_out, real& u_out,
                                          real& v_out, real& inv_out) {
     const V3 e1 = p1 - p0, e2 = p2 - p0;
-    const V3 pv = cross(d, e2);
+    const V3 pv = EXACT ? cross(d, e2) : cross_fast(d, e2);
     const real det = dot(e1, pv);
     if (det == 0) return false;
     const real inv = xrcp(det);  // == (real)(1.0 / (double)det)
     const V3 tv = o - p0;
     const real u = inv * dot(tv, pv);
     if (u < kShadowEps || u >= kOneMinusEpsUp) return false;
-    const V3 qv = cross(tv, e1);
+    const V3 qv = EXACT ? cross(tv, e1) : cross_fast(tv, e1);
     const real v = inv * dot(d, qv);
     if (v < kShadowEps || u + v >= kOneMinusEpsUp) return false;
     const real t = inv * dot(e2, qv);
@@ -168,16 +170,17 @@ __device__ __forceinline__ bool tri_test(V3 p0, V3 p1, V3 p2, V3 o, V3 d, real t
     return true;
 }
 // Triangle::simpleIntersect (shapes/Triangle.cu:50-84): swapped edges, grown bound.
+template <bool EXACT = true>
 __device__ __forceinline__ bool tri_test_shadow(V3 p0, V3 p1, V3 p2, V3 o, V3 d, real tmax) {
     const V3 e1 = p1 - p0, e2 = p2 - p0;
-    const V3 pv = cross(d, e1);
+    const V3 pv = EXACT ? cross(d, e1) : cross_fast(d, e1);
     const real det = dot(e2, pv);
     if (det == 0) return false;
     const real inv = xrcp(det);
     const V3 tv = o - p0;
     const real u = inv * dot(tv, pv);
     if (u < kShadowEps || u >= kOnePlusEpsUp) return false;
-    const V3 qv = cross(tv, e2);
+    const V3 qv = EXACT ? cross(tv, e2) : cross_fast(tv, e2);
     const real v = inv * dot(d, qv);
     if (v < kShadowEps || u + v >= kOnePlusEpsUp) return false;
     const real t = inv * dot(e1, qv);
@@ -364,6 +367,27 @@ __device__ __forceinline__ bool tri_test_wt(V3 p0, V3 p1, V3 p2, const TraceRay&
 // in the watertight mode so that only the hit test differs).
 __device__ __forceinline__ real mt_inv_det(V3 p0, V3 p1, V3 p2, V3 d) { return xrcp(dot(p1 - p0, cross(d, p2 - p0))); }
 
+// The closest hit's barycentrics, 1 / det and distance with the reference's arithmetic: the
+// traversal found triangle `prim` with the faster cross products; its test is repeated once with
+// the exact ones (diff_prod), so the surface interaction is built from the reference's values.
+// A hit the exact test rejects (within rounding of an edge) keeps the traversal's values.  The
+// watertight test's values are its own.
+__device__ __forceinline__ void hit_exact(const SceneView& sv, int prim, V3 o, V3 d, real& t, real& u, real& v,
+                                          real& inv) {
+#if !LTS_FP64
+    if (sv.watertight) return;
+    const float4* q = sv.prim_v + 3 * (size_t)prim;
+    const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    real t2, u2, v2, inv2;
+    if (tri_test<true>(v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), o, d, INFINITY, t2, u2, v2, inv2)) {
+        t = t2;
+        u = u2;
+        v = v2;
+        inv = inv2;
+    }
+#endif
+}
+
 // The hit word of a leaf triangle: its primitive id and shade class from the triangle (top-level
 // tree), or, inside instance `ii` of a two-level BVH, the instance's first primitive plus the
 // triangle's index in its prototype and the instance's class; then 1 / det (make_si's dpdu scale)
@@ -394,8 +418,8 @@ __device__ __forceinline__ bool leaf_test(const bool any, const float4* __restri
         best = hit_word(a, b, inst, ii, insts, binv);
         return false;
     }
-    if (any) return tri_test_shadow(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax);
-    if (tri_test(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax, t, u, v, inv)) {
+    if (any) return tri_test_shadow<false>(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax);
+    if (tri_test<false>(f4v(a), f4v(b), f4v(c), r.o, r.d, tmax, t, u, v, inv)) {
         tmax = t;
         bu = u;
         bv = v;
@@ -855,12 +879,14 @@ __device__ __forceinline__ bool scene_intersect(const SceneView& sv, int nleaf, 
     const TraceRay r = make_trace_ray(o, d);
     real bu = 0, bv = 0, binv = 0;
 #if !LTS_FP64
-    const int prim = sv.ninst ? traverse<false, true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk)
-                              : traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk);
+    // one traversal loop for both BVH forms (without instances the instance mask stays empty), so
+    // the megakernel inlines a single copy
+    const int prim = traverse<false, true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk);
 #else
     const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk);
 #endif
     if (prim < 0) return false;
+    hit_exact(sv, prim, o, d, tmax, bu, bv, binv);
     make_si(sv, prim, d, bu, bv, binv, si);
     return true;
 }
@@ -869,9 +895,10 @@ __device__ __forceinline__ bool scene_occluded(const SceneView& sv, int nleaf, V
     const TraceRay r = make_trace_ray(o, d);
     real bu, bv, binv;
 #if !LTS_FP64
-    if (sv.ninst) return traverse<true, true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk) > 0;
-#endif
+    return traverse<true, true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk) > 0;
+#else
     return traverse<true>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk) > 0;
+#endif
 }
 
 // ------------------------------------------------------------------ rays from interactions
@@ -1004,7 +1031,7 @@ __device__ __forceinline__ Spec img_bilerp(const SceneView& sv, const DevImage* 
 }
 // Mipmap::lookUp at the fixed width 0.01 (EVALUATION_WIDTH), whose level coordinate the loader
 // computes once per image.
-__device__ Spec img_lookup(const SceneView& sv, int idx, real st0, real st1) {
+__device__ __noinline__ Spec img_lookup(const SceneView& sv, int idx, real st0, real st1) {
     const DevImage* im = sv.images + idx;
     const real lod = __ldg(&im->lod);
     const int levels = __ldg(&im->levels);

@@ -469,7 +469,9 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
     SI si;
     if (hit) {
         const float4 h = st.huvi[p];
-        make_si(sv, prim, rd, h.x, h.y, h.z, si);
+        real ht = h.w, hu = h.x, hv = h.y, hinv = h.z;
+        hit_exact(sv, prim, ro, rd, ht, hu, hv, hinv);
+        make_si(sv, prim, rd, hu, hv, hinv, si);
     }
     if (bounce == 0 || specular) {
         if (hit) {
@@ -689,11 +691,13 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_finalize(const SceneView sv, co
             if (RECORD) fnv_mix(sig, 0x200000000ull + (uint64_t)st.mis_hit[p]);
             float4 c = st.ld_mis[p];
             if (c.w == 2.f) {  // the BSDF ray landed on the sampled area light (IntegratorHelper.cuh:225-243)
-                const float4 d = st.mis_d[p], fv = st.mis_fv[p], x = st.mis_x[p];
+                const float4 d = st.mis_d[p], fv = st.mis_fv[p], x = st.mis_x[p], mo = st.mis_o[p];
                 const V3 wi = v3(d.x, d.y, d.z);
                 const DevLight& Lt = sv.lights[__float_as_int(x.y)];
                 SI lit;
-                make_si(sv, st.mis_hit[p] - 1, wi, c.x, c.y, c.z, lit);
+                real ht = 0, hu = c.x, hv = c.y, hinv = c.z;
+                hit_exact(sv, st.mis_hit[p] - 1, v3(mo.x, mo.y, mo.z), wi, ht, hu, hv, hinv);
+                make_si(sv, st.mis_hit[p] - 1, wi, hu, hv, hinv, lit);
                 const Spec Li = dot(lit.n, -wi) > 0.f ? Spec{Lt.L[0], Lt.L[1], Lt.L[2]} : spec(0.0f);
                 Spec cs = spec(0.0f);
                 const bool add = !is_black(Li);

@@ -300,6 +300,7 @@ struct SI {
     V p, perr, wo, n;
     V dpdu, dpdv, sn, sdpdu;
     V dpdx, dpdy;
+    float tu = 0, tv = 0;  // uvHit (Triangle.cu:160)
     int prim = -1;
 };
 
@@ -342,6 +343,8 @@ static bool tri_intersect(const Scene& sc, int prim, V o, V d, float ray_tmax, f
     const float zs = fabsf(w * p0.z) + fabsf(u * p1.z) + fabsf(v * p2.z);
     si->perr = mk(xs, ys, zs) * gammaf(7);
     si->p = p0 * w + p1 * u + p2 * v;
+    si->tu = uv0x * w + uv1x * u + uv2x * v;
+    si->tv = uv0y * w + uv1y * u + uv2y * v;
     si->wo = -d;
     si->dpdu = dpdu;
     si->dpdv = dpdv;
@@ -532,8 +535,44 @@ static float turbulence(V p, V dx, V dy, float omega, int maxo, uint64_t* sig) {
 static const float kMarble[10][3] = {{.58f, .58f, .6f}, {.58f, .58f, .6f}, {.58f, .58f, .6f}, {.5f, .5f, .5f},
                                      {.6f, .59f, .58f}, {.58f, .58f, .6f}, {.58f, .58f, .6f}, {.2f, .2f, .33f},
                                      {.58f, .58f, .6f}, {.58f, .58f, .6f}};
-static S texture(const lts::HostTexture& t, const SI& si, uint64_t* sig) {
+// Image textures in the fixed mode (texel / Mipmap::triangle / Mipmap::lookUp, Mipmap.cuh:14-73,
+// with the repeat wrap taken into the level and the coarsest-level read fixed), over the loader's
+// row-major pyramid.
+static S img_texel(const lts::HostImage& im, int l, int s, int t) {
+    const int w = im.w[l], h = im.h[l];
+    if (im.wrap == 0) {
+        s %= w;
+        if (s < 0) s += w;
+        t %= h;
+        if (t < 0) t += h;
+    } else if (im.wrap == 2) {
+        s = s < 0 ? 0 : (s > w - 1 ? w - 1 : s);
+        t = t < 0 ? 0 : (t > h - 1 ? h - 1 : t);
+    } else if (s < 0 || s >= w || t < 0 || t >= h) {
+        return S{0, 0, 0};
+    }
+    const float* q = &im.rgb[l][3 * ((size_t)t * w + s)];
+    return S{q[0], q[1], q[2]};
+}
+static S img_bilerp(const lts::HostImage& im, int l, float st0, float st1) {
+    l = l < 0 ? 0 : (l > im.levels - 1 ? im.levels - 1 : l);
+    const float s = st0 * (float)im.w[l] - 0.5f, t = st1 * (float)im.h[l] - 0.5f;
+    const int s0 = (int)floorf(s), t0 = (int)floorf(t);
+    const float ds = s - (float)s0, dt = t - (float)t0;
+    return img_texel(im, l, s0, t0) * ((1 - ds) * (1 - dt)) + img_texel(im, l, s0, t0 + 1) * ((1 - ds) * dt) +
+           img_texel(im, l, s0 + 1, t0) * (ds * (1 - dt)) + img_texel(im, l, s0 + 1, t0 + 1) * (ds * dt);
+}
+static S img_lookup(const lts::HostImage& im, float st0, float st1) {
+    if (im.lod < 0) return img_bilerp(im, 0, st0, st1);
+    if (im.lod >= (float)(im.levels - 1)) return img_texel(im, im.levels - 1, 0, 0);
+    const int il = (int)floorf(im.lod);
+    const float delta = im.lod - (float)il;
+    return img_bilerp(im, il, st0, st1) * (1 - delta) + img_bilerp(im, il + 1, st0, st1) * delta;
+}
+
+static S texture(const Scene& sc, const lts::HostTexture& t, const SI& si, uint64_t* sig) {
     switch (t.kind) {
+        case lts::TEX_IMAGE: return img_lookup(sc.h->images[(size_t)t.v[0]], si.tu, si.tv);
         case lts::TEX_FBM: return sp(fbm(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0], sig));
         case lts::TEX_WRINKLED: return sp(turbulence(si.p, si.dpdx, si.dpdy, t.v[1], (int)t.v[0], sig));
         case lts::TEX_MARBLE: {
@@ -834,7 +873,7 @@ static bool make_bsdf(const Scene& sc, const SI& si, Bsdf* f, uint64_t* sig) {  
     f->ts = cross(f->ns, f->ss);
     switch (m.kind) {
         case lts::MAT_MATTE: {
-            const S kd = texture(m.tex[0], si, sig);
+            const S kd = texture(sc, m.tex[0], si, sig);
             if (!black(kd)) {
                 f->R = kd;
                 f->lobe = m.extra == 0 ? LAMBERT : OREN;
@@ -846,7 +885,7 @@ static bool make_bsdf(const Scene& sc, const SI& si, Bsdf* f, uint64_t* sig) {  
         }
         case lts::MAT_GLASS: {
             f->eta = m.extra;
-            const S r = texture(m.tex[0], si, sig), t = texture(m.tex[1], si, sig);
+            const S r = texture(sc, m.tex[0], si, sig), t = texture(sc, m.tex[1], si, sig);
             if (black(r) && black(t)) break;
             f->R = r;
             f->T = t;
@@ -855,7 +894,7 @@ static bool make_bsdf(const Scene& sc, const SI& si, Bsdf* f, uint64_t* sig) {  
             break;
         }
         case lts::MAT_MIRROR: {
-            const S r = texture(m.tex[0], si, sig);
+            const S r = texture(sc, m.tex[0], si, sig);
             if (black(r)) break;
             f->R = r;
             f->lobe = SREFL;
@@ -863,7 +902,7 @@ static bool make_bsdf(const Scene& sc, const SI& si, Bsdf* f, uint64_t* sig) {  
             break;
         }
         case lts::MAT_METAL: {
-            f->k = texture(m.tex[0], si, sig);
+            f->k = texture(sc, m.tex[0], si, sig);
             f->eta3 = S{m.tex[1].v[0], m.tex[1].v[1], m.tex[1].v[2]};
             f->R = sp(1.0f);
             f->alpha = m.extra;

@@ -68,6 +68,18 @@ def write_shipped(d):
     return digest
 
 
+def write_kernel_box(d):
+    """Recreates the reference's image-texture scene (res/kernel_box_scene) under d from
+    tests/golden/kernel_box_inputs.npz; returns (root, scene, subject) as lts_load_scene takes them."""
+    z = np.load(os.path.join(GOLDEN, "kernel_box_inputs.npz"))
+    for k in z.files:
+        rel = k[4:].replace("__", "/")
+        os.makedirs(os.path.join(d, os.path.dirname(rel)), exist_ok=True)
+        with open(os.path.join(d, rel), "wb") as fh:
+            fh.write(z[k].tobytes())
+    return d, "res/kernel_box_scene/kernel", ""
+
+
 @pytest.fixture(scope="session")
 def scene_dirs(tmp_path_factory):
     """Generated parity scenes and the reference's shipped scenes, checked against the digests

@@ -18,6 +18,12 @@ changed generator from a changed renderer.  Usage (from the repository root):
     oracle/ref/build_ref.sh && python tests/golden/make_golden.py
     python tests/golden/make_golden.py shipped /path/to/reference   # the shipped scenes (SHIPPED)
     python tests/golden/make_golden.py digests                      # the bench scene's digests
+    python tests/golden/make_golden.py kernel_box /path/to/reference  # the image-texture scene's inputs
+
+kernel_box_inputs.npz holds the input files of the reference's own image-texture scene
+(res/kernel_box_scene: a 64 x 64 PNG on a box); the reference cannot render it reproducibly (its
+texel storage is undefined), so only its inputs are stored, and the tests compare the renderer
+with the oracle's port and numpy restatement of the fixed mode.
 """
 import hashlib
 import os
@@ -155,7 +161,23 @@ def make_digests():
     print("digest_displaced ok")
 
 
+KERNEL_BOX_FILES = ["res/kernel_box_scene/kernel.scene", "res/kernel_box_scene/kernel.png",
+                    "res/kernel_box_scene/kernelBox_box.bin", "res/kernel_box_scene/kernelBox_light.bin"]
+
+
+def make_kernel_box(reference_root):
+    files = {}
+    for rel in KERNEL_BOX_FILES:
+        with open(os.path.join(reference_root, rel), "rb") as fh:
+            files[shipped_key(rel)] = np.frombuffer(fh.read(), np.uint8)
+    np.savez_compressed(os.path.join(OUT, "kernel_box_inputs.npz"), **files)
+    print("kernel_box_inputs ok")
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "kernel_box":
+        make_kernel_box(sys.argv[2] if len(sys.argv) > 2 else "/root/reference")
+        return
     if not os.path.exists(REF):
         sys.exit("oracle/_ref/lts_ref is missing: run oracle/ref/build_ref.sh first")
     if len(sys.argv) > 1 and sys.argv[1] == "digests":
