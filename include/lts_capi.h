@@ -163,6 +163,12 @@ int lts_bvh_build_noalloc(const float* d_tri_p9, int32_t n, int32_t mode, int32_
 #define LTS_INTEGRATOR_MEGAKERNEL 0 /* one thread per pixel, all spp and bounces        */
 #define LTS_INTEGRATOR_WAVEFRONT 1  /* generate / extend / shade / shadow / film queues  */
 #define LTS_INTEGRATOR_FP64 2       /* the megakernel in double: FP64 oracle renders      */
+/* Bidirectional path tracing (the reference's disabled BidirectionalPathIntegrator,
+ * intergrators/BidirectionalPathIntegrator.cuh:285-660, built as PBRT v3 states the algorithm):
+ * every connection of a camera and a light subpath, MIS-weighted; light-to-camera connections are
+ * splatted and added at lts_film_get.  Area and point lights only (LTS_ERR_UNSUPPORTED with an
+ * infinite light), max_bounce <= 8, no record mode, no Russian roulette. */
+#define LTS_INTEGRATOR_BDPT 3
 
 typedef struct {
     int32_t spp, max_bounce, rr_start;
@@ -264,6 +270,10 @@ int lts_autotune_views(lts_ctx* ctx, const lts_view* views, int32_t n, const lts
  *                             collapsed by the SAH-optimal choice of children; 2 the same tree
  *                             collapsed greedily (largest child opened first); 0 the LBVH itself,
  *                             collapsed greedily
+ *   "bdpt_strategy"           bidirectional integrator: 10000 (default) every strategy with its MIS
+ *                             weight; 100 s + t renders the one strategy of s light and t camera
+ *                             vertices unweighted (a debugging view: each strategy alone estimates
+ *                             the paths it can sample)
  *   "two_level_bvh"           scenes with an `instances` record: 1 (default) one 8-wide tree per
  *                             instanced mesh file (prototype) under a top-level tree over the
  *                             other triangles, each instance entered with its ray moved to object

@@ -29,6 +29,7 @@ BVH_SORTED = 1
 INTEGRATOR_MEGAKERNEL = 0
 INTEGRATOR_WAVEFRONT = 1
 INTEGRATOR_FP64 = 2
+INTEGRATOR_BDPT = 3
 
 # Every symbol include/lts_capi.h declares.
 EXPORTS = ["lts_create", "lts_destroy", "lts_last_error", "lts_stream", "lts_read_app_params", "lts_load_scene",

@@ -659,6 +659,9 @@ int lts_set_option(lts_ctx* ctx, const char* key, int64_t value) {
     } else if (!strcmp(key, "render_bvh")) {
         if (value < 0 || value > 2) return fail(ctx, LTS_ERR_ARG, "render_bvh must be 0, 1 or 2");
         ctx->tracer->render_bvh = (int)value;
+    } else if (!strcmp(key, "bdpt_strategy")) {
+        if (value > 10000) return fail(ctx, LTS_ERR_ARG, "bdpt_strategy must be 0..9999, or 10000 for all");
+        ctx->tracer->bdpt_strategy = value == 10000 ? -1 : (int)value;
     } else if (!strcmp(key, "two_level_bvh")) {
         if (value > 1) return fail(ctx, LTS_ERR_ARG, "two_level_bvh must be 0 or 1");
         ctx->tracer->two_level = (int)value;

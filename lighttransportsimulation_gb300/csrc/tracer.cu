@@ -37,20 +37,41 @@ namespace {
 }  // namespace lts
 
 #include "megakernel.cuh"
+#include "bdpt.cuh"
 
 namespace lts {
 namespace {
 
 // Camera::getRender (Camera.cu:256-289): divide by the filter weight (in FP64 here), clamp at 0,
 // flip rows.
-__global__ void k_resolve(const double* __restrict__ film, float* __restrict__ rgb, int W, int H) {
+// The filter weight that camera samples at unit density put on pixel x in expectation, along one
+// axis: samples lie in (0, n] and reach pixels with |x - pf| <= 1, at weight table(|x - pf - 0.5|)
+// (the footprint and lookup of Camera::addSample); the Gaussian table is a product of one factor
+// per axis, g(ix) = table[ix] / sqrt(table[0]).  Steps of 1/16 keep every lookup constant.
+__device__ __forceinline__ double film_weight_1d(const float* __restrict__ table, int x, int n) {
+    const double g0 = sqrt((double)table[0]);
+    double e = 0;
+    for (int k = 0; k < 32; ++k) {
+        const double d = -1.0 + (k + 0.5) / 16.0, pf = x + d;
+        if (pf <= 0 || pf > n) continue;
+        const int ix = min((int)floor(fabs(-d - 0.5) * 16), 15);
+        e += (double)table[ix] / g0 / 16.0;
+    }
+    return e;
+}
+
+__global__ void k_resolve(const double* __restrict__ film, float* __restrict__ rgb, int W, int H,
+                          const double* __restrict__ splat, double splat_scale, const float* __restrict__ table) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= W * H) return;
     const int i = idx % W, jj = idx / W;
     const int src = (H - 1 - jj) * W + i;
     const double w = film[4 * src + 3];
+    // the bidirectional integrator's splats, per sample per pixel, over the expected filter weight
+    const double sw = splat ? splat_scale / (film_weight_1d(table, i, W) * film_weight_1d(table, H - 1 - jj, H)) : 0.0;
     for (int c = 0; c < 3; ++c) {
-        const double v = film[4 * src + c] / w;
+        double v = film[4 * src + c] / w;
+        if (splat) v += splat[3 * src + c] * sw;
         rgb[3 * idx + c] = fmaxf(0.0f, (float)v);
     }
 }
@@ -388,6 +409,10 @@ void Tracer::free_all() {
     counters_ = nullptr;
     dev_free(rgb_);
     rgb_ = nullptr;
+    dev_free(splat_);
+    splat_ = nullptr;
+    splat_cap_ = 0;
+    splat_spp_ = 0;
     dev_free(trace_);
     trace_ = nullptr;
     dev_free(views_film_);
@@ -841,8 +866,15 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
                             uint32_t* d_err, RenderParams* rp, SceneView* sv, long* crop_samples) {
     if (d.spp < 1 || d.max_bounce < 0) return "bad argument: spp must be >= 1 and max_bounce >= 0";
     if (d.integrator != LTS_INTEGRATOR_MEGAKERNEL && d.integrator != LTS_INTEGRATOR_WAVEFRONT &&
-        d.integrator != LTS_INTEGRATOR_FP64)
+        d.integrator != LTS_INTEGRATOR_FP64 && d.integrator != LTS_INTEGRATOR_BDPT)
         return "bad argument: unknown integrator";
+    if (d.integrator == LTS_INTEGRATOR_BDPT) {
+        if (d.record_samples) return "bad argument: the bidirectional integrator has no record mode";
+        if (d.max_bounce > kBdptMaxBounce) return "bad argument: the bidirectional integrator takes max_bounce <= 8";
+        if (sc.lights.empty()) return "bad argument: the bidirectional integrator needs a light";
+        for (const HostLight& l : sc.lights)
+            if (l.kind == LIGHT_INFINITE) return "unsupported: the bidirectional integrator takes area and point lights";
+    }
     if (d.integrator == LTS_INTEGRATOR_WAVEFRONT && d.max_bounce < 1)
         return "bad argument: the wavefront integrator needs max_bounce >= 1";
     int x0 = d.x0, y0 = d.y0, x1 = d.x1, y1 = d.y1;
@@ -866,6 +898,22 @@ std::string Tracer::prepare(const HostScene& sc, const Lbvh& bvh, const lts_rend
         film_cap_ = film_bytes;
     }
     if (!film_accumulate) TRY(cudaMemsetAsync(film_, 0, film_bytes, s));
+    // light-to-camera splats of the bidirectional integrator, scaled by 1 / (samples so far)
+    if (!film_accumulate) splat_spp_ = 0;
+    if (d.integrator == LTS_INTEGRATOR_BDPT) {
+        const size_t sb = 24 * (size_t)sc.width * sc.height;
+        if (splat_cap_ < sb) {
+            dev_free(splat_);
+            splat_ = nullptr;
+            TRY(dev_alloc((void**)&splat_, sb));
+            splat_cap_ = sb;
+            TRY(cudaMemsetAsync(splat_, 0, sb, s));
+        }
+        if (splat_spp_ == 0) TRY(cudaMemsetAsync(splat_, 0, sb, s));
+        splat_spp_ += d.spp;
+    } else if (splat_spp_ > 0 && !film_accumulate) {
+        splat_spp_ = 0;
+    }
     TRY(cudaMemsetAsync(counters_, 0, 128, s));
     const long ns = (long)(x1 - x0) * (y1 - y0) * d.spp;
     *crop_samples = ns;
@@ -921,6 +969,8 @@ std::string Tracer::render_async(const HostScene& sc, const Lbvh& bvh, const lts
     if (d.integrator == LTS_INTEGRATOR_FP64) {
         e = render64_launch(sv, rp, bvh.n, d.record_samples != 0, s);
         if (!e.empty()) return e;
+    } else if (d.integrator == LTS_INTEGRATOR_BDPT) {
+        k_bdpt<<<grid, block, 0, s>>>(sv, rp, bvh.n, splat_, bdpt_strategy);
     } else if (d.record_samples) {
         k_pathtrace<true><<<grid, block, 0, s>>>(sv, rp, bvh.n);
     } else {
@@ -1367,7 +1417,8 @@ std::string Tracer::film_get(const HostScene& sc, float* rgb, double* sums, cuda
     if (!film_) return "nothing rendered";
     const int W = sc.width, H = sc.height;
     if (rgb) {
-        k_resolve<<<(W * H + 255) / 256, 256, 0, s>>>(film_, rgb_, W, H);
+        k_resolve<<<(W * H + 255) / 256, 256, 0, s>>>(film_, rgb_, W, H, splat_spp_ > 0 ? splat_ : nullptr,
+                                                      splat_spp_ > 0 ? 1.0 / splat_spp_ : 0.0, view_.filter);
         TRY(cudaGetLastError());
         TRY(cudaMemcpyAsync(rgb, rgb_, 12 * (size_t)W * H, cudaMemcpyDeviceToHost, s));
     }
@@ -1466,7 +1517,7 @@ std::string Tracer::render_views(const HostScene& sc, const Lbvh& bvh, const lts
     long off = 0;
     for (int v = 0; v < n; ++v) {
         const int W = views[v].width, H = views[v].height;
-        k_resolve<<<(W * H + 255) / 256, 256, 0, s>>>(views_film_ + 4 * off, rgb, W, H);
+        k_resolve<<<(W * H + 255) / 256, 256, 0, s>>>(views_film_ + 4 * off, rgb, W, H, nullptr, 0.0, nullptr);
         cudaError_t c = cudaGetLastError();
         if (c == cudaSuccess && films[v]) c = cudaMemcpyAsync(films[v], rgb, 12 * (size_t)W * H, cudaMemcpyDeviceToHost, s);
         if (c == cudaSuccess) c = cudaStreamSynchronize(s);

@@ -171,6 +171,8 @@ class Tracer {
     // Scenes with instanced meshes: 1 = the two-level 8-wide BVH (one tree per prototype under
     // a top level), 0 = one flat tree over every triangle.  Needs bvh_width 8 and render_bvh != 0.
     int two_level = 1;
+    // Bidirectional integrator: -1 all strategies MIS-weighted, else only s = v / 100, t = v % 100.
+    int bdpt_strategy = -1;
     bool last_two_level = false;  // the last render traversed the two-level BVH
     // Radiance cache (wavefront integrator): on/off, the MLP it queries and trains (owned by the
     // context), the share of paths traced in full (per mille), training records per render, Adam
@@ -248,6 +250,9 @@ class Tracer {
     float* iroot_ = nullptr;         // bounds of the whole two-level scene
     size_t inodes_cap_ = 0, itris_cap_ = 0;
     int icount_ = 0, itri_n_ = 0, ilevels_ = 0;
+    double* splat_ = nullptr;  // bidirectional integrator: light-to-camera splats, RGB per pixel
+    size_t splat_cap_ = 0;
+    long splat_spp_ = 0;       // samples per pixel the splats hold
     uint64_t ikey_ = 0;              // key of the scene upload and render-tree choice built from
     uint64_t upload_serial_ = 0;
     int two_level_ok_ = 0;

@@ -146,22 +146,26 @@ __device__ __forceinline__ int4 prim_word(const SceneView& sv, int prim) {
 
 // ------------------------------------------------------------------ triangle tests
 // Triangle::intersect test part (shapes/Triangle.cu:94-128).
-// EXACT: the reference's cross products (diff_prod); else the faster ones the traversal uses.
+// EXACT: the reference's arithmetic (its double-rounded cross products, unfused dot products);
+// else the traversal's faster form: Kahan cross products and FMA dot products, a few ulps from
+// the reference's values -- it only ranks the candidates, and the winner's values are recomputed
+// exactly (make_si's `ro`).
+__device__ __forceinline__ real dot_fma(V3 a, V3 b) { return xfma(a.z, b.z, xfma(a.y, b.y, a.x * b.x)); }
 template <bool EXACT = true>
 __device__ __forceinline__ bool tri_test(V3 p0, V3 p1, V3 p2, V3 o, V3 d, real tmax, real& t_out, real& u_out,
                                          real& v_out, real& inv_out) {
     const V3 e1 = p1 - p0, e2 = p2 - p0;
     const V3 pv = EXACT ? cross(d, e2) : cross_fast(d, e2);
-    const real det = dot(e1, pv);
+    const real det = EXACT ? dot(e1, pv) : dot_fma(e1, pv);
     if (det == 0) return false;
     const real inv = xrcp(det);  // == (real)(1.0 / (double)det)
     const V3 tv = o - p0;
-    const real u = inv * dot(tv, pv);
+    const real u = inv * (EXACT ? dot(tv, pv) : dot_fma(tv, pv));
     if (u < kShadowEps || u >= kOneMinusEpsUp) return false;
     const V3 qv = EXACT ? cross(tv, e1) : cross_fast(tv, e1);
-    const real v = inv * dot(d, qv);
+    const real v = inv * (EXACT ? dot(d, qv) : dot_fma(d, qv));
     if (v < kShadowEps || u + v >= kOneMinusEpsUp) return false;
-    const real t = inv * dot(e2, qv);
+    const real t = inv * (EXACT ? dot(e2, qv) : dot_fma(e2, qv));
     if (!(t > 0 && t < tmax)) return false;
     t_out = t;
     u_out = u;
@@ -174,16 +178,16 @@ template <bool EXACT = true>
 __device__ __forceinline__ bool tri_test_shadow(V3 p0, V3 p1, V3 p2, V3 o, V3 d, real tmax) {
     const V3 e1 = p1 - p0, e2 = p2 - p0;
     const V3 pv = EXACT ? cross(d, e1) : cross_fast(d, e1);
-    const real det = dot(e2, pv);
+    const real det = EXACT ? dot(e2, pv) : dot_fma(e2, pv);
     if (det == 0) return false;
     const real inv = xrcp(det);
     const V3 tv = o - p0;
-    const real u = inv * dot(tv, pv);
+    const real u = inv * (EXACT ? dot(tv, pv) : dot_fma(tv, pv));
     if (u < kShadowEps || u >= kOnePlusEpsUp) return false;
     const V3 qv = EXACT ? cross(tv, e2) : cross_fast(tv, e2);
-    const real v = inv * dot(d, qv);
+    const real v = inv * (EXACT ? dot(d, qv) : dot_fma(d, qv));
     if (v < kShadowEps || u + v >= kOnePlusEpsUp) return false;
-    const real t = inv * dot(e1, qv);
+    const real t = inv * (EXACT ? dot(e1, qv) : dot_fma(e1, qv));
     return t > 0 && t < tmax;
 }
 
@@ -207,25 +211,51 @@ struct SI {
     int mesh, light;    // material index, area-light index (-1: none) of the primitive
 };
 
+// Cross products of the interaction's frames (make_si's normals and tangents, coordinate_system,
+// make_bsdf): the faster form by default -- within 1.5 ulp, with every per-sample parity case
+// inside its bound, 4 % more throughput on the stress scene -- or the reference's rounding
+// (LTS_SI_CROSS=1: the stress scene's bit-exact share 0.76 instead of 0.70).  The hit's
+// barycentrics always use the reference's rounding (make_si's `ro`).
+#ifndef LTS_SI_CROSS
+#define LTS_SI_CROSS 0
+#endif
+__device__ __forceinline__ V3 cross_si(V3 a, V3 b) { return LTS_SI_CROSS ? cross(a, b) : cross_fast(a, b); }
+
 __device__ __forceinline__ void coordinate_system(V3 v1, V3& v2, V3& v3o) {
     // Geometry.cuh:250-258
     if (xabs(v1.x) > xabs(v1.y))
         v2 = v3(-v1.z, 0, v1.x) * rsqrt_q3(v1.x * v1.x + v1.z * v1.z);
     else
         v2 = v3(0, v1.z, -v1.y) * rsqrt_q3(v1.y * v1.y + v1.z * v1.z);
-    v3o = cross(v1, v2);
+    v3o = cross_si(v1, v2);
 }
 
 // Builds the SurfaceInteraction of a hit (Triangle.cu:128-199 and the SurfaceInteraction
 // constructor, geometry/Interaction.cuh:85-116).
 // Triangle::intersect's SurfaceInteraction (shapes/Triangle.cu:130-203) from the triangle's
 // shading record: positions, uvs (or the defaults) and vertex normals in one 128-byte line.
-__device__ void make_si(const SceneView& sv, int prim, V3 d, real u, real v, real inv, SI& si) {
+// With the ray's origin `ro` (closest hits found by the traversal, whose triangle tests use the
+// faster cross products), the triangle test is repeated on the record's positions with the
+// reference's rounding first, so that the interaction is built from the reference's barycentrics
+// and 1 / det (a hit the exact test rejects, within rounding of an edge, keeps the traversal's
+// values; the watertight test's values are its own).
+__device__ void make_si(const SceneView& sv, int prim, V3 d, real u, real v, real inv, SI& si,
+                        const V3* ro = nullptr) {
     const float4* rec = sv.prim_rec + 8 * (size_t)prim;
     const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2);
     const float4 r3 = __ldg(rec + 3), r4 = __ldg(rec + 4), r5 = __ldg(rec + 5);
     const int4 word = __ldg(reinterpret_cast<const int4*>(rec) + 6);
     const V3 p0 = v3(r0.x, r0.y, r0.z), p1 = v3(r1.x, r1.y, r1.z), p2 = v3(r2.x, r2.y, r2.z);
+#if !LTS_FP64
+    if (ro && !sv.watertight) {
+        real t2, u2, v2, inv2;
+        if (tri_test<true>(p0, p1, p2, *ro, d, INFINITY, t2, u2, v2, inv2)) {
+            u = u2;
+            v = v2;
+            inv = inv2;
+        }
+    }
+#endif
     const real w = 1 - u - v;
     const V3 e1 = p1 - p0, e2 = p2 - p0;
     const real uv0x = r0.w, uv0y = r1.w, uv1x = r2.w, uv1y = r3.w, uv2x = r4.w, uv2y = r5.w;
@@ -234,7 +264,7 @@ __device__ void make_si(const SceneView& sv, int prim, V3 d, real u, real v, rea
     const real determinant = d02x * d12y - d02y * d12x;
     V3 dpdu, dpdv;
     if (determinant == 0) {
-        coordinate_system(normalize(cross(e2, e1)), dpdu, dpdv);
+        coordinate_system(normalize(cross_si(e2, e1)), dpdu, dpdv);
     } else {
         // the reference scales by the ray's invDet, not the uv determinant (Triangle.cu:148-149)
         dpdu = (dp02 * d12y - dp12 * d02y) * inv;
@@ -250,7 +280,7 @@ __device__ void make_si(const SceneView& sv, int prim, V3 d, real u, real v, rea
     si.wo = -d;
     si.dpdu = dpdu;
     si.dpdv = dpdv;
-    si.n = normalize(cross(dpdu, dpdv));
+    si.n = normalize(cross_si(dpdu, dpdv));
     si.sn = si.n;
     si.sdpdu = dpdu;
     si.prim = prim;
@@ -260,14 +290,14 @@ __device__ void make_si(const SceneView& sv, int prim, V3 d, real u, real v, rea
         const V3 n0 = v3(r3.x, r3.y, r3.z), n1 = v3(r4.x, r4.y, r4.z), n2 = v3(r5.x, r5.y, r5.z);
         const V3 ns = normalize(n0 * w + n1 * u + n2 * v);
         V3 ss = si.dpdu;
-        V3 ts = cross(ns, ss);
+        V3 ts = cross_si(ns, ss);
         if (len2(ts) > 0.0f) {
             ts = normalize(ts);
-            ss = cross(ts, ns);
+            ss = cross_si(ts, ns);
         } else {
             coordinate_system(ns, ss, ts);
         }
-        si.sn = normalize(cross(ss, ts));         // setShaddingGeometry
+        si.sn = normalize(cross_si(ss, ts));         // setShaddingGeometry
         si.n = face_towards(si.n, si.sn);
         si.sdpdu = ss;
         si.n = face_towards(si.n, si.sn);         // Triangle.cu:196
@@ -886,8 +916,7 @@ __device__ __forceinline__ bool scene_intersect(const SceneView& sv, int nleaf, 
     const int prim = traverse<false>(sv, nleaf, r, tmax, bu, bv, binv, stack, err, wk);
 #endif
     if (prim < 0) return false;
-    hit_exact(sv, prim, o, d, tmax, bu, bv, binv);
-    make_si(sv, prim, d, bu, bv, binv, si);
+    make_si(sv, prim, d, bu, bv, binv, si, &o);
     return true;
 }
 __device__ __forceinline__ bool scene_occluded(const SceneView& sv, int nleaf, V3 o, V3 d, real tmax, uint32_t* stack,
@@ -1384,7 +1413,7 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* si
     f.ns = si.sn;
     f.ng = si.n;
     f.ss = normalize(si.sdpdu);
-    f.ts = cross(f.ns, f.ss);
+    f.ts = cross_si(f.ns, f.ss);
     f.lobe = LOBE_NONE;
     f.type = 0;
     f.eta = 1;
