@@ -551,6 +551,7 @@ __device__ __forceinline__ WideAxis wide_axis(real p, real o, real inv, uint32_t
     return a;
 }
 __device__ __forceinline__ real wide_byte(uint32_t lo, uint32_t hi, int s) {
+    // (a byte permute under the exponent of 2^23 and a subtraction measured 2.5 % slower)
     return __uint2float_rn(((s < 4 ? lo : hi) >> ((s & 3) * 8)) & 0xffu);
 }
 // Three-input min / max (one instruction on sm_100 and later: PTX ISA 8.8).

@@ -305,13 +305,16 @@ __device__ __forceinline__ void wf_ray_end(int kind, const Trav& t, const SceneV
 #define LTS_REFILL_IDLE 12 // idle lanes of a warp that trigger fetching new rays
 #endif
 constexpr int kRefillIdle = LTS_REFILL_IDLE;
-// Resident blocks per SM the trace kernel is compiled for (caps its registers).
 #ifndef LTS_LEAF_BIAS
 #define LTS_LEAF_BIAS 1  // leaf steps when lanes with pending leaves x 4 >= lanes due a node x this
 #endif
 constexpr int kLeafBias = LTS_LEAF_BIAS;
+// Resident blocks per SM the trace kernel is compiled for (caps its registers): 8 blocks = 32
+// warps at 64 registers without spills; the kernel waits on node and triangle loads, and the
+// extra warps hide them (stress scene: trace 420 ms per render at 8, 444 at 7, 484 at 6; 9 and
+// 10 spill).
 #ifndef LTS_TRACE_MIN_BLOCKS
-#define LTS_TRACE_MIN_BLOCKS 7
+#define LTS_TRACE_MIN_BLOCKS 8
 #endif
 constexpr int kTraceMinBlocks = LTS_TRACE_MIN_BLOCKS;
 
