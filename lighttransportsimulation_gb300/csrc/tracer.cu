@@ -514,6 +514,22 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
         }
         mats[m].shade_class = 1 + c % (kShadeClasses - 1);
     }
+    // each class's shade kernel variant: the lobes its materials can have, and whether any of
+    // their textures is procedural or an image (classes alias past 15 material kinds)
+    for (int c = 0; c < kShadeClasses; ++c) {
+        shade_used_[c] = c == 0;
+        shade_lm_[c] = 0;
+        shade_tex_[c] = false;
+    }
+    for (size_t m = 0; m < mats.size(); ++m) {
+        const HostMaterial& h = sc.materials[m];
+        const int c = mats[m].shade_class;
+        shade_used_[c] = true;
+        const int lm = h.kind == 1 ? LM_MATTE : h.kind == 2 ? LM_GLASS : h.kind == 3 ? LM_MIRROR : h.kind == 4 ? LM_METAL : 0;
+        shade_lm_[c] |= lm;
+        const bool tex = h.tex[0].kind != TEX_CONSTANT || (h.kind == 2 && h.tex[1].kind != TEX_CONSTANT);
+        shade_tex_[c] = shade_tex_[c] || tex;
+    }
     std::vector<DevLight> lights(sc.lights.size());
     for (size_t l = 0; l < lights.size(); ++l) {
         const HostLight& h = sc.lights[l];
@@ -1037,6 +1053,33 @@ long Tracer::auto_pool(bool cache) const {
 
 // The wavefront loop over batches of view slices (see WfView): per batch, the path pool runs
 // until it drains, then every slice is gathered into its view's film.
+// The shade launch of one class: the kernel variant compiled for its lobes and textures
+// (record mode, the parity runs, uses the general one).
+static std::string launch_shade(bool record, int cls, int lm, bool tex, unsigned grid, const SceneView& sv,
+                                const RenderParams& rp, const WfState& st, int pool, cudaStream_t s) {
+    if (record) {
+        k_wf_shade<true, LM_ALL, true><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+    } else if (cls == 0) {
+        k_wf_shade<false, 0, false><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+    } else if (lm == LM_MATTE) {
+        if (tex) k_wf_shade<false, LM_MATTE, true><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+        else k_wf_shade<false, LM_MATTE, false><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+    } else if (lm == LM_GLASS) {
+        if (tex) k_wf_shade<false, LM_GLASS, true><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+        else k_wf_shade<false, LM_GLASS, false><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+    } else if (lm == LM_MIRROR) {
+        if (tex) k_wf_shade<false, LM_MIRROR, true><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+        else k_wf_shade<false, LM_MIRROR, false><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+    } else if (lm == LM_METAL) {
+        if (tex) k_wf_shade<false, LM_METAL, true><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+        else k_wf_shade<false, LM_METAL, false><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+    } else {
+        k_wf_shade<false, LM_ALL, true><<<grid, kWfBlock, 0, s>>>(sv, rp, st, pool, cls);
+    }
+    TRY(cudaGetLastError());
+    return "";
+}
+
 std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batches, const Lbvh& bvh, cudaStream_t s,
                                   uint32_t* d_err, const RenderParams& rp, const SceneView& sv) {
     (void)d_err;
@@ -1160,6 +1203,9 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
         wf_trace_blocks_[1] = (unsigned)std::max(1, per_b * sms);
         wf_trace_blocks_[2] = (unsigned)std::max(1, per_i * sms);
         wf_sms_ = (unsigned)sms;
+        int per_s = 0;
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_s, k_wf_shade<false, LM_ALL, true>, kWfBlock, 0));
+        shade_grid_ = (unsigned)std::max(1, per_s * sms * 2);
     }
     const bool two_level = wide && sv.ninst > 0;
     unsigned tb = wf_trace_blocks_[two_level ? 2 : (wide ? 0 : 1)];
@@ -1205,8 +1251,12 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
         if (full || n_ext) {
             const unsigned g = full ? blocks(P) : blocks(n_ext);
             k_wf_classify<<<g, kWfBlock, 0, s>>>(sv, st, q_ext, d_ctl, (int)P);
-            if (rec) k_wf_shade<true><<<g + kShadeClasses, kWfBlock, 0, s>>>(sv, rp, st, (int)P);
-            else k_wf_shade<false><<<g + kShadeClasses, kWfBlock, 0, s>>>(sv, rp, st, (int)P);
+            const unsigned gs = std::min(g, shade_grid_);
+            for (int c = 0; c < kShadeClasses; ++c) {
+                if (!shade_used_[c]) continue;
+                const std::string le = launch_shade(rec, c, shade_lm_[c], shade_tex_[c], gs, sv, rp, st, (int)P, s);
+                if (!le.empty()) return le;
+            }
         }
         if (!full) TRY(cudaEventRecord(wf_ev_[4], s));
         k_wf_compact<<<cgrid, kCompactThreads, 0, s>>>(st, q_fin, (int)P);

@@ -250,6 +250,11 @@ class Tracer {
     float* iroot_ = nullptr;         // bounds of the whole two-level scene
     size_t inodes_cap_ = 0, itris_cap_ = 0;
     int icount_ = 0, itri_n_ = 0, ilevels_ = 0;
+    // shade classes of the loaded scene: used, lobe mask and textured (the shade kernel variant)
+    bool shade_used_[kShadeClasses] = {false};
+    int shade_lm_[kShadeClasses] = {0};
+    bool shade_tex_[kShadeClasses] = {false};
+    unsigned shade_grid_ = 0;  // resident blocks of the shade kernel on this device
     double* splat_ = nullptr;  // bidirectional integrator: light-to-camera splats, RGB per pixel
     size_t splat_cap_ = 0;
     long splat_spp_ = 0;       // samples per pixel the splats hold

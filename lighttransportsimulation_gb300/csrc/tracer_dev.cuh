@@ -45,6 +45,12 @@ enum BxdfType : uint32_t {
     BSDF_ALL = 31u
 };
 enum LobeKind : int { LOBE_NONE = 0, LOBE_LAMBERT, LOBE_OREN_NAYAR, LOBE_FRESNEL_SPECULAR, LOBE_SPECULAR_REFL, LOBE_MICROFACET };
+// Lobe masks (bit k: LobeKind k may occur): the BSDF functions take one as a template argument so
+// that a kernel specialised to one material kind compiles only its lobes (LM_ALL: every lobe).
+constexpr int LM_MATTE = (1 << LOBE_LAMBERT) | (1 << LOBE_OREN_NAYAR), LM_GLASS = 1 << LOBE_FRESNEL_SPECULAR,
+              LM_MIRROR = 1 << LOBE_SPECULAR_REFL, LM_METAL = 1 << LOBE_MICROFACET,
+              LM_ALL = LM_MATTE | LM_GLASS | LM_MIRROR | LM_METAL;
+#define LTS_HAS_LOBE(LM, L) ((((LM) >> (L)) & 1) != 0)
 
 // ------------------------------------------------------------------ sampler (project Philox)
 struct Rng {
@@ -1072,7 +1078,11 @@ __device__ __noinline__ Spec img_lookup(const SceneView& sv, int idx, real st0, 
     return img_bilerp(sv, im, il, st0, st1) * (1 - delta) + img_bilerp(sv, im, il + 1, st0, st1) * delta;
 }
 
+// TEX false: the material's textures are constants (a kernel specialised to such materials
+// compiles none of the procedural or image textures).
+template <bool TEX = true>
 __device__ Spec eval_texture(const SceneView& sv, const DevTex& t, const SI& si, EvSink* sig) {
+    if (!TEX) return Spec{t.v[0], t.v[1], t.v[2]};
     switch (t.kind) {
         case 5:  // ImageTexture with UVMapping2D(1, 1, 0, 0) (SceneLoader.cuh:375): st = uv
             return img_lookup(sv, (int)t.v[0], si.tu, si.tv);
@@ -1269,10 +1279,14 @@ __device__ __forceinline__ V3 to_world(const Bsdf& f, V3 v) {
 __device__ __forceinline__ bool matches(uint32_t type, uint32_t flags) { return (type & flags) == type; }
 
 // BxDF::f
+template <int LM = LM_ALL>
 __device__ Spec lobe_f(const Bsdf& f, V3 wo, V3 wi) {
     switch (f.lobe) {
-        case LOBE_LAMBERT: return f.R * LTS_INV_PI_F;
+        case LOBE_LAMBERT:
+            if (!LTS_HAS_LOBE(LM, LOBE_LAMBERT)) return spec(0.0f);
+            return f.R * LTS_INV_PI_F;
         case LOBE_OREN_NAYAR: {  // Microfacet.cuh:27-50
+            if (!LTS_HAS_LOBE(LM, LOBE_OREN_NAYAR)) return spec(0.0f);
             const real so = sint(wo), si_ = sint(wi);
             real maxcos = 0.0f;
             if (si_ >= 0.0001f && so >= 0.0001f) {
@@ -1291,6 +1305,7 @@ __device__ Spec lobe_f(const Bsdf& f, V3 wo, V3 wi) {
             return f.R * LTS_INV_PI_F * (f.a + f.b * maxcos * sin_a * tan_b);
         }
         case LOBE_MICROFACET: {  // Microfacet.cuh:200-209
+            if (!LTS_HAS_LOBE(LM, LOBE_MICROFACET)) return spec(0.0f);
             const real co = xabs(wo.z), ci = xabs(wi.z);
             V3 wh = wi + wo;
             if (ci == 0 || co == 0) return spec(0.0f);
@@ -1303,12 +1318,15 @@ __device__ Spec lobe_f(const Bsdf& f, V3 wo, V3 wi) {
     }
 }
 // BxDF::Pdf
+template <int LM = LM_ALL>
 __device__ real lobe_pdf(const Bsdf& f, V3 wo, V3 wi, EvSink* sig) {
     switch (f.lobe) {
         case LOBE_LAMBERT:
         case LOBE_OREN_NAYAR:
+            if (!(LM & LM_MATTE)) return 0.0f;
             return same_hemi(wo, wi, sig) ? mul_dc(xabs(wi.z), LTS_1_PI) : 0.0f;
         case LOBE_MICROFACET: {
+            if (!LTS_HAS_LOBE(LM, LOBE_MICROFACET)) return 0.0f;
             if (!same_hemi(wo, wi, sig)) return 0;
             const V3 wh = normalize(wo + wi);
             return tr_pdf(wo, wh, f.alpha, f.alpha) / (4 * dot(wo, wh));
@@ -1317,25 +1335,28 @@ __device__ real lobe_pdf(const Bsdf& f, V3 wo, V3 wi, EvSink* sig) {
     }
 }
 // BSDF::f (materials/BSDF.cuh:192-204)
+template <int LM = LM_ALL>
 __device__ Spec bsdf_f(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags, EvSink* sig) {
     const bool reflect = dot(wiW, f.ng) * dot(woW, f.ng) > 0;
     if (sig) sig->put(0x600000000ull + (reflect ? 1u : 0u));
     if (f.lobe == LOBE_NONE || !matches(f.type, flags)) return spec(0.0f);
     const V3 wi = to_local(f, wiW), wo = to_local(f, woW);
     if ((reflect && (f.type & BSDF_REFLECTION)) || (!reflect && (f.type & BSDF_TRANSMISSION)))
-        return spec(0.0f) + lobe_f(f, wo, wi);
+        return spec(0.0f) + lobe_f<LM>(f, wo, wi);
     return spec(0.0f);
 }
 // BSDF::Pdf (BSDF.cuh:261-276)
+template <int LM = LM_ALL>
 __device__ real bsdf_pdf(const Bsdf& f, V3 woW, V3 wiW, uint32_t flags, EvSink* sig) {
     if (f.lobe == LOBE_NONE) return 0.0f;
     const V3 wo = to_local(f, woW), wi = to_local(f, wiW);
     if (wo.z == 0) return 0.0f;
     if (!matches(f.type, flags)) return 0.0f;
-    const real pdf = 0.0f + lobe_pdf(f, wo, wi, sig);
+    const real pdf = 0.0f + lobe_pdf<LM>(f, wo, wi, sig);
     return pdf / 1;
 }
 // BSDF::sampleF with a single matching lobe (BSDF.cuh:206-259) and the lobes' sampleF.
+template <int LM = LM_ALL>
 __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, real& pdf, uint32_t flags, uint32_t& sampled,
                             EvSink* sig) {
     if (f.lobe == LOBE_NONE || !matches(f.type, flags)) {
@@ -1351,22 +1372,25 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, real& pdf, uin
     switch (f.lobe) {
         case LOBE_LAMBERT:
         case LOBE_OREN_NAYAR: {  // BxDF::sampleF (BxDF.cuh:196-204)
+            if (!(LM & LM_MATTE)) break;
             const real r = xsqrt(u.x);
             const real th = mul_dc(u.y, LTS_2PI);
             const real dx = r * xcos(th), dy = r * xsin(th);
             wi = v3(dx, dy, xsqrt(xmax(0.0f, 1 - dx * dx - dy * dy)));
             if (wo.z < 0) wi.z *= -1;
-            pdf = lobe_pdf(f, wo, wi, sig);
-            val = lobe_f(f, wo, wi);
+            pdf = lobe_pdf<LM>(f, wo, wi, sig);
+            val = lobe_f<LM>(f, wo, wi);
             break;
         }
         case LOBE_SPECULAR_REFL: {  // Specular.cuh:30-39, FresnelNoOp
+            if (!LTS_HAS_LOBE(LM, LOBE_SPECULAR_REFL)) break;
             wi = v3(-wo.x, -wo.y, wo.z);
             pdf = 1.0f;
             val = (spec(1.0f) * f.R) / xabs(wi.z);
             break;
         }
         case LOBE_FRESNEL_SPECULAR: {  // Specular.cuh:107-135
+            if (!LTS_HAS_LOBE(LM, LOBE_FRESNEL_SPECULAR)) break;
             const real F = fresnel_dielectric(wo.z, 1.0f, f.eta);
             if (u.x < F) {
                 wi = v3(-wo.x, -wo.y, -wo.z);  // the reference's "reflection" keeps going straight
@@ -1390,13 +1414,14 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, real& pdf, uin
             break;
         }
         case LOBE_MICROFACET: {  // Microfacet.cuh:211-222
+            if (!LTS_HAS_LOBE(LM, LOBE_MICROFACET)) break;
             if (wo.z == 0) return spec(0.0f);
             const V3 wh = tr_sample_wh(wo, f.alpha, f.alpha, u.x, u.y);
             if (dot(wo, wh) < 0) return spec(0.0f);
             wi = -wo + wh * (2 * dot(wo, wh));
             if (!same_hemi(wo, wi, sig)) return spec(0.0f);
             pdf = tr_pdf(wo, wh, f.alpha, f.alpha) / (4 * dot(wo, wh));
-            val = lobe_f(f, wo, wi);
+            val = lobe_f<LM>(f, wo, wi);
             break;
         }
     }
@@ -1407,6 +1432,7 @@ __device__ Spec bsdf_sample(const Bsdf& f, V3 woW, V3& wiW, F2 u, real& pdf, uin
 
 // Material::computeScatteringFunctions (materials/Material.cuh:31-130) into a Bsdf record.
 // Returns false when the primitive has no material (the reference's skipped 'M' entries).
+template <int LM = LM_ALL, bool TEX = true>
 __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* sig) {
     const int mesh = si.mesh;
     const DevMat& m = sv.mats[mesh];
@@ -1420,7 +1446,8 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* si
     f.eta = 1;
     switch (m.kind) {
         case 1: {  // Matte
-            const Spec kd = eval_texture(sv, m.tex[0], si, sig);
+            if (!(LM & LM_MATTE)) break;
+            const Spec kd = eval_texture<TEX>(sv, m.tex[0], si, sig);
             if (!is_black(kd)) {
                 f.R = kd;
                 if (m.extra == 0) {
@@ -1435,8 +1462,9 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* si
             break;
         }
         case 2: {  // Glass
+            if (!(LM & LM_GLASS)) break;
             f.eta = m.extra;
-            const Spec r = eval_texture(sv, m.tex[0], si, sig), t = eval_texture(sv, m.tex[1], si, sig);
+            const Spec r = eval_texture<TEX>(sv, m.tex[0], si, sig), t = eval_texture<TEX>(sv, m.tex[1], si, sig);
             if (is_black(r) && is_black(t)) break;
             f.R = r;
             f.T = t;
@@ -1445,7 +1473,8 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* si
             break;
         }
         case 3: {  // Mirror
-            const Spec r = eval_texture(sv, m.tex[0], si, sig);
+            if (!(LM & LM_MIRROR)) break;
+            const Spec r = eval_texture<TEX>(sv, m.tex[0], si, sig);
             if (is_black(r)) break;
             f.R = r;
             f.lobe = LOBE_SPECULAR_REFL;
@@ -1453,7 +1482,8 @@ __device__ bool make_bsdf(const SceneView& sv, const SI& si, Bsdf& f, EvSink* si
             break;
         }
         case 4: {  // Metal (alpha given directly)
-            f.k = eval_texture(sv, m.tex[0], si, sig);
+            if (!(LM & LM_METAL)) break;
+            f.k = eval_texture<TEX>(sv, m.tex[0], si, sig);
             f.eta3 = Spec{m.tex[1].v[0], m.tex[1].v[1], m.tex[1].v[2]};
             f.R = spec(1.0f);
             f.alpha = m.extra;

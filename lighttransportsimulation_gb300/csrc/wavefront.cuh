@@ -429,33 +429,13 @@ __global__ __launch_bounds__(kWfBlock) void k_wf_classify(const SceneView sv, Wf
     st.q_cls[(size_t)c * pool + base + __popc(grp & ((1u << lane) - 1u))] = p;
 }
 
-// Block b of shade -> (class, entry): classes take consecutive runs of blocks.
-__device__ __forceinline__ int shade_entry(const WfState& st, int pool) {
-    __shared__ uint32_t s_cnt[kShadeClasses];
-    if (threadIdx.x < kShadeClasses) s_cnt[threadIdx.x] = st.counts[16 + threadIdx.x];
-    __syncthreads();
-    uint32_t b = blockIdx.x;
-    for (int c = 0; c < kShadeClasses; ++c) {
-        const uint32_t nb = (s_cnt[c] + kWfBlock - 1) / kWfBlock;
-        if (b < nb) {
-            const uint32_t i = b * kWfBlock + threadIdx.x;
-            return i < s_cnt[c] ? st.q_cls[(size_t)c * pool + i] : -1;
-        }
-        b -= nb;
-    }
-    return -1;
-}
-
 // Resident blocks per SM the shade kernel is compiled for (caps its registers).
 #ifndef LTS_SHADE_MIN_BLOCKS
 #define LTS_SHADE_MIN_BLOCKS 5  // 6 and 4 measured 2 % and 5 % slower on the stress scene
 #endif
-// Launched with ceil(paths / kWfBlock) + kShadeClasses blocks over the class-grouped lists.
-template <bool RECORD>
-__global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(const SceneView sv, const RenderParams rp,
-                                                                              WfState st, int pool) {
-    const int p = shade_entry(st, pool);
-    if (p < 0) return;
+// One path's bounce; LM / TEX: the lobes and textures its material can have (shade_variant).
+template <bool RECORD, int LM, bool TEX>
+__device__ __forceinline__ void shade_one(const SceneView& sv, const RenderParams& rp, WfState& st, int p) {
     const uint32_t flags = st.flags[p];
     const int bounce = (int)(flags >> 8);
     bool specular = (flags & 1u) != 0;
@@ -514,7 +494,7 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
             si.dpdx = v3(0, 0, 0);
             si.dpdy = v3(0, 0, 0);
         }
-        if (!make_bsdf(sv, si, f, RECORD ? &evs : nullptr)) done = true;
+        if (!make_bsdf<LM, TEX>(sv, si, f, RECORD ? &evs : nullptr)) done = true;
     }
     bool recorded = (flags & FL_RECORDED) != 0, rough_seen = (flags & FL_ROUGH) != 0;
     bool offered = (flags & FL_OFFERED) != 0;
@@ -576,8 +556,8 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
             LightSample ls;
             const bool delta = sample_li(sv, Lt, si, ulight, ls);
             if (ls.pdf > 0 && !is_black(ls.Li)) {
-                const Spec fv = bsdf_f(f, si.wo, ls.wi, fl, RECORD ? &evs : nullptr) * absdot(ls.wi, si.sn);
-                const float spdf = bsdf_pdf(f, si.wo, ls.wi, fl, RECORD ? &evs : nullptr);
+                const Spec fv = bsdf_f<LM>(f, si.wo, ls.wi, fl, RECORD ? &evs : nullptr) * absdot(ls.wi, si.sn);
+                const float spdf = bsdf_pdf<LM>(f, si.wo, ls.wi, fl, RECORD ? &evs : nullptr);
                 if (!is_black(fv)) {
                     const V3 org = offset_origin(si.p, si.perr, si.n, ls.p1 - si.p);
                     const V3 tgt = offset_origin(ls.p1, ls.perr1, ls.n1, org - ls.p1);
@@ -601,7 +581,7 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
                 float spdf = 0;
                 uint32_t stype = 0;
                 EvSink cap{nullptr, 0};
-                Spec fv = bsdf_sample(f, si.wo, wi, uscat, spdf, fl, stype, RECORD ? &cap : nullptr);
+                Spec fv = bsdf_sample<LM>(f, si.wo, wi, uscat, spdf, fl, stype, RECORD ? &cap : nullptr);
                 ev_mis = cap.cap;
                 fv = fv * absdot(wi, si.sn);
                 const bool sampled_spec = (stype & BSDF_SPECULAR) != 0;
@@ -636,7 +616,7 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
         uint32_t stype = 0;
         const F2 ub = rng_2d(rng);
         EvSink cap{nullptr, 0};
-        const Spec fv = bsdf_sample(f, si.wo, wi, ub, pdf, BSDF_ALL, stype, RECORD ? &cap : nullptr);
+        const Spec fv = bsdf_sample<LM>(f, si.wo, wi, ub, pdf, BSDF_ALL, stype, RECORD ? &cap : nullptr);
         ev_main = cap.cap;
         if (is_black(fv) || pdf == 0) {
             done = true;
@@ -666,6 +646,18 @@ __global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(con
         st.ev_main[p] = ev_main;
     }
 }
+
+// shade over one class's list (k_wf_classify), grid-stride: one launch per shade class present in
+// the scene, each compiled for its material kind (fewer registers, no spills, a smaller kernel).
+template <bool RECORD, int LM, bool TEX>
+__global__ __launch_bounds__(kWfBlock, LTS_SHADE_MIN_BLOCKS) void k_wf_shade(const SceneView sv, const RenderParams rp,
+                                                                              WfState st, int pool, int cls) {
+    const uint32_t n = st.counts[16 + cls];
+    const int32_t* __restrict__ q = st.q_cls + (size_t)cls * pool;
+    for (uint32_t i = blockIdx.x * kWfBlock + threadIdx.x; i < n; i += gridDim.x * kWfBlock)
+        shade_one<RECORD, LM, TEX>(sv, rp, st, q[i]);
+}
+
 
 // finalize: direct light of the bounce, deferred parity events; a finished path stores its
 // sample and frees its slot (pix = -1).
