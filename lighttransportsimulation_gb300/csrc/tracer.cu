@@ -460,6 +460,11 @@ Tracer::~Tracer() {
     if (ev1_) cudaEventDestroy(ev1_);
     for (cudaEvent_t e : wf_ev_)
         if (e) cudaEventDestroy(e);
+    for (int k = 0; k < kShadeClasses; ++k) {
+        if (shade_streams_[k]) cudaStreamDestroy(shade_streams_[k]);
+        if (shade_join_[k]) cudaEventDestroy(shade_join_[k]);
+    }
+    if (shade_fork_) cudaEventDestroy(shade_fork_);
 }
 
 void Tracer::drop_scene() {
@@ -1206,6 +1211,11 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
         int per_s = 0;
         TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_s, k_wf_shade<false, LM_ALL, true>, kWfBlock, 0));
         shade_grid_ = (unsigned)std::max(1, per_s * sms * 2);
+        for (int k = 0; k < kShadeClasses; ++k) {
+            TRY(cudaStreamCreateWithFlags(&shade_streams_[k], cudaStreamNonBlocking));
+            TRY(cudaEventCreateWithFlags(&shade_join_[k], cudaEventDisableTiming));
+        }
+        TRY(cudaEventCreateWithFlags(&shade_fork_, cudaEventDisableTiming));
     }
     const bool two_level = wide && sv.ninst > 0;
     unsigned tb = wf_trace_blocks_[two_level ? 2 : (wide ? 0 : 1)];
@@ -1252,11 +1262,18 @@ std::string Tracer::run_wavefront(const std::vector<std::vector<WfView>>& batche
             const unsigned g = full ? blocks(P) : blocks(n_ext);
             k_wf_classify<<<g, kWfBlock, 0, s>>>(sv, st, q_ext, d_ctl, (int)P);
             const unsigned gs = std::min(g, shade_grid_);
+            TRY(cudaEventRecord(shade_fork_, s));
+            int nb = 0;
             for (int c = 0; c < kShadeClasses; ++c) {
                 if (!shade_used_[c]) continue;
-                const std::string le = launch_shade(rec, c, shade_lm_[c], shade_tex_[c], gs, sv, rp, st, (int)P, s);
+                cudaStream_t cs = shade_streams_[nb];
+                TRY(cudaStreamWaitEvent(cs, shade_fork_, 0));
+                const std::string le = launch_shade(rec, c, shade_lm_[c], shade_tex_[c], gs, sv, rp, st, (int)P, cs);
                 if (!le.empty()) return le;
+                TRY(cudaEventRecord(shade_join_[nb], cs));
+                ++nb;
             }
+            for (int k = 0; k < nb; ++k) TRY(cudaStreamWaitEvent(s, shade_join_[k], 0));
         }
         if (!full) TRY(cudaEventRecord(wf_ev_[4], s));
         k_wf_compact<<<cgrid, kCompactThreads, 0, s>>>(st, q_fin, (int)P);

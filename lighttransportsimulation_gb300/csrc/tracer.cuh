@@ -255,6 +255,10 @@ class Tracer {
     int shade_lm_[kShadeClasses] = {0};
     bool shade_tex_[kShadeClasses] = {false};
     unsigned shade_grid_ = 0;  // resident blocks of the shade kernel on this device
+    // side streams and fork / join events: the classes' shade launches run concurrently (as
+    // parallel branches of the captured iteration graph)
+    cudaStream_t shade_streams_[kShadeClasses] = {nullptr};
+    cudaEvent_t shade_fork_ = nullptr, shade_join_[kShadeClasses] = {nullptr};
     double* splat_ = nullptr;  // bidirectional integrator: light-to-camera splats, RGB per pixel
     size_t splat_cap_ = 0;
     long splat_spp_ = 0;       // samples per pixel the splats hold
