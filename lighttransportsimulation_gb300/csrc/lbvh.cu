@@ -762,8 +762,8 @@ std::string Lbvh::build(const float* d_tri, int nn, int md, int code_limit, cuda
         clear_arrivals_ = true;
         epoch_ = 1u;
     }
-    if (clear_arrivals_) {
-        LTS_TRY(cudaMemsetAsync(flags_, 0, 4 * (N > 1 ? N - 1 : 1), s));
+    if (clear_arrivals_) {  // every word of the allocation: a later, larger build reads past n - 1
+        LTS_TRY(cudaMemsetAsync(flags_, 0, 4 * (size_t)(cap_ > 1 ? cap_ - 1 : 1), s));
         clear_arrivals_ = false;
     }
     LTS_TRY(cudaEventRecord(ev_[4], s));  // topology and refit run as one kernel, timed as the refit stage

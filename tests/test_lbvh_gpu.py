@@ -109,6 +109,35 @@ def test_rebuilds_reuse_the_arrival_words(ctx):
         lbvh_np.check_tree(out["node_left"], out["node_right"], out["node_bounds"], np.concatenate([mn, mx], 1)[ids])
 
 
+def test_rebuilds_across_epoch_wraps(built_lib):
+    """The tree's arrival words carry the build's epoch (127 epochs) instead of being cleared per
+    build; they are cleared when the epoch wraps.  Build 0 sizes the buffers (60,001 triangles);
+    build 2 (60,001) has epoch 3; build 33 (30,001) rewrites the first half of the words; the wrap
+    falls on a 3,001-triangle build (127); build 129 (60,001, other triangles) has epoch 3 again
+    over words past 30,000 that still hold build 2's.  Every build must equal a fresh build."""
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    from oracle import lbvh_np
+    cases = {}
+    for key, n, seed in (("big_x", 60_001, 10), ("big_a", 60_001, 11), ("mid", 30_001, 12), ("big_c", 60_001, 13),
+                         ("small", 3_001, 14)):
+        tris = scenes.random_triangles(n, seed=seed)
+        codes, ids = lbvh_np.stable_sort(*lbvh_np.morton_codes(tris))
+        cases[key] = (tris, codes, ids, *lbvh_np.karras_topology(codes))
+    c = lts.Context(0)  # a fresh context: its builds start at epoch 1
+    try:
+        for k in range(130):
+            key = {0: "big_x", 2: "big_a", 33: "mid", 129: "big_c"}.get(k, "small")
+            tris, codes, ids, left, right = cases[key]
+            out = lts.build_bvh_triangles(c, tris, lts.BVH_SORTED)
+            n = len(tris)
+            assert np.array_equal(out["sorted_codes"], codes) and np.array_equal(out["sorted_ids"], ids), (k, key)
+            assert np.array_equal(out["node_left"][: n - 1], left), (k, key)
+            assert np.array_equal(out["node_right"][: n - 1], right), (k, key)
+    finally:
+        c.close()
+
+
 @pytest.mark.parametrize("n", [1_000_000, 16_000_000])
 def test_benchmark_sizes_both_modes(ctx, n):
     """The build benchmark's random triangles (seed 1) at 1M and 16M, in the reference's mode
