@@ -66,8 +66,9 @@ int lts_obj_to_bin(const char* mesh_name);
  * reference's parseMesh does, core/FileIO.cuh:213-232), transforms subject meshes, builds the camera for a width x height film and
  * the light table, and uploads SoA tables to the device.  subject may be NULL or "".
  * Replaces parseScene (core/SceneLoader.cuh:195-360) and the init kernels of
- * core/SceneLoader_kernels.cu:8-111.  Image textures ('i') load PNG files in the fixed mode of
- * lts_scene_get_image; other image formats and interlaced PNGs give LTS_ERR_UNSUPPORTED. */
+ * core/SceneLoader_kernels.cu:8-111.  Image textures ('i') load PNG and baseline JPEG files in
+ * the fixed mode of lts_scene_get_image; other image formats, interlaced PNGs and progressive
+ * JPEGs give LTS_ERR_UNSUPPORTED. */
 int lts_load_scene(lts_ctx* ctx, const char* root, const char* scene, const char* subject,
                    int32_t width, int32_t height);
 
@@ -92,7 +93,8 @@ int lts_scene_get_light_distribution(lts_ctx* ctx, float* func, float* cdf);
  * the fixed mode of ImageTexture / Mipmap (materials/textures/ImageTexture.cuh:13-28,
  * Mipmap.cuh:34-73, Mipmap_kernel.cu:39-73), whose reference storage is undefined (its
  * BlockedArray shares rows and writes past its allocation, core/MemoryHelper.cuh:86-100).  PNG
- * files only (the reference decodes through stb_image); texel = (c / 255)^2.2 in float, rows
+ * and baseline JPEG files, decoded to the 8-bit values the reference's stb_image gives;
+ * texel = (c / 255)^2.2 in float, rows
  * flipped so v = 0 is the bottom row; floor(log2(max(w, h))) levels (at least one), level l the
  * 2 x 2 box mean of level l - 1 with black outside.  wh_levels[3] receives the level's width,
  * height and the image's level count; rgb (NULL or 3 w h floats) its texels, row-major. */

@@ -533,7 +533,7 @@ std::string load_scene(const std::string& root, const std::string& scene_name, c
             const std::string path = root + tok(s, "image path");
             int w = 0, h = 0, icode = 0;
             std::vector<uint8_t> rgb8;
-            const std::string ie = decode_png_file(path, &w, &h, &rgb8, &icode);
+            const std::string ie = decode_image_file(path, &w, &h, &rgb8, &icode);
             if (!ie.empty()) throw ParseError{icode, ie};
             build_pyramid(w, h, rgb8, wrap, &sc->images[(size_t)i]);
         }

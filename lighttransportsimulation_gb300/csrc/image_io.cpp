@@ -1,7 +1,7 @@
 // PNG decoding (RFC 2083) with its zlib inflate (RFC 1950 / 1951), and the image-texture pyramid
-// of the fixed mode.  The reference reads its images through stb_image (core/ImageI.cuh:11-34,
-// an external header absent from the reference tree); this file restates the published formats,
-// producing what stbi_load / stbi_loadf document for three requested channels.
+// of the fixed mode.  The reference reads its images through its vendored stb_image v2.27
+// (core/ImageI.cuh:11-34, extern/stb_image.h); this file restates the published formats,
+// producing what stbi_load / stbi_loadf give for three requested channels (JPEG: jpeg_io.cpp).
 #include "image_io.hpp"
 
 #include <algorithm>
@@ -385,14 +385,38 @@ std::string decode_png(const uint8_t* d, size_t n, int* w_out, int* h_out, std::
     return "";
 }
 
-std::string decode_png_file(const std::string& path, int* w, int* h, std::vector<uint8_t>* rgb, int* code) {
+namespace {
+std::string read_file(const std::string& path, std::vector<uint8_t>* data, int* code) {
     std::ifstream f(path, std::ios::binary);
     if (!f.is_open()) {
         *code = LTS_ERR_IO;
         return "cannot open " + path;
     }
-    std::vector<uint8_t> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
-    const std::string e = decode_png(data.data(), data.size(), w, h, rgb, code);
+    data->assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+    return "";
+}
+}  // namespace
+
+std::string decode_png_file(const std::string& path, int* w, int* h, std::vector<uint8_t>* rgb, int* code) {
+    std::vector<uint8_t> data;
+    std::string e = read_file(path, &data, code);
+    if (!e.empty()) return e;
+    e = decode_png(data.data(), data.size(), w, h, rgb, code);
+    return e.empty() ? e : path + ": " + e;
+}
+
+std::string decode_image(const uint8_t* d, size_t n, int* w, int* h, std::vector<uint8_t>* rgb, int* code) {
+    if (n >= 2 && d[0] == 0xFF && d[1] == 0xD8) return decode_jpeg(d, n, w, h, rgb, code);
+    if (n >= 8 && d[0] == 137 && d[1] == 'P' && d[2] == 'N' && d[3] == 'G') return decode_png(d, n, w, h, rgb, code);
+    *code = LTS_ERR_UNSUPPORTED;
+    return "not a PNG or JPEG file (only these image formats are decoded)";
+}
+
+std::string decode_image_file(const std::string& path, int* w, int* h, std::vector<uint8_t>* rgb, int* code) {
+    std::vector<uint8_t> data;
+    std::string e = read_file(path, &data, code);
+    if (!e.empty()) return e;
+    e = decode_image(data.data(), data.size(), w, h, rgb, code);
     return e.empty() ? e : path + ": " + e;
 }
 

@@ -18,6 +18,16 @@ namespace lts {
 std::string decode_png_file(const std::string& path, int* w, int* h, std::vector<uint8_t>* rgb, int* code);
 std::string decode_png(const uint8_t* data, size_t n, int* w, int* h, std::vector<uint8_t>* rgb, int* code);
 
+// Decodes a baseline JPEG (T.81 sequential DCT, Huffman, 8-bit; any sampling factors, restart
+// intervals, greyscale, YCbCr, Adobe RGB / CMYK / YCCK) into 8-bit RGB, top row first, as
+// stb_image v2.27 does for three requested channels.  Codes as decode_png (UNSUPPORTED for
+// progressive, lossless, arithmetic-coded or 12-bit files).
+std::string decode_jpeg(const uint8_t* data, size_t n, int* w, int* h, std::vector<uint8_t>* rgb, int* code);
+
+// A PNG or JPEG file by its signature (UNSUPPORTED for any other format).
+std::string decode_image(const uint8_t* data, size_t n, int* w, int* h, std::vector<uint8_t>* rgb, int* code);
+std::string decode_image_file(const std::string& path, int* w, int* h, std::vector<uint8_t>* rgb, int* code);
+
 // zlib stream (RFC 1950) inflated (RFC 1951: stored, fixed and dynamic Huffman blocks).
 bool zlib_inflate(const uint8_t* data, size_t n, std::vector<uint8_t>* out, std::string* err);
 

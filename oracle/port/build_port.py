@@ -16,7 +16,8 @@ def build():
     os.makedirs(OUT, exist_ok=True)
     exe = os.path.join(OUT, "lts_port")
     csrc = os.path.join(ROOT, "lighttransportsimulation_gb300", "csrc")
-    srcs = [os.path.join(HERE, "lts_port.cpp"), os.path.join(csrc, "host_scene.cpp"), os.path.join(csrc, "image_io.cpp")]
+    srcs = [os.path.join(HERE, "lts_port.cpp"), os.path.join(csrc, "host_scene.cpp"), os.path.join(csrc, "image_io.cpp"),
+            os.path.join(csrc, "jpeg_io.cpp")]
     deps = srcs + [os.path.join(HERE, "lts_rng.h"), os.path.join(ROOT, "include", "lts_capi.h"),
                    os.path.join(csrc, "host_scene.hpp"), os.path.join(csrc, "image_io.hpp")]
     if os.path.exists(exe) and all(os.path.getmtime(d) <= os.path.getmtime(exe) for d in deps):

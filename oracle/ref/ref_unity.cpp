@@ -18,6 +18,9 @@
  *       sample's events (extension hit primitive per bounce, shadow-ray visibility, MIS-ray
  *       hit primitive, texture branch decisions, BSDF grazing tests), the render wall time, and (FILM=1) the resolved film of
  *       Camera::getRender (Camera.cu:256-289).
+ *   lts_ref imread FILE OUT / lts_ref jpgwrite RAW W H COMP QUALITY OUT
+ *       the reference's image reader loadImageFile_s (core/ImageI.cuh:11-34, stb_image) on a
+ *       PNG or JPEG file; stb_image_write's JPEG writer (test inputs).
  *   lts_ref kat FN IN OUT
  *       the reference's own single functions (Trowbridge-Reitz distribution and sampling,
  *       MicrofacetReflection, Fresnel terms, Perlin noise, fbm, turbulence, offsetRayOrigin,
@@ -262,6 +265,39 @@ static int cmd_image(int argc, char** argv) {
     return ok ? 0 : 3;
 }
 
+/* lts_ref imread FILE OUT: the reference's image reader, loadImageFile_s (core/ImageI.cuh:11-34:
+ * stbi_loadf with three channels, rows flipped) -> OUT: int32 width, int32 height, then
+ * width*height*3 float32 texels.  An unreadable image ends the program with status 1, as the
+ * reference does. */
+static int cmd_imread(int argc, char** argv) {
+    if (argc < 4) return 2;
+    int w = 0, h = 0;
+    Spectrum* img = loadImageFile_s(argv[2], &w, &h);
+    FILE* g = fopen(argv[3], "wb");
+    if (!g) return 3;
+    const int32_t dims[2] = {w, h};
+    bool ok = fwrite(dims, 4, 2, g) == 2;
+    for (long i = 0; ok && i < (long)w * h; ++i) {
+        const float t[3] = {img[i].r, img[i].g, img[i].b};
+        ok = fwrite(t, 4, 3, g) == 3;
+    }
+    fclose(g);
+    delete[] img;
+    return ok ? 0 : 3;
+}
+
+/* lts_ref jpgwrite RAW W H COMP QUALITY OUT: stbi_write_jpg of the vendored stb_image_write
+ * (extern/stb_image_write.h) on W x H x COMP raw bytes (test inputs for the JPEG decoder). */
+static int cmd_jpgwrite(int argc, char** argv) {
+    if (argc < 8) return 2;
+    const int w = atoi(argv[3]), h = atoi(argv[4]), comp = atoi(argv[5]), quality = atoi(argv[6]);
+    std::vector<unsigned char> px((size_t)w * h * comp);
+    FILE* f = fopen(argv[2], "rb");
+    if (!f || fread(px.data(), 1, px.size(), f) != px.size()) return 3;
+    fclose(f);
+    return stbi_write_jpg(argv[7], w, h, comp, px.data(), quality) ? 0 : 3;
+}
+
 /* ------------------------------------------------------------------ known-answer vectors
  * lts_ref kat FN IN OUT: IN holds n records of 16 raw float32 inputs; OUT receives 16 floats per
  * record, the reference's own function FN (LTS_KAT_* and record layouts of include/lts_capi.h)
@@ -357,7 +393,7 @@ static int cmd_kat(int argc, char** argv) {
 
 int main(int argc, char** argv) {
     if (argc < 2) {
-        fprintf(stderr, "usage: lts_ref bvh|render|image|kat ...\n");
+        fprintf(stderr, "usage: lts_ref bvh|render|image|imread|jpgwrite|kat ...\n");
         return 2;
     }
     std::cout.setstate(std::ios_base::failbit); /* silence the loader's banners */
@@ -367,6 +403,8 @@ int main(int argc, char** argv) {
     if (c == "render") rc = cmd_render(argc, argv);
     if (c == "image") rc = cmd_image(argc, argv);
     if (c == "kat") rc = cmd_kat(argc, argv);
+    if (c == "imread") rc = cmd_imread(argc, argv);
+    if (c == "jpgwrite") rc = cmd_jpgwrite(argc, argv);
     if (rc == 2) fprintf(stderr, "bad arguments\n");
     return rc;
 }

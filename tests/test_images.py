@@ -1,7 +1,10 @@
 """Image textures on the CPU: the oracle's PNG reader against its own writer for every colour type,
 bit depth and filter, then the renderer's loader (its own inflate, filters and pyramid) against
 the oracle's numpy restatement, bit for bit, on generated images and on the reference's own
-image-texture scene (res/kernel_box_scene/kernel.png)."""
+image-texture scene (res/kernel_box_scene/kernel.png); its JPEG decoder against the reference's
+own reader (stb_image through loadImageFile_s: tests/golden/jpeg_golden.npz, made by
+tests/golden/make_golden_jpeg.py), bit for bit, on 22 JPEG forms and on res/blackDragon.jpg."""
+import hashlib
 import os
 
 import numpy as np
@@ -121,4 +124,91 @@ def test_malformed_png_is_a_parse_error(built_lib, tmp_path):
         with pytest.raises(lts.LtsError) as e:
             lts.Scene.parse(ctx, d, sc, sub, 32, 32)
         assert e.value.code == 3, name
+        ctx.close()
+
+
+def _jpeg_golden():
+    from conftest import GOLDEN
+    g = np.load(os.path.join(GOLDEN, "jpeg_golden.npz"))
+    cases = []
+    for k, name in enumerate(g["names"]):
+        data = g["jpeg"][g["jpeg_off"][k]:g["jpeg_off"][k + 1]].tobytes()
+        w, h = (int(x) for x in g["dims"][k])
+        rgb = g["rgb"][g["rgb_off"][k]:g["rgb_off"][k + 1]].reshape(h, w, 3)
+        cases.append((str(name), data, rgb))
+    return g, cases
+
+
+def test_jpeg_decoder_matches_the_reference_reader(built_lib, tmp_path):
+    """Every JPEG form of the golden set (stb's own writer at 4:2:0 / 4:4:4; greyscale, 4:2:2,
+    4:4:0, 4:1:1, 1 x 4 and mixed sampling, one scan per component, restart intervals, 16-bit
+    tables, SOF1, Adobe RGB / CMYK / YCCK, RGB component ids, widths 1 and 2): the loader's level 0
+    equals the reference's decoded, row-flipped texels bit for bit."""
+    import lighttransportsimulation_gb300 as lts
+    d = str(tmp_path)
+    _, cases = _jpeg_golden()
+    for name, data, _ in cases:
+        open(os.path.join(d, name + ".jpg"), "wb").write(data)
+    sc, sub = _scene_with_images(d, [(name + ".jpg", 1) for name, _, _ in cases])
+    ctx = lts.Context(-1)
+    s = lts.Scene.parse(ctx, d, sc, sub, 32, 32)
+    for k, (name, _, rgb) in enumerate(cases):
+        got, _ = s.image(k, 0)
+        got = got.reshape(rgb.shape)
+        assert np.array_equal(got.view(np.uint32), rgb.view(np.uint32)), name
+    ctx.close()
+
+
+def test_black_dragon_jpeg(built_lib, tmp_path):
+    """The reference's res/blackDragon.jpg (512 x 512, 4:2:0, JFIF + Exif): texels hash-equal to
+    the reference reader's, and the pyramid of a JPEG is built like a PNG's."""
+    import lighttransportsimulation_gb300 as lts
+    from oracle import image_np
+    d = str(tmp_path)
+    g, _ = _jpeg_golden()
+    open(os.path.join(d, "blackDragon.jpg"), "wb").write(g["dragon_jpeg"].tobytes())
+    sc, sub = _scene_with_images(d, [("blackDragon.jpg", 1)])
+    ctx = lts.Context(-1)
+    s = lts.Scene.parse(ctx, d, sc, sub, 32, 32)
+    w, h = (int(x) for x in g["dragon_dims"])
+    got, levels = s.image(0, 0)
+    got = got.reshape(h, w, 3)
+    assert np.array_equal(got[224:288, 224:288].view(np.uint32), g["dragon_crop"].view(np.uint32))
+    assert hashlib.sha256(got.tobytes()).hexdigest() == str(g["dragon_sha256"])
+    # the pyramid over the decoded 8-bit texels: invert the float conversion of level 0
+    lut = np.array([np.float32(np.power(np.float64(np.float32(c) / np.float32(255)), np.float64(np.float32(2.2))))
+                    for c in range(256)], np.float32)
+    rgb8 = np.searchsorted(lut, got[::-1].reshape(-1)).astype(np.uint8).reshape(h, w, 3)
+    assert np.array_equal(lut[rgb8][::-1].view(np.uint32), got.view(np.uint32))
+    want = image_np.pyramid(w, h, rgb8, 1)
+    assert levels == want["levels"] == 9
+    for level in range(levels):
+        lv, _ = s.image(0, level)
+        assert np.array_equal(lv.view(np.uint32), want["rgb"][level].view(np.uint32)), level
+    ctx.close()
+
+
+def test_malformed_and_unsupported_jpeg(built_lib, tmp_path):
+    """Progressive and 12-bit JPEGs are refused as unsupported (code 6); a truncated stream, a
+    coefficient run past its block and a missing restart marker are parse errors (code 3)."""
+    import lighttransportsimulation_gb300 as lts
+    from oracle import jpeg_np
+    d = str(tmp_path)
+    rng = np.random.default_rng(5)
+    q = [jpeg_np.quant_table(2.0), jpeg_np.quant_table(3.0)]
+    good = jpeg_np.encode(jpeg_np.test_planes(rng, 24, 16, [(2, 2), (1, 1), (1, 1)]), [(2, 2), (1, 1), (1, 1)], q,
+                          width=24, height=16, restart=1)
+    sof = good.index(b"\xff\xc0")
+    rst = good.index(b"\xff\xd0")
+    cases = [("prog.jpg", good[:sof + 1] + b"\xc2" + good[sof + 2:], 6),
+             ("p12.jpg", good[:sof + 4] + b"\x0c" + good[sof + 5:], 6),
+             ("trunc.jpg", good[:len(good) // 2], 3),
+             ("norst.jpg", good[:rst] + good[rst + 2:], 3)]
+    for name, data, code in cases:
+        open(os.path.join(d, name), "wb").write(data)
+        sc, sub = _scene_with_images(d, [(name, 1)])
+        ctx = lts.Context(-1)
+        with pytest.raises(lts.LtsError) as e:
+            lts.Scene.parse(ctx, d, sc, sub, 32, 32)
+        assert e.value.code == code, (name, str(e.value))
         ctx.close()
