@@ -80,6 +80,19 @@ def write_kernel_box(d):
     return d, "res/kernel_box_scene/kernel", ""
 
 
+def write_dragon(d):
+    """Recreates the reference's JPEG-textured subject on its closeupPlane platform
+    (res/blackDragon.subject / .bin / .jpg, res/platforms/closeupPlane.scene / triPlane.bin) under d
+    from tests/golden/dragon_inputs.npz; returns (root, scene, subject)."""
+    z = np.load(os.path.join(GOLDEN, "dragon_inputs.npz"))
+    for k in z.files:
+        rel = k[4:].replace("__", "/")
+        os.makedirs(os.path.join(d, os.path.dirname(rel)), exist_ok=True)
+        with open(os.path.join(d, rel), "wb") as fh:
+            fh.write(z[k].tobytes())
+    return d, "res/platforms/closeupPlane", "res/blackDragon"
+
+
 @pytest.fixture(scope="session")
 def scene_dirs(tmp_path_factory):
     """Generated parity scenes and the reference's shipped scenes, checked against the digests

@@ -19,6 +19,7 @@ changed generator from a changed renderer.  Usage (from the repository root):
     python tests/golden/make_golden.py shipped /path/to/reference   # the shipped scenes (SHIPPED)
     python tests/golden/make_golden.py digests                      # the bench scene's digests
     python tests/golden/make_golden.py kernel_box /path/to/reference  # the image-texture scene's inputs
+    python tests/golden/make_golden.py dragon /path/to/reference  # res/blackDragon on closeupPlane
 
 kernel_box_inputs.npz holds the input files of the reference's own image-texture scene
 (res/kernel_box_scene: a 64 x 64 PNG on a box); the reference cannot render it reproducibly (its
@@ -174,7 +175,45 @@ def make_kernel_box(reference_root):
     print("kernel_box_inputs ok")
 
 
+DRAGON_FILES = ["res/platforms/closeupPlane.scene", "res/platforms/triPlane.bin", "res/blackDragon.subject",
+                "res/blackDragon.bin", "res/blackDragon.jpg"]
+
+
+DRAGON_CONSTANT_SUBJECT = "0\n1\tres/blackDragon\n1\nL\tc\t0.5 0.5 0.5\t0.5"
+
+
+def make_dragon(reference_root):
+    """dragon_inputs.npz: the reference's JPEG-textured subject (res/blackDragon.subject, .bin,
+    .jpg) on res/platforms/closeupPlane; digest_dragon.npz: sha256 of every array the reference's
+    loader and LBVH build produce for it at 480 x 270.  The reference's loader crashes (SIGSEGV) in
+    its image-texture set-up on this subject in the host build (its BlockedArray writes past its
+    allocation for images taller than 16 texels), so the digests are taken on the same subject
+    with its texture replaced by a constant (DRAGON_CONSTANT_SUBJECT): triangles, camera, light
+    distribution and the LBVH do not depend on the subject's material."""
+    files = {}
+    for rel in DRAGON_FILES:
+        with open(os.path.join(reference_root, rel), "rb") as fh:
+            files[shipped_key(rel)] = np.frombuffer(fh.read(), np.uint8)
+    inputs = os.path.join(OUT, "dragon_inputs.npz")
+    np.savez_compressed(inputs, **files)
+    with tempfile.TemporaryDirectory() as td:
+        write_shipped_inputs(inputs, td)
+        with open(os.path.join(td, "res", "blackDragon_constant.subject"), "w") as fh:
+            fh.write(DRAGON_CONSTANT_SUBJECT)
+        b = os.path.join(td, "bvh.ltsd")
+        run(["bvh", td + "/", "res/platforms/closeupPlane", "res/blackDragon_constant", b, 480, 270])
+        d = ltsd.read(b)
+        sums = {k: np.array(hashlib.sha256(np.ascontiguousarray(v).tobytes()).hexdigest()) for k, v in d.items()}
+        np.savez_compressed(os.path.join(OUT, "digest_dragon.npz"), n=np.array(len(d["sorted_codes"])), **sums)
+    print("dragon ok")
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "dragon":
+        if not os.path.exists(REF):
+            sys.exit("oracle/_ref/lts_ref is missing: run oracle/ref/build_ref.sh first")
+        make_dragon(sys.argv[2] if len(sys.argv) > 2 else "/root/reference")
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "kernel_box":
         make_kernel_box(sys.argv[2] if len(sys.argv) > 2 else "/root/reference")
         return

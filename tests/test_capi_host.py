@@ -265,6 +265,30 @@ def test_loader_matches_reference_on_the_bench_scene(built_lib, tmp_path):
     ctx.close()
 
 
+def test_loader_matches_reference_on_the_dragon_scene(built_lib, tmp_path):
+    """The reference's JPEG-textured subject res/blackDragon on res/platforms/closeupPlane (37,986
+    triangles, 480 x 270): world triangles, camera and light distribution have the sha256 digests
+    of the reference's parseScene outputs (tests/golden/digest_dragon.npz; taken with the
+    subject's texture replaced by a constant, since the reference's loader crashes in its texture
+    set-up on this subject), and the texture's level 0 is the reference reader's decoding of
+    res/blackDragon.jpg (its digest in tests/golden/jpeg_golden.npz)."""
+    import lighttransportsimulation_gb300 as lts
+    from conftest import write_dragon
+    z = np.load(os.path.join(GOLDEN, "digest_dragon.npz"))
+    g = np.load(os.path.join(GOLDEN, "jpeg_golden.npz"))
+    root, sc, sub = write_dragon(str(tmp_path))
+    ctx = lts.Context(-1)
+    s = lts.Scene.parse(ctx, root, sc, sub, 480, 270)
+    assert s.info["triangles"] == int(z["n"]) and s.info["images"] == 1
+    assert _sha(s.triangles().reshape(-1)) == str(z["tri_p"])
+    assert _sha(s.camera()) == str(z["camera"])
+    func, cdf = s.light_distribution()
+    assert _sha(func) == str(z["light_func"]) and _sha(cdf) == str(z["light_cdf"])
+    tex, levels = s.image(0, 0)
+    assert levels == 9 and _sha(tex.reshape(512, 512, 3)) == str(g["dragon_sha256"])
+    ctx.close()
+
+
 def test_instances_grammar_extension(built_lib, tmp_path):
     """`instances K` and per instance `meshIndex tx ty tz s` after the infinite-light record (no
     counterpart in the reference): mesh entry meshIndex holds its file's triangles at p * s + t,

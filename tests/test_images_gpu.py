@@ -9,7 +9,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import write_kernel_box
+from conftest import write_dragon, write_kernel_box
 from test_render_gpu import check_samples
 
 pytestmark = pytest.mark.gpu
@@ -81,3 +81,32 @@ def test_reference_image_scene_matches_the_port(ctx, port_exe, tmp_path):
     for integ in (lts.INTEGRATOR_MEGAKERNEL, lts.INTEGRATOR_WAVEFRONT):
         L, sig = res[integ]
         check_samples(L, sig, Lr, sr, L64, s64, f"kernel_box integrator={integ}")
+
+
+def test_reference_jpeg_scene_matches_the_port(ctx, port_exe, tmp_path):
+    """The reference's JPEG-textured subject res/blackDragon on res/platforms/closeupPlane,
+    480 x 270, a 48 x 48 crop on the dragon, 4 spp, 5 bounces: the megakernel and the wavefront
+    integrator against the port's samples."""
+    import lighttransportsimulation_gb300 as lts
+    from oracle import ltsd
+    root, sc, sub = write_dragon(str(tmp_path))
+    w, h, spp, maxb, rr, seed = 480, 270, 4, 5, 3, 2
+    x0, y0, x1, y1 = 216, 111, 264, 159
+    out = str(tmp_path / "port.ltsd")
+    args = (port_exe, "render", root + "/", sc, sub, out, w, h, spp, maxb, rr, seed, x0, y0, x1, y1,
+            os.cpu_count(), 0, 0)
+    subprocess.run([str(a) for a in args], check=True)
+    ref = ltsd.read(out)
+    Lr, sr = ref["L"].reshape(-1, 3), ref["sig"].reshape(-1)
+    s = lts.Scene.parse(ctx, root, sc, sub, w, h)
+    assert s.info["images"] == 1
+    res = {}
+    for integ in (lts.INTEGRATOR_FP64, lts.INTEGRATOR_MEGAKERNEL, lts.INTEGRATOR_WAVEFRONT):
+        r = lts.PathTracingIntegrator(maxb, rr, s, integrator=integ).render(spp, seed, crop=(x0, y0, x1, y1),
+                                                                            record=True, film=False)
+        res[integ] = (r["L"].reshape(-1, 3).copy(), r["sig"].reshape(-1).copy())
+    L64, s64 = res[lts.INTEGRATOR_FP64]
+    assert Lr.mean() > 0
+    for integ in (lts.INTEGRATOR_MEGAKERNEL, lts.INTEGRATOR_WAVEFRONT):
+        L, sig = res[integ]
+        check_samples(L, sig, Lr, sr, L64, s64, f"blackDragon integrator={integ}")

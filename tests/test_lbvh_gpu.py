@@ -189,3 +189,19 @@ def test_reference_mode_on_the_bench_scene(ctx, tmp_path):
     out = s.create_bvh_tree(lts.BVH_REFERENCE)
     for k in ("sorted_codes", "sorted_ids", "node_key", "node_left", "node_right", "node_bounds"):
         assert hashlib.sha256(np.ascontiguousarray(out[k]).tobytes()).hexdigest() == str(z[k]), k
+
+
+def test_reference_mode_on_the_dragon_scene(ctx, tmp_path):
+    """The reference's res/blackDragon subject on res/platforms/closeupPlane (37,986 triangles) in
+    the reference's mode: codes, order, children and every node box have the sha256 digests of
+    the reference's own build (tests/golden/digest_dragon.npz)."""
+    import hashlib
+
+    import lighttransportsimulation_gb300 as lts
+    from conftest import write_dragon
+    z = np.load(os.path.join(GOLDEN, "digest_dragon.npz"))
+    root, sc, sub = write_dragon(str(tmp_path))
+    s = lts.Scene.parse(ctx, root, sc, sub, 480, 270)
+    out = s.create_bvh_tree(lts.BVH_REFERENCE)
+    for k in ("sorted_codes", "sorted_ids", "node_key", "node_left", "node_right", "node_bounds"):
+        assert hashlib.sha256(np.ascontiguousarray(out[k]).tobytes()).hexdigest() == str(z[k]), k
