@@ -233,10 +233,6 @@ __device__ __forceinline__ void wg_publish(int id) {
     tc_fence_after();
 }
 
-#ifndef LTS_MLP_PREFETCH
-#define LTS_MLP_PREFETCH 1  // prefetch each warpgroup's next feature tile into L2
-#endif
-
 // Inference: out[r * stride + c] = exp(z_c), c < 3, for the feature rows r = rows[i] (rows null:
 // r = i), i < n.  Persistent CTAs of kFwdGroups warpgroups; warpgroup g runs tiles
 // blockIdx.x * kFwdGroups + g, + gridDim.x * kFwdGroups, ..., one row per thread, and
@@ -270,19 +266,6 @@ __global__ __launch_bounds__(128 * kFwdGroups) void k_mlp_forward(const uint16_t
             const uint4 q = valid ? __ldg(src + j) : make_uint4(0, 0, 0, 0);
             *(uint4*)(smem + buf + rc_offset(row, 8 * j, kMlpIn)) = q;
         }
-#if LTS_MLP_PREFETCH
-        {
-            // the next tile's feature row into L2 while this tile's six layers run (a 192-byte
-            // row at a 64-byte boundary spans two 128-byte lines)
-            const long inext = i + (long)gridDim.x * kFwdGroups * 128;
-            if (inext < n) {
-                const long rn = rows ? (long)__ldg(rows + inext) : inext;
-                const char* p = (const char*)(feat + rn * kMlpIn);
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(p + 128));
-            }
-        }
-#endif
         wg_publish(bar_id);
         bool ok = true;
         for (int L = 0; L < kMlpLayers; ++L) {
