@@ -89,7 +89,9 @@ def test_loader_errors(tmp_path, built_lib):
     open(os.path.join(d, "sphere.subject"), "w").write(img)
     assert _load_err(d, sc, sub) == 2                            # missing image file -> IO
     open(os.path.join(d, "tex.jpg"), "wb").write(b"\xff\xd8\xff\xe0" + bytes(60))
-    assert _load_err(d, sc, sub) == 6                            # not a PNG -> UNSUPPORTED
+    assert _load_err(d, sc, sub) == 3                            # malformed JPEG -> PARSE
+    open(os.path.join(d, "tex.jpg"), "wb").write(b"GIF89a" + bytes(60))
+    assert _load_err(d, sc, sub) == 6                            # neither PNG nor JPEG -> UNSUPPORTED
     open(os.path.join(d, "sphere.subject"), "w").write("0\n1\tsphere\n")
     assert _load_err(d, sc, sub) == 3                            # premature end of file
 
