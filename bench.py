@@ -33,7 +33,10 @@ Reported (one JSON line on rank 0):
   watertight the same render with the watertight triangle test (option "watertight");
   instanced  the stress scene with its conductor spheres as instances of one mesh file, 64 spp:
              Mpaths/s, render-BVH bytes and build time through the two-level BVH and through one
-             flat tree.
+             flat tree;
+  bdpt       bidirectional path tracing on a box lit by one triangle (256 x 256, 5 bounces):
+             Msamples/s beside the two path tracers, and the RMSE BDPT and the wavefront path
+             tracer reach in equal device time against a 16,384-spp render.
 --impl reference times that CPU port alone, on the same workload and metric.
 Inputs (BVH + triangles, ~400 MB) exceed the 129 MB L2, so no flush runs between steps.
 """
@@ -460,6 +463,54 @@ def instanced_extra(args, ctx):
     return out
 
 
+BDPT_BOX = dict(width=256, height=256, max_bounce=5, rr_start=3, spp=64, seed=11, ref_spp=16384)
+
+
+def bdpt_extra(args, ctx):
+    """Bidirectional path tracing (LTS_INTEGRATOR_BDPT) on the box + icosphere scene lit by one
+    ceiling triangle (Lambertian walls, 256 x 256, 5 bounces): device Msamples/s of BDPT and of
+    the two path tracers at 64 spp, and the film RMSE that BDPT and the wavefront path tracer
+    reach in the same device time (BDPT's 64 spp), against a 16,384-spp wavefront render."""
+    import numpy as np
+    import torch
+
+    import lighttransportsimulation_gb300 as lts
+    from lighttransportsimulation_gb300 import scenes
+    wl = BDPT_BOX
+    d = os.path.join(tempfile.gettempdir(), "lts_bench_bdpt_box")
+    sc, sub = scenes.write_tri_light_box(d)
+    scene = lts.Scene.parse(ctx, d, sc, sub, wl["width"], wl["height"])
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    px = wl["width"] * wl["height"]
+
+    def integ(kind):
+        return lts.PathTracingIntegrator(wl["max_bounce"], wl["rr_start"], scene, integrator=kind)
+
+    def timed(kind, spp, seed):
+        desc = integ(kind).desc(spp, seed)
+        render_timed(ctx, desc, 1, stream)
+        return render_timed(ctx, desc, 2, stream)
+
+    out = {"workload": "box_icosphere_one_triangle_light", "width": wl["width"], "height": wl["height"],
+           "max_bounce": wl["max_bounce"], "spp": wl["spp"], "unit": "Msamples/s"}
+    ms = {}
+    for name, kind in (("bdpt", lts.INTEGRATOR_BDPT), ("megakernel", lts.INTEGRATOR_MEGAKERNEL),
+                       ("wavefront", lts.INTEGRATOR_WAVEFRONT)):
+        ms[name] = timed(kind, wl["spp"], wl["seed"])
+        out[name] = round(px * wl["spp"] / (ms[name] * 1e-3) / 1e6, 3)
+    out["value"] = out["bdpt"]
+    ref = integ(lts.INTEGRATOR_WAVEFRONT).render(wl["ref_spp"], wl["seed"] + 1)["film"].astype(np.float64)
+    spp_pt = max(1, int(round(wl["spp"] * ms["bdpt"] / ms["wavefront"])))
+    bd = integ(lts.INTEGRATOR_BDPT).render(wl["spp"], wl["seed"] + 2)["film"].astype(np.float64)
+    pt = integ(lts.INTEGRATOR_WAVEFRONT).render(spp_pt, wl["seed"] + 3)["film"].astype(np.float64)
+    out["equal_time"] = {"device_ms": round(ms["bdpt"], 3), "bdpt_spp": wl["spp"], "wavefront_spp": spp_pt,
+                         "reference_spp": wl["ref_spp"],
+                         "rmse_bdpt": float(np.sqrt(np.mean((bd - ref) ** 2))),
+                         "rmse_wavefront": float(np.sqrt(np.mean((pt - ref) ** 2))),
+                         "mean_bdpt": float(bd.mean()), "mean_reference": float(ref.mean())}
+    return out
+
+
 def run_gpu(args, wl):
     import ctypes
 
@@ -546,6 +597,7 @@ def run_gpu(args, wl):
     ttr = time_to_rmse(args, ctx) if (solo and wl is STRESS and not args.skip_ttr) else None
     extra = displaced_extra(args, ctx) if (solo and wl is STRESS and not args.skip_displaced) else None
     inst = instanced_extra(args, ctx) if (solo and wl is STRESS and not args.skip_instanced) else None
+    bdpt = bdpt_extra(args, ctx) if (solo and wl is STRESS and not args.skip_bdpt) else None
     if rank == 0:
         line = {
             "metric": "Mpaths/s", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
@@ -575,6 +627,7 @@ def run_gpu(args, wl):
             "cpu_baseline": cpu,
             "displaced_icosphere": extra,
             "instanced": inst,
+            "bdpt": bdpt,
             "clocks": clocks,
             "gpu_launches": int(args.steps) * launches_step,
             "kernel_launches_per_step": launches_step,
@@ -805,6 +858,7 @@ def main():
     ap.add_argument("--skip-displaced", action="store_true", help="leave out the displaced-icosphere figures")
     ap.add_argument("--skip-watertight", action="store_true", help="leave out the watertight-test render")
     ap.add_argument("--skip-instanced", action="store_true", help="leave out the instanced stress-scene figures")
+    ap.add_argument("--skip-bdpt", action="store_true", help="leave out the bidirectional path tracing figures")
     ap.add_argument("--libm-double", type=int, default=None, choices=[0, 1],
                     help="set the renderer's libm_double option (float cos/sin/acos/log2 evaluated in double)")
     ap.add_argument("--integrator", type=int, default=1, choices=[0, 1], help="0 megakernel, 1 wavefront")
@@ -820,6 +874,8 @@ def main():
     ap.add_argument("--views64", action="store_true", help="64 batched uneven views (autotuned, with the cache)")
     ap.add_argument("--views-oracle-spp", type=int, default=1024,
                     help="spp of the FP64 oracle crops the 64 views' RMSE is taken against")
+    ap.add_argument("--bdpt-only", action="store_true",
+                    help="only the bidirectional path tracing figures (the bdpt key)")
     ap.add_argument("--mlp-only", action="store_true",
                     help="radiance-cache network alone: inference over 1920x1080 queries, one 65,536-sample training step")
     ap.add_argument("--time-to-rmse", action="store_true",
@@ -854,6 +910,12 @@ def main():
         import lighttransportsimulation_gb300 as lts
         ctx = lts.Context(0)
         print(json.dumps({"mlp": mlp_bench(ctx, args.steps, args.warmup, measured_peaks()[0])}))
+        ctx.close()
+        return
+    if args.bdpt_only:
+        import lighttransportsimulation_gb300 as lts
+        ctx = lts.Context(0)
+        print(json.dumps({"bdpt": bdpt_extra(args, ctx)}))
         ctx.close()
         return
     if args.impl == "reference":

@@ -355,7 +355,10 @@ __device__ __forceinline__ void bdpt_add_splat(const SceneView& sv, real rx, rea
         }
 }
 
-__global__ __launch_bounds__(kThreads, 1) void k_bdpt(const SceneView sv, const RenderParams rp, int nleaf,
+#ifndef LTS_BDPT_MIN_BLOCKS
+#define LTS_BDPT_MIN_BLOCKS 3  // resident blocks per SM the register budget is cut for (168, no spills)
+#endif
+__global__ __launch_bounds__(kThreads, LTS_BDPT_MIN_BLOCKS) void k_bdpt(const SceneView sv, const RenderParams rp, int nleaf,
                                                       double* __restrict__ splat, int only) {
     __shared__ uint32_t s_stack[kStack * kThreads];
     const int tid = threadIdx.y * kBX + threadIdx.x;
@@ -372,7 +375,9 @@ __global__ __launch_bounds__(kThreads, 1) void k_bdpt(const SceneView sv, const 
     Work wk{0u, 0u};
     const int maxb = min(rp.max_bounce, kBdptMaxBounce);
     BVert cp[kBdptMaxBounce + 2], lp[kBdptMaxBounce + 1];
-    for (int s_ix = 0; s_ix < rp.spp; ++s_ix) {
+    // the pixel's samples are split over gridDim.z slices of the grid (sample s_ix draws the same
+    // numbers whatever the split; the film and splat sums are atomic)
+    for (int s_ix = (int)blockIdx.z; s_ix < rp.spp; s_ix += (int)gridDim.z) {
         rng.sample = (uint32_t)s_ix;
         rng.draw = 0;
         // camera subpath (GenerateCameraSubpath): the path tracer's primary ray and differentials

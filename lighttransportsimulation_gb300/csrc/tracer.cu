@@ -991,7 +991,14 @@ std::string Tracer::render_async(const HostScene& sc, const Lbvh& bvh, const lts
         e = render64_launch(sv, rp, bvh.n, d.record_samples != 0, s);
         if (!e.empty()) return e;
     } else if (d.integrator == LTS_INTEGRATOR_BDPT) {
-        k_bdpt<<<grid, block, 0, s>>>(sv, rp, bvh.n, splat_, bdpt_strategy);
+        // one thread per pixel and sample slice: enough blocks for every SM to hold its resident
+        // ones about four times over (a small film alone would leave most SMs idle)
+        int dev = 0, sms = 0;
+        TRY(cudaGetDevice(&dev));
+        TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const long want = 4L * LTS_BDPT_MIN_BLOCKS * sms, have = (long)grid.x * grid.y;
+        const dim3 gridz(grid.x, grid.y, (unsigned)std::max(1L, std::min<long>(rp.spp, (want + have - 1) / have)));
+        k_bdpt<<<gridz, block, 0, s>>>(sv, rp, bvh.n, splat_, bdpt_strategy);
     } else if (d.record_samples) {
         k_pathtrace<true><<<grid, block, 0, s>>>(sv, rp, bvh.n);
     } else {

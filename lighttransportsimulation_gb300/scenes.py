@@ -236,6 +236,25 @@ def write_box_sphere(d, level=4):
     return "box", "sphere"
 
 
+def write_tri_light_box(d, level=3):
+    """The box + icosphere scene with its ceiling light as one triangle (the path tracer's light
+    choice never picks the last light, a reference quirk that is exact with one light, so the path
+    tracer and bidirectional path tracing estimate the same image); returns (scene, subject)."""
+    os.makedirs(d, exist_ok=True)
+    _box_meshes(d)
+    p = np.array([(-0.3, 0.999, -0.3), (0.3, 0.999, -0.3), (0.0, 0.999, 0.3)])
+    write_bin(os.path.join(d, "tri_light.bin"), p, np.array([(0.0, -1.0, 0.0)]), np.array([[0, 2, 1]]),
+              np.zeros((1, 3), np.int64))
+    v, f = icosphere(level)
+    write_bin(os.path.join(d, "sphere.bin"), v * 0.5, v, f, f)
+    text = _box_scene_text().replace("box_light", "tri_light").replace("1\t10 10 10\n", "1\t12 12 12\n")
+    with open(os.path.join(d, "tribox.scene"), "w") as fh:
+        fh.write(text)
+    with open(os.path.join(d, "sphere.subject"), "w") as fh:
+        fh.write("0\n1\tsphere\n1\nL\tc\t0.8 0.8 0.8\t0\n")
+    return "tribox", "sphere"
+
+
 # Point lights of the point-light scene: world position, intensity (the `pointLights` grammar
 # extension of the loader; the reference has a PointLight but no file syntax for it).
 POINT_LIGHTS = [((-0.6, 0.55, 0.35), (1.6, 1.2, 0.8)), ((0.55, -0.45, 0.5), (0.4, 0.8, 1.6))]
