@@ -356,7 +356,11 @@ __device__ __forceinline__ void bdpt_add_splat(const SceneView& sv, real rx, rea
 }
 
 #ifndef LTS_BDPT_MIN_BLOCKS
-#define LTS_BDPT_MIN_BLOCKS 3  // resident blocks per SM the register budget is cut for (168, no spills)
+// Resident blocks per SM the register budget is cut for: the kernel is bound by latency, and more
+// warps pay even with spills (Msamples/s on the bench's box: 2 blocks 5.44, 3 (168 registers, no
+// spills) 5.84, 4 6.27, 5 6.60, 6 7.14, 8 (64 registers) 8.19; the traversal stacks' shared
+// memory allows 9).
+#define LTS_BDPT_MIN_BLOCKS 8
 #endif
 __global__ __launch_bounds__(kThreads, LTS_BDPT_MIN_BLOCKS) void k_bdpt(const SceneView sv, const RenderParams rp, int nleaf,
                                                       double* __restrict__ splat, int only) {
