@@ -22,11 +22,12 @@ __device__ __forceinline__ void kahan_add(float* sum, float* c, float v) {
 }
 
 // ------------------------------------------------------------------ the kernel
+// Resident blocks per SM the register budget is cut for.
+#ifndef LTS_MEGA_MIN_BLOCKS
+#define LTS_MEGA_MIN_BLOCKS 1
+#endif
 template <bool RECORD>
-// One resident block per SM is all the bound asks: left to itself ptxas caps the kernel at 168
-// registers (three blocks) and spills ~200 bytes per thread; with this bound it takes ~216 and
-// spills nothing.
-__global__ __launch_bounds__(kThreads, 1) void k_pathtrace(const SceneView sv, const RenderParams rp, int nleaf) {
+__global__ __launch_bounds__(kThreads, LTS_MEGA_MIN_BLOCKS) void k_pathtrace(const SceneView sv, const RenderParams rp, int nleaf) {
     __shared__ uint32_t s_stack[kStack * kThreads];
     const int tid = threadIdx.y * kBX + threadIdx.x;
     uint32_t* stack = s_stack + tid;
