@@ -2,7 +2,7 @@
 thread on cuda:0) against the reference's own functions on the same inputs
 (tests/golden/kat_reference.npz, made by oracle/_ref/lts_ref kat from the reference's sources).
 
-Tolerance: the benchmark spec FP32 bar, 1e-4 relative, plus 1e-6 absolute for values near zero.
+Tolerance: the FP32 parity bar, 1e-4 relative, plus 1e-6 absolute for values near zero.
 The device code rounds with FMA contraction and CUDA's transcendentals, the reference's host
 build without FMA and with glibc's, so values agree to a few ulps, not bit for bit; the worst
 relative error of each function is printed."""

@@ -44,5 +44,5 @@ def test_point_lights_match_the_port(built_lib, port_exe, tmp_path, integrator):
     assert np.isfinite(L).all() and Lr.mean() > 0
     assert 1 - same.mean() <= MAX_DIVERGENT
     # the port rounds as the reference's host build: on this short-path scene every
-    # non-divergent sample is within the benchmark spec tolerance
+    # non-divergent sample is within the FP32 parity tolerance (1e-4 relative)
     assert ok[same].all()

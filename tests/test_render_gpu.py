@@ -16,7 +16,7 @@ build rounds):
     value is itself that far from the exact value (long mirror, glass and glossy chains amplify the
     last-bit differences of single operations, including the transcendentals of two libms), a
     second correct float evaluation differs from it by that much as well.  On paths the reference
-    evaluates accurately the bound is the benchmark spec tolerance, 1e-4.
+    evaluates accurately the bound is the FP32 parity tolerance, 1e-4.
 
 The FP64 renderer itself is held to 1e-2 per sample (it does not round like the reference's
 float code); on the stress scene at most 0.1 % of its samples may leave the 5e-2 bound.
