@@ -137,10 +137,13 @@ __device__ __forceinline__ real bdpt_shading_fix(const Bsdf& f, V3 wo, V3 wi) {
     if (den == 0) return 0;
     return absdot(wo, f.ns) * absdot(wi, f.ng) / den;
 }
-// Vertex::f: scattering at surface vertex v toward `next`.
+// Vertex::f: scattering at surface vertex v toward `next`.  LM (and TEX below): the lobes (and
+// textures) the scene's materials can have -- the kernel is compiled for them only, as the
+// wavefront's shade kernels are.
+template <int LM>
 __device__ __forceinline__ Spec bv_f(const BVert& v, const BVert& next, bool importance) {
     const V3 wi = normalize(next.p - v.p);
-    Spec c = bsdf_f(v.f, v.wo, wi, BSDF_ALL, nullptr);
+    Spec c = bsdf_f<LM>(v.f, v.wo, wi, BSDF_ALL, nullptr);
     if (importance) c = c * bdpt_shading_fix(v.f, v.wo, wi);
     return c;
 }
@@ -171,6 +174,7 @@ __device__ __forceinline__ real bv_pdf_light_origin(const SceneView& sv, const B
 }
 // Vertex::Pdf: density (area measure at `next`) of sampling `next` from v, which was reached from
 // `prev` (null for an endpoint).
+template <int LM>
 __device__ __forceinline__ real bv_pdf(const SceneView& sv, const BCam& cam, const BVert& v, const BVert* prev,
                                        const BVert& next) {
     if (v.type == BV_LIGHT) return bv_pdf_light(sv, v, next);
@@ -185,7 +189,7 @@ __device__ __forceinline__ real bv_pdf(const SceneView& sv, const BCam& cam, con
     } else {
         if (!prev) return 0;
         const V3 wp = normalize(prev->p - v.p);
-        pdf = bsdf_pdf(v.f, wp, wn, BSDF_ALL, nullptr);
+        pdf = bsdf_pdf<LM>(v.f, wp, wn, BSDF_ALL, nullptr);
     }
     return bv_convert(pdf, v, next);
 }
@@ -200,6 +204,7 @@ __device__ __forceinline__ bool bdpt_visible(const SceneView& sv, int nleaf, con
 
 // RandomWalk: extends `path` (path[0] is the walk's start, already filled) by up to max_depth
 // surface vertices; returns the vertices added.
+template <int LM, bool TEX>
 __device__ int bdpt_walk(const SceneView& sv, int nleaf, BVert* path, V3 ro, V3 rd, Spec beta, real pdf_fwd,
                          int max_depth, bool importance, Rng& rng, bool diff0, V3 rxo, V3 rxd, V3 ryd,
                          uint32_t* stack, uint32_t* err, Work& wk, unsigned long long& rays) {
@@ -233,17 +238,17 @@ __device__ int bdpt_walk(const SceneView& sv, int nleaf, BVert* path, V3 ro, V3 
         v.beta = beta;
         v.pdf_rev = 0;
         v.pdf_fwd = bv_convert(pdf_fwd, prev, v);
-        if (!make_bsdf(sv, si, v.f, nullptr)) v.f.lobe = LOBE_NONE;
+        if (!make_bsdf<LM, TEX>(sv, si, v.f, nullptr)) v.f.lobe = LOBE_NONE;
         ++bounces;
         if (bounces >= max_depth || v.f.lobe == LOBE_NONE) break;
         V3 wi;
         uint32_t stype = 0;
         real pdf = 0;
-        const Spec fv = bsdf_sample(v.f, v.wo, wi, rng_2d(rng), pdf, BSDF_ALL, stype, nullptr);
+        const Spec fv = bsdf_sample<LM>(v.f, v.wo, wi, rng_2d(rng), pdf, BSDF_ALL, stype, nullptr);
         if (is_black(fv) || pdf == 0) break;
         beta = beta * (fv * absdot(wi, v.f.ns) / pdf);
         pdf_fwd = pdf;
-        pdf_rev = bsdf_pdf(v.f, wi, v.wo, BSDF_ALL, nullptr);
+        pdf_rev = bsdf_pdf<LM>(v.f, wi, v.wo, BSDF_ALL, nullptr);
         if (stype & BSDF_SPECULAR) {
             v.delta = 1;
             pdf_fwd = pdf_rev = 0;
@@ -268,6 +273,7 @@ __device__ int bdpt_walk(const SceneView& sv, int nleaf, BVert* path, V3 ro, V3 
 // MISWeight: the balance heuristic over every strategy that could have made the same path, from
 // the ratio chain of forward and reverse densities; the connection endpoints' densities (and the
 // resampled endpoint of s = 1 or t = 1) replace the stored ones for the evaluation.
+template <int LM>
 __device__ real bdpt_mis(const SceneView& sv, const BCam& cam, const BVert* lp, const BVert* cp, const BVert& sampled,
                          int s, int t) {
     if (s + t == 2) return 1;
@@ -278,19 +284,19 @@ __device__ real bdpt_mis(const SceneView& sv, const BCam& cam, const BVert* lp, 
     // overridden reverse densities of the four vertices around the connection
     real pt_rev = 0, ptm_rev = 0, qs_rev = 0, qsm_rev = 0;
     if (pt) {
-        if (s > 0) pt_rev = bv_pdf(sv, cam, *qs, qsm, *pt);
+        if (s > 0) pt_rev = bv_pdf<LM>(sv, cam, *qs, qsm, *pt);
         else pt_rev = bv_pdf_light_origin(sv, *pt);  // pt is an emitting surface
     }
     if (ptm) {
-        if (s > 0) ptm_rev = bv_pdf(sv, cam, *pt, qs, *ptm);
+        if (s > 0) ptm_rev = bv_pdf<LM>(sv, cam, *pt, qs, *ptm);
         else {  // PdfLight of the emitting surface pt toward ptm
             BVert lv = *pt;
             lv.type = BV_LIGHT;
             ptm_rev = bv_pdf_light(sv, lv, *ptm);
         }
     }
-    if (qs) qs_rev = bv_pdf(sv, cam, *pt, ptm, *qs);
-    if (qsm) qsm_rev = bv_pdf(sv, cam, *qs, pt, *qsm);
+    if (qs) qs_rev = bv_pdf<LM>(sv, cam, *pt, ptm, *qs);
+    if (qsm) qsm_rev = bv_pdf<LM>(sv, cam, *qs, pt, *qsm);
     auto remap0 = [](real f) -> real { return f != 0 ? f : 1; };
     real sum = 0, ri = 1;
     for (int i = t - 1; i > 0; --i) {
@@ -362,6 +368,7 @@ __device__ __forceinline__ void bdpt_add_splat(const SceneView& sv, real rx, rea
 // memory allows 9).
 #define LTS_BDPT_MIN_BLOCKS 8
 #endif
+template <int LM, bool TEX>
 __global__ __launch_bounds__(kThreads, LTS_BDPT_MIN_BLOCKS) void k_bdpt(const SceneView sv, const RenderParams rp, int nleaf,
                                                       double* __restrict__ splat, int only) {
     __shared__ uint32_t s_stack[kStack * kThreads];
@@ -404,7 +411,7 @@ __global__ __launch_bounds__(kThreads, LTS_BDPT_MIN_BLOCKS) void k_bdpt(const Sc
         c0.f.lobe = LOBE_NONE;
         real cpx, cpy, cos_t;
         bdpt_raster(cam, rd, cpx, cpy, cos_t);
-        const int n_cam = 1 + bdpt_walk(sv, nleaf, cp, cam.o, rd, spec(1.0f), bdpt_pdf_dir(cam, cos_t), maxb + 1,
+        const int n_cam = 1 + bdpt_walk<LM, TEX>(sv, nleaf, cp, cam.o, rd, spec(1.0f), bdpt_pdf_dir(cam, cos_t), maxb + 1,
                                         false, rng, true, cam.o, rxd, ryd, stack, rp.err, wk, rays);
         // light subpath (GenerateLightSubpath)
         int n_light = 0;
@@ -460,7 +467,7 @@ __global__ __launch_bounds__(kThreads, LTS_BDPT_MIN_BLOCKS) void k_bdpt(const Sc
                 l0.pdf_fwd = pdf_pos * lpick;
                 const Spec beta = Le * (absdot(nl, dir) / (lpick * pdf_pos * pdf_dir));
                 const V3 org = offset_origin(l0.p, l0.perr, l0.n, dir);
-                n_light = 1 + bdpt_walk(sv, nleaf, lp, org, dir, beta, pdf_dir, maxb, true, rng, false, org, dir, dir,
+                n_light = 1 + bdpt_walk<LM, TEX>(sv, nleaf, lp, org, dir, beta, pdf_dir, maxb, true, rng, false, org, dir, dir,
                                         stack, rp.err, wk, rays);
             }
         }
@@ -499,7 +506,7 @@ __global__ __launch_bounds__(kThreads, LTS_BDPT_MIN_BLOCKS) void k_bdpt(const Sc
                             sampled.pdf_fwd = sampled.pdf_rev = 0;
                             sampled.f.lobe = LOBE_NONE;
                             // qs is a surface vertex: s >= 2 whenever t = 1
-                            c = qs.beta * bv_f(qs, sampled, true) * sampled.beta * absdot(wi, qs.f.ns);
+                            c = qs.beta * bv_f<LM>(qs, sampled, true) * sampled.beta * absdot(wi, qs.f.ns);
                             if (!is_black(c)) {
                                 ++rays;
                                 if (!bdpt_visible(sv, nleaf, qs, sampled, stack, rp.err, wk)) c = spec(0.0f);
@@ -531,7 +538,7 @@ __global__ __launch_bounds__(kThreads, LTS_BDPT_MIN_BLOCKS) void k_bdpt(const Sc
                             sampled.pdf_rev = 0;
                             sampled.f.lobe = LOBE_NONE;
                             sampled.pdf_fwd = bv_pdf_light_origin(sv, sampled);
-                            c = pt.beta * bv_f(pt, sampled, false) * sampled.beta;
+                            c = pt.beta * bv_f<LM>(pt, sampled, false) * sampled.beta;
                             c = c * absdot(ls.wi, pt.f.ns);
                             if (!is_black(c)) {
                                 ++rays;
@@ -543,7 +550,7 @@ __global__ __launch_bounds__(kThreads, LTS_BDPT_MIN_BLOCKS) void k_bdpt(const Sc
                     const BVert& qs = lp[s - 1];
                     const BVert& pt = cp[t - 1];
                     if (bv_connectible(qs) && bv_connectible(pt)) {
-                        c = qs.beta * bv_f(qs, pt, true) * bv_f(pt, qs, false) * pt.beta;
+                        c = qs.beta * bv_f<LM>(qs, pt, true) * bv_f<LM>(pt, qs, false) * pt.beta;
                         if (!is_black(c)) {  // generalized geometry term G with visibility
                             V3 d = qs.p - pt.p;
                             real g = 1 / len2(d);
@@ -555,7 +562,7 @@ __global__ __launch_bounds__(kThreads, LTS_BDPT_MIN_BLOCKS) void k_bdpt(const Sc
                     }
                 }
                 if (is_black(c)) continue;
-                if (only < 0) c = c * bdpt_mis(sv, cam, lp, cp, sampled, s, t);
+                if (only < 0) c = c * bdpt_mis<LM>(sv, cam, lp, cp, sampled, s, t);
                 if (splat_it) {
                     bdpt_add_splat(sv, spx, spy, c, splat);
                 } else {

@@ -526,6 +526,7 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
         shade_lm_[c] = 0;
         shade_tex_[c] = false;
     }
+    bdpt_matte_only_ = true;
     for (size_t m = 0; m < mats.size(); ++m) {
         const HostMaterial& h = sc.materials[m];
         const int c = mats[m].shade_class;
@@ -534,6 +535,7 @@ std::string Tracer::upload_scene(const HostScene& sc, cudaStream_t s) {
         shade_lm_[c] |= lm;
         const bool tex = h.tex[0].kind != TEX_CONSTANT || (h.kind == 2 && h.tex[1].kind != TEX_CONSTANT);
         shade_tex_[c] = shade_tex_[c] || tex;
+        if ((lm & ~LM_MATTE) || tex) bdpt_matte_only_ = false;
     }
     std::vector<DevLight> lights(sc.lights.size());
     for (size_t l = 0; l < lights.size(); ++l) {
@@ -998,7 +1000,9 @@ std::string Tracer::render_async(const HostScene& sc, const Lbvh& bvh, const lts
         TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         const long want = 4L * LTS_BDPT_MIN_BLOCKS * sms, have = (long)grid.x * grid.y;
         const dim3 gridz(grid.x, grid.y, (unsigned)std::max(1L, std::min<long>(rp.spp, (want + have - 1) / have)));
-        k_bdpt<<<gridz, block, 0, s>>>(sv, rp, bvh.n, splat_, bdpt_strategy);
+        // compiled for the lobes the scene has: Lambertian / Oren-Nayar alone, or every lobe
+        if (bdpt_matte_only_) k_bdpt<LM_MATTE, false><<<gridz, block, 0, s>>>(sv, rp, bvh.n, splat_, bdpt_strategy);
+        else k_bdpt<LM_ALL, true><<<gridz, block, 0, s>>>(sv, rp, bvh.n, splat_, bdpt_strategy);
     } else if (d.record_samples) {
         k_pathtrace<true><<<grid, block, 0, s>>>(sv, rp, bvh.n);
     } else {

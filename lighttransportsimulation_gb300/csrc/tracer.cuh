@@ -253,6 +253,7 @@ class Tracer {
     // shade classes of the loaded scene: used, lobe mask and textured (the shade kernel variant)
     bool shade_used_[kShadeClasses] = {false};
     int shade_lm_[kShadeClasses] = {0};
+    bool bdpt_matte_only_ = false;  // every material Lambertian / Oren-Nayar with constant textures
     bool shade_tex_[kShadeClasses] = {false};
     unsigned shade_grid_ = 0;  // resident blocks of the shade kernel on this device
     // side streams and fork / join events: the classes' shade launches run concurrently (as
