@@ -36,7 +36,8 @@ Reported (one JSON line on rank 0):
              flat tree;
   bdpt       bidirectional path tracing on a box lit by one triangle (256 x 256, 5 bounces):
              Msamples/s beside the two path tracers, and the RMSE BDPT and the wavefront path
-             tracer reach in equal device time against a 16,384-spp render.
+             tracer reach in equal device time against a 16,384-spp render; the same for the box
+             lit indirectly (the triangle facing the ceiling) against a 65,536-spp render.
 --impl reference times that CPU port alone, on the same workload and metric.
 Inputs (BVH + triangles, ~400 MB) exceed the 129 MB L2, so no flush runs between steps.
 """
@@ -508,6 +509,24 @@ def bdpt_extra(args, ctx):
                          "rmse_bdpt": float(np.sqrt(np.mean((bd - ref) ** 2))),
                          "rmse_wavefront": float(np.sqrt(np.mean((pt - ref) ** 2))),
                          "mean_bdpt": float(bd.mean()), "mean_reference": float(ref.mean())}
+    # the same box lit indirectly: the triangle faces the ceiling, so next-event estimation from
+    # the room never reaches its emitting side and the path tracer finds the light only by
+    # BSDF-sampled bounces off the ceiling, while BDPT's light subpaths start there
+    d2 = os.path.join(tempfile.gettempdir(), "lts_bench_bdpt_box_up")
+    sc2, sub2 = scenes.write_tri_light_box(d2, facing_up=True)
+    scene = lts.Scene.parse(ctx, d2, sc2, sub2, wl["width"], wl["height"])
+    ms_b = timed(lts.INTEGRATOR_BDPT, wl["spp"], wl["seed"])
+    ms_w = timed(lts.INTEGRATOR_WAVEFRONT, wl["spp"], wl["seed"])
+    ref = integ(lts.INTEGRATOR_WAVEFRONT).render(4 * wl["ref_spp"], wl["seed"] + 1)["film"].astype(np.float64)
+    spp_pt = max(1, int(round(wl["spp"] * ms_b / ms_w)))
+    bd = integ(lts.INTEGRATOR_BDPT).render(wl["spp"], wl["seed"] + 2)["film"].astype(np.float64)
+    pt = integ(lts.INTEGRATOR_WAVEFRONT).render(spp_pt, wl["seed"] + 3)["film"].astype(np.float64)
+    out["equal_time_indirect"] = {"device_ms": round(ms_b, 3), "bdpt_spp": wl["spp"], "wavefront_spp": spp_pt,
+                                  "reference_spp": 4 * wl["ref_spp"],
+                                  "bdpt_msamples_s": round(px * wl["spp"] / (ms_b * 1e-3) / 1e6, 3),
+                                  "rmse_bdpt": float(np.sqrt(np.mean((bd - ref) ** 2))),
+                                  "rmse_wavefront": float(np.sqrt(np.mean((pt - ref) ** 2))),
+                                  "mean_bdpt": float(bd.mean()), "mean_reference": float(ref.mean())}
     return out
 
 

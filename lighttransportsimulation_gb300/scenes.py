@@ -236,15 +236,22 @@ def write_box_sphere(d, level=4):
     return "box", "sphere"
 
 
-def write_tri_light_box(d, level=3):
+def write_tri_light_box(d, level=3, facing_up=False):
     """The box + icosphere scene with its ceiling light as one triangle (the path tracer's light
     choice never picks the last light, a reference quirk that is exact with one light, so the path
-    tracer and bidirectional path tracing estimate the same image); returns (scene, subject)."""
+    tracer and bidirectional path tracing estimate the same image); returns (scene, subject).
+    facing_up: the triangle hangs at y = 0.9 and emits toward the ceiling, which then lights the
+    room indirectly (next-event estimation from the room never sees its emitting side)."""
     os.makedirs(d, exist_ok=True)
     _box_meshes(d)
-    p = np.array([(-0.3, 0.999, -0.3), (0.3, 0.999, -0.3), (0.0, 0.999, 0.3)])
-    write_bin(os.path.join(d, "tri_light.bin"), p, np.array([(0.0, -1.0, 0.0)]), np.array([[0, 2, 1]]),
-              np.zeros((1, 3), np.int64))
+    if facing_up:
+        p = np.array([(-0.3, 0.9, -0.3), (0.3, 0.9, -0.3), (0.0, 0.9, 0.3)])
+        write_bin(os.path.join(d, "tri_light.bin"), p, np.array([(0.0, 1.0, 0.0)]), np.array([[0, 2, 1]]),
+                  np.zeros((1, 3), np.int64))
+    else:
+        p = np.array([(-0.3, 0.999, -0.3), (0.3, 0.999, -0.3), (0.0, 0.999, 0.3)])
+        write_bin(os.path.join(d, "tri_light.bin"), p, np.array([(0.0, -1.0, 0.0)]), np.array([[0, 2, 1]]),
+                  np.zeros((1, 3), np.int64))
     v, f = icosphere(level)
     write_bin(os.path.join(d, "sphere.bin"), v * 0.5, v, f, f)
     text = _box_scene_text().replace("box_light", "tri_light").replace("1\t10 10 10\n", "1\t12 12 12\n")
