@@ -524,7 +524,7 @@ struct Decoder {
         return true;
     }
 
-    // Row schedule of one component's upsampling (stb_image.h:3815-3845): output row j reads
+    // Row schedule of one component's upsampling (stb_image.h:3850-3888): output row j reads
     // `near` and `far` input rows; far is the neighbour row on the side of the output row.
     struct Resampler {
         int hs, vs, ystep, ypos = 0, wlo;
@@ -573,7 +573,7 @@ struct Decoder {
         }
     }
 
-    static uint8_t blend(uint8_t x, uint8_t y) {  // x y / 255, rounded (stb_image.h:3788-3792)
+    static uint8_t blend(uint8_t x, uint8_t y) {  // x y / 255, rounded (stb_image.h:3804-3808)
         const unsigned t = (unsigned)x * y + 128;
         return (uint8_t)((t + (t >> 8)) >> 8);
     }
